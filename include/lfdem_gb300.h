@@ -1,0 +1,250 @@
+/*
+ * lfdem_gb300.h -- C ABI of the GB300 (sm_103a) engine for LF_DEM's
+ * per-timestep hydrodynamic core.
+ *
+ * Two nested boundaries, both plain C (pointers and sizes, no CUDA or torch
+ * types), every call returns an int status (LFG_OK = 0) and never throws:
+ *
+ *  1. lfg_solver_*  replaces the linear algebra behind LF_DEM's StokesSolver
+ *     (LF_DEM/StokesSolver.h:198-285): block fill, CHOLMOD analyse/factorise
+ *     (StokesSolver.cpp:937-978) and cholmod_solve2 (StokesSolver.cpp:671-703).
+ *
+ *  2. lfg_sim_*     replaces System::timeEvolution (LF_DEM/System.cpp:1203-1279)
+ *     with a device-resident step loop: Lees-Edwards cell lists and pair
+ *     discovery (System.cpp:1328-1373, BoxSet.cpp), Interaction::updateState
+ *     (Interaction.cpp:171-236), resistance assembly (System.cpp:1429-1473),
+ *     the resistance solve, RHS force components (System.cpp:1727-1828),
+ *     stress-controlled shear rate (System.cpp:2017-2055), stresslets
+ *     (Stress.cpp:77-287) and the predictor-corrector integrator
+ *     (System.cpp:888-1187).
+ *
+ * Conventions: particle-major vectors of 6 doubles per particle (Fx Fy Fz Tx
+ * Ty Tz, or Ux Uy Uz Wx Wy Wz), as in StokesSolver's RHS layout
+ * (StokesSolver.h:31-45).  Resistance blocks are passed in LF_DEM's compact
+ * forms: a DBlock is 15 doubles (col0[5] col1[3] col2[1] col3[3] col4[2]
+ * col5[1]) and an ODBlock 18 doubles (col0[5] col1[3] col2[1] col3[5]
+ * col4[3] col5[1]), MatrixBlocks.h:5-122.  An off-diagonal block (row r,
+ * column c) has r > c.
+ */
+#ifndef LFDEM_GB300_H
+#define LFDEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+	LFG_OK = 0,
+	LFG_ERR_BAD_ARG = 1,   /* invalid argument or unsupported option */
+	LFG_ERR_OOM = 2,       /* device or host allocation failed */
+	LFG_ERR_NOT_SPD = 3,   /* non-positive pivot; lfg_status.info = scalar column + 1 */
+	LFG_ERR_TIMEOUT = 4,   /* a bounded device wait gave up */
+	LFG_ERR_CUDA = 5,      /* CUDA runtime error; lfg_status.msg has the text */
+	LFG_ERR_NO_DEVICE = 6, /* no usable sm_103 device */
+	LFG_ERR_NOT_CONVERGED = 7 /* FP32 + refinement did not reach the tolerance */
+};
+
+enum {
+	LFG_PREC_FP64 = 0,        /* FP64 multifrontal Cholesky ("plain form") */
+	LFG_PREC_FP32_REFINE = 1  /* FP32 factor + FP64 iterative refinement */
+};
+
+typedef struct {
+	int code;
+	int info;
+	int refine_iters;      /* last solve's refinement iterations (FP32 form) */
+	int pad_;
+	double refine_residual; /* last solve's relative residual (FP32 form) */
+	char msg[200];
+} lfg_status;
+
+/* Flat, already non-dimensionalised parameters (the subset of LF_DEM's
+ * ParameterSet.h + System flags the step reads). */
+typedef struct {
+	double kn, kt;
+	double mu_static, mu_dynamic;    /* mu_dynamic < 0 -> mu_static (System.cpp:370-372) */
+	double critical_load;
+	double ft_max;
+	int friction_model;              /* 0,1,2,3,5,6 (Contact.cpp:10-33) */
+	int repulsion_on;                /* "repulsion" present in the unit system */
+	double repulsion;
+	double repulsive_length;         /* <= 0 disables repulsion (System.cpp:415-418) */
+	double repulsive_max_length;     /* -1: no tanh cutoff */
+	int lubrication_model;           /* 0 none, 1 normal, 2 tangential */
+	double lub_reduce_parameter;
+	double lub_max_gap;
+	double interaction_range;        /* -1: lubrication range (System.cpp:405-410) */
+	double sd_coeff;
+	double contact_relaxation_time;
+	double contact_relaxation_time_tan;
+	double disp_max, dt, dt_max, dt_min;
+	int fixed_dt;
+	int integration_method;          /* 0 Euler, 1 predictor-corrector */
+	int control;                     /* 0 rate, 1 stress */
+	double shear_rate;               /* rate control: imposed rate in internal units */
+	double target_stress;            /* stress control: sigma/(6 pi), internal units */
+	double Ehat[6];                  /* (xx,xy,xz,yz,yy,zz) at unit rate */
+	double Ohat[3];
+	double init_strain_shear_rate_limit;
+	double init_shear_rate_limit;
+} lfg_params;
+
+/* Engine options (not physics). */
+typedef struct {
+	int precision;          /* LFG_PREC_* */
+	int device;             /* CUDA device ordinal */
+	double refine_tol;      /* relative residual target of the FP32 form (default 1e-12) */
+	int refine_max_iter;    /* default 30 */
+	double skin;            /* pair superset skin, units of (a_i+a_j)/2 (default 0.4) */
+	int use_graphs;         /* capture factor/solve launch sequences in CUDA graphs (default 1) */
+	int leaf_size;          /* nested-dissection leaf size in particles (default 16) */
+	int pad_;
+} lfg_options;
+
+void lfg_default_options(lfg_options *opt);
+
+/* Library / device information.  Returns LFG_OK if an sm_103 device is usable. */
+int lfg_device_info(int device, char *name, int name_len, int *sm_major, int *sm_minor, int *sm_count);
+
+/* ------------------------------------------------------------------ */
+/* 1. Inner boundary: the resistance solve (StokesSolver replacement). */
+/* ------------------------------------------------------------------ */
+typedef struct lfg_solver lfg_solver;
+
+/* StokesSolver::init (StokesSolver.cpp:77-106): n_mobile particles, dof 6. */
+int lfg_solver_create(int n_mobile, int dof, const lfg_options *opt, lfg_solver **out,
+                      lfg_status *st);
+
+/* StokesSolver::resetResistanceMatrix + addResistanceBlocks + matrixFillingDone
+ * (StokesSolver.cpp:121-152, 474-511, 937-948): the complete lower block
+ * matrix.  dblocks: n x 15; od_row/od_col/odblocks: nb entries of 18.
+ * pattern_changed = 1 re-runs the symbolic analysis (cholmod_analyze,
+ * StokesSolver.cpp:955-962); 0 reuses it (the (row,col) list must then be
+ * identical to the previous call's).  positions (3n, may be NULL) guide the
+ * nested-dissection ordering; without them a graph ordering is used. */
+int lfg_solver_set_blocks(lfg_solver *s, const double *dblocks, int nb, const int32_t *od_row,
+                          const int32_t *od_col, const double *odblocks, int pattern_changed,
+                          const double *positions, lfg_status *st);
+
+/* cholmod_factorize (StokesSolver.cpp:950-978).  LFG_ERR_NOT_SPD carries the
+ * failing scalar column (original numbering) + 1 in st->info. */
+int lfg_solver_factorize(lfg_solver *s, lfg_status *st);
+
+/* cholmod_solve2(CHOLMOD_A) for k right-hand sides (StokesSolver.cpp:671-703):
+ * rhs and x are k x 6n host arrays (x may alias rhs). */
+int lfg_solver_solve(lfg_solver *s, int k, const double *rhs, double *x, lfg_status *st);
+
+/* Device-pointer variant: rhs and x are k x 6n device arrays. */
+int lfg_solver_solve_device(lfg_solver *s, int k, const double *d_rhs, double *d_x,
+                            lfg_status *st);
+
+/* Symbolic statistics of the current analysis. */
+typedef struct {
+	int n_blocks, n_supernodes, n_levels, max_front;
+	int64_t nnz_L;          /* scalar nonzeros of L (dense supernodal panels) */
+	double flops_factor;    /* sum_s n^3/3 + n^2 m + n m^2 (scalar columns) */
+	int64_t front_bytes;    /* device bytes of the front arena */
+	int n_factor_launches, n_solve_launches;
+} lfg_solver_stats;
+int lfg_solver_get_stats(const lfg_solver *s, lfg_solver_stats *out);
+
+void lfg_solver_destroy(lfg_solver *s);
+
+/* ------------------------------------------------------------------ */
+/* 2. Outer boundary: the per-timestep core (System::timeEvolution).   */
+/* ------------------------------------------------------------------ */
+typedef struct lfg_sim lfg_sim;
+
+/* System::setupConfiguration (System.cpp:468-521) + the first-time block of
+ * timeEvolution.  pos: 3n, radius: n, le_disp: 2 (may be NULL), contact
+ * states (ncs entries of p0 < p1 with disp_tan, System::setContacts
+ * System.cpp:266-285). */
+int lfg_sim_create(const lfg_params *p, const lfg_options *opt, int n, const double *pos,
+                   const double *radius, double lx, double ly, double lz, const double *le_disp,
+                   int ncs, const int32_t *cs_p0, const int32_t *cs_p1, const double *cs_disp_tan,
+                   lfg_sim **out, lfg_status *st);
+
+/* System::timeEvolution(time_end, strain_end), System.cpp:1203-1279: steps
+ * until the end (negative = unused), then one stress-computing step. */
+int lfg_sim_advance(lfg_sim *s, double time_end, double strain_end, lfg_status *st);
+
+/* One timeEvolutionDt call (System.cpp:843-983) preceded by the loop's
+ * adaptTimeStep (System.cpp:1243-1245). */
+int lfg_sim_step(lfg_sim *s, int calc_stress, double time_end, double strain_end, lfg_status *st);
+
+/* nsteps steps without stress output (the throughput loop). */
+int lfg_sim_run(lfg_sim *s, int nsteps, double time_end, double strain_end, lfg_status *st);
+
+typedef struct {
+	double time, strain, shear_rate, dt;
+	double shear_disp[2];
+	double max_velocity, max_sliding_velocity;
+	double total_stress[6];
+	double viscosity, N1, N2;
+	double rate_prop_shearstress, rate_indep_shearstress;
+	int64_t total_num_timesteps;
+	int n_pairs, n_contacts, n_lub, n_resistance_pairs;
+	int n_superset_pairs, n_symbolic_runs;
+	int last_refine_iters, pad_;
+	double last_refine_residual;
+} lfg_sim_scalars;
+int lfg_sim_get_scalars(lfg_sim *s, lfg_sim_scalars *out);
+
+/* pos, vel, angvel, na_vel, na_angvel: 3n each, any may be NULL. */
+int lfg_sim_get_particles(lfg_sim *s, double *pos, double *vel, double *angvel, double *na_vel,
+                          double *na_angvel);
+
+/* Interactions (pairs with an Interaction object), sorted by (p0, p1). */
+typedef struct {
+	int32_t p0, p1, z_offset, contact_active, state, lub_active, pad0_, pad1_;
+	double r, reduced_gap;
+	double nvec[3], rvec[3], disp_tan[3], f_spring_total[3];
+	double lub_coeff, log_lub_coeff;
+	double rep_force[3];
+} lfg_pair;
+int lfg_sim_get_num_pairs(lfg_sim *s);
+int lfg_sim_get_pairs(lfg_sim *s, lfg_pair *out, int cap);
+
+/* Per-particle stress of one component (6n, Sym2Tensor order xx xy xz yz yy
+ * zz): 0 GU contact, 1 GU dashpot, 2 GU hydro, 3 GU repulsion, 4 M_E_hydro,
+ * 5 xF_contact (rate) / xF_contact_rateprop (stress), 6 xF_contact_rateindep,
+ * 7 xF_repulsion.  Valid after a stress-computing step. */
+int lfg_sim_get_particle_stress(lfg_sim *s, int comp, double *out);
+/* Non-affine velocity component (6n): 0 contact 1 dashpot 2 hydro 3 repulsion. */
+int lfg_sim_get_velocity_component(lfg_sim *s, int comp, double *out);
+
+/* Restart hooks (parity tests and checkpoint restore): set pair (p0,p1)'s
+ * tangential spring and friction state; set clocks; recompute every pair's
+ * forces at the current positions with dt = 0 (System.cpp:1216-1226). */
+int lfg_sim_set_contact(lfg_sim *s, int p0, int p1, int state, const double *disp_tan);
+int lfg_sim_set_clock(lfg_sim *s, double time, double strain, double dt, double shear_rate,
+                      double max_velocity, double max_sliding_velocity);
+int lfg_sim_refresh(lfg_sim *s);
+
+/* Stage-level entry points (kernel parity tests): assemble R_FU for the
+ * current state and copy it out (dblocks n x 15; odblocks for the nb
+ * resistance pairs, sorted by (col,row)); force component comp at the current
+ * state (6n). */
+int lfg_sim_assemble(lfg_sim *s, double *dblocks, int32_t *od_row, int32_t *od_col,
+                     double *odblocks, int cap, int *nb_out);
+int lfg_sim_force_component(lfg_sim *s, int comp, double *out);
+
+/* Timing of the last lfg_sim_run / lfg_sim_step, device milliseconds by stage
+ * (0 pairs, 1 assembly, 2 factorisation, 3 solves, 4 forces+stress, 5 move)
+ * and kernels launched. */
+typedef struct {
+	double ms[8];
+	int64_t launches;
+	double factor_flops;     /* algorithmic flops of one factorisation */
+	double solve_bytes;      /* algorithmic bytes of one forward+backward solve, 1 RHS */
+} lfg_sim_timing;
+int lfg_sim_get_timing(lfg_sim *s, lfg_sim_timing *out);
+
+void lfg_sim_destroy(lfg_sim *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

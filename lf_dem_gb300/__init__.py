@@ -1,0 +1,243 @@
+"""lf_dem_gb300 -- GB300 (sm_103a) engine for LF_DEM's per-timestep hydrodynamic core.
+
+The product is the C-ABI shared library lf_dem_gb300/_lib/liblfdem_gb300.so
+(declared in include/lfdem_gb300.h).  This module is a thin ctypes front-end
+used by the tests and the benchmark; it loads the library and fails loudly if
+it is missing or if no GB300 is present.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "liblfdem_gb300.so")
+
+LFG_OK = 0
+LFG_ERR_BAD_ARG = 1
+LFG_ERR_OOM = 2
+LFG_ERR_NOT_SPD = 3
+LFG_ERR_TIMEOUT = 4
+LFG_ERR_CUDA = 5
+LFG_ERR_NO_DEVICE = 6
+LFG_ERR_NOT_CONVERGED = 7
+PREC_FP64 = 0
+PREC_FP32_REFINE = 1
+
+
+class Status(C.Structure):
+    _fields_ = [("code", C.c_int), ("info", C.c_int), ("refine_iters", C.c_int), ("pad_", C.c_int),
+                ("refine_residual", C.c_double), ("msg", C.c_char * 200)]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("kn", C.c_double), ("kt", C.c_double),
+        ("mu_static", C.c_double), ("mu_dynamic", C.c_double),
+        ("critical_load", C.c_double), ("ft_max", C.c_double),
+        ("friction_model", C.c_int), ("repulsion_on", C.c_int),
+        ("repulsion", C.c_double), ("repulsive_length", C.c_double),
+        ("repulsive_max_length", C.c_double),
+        ("lubrication_model", C.c_int),
+        ("lub_reduce_parameter", C.c_double), ("lub_max_gap", C.c_double),
+        ("interaction_range", C.c_double), ("sd_coeff", C.c_double),
+        ("contact_relaxation_time", C.c_double), ("contact_relaxation_time_tan", C.c_double),
+        ("disp_max", C.c_double), ("dt", C.c_double), ("dt_max", C.c_double), ("dt_min", C.c_double),
+        ("fixed_dt", C.c_int), ("integration_method", C.c_int), ("control", C.c_int),
+        ("shear_rate", C.c_double), ("target_stress", C.c_double),
+        ("Ehat", C.c_double * 6), ("Ohat", C.c_double * 3),
+        ("init_strain_shear_rate_limit", C.c_double), ("init_shear_rate_limit", C.c_double),
+    ]
+
+
+class Options(C.Structure):
+    _fields_ = [("precision", C.c_int), ("device", C.c_int), ("refine_tol", C.c_double),
+                ("refine_max_iter", C.c_int), ("pad0_", C.c_int), ("skin", C.c_double),
+                ("use_graphs", C.c_int), ("leaf_size", C.c_int), ("pad_", C.c_int), ("pad2_", C.c_int)]
+
+
+class SolverStats(C.Structure):
+    _fields_ = [("n_blocks", C.c_int), ("n_supernodes", C.c_int), ("n_levels", C.c_int),
+                ("max_front", C.c_int), ("nnz_L", C.c_int64), ("flops_factor", C.c_double),
+                ("front_bytes", C.c_int64), ("n_factor_launches", C.c_int), ("n_solve_launches", C.c_int)]
+
+
+class SimScalars(C.Structure):
+    _fields_ = [
+        ("time", C.c_double), ("strain", C.c_double), ("shear_rate", C.c_double), ("dt", C.c_double),
+        ("shear_disp", C.c_double * 2), ("max_velocity", C.c_double), ("max_sliding_velocity", C.c_double),
+        ("total_stress", C.c_double * 6), ("viscosity", C.c_double), ("N1", C.c_double), ("N2", C.c_double),
+        ("rate_prop_shearstress", C.c_double), ("rate_indep_shearstress", C.c_double),
+        ("total_num_timesteps", C.c_int64), ("n_pairs", C.c_int), ("n_contacts", C.c_int),
+        ("n_lub", C.c_int), ("n_resistance_pairs", C.c_int), ("n_superset_pairs", C.c_int),
+        ("n_symbolic_runs", C.c_int), ("last_refine_iters", C.c_int), ("pad_", C.c_int),
+        ("last_refine_residual", C.c_double),
+    ]
+
+
+class Pair(C.Structure):
+    _fields_ = [
+        ("p0", C.c_int32), ("p1", C.c_int32), ("z_offset", C.c_int32), ("contact_active", C.c_int32),
+        ("state", C.c_int32), ("lub_active", C.c_int32), ("pad0_", C.c_int32), ("pad1_", C.c_int32),
+        ("r", C.c_double), ("reduced_gap", C.c_double),
+        ("nvec", C.c_double * 3), ("rvec", C.c_double * 3), ("disp_tan", C.c_double * 3),
+        ("f_spring_total", C.c_double * 3), ("lub_coeff", C.c_double), ("log_lub_coeff", C.c_double),
+        ("rep_force", C.c_double * 3),
+    ]
+
+
+class SimTiming(C.Structure):
+    _fields_ = [("ms", C.c_double * 8), ("launches", C.c_int64), ("factor_flops", C.c_double),
+                ("solve_bytes", C.c_double)]
+
+
+# Every extern "C" symbol declared in include/lfdem_gb300.h.
+EXPORTS = [
+    "lfg_default_options", "lfg_device_info",
+    "lfg_solver_create", "lfg_solver_set_blocks", "lfg_solver_factorize", "lfg_solver_solve",
+    "lfg_solver_solve_device", "lfg_solver_get_stats", "lfg_solver_destroy",
+    "lfg_sim_create", "lfg_sim_advance", "lfg_sim_step", "lfg_sim_run", "lfg_sim_get_scalars",
+    "lfg_sim_get_particles", "lfg_sim_get_num_pairs", "lfg_sim_get_pairs", "lfg_sim_get_particle_stress",
+    "lfg_sim_get_velocity_component", "lfg_sim_set_contact", "lfg_sim_set_clock", "lfg_sim_refresh",
+    "lfg_sim_assemble", "lfg_sim_force_component", "lfg_sim_get_timing", "lfg_sim_destroy",
+]
+
+_lib = None
+
+
+class LFGError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"lfg error {code}: {msg}")
+        self.code = code
+
+
+def load(path: str | None = None):
+    """Load the engine library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"{p} not found: build it with `python -m lf_dem_gb300.build` "
+                           "(or __graft_entry__.build()); there is no CPU fallback")
+    L = C.CDLL(p)
+    vp = C.c_void_p
+    pst = C.POINTER(Status)
+    L.lfg_default_options.argtypes = [C.POINTER(Options)]
+    L.lfg_default_options.restype = None
+    L.lfg_device_info.argtypes = [C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                  C.POINTER(C.c_int)]
+    L.lfg_solver_create.argtypes = [C.c_int, C.c_int, C.POINTER(Options), C.POINTER(vp), pst]
+    L.lfg_solver_set_blocks.argtypes = [vp, vp, C.c_int, vp, vp, vp, C.c_int, vp, pst]
+    L.lfg_solver_factorize.argtypes = [vp, pst]
+    L.lfg_solver_solve.argtypes = [vp, C.c_int, vp, vp, pst]
+    L.lfg_solver_solve_device.argtypes = [vp, C.c_int, vp, vp, pst]
+    L.lfg_solver_get_stats.argtypes = [vp, C.POINTER(SolverStats)]
+    L.lfg_solver_destroy.argtypes = [vp]
+    L.lfg_solver_destroy.restype = None
+    if hasattr(L, "lfg_sim_create"):
+        L.lfg_sim_create.argtypes = [C.POINTER(Params), C.POINTER(Options), C.c_int, vp, vp, C.c_double,
+                                     C.c_double, C.c_double, vp, C.c_int, vp, vp, vp, C.POINTER(vp), pst]
+        L.lfg_sim_advance.argtypes = [vp, C.c_double, C.c_double, pst]
+        L.lfg_sim_step.argtypes = [vp, C.c_int, C.c_double, C.c_double, pst]
+        L.lfg_sim_run.argtypes = [vp, C.c_int, C.c_double, C.c_double, pst]
+        L.lfg_sim_get_scalars.argtypes = [vp, C.POINTER(SimScalars)]
+        L.lfg_sim_get_particles.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.lfg_sim_get_num_pairs.argtypes = [vp]
+        L.lfg_sim_get_pairs.argtypes = [vp, vp, C.c_int]
+        L.lfg_sim_get_particle_stress.argtypes = [vp, C.c_int, vp]
+        L.lfg_sim_get_velocity_component.argtypes = [vp, C.c_int, vp]
+        L.lfg_sim_set_contact.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp]
+        L.lfg_sim_set_clock.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                        C.c_double]
+        L.lfg_sim_refresh.argtypes = [vp]
+        L.lfg_sim_assemble.argtypes = [vp, vp, vp, vp, vp, C.c_int, C.POINTER(C.c_int)]
+        L.lfg_sim_force_component.argtypes = [vp, C.c_int, vp]
+        L.lfg_sim_get_timing.argtypes = [vp, C.POINTER(SimTiming)]
+        L.lfg_sim_destroy.argtypes = [vp]
+        L.lfg_sim_destroy.restype = None
+    _lib = L
+    return L
+
+
+def _check(rc, st: Status):
+    if rc != LFG_OK:
+        raise LFGError(rc, st.msg.decode(errors="replace"))
+
+
+def default_options(**kw) -> Options:
+    o = Options()
+    load().lfg_default_options(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def device_info(device: int = 0):
+    name = C.create_string_buffer(128)
+    a, b, c = C.c_int(), C.c_int(), C.c_int()
+    rc = load().lfg_device_info(device, name, 128, C.byref(a), C.byref(b), C.byref(c))
+    return rc, name.value.decode(), (a.value, b.value), c.value
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Solver:
+    """Device resistance solver (lfg_solver_*): the StokesSolver linear algebra."""
+
+    def __init__(self, n: int, precision: int = PREC_FP64, **opts):
+        L = load()
+        self.n = n
+        self.opt = default_options(precision=precision, **opts)
+        h = C.c_void_p()
+        st = Status()
+        _check(L.lfg_solver_create(n, 6, C.byref(self.opt), C.byref(h), C.byref(st)), st)
+        self.h = h
+        self.last = st
+
+    def set_blocks(self, dblocks, od_row, od_col, odblocks, pattern_changed=True, positions=None):
+        d = np.ascontiguousarray(dblocks, dtype=np.float64)
+        r = np.ascontiguousarray(od_row, dtype=np.int32)
+        c = np.ascontiguousarray(od_col, dtype=np.int32)
+        o = np.ascontiguousarray(odblocks, dtype=np.float64)
+        pos = None if positions is None else np.ascontiguousarray(positions, dtype=np.float64)
+        st = Status()
+        _check(load().lfg_solver_set_blocks(self.h, _ptr(d), len(r), _ptr(r), _ptr(c), _ptr(o),
+                                            int(pattern_changed), None if pos is None else _ptr(pos),
+                                            C.byref(st)), st)
+
+    def factorize(self):
+        st = Status()
+        rc = load().lfg_solver_factorize(self.h, C.byref(st))
+        self.last = st
+        _check(rc, st)
+
+    def solve(self, b):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        k = b.size // (6 * self.n)
+        x = np.zeros_like(b)
+        st = Status()
+        rc = load().lfg_solver_solve(self.h, k, _ptr(b), _ptr(x), C.byref(st))
+        self.last = st
+        _check(rc, st)
+        return x
+
+    def stats(self) -> dict:
+        s = SolverStats()
+        load().lfg_solver_get_stats(self.h, C.byref(s))
+        return {k: getattr(s, k) for k, _ in SolverStats._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().lfg_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,759 @@
+// lfg_factor.cu -- device multifrontal Cholesky of R_FU (replaces CHOLMOD's
+// supernodal cholmod_factorize / cholmod_solve2, LF_DEM/StokesSolver.cpp:
+// 671-703, 950-978), in FP64 ("plain form") or FP32 (factor of the FP32 +
+// FP64-refinement form).
+//
+// Front layout: supernode s with n (own) and m (below) block columns has a
+// dense column-major front of 6F x ... (F = n + m) with leading dimension
+// ld = 6F + 6n.  Rows [6F, 6F + 6n) are an appended identity block: the same
+// panel triangular solves that produce L21 = A21 L11^-T turn it into
+// E = L11^-T, so both triangular solves become parallel matrix-vector
+// products.  Columns [0, 6n) hold L after factorisation; the lower triangle
+// of rows/columns [6n, 6F) holds the update (Schur complement) matrix that the
+// parent gathers.
+//
+// Per level of the assembly tree (leaves first):
+//   assemble  : zero + gather children's update matrices (fixed child order),
+//   scatter   : add the compact D / OD blocks of the level's columns,
+//   panel k   : factor the k-th diagonal block (redundantly per CTA) and
+//               solve the rows below it (real rows and identity rows),
+//   update k  : trailing rank-w update of the lower triangle (tiles) and
+//               write-back of the factored diagonal block.
+// Nothing uses atomics except the failure flag, so results are bitwise
+// reproducible run to run.
+#include <cstdio>
+#include <cuda_runtime.h>
+
+#include "lfg_internal.h"
+
+namespace lfg {
+
+enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4 };
+
+template <typename T> struct Cfg;
+template <> struct Cfg<double> { static constexpr int NB = 32, TILE = 64, TPT = 4; };
+template <> struct Cfg<float>  { static constexpr int NB = 32, TILE = 128, TPT = 8; };
+
+// ---------------------------------------------------------------------------
+// compact blocks -> dense (StokesSolver.cpp:154-231), m[r*6+c]
+// ---------------------------------------------------------------------------
+__device__ inline void d15_to_dense(const double *d, double *m)
+{
+#pragma unroll
+	for (int i = 0; i < 36; i++) m[i] = 0;
+	m[0*6+0] = d[0]; m[1*6+0] = d[1]; m[2*6+0] = d[2]; m[4*6+0] = d[3]; m[5*6+0] = d[4];
+	m[1*6+1] = d[5]; m[2*6+1] = d[6]; m[3*6+1] = -d[3]; m[5*6+1] = d[7];
+	m[2*6+2] = d[8]; m[3*6+2] = -d[4]; m[4*6+2] = -d[7];
+	m[3*6+3] = d[9]; m[4*6+3] = d[10]; m[5*6+3] = d[11];
+	m[4*6+4] = d[12]; m[5*6+4] = d[13];
+	m[5*6+5] = d[14];
+}
+
+__device__ inline void od18_to_dense(const double *o, double *m)
+{
+#pragma unroll
+	for (int i = 0; i < 36; i++) m[i] = 0;
+	m[0*6+0] = o[0]; m[1*6+0] = o[1]; m[2*6+0] = o[2]; m[4*6+0] = o[3]; m[5*6+0] = o[4];
+	m[0*6+1] = o[1]; m[1*6+1] = o[5]; m[2*6+1] = o[6]; m[3*6+1] = -o[3]; m[5*6+1] = o[7];
+	m[0*6+2] = o[2]; m[1*6+2] = o[6]; m[2*6+2] = o[8]; m[3*6+2] = -o[4]; m[4*6+2] = -o[7];
+	m[1*6+3] = o[9]; m[2*6+3] = o[10]; m[3*6+3] = o[11]; m[4*6+3] = o[12]; m[5*6+3] = o[13];
+	m[0*6+4] = -o[9]; m[2*6+4] = o[14]; m[3*6+4] = o[12]; m[4*6+4] = o[15]; m[5*6+4] = o[16];
+	m[0*6+5] = -o[10]; m[1*6+5] = -o[14]; m[3*6+5] = o[13]; m[4*6+5] = o[16]; m[5*6+5] = o[17];
+}
+
+// ---------------------------------------------------------------------------
+// assembly: one CTA per (supernode, scalar column)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_assemble(const int *__restrict__ col_tasks, const int *__restrict__ sn_n,
+                           const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
+                           const int64_t *__restrict__ sn_off, const int *__restrict__ child_off,
+                           const int *__restrict__ children, const int64_t *__restrict__ cinv_off,
+                           const int *__restrict__ cinv, T *__restrict__ arena)
+{
+	int s = col_tasks[2*blockIdx.x], c = col_tasks[2*blockIdx.x+1];
+	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
+	T *col = arena+sn_off[s]+(int64_t)c*ld;
+	int cb = c/6, cr = c%6;
+	int ca = child_off[s], cz = child_off[s+1];
+	for (int r = c+threadIdx.x; r < F6; r += blockDim.x) {
+		int rb = r/6, rr = r%6;
+		T v = 0;
+		for (int q = ca; q < cz; q++) {
+			int ch = children[q];
+			const int *inv = cinv+cinv_off[ch];
+			int ir = inv[rb], ic = inv[cb];
+			if (ir >= 0 && ic >= 0) {
+				int cld = sn_ld[ch];
+				v += arena[sn_off[ch]+(int64_t)(6*ic+cr)*cld+6*ir+rr];
+			}
+		}
+		col[r] = v;
+	}
+	if (c < n6)
+		for (int r = threadIdx.x; r < n6; r += blockDim.x) col[F6+r] = (r == c) ? T(1) : T(0);
+}
+
+template <typename T>
+__global__ void k_scatter_d(int count, const int *__restrict__ list, const double *__restrict__ dblocks,
+                            const int *__restrict__ d_sn, const int *__restrict__ d_bc,
+                            const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
+                            T *__restrict__ arena)
+{
+	int t = blockIdx.x*blockDim.x+threadIdx.x;
+	if (t >= count) return;
+	int i = list[t];
+	double m[36];
+	d15_to_dense(dblocks+15*(int64_t)i, m);
+	int s = d_sn[i], b = d_bc[i], ld = sn_ld[s];
+	T *base = arena+sn_off[s];
+	for (int c = 0; c < 6; c++)
+		for (int r = c; r < 6; r++)
+			base[(int64_t)(6*b+c)*ld+6*b+r] += (T)m[r*6+c];
+}
+
+template <typename T>
+__global__ void k_scatter_od(int count, const int *__restrict__ list, const double *__restrict__ odblocks,
+                             const int *__restrict__ od_sn, const int *__restrict__ od_br,
+                             const int *__restrict__ od_bc, const int *__restrict__ od_tr,
+                             const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
+                             T *__restrict__ arena)
+{
+	int t = blockIdx.x*blockDim.x+threadIdx.x;
+	if (t >= count) return;
+	int e = list[t];
+	double m[36];
+	od18_to_dense(odblocks+18*(int64_t)e, m);
+	int s = od_sn[e], br = od_br[e], bc = od_bc[e], ld = sn_ld[s];
+	T *base = arena+sn_off[s];
+	bool tr = od_tr[e];
+	for (int c = 0; c < 6; c++)
+		for (int r = 0; r < 6; r++)
+			base[(int64_t)(6*bc+c)*ld+6*br+r] += (T)(tr ? m[c*6+r] : m[r*6+c]);
+}
+
+// ---------------------------------------------------------------------------
+// w x w Cholesky of a shared-memory block (row-major A[i*NB+j], lower), by
+// one warp; rows owned by lanes i = lane + 32q.  Non-positive pivots are
+// replaced by 1 and reported through *fail (first column, global index + 1).
+// ---------------------------------------------------------------------------
+template <typename T, int NB>
+__device__ void warp_potrf(T *A, int w, int gcol0, int *fail)
+{
+	int lane = threadIdx.x & 31;
+	for (int j = 0; j < w; j++) {
+		// s_i = A[i][j] - sum_{t<j} L[i][t] L[j][t] for i >= j
+		T sv[(NB+31)/32];
+#pragma unroll
+		for (int q = 0; q < (NB+31)/32; q++) {
+			int i = lane+32*q;
+			T s = 0;
+			if (i >= j && i < w) {
+				s = A[i*NB+j];
+				for (int t = 0; t < j; t++) s -= A[i*NB+t]*A[j*NB+t];
+			}
+			sv[q] = s;
+		}
+		T d = __shfl_sync(0xffffffffu, sv[j/32], j%32);
+		if (!(d > T(0))) {
+			if (lane == 0 && fail) atomicMin(fail, gcol0+j+1);
+			d = T(1);
+		}
+		d = sqrt(d);
+		__syncwarp();
+#pragma unroll
+		for (int q = 0; q < (NB+31)/32; q++) {
+			int i = lane+32*q;
+			if (i == j) A[i*NB+j] = d;
+			else if (i > j && i < w) A[i*NB+j] = sv[q]/d;
+		}
+		__syncwarp();
+	}
+}
+
+// panel: CTA (128 threads) = one task (sn, row0, k, nrows)
+template <typename T>
+__global__ void __launch_bounds__(128) k_panel(const int4 *__restrict__ tasks, const int *__restrict__ sn_first,
+                                               const int *__restrict__ sn_n, const int *__restrict__ sn_ld,
+                                               const int64_t *__restrict__ sn_off, T *__restrict__ arena,
+                                               int *fail)
+{
+	constexpr int NB = Cfg<T>::NB;
+	__shared__ T Lkk[NB*NB];
+	int4 tk = tasks[blockIdx.x];
+	int s = tk.x, row0 = tk.y, k = tk.z, nrows = tk.w;
+	int n6 = 6*sn_n[s], ld = sn_ld[s];
+	int c0 = k*NB, w = min(NB, n6-c0);
+	T *base = arena+sn_off[s];
+	for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
+		int i = e/NB, j = e%NB;
+		Lkk[e] = (i < w && j <= i) ? base[(int64_t)(c0+j)*ld+c0+i] : T(0);
+	}
+	__syncthreads();
+	if (threadIdx.x < 32) warp_potrf<T, NB>(Lkk, w, 6*sn_first[s]+c0, nullptr);
+	__syncthreads();
+	int r = threadIdx.x;
+	if (r < nrows) {
+		int row = row0+r;
+		T x[NB];
+#pragma unroll
+		for (int j = 0; j < NB; j++) x[j] = (j < w) ? base[(int64_t)(c0+j)*ld+row] : T(0);
+#pragma unroll
+		for (int j = 0; j < NB; j++) {
+			if (j < w) {
+				T v = x[j];
+#pragma unroll
+				for (int t = 0; t < NB; t++) if (t < j) v -= x[t]*Lkk[j*NB+t];
+				x[j] = v/Lkk[j*NB+j];
+			}
+		}
+#pragma unroll
+		for (int j = 0; j < NB; j++) if (j < w) base[(int64_t)(c0+j)*ld+row] = x[j];
+	}
+}
+
+// trailing update: CTA = one tile (sn, r0, c0, k); c0 == -1 writes the
+// factored diagonal block of panel k
+template <typename T>
+__global__ void __launch_bounds__(256) k_update(const int4 *__restrict__ tasks, const int *__restrict__ sn_first,
+                                                const int *__restrict__ sn_n, const int *__restrict__ sn_m,
+                                                const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
+                                                T *__restrict__ arena, int *fail)
+{
+	constexpr int NB = Cfg<T>::NB, TL = Cfg<T>::TILE, TPT = Cfg<T>::TPT;
+	constexpr int TD = TL/TPT; // threads per dimension (16)
+	__shared__ T As[NB][TL];
+	__shared__ T Bs[NB][TL];
+	int4 tk = tasks[blockIdx.x];
+	int s = tk.x, r0 = tk.y, cc0 = tk.z, k = tk.w;
+	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
+	int p0 = k*NB, w = min(NB, n6-p0), t0 = p0+w;
+	T *base = arena+sn_off[s];
+	if (cc0 < 0) {
+		T *Lkk = &As[0][0];  // NB*NB <= NB*TL
+		for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
+			int i = e/NB, j = e%NB;
+			Lkk[e] = (i < w && j <= i) ? base[(int64_t)(p0+j)*ld+p0+i] : T(0);
+		}
+		__syncthreads();
+		if (threadIdx.x < 32) warp_potrf<T, NB>(Lkk, w, 6*sn_first[s]+p0, fail);
+		__syncthreads();
+		for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
+			int i = e/NB, j = e%NB;
+			if (i < w && j <= i) base[(int64_t)(p0+j)*ld+p0+i] = Lkk[e];
+		}
+		return;
+	}
+	bool extra = r0 >= F6;
+	int rlim = extra ? F6+t0 : F6;
+	int clim = extra ? n6 : F6;
+	// load panel rows of the tile rows and tile columns
+	for (int e = threadIdx.x; e < NB*TL; e += blockDim.x) {
+		int t = e/TL, i = e%TL;
+		int ra = r0+i, rb = cc0+i;
+		As[t][i] = (t < w && ra < rlim) ? base[(int64_t)(p0+t)*ld+ra] : T(0);
+		Bs[t][i] = (t < w && rb < clim) ? base[(int64_t)(p0+t)*ld+rb] : T(0);
+	}
+	__syncthreads();
+	int tx = threadIdx.x%TD, ty = threadIdx.x/TD;
+	T acc[TPT][TPT];
+#pragma unroll
+	for (int a = 0; a < TPT; a++)
+#pragma unroll
+		for (int b = 0; b < TPT; b++) acc[a][b] = 0;
+	for (int t = 0; t < w; t++) {
+		T av[TPT], bv[TPT];
+#pragma unroll
+		for (int a = 0; a < TPT; a++) av[a] = As[t][tx+TD*a];
+#pragma unroll
+		for (int b = 0; b < TPT; b++) bv[b] = Bs[t][ty+TD*b];
+#pragma unroll
+		for (int a = 0; a < TPT; a++)
+#pragma unroll
+			for (int b = 0; b < TPT; b++) acc[a][b] += av[a]*bv[b];
+	}
+#pragma unroll
+	for (int b = 0; b < TPT; b++) {
+		int c = cc0+ty+TD*b;
+		if (c >= clim) continue;
+#pragma unroll
+		for (int a = 0; a < TPT; a++) {
+			int r = r0+tx+TD*a;
+			if (r >= rlim) continue;
+			if (!extra && r < c) continue;
+			base[(int64_t)c*ld+r] -= acc[a][b];
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------
+// allocation and launch
+// ---------------------------------------------------------------------------
+template <typename T> static void set_smem_limits(int maxn6);
+
+template <typename T> void factor_alloc(DevFactor<T> &F, const DevSymbolic &D, int kmax)
+{
+	if (F.arena_cap < D.arena_elems) {
+		if (F.arena) cudaFree(F.arena);
+		F.arena = nullptr;
+		LFG_CUDA(cudaMalloc((void **)&F.arena, sizeof(T)*D.arena_elems));
+		F.arena_cap = D.arena_elems;
+	}
+	int64_t wneed = D.w_elems*kmax;
+	if (F.w_cap < wneed) {
+		if (F.w) cudaFree(F.w);
+		F.w = nullptr;
+		LFG_CUDA(cudaMalloc((void **)&F.w, sizeof(T)*wneed));
+		F.w_cap = wneed;
+	}
+	int64_t xneed = (int64_t)6*D.nblk*kmax;
+	if (F.x_cap < xneed) {
+		if (F.xp) cudaFree(F.xp);
+		if (F.yp) cudaFree(F.yp);
+		F.xp = F.yp = nullptr;
+		LFG_CUDA(cudaMalloc((void **)&F.xp, sizeof(T)*xneed));
+		LFG_CUDA(cudaMalloc((void **)&F.yp, sizeof(T)*xneed));
+		F.x_cap = xneed;
+	}
+	if (!F.status) LFG_CUDA(cudaMalloc((void **)&F.status, sizeof(int)*4));
+	if ((int64_t)sizeof(T)*4*D.max_n6 > 227*1024)
+		throw Error{LFG_ERR_BAD_ARG, 0, "supernode too wide for the shared-memory solve"};
+	set_smem_limits<T>(D.max_n6);
+}
+
+template <typename T> void factor_free(DevFactor<T> &F)
+{
+	if (F.arena) cudaFree(F.arena);
+	if (F.w) cudaFree(F.w);
+	if (F.xp) cudaFree(F.xp);
+	if (F.yp) cudaFree(F.yp);
+	if (F.status) cudaFree(F.status);
+	F = DevFactor<T>();
+}
+
+__global__ void k_set_int(int *p, int v) { *p = v; }
+
+template <typename T>
+int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, const double *odbl,
+                   cudaStream_t st)
+{
+	int launches = 0;
+	k_set_int<<<1, 1, 0, st>>>(F.status, 0x7fffffff);
+	launches++;
+	for (const auto &L : D.factor_plan) {
+		if (L.count <= 0) continue;
+		switch (L.kind) {
+		case PLAN_ASSEMBLE:
+			k_assemble<T><<<L.count, 256, 0, st>>>(D.col_tasks+2*L.off, D.sn_n, D.sn_m, D.sn_ld, D.sn_off,
+			                                       D.child_off, D.children, D.cinv_off, D.cinv, F.arena);
+			break;
+		case PLAN_SCATTER_D:
+			k_scatter_d<T><<<(L.count+127)/128, 128, 0, st>>>(L.count, D.level_d+L.off, dbl, D.d_sn, D.d_bc,
+			                                                    D.sn_ld, D.sn_off, F.arena);
+			break;
+		case PLAN_SCATTER_OD:
+			k_scatter_od<T><<<(L.count+127)/128, 128, 0, st>>>(L.count, D.level_od+L.off, odbl, D.od_sn,
+			                                                     D.od_br, D.od_bc, D.od_tr, D.sn_ld, D.sn_off,
+			                                                     F.arena);
+			break;
+		case PLAN_PANEL:
+			k_panel<T><<<L.count, 128, 0, st>>>(D.panel_tasks+L.off, D.sn_first, D.sn_n, D.sn_ld, D.sn_off,
+			                                    F.arena, F.status);
+			break;
+		case PLAN_UPDATE:
+			k_update<T><<<L.count, 256, 0, st>>>(D.tile_tasks+L.off, D.sn_first, D.sn_n, D.sn_m, D.sn_ld,
+			                                     D.sn_off, F.arena, F.status);
+			break;
+		}
+		launches++;
+	}
+	LFG_CUDA(cudaGetLastError());
+	return launches;
+}
+
+// ---------------------------------------------------------------------------
+// solves (k <= 4 right-hand sides, RHS-major: v[r*6n + i])
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_permute_in(int n, int k, const int *__restrict__ iperm, const double *__restrict__ b,
+                             T *__restrict__ xp)
+{
+	int t = blockIdx.x*blockDim.x+threadIdx.x;
+	if (t >= 6*n) return;
+	int i = t/6, d = t%6;
+	int q = 6*iperm[i]+d;
+	for (int r = 0; r < k; r++) xp[(int64_t)r*6*n+q] = (T)b[(int64_t)r*6*n+t];
+}
+
+template <typename T>
+__global__ void k_permute_out(int n, int k, const int *__restrict__ iperm, const T *__restrict__ xp,
+                              double *__restrict__ x)
+{
+	int t = blockIdx.x*blockDim.x+threadIdx.x;
+	if (t >= 6*n) return;
+	int i = t/6, d = t%6;
+	int q = 6*iperm[i]+d;
+	for (int r = 0; r < k; r++) x[(int64_t)r*6*n+t] = (double)xp[(int64_t)r*6*n+q];
+}
+
+// gather of the children's forward-update vectors into front row rloc
+template <typename T>
+__device__ inline T gather_w(int s, int rloc, int rr, int rhs, int64_t wstride, const int *child_off,
+                             const int *children, const int64_t *cinv_off, const int *cinv,
+                             const int *sn_n, const int64_t *sn_woff, const T *w)
+{
+	T v = 0;
+	for (int q = child_off[s]; q < child_off[s+1]; q++) {
+		int ch = children[q];
+		int ic = cinv[cinv_off[ch]+rloc];
+		if (ic >= 0) v += w[rhs*wstride+sn_woff[ch]+6*(ic-sn_n[ch])+rr];
+	}
+	return v;
+}
+
+// forward part 1: y_s = E^T v_top, one warp per output column j
+template <typename T, int K>
+__global__ void k_fwd_y(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
+                        const int *__restrict__ sn_n, const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
+                        const int64_t *__restrict__ sn_off, const int *__restrict__ child_off,
+                        const int *__restrict__ children, const int64_t *__restrict__ cinv_off,
+                        const int *__restrict__ cinv, const int64_t *__restrict__ sn_woff,
+                        const T *__restrict__ arena, const T *__restrict__ w, int64_t wstride,
+                        const T *__restrict__ xp, T *__restrict__ yp, int n6tot, int chunk)
+{
+	extern __shared__ unsigned char smem_raw[];
+	T *v = reinterpret_cast<T *>(smem_raw);
+	int s = lev_sn[blockIdx.y];
+	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
+	int j0 = blockIdx.x*chunk;
+	if (j0 >= n6) return;
+	int f6 = 6*sn_first[s];
+	for (int i = threadIdx.x; i < n6; i += blockDim.x) {
+#pragma unroll
+		for (int r = 0; r < K; r++)
+			v[r*n6+i] = xp[(int64_t)r*n6tot+f6+i] +
+			            gather_w<T>(s, i/6, i%6, r, wstride, child_off, children, cinv_off, cinv, sn_n, sn_woff, w);
+	}
+	__syncthreads();
+	const T *E = arena+sn_off[s]+F6;
+	int warp = threadIdx.x/32, lane = threadIdx.x%32, nw = blockDim.x/32;
+	for (int j = j0+warp; j < min(n6, j0+chunk); j += nw) {
+		const T *col = E+(int64_t)j*ld;
+		T acc[K];
+#pragma unroll
+		for (int r = 0; r < K; r++) acc[r] = 0;
+		for (int i = lane; i <= j; i += 32) {
+			T e = col[i];
+#pragma unroll
+			for (int r = 0; r < K; r++) acc[r] += e*v[r*n6+i];
+		}
+#pragma unroll
+		for (int r = 0; r < K; r++) {
+			T a = acc[r];
+			for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+			if (lane == 0) yp[(int64_t)r*n6tot+f6+j] = a;
+		}
+	}
+}
+
+// forward part 2: w_s = v_bottom - L21 y_s, one thread per update row
+template <typename T, int K>
+__global__ void k_fwd_w(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
+                        const int *__restrict__ sn_n, const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
+                        const int64_t *__restrict__ sn_off, const int *__restrict__ child_off,
+                        const int *__restrict__ children, const int64_t *__restrict__ cinv_off,
+                        const int *__restrict__ cinv, const int64_t *__restrict__ sn_woff,
+                        const T *__restrict__ arena, T *__restrict__ w, int64_t wstride,
+                        const T *__restrict__ yp, int n6tot, int chunk)
+{
+	extern __shared__ unsigned char smem_raw[];
+	T *y = reinterpret_cast<T *>(smem_raw);
+	int s = lev_sn[blockIdx.y];
+	int n6 = 6*sn_n[s], m6 = 6*sn_m[s], ld = sn_ld[s];
+	int r0 = blockIdx.x*chunk;
+	if (r0 >= m6) return;
+	int f6 = 6*sn_first[s];
+	for (int i = threadIdx.x; i < n6; i += blockDim.x)
+#pragma unroll
+		for (int r = 0; r < K; r++) y[r*n6+i] = yp[(int64_t)r*n6tot+f6+i];
+	__syncthreads();
+	const T *L = arena+sn_off[s];
+	for (int t = r0+threadIdx.x; t < min(m6, r0+chunk); t += blockDim.x) {
+		int row = n6+t;
+		T acc[K];
+#pragma unroll
+		for (int r = 0; r < K; r++)
+			acc[r] = gather_w<T>(s, row/6, row%6, r, wstride, child_off, children, cinv_off, cinv, sn_n, sn_woff, w);
+		for (int j = 0; j < n6; j++) {
+			T l = L[(int64_t)j*ld+row];
+#pragma unroll
+			for (int r = 0; r < K; r++) acc[r] -= l*y[r*n6+j];
+		}
+#pragma unroll
+		for (int r = 0; r < K; r++) w[r*wstride+sn_woff[s]+t] = acc[r];
+	}
+}
+
+// backward part 1: z_s = y_s - L21^T x[rows], one warp per column j; z -> yp
+template <typename T, int K>
+__global__ void k_bwd_z(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
+                        const int *__restrict__ sn_n, const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
+                        const int64_t *__restrict__ sn_off, const int *__restrict__ sn_rows_off,
+                        const int *__restrict__ rows, const T *__restrict__ arena, const T *__restrict__ xp,
+                        T *__restrict__ yp, int n6tot, int chunk)
+{
+	int s = lev_sn[blockIdx.y];
+	int n6 = 6*sn_n[s], m6 = 6*sn_m[s], ld = sn_ld[s];
+	int j0 = blockIdx.x*chunk;
+	if (j0 >= n6) return;
+	int f6 = 6*sn_first[s];
+	const T *L = arena+sn_off[s];
+	const int *R = rows+sn_rows_off[s];
+	int warp = threadIdx.x/32, lane = threadIdx.x%32, nw = blockDim.x/32;
+	for (int j = j0+warp; j < min(n6, j0+chunk); j += nw) {
+		const T *col = L+(int64_t)j*ld+n6;
+		T acc[K];
+#pragma unroll
+		for (int r = 0; r < K; r++) acc[r] = 0;
+		for (int t = lane; t < m6; t += 32) {
+			T l = col[t];
+			int g = 6*R[t/6]+t%6;
+#pragma unroll
+			for (int r = 0; r < K; r++) acc[r] += l*xp[(int64_t)r*n6tot+g];
+		}
+#pragma unroll
+		for (int r = 0; r < K; r++) {
+			T a = acc[r];
+			for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+			if (lane == 0) yp[(int64_t)r*n6tot+f6+j] -= a;
+		}
+	}
+}
+
+// backward part 2: x_s = E z, one thread per row i (E upper triangular)
+template <typename T, int K>
+__global__ void k_bwd_x(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
+                        const int *__restrict__ sn_n, const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
+                        const int64_t *__restrict__ sn_off, const T *__restrict__ arena,
+                        const T *__restrict__ yp, T *__restrict__ xp, int n6tot, int chunk)
+{
+	extern __shared__ unsigned char smem_raw[];
+	T *z = reinterpret_cast<T *>(smem_raw);
+	int s = lev_sn[blockIdx.y];
+	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
+	int i0 = blockIdx.x*chunk;
+	if (i0 >= n6) return;
+	int f6 = 6*sn_first[s];
+	for (int i = threadIdx.x; i < n6; i += blockDim.x)
+#pragma unroll
+		for (int r = 0; r < K; r++) z[r*n6+i] = yp[(int64_t)r*n6tot+f6+i];
+	__syncthreads();
+	const T *E = arena+sn_off[s]+F6;
+	for (int i = i0+threadIdx.x; i < min(n6, i0+chunk); i += blockDim.x) {
+		T acc[K];
+#pragma unroll
+		for (int r = 0; r < K; r++) acc[r] = 0;
+		for (int j = i; j < n6; j++) {
+			T e = E[(int64_t)j*ld+i];
+#pragma unroll
+			for (int r = 0; r < K; r++) acc[r] += e*z[r*n6+j];
+		}
+#pragma unroll
+		for (int r = 0; r < K; r++) xp[(int64_t)r*n6tot+f6+i] = acc[r];
+	}
+}
+
+template <typename T, int K>
+static int solve_k(DevFactor<T> &F, const DevSymbolic &D, const double *b, double *x, cudaStream_t st)
+{
+	int n = D.nblk, n6tot = 6*n;
+	int launches = 0;
+	int64_t wstride = D.w_elems;
+	k_permute_in<T><<<(6*n+255)/256, 256, 0, st>>>(n, K, D.iperm, b, F.xp);
+	launches++;
+	const int CH = 256;  // outputs / rows per CTA
+	// forward: leaves -> root
+	for (int l = 0; l < D.nlevels; l++) {
+		int cnt = D.h_level_off[l+1]-D.h_level_off[l];
+		if (!cnt) continue;
+		int maxn6 = D.max_n6;
+		int gx = (std::max(maxn6, 1)+CH-1)/CH;
+		size_t sm = sizeof(T)*K*(size_t)maxn6;
+		dim3 g1(gx, cnt);
+		k_fwd_y<T, K><<<g1, 256, sm, st>>>(D.level_sn+D.h_level_off[l], D.sn_first, D.sn_n, D.sn_m, D.sn_ld,
+		                                    D.sn_off, D.child_off, D.children, D.cinv_off, D.cinv, D.sn_woff,
+		                                    F.arena, F.w, wstride, F.xp, F.yp, n6tot, CH);
+		int gxw = (D.max_F+CH-1)/CH;
+		dim3 g2(gxw, cnt);
+		k_fwd_w<T, K><<<g2, 256, sm, st>>>(D.level_sn+D.h_level_off[l], D.sn_first, D.sn_n, D.sn_m, D.sn_ld,
+		                                    D.sn_off, D.child_off, D.children, D.cinv_off, D.cinv, D.sn_woff,
+		                                    F.arena, F.w, wstride, F.yp, n6tot, CH);
+		launches += 2;
+	}
+	// backward: root -> leaves
+	for (int l = D.nlevels-1; l >= 0; l--) {
+		int cnt = D.h_level_off[l+1]-D.h_level_off[l];
+		if (!cnt) continue;
+		int maxn6 = D.max_n6;
+		int gx = (std::max(maxn6, 1)+CH-1)/CH;
+		dim3 g(gx, cnt);
+		k_bwd_z<T, K><<<g, 256, 0, st>>>(D.level_sn+D.h_level_off[l], D.sn_first, D.sn_n, D.sn_m, D.sn_ld,
+		                                  D.sn_off, D.sn_rows_off, D.rows, F.arena, F.xp, F.yp, n6tot, CH);
+		size_t sm = sizeof(T)*K*(size_t)maxn6;
+		k_bwd_x<T, K><<<g, 256, sm, st>>>(D.level_sn+D.h_level_off[l], D.sn_first, D.sn_n, D.sn_m, D.sn_ld,
+		                                   D.sn_off, F.arena, F.yp, F.xp, n6tot, CH);
+		launches += 2;
+	}
+	k_permute_out<T><<<(6*n+255)/256, 256, 0, st>>>(n, K, D.iperm, F.xp, x);
+	launches++;
+	LFG_CUDA(cudaGetLastError());
+	return launches;
+}
+
+template <typename T>
+static void set_smem_limits(int maxn6)
+{
+	static int done_for = -1;
+	size_t need = sizeof(T)*4*(size_t)maxn6;
+	if ((int)need <= done_for) return;
+	if (need > 48*1024) {
+		cudaFuncSetAttribute(k_fwd_y<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+		cudaFuncSetAttribute(k_fwd_y<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+		cudaFuncSetAttribute(k_fwd_y<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+		cudaFuncSetAttribute(k_fwd_y<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+		cudaFuncSetAttribute(k_fwd_w<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+		cudaFuncSetAttribute(k_fwd_w<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+		cudaFuncSetAttribute(k_fwd_w<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+		cudaFuncSetAttribute(k_fwd_w<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+		cudaFuncSetAttribute(k_bwd_x<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+		cudaFuncSetAttribute(k_bwd_x<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+		cudaFuncSetAttribute(k_bwd_x<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+		cudaFuncSetAttribute(k_bwd_x<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+	}
+	done_for = (int)need;
+}
+
+template <typename T>
+int factor_solve(DevFactor<T> &F, const DevSymbolic &D, int k, const double *b, double *x, cudaStream_t st)
+{
+	int launches = 0;
+	for (int r0 = 0; r0 < k; r0 += 4) {
+		int kk = std::min(4, k-r0);
+		const double *bb = b+(int64_t)r0*6*D.nblk;
+		double *xx = x+(int64_t)r0*6*D.nblk;
+		switch (kk) {
+		case 1: launches += solve_k<T, 1>(F, D, bb, xx, st); break;
+		case 2: launches += solve_k<T, 2>(F, D, bb, xx, st); break;
+		case 3: launches += solve_k<T, 3>(F, D, bb, xx, st); break;
+		default: launches += solve_k<T, 4>(F, D, bb, xx, st); break;
+		}
+	}
+	return launches;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 block residual r = b - A x (row-block gather, deterministic)
+// ---------------------------------------------------------------------------
+__global__ void k_residual(int n, int k, const double *__restrict__ dbl, const double *__restrict__ odbl,
+                           const int *__restrict__ od_row, const int *__restrict__ od_col,
+                           const int *__restrict__ lo_ptr, const int *__restrict__ lo_idx,
+                           const int *__restrict__ up_ptr, const int *__restrict__ up_idx,
+                           const double *__restrict__ b, const double *__restrict__ x, double *__restrict__ r)
+{
+	int i = blockIdx.x*blockDim.x+threadIdx.x;
+	if (i >= n) return;
+	double m[36];
+	for (int rh = 0; rh < k; rh++) {
+		const double *xv = x+(int64_t)rh*6*n;
+		double acc[6];
+		d15_to_dense(dbl+15*(int64_t)i, m);
+		for (int a = 0; a < 6; a++) {
+			double s = 0;
+			for (int c = 0; c < 6; c++) {
+				double mv = (a >= c) ? m[a*6+c] : m[c*6+a];
+				s += mv*xv[6*i+c];
+			}
+			acc[a] = s;
+		}
+		// blocks in row i below the diagonal: (row i, col j<i) = M
+		for (int t = lo_ptr[i]; t < lo_ptr[i+1]; t++) {
+			int e = lo_idx[t];
+			int j = od_col[e];
+			od18_to_dense(odbl+18*(int64_t)e, m);
+			for (int a = 0; a < 6; a++) {
+				double s = 0;
+				for (int c = 0; c < 6; c++) s += m[a*6+c]*xv[6*j+c];
+				acc[a] += s;
+			}
+		}
+		// blocks in row i above the diagonal: (row i, col j>i) = M(j,i)^T
+		for (int t = up_ptr[i]; t < up_ptr[i+1]; t++) {
+			int e = up_idx[t];
+			int j = od_row[e];
+			od18_to_dense(odbl+18*(int64_t)e, m);
+			for (int a = 0; a < 6; a++) {
+				double s = 0;
+				for (int c = 0; c < 6; c++) s += m[c*6+a]*xv[6*j+c];
+				acc[a] += s;
+			}
+		}
+		for (int a = 0; a < 6; a++) r[(int64_t)rh*6*n+6*i+a] = b[(int64_t)rh*6*n+6*i+a]-acc[a];
+	}
+}
+
+void block_residual(const DevBlockMatrix &A, int k, const double *b, const double *x, double *r,
+                    cudaStream_t st)
+{
+	k_residual<<<(A.n+127)/128, 128, 0, st>>>(A.n, k, A.dblocks, A.odblocks, A.od_row, A.od_col, A.lo_ptr,
+	                                          A.lo_idx, A.up_ptr, A.up_idx, b, x, r);
+}
+
+__global__ void k_axpy(int64_t total, const double *__restrict__ d, double *__restrict__ x)
+{
+	int64_t t = blockIdx.x*(int64_t)blockDim.x+threadIdx.x;
+	if (t < total) x[t] += d[t];
+}
+
+void axpy_vec(int n, int k, const double *d, double *x, cudaStream_t st)
+{
+	int64_t total = (int64_t)6*n*k;
+	k_axpy<<<(int)((total+255)/256), 256, 0, st>>>(total, d, x);
+}
+
+// per-RHS sums of squares of r and b, single CTA per RHS (fixed order)
+__global__ void k_norms(int n6, const double *__restrict__ r, const double *__restrict__ b, double *out)
+{
+	__shared__ double sr[256], sb[256];
+	int rh = blockIdx.x;
+	double a = 0, c = 0;
+	for (int i = threadIdx.x; i < n6; i += 256) {
+		double u = r[(int64_t)rh*n6+i], v = b[(int64_t)rh*n6+i];
+		a += u*u; c += v*v;
+	}
+	sr[threadIdx.x] = a; sb[threadIdx.x] = c;
+	__syncthreads();
+	for (int o = 128; o > 0; o >>= 1) {
+		if (threadIdx.x < o) { sr[threadIdx.x] += sr[threadIdx.x+o]; sb[threadIdx.x] += sb[threadIdx.x+o]; }
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) { out[2*rh] = sr[0]; out[2*rh+1] = sb[0]; }
+}
+
+void residual_norms(int n6, int k, const double *r, const double *b, double *out, cudaStream_t st)
+{
+	k_norms<<<k, 256, 0, st>>>(n6, r, b, out);
+}
+
+int factor_tile_size(int precision) { return precision == LFG_PREC_FP64 ? Cfg<double>::TILE : Cfg<float>::TILE; }
+int factor_panel_width(int precision) { return precision == LFG_PREC_FP64 ? Cfg<double>::NB : Cfg<float>::NB; }
+
+template void factor_alloc<double>(DevFactor<double> &, const DevSymbolic &, int);
+template void factor_alloc<float>(DevFactor<float> &, const DevSymbolic &, int);
+template void factor_free<double>(DevFactor<double> &);
+template void factor_free<float>(DevFactor<float> &);
+template int factor_numeric<double>(DevFactor<double> &, const DevSymbolic &, const double *, const double *, cudaStream_t);
+template int factor_numeric<float>(DevFactor<float> &, const DevSymbolic &, const double *, const double *, cudaStream_t);
+template int factor_solve<double>(DevFactor<double> &, const DevSymbolic &, int, const double *, double *, cudaStream_t);
+template int factor_solve<float>(DevFactor<float> &, const DevSymbolic &, int, const double *, double *, cudaStream_t);
+
+} // namespace lfg

@@ -1,0 +1,158 @@
+// lfg_internal.h -- internal declarations shared by the host driver (C++) and
+// the CUDA translation units of the GB300 engine.  Not part of the C ABI.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/lfdem_gb300.h"
+
+namespace lfg {
+
+// ---------------------------------------------------------------------------
+// error handling: every CUDA call in the host driver goes through LFG_CUDA,
+// which throws lfg::Error; the C-ABI layer converts it to a status code.
+// ---------------------------------------------------------------------------
+struct Error {
+	int code;
+	int info;
+	std::string msg;
+};
+
+#define LFG_CUDA(call)                                                                     \
+	do {                                                                                   \
+		cudaError_t e_ = (call);                                                       \
+		if (e_ != cudaSuccess)                                                         \
+			throw ::lfg::Error{e_ == cudaErrorMemoryAllocation ? LFG_ERR_OOM : LFG_ERR_CUDA, \
+			                   (int)e_, std::string(#call) + ": " + cudaGetErrorString(e_)}; \
+	} while (0)
+
+// ---------------------------------------------------------------------------
+// Symbolic analysis of the block matrix (nested dissection + multifrontal
+// assembly tree).  Computed on the host, mirrored to the device.
+// ---------------------------------------------------------------------------
+struct Symbolic {
+	int nblk = 0;                 // particles (6x6 blocks)
+	std::vector<int> perm;        // perm[k] = particle at permuted position k
+	std::vector<int> iperm;       // iperm[particle] = permuted position
+	// supernodes, in postorder (children before parents)
+	int nsn = 0;
+	std::vector<int> sn_first, sn_n, sn_m, sn_parent, sn_level;
+	std::vector<int> sn_rows_off;     // into rows[] (m entries each, permuted block ids)
+	std::vector<int> rows;
+	std::vector<int64_t> sn_off;      // front arena offsets (elements)
+	std::vector<int> sn_ld;           // front leading dimension = 6F + 6n
+	std::vector<int64_t> sn_woff;     // forward-solve update vector offsets (elements)
+	// children and inverse maps: for child c of parent p, inv[cinv_off[c] + b]
+	// (b in [0, F_p)) = child front block index or -1
+	std::vector<int> child_off, children;   // CSR over supernodes
+	std::vector<int64_t> cinv_off;
+	std::vector<int> cinv;
+	// levels (0 = leaves)
+	int nlevels = 0;
+	std::vector<int> level_off, level_sn;   // CSR: supernodes of each level
+	// A-block scatter: for each particle (D block) and each off-diagonal
+	// block e (in the caller's order): target supernode, front block row/col,
+	// transpose flag.
+	std::vector<int> d_sn, d_bc;
+	std::vector<int> od_sn, od_br, od_bc, od_tr;
+	std::vector<int> level_d_off, level_d;     // D blocks per level
+	std::vector<int> level_od_off, level_od;   // OD blocks per level
+	int64_t arena_elems = 0;
+	int64_t w_elems = 0;
+	int max_F = 0;
+	int64_t nnz_L = 0;
+	double flops = 0;
+};
+
+// Build the symbolic analysis.  od_row/od_col: nb lower off-diagonal blocks
+// (the pattern).  pos (3 * nblk, may be null) drives a geometric nested
+// dissection; otherwise a breadth-first level-set dissection is used.
+void symbolic_analyze(Symbolic &S, int nblk, int nb, const int32_t *od_row,
+                      const int32_t *od_col, const double *pos, double lx, double ly, double lz,
+                      int leaf_size);
+
+// ---------------------------------------------------------------------------
+// Device-side multifrontal factor (one precision per instance).
+// ---------------------------------------------------------------------------
+struct DevSymbolic {
+	int nblk = 0, nsn = 0, nlevels = 0, nb = 0;
+	int *perm = nullptr, *iperm = nullptr;
+	int *sn_first = nullptr, *sn_n = nullptr, *sn_m = nullptr, *sn_ld = nullptr;
+	int *sn_rows_off = nullptr, *rows = nullptr;
+	int64_t *sn_off = nullptr, *sn_woff = nullptr;
+	int *child_off = nullptr, *children = nullptr;
+	int64_t *cinv_off = nullptr;
+	int *cinv = nullptr;
+	int *level_sn = nullptr;
+	int *d_sn = nullptr, *d_bc = nullptr;
+	int *od_sn = nullptr, *od_br = nullptr, *od_bc = nullptr, *od_tr = nullptr;
+	int *level_d = nullptr, *level_od = nullptr;
+	// per-level / per-panel task lists
+	int *col_tasks = nullptr;      // (sn, col) pairs for the assembly kernel
+	int4 *panel_tasks = nullptr;   // (sn, row0, k, nrows)
+	int4 *tile_tasks = nullptr;    // (sn, row0, col0, k)
+	// host-side launch plan
+	struct Launch { int kind; int level; int k; int64_t off; int count; };
+	std::vector<Launch> factor_plan;
+	std::vector<int> h_level_off, h_level_d_off, h_level_od_off;
+	std::vector<int64_t> h_col_task_off;
+	int64_t arena_elems = 0, w_elems = 0;
+	int max_F = 0;
+	int max_n6 = 0;
+	double flops = 0;
+	int64_t nnz_L = 0;
+};
+
+// Tile edge and panel width the factor kernels use for a precision; the
+// launch plan built by dev_symbolic_upload must use the same values.
+int factor_tile_size(int precision);
+int factor_panel_width(int precision);
+
+void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb, int tile,
+                         cudaStream_t st);
+void dev_symbolic_free(DevSymbolic &D);
+
+// Factor arenas and launchers (lfg_factor.cu).
+template <typename T> struct DevFactor {
+	T *arena = nullptr;   // fronts
+	T *w = nullptr;       // forward-solve update vectors
+	T *xp = nullptr, *yp = nullptr; // permuted solve workspaces (k * 6n)
+	int64_t arena_cap = 0, w_cap = 0, x_cap = 0;
+	int *status = nullptr; // device: first non-positive pivot column + 1 (0 = ok)
+};
+
+template <typename T> void factor_alloc(DevFactor<T> &F, const DevSymbolic &D, int kmax);
+template <typename T> void factor_free(DevFactor<T> &F);
+
+// Numeric factorisation from compact blocks (dblocks n x 15, odblocks nb x 18,
+// both FP64 device arrays).  Launches only; status left in F.status.
+template <typename T>
+int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *d_dblocks,
+                   const double *d_odblocks, cudaStream_t st);
+
+// Solve with k right-hand sides: b, x device arrays k x 6n, FP64 (x may alias b).
+template <typename T>
+int factor_solve(DevFactor<T> &F, const DevSymbolic &D, int k, const double *b, double *x,
+                 cudaStream_t st);
+
+// y = A x for the compact block matrix (FP64), k vectors, and r = b - A x.
+// Lower/upper adjacency lists for the per-block-row gather.
+struct DevBlockMatrix {
+	int n = 0, nb = 0;
+	double *dblocks = nullptr;   // n x 15
+	double *odblocks = nullptr;  // nb x 18
+	int *od_row = nullptr, *od_col = nullptr;
+	int *lo_ptr = nullptr, *lo_idx = nullptr;   // for row block i: OD entries with row == i
+	int *up_ptr = nullptr, *up_idx = nullptr;   // OD entries with col == i
+};
+void block_residual(const DevBlockMatrix &A, int k, const double *b, const double *x, double *r,
+                    cudaStream_t st);
+void axpy_vec(int n, int k, const double *d, double *x, cudaStream_t st);
+// per-RHS squared norms of r and b, written to out[2k] (device)
+void residual_norms(int n6, int k, const double *r, const double *b, double *out, cudaStream_t st);
+
+} // namespace lfg

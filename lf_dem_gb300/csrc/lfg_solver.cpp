@@ -1,0 +1,252 @@
+// lfg_solver.cpp -- the resistance solve behind LF_DEM's StokesSolver
+// (StokesSolver.h:198-285), as a device object: compact block matrix in HBM,
+// symbolic analysis on pattern change only (StokesSolver.cpp:955-962),
+// multifrontal factorisation in FP64 or FP32, solves with k right-hand sides,
+// FP64 iterative refinement for the FP32 form.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "lfg_solver.h"
+
+namespace lfg {
+
+Solver::Solver(int n, const lfg_options &o, cudaStream_t st) : n_(n), opt_(o), st_(st)
+{
+	A_.n = n;
+	LFG_CUDA(cudaMalloc((void **)&A_.dblocks, sizeof(double)*15*(size_t)std::max(n, 1)));
+	LFG_CUDA(cudaMalloc((void **)&A_.lo_ptr, sizeof(int)*(n+1)));
+	LFG_CUDA(cudaMalloc((void **)&A_.up_ptr, sizeof(int)*(n+1)));
+	LFG_CUDA(cudaMallocHost((void **)&h_norms_, sizeof(double)*64));
+	LFG_CUDA(cudaMalloc((void **)&d_norms_, sizeof(double)*64));
+	LFG_CUDA(cudaMallocHost((void **)&h_status_, sizeof(int)*4));
+}
+
+Solver::~Solver()
+{
+	dev_symbolic_free(D_);
+	factor_free(F64_);
+	factor_free(F32_);
+	void *p[] = {A_.dblocks, A_.odblocks, A_.od_row, A_.od_col, A_.lo_ptr, A_.lo_idx, A_.up_ptr, A_.up_idx,
+	             d_norms_, ref_x_, ref_r_, ref_d_, hb_, hx_};
+	for (void *q : p) if (q) cudaFree(q);
+	if (h_norms_) cudaFreeHost(h_norms_);
+	if (h_status_) cudaFreeHost(h_status_);
+	for (auto &g : graphs_) if (g.exec) cudaGraphExecDestroy(g.exec);
+}
+
+void Solver::set_pattern(int nb, const int32_t *row, const int32_t *col, const double *pos, double lx,
+                         double ly, double lz, bool device_ptrs)
+{
+	std::vector<int32_t> r(nb), c(nb);
+	if (device_ptrs) {
+		if (nb) {
+			LFG_CUDA(cudaMemcpyAsync(r.data(), row, sizeof(int32_t)*nb, cudaMemcpyDeviceToHost, st_));
+			LFG_CUDA(cudaMemcpyAsync(c.data(), col, sizeof(int32_t)*nb, cudaMemcpyDeviceToHost, st_));
+			LFG_CUDA(cudaStreamSynchronize(st_));
+		}
+	} else {
+		std::copy(row, row+nb, r.begin());
+		std::copy(col, col+nb, c.begin());
+	}
+	for (int e = 0; e < nb; e++)
+		if (r[e] <= c[e] || r[e] >= n_ || c[e] < 0)
+			throw Error{LFG_ERR_BAD_ARG, e, "off-diagonal block must have n > row > col >= 0"};
+	nb_ = nb;
+	symbolic_analyze(S_, n_, nb, r.data(), c.data(), pos, lx, ly, lz, opt_.leaf_size);
+	dev_symbolic_upload(D_, S_, nb, factor_panel_width(opt_.precision), factor_tile_size(opt_.precision), st_);
+	if (opt_.precision == LFG_PREC_FP64) factor_alloc(F64_, D_, 4);
+	else factor_alloc(F32_, D_, 4);
+	// block matrix pattern + row adjacency for the residual
+	if (A_.odblocks) cudaFree(A_.odblocks);
+	if (A_.od_row) cudaFree(A_.od_row);
+	if (A_.od_col) cudaFree(A_.od_col);
+	if (A_.lo_idx) cudaFree(A_.lo_idx);
+	if (A_.up_idx) cudaFree(A_.up_idx);
+	A_.odblocks = nullptr; A_.od_row = A_.od_col = A_.lo_idx = A_.up_idx = nullptr;
+	A_.nb = nb;
+	size_t nbb = std::max(nb, 1);
+	LFG_CUDA(cudaMalloc((void **)&A_.odblocks, sizeof(double)*18*nbb));
+	LFG_CUDA(cudaMalloc((void **)&A_.od_row, sizeof(int)*nbb));
+	LFG_CUDA(cudaMalloc((void **)&A_.od_col, sizeof(int)*nbb));
+	LFG_CUDA(cudaMalloc((void **)&A_.lo_idx, sizeof(int)*nbb));
+	LFG_CUDA(cudaMalloc((void **)&A_.up_idx, sizeof(int)*nbb));
+	std::vector<int> lp(n_+1, 0), upp(n_+1, 0), li(nb), ui(nb);
+	for (int e = 0; e < nb; e++) { lp[r[e]+1]++; upp[c[e]+1]++; }
+	for (int i = 0; i < n_; i++) { lp[i+1] += lp[i]; upp[i+1] += upp[i]; }
+	{
+		std::vector<int> f1(lp.begin(), lp.end()-1), f2(upp.begin(), upp.end()-1);
+		for (int e = 0; e < nb; e++) { li[f1[r[e]]++] = e; ui[f2[c[e]]++] = e; }
+	}
+	if (nb) {
+		LFG_CUDA(cudaMemcpyAsync(A_.od_row, r.data(), sizeof(int)*nb, cudaMemcpyHostToDevice, st_));
+		LFG_CUDA(cudaMemcpyAsync(A_.od_col, c.data(), sizeof(int)*nb, cudaMemcpyHostToDevice, st_));
+		LFG_CUDA(cudaMemcpyAsync(A_.lo_idx, li.data(), sizeof(int)*nb, cudaMemcpyHostToDevice, st_));
+		LFG_CUDA(cudaMemcpyAsync(A_.up_idx, ui.data(), sizeof(int)*nb, cudaMemcpyHostToDevice, st_));
+	}
+	LFG_CUDA(cudaMemcpyAsync(A_.lo_ptr, lp.data(), sizeof(int)*(n_+1), cudaMemcpyHostToDevice, st_));
+	LFG_CUDA(cudaMemcpyAsync(A_.up_ptr, upp.data(), sizeof(int)*(n_+1), cudaMemcpyHostToDevice, st_));
+	LFG_CUDA(cudaStreamSynchronize(st_));
+	for (auto &g : graphs_) if (g.exec) cudaGraphExecDestroy(g.exec);
+	graphs_.clear();
+	analyzed_ = true;
+	symbolic_runs_++;
+}
+
+void Solver::set_values_host(const double *dblocks, const double *odblocks)
+{
+	LFG_CUDA(cudaMemcpyAsync(A_.dblocks, dblocks, sizeof(double)*15*n_, cudaMemcpyHostToDevice, st_));
+	if (nb_) LFG_CUDA(cudaMemcpyAsync(A_.odblocks, odblocks, sizeof(double)*18*nb_, cudaMemcpyHostToDevice, st_));
+}
+
+// Launch the factorisation; with graphs, the launch sequence is captured once
+// per symbolic analysis and replayed.
+void Solver::factorize_async()
+{
+	if (!analyzed_) throw Error{LFG_ERR_BAD_ARG, 0, "factorize before set_blocks"};
+	auto body = [&]() {
+		if (opt_.precision == LFG_PREC_FP64) launches_factor_ = factor_numeric(F64_, D_, A_.dblocks, A_.odblocks, st_);
+		else launches_factor_ = factor_numeric(F32_, D_, A_.dblocks, A_.odblocks, st_);
+	};
+	run_graph(0, 0, A_.dblocks, A_.odblocks, body);
+}
+
+void Solver::run_graph(int kind, int k, const void *b, const void *x, const std::function<void()> &body)
+{
+	if (!opt_.use_graphs) { body(); return; }
+	for (auto &g : graphs_) {
+		if (g.kind == kind && g.k == k && g.b == b && g.x == x) {
+			LFG_CUDA(cudaGraphLaunch(g.exec, st_));
+			return;
+		}
+	}
+	cudaGraph_t graph;
+	LFG_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+	try {
+		body();
+	} catch (...) {
+		cudaStreamEndCapture(st_, &graph);
+		throw;
+	}
+	LFG_CUDA(cudaStreamEndCapture(st_, &graph));
+	GraphEntry e;
+	e.kind = kind; e.k = k; e.b = b; e.x = x;
+	LFG_CUDA(cudaGraphInstantiate(&e.exec, graph, 0));
+	cudaGraphDestroy(graph);
+	graphs_.push_back(e);
+	LFG_CUDA(cudaGraphLaunch(e.exec, st_));
+}
+
+int Solver::check_factor(lfg_status *st)
+{
+	int *dst = opt_.precision == LFG_PREC_FP64 ? F64_.status : F32_.status;
+	LFG_CUDA(cudaMemcpyAsync(h_status_, dst, sizeof(int), cudaMemcpyDeviceToHost, st_));
+	LFG_CUDA(cudaStreamSynchronize(st_));
+	if (*h_status_ != 0x7fffffff) {
+		int q = *h_status_-1;
+		int orig = S_.perm[q/6]*6+q%6;
+		if (st) {
+			st->code = LFG_ERR_NOT_SPD;
+			st->info = orig+1;
+			snprintf(st->msg, sizeof st->msg, "non-positive pivot at column %d (particle %d)", orig, orig/6);
+		}
+		return LFG_ERR_NOT_SPD;
+	}
+	return LFG_OK;
+}
+
+void Solver::ensure_refine_ws(int k)
+{
+	int64_t need = (int64_t)6*n_*std::max(k, 1);
+	if (ref_cap_ >= need) return;
+	if (ref_x_) cudaFree(ref_x_);
+	if (ref_r_) cudaFree(ref_r_);
+	if (ref_d_) cudaFree(ref_d_);
+	LFG_CUDA(cudaMalloc((void **)&ref_x_, sizeof(double)*need));
+	LFG_CUDA(cudaMalloc((void **)&ref_r_, sizeof(double)*need));
+	LFG_CUDA(cudaMalloc((void **)&ref_d_, sizeof(double)*need));
+	ref_cap_ = need;
+}
+
+// k RHS on the device.  FP64: one direct solve.  FP32: x = 0, repeat
+// { d = (L L^T)_32^-1 r ; x += d ; r = b - A x } until max relative residual
+// <= refine_tol.
+int Solver::solve_device(int k, const double *b, double *x, lfg_status *st, bool sync_check)
+{
+	if (k <= 0) return LFG_OK;
+	if (opt_.precision == LFG_PREC_FP64) {
+		run_graph(1, k, b, x, [&]() { launches_solve_ = factor_solve(F64_, D_, k, b, x, st_); });
+		last_iters_ = 0;
+		last_resid_ = 0;
+		return LFG_OK;
+	}
+	ensure_refine_ws(k);
+	int64_t tot = (int64_t)6*n_*k;
+	LFG_CUDA(cudaMemsetAsync(ref_x_, 0, sizeof(double)*tot, st_));
+	LFG_CUDA(cudaMemcpyAsync(ref_r_, b, sizeof(double)*tot, cudaMemcpyDeviceToDevice, st_));
+	int it = 0;
+	double worst = 0;
+	for (it = 1; it <= opt_.refine_max_iter; it++) {
+		run_graph(2, k, b, nullptr, [&]() {
+			launches_solve_ = factor_solve(F32_, D_, k, ref_r_, ref_d_, st_);
+			axpy_vec(n_, k, ref_d_, ref_x_, st_);
+			block_residual(A_, k, b, ref_x_, ref_r_, st_);
+			residual_norms(6*n_, k, ref_r_, b, d_norms_, st_);
+		});
+		LFG_CUDA(cudaMemcpyAsync(h_norms_, d_norms_, sizeof(double)*2*k, cudaMemcpyDeviceToHost, st_));
+		LFG_CUDA(cudaStreamSynchronize(st_));
+		worst = 0;
+		for (int r = 0; r < k; r++) {
+			double rb = h_norms_[2*r+1] > 0 ? std::sqrt(h_norms_[2*r]/h_norms_[2*r+1]) : std::sqrt(h_norms_[2*r]);
+			if (!(rb == rb)) rb = INFINITY;
+			worst = std::max(worst, rb);
+		}
+		if (worst <= opt_.refine_tol) break;
+	}
+	last_iters_ = std::min(it, opt_.refine_max_iter);
+	last_resid_ = worst;
+	LFG_CUDA(cudaMemcpyAsync(x, ref_x_, sizeof(double)*tot, cudaMemcpyDeviceToDevice, st_));
+	if (st) { st->refine_iters = last_iters_; st->refine_residual = worst; }
+	if (!(worst <= opt_.refine_tol)) {
+		if (st) {
+			st->code = LFG_ERR_NOT_CONVERGED;
+			snprintf(st->msg, sizeof st->msg, "FP32 refinement reached %.3e after %d iterations", worst, last_iters_);
+		}
+		return LFG_ERR_NOT_CONVERGED;
+	}
+	(void)sync_check;
+	return LFG_OK;
+}
+
+int Solver::solve_host(int k, const double *rhs, double *x, lfg_status *st)
+{
+	int64_t tot = (int64_t)6*n_*k;
+	if (hcap_ < tot) {
+		if (hb_) cudaFree(hb_);
+		if (hx_) cudaFree(hx_);
+		LFG_CUDA(cudaMalloc((void **)&hb_, sizeof(double)*tot));
+		LFG_CUDA(cudaMalloc((void **)&hx_, sizeof(double)*tot));
+		hcap_ = tot;
+	}
+	LFG_CUDA(cudaMemcpyAsync(hb_, rhs, sizeof(double)*tot, cudaMemcpyHostToDevice, st_));
+	int rc = solve_device(k, hb_, hx_, st, true);
+	LFG_CUDA(cudaMemcpyAsync(x, hx_, sizeof(double)*tot, cudaMemcpyDeviceToHost, st_));
+	LFG_CUDA(cudaStreamSynchronize(st_));
+	return rc;
+}
+
+void Solver::stats(lfg_solver_stats *o) const
+{
+	std::memset(o, 0, sizeof *o);
+	o->n_blocks = S_.nblk;
+	o->n_supernodes = S_.nsn;
+	o->n_levels = S_.nlevels;
+	o->max_front = S_.max_F;
+	o->nnz_L = S_.nnz_L;
+	o->flops_factor = S_.flops;
+	o->front_bytes = S_.arena_elems*(opt_.precision == LFG_PREC_FP64 ? 8 : 4);
+	o->n_factor_launches = launches_factor_;
+	o->n_solve_launches = launches_solve_;
+}
+
+} // namespace lfg

@@ -1,0 +1,69 @@
+// lfg_solver.h -- device resistance solver (C++ side of lfg_solver_*).
+#pragma once
+#include <functional>
+
+#include "lfg_internal.h"
+
+namespace lfg {
+
+class Solver {
+public:
+	Solver(int n, const lfg_options &o, cudaStream_t st);
+	~Solver();
+	// pattern of the lower off-diagonal blocks; re-runs the symbolic analysis
+	void set_pattern(int nb, const int32_t *row, const int32_t *col, const double *pos, double lx,
+	                 double ly, double lz, bool device_ptrs);
+	void set_values_host(const double *dblocks, const double *odblocks);
+	// device arrays of the compact values (dblocks n x 15, odblocks nb x 18)
+	double *d_dblocks() { return A_.dblocks; }
+	double *d_odblocks() { return A_.odblocks; }
+	void factorize_async();
+	int check_factor(lfg_status *st);
+	int solve_device(int k, const double *b, double *x, lfg_status *st, bool sync_check);
+	int solve_host(int k, const double *rhs, double *x, lfg_status *st);
+	void stats(lfg_solver_stats *o) const;
+	bool analyzed() const { return analyzed_; }
+	int n() const { return n_; }
+	int nb() const { return nb_; }
+	int symbolic_runs() const { return symbolic_runs_; }
+	int last_iters() const { return last_iters_; }
+	double last_resid() const { return last_resid_; }
+	double flops() const { return S_.flops; }
+	int64_t nnz_L() const { return S_.nnz_L; }
+	int launches_factor() const { return launches_factor_; }
+	int launches_solve() const { return launches_solve_; }
+	const lfg_options &options() const { return opt_; }
+
+private:
+	struct GraphEntry {
+		int kind = 0, k = 0;
+		const void *b = nullptr;
+		const void *x = nullptr;
+		cudaGraphExec_t exec = nullptr;
+	};
+	void run_graph(int kind, int k, const void *b, const void *x, const std::function<void()> &body);
+	void ensure_refine_ws(int k);
+
+	int n_ = 0, nb_ = 0;
+	lfg_options opt_;
+	cudaStream_t st_;
+	Symbolic S_;
+	DevSymbolic D_;
+	DevFactor<double> F64_;
+	DevFactor<float> F32_;
+	DevBlockMatrix A_;
+	bool analyzed_ = false;
+	int symbolic_runs_ = 0;
+	double *h_norms_ = nullptr, *d_norms_ = nullptr;
+	int *h_status_ = nullptr;
+	double *ref_x_ = nullptr, *ref_r_ = nullptr, *ref_d_ = nullptr;
+	int64_t ref_cap_ = 0;
+	double *hb_ = nullptr, *hx_ = nullptr;
+	int64_t hcap_ = 0;
+	std::vector<GraphEntry> graphs_;
+	int last_iters_ = 0;
+	double last_resid_ = 0;
+	int launches_factor_ = 0, launches_solve_ = 0;
+};
+
+} // namespace lfg

@@ -1,0 +1,464 @@
+// lfg_symbolic.cpp -- symbolic analysis for the device multifrontal Cholesky
+// that replaces CHOLMOD's cholmod_analyze (LF_DEM/StokesSolver.cpp:950-962).
+//
+// The matrix is R_FU in 6x6 blocks (one block row/column per particle).  The
+// ordering is a nested dissection of the block graph: recursive bisection
+// (coordinate median when particle positions are given, breadth-first level
+// sets otherwise) with the smaller one-sided vertex boundary as separator.
+// The dissection tree is used directly as the multifrontal assembly tree:
+// each separator (and each leaf sub-domain) is one supernode whose columns are
+// contiguous in the ordering, and whose front is dense.  The row structure of
+// a supernode is the union of its columns' adjacency and its children's row
+// structures, restricted to later columns -- every such row belongs to an
+// ancestor, so a child's update matrix always fits in its parent's front.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <queue>
+
+#include "lfg_internal.h"
+
+namespace lfg {
+namespace {
+
+struct Graph {
+	std::vector<int> ptr, adj;
+};
+
+Graph build_graph(int n, int nb, const int32_t *r, const int32_t *c)
+{
+	Graph g;
+	std::vector<int> deg(n, 0);
+	for (int e = 0; e < nb; e++) {
+		if (r[e] == c[e]) continue;
+		deg[r[e]]++;
+		deg[c[e]]++;
+	}
+	g.ptr.assign(n+1, 0);
+	for (int i = 0; i < n; i++) g.ptr[i+1] = g.ptr[i] + deg[i];
+	g.adj.resize(g.ptr[n]);
+	std::vector<int> fill(g.ptr.begin(), g.ptr.end()-1);
+	for (int e = 0; e < nb; e++) {
+		if (r[e] == c[e]) continue;
+		g.adj[fill[r[e]]++] = c[e];
+		g.adj[fill[c[e]]++] = r[e];
+	}
+	for (int i = 0; i < n; i++) {
+		std::sort(g.adj.begin()+g.ptr[i], g.adj.begin()+g.ptr[i+1]);
+		auto end = std::unique(g.adj.begin()+g.ptr[i], g.adj.begin()+g.ptr[i+1]);
+		// keep duplicates out of the degree count (pattern lists are unique
+		// pairs; this only guards against repeated entries)
+		for (auto it = end; it != g.adj.begin()+g.ptr[i+1]; ++it) *it = -1;
+	}
+	return g;
+}
+
+struct TNode {
+	std::vector<int> cols;
+	std::vector<int> kids;
+};
+
+struct Dissector {
+	const Graph &g;
+	const double *pos;
+	bool twod;
+	int leaf;
+	std::vector<TNode> nodes;
+	std::vector<int> stamp, side, level;
+	int cur = 0;
+
+	Dissector(const Graph &g_, const double *pos_, bool twod_, int leaf_, int n)
+	    : g(g_), pos(pos_), twod(twod_), leaf(leaf_), stamp(n, -1), side(n, 0), level(n, -1) {}
+
+	// one-sided vertex separator for the current side[] labelling of S
+	void boundary(const std::vector<int> &S, int st, std::vector<int> &b0, std::vector<int> &b1)
+	{
+		b0.clear(); b1.clear();
+		for (int v : S) {
+			bool cross = false;
+			for (int k = g.ptr[v]; k < g.ptr[v+1]; k++) {
+				int u = g.adj[k];
+				if (u < 0 || stamp[u] != st) continue;
+				if (side[u] != side[v]) { cross = true; break; }
+			}
+			if (cross) (side[v] == 0 ? b0 : b1).push_back(v);
+		}
+	}
+
+	std::vector<int> split_geometric(const std::vector<int> &S, int st)
+	{
+		std::vector<int> best;
+		bool have = false;
+		std::vector<int> b0, b1;
+		std::vector<std::pair<double,int>> key(S.size());
+		std::vector<int> best_side;
+		for (int ax = 0; ax < 3; ax++) {
+			if (twod && ax == 1) continue;
+			for (size_t t = 0; t < S.size(); t++) key[t] = {pos[3*S[t]+ax], S[t]};
+			size_t mid = S.size()/2;
+			std::nth_element(key.begin(), key.begin()+mid, key.end());
+			for (size_t t = 0; t < S.size(); t++) side[key[t].second] = t < mid ? 0 : 1;
+			boundary(S, st, b0, b1);
+			const std::vector<int> &sep = b0.size() <= b1.size() ? b0 : b1;
+			if (!have || sep.size() < best.size()) {
+				best = sep;
+				have = true;
+				best_side.resize(S.size());
+				for (size_t t = 0; t < S.size(); t++) best_side[t] = side[S[t]];
+			}
+		}
+		for (size_t t = 0; t < S.size(); t++) side[S[t]] = best_side[t];
+		return best;
+	}
+
+	// breadth-first level structure from a pseudo-peripheral vertex; the
+	// level holding the median vertex is the separator
+	std::vector<int> split_bfs(const std::vector<int> &S, int st)
+	{
+		auto bfs = [&](int src, std::vector<int> &order) {
+			for (int v : S) level[v] = -1;
+			order.clear();
+			std::queue<int> q;
+			q.push(src); level[src] = 0;
+			while (!q.empty()) {
+				int v = q.front(); q.pop(); order.push_back(v);
+				for (int k = g.ptr[v]; k < g.ptr[v+1]; k++) {
+					int u = g.adj[k];
+					if (u < 0 || stamp[u] != st || level[u] >= 0) continue;
+					level[u] = level[v]+1;
+					q.push(u);
+				}
+			}
+		};
+		std::vector<int> order;
+		int src = S[0];
+		for (int it = 0; it < 3; it++) {
+			bfs(src, order);
+			src = order.back();
+		}
+		bfs(src, order);
+		if (order.size() < S.size()) {
+			// disconnected: reachable part vs the rest, empty separator
+			for (int v : S) side[v] = level[v] >= 0 ? 0 : 1;
+			return {};
+		}
+		int lmid = level[order[order.size()/2]];
+		std::vector<int> sep;
+		for (int v : S) {
+			if (level[v] < lmid) side[v] = 0;
+			else if (level[v] > lmid) side[v] = 1;
+			else { side[v] = 2; sep.push_back(v); }
+		}
+		return sep;
+	}
+
+	std::vector<int> dissect(std::vector<int> S)
+	{
+		if ((int)S.size() <= leaf) {
+			nodes.push_back(TNode{S, {}});
+			return {(int)nodes.size()-1};
+		}
+		int st = cur++;
+		for (int v : S) stamp[v] = st;
+		std::vector<int> sep = pos ? split_geometric(S, st) : split_bfs(S, st);
+		std::vector<char> insep;
+		for (int v : sep) side[v] = 2;
+		std::vector<int> L, R;
+		for (int v : S) {
+			if (side[v] == 0) L.push_back(v);
+			else if (side[v] == 1) R.push_back(v);
+		}
+		std::vector<int> roots;
+		if (L.size() == S.size() || R.size() == S.size()) {
+			// no progress (should not happen); make a leaf
+			nodes.push_back(TNode{S, {}});
+			return {(int)nodes.size()-1};
+		}
+		std::vector<int> kl = L.empty() ? std::vector<int>{} : dissect(L);
+		std::vector<int> kr = R.empty() ? std::vector<int>{} : dissect(R);
+		if (sep.empty()) {
+			roots = kl;
+			roots.insert(roots.end(), kr.begin(), kr.end());
+			return roots;
+		}
+		TNode nd;
+		nd.cols = sep;
+		nd.kids = kl;
+		nd.kids.insert(nd.kids.end(), kr.begin(), kr.end());
+		nodes.push_back(nd);
+		return {(int)nodes.size()-1};
+	}
+};
+
+} // namespace
+
+void symbolic_analyze(Symbolic &S, int n, int nb, const int32_t *od_row, const int32_t *od_col,
+                      const double *pos, double lx, double ly, double lz, int leaf_size)
+{
+	(void)lx; (void)lz;
+	S = Symbolic();
+	S.nblk = n;
+	Graph g = build_graph(n, nb, od_row, od_col);
+	Dissector D(g, pos, ly == 0, std::max(1, leaf_size), n);
+	std::vector<int> all(n);
+	std::iota(all.begin(), all.end(), 0);
+	std::vector<int> roots = D.dissect(all);
+
+	// postorder numbering of tree nodes -> supernodes
+	std::vector<int> post;                 // tree node ids in postorder
+	std::vector<int> sn_of_node(D.nodes.size(), -1);
+	{
+		std::vector<std::pair<int,int>> stk;
+		for (auto it = roots.rbegin(); it != roots.rend(); ++it) stk.push_back({*it, 0});
+		while (!stk.empty()) {
+			auto &top = stk.back();
+			TNode &t = D.nodes[top.first];
+			if (top.second < (int)t.kids.size()) {
+				int kid = t.kids[top.second++];
+				stk.push_back({kid, 0});
+			} else {
+				sn_of_node[top.first] = (int)post.size();
+				post.push_back(top.first);
+				stk.pop_back();
+			}
+		}
+	}
+	int nsn = (int)post.size();
+	S.nsn = nsn;
+	S.perm.resize(n);
+	S.iperm.resize(n);
+	S.sn_first.resize(nsn); S.sn_n.resize(nsn); S.sn_m.resize(nsn);
+	S.sn_parent.assign(nsn, -1); S.sn_level.assign(nsn, 0);
+	int k = 0;
+	for (int s = 0; s < nsn; s++) {
+		TNode &t = D.nodes[post[s]];
+		S.sn_first[s] = k;
+		S.sn_n[s] = (int)t.cols.size();
+		for (int v : t.cols) { S.perm[k] = v; S.iperm[v] = k; k++; }
+		for (int kid : t.kids) S.sn_parent[sn_of_node[kid]] = s;
+	}
+	std::vector<int> colsn(n);
+	for (int s = 0; s < nsn; s++)
+		for (int q = S.sn_first[s]; q < S.sn_first[s]+S.sn_n[s]; q++) colsn[q] = s;
+	// children CSR (in postorder, i.e. increasing supernode id)
+	S.child_off.assign(nsn+1, 0);
+	for (int s = 0; s < nsn; s++) if (S.sn_parent[s] >= 0) S.child_off[S.sn_parent[s]+1]++;
+	for (int s = 0; s < nsn; s++) S.child_off[s+1] += S.child_off[s];
+	S.children.resize(S.child_off[nsn]);
+	{
+		std::vector<int> fill(S.child_off.begin(), S.child_off.end()-1);
+		for (int s = 0; s < nsn; s++) if (S.sn_parent[s] >= 0) S.children[fill[S.sn_parent[s]]++] = s;
+	}
+	// row structures (bottom-up)
+	std::vector<std::vector<int>> R(nsn);
+	for (int s = 0; s < nsn; s++) {
+		int last = S.sn_first[s]+S.sn_n[s]-1;
+		std::vector<int> tmp;
+		for (int q = S.sn_first[s]; q <= last; q++) {
+			int v = S.perm[q];
+			for (int e = g.ptr[v]; e < g.ptr[v+1]; e++) {
+				int u = g.adj[e];
+				if (u < 0) continue;
+				int qu = S.iperm[u];
+				if (qu > last) tmp.push_back(qu);
+			}
+		}
+		for (int c = S.child_off[s]; c < S.child_off[s+1]; c++)
+			for (int r : R[S.children[c]]) if (r > last) tmp.push_back(r);
+		std::sort(tmp.begin(), tmp.end());
+		tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+		R[s] = std::move(tmp);
+		S.sn_m[s] = (int)R[s].size();
+		int lev = 0;
+		for (int c = S.child_off[s]; c < S.child_off[s+1]; c++)
+			lev = std::max(lev, S.sn_level[S.children[c]]+1);
+		S.sn_level[s] = lev;
+	}
+	S.sn_rows_off.resize(nsn+1);
+	S.sn_rows_off[0] = 0;
+	for (int s = 0; s < nsn; s++) S.sn_rows_off[s+1] = S.sn_rows_off[s]+S.sn_m[s];
+	S.rows.resize(S.sn_rows_off[nsn]);
+	for (int s = 0; s < nsn; s++)
+		std::copy(R[s].begin(), R[s].end(), S.rows.begin()+S.sn_rows_off[s]);
+	// front sizes, arena offsets, flops
+	S.sn_off.resize(nsn); S.sn_ld.resize(nsn); S.sn_woff.resize(nsn);
+	int64_t off = 0, woff = 0;
+	S.max_F = 0; S.nnz_L = 0; S.flops = 0;
+	for (int s = 0; s < nsn; s++) {
+		int n6 = 6*S.sn_n[s], m6 = 6*S.sn_m[s], F6 = n6+m6;
+		S.sn_ld[s] = F6+n6;
+		S.sn_off[s] = off;
+		off += (int64_t)S.sn_ld[s]*F6;
+		off = (off+31)/32*32;
+		S.sn_woff[s] = woff;
+		woff += m6;
+		S.max_F = std::max(S.max_F, F6);
+		S.nnz_L += (int64_t)n6*(n6+1)/2 + (int64_t)n6*m6;
+		double dn = n6, dm = m6;
+		S.flops += dn*dn*dn/3 + dn*dn*dm + dn*dm*dm;
+	}
+	S.arena_elems = off;
+	S.w_elems = std::max<int64_t>(woff, 1);
+	// inverse maps child -> parent front
+	S.cinv_off.assign(nsn+1, 0);
+	for (int c = 0; c < nsn; c++) {
+		int p = S.sn_parent[c];
+		S.cinv_off[c+1] = S.cinv_off[c] + (p >= 0 ? S.sn_n[p]+S.sn_m[p] : 0);
+	}
+	S.cinv.assign(S.cinv_off[nsn], -1);
+	auto front_index = [&](int s, int q) -> int {
+		int f = S.sn_first[s];
+		if (q >= f && q < f+S.sn_n[s]) return q-f;
+		const int *b = &S.rows[S.sn_rows_off[s]], *e = b+S.sn_m[s];
+		const int *it = std::lower_bound(b, e, q);
+		if (it == e || *it != q) return -1;
+		return S.sn_n[s]+(int)(it-b);
+	};
+	for (int c = 0; c < nsn; c++) {
+		int p = S.sn_parent[c];
+		if (p < 0) continue;
+		for (int t = 0; t < S.sn_m[c]; t++) {
+			int fi = front_index(p, S.rows[S.sn_rows_off[c]+t]);
+			if (fi < 0) throw Error{LFG_ERR_BAD_ARG, 0, "symbolic: child row outside parent front"};
+			S.cinv[S.cinv_off[c]+fi] = S.sn_n[c]+t;
+		}
+	}
+	// levels
+	S.nlevels = 0;
+	for (int s = 0; s < nsn; s++) S.nlevels = std::max(S.nlevels, S.sn_level[s]+1);
+	S.level_off.assign(S.nlevels+1, 0);
+	for (int s = 0; s < nsn; s++) S.level_off[S.sn_level[s]+1]++;
+	for (int l = 0; l < S.nlevels; l++) S.level_off[l+1] += S.level_off[l];
+	S.level_sn.resize(nsn);
+	{
+		std::vector<int> fill(S.level_off.begin(), S.level_off.end()-1);
+		for (int s = 0; s < nsn; s++) S.level_sn[fill[S.sn_level[s]]++] = s;
+	}
+	// A-block scatter maps
+	S.d_sn.resize(n); S.d_bc.resize(n);
+	for (int i = 0; i < n; i++) {
+		int q = S.iperm[i], s = colsn[q];
+		S.d_sn[i] = s;
+		S.d_bc[i] = q-S.sn_first[s];
+	}
+	S.od_sn.resize(nb); S.od_br.resize(nb); S.od_bc.resize(nb); S.od_tr.resize(nb);
+	for (int e = 0; e < nb; e++) {
+		int qr = S.iperm[od_row[e]], qc = S.iperm[od_col[e]];
+		int lo = std::min(qr, qc), hi = std::max(qr, qc);
+		int s = colsn[lo];
+		S.od_sn[e] = s;
+		S.od_bc[e] = lo-S.sn_first[s];
+		int fi = front_index(s, hi);
+		if (fi < 0) throw Error{LFG_ERR_BAD_ARG, 0, "symbolic: matrix entry outside its front"};
+		S.od_br[e] = fi;
+		S.od_tr[e] = qr > qc ? 0 : 1;
+	}
+	S.level_d_off.assign(S.nlevels+1, 0);
+	S.level_od_off.assign(S.nlevels+1, 0);
+	for (int i = 0; i < n; i++) S.level_d_off[S.sn_level[S.d_sn[i]]+1]++;
+	for (int e = 0; e < nb; e++) S.level_od_off[S.sn_level[S.od_sn[e]]+1]++;
+	for (int l = 0; l < S.nlevels; l++) {
+		S.level_d_off[l+1] += S.level_d_off[l];
+		S.level_od_off[l+1] += S.level_od_off[l];
+	}
+	S.level_d.resize(n); S.level_od.resize(nb);
+	{
+		std::vector<int> f1(S.level_d_off.begin(), S.level_d_off.end()-1);
+		for (int i = 0; i < n; i++) S.level_d[f1[S.sn_level[S.d_sn[i]]]++] = i;
+		std::vector<int> f2(S.level_od_off.begin(), S.level_od_off.end()-1);
+		for (int e = 0; e < nb; e++) S.level_od[f2[S.sn_level[S.od_sn[e]]]++] = e;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// device mirror + launch plan
+// ---------------------------------------------------------------------------
+template <typename V> static void up(V *&d, const std::vector<V> &h, cudaStream_t st)
+{
+	size_t bytes = std::max<size_t>(h.size(), 1)*sizeof(V);
+	LFG_CUDA(cudaMalloc((void **)&d, bytes));
+	if (!h.empty()) LFG_CUDA(cudaMemcpyAsync(d, h.data(), h.size()*sizeof(V), cudaMemcpyHostToDevice, st));
+}
+
+void dev_symbolic_free(DevSymbolic &D)
+{
+	void *ptrs[] = {D.perm, D.iperm, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_rows_off, D.rows,
+	                D.sn_off, D.sn_woff, D.child_off, D.children, D.cinv_off, D.cinv, D.level_sn,
+	                D.d_sn, D.d_bc, D.od_sn, D.od_br, D.od_bc, D.od_tr, D.level_d, D.level_od,
+	                D.col_tasks, D.panel_tasks, D.tile_tasks};
+	for (void *p : ptrs) if (p) cudaFree(p);
+	D = DevSymbolic();
+}
+
+// Launch kinds of the factor plan (interpreted by factor_numeric).
+enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4 };
+
+void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb, int tile,
+                         cudaStream_t st)
+{
+	dev_symbolic_free(D);
+	D.nblk = S.nblk; D.nsn = S.nsn; D.nlevels = S.nlevels; D.nb = nb;
+	D.arena_elems = S.arena_elems; D.w_elems = S.w_elems; D.max_F = S.max_F;
+	D.flops = S.flops; D.nnz_L = S.nnz_L;
+	up(D.perm, S.perm, st); up(D.iperm, S.iperm, st);
+	up(D.sn_first, S.sn_first, st); up(D.sn_n, S.sn_n, st); up(D.sn_m, S.sn_m, st);
+	up(D.sn_ld, S.sn_ld, st); up(D.sn_rows_off, S.sn_rows_off, st); up(D.rows, S.rows, st);
+	up(D.sn_off, S.sn_off, st); up(D.sn_woff, S.sn_woff, st);
+	up(D.child_off, S.child_off, st); up(D.children, S.children, st);
+	up(D.cinv_off, S.cinv_off, st); up(D.cinv, S.cinv, st);
+	up(D.level_sn, S.level_sn, st);
+	up(D.d_sn, S.d_sn, st); up(D.d_bc, S.d_bc, st);
+	up(D.od_sn, S.od_sn, st); up(D.od_br, S.od_br, st); up(D.od_bc, S.od_bc, st); up(D.od_tr, S.od_tr, st);
+	up(D.level_d, S.level_d, st); up(D.level_od, S.level_od, st);
+	D.h_level_off = S.level_off;
+	D.h_level_d_off = S.level_d_off;
+	D.h_level_od_off = S.level_od_off;
+	D.max_n6 = 0;
+	for (int s = 0; s < S.nsn; s++) D.max_n6 = std::max(D.max_n6, 6*S.sn_n[s]);
+	// assembly column tasks, panel tasks and update tiles, level by level
+	std::vector<int> col_tasks;
+	std::vector<int4> panel_tasks, tile_tasks;
+	const int RC = 128;  // rows per panel task
+	D.factor_plan.clear();
+	for (int l = 0; l < S.nlevels; l++) {
+		int64_t c0 = (int64_t)col_tasks.size()/2;
+		int kmax = 0;
+		for (int t = S.level_off[l]; t < S.level_off[l+1]; t++) {
+			int s = S.level_sn[t];
+			int F6 = 6*(S.sn_n[s]+S.sn_m[s]);
+			for (int c = 0; c < F6; c++) { col_tasks.push_back(s); col_tasks.push_back(c); }
+			kmax = std::max(kmax, (6*S.sn_n[s]+panel_nb-1)/panel_nb);
+		}
+		D.factor_plan.push_back({PLAN_ASSEMBLE, l, 0, c0, (int)((int64_t)col_tasks.size()/2-c0)});
+		D.factor_plan.push_back({PLAN_SCATTER_D, l, 0, S.level_d_off[l], S.level_d_off[l+1]-S.level_d_off[l]});
+		D.factor_plan.push_back({PLAN_SCATTER_OD, l, 0, S.level_od_off[l], S.level_od_off[l+1]-S.level_od_off[l]});
+		for (int k = 0; k < kmax; k++) {
+			int64_t p0 = (int64_t)panel_tasks.size(), t0i = (int64_t)tile_tasks.size();
+			for (int t = S.level_off[l]; t < S.level_off[l+1]; t++) {
+				int s = S.level_sn[t];
+				int n6 = 6*S.sn_n[s], F6 = n6+6*S.sn_m[s];
+				if (n6 <= k*panel_nb) continue;
+				int w = std::min(panel_nb, n6-k*panel_nb);
+				int t0 = k*panel_nb+w;
+				// panel rows: real [t0, F6), extra [F6, F6+t0)
+				for (int r = t0; r < F6; r += RC) panel_tasks.push_back(make_int4(s, r, k, std::min(RC, F6-r)));
+				for (int r = F6; r < F6+t0; r += RC) panel_tasks.push_back(make_int4(s, r, k, std::min(RC, F6+t0-r)));
+				// diagonal-block writer + trailing tiles
+				tile_tasks.push_back(make_int4(s, k*panel_nb, -1, k));
+				for (int r = t0; r < F6; r += tile)
+					for (int c = t0; c <= r && c < F6; c += tile)
+						tile_tasks.push_back(make_int4(s, r, c, k));
+				for (int r = F6; r < F6+t0; r += tile)
+					for (int c = t0; c < n6; c += tile)
+						tile_tasks.push_back(make_int4(s, r, c, k));
+			}
+			D.factor_plan.push_back({PLAN_PANEL, l, k, p0, (int)((int64_t)panel_tasks.size()-p0)});
+			D.factor_plan.push_back({PLAN_UPDATE, l, k, t0i, (int)((int64_t)tile_tasks.size()-t0i)});
+		}
+	}
+	up(D.col_tasks, col_tasks, st);
+	up(D.panel_tasks, panel_tasks, st);
+	up(D.tile_tasks, tile_tasks, st);
+}
+
+} // namespace lfg
