@@ -241,3 +241,145 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+
+def make_params(d: dict) -> Params:
+    """lfg_params from a dict of already non-dimensionalised values."""
+    p = Params()
+    defaults = dict(mu_dynamic=-1.0, repulsive_max_length=-1.0, interaction_range=-1.0, sd_coeff=1.0,
+                    contact_relaxation_time=1e-3, contact_relaxation_time_tan=-1.0, disp_max=1e-3,
+                    dt=1e-4, dt_max=-1.0, dt_min=-1.0, integration_method=1, lubrication_model=2,
+                    lub_reduce_parameter=1e-3, lub_max_gap=0.5, friction_model=1, mu_static=1.0,
+                    repulsive_length=0.05, init_strain_shear_rate_limit=0.0, init_shear_rate_limit=999.0,
+                    Ehat=(0, 0, 0.5, 0, 0, 0), Ohat=(0, 0.5, 0))
+    full = dict(defaults)
+    full.update(d)
+    for k, _ in Params._fields_:
+        if k not in full:
+            continue
+        v = full[k]
+        if k in ("Ehat", "Ohat"):
+            arr = getattr(p, k)
+            for i, x in enumerate(v):
+                arr[i] = float(x)
+        elif isinstance(getattr(p, k), int):
+            setattr(p, k, int(v))
+        else:
+            setattr(p, k, float(v))
+    return p
+
+
+class Sim:
+    """One suspension advanced on the device (lfg_sim_*): System::timeEvolution."""
+
+    def __init__(self, params: dict, position, radius, lx, ly, lz, le_disp=(0.0, 0.0), contacts=None,
+                 precision: int = PREC_FP64, **opts):
+        L = load()
+        self.n = len(radius)
+        self.p = make_params(params)
+        self.opt = default_options(precision=precision, **opts)
+        pos = np.ascontiguousarray(position, dtype=np.float64).reshape(-1)
+        rad = np.ascontiguousarray(radius, dtype=np.float64)
+        led = np.ascontiguousarray(le_disp, dtype=np.float64)
+        h = C.c_void_p()
+        st = Status()
+        if contacts:
+            c0 = np.ascontiguousarray([c[0] for c in contacts], dtype=np.int32)
+            c1 = np.ascontiguousarray([c[1] for c in contacts], dtype=np.int32)
+            cd = np.ascontiguousarray([c[2] for c in contacts], dtype=np.float64).reshape(-1)
+            rc = L.lfg_sim_create(C.byref(self.p), C.byref(self.opt), self.n, _ptr(pos), _ptr(rad), lx, ly, lz,
+                                  _ptr(led), len(contacts), _ptr(c0), _ptr(c1), _ptr(cd), C.byref(h), C.byref(st))
+        else:
+            rc = L.lfg_sim_create(C.byref(self.p), C.byref(self.opt), self.n, _ptr(pos), _ptr(rad), lx, ly, lz,
+                                  _ptr(led), 0, None, None, None, C.byref(h), C.byref(st))
+        _check(rc, st)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().lfg_sim_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, calc_stress=False, time_end=-1.0, strain_end=1e9):
+        st = Status()
+        _check(load().lfg_sim_step(self.h, int(calc_stress), time_end, strain_end, C.byref(st)), st)
+
+    def run(self, nsteps, time_end=-1.0, strain_end=1e9):
+        st = Status()
+        _check(load().lfg_sim_run(self.h, int(nsteps), time_end, strain_end, C.byref(st)), st)
+
+    def advance(self, time_end=-1.0, strain_end=-1.0):
+        st = Status()
+        _check(load().lfg_sim_advance(self.h, time_end, strain_end, C.byref(st)), st)
+
+    def scalars(self) -> dict:
+        s = SimScalars()
+        load().lfg_sim_get_scalars(self.h, C.byref(s))
+        out = {}
+        for k, _ in SimScalars._fields_:
+            v = getattr(s, k)
+            out[k] = np.array(v[:]) if hasattr(v, "__len__") else v
+        return out
+
+    def particles(self) -> dict:
+        arrs = {k: np.zeros(3 * self.n) for k in ("pos", "vel", "ang", "na_vel", "na_ang")}
+        load().lfg_sim_get_particles(self.h, *[_ptr(a) for a in arrs.values()])
+        return {k: v.reshape(-1, 3) for k, v in arrs.items()}
+
+    def pairs(self) -> np.ndarray:
+        L = load()
+        n = L.lfg_sim_get_num_pairs(self.h)
+        buf = (Pair * max(n, 1))()
+        L.lfg_sim_get_pairs(self.h, buf, n)
+        return np.ctypeslib.as_array(buf)[:n].copy()
+
+    def particle_stress(self, comp: int):
+        out = np.zeros(6 * self.n)
+        rc = load().lfg_sim_get_particle_stress(self.h, comp, _ptr(out))
+        return None if rc else out.reshape(-1, 6)
+
+    def velocity_component(self, comp: int):
+        out = np.zeros(6 * self.n)
+        rc = load().lfg_sim_get_velocity_component(self.h, comp, _ptr(out))
+        return None if rc else out.reshape(-1, 6)
+
+    def set_contact(self, p0, p1, state, disp_tan):
+        d = np.ascontiguousarray(disp_tan, dtype=np.float64)
+        rc = load().lfg_sim_set_contact(self.h, int(p0), int(p1), int(state), _ptr(d))
+        if rc:
+            raise LFGError(rc, f"no pair ({p0},{p1})")
+
+    def set_clock(self, time, strain, dt, shear_rate, max_velocity, max_sliding_velocity):
+        load().lfg_sim_set_clock(self.h, time, strain, dt, shear_rate, max_velocity, max_sliding_velocity)
+
+    def refresh(self):
+        load().lfg_sim_refresh(self.h)
+
+    def assemble(self):
+        L = load()
+        nb = C.c_int()
+        L.lfg_sim_assemble(self.h, None, None, None, None, 0, C.byref(nb))
+        k = nb.value
+        d = np.zeros(15 * self.n)
+        r = np.zeros(max(k, 1), dtype=np.int32)
+        c = np.zeros(max(k, 1), dtype=np.int32)
+        o = np.zeros(18 * max(k, 1))
+        L.lfg_sim_assemble(self.h, _ptr(d), _ptr(r), _ptr(c), _ptr(o), k, C.byref(nb))
+        return d.reshape(-1, 15), r[:k], c[:k], o[:18 * k].reshape(-1, 18)
+
+    def force_component(self, comp: int):
+        out = np.zeros(6 * self.n)
+        rc = load().lfg_sim_force_component(self.h, comp, _ptr(out))
+        return None if rc else out.reshape(-1, 6)
+
+    def timing(self) -> dict:
+        t = SimTiming()
+        load().lfg_sim_get_timing(self.h, C.byref(t))
+        return {"ms": list(t.ms), "launches": t.launches, "factor_flops": t.factor_flops,
+                "solve_bytes": t.solve_bytes}

@@ -1,0 +1,1455 @@
+// lfg_physics.cu -- per-step physics of LF_DEM's hydrodynamic core on the
+// device: Lees-Edwards cell lists and pair discovery, Interaction updates
+// (contact springs, friction laws, lubrication coefficients, repulsion),
+// R_FU block assembly, RHS force components, stresslets, stress-controlled
+// shear rate, velocity assembly and the predictor-corrector moves.
+//
+// Compiled with --fmad=false: geometry and contact tests round exactly like
+// LF_DEM's scalar C++ (System.cpp:2517-2548, Interaction.cpp:124-135), so the
+// pair list and the contact states are bit-identical on identical inputs.
+// Every per-particle sum is a gather over the pair list in a fixed order (no
+// floating-point atomics), so the engine is bitwise reproducible.
+#include <cstdio>
+
+#include "lfg_physics.h"
+
+namespace lfg {
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+// ---------------------------------------------------------------------------
+// small vector / tensor helpers (vec3d.h, Sym2Tensor.h)
+// ---------------------------------------------------------------------------
+struct v3 { double x, y, z; };
+__device__ __forceinline__ v3 V(double x, double y, double z) { v3 r; r.x = x; r.y = y; r.z = z; return r; }
+__device__ __forceinline__ v3 vadd(v3 a, v3 b) { return V(a.x+b.x, a.y+b.y, a.z+b.z); }
+__device__ __forceinline__ v3 vsub(v3 a, v3 b) { return V(a.x-b.x, a.y-b.y, a.z-b.z); }
+__device__ __forceinline__ v3 vscale(double s, v3 a) { return V(s*a.x, s*a.y, s*a.z); }
+__device__ __forceinline__ v3 vneg(v3 a) { return V(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ double vdot(v3 a, v3 b) { return a.x*b.x+a.y*b.y+a.z*b.z; }
+__device__ __forceinline__ double vsq(v3 a) { return a.x*a.x+a.y*a.y+a.z*a.z; }
+__device__ __forceinline__ v3 vcross(v3 a, v3 b) { return V(a.y*b.z-a.z*b.y, a.z*b.x-a.x*b.z, a.x*b.y-a.y*b.x); }
+__device__ __forceinline__ v3 vzero() { return V(0, 0, 0); }
+__device__ __forceinline__ v3 ld3(const double *p) { return V(p[0], p[1], p[2]); }
+__device__ __forceinline__ void st3(double *p, v3 v) { p[0] = v.x; p[1] = v.y; p[2] = v.z; }
+// Sym2Tensor.h:227-234
+__device__ __forceinline__ v3 sdot(const double *s, v3 v)
+{
+	return V(s[0]*v.x + s[1]*v.y + s[2]*v.z, s[1]*v.x + s[4]*v.y + s[3]*v.z, s[2]*v.x + s[3]*v.y + s[5]*v.z);
+}
+struct s2 { double e[6]; };
+__device__ __forceinline__ s2 szero() { s2 r; for (int i = 0; i < 6; i++) r.e[i] = 0; return r; }
+__device__ __forceinline__ void sadd_to(s2 &a, const s2 &b) { for (int i = 0; i < 6; i++) a.e[i] += b.e[i]; }
+__device__ __forceinline__ s2 sscale(double c, const s2 &a) { s2 r; for (int i = 0; i < 6; i++) r.e[i] = c*a.e[i]; return r; }
+__device__ __forceinline__ s2 ssub(const s2 &a, const s2 &b) { s2 r; for (int i = 0; i < 6; i++) r.e[i] = a.e[i]-b.e[i]; return r; }
+__device__ __forceinline__ s2 saddv(const s2 &a, const s2 &b) { s2 r; for (int i = 0; i < 6; i++) r.e[i] = a.e[i]+b.e[i]; return r; }
+__device__ __forceinline__ s2 outer_sym(v3 a, v3 b)
+{
+	s2 r;
+	r.e[0] = a.x*b.x; r.e[1] = 0.5*(a.x*b.y+a.y*b.x); r.e[2] = 0.5*(a.x*b.z+a.z*b.x);
+	r.e[3] = 0.5*(a.y*b.z+a.z*b.y); r.e[4] = a.y*b.y; r.e[5] = a.z*b.z;
+	return r;
+}
+__device__ __forceinline__ s2 outer(v3 a)
+{
+	s2 r;
+	r.e[0] = a.x*a.x; r.e[1] = a.x*a.y; r.e[2] = a.x*a.z; r.e[3] = a.y*a.z; r.e[4] = a.y*a.y; r.e[5] = a.z*a.z;
+	return r;
+}
+__device__ __forceinline__ double doubledot(const double *a, const double *b)
+{
+	return a[0]*b[0] + 2*a[1]*b[1] + 2*a[2]*b[2] + 2*a[3]*b[3] + a[4]*b[4] + a[5]*b[5];
+}
+__device__ __forceinline__ double dmax_atomic_value(unsigned long long bits) { return __longlong_as_double((long long)bits); }
+
+static inline unsigned blocks_for(int64_t n, int t) { return (unsigned)((n+t-1)/t); }
+
+// ---------------------------------------------------------------------------
+// periodic boundaries, System.cpp:2478-2548
+// ---------------------------------------------------------------------------
+__device__ int periodize(const DevParams &P, const double *sd, v3 &p)
+{
+	int z_shift = 0;
+	if (p.z >= P.lz) {
+		p.z -= P.lz;
+		p = vsub(p, V(sd[0], sd[1], sd[2]));
+		z_shift = -1;
+	} else if (p.z < 0) {
+		p.z += P.lz;
+		p = vadd(p, V(sd[0], sd[1], sd[2]));
+		z_shift = 1;
+	}
+	while (p.x >= P.lx) p.x -= P.lx;
+	while (p.x < 0) p.x += P.lx;
+	if (!P.twodim) {
+		if (p.y >= P.ly) p.y -= P.ly;
+		else if (p.y < 0) p.y += P.ly;
+	}
+	return z_shift;
+}
+
+__device__ int periodize_diff(const DevParams &P, const double *sd, v3 &d)
+{
+	int zshift = 0;
+	if (d.z > P.lz_half) {
+		d.z -= P.lz;
+		d = vsub(d, V(sd[0], sd[1], sd[2]));
+		zshift = -1;
+	} else if (d.z < -P.lz_half) {
+		d.z += P.lz;
+		d = vadd(d, V(sd[0], sd[1], sd[2]));
+		zshift = 1;
+	}
+	while (d.x > P.lx_half) d.x -= P.lx;
+	while (d.x < -P.lx_half) d.x += P.lx;
+	if (!P.twodim) {
+		if (d.y > P.ly_half) d.y -= P.ly;
+		else if (d.y < -P.ly_half) d.y += P.ly;
+	}
+	return zshift;
+}
+
+// System::calcLubricationRange (System.cpp:2665-2674) and the interaction
+// range (System.cpp:2660-2663, 405-410)
+__device__ __forceinline__ double lub_range(const DevParams &P, double ri, double rj)
+{
+	double rad_ratio = ri/rj;
+	if (rad_ratio < 2 && rad_ratio > 0.5) return (2+P.lub_max_gap)*0.5*(ri+rj);
+	double minradius = ri < rj ? ri : rj;
+	return ri+rj+P.lub_max_gap*minradius;
+}
+__device__ __forceinline__ double inter_range(const DevParams &P, double ri, double rj)
+{
+	if (P.interaction_range < 0) return lub_range(P, ri, rj);
+	return P.interaction_range*0.5*(ri+rj);
+}
+
+// ---------------------------------------------------------------------------
+// pair constants (LubricationFunctions.h:12-90, Lubrication.cpp:165-294,
+// ContactDashpot.cpp:107-183)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double g1_XA(double l) { double p = l+1; return 2*l*l/(p*p*p); }
+__device__ __forceinline__ double g2_YA(double l) { double p = l+1; return (4./15)*l*(2+l+2*l*l)/(p*p*p); }
+__device__ __forceinline__ double g2_YB(double l) { double p = l+1; return -(1./5)*l*(4+l)/(p*p); }
+__device__ __forceinline__ double g2_YC(double l) { return (2./5)*l/(l+1); }
+__device__ __forceinline__ double g4_YC(double l) { double p = l+1; return (4./5)*l*l/(p*p*p*p); }
+__device__ __forceinline__ double g1_XG(double l) { double p = l+1; return 3*l*l/(p*p*p); }
+__device__ __forceinline__ double g2_YG(double l) { double p = l+1; return (1./10)*l*(4-l+7*l*l)/(p*p*p); }
+__device__ __forceinline__ double g2_YH(double l) { double p = l+1; return (1./10)*l*(2-l)/(p*p); }
+__device__ __forceinline__ double g5_YH(double l) { double p = l+1; return (1./20)*l*l*(1+7*l)/(p*p); }
+__device__ __forceinline__ double g1_XM(double l) { double p = l+1; return (6./5)*l*l/(p*p*p); }
+__device__ __forceinline__ double g4_XM(double l) { double p = l+1; return (6./5)*l*l*l/(p*p*p); }
+__device__ __forceinline__ double g2_YM(double l) { double p = l+1; return (6./25)*l*(1-l+4*l*l)/(p*p*p); }
+__device__ __forceinline__ double g5_YM(double l) { double p = l+1; return (3./50)*l*l*(7-10*l+7*l*l)/(p*p*p); }
+
+enum { CXA = 0, CYA = 4, CYB = 8, CYC = 12, CXG = 16, CYG = 20, CYH = 24, CXM = 28, CYM = 32 };
+enum { DXA = 0, DYA = 4, DYB = 8, DYC = 12 };
+
+__global__ void k_pair_constants(DevParams P, int np, const DPair *__restrict__ pairs,
+                                 const double *__restrict__ radius, DPairConst *__restrict__ pc)
+{
+	int t = blockIdx.x*blockDim.x+threadIdx.x;
+	if (t >= np) return;
+	int i = pairs[t].p0, j = pairs[t].p1;
+	DPairConst c;
+	double a0 = radius[i], a1 = radius[j];
+	c.a0 = a0; c.a1 = a1;
+	double ro = a0+a1;
+	c.ro = ro;
+	c.range = inter_range(P, a0, a1);
+	c.lub_range = lub_range(P, a0, a1);
+	double ro_12 = (a0+a1)/2;
+	c.kn_s = ro_12*ro_12*P.kn;
+	c.kt_s = P.friction ? ro_12*P.kt : 0;
+	c.rep_geo = a0*a1/(a0+a1);
+	// Lubrication::calcLubConstants
+	double r12 = ro/2;
+	double lambda = a1/a0, invlambda = 1/lambda;
+	double lambda_square = lambda*lambda, lambda_cubic = lambda*lambda*lambda;
+	double lambda_p_1 = 1+lambda, lambda_p_1_square = lambda_p_1*lambda_p_1;
+	double lambda_p_1_cubic = lambda_p_1_square*lambda_p_1;
+	double a0a0_23 = a0*a0*(2.0/3), a1a1_23 = a1*a1*(2.0/3), roro_16 = ro*ro*(1.0/6);
+	double a0a0a0 = a0*a0*a0, a1a1a1 = a1*a1*a1, rororo = ro*ro*ro;
+	double a0a0a0_43 = a0a0a0*(4.0/3), a1a1a1_43 = a1a1a1*(4.0/3), rororo_16 = rororo*(1.0/6);
+	double a0a0a0_109 = a0a0a0*(10.0/9), a1a1a1_109 = a1a1a1*(10.0/9), rororo_536 = rororo*(5.0/36);
+	double *L = c.lc;
+	double g = g1_XA(lambda);
+	L[CXA+0] = a0*g; L[CXA+1] = r12*(-2/lambda_p_1)*g; L[CXA+2] = L[CXA+1]; L[CXA+3] = a1*g1_XA(invlambda);
+	g = g2_YA(lambda);
+	L[CYA+0] = a0*g; L[CYA+1] = r12*(-2/lambda_p_1)*g; L[CYA+2] = L[CYA+1]; L[CYA+3] = a1*g2_YA(invlambda);
+	g = g2_YB(lambda);
+	L[CYB+0] = a0a0_23*g; L[CYB+1] = roro_16*(-4/lambda_p_1_square)*g;
+	L[CYB+2] = roro_16*(4*lambda_square/lambda_p_1_square)*g2_YB(invlambda); L[CYB+3] = -a1a1_23*g2_YB(invlambda);
+	L[CYC+0] = a0a0a0_43*g2_YC(lambda); L[CYC+1] = rororo_16*g4_YC(lambda); L[CYC+2] = L[CYC+1];
+	L[CYC+3] = a1a1a1_43*g2_YC(invlambda);
+	g = g1_XG(lambda);
+	L[CXG+0] = a0a0_23*g; L[CXG+1] = roro_16*(-4/lambda_p_1_square)*g;
+	L[CXG+2] = roro_16*(4*lambda_square/lambda_p_1_square)*g1_XG(invlambda); L[CXG+3] = -a1a1_23*g1_XG(invlambda);
+	g = g2_YG(lambda);
+	L[CYG+0] = a0a0_23*g; L[CYG+1] = roro_16*(-4/lambda_p_1_square)*g;
+	L[CYG+2] = roro_16*(4*lambda_square/lambda_p_1_square)*g2_YG(invlambda); L[CYG+3] = -a1a1_23*g2_YG(invlambda);
+	L[CYH+0] = a0a0a0_43*g2_YH(lambda); L[CYH+1] = rororo_16*(8/lambda_p_1_cubic)*g5_YH(lambda);
+	L[CYH+2] = rororo_16*(8*lambda_cubic/lambda_p_1_cubic)*g5_YH(invlambda); L[CYH+3] = a1a1a1_43*g2_YH(invlambda);
+	L[CXM+0] = a0a0a0_109*g1_XM(lambda); L[CXM+1] = rororo_536*(8/lambda_p_1_cubic)*g4_XM(lambda);
+	L[CXM+2] = L[CXM+1]; L[CXM+3] = a1a1a1_109*g1_XM(invlambda);
+	L[CYM+0] = a0a0a0_109*g2_YM(lambda); L[CYM+1] = rororo_536*(8/lambda_p_1_cubic)*g5_YM(lambda);
+	L[CYM+2] = L[CYM+1]; L[CYM+3] = a1a1a1_109*g2_YM(invlambda);
+	// ContactDashpot::calcDashpotResistances
+	double *D = c.dc;
+	double nc = P.dp_normal_coeff, tc = P.dp_tan_coeff;
+	D[DXA+0] = a0*g1_XA(lambda);
+	D[DXA+1] = ro_12*(-2/lambda_p_1)*g1_XA(lambda);
+	D[DXA+2] = ro_12*D[DXA+1];
+	D[DXA+3] = a1*g1_XA(invlambda);
+	for (int k = 0; k < 4; k++) D[DXA+k] *= nc;
+	for (int k = 0; k < 12; k++) D[DYA+k] = 0;
+	if (tc != 0) {
+		D[DYA+0] = a0*g2_YA(lambda);
+		D[DYA+1] = ro_12*(-2/lambda_p_1)*g2_YA(lambda);
+		D[DYA+2] = ro_12*D[DYA+1];
+		D[DYA+3] = a1*g2_YA(invlambda);
+		for (int k = 0; k < 4; k++) D[DYA+k] *= tc;
+		D[DYB+0] = a0a0_23*g2_YB(lambda);
+		D[DYB+1] = roro_16*(-4/lambda_p_1_square)*g2_YB(lambda);
+		D[DYB+2] = roro_16*(4*lambda_square/lambda_p_1_square)*g2_YB(invlambda);
+		D[DYB+3] = -a1a1_23*g2_YB(invlambda);
+		for (int k = 0; k < 4; k++) D[DYB+k] *= tc;
+		D[DYC+0] = a0a0a0_43*g2_YC(lambda);
+		D[DYC+1] = rororo_16*g4_YC(lambda);
+		D[DYC+2] = rororo_16*D[DYC+1];
+		D[DYC+3] = a1a1a1_43*g2_YC(invlambda);
+		for (int k = 0; k < 4; k++) D[DYC+k] *= tc;
+	}
+	pc[t] = c;
+}
+
+// ---------------------------------------------------------------------------
+// cell lists with Lees-Edwards shifted neighbour rows (BoxSet.cpp)
+// ---------------------------------------------------------------------------
+struct CellView {
+	int ncx, ncy, ncz, brute, n;
+	double csx, csy, csz;
+	const int *start, *count, *list;
+};
+
+__device__ __forceinline__ int wrapc(int c, int nc) { c %= nc; return c < 0 ? c+nc : c; }
+__device__ __forceinline__ int cell_coord(double x, double L, double cs, int nc)
+{
+	double w = x-floor(x/L)*L;
+	int c = (int)(w/cs);
+	return c < 0 ? 0 : (c >= nc ? nc-1 : c);
+}
+
+template <typename F>
+__device__ void for_neighbours(const CellView &C, const DevParams &P, const double *sd, int i, v3 pi, F f)
+{
+	if (C.brute) {
+		for (int j = i+1; j < C.n; j++) f(j);
+		return;
+	}
+	int cz = cell_coord(pi.z, P.lz, C.csz, C.ncz);
+	for (int dz = -1; dz <= 1; dz++) {
+		int zc = cz+dz;
+		double sx = 0, sy = 0;
+		if (zc < 0) { zc += C.ncz; sx = sd[0]; sy = sd[1]; }
+		else if (zc >= C.ncz) { zc -= C.ncz; sx = -sd[0]; sy = -sd[1]; }
+		int xc = cell_coord(pi.x+sx, P.lx, C.csx, C.ncx);
+		int yc = P.twodim ? 0 : cell_coord(pi.y+sy, P.ly, C.csy, C.ncy);
+		int ylo = P.twodim ? 0 : -1, yhi = P.twodim ? 0 : 1;
+		for (int dy = ylo; dy <= yhi; dy++) {
+			int yy = P.twodim ? 0 : wrapc(yc+dy, C.ncy);
+			for (int dx = -1; dx <= 1; dx++) {
+				int xx = wrapc(xc+dx, C.ncx);
+				int cell = (zc*C.ncy+yy)*C.ncx+xx;
+				int s = C.start[cell], e = s+C.count[cell];
+				for (int k = s; k < e; k++) {
+					int j = C.list[k];
+					if (j > i) f(j);
+				}
+			}
+		}
+	}
+}
+
+__global__ void k_cell_assign(DevParams P, CellView C, const double *__restrict__ pos, int *__restrict__ cell_of,
+                              int *__restrict__ count)
+{
+	int i = blockIdx.x*blockDim.x+threadIdx.x;
+	if (i >= C.n) return;
+	int cx = cell_coord(pos[3*i], P.lx, C.csx, C.ncx);
+	int cy = P.twodim ? 0 : cell_coord(pos[3*i+1], P.ly, C.csy, C.ncy);
+	int cz = cell_coord(pos[3*i+2], P.lz, C.csz, C.ncz);
+	int c = (cz*C.ncy+cy)*C.ncx+cx;
+	cell_of[i] = c;
+	atomicAdd(&count[c], 1);
+}
+
+// exclusive scan of n ints by one CTA (n up to a few 10^5)
+__global__ void k_scan(int n, const int *__restrict__ in, int *__restrict__ out, int *total)
+{
+	__shared__ int part[1024];
+	int t = threadIdx.x, T = blockDim.x;
+	int chunk = (n+T-1)/T;
+	int lo = t*chunk, hi = min(n, lo+chunk);
+	int s = 0;
+	for (int k = lo; k < hi; k++) s += in[k];
+	part[t] = s;
+	__syncthreads();
+	if (t == 0) {
+		int acc = 0;
+		for (int k = 0; k < T; k++) { int v = part[k]; part[k] = acc; acc += v; }
+		if (total) *total = acc;
+		out[n] = acc;
+	}
+	__syncthreads();
+	int acc = part[t];
+	for (int k = lo; k < hi; k++) { out[k] = acc; acc += in[k]; }
+}
+
+__global__ void k_cell_fill(int n, const int *__restrict__ cell_of, const int *__restrict__ start,
+                            int *__restrict__ fill, int *__restrict__ list)
+{
+	int i = blockIdx.x*blockDim.x+threadIdx.x;
+	if (i >= n) return;
+	int c = cell_of[i];
+	int k = atomicAdd(&fill[c], 1);
+	list[start[c]+k] = i;
+}
+
+// sort each cell's particle list (deterministic neighbour order)
+__global__ void k_cell_sort(int ncell, const int *__restrict__ start, const int *__restrict__ count,
+                            int *__restrict__ list)
+{
+	int c = blockIdx.x*blockDim.x+threadIdx.x;
+	if (c >= ncell) return;
+	int s = start[c], e = s+count[c];
+	for (int a = s+1; a < e; a++) {
+		int x = list[a], b = a-1;
+		while (b >= s && list[b] > x) { list[b+1] = list[b]; b--; }
+		list[b+1] = x;
+	}
+}
+
+// candidate pairs within the superset range (range + skin (a_i+a_j)/2)
+__global__ void k_candidates(DevParams P, CellView C, const DevClock *__restrict__ clk,
+                             const double *__restrict__ pos, const double *__restrict__ radius,
+                             int *__restrict__ count, const int *__restrict__ ptr, int *__restrict__ cand)
+{
+	int i = blockIdx.x*blockDim.x+threadIdx.x;
+	if (i >= C.n) return;
+	const double *sd = clk->shear_disp;
+	v3 pi = ld3(pos+3*i);
+	double ri = radius[i];
+	int c = 0;
+	int base = ptr ? ptr[i] : 0;
+	for_neighbours(C, P, sd, i, pi, [&](int j) {
+		v3 d = vsub(ld3(pos+3*j), pi);
+		periodize_diff(P, sd, d);
+		double rj = radius[j];
+		double rs = inter_range(P, ri, rj)+P.skin*0.5*(ri+rj);
+		if (vsq(d) < rs*rs) {
+			if (ptr) cand[base+c] = j;
+			c++;
+		}
+	});
+	if (!ptr) count[i] = c;
+	else {
+		// sort the row
+		for (int a = base+1; a < base+c; a++) {
+			int x = cand[a], b = a-1;
+			while (b >= base && cand[b] > x) { cand[b+1] = cand[b]; b--; }
+			cand[b+1] = x;
+		}
+	}
+}
+
+// every pair within the interaction range must be in the superset
+// (System::checkNewInteraction's test, System.cpp:1328-1373)
+__global__ void k_check_superset(DevParams P, CellView C, DevClock *__restrict__ clk,
+                                 const double *__restrict__ pos, const double *__restrict__ radius,
+                                 const int *__restrict__ row_ptr, const DPair *__restrict__ pairs)
+{
+	int i = blockIdx.x*blockDim.x+threadIdx.x;
+	if (i >= C.n) return;
+	const double *sd = clk->shear_disp;
+	v3 pi = ld3(pos+3*i);
+	double ri = radius[i];
+	int lo0 = row_ptr[i], hi0 = row_ptr[i+1];
+	bool missing = false;
+	for_neighbours(C, P, sd, i, pi, [&](int j) {
+		v3 d = vsub(ld3(pos+3*j), pi);
+		periodize_diff(P, sd, d);
+		double range = inter_range(P, ri, radius[j]);
+		if (vsq(d) < range*range) {
+			int lo = lo0, hi = hi0-1;
+			bool found = false;
+			while (lo <= hi) {
+				int m = (lo+hi) >> 1;
+				int pj = pairs[m].p1;
+				if (pj == j) { found = true; break; }
+				if (pj < j) lo = m+1; else hi = m-1;
+			}
+			if (!found) missing = true;
+		}
+	});
+	if (missing) atomicOr(&clk->stale, 1);
+}
+
+// ---------------------------------------------------------------------------
+// Interaction life cycle (Interaction.cpp, Contact.cpp, Lubrication.cpp,
+// RepulsiveForce.cpp)
+// ---------------------------------------------------------------------------
+__device__ void pair_geometry(const DevParams &P, const double *sd, const double *pos, DPair &q, const DPairConst &c)
+{
+	v3 rv = vsub(ld3(pos+3*q.p1), ld3(pos+3*q.p0));
+	q.zoff = periodize_diff(P, sd, rv);
+	double r = sqrt(vsq(rv));
+	q.r = r;
+	st3(q.rvec, rv);
+	q.nvec[0] = rv.x/r; q.nvec[1] = rv.y/r; q.nvec[2] = rv.z/r;
+	q.gap = 2*r/c.ro-2;
+}
+
+__device__ void contact_activate(const DevParams &P, DPair &q)
+{
+	q.flags |= PF_CONTACT | PF_DASHPOT;
+	q.fsn_norm = 0;
+	q.normal_load = 0;
+	for (int k = 0; k < 3; k++) q.fs_total[k] = 0;
+	if (P.friction) {
+		q.state = (P.friction_model == 2 || P.friction_model == 3) ? 1 : 2;
+		for (int k = 0; k < 3; k++) { q.disp_tan[k] = 0; q.prev_disp_tan[k] = 0; }
+	} else {
+		q.state = 1;
+	}
+}
+
+__device__ void contact_deactivate(const DevParams &P, DPair &q)
+{
+	q.state = 0;
+	q.flags &= ~(PF_CONTACT | PF_DASHPOT);
+	q.fsn_norm = 0;
+	for (int k = 0; k < 3; k++) q.fs_total[k] = 0;
+	if (P.friction)
+		for (int k = 0; k < 3; k++) { q.disp_tan[k] = 0; q.fs_tan[k] = 0; }
+}
+
+__device__ void lub_update(const DevParams &P, DPair &q, const DPairConst &c)
+{
+	if (!P.lub_on) return;
+	bool in_range = q.r < c.lub_range && q.r > c.ro;
+	bool act = q.flags & PF_LUB;
+	if (!act && in_range) { q.flags |= PF_LUB; act = true; }
+	if (act && !in_range) { q.flags &= ~PF_LUB; act = false; }
+	if (act && q.gap > 0) {
+		double coeff = 1/(q.gap+P.lub_reduce);
+		q.lub_coeff = coeff;
+		q.log_lub_coeff = coeff > 1. ? log(coeff) : 0.;
+	}
+}
+
+__device__ void set_tan_norm(DPair &q, const DPairConst &c, double cur, double target)
+{
+	double s = target/cur;
+	for (int k = 0; k < 3; k++) q.disp_tan[k] = s*q.disp_tan[k];
+	for (int k = 0; k < 3; k++) q.fs_tan[k] = c.kt_s*q.disp_tan[k];
+}
+
+__device__ void friction_law(const DevParams &P, DPair &q, const DPairConst &c)
+{
+	int fm = P.friction_model;
+	v3 ft = ld3(q.fs_tan);
+	if (fm == 1) {
+		double sup;
+		double sq = vsq(ft);
+		q.normal_load = q.fsn_norm;
+		sup = (q.state == 2) ? P.mu_s*q.normal_load : P.mu_d*q.normal_load;
+		if (sq > sup*sup) { q.state = 3; sup = P.mu_d*q.normal_load; }
+		else q.state = 2;
+		if (q.state == 3) set_tan_norm(q, c, sqrt(sq), sup);
+	} else if (fm == 2) {
+		double sup = q.fsn_norm-P.critical_load;
+		if (sup < 0) {
+			q.state = 1;
+			for (int k = 0; k < 3; k++) { q.disp_tan[k] = 0; q.fs_tan[k] = 0; }
+		} else {
+			sup *= P.mu_s;
+			double sq = vsq(ft);
+			if (sq > sup*sup) { q.state = 3; set_tan_norm(q, c, sqrt(sq), sup); }
+			else q.state = 2;
+		}
+	} else if (fm == 3) {
+		double sup = q.fsn_norm-P.critical_load;
+		if (sup < 0) {
+			q.state = 1;
+			for (int k = 0; k < 3; k++) { q.disp_tan[k] = 0; q.fs_tan[k] = 0; }
+		} else q.state = 2;
+	} else if (fm == 5) {
+		double sq = vsq(ft);
+		if (sq > P.ft_max*P.ft_max) { q.state = 3; set_tan_norm(q, c, sqrt(sq), P.ft_max); }
+		else q.state = 2;
+	} else if (fm == 6) {
+		q.normal_load = q.fsn_norm;
+		double sup = (q.state == 2) ? P.mu_s*q.normal_load : P.mu_d*q.normal_load;
+		if (sup > P.ft_max) sup = P.ft_max;
+		double sq = vsq(ft);
+		if (sq > sup*sup) { q.state = 3; set_tan_norm(q, c, sqrt(sq), sup); }
+		else q.state = 2;
+	}
+}
+
+__device__ void contact_spring(const DevParams &P, DPair &q, const DPairConst &c)
+{
+	if (!(q.flags & PF_CONTACT)) return;
+	q.fsn_norm = -c.kn_s*q.gap;
+	v3 n = ld3(q.nvec);
+	v3 fn = vscale(-q.fsn_norm, n);
+	if (P.friction) {
+		v3 d = ld3(q.disp_tan);
+		d = vsub(d, vscale(vdot(d, n), n));
+		st3(q.disp_tan, d);
+		st3(q.fs_tan, vscale(c.kt_s, d));
+		friction_law(P, q, c);
+	}
+	if (q.state <= 1) st3(q.fs_total, fn);
+	else st3(q.fs_total, vadd(fn, ld3(q.fs_tan)));
+}
+
+__device__ void contact_increment(const DevParams &P, const DevClock &K, const double *vel, const double *ang,
+                                  DPair &q, const DPairConst &c, double dt, int in_predictor)
+{
+	if (!P.friction) return;
+	v3 off = vscale((double)q.zoff, ld3(K.vel_diff));
+	v3 tdv = vadd(vsub(ld3(vel+3*q.p1), ld3(vel+3*q.p0)), off);
+	v3 n = ld3(q.nvec);
+	v3 rdv = vneg(vcross(vadd(vscale(c.a0, ld3(ang+3*q.p0)), vscale(c.a1, ld3(ang+3*q.p1))), n));
+	v3 rsv = vadd(tdv, rdv);
+	rsv = vsub(rsv, vscale(vdot(rsv, n), n));
+	q.rsv_sq = vsq(rsv);
+	if (in_predictor) for (int k = 0; k < 3; k++) q.prev_disp_tan[k] = q.disp_tan[k];
+	st3(q.disp_tan, vadd(ld3(q.prev_disp_tan), vscale(dt, rsv)));
+}
+
+__device__ void repulsion_force(const DevParams &P, DPair &q, const DPairConst &c)
+{
+	double gap = q.r-c.ro;
+	double red;
+	if (gap > 0) {
+		if (P.rep_max_len == -1) red = exp(-gap/P.rep_len);
+		else red = exp(-gap/P.rep_len)*0.5*(1+tanh(-(gap-P.rep_max_len)/1e-3));
+		red *= c.rep_geo;
+	} else {
+		red = c.rep_geo;
+	}
+	q.rep_reduced = red;
+	double fn = P.repulsion*red;
+	st3(q.rep_force, vscale(-fn, ld3(q.nvec)));
+}
+
+__global__ void k_pairs_update(DevParams P, int np, DevClock *__restrict__ clk, const double *__restrict__ pos,
+                               const double *__restrict__ vel, const double *__restrict__ ang,
+                               DPair *__restrict__ pairs, const DPairConst *__restrict__ pc, int mode,
+                               int in_predictor, int zero_dt)
+{
+	int t = blockIdx.x*blockDim.x+threadIdx.x;
+	double sq_local = 0;
+	if (t < np) {
+		DPair q = pairs[t];
+		const DPairConst &c = pc[t];
+		DevClock K = *clk;
+		const double *sd = K.shear_disp;
+		double dt = zero_dt ? 0.0 : K.dt;
+		if (mode >= 1 && !(q.flags & PF_INTER)) {
+			v3 d = vsub(ld3(pos+3*q.p1), ld3(pos+3*q.p0));
+			periodize_diff(P, sd, d);
+			double range = c.range;
+			if (vsq(d) < range*range) {
+				// Interaction ctor + activateForceMembers (Interaction.cpp:13-36, 137-156)
+				int p0 = q.p0, p1 = q.p1;
+				memset(&q, 0, sizeof q);
+				q.p0 = p0; q.p1 = p1;
+				q.flags = PF_INTER;
+				pair_geometry(P, sd, pos, q, c);
+				if (q.gap <= 0) contact_activate(P, q);
+				lub_update(P, q, c);
+			}
+		}
+		if (mode != 2 && (q.flags & PF_INTER)) {
+			// Interaction::updateState (Interaction.cpp:171-198)
+			if (q.flags & PF_CONTACT) contact_increment(P, K, vel, ang, q, c, dt, in_predictor);
+			pair_geometry(P, sd, pos, q, c);
+			if (q.r > c.range) {
+				if (q.flags & PF_CONTACT) contact_deactivate(P, q);
+				q.flags = 0;   // interaction removed (System.cpp:1395-1400)
+			} else {
+				if (q.flags & PF_CONTACT) {
+					if (q.gap > 0) contact_deactivate(P, q);
+				} else if (q.gap <= 0) {
+					contact_activate(P, q);
+				}
+				if (q.flags & PF_CONTACT) contact_spring(P, q, c);
+				lub_update(P, q, c);
+				if (P.repulsiveforce) repulsion_force(P, q, c);
+				if (P.friction && (q.flags & PF_CONTACT)) sq_local = q.rsv_sq;
+			}
+		}
+		pairs[t] = q;
+	}
+	// block max of the sliding velocity, then one atomic per block
+	__shared__ double red[256];
+	red[threadIdx.x] = sq_local;
+	__syncthreads();
+	for (int o = blockDim.x/2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x+o]);
+		__syncthreads();
+	}
+	if (threadIdx.x == 0 && red[0] > 0)
+		atomicMax(&clk->sq_max_sliding_bits, (unsigned long long)__double_as_longlong(red[0]));
+}
+
+__global__ void k_clear_sliding(DevClock *clk) { clk->sq_max_sliding_bits = 0; }
+__global__ void k_finish_sliding(DevClock *clk)
+{
+	clk->max_sliding_velocity = sqrt(dmax_atomic_value(clk->sq_max_sliding_bits));
+}
+
+// ---------------------------------------------------------------------------
+// resistance blocks (Lubrication.cpp:406-580, ContactDashpot.cpp:186-340,
+// Interaction.cpp:238-311) and diagonal accumulation (System.cpp:1429-1473)
+// ---------------------------------------------------------------------------
+__device__ void xa_blocks(double XA0, double XA1, double XA3, v3 n, double *od, double *b0, double *b1)
+{
+	for (int k = 0; k < 18; k++) od[k] = 0;
+	for (int k = 0; k < 15; k++) { b0[k] = 0; b1[k] = 0; }
+	od[0] = XA1*n.x*n.x; od[1] = XA1*n.x*n.y; od[2] = XA1*n.x*n.z;
+	od[5] = XA1*n.y*n.y; od[6] = XA1*n.y*n.z; od[8] = XA1*n.z*n.z;
+	b0[0] = XA0*n.x*n.x; b0[1] = XA0*n.x*n.y; b0[2] = XA0*n.x*n.z;
+	b0[5] = XA0*n.y*n.y; b0[6] = XA0*n.y*n.z; b0[8] = XA0*n.z*n.z;
+	b1[0] = XA3*n.x*n.x; b1[1] = XA3*n.x*n.y; b1[2] = XA3*n.x*n.z;
+	b1[5] = XA3*n.y*n.y; b1[6] = XA3*n.y*n.z; b1[8] = XA3*n.z*n.z;
+}
+
+// full (squeeze + tangential) blocks; the lubrication and dashpot forms
+// share this algebra (the dashpot writes YA+(XA-YA)nn where lubrication
+// writes XA nn + YA(1-nn) for the diagonal blocks, handled by `dp`).
+__device__ void full_blocks(const double *XA, const double *YA, const double *YB, const double *YC, v3 n,
+                            bool dp, double *od, double *b0, double *b1)
+{
+	double nx = n.x, ny = n.y, nz = n.z;
+	double XA1_YA1 = XA[1]-YA[1];
+	od[0] = YA[1] + XA1_YA1*nx*nx;
+	od[1] = XA1_YA1*nx*ny;
+	od[2] = XA1_YA1*nx*nz;
+	od[3] = -YB[2]*nz;
+	od[4] = YB[2]*ny;
+	od[5] = YA[1] + XA1_YA1*ny*ny;
+	od[6] = XA1_YA1*ny*nz;
+	od[7] = -YB[2]*nx;
+	od[8] = YA[1] + XA1_YA1*nz*nz;
+	od[9] = YB[1]*nz;
+	od[10] = -YB[1]*ny;
+	od[11] = YC[1]*(1-nx*nx);
+	od[12] = -YC[1]*nx*ny;
+	od[13] = -YC[1]*nx*nz;
+	od[14] = YB[1]*nx;
+	od[15] = YC[1]*(1-ny*ny);
+	od[16] = -YC[1]*ny*nz;
+	od[17] = YC[1]*(1-nz*nz);
+	for (int s = 0; s < 2; s++) {
+		int a = s == 0 ? 0 : 3;
+		double *b = s == 0 ? b0 : b1;
+		if (dp) {
+			double XmY = XA[a]-YA[a];
+			b[0] = YA[a] + XmY*nx*nx;
+			b[1] = XmY*nx*ny;
+			b[2] = XmY*nx*nz;
+			b[3] = -YB[a]*nz;
+			b[4] = YB[a]*ny;
+			b[5] = YA[a] + XmY*ny*ny;
+			b[6] = XmY*ny*nz;
+			b[7] = -YB[a]*nx;
+			b[8] = YA[a] + XmY*nz*nz;
+			b[9] = YC[a]*(1-nx*nx);
+			b[10] = -YC[a]*nx*ny;
+			b[11] = -YC[a]*nx*nz;
+			b[12] = YC[a]*(1-ny*ny);
+			b[13] = -YC[a]*ny*nz;
+			b[14] = YC[a]*(1-nz*nz);
+		} else {
+			double n0n0 = nx*nx, n0n1 = nx*ny, n0n2 = nx*nz, n1n1 = ny*ny, n1n2 = ny*nz, n2n2 = nz*nz;
+			double one_n0n0 = 1-n0n0, one_n1n1 = 1-n1n1, one_n2n2 = 1-n2n2;
+			double XmY = XA[a]-YA[a];
+			b[0] = XA[a]*n0n0+YA[a]*one_n0n0;
+			b[1] = XmY*n0n1;
+			b[2] = XmY*n0n2;
+			b[3] = -YB[a]*nz;
+			b[4] = YB[a]*ny;
+			b[5] = XA[a]*n1n1+YA[a]*one_n1n1;
+			b[6] = XmY*n1n2;
+			b[7] = -YB[a]*nx;
+			b[8] = XA[a]*n2n2+YA[a]*one_n2n2;
+			b[9] = YC[a]*one_n0n0;
+			b[10] = -YC[a]*n0n1;
+			b[11] = -YC[a]*n0n2;
+			b[12] = YC[a]*one_n1n1;
+			b[13] = -YC[a]*n1n2;
+			b[14] = YC[a]*one_n2n2;
+		}
+	}
+}
+
+__device__ __forceinline__ bool has_resistance(const DevParams &P, int flags)
+{
+	if (!(flags & PF_INTER)) return false;
+	if (P.lub_on) return (flags & PF_DASHPOT) || (flags & PF_LUB);
+	return flags & PF_DASHPOT;
+}
+
+__global__ void k_pair_blocks(DevParams P, int np, const DPair *__restrict__ pairs, const DPairConst *__restrict__ pc,
+                              double *__restrict__ odb, double *__restrict__ bscr)
+{
+	int t = blockIdx.x*blockDim.x+threadIdx.x;
+	if (t >= np) return;
+	const DPair &q = pairs[t];
+	double od[18], b0[15], b1[15];
+	if (!has_resistance(P, q.flags)) {
+		for (int k = 0; k < 18; k++) od[k] = 0;
+		for (int k = 0; k < 15; k++) { b0[k] = 0; b1[k] = 0; }
+	} else {
+		const DPairConst &c = pc[t];
+		v3 n = ld3(q.nvec);
+		if (q.flags & PF_DASHPOT) {
+			const double *D = c.dc;
+			if (P.dp_tan_coeff > 0) full_blocks(D+DXA, D+DYA, D+DYB, D+DYC, n, true, od, b0, b1);
+			else xa_blocks(D[DXA+0], D[DXA+1], D[DXA+3], n, od, b0, b1);
+		} else {
+			double XA[4], YA[4], YB[4], YC[4];
+			for (int k = 0; k < 4; k++) {
+				XA[k] = c.lc[CXA+k]*q.lub_coeff;
+				YA[k] = c.lc[CYA+k]*q.log_lub_coeff;
+				YB[k] = c.lc[CYB+k]*q.log_lub_coeff;
+				YC[k] = c.lc[CYC+k]*q.log_lub_coeff;
+			}
+			if (P.tangential) full_blocks(XA, YA, YB, YC, n, false, od, b0, b1);
+			else xa_blocks(XA[0], XA[1], XA[3], n, od, b0, b1);
+		}
+	}
+	for (int k = 0; k < 18; k++) odb[18*(int64_t)t+k] = od[k];
+	for (int k = 0; k < 15; k++) { bscr[30*(int64_t)t+k] = b0[k]; bscr[30*(int64_t)t+15+k] = b1[k]; }
+}
+
+// DBlock of particle i: Stokes drag (System.cpp:558-575), then the b1 blocks
+// of the pairs where i is the larger index (ascending partner), then the b0
+// blocks of the pairs where i is the smaller index -- the reference's
+// column-by-column accumulation order.
+__global__ void k_dblocks(DevParams P, int n, const double *__restrict__ radius, const int *__restrict__ row_ptr,
+                          const int *__restrict__ col_ptr, const int *__restrict__ col_idx,
+                          const double *__restrict__ bscr, double *__restrict__ dbl)
+{
+	int i = blockIdx.x*blockDim.x+threadIdx.x;
+	if (i >= n) return;
+	double d[15];
+	for (int k = 0; k < 15; k++) d[k] = 0;
+	double a = radius[i];
+	double FU = P.sd_coeff*a;
+	double TW = P.sd_coeff*pow(a, 3)*4.0/3;
+	d[0] = FU; d[5] = FU; d[8] = FU;
+	d[9] = TW; d[12] = TW; d[14] = TW;
+	for (int k = col_ptr[i]; k < col_ptr[i+1]; k++) {
+		const double *b1 = bscr+30*(int64_t)col_idx[k]+15;
+		for (int e = 0; e < 15; e++) d[e] += b1[e];
+	}
+	for (int t = row_ptr[i]; t < row_ptr[i+1]; t++) {
+		const double *b0 = bscr+30*(int64_t)t;
+		for (int e = 0; e < 15; e++) d[e] += b0[e];
+	}
+	for (int k = 0; k < 15; k++) dbl[15*(int64_t)i+k] = d[k];
+}
+
+// ---------------------------------------------------------------------------
+// force components (System.cpp:1727-1828)
+// ---------------------------------------------------------------------------
+// ContactDashpot::getForceOnP0 (ContactDashpot.cpp:342-385)
+__device__ v3 dashpot_force_p0(const DevParams &P, const double *vel_diff, const DPair &q, const DPairConst &c,
+                               v3 vi, v3 vj, v3 oi, v3 oj, bool affine)
+{
+	if (!(q.flags & PF_DASHPOT)) return vzero();
+	if (affine) vj = vadd(vj, vscale((double)q.zoff, ld3(vel_diff)));
+	v3 n = ld3(q.nvec);
+	const double *D = c.dc;
+	v3 f = vscale(-vdot(vadd(vscale(D[DXA+0], vi), vscale(D[DXA+1], vj)), n), n);
+	if (P.dp_tan_coeff > 0) {
+		v3 t1 = vsub(vscale(-D[DYA+0], vsub(vi, vscale(vdot(n, vi), n))), vscale(D[DYA+1], vsub(vj, vscale(vdot(n, vj), n))));
+		f = vadd(f, t1);
+		v3 t2 = vsub(vscale(-D[DYB+0], vcross(n, oi)), vscale(D[DYB+2], vcross(n, oj)));
+		f = vadd(f, t2);
+	}
+	return f;
+}
+
+// per pair: 4 components x (F0, T0, F1, T1)
+__global__ void k_pair_forces(DevParams P, int np, const DevClock *__restrict__ clk, const DPair *__restrict__ pairs,
+                              const DPairConst *__restrict__ pc, const double *__restrict__ u_inf,
+                              double *__restrict__ scr)
+{
+	int t = blockIdx.x*blockDim.x+threadIdx.x;
+	if (t >= np) return;
+	const DPair &q = pairs[t];
+	double *o = scr+48*(int64_t)t;
+	for (int k = 0; k < 48; k++) o[k] = 0;
+	if (!(q.flags & PF_INTER)) return;
+	const DPairConst &c = pc[t];
+	v3 n = ld3(q.nvec);
+	// contact (Contact::addUpForceTorque, Contact.cpp:419-437)
+	if (q.flags & PF_CONTACT) {
+		v3 f = ld3(q.fs_total);
+		st3(o+0, f);
+		st3(o+6, vneg(f));
+		if (q.state >= 2) {
+			v3 tq = vcross(n, ld3(q.fs_tan));
+			st3(o+3, vscale(c.a0, tq));
+			st3(o+9, vscale(c.a1, tq));
+		}
+	}
+	// dashpot R_FU U_inf (ContactDashpot::getRFU_Uinf, :426-441)
+	if ((q.flags & PF_CONTACT) && (q.flags & PF_DASHPOT)) {
+		v3 om = V(clk->Omega[0], clk->Omega[1], clk->Omega[2]);
+		v3 f0 = dashpot_force_p0(P, clk->vel_diff, q, c, ld3(u_inf+3*q.p0), ld3(u_inf+3*q.p1), om, om, true);
+		v3 t0 = vzero();
+		if (P.dp_tan_coeff > 0) t0 = vscale(c.a0, vcross(n, f0));
+		st3(o+12, f0);
+		st3(o+15, t0);
+		st3(o+18, vneg(f0));
+		st3(o+21, vscale(c.a1/c.a0, t0));
+	}
+	// hydro (Lubrication::calcGEHE_squeeze_tangential / calcGE_squeeze, :332-403)
+	if (P.lub_on && (q.flags & PF_LUB)) {
+		double XG[4], YG[4], YH[4];
+		for (int k = 0; k < 4; k++) {
+			XG[k] = c.lc[CXG+k]*q.lub_coeff;
+			YG[k] = c.lc[CYG+k]*q.log_lub_coeff;
+			YH[k] = c.lc[CYH+k]*q.log_lub_coeff;
+		}
+		double nnE = vdot(n, sdot(clk->Einf, n));
+		if (!P.tangential) {
+			double ci = (XG[0]+XG[2])*nnE, cj = (XG[1]+XG[3])*nnE;
+			st3(o+24, V(ci*n.x, ci*n.y, ci*n.z));
+			st3(o+30, V(cj*n.x, cj*n.y, cj*n.z));
+		} else {
+			double YG0_YG2 = YG[0]+YG[2], YG1_YG3 = YG[1]+YG[3];
+			double cGE_i = (XG[0]+XG[2]-2*YG0_YG2)*nnE;
+			double cGE_j = (XG[1]+XG[3]-2*YG1_YG3)*nnE;
+			double cHE_i = YH[0]+YH[2], cHE_j = YH[1]+YH[3];
+			v3 En = sdot(clk->Einf, n);
+			st3(o+24, vadd(vscale(cGE_i, n), vscale(YG0_YG2*2, En)));
+			st3(o+30, vadd(vscale(cGE_j, n), vscale(YG1_YG3*2, En)));
+			v3 nExn = vcross(En, n);
+			st3(o+27, vscale(-2*cHE_i, nExn));
+			st3(o+33, vscale(-2*cHE_j, nExn));
+		}
+	}
+	// repulsion (RepulsiveForce::addUpForce, :101-105)
+	if (P.repulsiveforce) {
+		v3 f = ld3(q.rep_force);
+		st3(o+36, f);
+		st3(o+42, vneg(f));
+	}
+}
+
+// per particle gather: components c with stride 12 in scratch of width W
+__global__ void k_gather_pairs(int n, int ncomp, int width, const int *__restrict__ row_ptr,
+                               const int *__restrict__ col_ptr, const int *__restrict__ col_idx,
+                               const double *__restrict__ scr, double *__restrict__ out)
+{
+	int i = blockIdx.x*blockDim.x+threadIdx.x;
+	if (i >= n) return;
+	for (int c = 0; c < ncomp; c++) {
+		double a[6] = {0, 0, 0, 0, 0, 0};
+		for (int k = col_ptr[i]; k < col_ptr[i+1]; k++) {
+			const double *s = scr+width*(int64_t)col_idx[k]+12*c+6;
+			for (int e = 0; e < 6; e++) a[e] += s[e];
+		}
+		for (int t = row_ptr[i]; t < row_ptr[i+1]; t++) {
+			const double *s = scr+width*(int64_t)t+12*c;
+			for (int e = 0; e < 6; e++) a[e] += s[e];
+		}
+		for (int e = 0; e < 6; e++) out[(int64_t)c*6*n+6*i+e] = a[e];
+	}
+}
+
+// torque mask per component: contact (friction), dashpot (1), hydro (tangential), repulsion (0)
+__global__ void k_rhs(DevParams P, int n, int divided, const double *__restrict__ fc, double *__restrict__ rhs)
+{
+	int t = blockIdx.x*blockDim.x+threadIdx.x;
+	if (t >= 6*n) return;
+	int d = t%6;
+	bool has[NFC] = {true, true, (bool)P.lub_on, (bool)P.repulsiveforce};
+	bool tq[NFC] = {(bool)P.friction, true, (bool)P.tangential, false};
+	if (divided) {
+		for (int c = 0; c < NFC; c++)
+			rhs[(int64_t)c*6*n+t] = (!has[c] || (d >= 3 && !tq[c])) ? 0.0 : fc[(int64_t)c*6*n+t];
+	} else {
+		double s = 0;
+		for (int c = 0; c < NFC; c++)
+			if (has[c] && (d < 3 || tq[c])) s += fc[(int64_t)c*6*n+t];
+		rhs[t] = s;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// stresslets (Stress.cpp:77-287, Lubrication.cpp:587-650, Contact.cpp:439-467,
+// RepulsiveForce.cpp:108-131)
+// ---------------------------------------------------------------------------
+__global__ void k_rate_split(int n, const DevParams P, const DevClock *__restrict__ clk, const double *__restrict__ vc,
+                             const double *__restrict__ u_inf, double *__restrict__ split)
+{
+	// split[12 i + 0..5] = rate-proportional (v, w) incl. u_inf, Omega;
+	// split[12 i + 6..11] = rate-independent (v, w)  (Stress.cpp:112-148)
+	int i = blockIdx.x*blockDim.x+threadIdx.x;
+	if (i >= n) return;
+	double pv[6] = {0, 0, 0, 0, 0, 0}, iv[6] = {0, 0, 0, 0, 0, 0};
+	bool has[NFC] = {true, true, (bool)P.lub_on, (bool)P.repulsiveforce};
+	bool prop[NFC] = {false, true, true, false};
+	for (int c = 0; c < NFC; c++) {
+		if (!has[c]) continue;
+		const double *v = vc+(int64_t)c*6*n+6*i;
+		for (int e = 0; e < 6; e++) {
+			if (prop[c]) pv[e] += v[e];
+			else iv[e] += v[e];
+		}
+	}
+	for (int e = 0; e < 3; e++) pv[e] += u_inf[3*i+e];
+	for (int e = 0; e < 3; e++) pv[3+e] += clk->Omega[e];
+	for (int e = 0; e < 6; e++) { split[12*i+e] = pv[e]; split[12*i+6+e] = iv[e]; }
+}
+
+__global__ void k_pair_stress(DevParams P, int np, const DevClock *__restrict__ clk, const DPair *__restrict__ pairs,
+                              const DPairConst *__restrict__ pc, const double *__restrict__ vc,
+                              const double *__restrict__ vel, const double *__restrict__ ang,
+                              const double *__restrict__ split, int n, double *__restrict__ scr)
+{
+	int t = blockIdx.x*blockDim.x+threadIdx.x;
+	if (t >= np) return;
+	const int W = 12*NSC;
+	double *o = scr+W*(int64_t)t;
+	for (int k = 0; k < W; k++) o[k] = 0;
+	const DPair &q = pairs[t];
+	if (!(q.flags & PF_INTER)) return;
+	const DPairConst &c = pc[t];
+	int i = q.p0, j = q.p1;
+	v3 nv = ld3(q.nvec);
+	s2 Si, Sj;
+	if (P.lub_on && (q.flags & PF_LUB)) {
+		double XG[4], YG[4], XM[4], YM[4];
+		for (int k = 0; k < 4; k++) {
+			XG[k] = c.lc[CXG+k]*q.lub_coeff;
+			YG[k] = c.lc[CYG+k]*q.log_lub_coeff;
+			XM[k] = c.lc[CXM+k]*q.lub_coeff;
+			YM[k] = c.lc[CYM+k]*q.log_lub_coeff;
+		}
+		s2 nn = outer(nv);
+		// GU per velocity component (Lubrication::addGUStresslet)
+		bool has[NFC] = {true, true, (bool)P.lub_on, (bool)P.repulsiveforce};
+		for (int cc = 0; cc < NFC; cc++) {
+			if (!has[cc]) continue;
+			const double *v = vc+(int64_t)cc*6*n;
+			v3 vi = ld3(v+6*i), vj = ld3(v+6*j), oi = ld3(v+6*i+3), oj = ld3(v+6*j+3);
+			double nvi = vdot(nv, vi), nvj = vdot(nv, vj);
+			Si = sscale(-(XG[0]*nvi+XG[1]*nvj), nn);
+			Sj = sscale(-(XG[2]*nvi+XG[3]*nvj), nn);
+			if (P.tangential) {
+				s2 ti = ssub(outer_sym(nv, vi), sscale(nvi, nn));
+				s2 tj = ssub(outer_sym(nv, vj), sscale(nvj, nn));
+				sadd_to(Si, sscale(-2, saddv(sscale(YG[0], ti), sscale(YG[1], tj))));
+				sadd_to(Sj, sscale(-2, saddv(sscale(YG[2], ti), sscale(YG[3], tj))));
+				s2 t2i = outer_sym(nv, vcross(oi, nv));
+				s2 t2j = outer_sym(nv, vcross(oj, nv));
+				sadd_to(Si, sscale(-2, saddv(sscale(YM[0], t2i), sscale(YM[1], t2j))));
+				sadd_to(Sj, sscale(-2, saddv(sscale(YM[2], t2i), sscale(YM[3], t2j))));
+			}
+			int slot = SC_GU_CONTACT+cc;
+			for (int e = 0; e < 6; e++) { o[12*slot+e] = Si.e[e]; o[12*slot+6+e] = Sj.e[e]; }
+		}
+		// ME (Lubrication::addMEStresslet)
+		double nnE = vdot(nv, sdot(clk->Einf, nv));
+		double coeff = 1.5*nnE;
+		Si = sscale(coeff*(XM[0]+XM[1]), nn);
+		Sj = sscale(coeff*(XM[2]+XM[3]), nn);
+		if (P.tangential) {
+			v3 En = sdot(clk->Einf, nv);
+			s2 T = sscale(2, ssub(outer_sym(nv, En), sscale(nnE, nn)));
+			sadd_to(Si, sscale(YM[0]+YM[1], T));
+			sadd_to(Sj, sscale(YM[2]+YM[3], T));
+		}
+		for (int e = 0; e < 6; e++) { o[12*SC_ME+e] = Si.e[e]; o[12*SC_ME+6+e] = Sj.e[e]; }
+	}
+	v3 rv = ld3(q.rvec);
+	double r_ij = c.a0+c.a1;
+	if (P.control == 0) {
+		if (q.flags & PF_CONTACT) {
+			// Contact::addUpStress with total velocities
+			v3 F = vadd(ld3(q.fs_total), dashpot_force_p0(P, clk->vel_diff, q, c, ld3(vel+3*i), ld3(vel+3*j),
+			                                             ld3(ang+3*i), ld3(ang+3*j), true));
+			s2 XF = outer_sym(rv, F);
+			s2 a = sscale(c.a0/r_ij, XF), b = sscale(c.a1/r_ij, XF);
+			for (int e = 0; e < 6; e++) { o[12*SC_XF_CONTACT+e] = a.e[e]; o[12*SC_XF_CONTACT+6+e] = b.e[e]; }
+		}
+	} else {
+		s2 pi_ = szero(), pj_ = szero(), ii_ = szero(), ij_ = szero();
+		if (q.flags & PF_CONTACT) {
+			s2 sp = outer_sym(rv, ld3(q.fs_total));
+			sadd_to(ii_, sscale(c.a0/r_ij, sp));
+			sadd_to(ij_, sscale(c.a1/r_ij, sp));
+		}
+		if (q.flags & PF_DASHPOT) {
+			const double *si = split+12*i, *sj = split+12*j;
+			s2 rp = outer_sym(rv, dashpot_force_p0(P, clk->vel_diff, q, c, ld3(si), ld3(sj), ld3(si+3), ld3(sj+3), true));
+			sadd_to(pi_, sscale(c.a0/r_ij, rp));
+			sadd_to(pj_, sscale(c.a1/r_ij, rp));
+			s2 ri = outer_sym(rv, dashpot_force_p0(P, clk->vel_diff, q, c, ld3(si+6), ld3(sj+6), ld3(si+9), ld3(sj+9), false));
+			sadd_to(ii_, sscale(c.a0/r_ij, ri));
+			sadd_to(ij_, sscale(c.a1/r_ij, ri));
+		}
+		for (int e = 0; e < 6; e++) {
+			o[12*SC_XF_RATEPROP+e] = pi_.e[e]; o[12*SC_XF_RATEPROP+6+e] = pj_.e[e];
+			o[12*SC_XF_RATEINDEP+e] = ii_.e[e]; o[12*SC_XF_RATEINDEP+6+e] = ij_.e[e];
+		}
+	}
+	if (P.repulsiveforce) {
+		v3 F = vscale(-(P.repulsion*q.rep_reduced), nv);
+		s2 sc = sscale(0.5, outer_sym(rv, F));
+		for (int e = 0; e < 6; e++) { o[12*SC_XF_REPULSION+e] = sc.e[e]; o[12*SC_XF_REPULSION+6+e] = sc.e[e]; }
+	}
+}
+
+// per-component totals over particles (fixed-order tree reduction)
+__global__ void k_stress_totals(int n, const double *__restrict__ sc, double *__restrict__ tot)
+{
+	__shared__ double red[256][6];
+	int c = blockIdx.x;
+	double a[6] = {0, 0, 0, 0, 0, 0};
+	for (int i = threadIdx.x; i < n; i += blockDim.x)
+		for (int e = 0; e < 6; e++) a[e] += sc[(int64_t)c*6*n+6*i+e];
+	for (int e = 0; e < 6; e++) red[threadIdx.x][e] = a[e];
+	__syncthreads();
+	for (int o = blockDim.x/2; o > 0; o >>= 1) {
+		if (threadIdx.x < o)
+			for (int e = 0; e < 6; e++) red[threadIdx.x][e] += red[threadIdx.x+o][e];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0)
+		for (int e = 0; e < 6; e++) tot[6*c+e] = red[0][e];
+}
+
+__device__ void set_rate(const DevParams &P, DevClock &K, double rate)
+{
+	// System::set_shear_rate + setVelocityDifference (System.cpp:1967-1982)
+	K.shear_rate = rate;
+	for (int k = 0; k < 3; k++) K.Omega[k] = P.Ohat[k]*rate;
+	for (int k = 0; k < 6; k++) K.Einf[k] = P.Ehat[k]*rate;
+	v3 vd = vscale(2, sdot(K.Einf, V(0, 0, P.lz)));
+	K.vel_diff[0] = vd.x; K.vel_diff[1] = vd.y; K.vel_diff[2] = vd.z;
+}
+
+__global__ void k_set_rate(DevParams P, DevClock *clk, double rate) { set_rate(P, *clk, rate); }
+
+// System::computeShearRate (System.cpp:2017-2055) from the component totals
+__global__ void k_shear_rate(DevParams P, DevClock *clk, const double *__restrict__ tot, int has_mask)
+{
+	DevClock &K = *clk;
+	const int rate_of[NSC] = {1, 0, 1, 1, 0, 2, 0, 1, 0};  // 0 indep 1 prop 2 dependent
+	double prop[6] = {0, 0, 0, 0, 0, 0}, indep[6] = {0, 0, 0, 0, 0, 0};
+	for (int c = 0; c < NSC; c++) {
+		if (!(has_mask & (1 << c))) continue;
+		for (int e = 0; e < 6; e++) {
+			if (rate_of[c] == 0) indep[e] += tot[6*c+e];
+			if (rate_of[c] == 1) prop[e] += tot[6*c+e];
+		}
+	}
+	double inv = 1.0/P.system_volume;
+	for (int e = 0; e < 6; e++) { prop[e] *= inv; indep[e] *= inv; }
+	for (int e = 0; e < 6; e++) prop[e] += 2*K.Einf[e]/(6*M_PI);
+	double rp = doubledot(prop, K.Einf), ri = doubledot(indep, K.Einf);
+	K.rate_prop = rp;
+	K.rate_indep = ri;
+	if (rp != 0) set_rate(P, K, (P.target_stress-ri)/rp);
+	if (K.strain < P.init_strain_limit && K.shear_rate > P.init_rate_limit) set_rate(P, K, P.init_rate_limit);
+}
+
+// rescale rate-proportional components (System.cpp:2264-2271), sum
+// components into na (System.cpp:2236-2250) and the max |U_na|
+__global__ void k_velocities(DevParams P, int n, int divided, int stress_ctl, int want_max, DevClock *__restrict__ clk,
+                             double *__restrict__ vc, const double *__restrict__ sol, double *__restrict__ na)
+{
+	int i = blockIdx.x*blockDim.x+threadIdx.x;
+	double sq = 0;
+	if (i < n) {
+		double v[6];
+		if (divided) {
+			bool has[NFC] = {true, true, (bool)P.lub_on, (bool)P.repulsiveforce};
+			bool prop[NFC] = {false, true, true, false};
+			double rate = clk->shear_rate;
+			for (int e = 0; e < 6; e++) v[e] = 0;
+			for (int c = 0; c < NFC; c++) {
+				if (!has[c]) continue;
+				double *x = vc+(int64_t)c*6*n+6*i;
+				if (stress_ctl && prop[c])
+					for (int e = 0; e < 6; e++) x[e] *= rate;
+				for (int e = 0; e < 6; e++) v[e] += x[e];
+			}
+		} else {
+			for (int e = 0; e < 6; e++) v[e] = sol[6*i+e];
+		}
+		for (int e = 0; e < 6; e++) na[6*i+e] = v[e];
+		sq = v[0]*v[0]+v[1]*v[1]+v[2]*v[2];
+	}
+	if (!want_max) return;
+	__shared__ double red[256];
+	red[threadIdx.x] = sq;
+	__syncthreads();
+	for (int o = blockDim.x/2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x+o]);
+		__syncthreads();
+	}
+	if (threadIdx.x == 0 && red[0] > 0)
+		atomicMax(&clk->sq_max_vel_bits, (unsigned long long)__double_as_longlong(red[0]));
+}
+
+__global__ void k_clear_maxvel(DevClock *clk) { clk->sq_max_vel_bits = 0; }
+__global__ void k_finish_maxvel(DevClock *clk) { clk->max_velocity = sqrt(dmax_atomic_value(clk->sq_max_vel_bits)); }
+
+// System::computeUInf (System.cpp:2357-2367)
+__global__ void k_u_inf(int n, const DevClock *__restrict__ clk, const double *__restrict__ pos, double *__restrict__ u)
+{
+	int i = blockIdx.x*blockDim.x+threadIdx.x;
+	if (i >= n) return;
+	v3 p = ld3(pos+3*i);
+	v3 om = V(clk->Omega[0], clk->Omega[1], clk->Omega[2]);
+	st3(u+3*i, vadd(sdot(clk->Einf, p), vcross(om, p)));
+}
+
+// System::adjustVelocityPeriodicBoundary (System.cpp:2369-2392)
+__global__ void k_total_velocity(int n, const DevClock *__restrict__ clk, const double *__restrict__ na,
+                                 const double *__restrict__ u_inf, double *__restrict__ vel, double *__restrict__ ang)
+{
+	int i = blockIdx.x*blockDim.x+threadIdx.x;
+	if (i >= n) return;
+	st3(vel+3*i, vadd(ld3(na+6*i), ld3(u_inf+3*i)));
+	st3(ang+3*i, vadd(ld3(na+6*i+3), V(clk->Omega[0], clk->Omega[1], clk->Omega[2])));
+}
+
+// System::adaptTimeStep(time_end, strain_end) (System.cpp:1013-1066)
+__global__ void k_adapt_dt(DevParams P, DevClock *clk, double time_end, double strain_end)
+{
+	DevClock &K = *clk;
+	double dt;
+	if (K.max_velocity > 0 || K.max_sliding_velocity > 0) {
+		if (K.max_velocity > K.max_sliding_velocity) dt = P.disp_max/K.max_velocity;
+		else dt = P.disp_max/K.max_sliding_velocity;
+	} else {
+		dt = P.disp_max/K.shear_rate;
+	}
+	if (dt*K.shear_rate > P.disp_max) dt = P.disp_max/K.shear_rate;
+	if (P.dt_max > 0 && dt > P.dt_max) dt = P.dt_max;
+	if (P.dt_min > 0 && dt < P.dt_min) dt = P.dt_min;
+	if (strain_end >= 0) {
+		if (fabs(dt*K.shear_rate) > strain_end-K.strain) dt = fabs((strain_end-K.strain)/K.shear_rate);
+	}
+	if (time_end >= 0) {
+		if (K.time+dt > time_end) dt = time_end-K.time;
+	}
+	K.dt = dt;
+}
+
+// clocks + System::timeStepBoxing (System.cpp:672-717)
+__global__ void k_boxing(DevParams P, DevClock *clk)
+{
+	DevClock &K = *clk;
+	K.time += K.dt;
+	K.steps++;
+	K.strain += K.shear_rate*K.dt;
+	v3 ez = sdot(K.Einf, V(0, 0, 1));
+	v3 inc = V(2*ez.x*K.dt, 2*ez.y*K.dt, 2*ez.z*K.dt);
+	for (int k = 0; k < 3; k++) K.shear_disp[k] += P.lz*(k == 0 ? inc.x : (k == 1 ? inc.y : inc.z));
+	int m = (int)(K.shear_disp[0]/P.lx);
+	if (K.shear_disp[0] < 0) m--;
+	K.shear_disp[0] = K.shear_disp[0]-m*P.lx;
+	if (!P.twodim) {
+		m = (int)(K.shear_disp[1]/P.ly);
+		if (K.shear_disp[1] < 0) m--;
+		K.shear_disp[1] = K.shear_disp[1]-m*P.ly;
+	}
+}
+
+// System::displacement (System.cpp:2418-2443); corrector: the velocity
+// average of timeStepMoveCorrector (System.cpp:1164-1187) first
+__global__ void k_move(DevParams P, int n, int corrector, const DevClock *__restrict__ clk, double *__restrict__ pos,
+                       double *__restrict__ vel, double *__restrict__ ang, const double *__restrict__ vel_pred,
+                       const double *__restrict__ ang_pred)
+{
+	int i = blockIdx.x*blockDim.x+threadIdx.x;
+	if (i >= n) return;
+	double dt = clk->dt;
+	v3 v = ld3(vel+3*i);
+	v3 dr;
+	if (corrector) {
+		v3 vp = ld3(vel_pred+3*i);
+		v = vscale(0.5, vadd(v, vp));
+		st3(ang+3*i, vscale(0.5, vadd(ld3(ang+3*i), ld3(ang_pred+3*i))));
+		dr = vscale(dt, vsub(v, vp));
+	} else {
+		dr = vscale(dt, v);
+	}
+	v3 p = vadd(ld3(pos+3*i), dr);
+	int zs = periodize(P, clk->shear_disp, p);
+	if (zs != 0) v = vadd(v, vscale((double)zs, ld3(clk->vel_diff)));
+	st3(pos+3*i, p);
+	st3(vel+3*i, v);
+}
+
+__global__ void k_copy(int64_t n, const double *__restrict__ a, double *__restrict__ b)
+{
+	int64_t t = blockIdx.x*(int64_t)blockDim.x+threadIdx.x;
+	if (t < n) b[t] = a[t];
+}
+
+__global__ void k_set_dt(DevClock *clk, double dt) { clk->dt = dt; }
+
+__global__ void k_sticky(const int *status, int *err)
+{
+	if (*status != 0x7fffffff) atomicMin(err, *status);
+}
+
+// merge pair state from the previous superset (rows sorted by p1)
+__global__ void k_merge(int np, int n, const int *__restrict__ new_row_ptr, const int *__restrict__ new_cand,
+                        const DPair *__restrict__ old_pairs, const int *__restrict__ old_row_ptr, int old_n,
+                        DPair *__restrict__ out)
+{
+	int i = blockIdx.x*blockDim.x+threadIdx.x;
+	if (i >= n) return;
+	for (int t = new_row_ptr[i]; t < new_row_ptr[i+1]; t++) {
+		int j = new_cand[t];
+		int found = -1;
+		if (old_pairs && i < old_n) {
+			int lo = old_row_ptr[i], hi = old_row_ptr[i+1]-1;
+			while (lo <= hi) {
+				int m = (lo+hi) >> 1;
+				int pj = old_pairs[m].p1;
+				if (pj == j) { found = m; break; }
+				if (pj < j) lo = m+1; else hi = m-1;
+			}
+		}
+		DPair q;
+		if (found >= 0) q = old_pairs[found];
+		else {
+			memset(&q, 0, sizeof q);
+			q.p0 = i; q.p1 = j;
+		}
+		out[t] = q;
+	}
+	(void)np;
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static CellView view(const DevSim &S)
+{
+	CellView C;
+	C.ncx = S.ncx; C.ncy = S.ncy; C.ncz = S.ncz; C.brute = S.brute; C.n = S.n;
+	C.csx = S.csx; C.csy = S.csy; C.csz = S.csz;
+	C.start = S.cell_start; C.count = S.cell_count; C.list = S.cell_list;
+	return C;
+}
+
+void phys_set_shear_rate(DevSim &S, double rate, bool, cudaStream_t st)
+{
+	k_set_rate<<<1, 1, 0, st>>>(S.P, S.clock, rate);
+	S.launches++;
+}
+
+void phys_u_inf(DevSim &S, cudaStream_t st)
+{
+	k_u_inf<<<blocks_for(S.n, 128), 128, 0, st>>>(S.n, S.clock, S.pos, S.u_inf);
+	S.launches++;
+}
+
+void phys_cells(DevSim &S, double, cudaStream_t st)
+{
+	if (S.brute) return;
+	int ncell = S.ncx*S.ncy*S.ncz;
+	LFG_CUDA(cudaMemsetAsync(S.cell_count, 0, sizeof(int)*ncell, st));
+	CellView C = view(S);
+	k_cell_assign<<<blocks_for(S.n, 128), 128, 0, st>>>(S.P, C, S.pos, S.cell_of, S.cell_count);
+	k_scan<<<1, 1024, 0, st>>>(ncell, S.cell_count, S.cell_start, nullptr);
+	// reuse cand_count as the fill counter
+	LFG_CUDA(cudaMemsetAsync(S.cand_count, 0, sizeof(int)*ncell, st));
+	k_cell_fill<<<blocks_for(S.n, 128), 128, 0, st>>>(S.n, S.cell_of, S.cell_start, S.cand_count, S.cell_list);
+	k_cell_sort<<<blocks_for(ncell, 128), 128, 0, st>>>(ncell, S.cell_start, S.cell_count, S.cell_list);
+	S.launches += 4;
+}
+
+void phys_candidates(DevSim &S, cudaStream_t st, int *h_total)
+{
+	CellView C = view(S);
+	k_candidates<<<blocks_for(S.n, 128), 128, 0, st>>>(S.P, C, S.clock, S.pos, S.radius, S.cand_count, nullptr, nullptr);
+	k_scan<<<1, 1024, 0, st>>>(S.n, S.cand_count, S.cand_ptr, nullptr);
+	LFG_CUDA(cudaMemcpyAsync(h_total, S.cand_ptr+S.n, sizeof(int), cudaMemcpyDeviceToHost, st));
+	LFG_CUDA(cudaStreamSynchronize(st));
+	if (*h_total > S.cand_cap) {
+		if (S.cand) cudaFree(S.cand);
+		S.cand_cap = *h_total+*h_total/4+1024;
+		LFG_CUDA(cudaMalloc((void **)&S.cand, sizeof(int)*S.cand_cap));
+	}
+	k_candidates<<<blocks_for(S.n, 128), 128, 0, st>>>(S.P, C, S.clock, S.pos, S.radius, S.cand_count, S.cand_ptr, S.cand);
+	S.launches += 3;
+}
+
+void phys_check_superset(DevSim &S, cudaStream_t st)
+{
+	CellView C = view(S);
+	k_check_superset<<<blocks_for(S.n, 128), 128, 0, st>>>(S.P, C, S.clock, S.pos, S.radius, S.row_ptr, S.pairs);
+	S.launches++;
+}
+
+void phys_pair_constants(DevSim &S, cudaStream_t st)
+{
+	if (!S.npairs) return;
+	k_pair_constants<<<blocks_for(S.npairs, 128), 128, 0, st>>>(S.P, S.npairs, S.pairs, S.radius, S.pconst);
+	S.launches++;
+}
+
+void phys_clear_sliding(DevSim &S, cudaStream_t st) { k_clear_sliding<<<1, 1, 0, st>>>(S.clock); S.launches++; }
+void phys_finish_sliding(DevSim &S, cudaStream_t st) { k_finish_sliding<<<1, 1, 0, st>>>(S.clock); S.launches++; }
+
+void phys_pairs_update(DevSim &S, int mode, int in_predictor, bool zero_dt, cudaStream_t st)
+{
+	k_clear_sliding<<<1, 1, 0, st>>>(S.clock);
+	if (S.npairs)
+		k_pairs_update<<<blocks_for(S.npairs, 256), 256, 0, st>>>(S.P, S.npairs, S.clock, S.pos, S.vel, S.ang, S.pairs,
+		                                                          S.pconst, mode, in_predictor, zero_dt ? 1 : 0);
+	k_finish_sliding<<<1, 1, 0, st>>>(S.clock);
+	S.launches += 3;
+}
+
+void phys_blocks(DevSim &S, double *dbl, double *odbl, cudaStream_t st)
+{
+	if (S.npairs)
+		k_pair_blocks<<<blocks_for(S.npairs, 128), 128, 0, st>>>(S.P, S.npairs, S.pairs, S.pconst, odbl, S.blk_scratch);
+	k_dblocks<<<blocks_for(S.n, 128), 128, 0, st>>>(S.P, S.n, S.radius, S.row_ptr, S.col_ptr, S.col_idx,
+	                                                S.blk_scratch, dbl);
+	S.launches += 2;
+}
+
+void phys_force_components(DevSim &S, cudaStream_t st)
+{
+	if (S.npairs)
+		k_pair_forces<<<blocks_for(S.npairs, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst, S.u_inf,
+		                                                         S.pair_scratch);
+	k_gather_pairs<<<blocks_for(S.n, 128), 128, 0, st>>>(S.n, NFC, 48, S.row_ptr, S.col_ptr, S.col_idx,
+	                                                     S.pair_scratch, S.fc);
+	S.launches += 2;
+}
+
+void phys_rhs(DevSim &S, int divided, cudaStream_t st)
+{
+	k_rhs<<<blocks_for(6*S.n, 256), 256, 0, st>>>(S.P, S.n, divided, S.fc, S.rhs);
+	S.launches++;
+}
+
+void phys_stresslets(DevSim &S, cudaStream_t st)
+{
+	double *split = S.sc_tot+6*NSC;  // n x 12 region after the totals
+	if (S.P.control == 1) {
+		k_rate_split<<<blocks_for(S.n, 128), 128, 0, st>>>(S.n, S.P, S.clock, S.vc, S.u_inf, split);
+		S.launches++;
+	}
+	if (S.npairs)
+		k_pair_stress<<<blocks_for(S.npairs, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst, S.vc,
+		                                                         S.vel, S.ang, split, S.n, S.pair_scratch);
+	k_gather_pairs<<<blocks_for(S.n, 128), 128, 0, st>>>(S.n, NSC, 12*NSC, S.row_ptr, S.col_ptr, S.col_idx,
+	                                                     S.pair_scratch, S.sc);
+	k_stress_totals<<<NSC, 256, 0, st>>>(S.n, S.sc, S.sc_tot);
+	S.launches += 3;
+}
+
+static int sc_mask(const DevParams &P)
+{
+	int m = 0;
+	if (P.lub_on) {
+		m |= 1 << SC_ME;
+		m |= 1 << SC_GU_CONTACT;
+		m |= 1 << SC_GU_DASHPOT;
+		m |= 1 << SC_GU_HYDRO;
+		if (P.repulsiveforce) m |= 1 << SC_GU_REPULSION;
+	}
+	if (P.control == 0) m |= 1 << SC_XF_CONTACT;
+	else m |= (1 << SC_XF_RATEPROP) | (1 << SC_XF_RATEINDEP);
+	if (P.repulsiveforce) m |= 1 << SC_XF_REPULSION;
+	return m;
+}
+
+void phys_shear_rate_from_stress(DevSim &S, cudaStream_t st)
+{
+	k_shear_rate<<<1, 1, 0, st>>>(S.P, S.clock, S.sc_tot, sc_mask(S.P));
+	S.launches++;
+}
+
+void phys_velocities(DevSim &S, int divided, int in_predictor, cudaStream_t st)
+{
+	int want_max = (!S.P.fixed_dt && in_predictor) ? 1 : 0;
+	if (want_max) { k_clear_maxvel<<<1, 1, 0, st>>>(S.clock); S.launches++; }
+	k_velocities<<<blocks_for(S.n, 256), 256, 0, st>>>(S.P, S.n, divided, S.P.control == 1, want_max, S.clock, S.vc,
+	                                                   S.sol, S.na);
+	S.launches++;
+	if (want_max) { k_finish_maxvel<<<1, 1, 0, st>>>(S.clock); S.launches++; }
+	if (S.P.control == 1) phys_u_inf(S, st);
+	k_total_velocity<<<blocks_for(S.n, 128), 128, 0, st>>>(S.n, S.clock, S.na, S.u_inf, S.vel, S.ang);
+	S.launches++;
+}
+
+void phys_adapt_dt(DevSim &S, double time_end, double strain_end, cudaStream_t st)
+{
+	k_adapt_dt<<<1, 1, 0, st>>>(S.P, S.clock, time_end, strain_end);
+	S.launches++;
+}
+
+void phys_boxing(DevSim &S, cudaStream_t st)
+{
+	k_boxing<<<1, 1, 0, st>>>(S.P, S.clock);
+	S.launches++;
+}
+
+void phys_move(DevSim &S, int corrector, cudaStream_t st)
+{
+	k_move<<<blocks_for(S.n, 128), 128, 0, st>>>(S.P, S.n, corrector, S.clock, S.pos, S.vel, S.ang, S.vel_pred, S.ang_pred);
+	S.launches++;
+}
+
+void phys_save_pred(DevSim &S, cudaStream_t st)
+{
+	k_copy<<<blocks_for(3*S.n, 256), 256, 0, st>>>(3*(int64_t)S.n, S.vel, S.vel_pred);
+	k_copy<<<blocks_for(3*S.n, 256), 256, 0, st>>>(3*(int64_t)S.n, S.ang, S.ang_pred);
+	S.launches += 2;
+}
+
+void phys_set_dt(DevSim &S, double dt, cudaStream_t st)
+{
+	k_set_dt<<<1, 1, 0, st>>>(S.clock, dt);
+	S.launches++;
+}
+
+void phys_sticky_status(const int *status, int *err, cudaStream_t st)
+{
+	k_sticky<<<1, 1, 0, st>>>(status, err);
+}
+
+void phys_merge_pairs(DevSim &S, const DPair *old_pairs, const int *old_row_ptr, int old_n, cudaStream_t st)
+{
+	k_merge<<<blocks_for(S.n, 128), 128, 0, st>>>(S.npairs, S.n, S.cand_ptr, S.cand, old_pairs, old_row_ptr, old_n, S.pairs);
+	S.launches++;
+}
+
+} // namespace lfg

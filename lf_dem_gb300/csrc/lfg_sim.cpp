@@ -1,0 +1,841 @@
+// lfg_sim.cpp -- host driver of the device-resident time step that replaces
+// System::timeEvolution (LF_DEM/System.cpp:1203-1279), and the lfg_sim_* C ABI.
+//
+// All state lives on the device.  Per step the host only launches kernels
+// (factorisation and solves are CUDA graphs) and synchronises once, after the
+// corrector move, to read the clock and the "superset stale" flag.  The pair
+// list is a superset of the interactions (every pair within range + skin);
+// its sparsity pattern is the pattern of R_FU, so the nested-dissection
+// analysis is redone only when a pair within range falls outside it.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "lfg_physics.h"
+#include "lfg_solver.h"
+
+namespace lfg {
+int fail(lfg_status *st, int code, int info, const char *msg);
+int ok(lfg_status *st);
+int check_device(int device, lfg_status *st);
+
+class Sim {
+public:
+	Sim(const lfg_params &p, const lfg_options &o, int n, const double *pos, const double *radius, double lx,
+	    double ly, double lz, const double *le_disp, cudaStream_t st);
+	~Sim();
+	void set_contacts(int ncs, const int32_t *p0, const int32_t *p1, const double *dt);
+	void first_time();
+	void step(int calc_stress, double time_end, double strain_end);
+	void advance(double time_end, double strain_end);
+	void scalars(lfg_sim_scalars *o);
+	void particles(double *pos, double *vel, double *ang, double *na_vel, double *na_ang);
+	int num_pairs();
+	int get_pairs(lfg_pair *out, int cap);
+	int particle_stress(int comp, double *out);
+	int velocity_component(int comp, double *out);
+	int set_contact(int p0, int p1, int state, const double *disp_tan);
+	void set_clock(double time, double strain, double dt, double rate, double maxv, double maxsv);
+	void refresh();
+	int assemble(double *dbl, int32_t *row, int32_t *col, double *odbl, int cap, int *nb_out);
+	int force_component(int comp, double *out);
+	void timing(lfg_sim_timing *o) const;
+	int error_code = 0, error_info = 0;
+	std::string error_msg;
+
+private:
+	void rebuild_superset();
+	void compute_velocities(int calc_stress, int in_predictor);
+	void check_error();
+	void pull_clock();
+	void stage_begin(int s);
+	void stage_end(int s);
+
+	lfg_params prm_;
+	lfg_options opt_;
+	DevSim S_;
+	Solver *solver_ = nullptr;
+	cudaStream_t st_;
+	bool firsttime_ = true;
+	DevClock *h_clock_ = nullptr;
+	int *d_err_ = nullptr, *h_err_ = nullptr;
+	std::vector<double> h_pos_;
+	int symbolic_runs_ = 0;
+	// stage timing
+	struct Ev { cudaEvent_t a, b; int stage; };
+	std::vector<Ev> evs_;
+	size_t ev_used_ = 0;
+	int cur_stage_ = -1;
+	double stage_ms_[8] = {0};
+	int64_t launches_mark_ = 0;
+	int64_t last_launches_ = 0;
+};
+
+static DevParams make_dev_params(const lfg_params &p, int n, double lx, double ly, double lz, double skin)
+{
+	DevParams P;
+	std::memset(&P, 0, sizeof P);
+	P.n = n;
+	P.friction = p.friction_model != 0;
+	P.friction_model = p.friction_model;
+	P.mu_s = P.friction ? p.mu_static : 0;
+	P.mu_d = p.mu_dynamic < 0 ? P.mu_s : p.mu_dynamic;
+	P.kn = p.kn; P.kt = p.kt;
+	P.critical_load = p.critical_load; P.ft_max = p.ft_max;
+	P.repulsiveforce = p.repulsion_on && p.repulsive_length > 0;
+	P.repulsion = p.repulsion; P.rep_len = p.repulsive_length; P.rep_max_len = p.repulsive_max_length;
+	P.lub_on = p.lubrication_model != 0;
+	P.tangential = p.lubrication_model == 2;
+	P.lub_reduce = p.lub_reduce_parameter; P.lub_max_gap = p.lub_max_gap;
+	P.interaction_range = p.interaction_range;
+	P.sd_coeff = p.sd_coeff;
+	// ContactDashpot::setDashpotResistanceCoeffs (ContactDashpot.cpp:65-105),
+	// evaluated on the host as in the reference
+	double rn = p.contact_relaxation_time, rt = p.contact_relaxation_time_tan;
+	if (rn > 0) P.dp_normal_coeff = 4*p.kn*rn;
+	else if (P.lub_on) P.dp_normal_coeff = 1/p.lub_reduce_parameter;
+	else throw Error{LFG_ERR_BAD_ARG, 0, "normal relaxation time <= 0 without lubrication"};
+	if (!P.friction && !P.tangential) P.dp_tan_coeff = 0;
+	else if (rt > 0) {
+		if (P.lub_on) throw Error{LFG_ERR_BAD_ARG, 0, "with lubrication the tangential relaxation time cannot be positive"};
+		P.dp_tan_coeff = 6*p.kt*rt;
+	} else {
+		if (!P.lub_on) throw Error{LFG_ERR_BAD_ARG, 0, "tangential relaxation time <= 0 without lubrication"};
+		P.dp_tan_coeff = p.lub_reduce_parameter < 1 ? std::log(1/p.lub_reduce_parameter) : 0;
+	}
+	P.lx = lx; P.ly = ly; P.lz = lz;
+	P.lx_half = lx/2; P.ly_half = ly/2; P.lz_half = lz/2;
+	P.twodim = ly == 0;
+	for (int k = 0; k < 6; k++) P.Ehat[k] = p.Ehat[k];
+	for (int k = 0; k < 3; k++) P.Ohat[k] = p.Ohat[k];
+	P.disp_max = p.disp_max; P.dt_max = p.dt_max; P.dt_min = p.dt_min;
+	P.fixed_dt = p.fixed_dt;
+	P.control = p.control;
+	P.integration_method = p.integration_method;
+	P.target_stress = p.target_stress;
+	P.init_strain_limit = p.init_strain_shear_rate_limit;
+	P.init_rate_limit = p.init_shear_rate_limit;
+	P.system_volume = P.twodim ? lx*lz : lx*ly*lz;
+	P.skin = skin;
+	return P;
+}
+
+template <typename V> static void dalloc(V *&p, size_t count)
+{
+	LFG_CUDA(cudaMalloc((void **)&p, sizeof(V)*std::max<size_t>(count, 1)));
+	LFG_CUDA(cudaMemset(p, 0, sizeof(V)*std::max<size_t>(count, 1)));
+	LFG_CUDA(cudaDeviceSynchronize());
+}
+
+Sim::Sim(const lfg_params &p, const lfg_options &o, int n, const double *pos, const double *radius, double lx,
+         double ly, double lz, const double *le_disp, cudaStream_t st)
+    : prm_(p), opt_(o), st_(st)
+{
+	if (p.friction_model == 4 || p.friction_model < 0 || p.friction_model > 6)
+		throw Error{LFG_ERR_BAD_ARG, p.friction_model, "unknown friction model"};
+	if (p.lubrication_model < 0 || p.lubrication_model > 2)
+		throw Error{LFG_ERR_BAD_ARG, p.lubrication_model, "unknown lubrication model"};
+	if (p.lubrication_model == 2 && p.lub_max_gap >= 1)
+		throw Error{LFG_ERR_BAD_ARG, 0, "lub_max_gap must be smaller than 1 (System.cpp:340-346)"};
+	S_.n = n;
+	S_.P = make_dev_params(p, n, lx, ly, lz, o.skin);
+	dalloc(S_.clock, 1);
+	dalloc(S_.pos, 3*n); dalloc(S_.radius, n);
+	dalloc(S_.vel, 3*n); dalloc(S_.ang, 3*n); dalloc(S_.vel_pred, 3*n); dalloc(S_.ang_pred, 3*n);
+	dalloc(S_.u_inf, 3*n); dalloc(S_.na, 6*n);
+	dalloc(S_.vc, (size_t)NFC*6*n); dalloc(S_.fc, (size_t)NFC*6*n);
+	dalloc(S_.rhs, (size_t)NFC*6*n); dalloc(S_.sol, (size_t)NFC*6*n);
+	dalloc(S_.sc, (size_t)NSC*6*n); dalloc(S_.sc_tot, (size_t)NSC*6+12*(size_t)n);
+	dalloc(S_.row_ptr, n+1); dalloc(S_.col_ptr, n+1);
+	dalloc(d_err_, 1);
+	LFG_CUDA(cudaMallocHost((void **)&h_clock_, sizeof(DevClock)));
+	LFG_CUDA(cudaMallocHost((void **)&h_err_, sizeof(int)));
+	LFG_CUDA(cudaMemcpyAsync(S_.pos, pos, sizeof(double)*3*n, cudaMemcpyHostToDevice, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	LFG_CUDA(cudaMemcpyAsync(S_.radius, radius, sizeof(double)*n, cudaMemcpyHostToDevice, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	int big = 0x7fffffff;
+	LFG_CUDA(cudaMemcpyAsync(d_err_, &big, sizeof(int), cudaMemcpyHostToDevice, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	// clock: rate control starts at the imposed rate, stress control at 0
+	// (SimulationInit.cpp:276); dt = p.dt (System.cpp:607)
+	DevClock K;
+	std::memset(&K, 0, sizeof K);
+	K.dt = p.dt;
+	if (le_disp) { K.shear_disp[0] = le_disp[0]; K.shear_disp[1] = le_disp[1]; }
+	LFG_CUDA(cudaMemcpyAsync(S_.clock, &K, sizeof K, cudaMemcpyHostToDevice, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	phys_set_shear_rate(S_, p.control == 0 ? p.shear_rate : 0.0, false, st_);
+	// cells sized for the largest superset range
+	double amax = 0;
+	for (int i = 0; i < n; i++) amax = std::max(amax, radius[i]);
+	double rc = (p.interaction_range < 0 ? 2+p.lub_max_gap+o.skin : p.interaction_range+o.skin)*amax;
+	S_.ncx = std::max(1, (int)(lx/rc));
+	S_.ncy = S_.P.twodim ? 1 : std::max(1, (int)(ly/rc));
+	S_.ncz = std::max(1, (int)(lz/rc));
+	S_.brute = (S_.ncx < 3 || S_.ncz < 3 || (!S_.P.twodim && S_.ncy < 3)) ? 1 : 0;
+	S_.csx = lx/S_.ncx; S_.csy = S_.P.twodim ? 1.0 : ly/S_.ncy; S_.csz = lz/S_.ncz;
+	int ncell = S_.ncx*S_.ncy*S_.ncz;
+	dalloc(S_.cell_of, n); dalloc(S_.cell_count, ncell); dalloc(S_.cell_start, ncell+1); dalloc(S_.cell_list, n);
+	dalloc(S_.cand_count, std::max(n, ncell)); dalloc(S_.cand_ptr, n+1);
+	solver_ = new Solver(n, opt_, st_);
+	h_pos_.assign(pos, pos+3*n);
+	rebuild_superset();
+	// System::setupGenericConfiguration -> checkNewInteraction (System.cpp:517-519)
+	phys_pairs_update(S_, 2, 0, true, st_);
+}
+
+Sim::~Sim()
+{
+	delete solver_;
+	void *p[] = {S_.clock, S_.pos, S_.radius, S_.vel, S_.ang, S_.vel_pred, S_.ang_pred, S_.u_inf, S_.na, S_.vc,
+	             S_.fc, S_.rhs, S_.sol, S_.sc, S_.sc_tot, S_.pairs, S_.pconst, S_.row_ptr, S_.col_ptr, S_.col_idx,
+	             S_.blk_scratch, S_.pair_scratch, S_.cell_of, S_.cell_start, S_.cell_count, S_.cell_list,
+	             S_.cand_count, S_.cand_ptr, S_.cand, d_err_};
+	for (void *q : p) if (q) cudaFree(q);
+	if (h_clock_) cudaFreeHost(h_clock_);
+	if (h_err_) cudaFreeHost(h_err_);
+	for (auto &e : evs_) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
+}
+
+// Build the pair superset at the current positions, carry the pair state of
+// the previous superset over, and redo the symbolic analysis.
+void Sim::rebuild_superset()
+{
+	phys_cells(S_, 0, st_);
+	int total = 0;
+	phys_candidates(S_, st_, &total);
+	DPair *old = S_.pairs;
+	int *old_row = nullptr;
+	int old_n = old ? S_.n : 0;
+	if (old) {
+		LFG_CUDA(cudaMalloc((void **)&old_row, sizeof(int)*(S_.n+1)));
+		LFG_CUDA(cudaMemcpyAsync(old_row, S_.row_ptr, sizeof(int)*(S_.n+1), cudaMemcpyDeviceToDevice, st_));
+	}
+	S_.npairs = total;
+	if (total > S_.cap || !old) {
+		S_.cap = std::max(total+total/4+256, S_.cap);
+		if (S_.pconst) cudaFree(S_.pconst);
+		if (S_.blk_scratch) cudaFree(S_.blk_scratch);
+		if (S_.pair_scratch) cudaFree(S_.pair_scratch);
+		if (S_.col_idx) cudaFree(S_.col_idx);
+		S_.pconst = nullptr; S_.blk_scratch = S_.pair_scratch = nullptr; S_.col_idx = nullptr;
+		dalloc(S_.pconst, S_.cap);
+		dalloc(S_.blk_scratch, (size_t)30*S_.cap);
+		dalloc(S_.pair_scratch, (size_t)12*NSC*S_.cap);
+		dalloc(S_.col_idx, S_.cap);
+	}
+	DPair *fresh = nullptr;
+	dalloc(fresh, S_.cap);
+	S_.pairs = fresh;
+	phys_merge_pairs(S_, old, old_row, old_n, st_);
+	LFG_CUDA(cudaMemcpyAsync(S_.row_ptr, S_.cand_ptr, sizeof(int)*(S_.n+1), cudaMemcpyDeviceToDevice, st_));
+	phys_pair_constants(S_, st_);
+	// host copies of the pattern: transpose lists and the symbolic analysis
+	std::vector<int> rp(S_.n+1), cand(total);
+	LFG_CUDA(cudaMemcpyAsync(rp.data(), S_.cand_ptr, sizeof(int)*(S_.n+1), cudaMemcpyDeviceToHost, st_));
+	if (total) LFG_CUDA(cudaMemcpyAsync(cand.data(), S_.cand, sizeof(int)*total, cudaMemcpyDeviceToHost, st_));
+	std::vector<double> pos(3*S_.n);
+	LFG_CUDA(cudaMemcpyAsync(pos.data(), S_.pos, sizeof(double)*3*S_.n, cudaMemcpyDeviceToHost, st_));
+	LFG_CUDA(cudaStreamSynchronize(st_));
+	if (old) cudaFree(old);
+	if (old_row) cudaFree(old_row);
+	std::vector<int32_t> od_row(total), od_col(total);
+	std::vector<int> cp(S_.n+1, 0), ci(total);
+	for (int i = 0; i < S_.n; i++)
+		for (int t = rp[i]; t < rp[i+1]; t++) { od_col[t] = i; od_row[t] = cand[t]; cp[cand[t]+1]++; }
+	for (int i = 0; i < S_.n; i++) cp[i+1] += cp[i];
+	{
+		std::vector<int> f(cp.begin(), cp.end()-1);
+		for (int t = 0; t < total; t++) ci[f[od_row[t]]++] = t;   // ascending t = ascending p0 per p1
+	}
+	LFG_CUDA(cudaMemcpyAsync(S_.col_ptr, cp.data(), sizeof(int)*(S_.n+1), cudaMemcpyHostToDevice, st_));
+	if (total) LFG_CUDA(cudaMemcpyAsync(S_.col_idx, ci.data(), sizeof(int)*total, cudaMemcpyHostToDevice, st_));
+	solver_->set_pattern(total, od_row.data(), od_col.data(), pos.data(), S_.P.lx, S_.P.ly, S_.P.lz, false);
+	symbolic_runs_++;
+}
+
+void Sim::set_contacts(int ncs, const int32_t *p0, const int32_t *p1, const double *dt)
+{
+	for (int c = 0; c < ncs; c++)
+		if (set_contact(p0[c], p1[c], -1, dt+3*c) != 0)
+			throw Error{LFG_ERR_BAD_ARG, c, "contact state for a pair that is not within interaction range"};
+}
+
+// System::timeEvolution first-time block (System.cpp:1216-1226); the
+// interactions of the configuration are created here as well
+// (System::setupGenericConfiguration, System.cpp:517-520).
+void Sim::first_time()
+{
+	if (!firsttime_) return;
+	phys_pairs_update(S_, 1, 1, true, st_);
+	firsttime_ = false;
+}
+
+void Sim::stage_begin(int s)
+{
+	if (ev_used_ == evs_.size()) {
+		Ev e;
+		LFG_CUDA(cudaEventCreate(&e.a));
+		LFG_CUDA(cudaEventCreate(&e.b));
+		evs_.push_back(e);
+	}
+	evs_[ev_used_].stage = s;
+	LFG_CUDA(cudaEventRecord(evs_[ev_used_].a, st_));
+	cur_stage_ = s;
+}
+
+void Sim::stage_end(int)
+{
+	LFG_CUDA(cudaEventRecord(evs_[ev_used_].b, st_));
+	ev_used_++;
+	cur_stage_ = -1;
+}
+
+void Sim::compute_velocities(int calc_stress, int in_predictor)
+{
+	// System::computeVelocities (System.cpp:2273-2319)
+	bool stress_ctl = prm_.control == 1;
+	int divided = (calc_stress || stress_ctl) ? 1 : 0;
+	stage_begin(1);
+	if (stress_ctl) phys_set_shear_rate(S_, 1.0, false, st_);
+	phys_u_inf(S_, st_);
+	phys_blocks(S_, solver_->d_dblocks(), solver_->d_odblocks(), st_);
+	stage_end(1);
+	stage_begin(2);
+	solver_->factorize_async();
+	phys_sticky_status(solver_->d_status(), d_err_, st_);
+	stage_end(2);
+	stage_begin(4);
+	phys_force_components(S_, st_);
+	phys_rhs(S_, divided, st_);
+	stage_end(4);
+	stage_begin(3);
+	lfg_status st;
+	std::memset(&st, 0, sizeof st);
+	int rc = solver_->solve_device(divided ? NFC : 1, S_.rhs, divided ? S_.vc : S_.sol, &st, false);
+	stage_end(3);
+	if (rc == LFG_ERR_NOT_CONVERGED) { error_code = rc; error_msg = st.msg; }
+	stage_begin(4);
+	if (divided && stress_ctl) {
+		phys_stresslets(S_, st_);
+		phys_shear_rate_from_stress(S_, st_);
+	}
+	phys_velocities(S_, divided, in_predictor, st_);
+	stage_end(4);
+}
+
+void Sim::pull_clock()
+{
+	LFG_CUDA(cudaMemcpyAsync(h_clock_, S_.clock, sizeof(DevClock), cudaMemcpyDeviceToHost, st_));
+	LFG_CUDA(cudaStreamSynchronize(st_));
+}
+
+void Sim::step(int calc_stress, double time_end, double strain_end)
+{
+	first_time();
+	ev_used_ = 0;
+	int64_t l0 = S_.launches;
+	if (!prm_.fixed_dt) phys_adapt_dt(S_, time_end, strain_end, st_);
+	if (prm_.integration_method == 0) {
+		// System::timeEvolutionEulersMethod + timeStepMove (System.cpp:843-882, 1083-1122)
+		compute_velocities(calc_stress, 1);
+		if (calc_stress) { stage_begin(4); phys_stresslets(S_, st_); stage_end(4); }
+		stage_begin(5);
+		if (!prm_.fixed_dt) phys_adapt_dt(S_, time_end, strain_end, st_);
+		phys_boxing(S_, st_);
+		phys_move(S_, 0, st_);
+		stage_end(5);
+	} else {
+		// predictor (System.cpp:888-930, 1124-1162)
+		compute_velocities(calc_stress, 1);
+		if (calc_stress) { stage_begin(4); phys_stresslets(S_, st_); stage_end(4); }
+		stage_begin(5);
+		if (!prm_.fixed_dt) phys_adapt_dt(S_, time_end, strain_end, st_);
+		phys_boxing(S_, st_);
+		phys_move(S_, 0, st_);
+		stage_end(5);
+		stage_begin(0);
+		phys_pairs_update(S_, 0, 1, false, st_);
+		stage_end(0);
+		phys_save_pred(S_, st_);
+		// corrector (System.cpp:931-983, 1164-1187)
+		compute_velocities(calc_stress, 0);
+		if (calc_stress) { stage_begin(4); phys_stresslets(S_, st_); stage_end(4); }
+		stage_begin(5);
+		phys_move(S_, 1, st_);
+		stage_end(5);
+	}
+	// checkNewInteraction: the superset must hold every pair within range
+	stage_begin(0);
+	LFG_CUDA(cudaMemsetAsync(&S_.clock->stale, 0, sizeof(int), st_));
+	phys_cells(S_, 0, st_);
+	phys_check_superset(S_, st_);
+	stage_end(0);
+	pull_clock();
+	if (h_clock_->stale) rebuild_superset();
+	stage_begin(0);
+	phys_pairs_update(S_, 1, 0, false, st_);
+	stage_end(0);
+	LFG_CUDA(cudaMemcpyAsync(h_err_, d_err_, sizeof(int), cudaMemcpyDeviceToHost, st_));
+	pull_clock();
+	last_launches_ = S_.launches-l0;
+	for (int k = 0; k < 8; k++) stage_ms_[k] = 0;
+	for (size_t e = 0; e < ev_used_; e++) {
+		float ms = 0;
+		cudaEventElapsedTime(&ms, evs_[e].a, evs_[e].b);
+		stage_ms_[evs_[e].stage] += ms;
+	}
+	check_error();
+}
+
+void Sim::check_error()
+{
+	if (*h_err_ != 0x7fffffff) {
+		error_code = LFG_ERR_NOT_SPD;
+		error_info = *h_err_;
+		error_msg = "non-positive pivot in the resistance factorisation";
+	}
+}
+
+void Sim::advance(double time_end, double strain_end)
+{
+	// System::timeEvolution loop and final stress step (System.cpp:1227-1279)
+	first_time();
+	pull_clock();
+	double adj = prm_.fixed_dt ? prm_.dt : 0;
+	auto keep = [&](double te, double se) {
+		if (h_clock_->strain > se-1e-8 && se >= 0) return false;
+		if (h_clock_->time > te-1e-8 && te >= 0) return false;
+		return true;
+	};
+	while (keep(time_end-adj, strain_end-adj)) {
+		step(0, time_end, strain_end);
+		if (error_code) return;
+	}
+	step(1, time_end, strain_end);
+}
+
+void Sim::scalars(lfg_sim_scalars *o)
+{
+	pull_clock();
+	std::memset(o, 0, sizeof *o);
+	const DevClock &K = *h_clock_;
+	o->time = K.time; o->strain = K.strain; o->shear_rate = K.shear_rate; o->dt = K.dt;
+	o->shear_disp[0] = K.shear_disp[0]; o->shear_disp[1] = K.shear_disp[1];
+	o->max_velocity = K.max_velocity; o->max_sliding_velocity = K.max_sliding_velocity;
+	o->rate_prop_shearstress = K.rate_prop; o->rate_indep_shearstress = K.rate_indep;
+	o->total_num_timesteps = K.steps;
+	// System::calcStress (Stress.cpp:342-384) from the per-component totals
+	std::vector<double> tot(NSC*6);
+	LFG_CUDA(cudaMemcpyAsync(tot.data(), S_.sc_tot, sizeof(double)*6*NSC, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	const DevParams &P = S_.P;
+	bool has[NSC] = {(bool)P.lub_on, (bool)P.lub_on, (bool)P.lub_on, (bool)P.lub_on,
+	                 P.lub_on && P.repulsiveforce, P.control == 0, P.control == 1, P.control == 1,
+	                 (bool)P.repulsiveforce};
+	const int group[NSC] = {2, 0, 1, 2, 3, 0, 0, 0, 3};
+	double g[4][6] = {{0}};
+	for (int c = 0; c < NSC; c++)
+		if (has[c]) for (int e = 0; e < 6; e++) g[group[c]][e] += tot[6*c+e];
+	double inv = 1.0/P.system_volume;
+	for (int a = 0; a < 4; a++) for (int e = 0; e < 6; e++) g[a][e] *= inv;
+	for (int e = 0; e < 6; e++) g[2][e] += 2*K.Einf[e]/(6*M_PI);
+	for (int e = 0; e < 6; e++) o->total_stress[e] = g[0][e]+g[1][e]+g[2][e]+g[3][e];
+	const double *E = K.Einf;
+	double EE = E[0]*E[0]+2*E[1]*E[1]+2*E[2]*E[2]+2*E[3]*E[3]+E[4]*E[4]+E[5]*E[5];
+	if (K.shear_rate != 0 && EE != 0) {
+		const double *s = o->total_stress;
+		double sE = s[0]*E[0]+2*s[1]*E[1]+2*s[2]*E[2]+2*s[3]*E[3]+s[4]*E[4]+s[5]*E[5];
+		o->viscosity = 0.5*sE/EE;
+		o->N1 = (s[0]-s[5])/K.shear_rate;
+		o->N2 = (s[5]-s[4])/K.shear_rate;
+	}
+	std::vector<DPair> pairs(S_.npairs);
+	if (S_.npairs) LFG_CUDA(cudaMemcpyAsync(pairs.data(), S_.pairs, sizeof(DPair)*S_.npairs, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	for (const DPair &q : pairs) {
+		if (!(q.flags & PF_INTER)) continue;
+		o->n_pairs++;
+		if (q.flags & PF_CONTACT) o->n_contacts++;
+		if (q.flags & PF_LUB) o->n_lub++;
+		bool res = P.lub_on ? ((q.flags & PF_DASHPOT) || (q.flags & PF_LUB)) : (q.flags & PF_DASHPOT);
+		if (res) o->n_resistance_pairs++;
+	}
+	o->n_superset_pairs = S_.npairs;
+	o->n_symbolic_runs = symbolic_runs_;
+	o->last_refine_iters = solver_->last_iters();
+	o->last_refine_residual = solver_->last_resid();
+}
+
+void Sim::particles(double *pos, double *vel, double *ang, double *na_vel, double *na_ang)
+{
+	int n = S_.n;
+	if (pos) LFG_CUDA(cudaMemcpyAsync(pos, S_.pos, sizeof(double)*3*n, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	if (vel) LFG_CUDA(cudaMemcpyAsync(vel, S_.vel, sizeof(double)*3*n, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	if (ang) LFG_CUDA(cudaMemcpyAsync(ang, S_.ang, sizeof(double)*3*n, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	if (na_vel || na_ang) {
+		std::vector<double> na(6*n);
+		LFG_CUDA(cudaMemcpyAsync(na.data(), S_.na, sizeof(double)*6*n, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+		for (int i = 0; i < n; i++)
+			for (int e = 0; e < 3; e++) {
+				if (na_vel) na_vel[3*i+e] = na[6*i+e];
+				if (na_ang) na_ang[3*i+e] = na[6*i+3+e];
+			}
+	}
+}
+
+int Sim::num_pairs()
+{
+	std::vector<DPair> pairs(S_.npairs);
+	if (S_.npairs) LFG_CUDA(cudaMemcpyAsync(pairs.data(), S_.pairs, sizeof(DPair)*S_.npairs, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	int c = 0;
+	for (const DPair &q : pairs) c += (q.flags & PF_INTER) ? 1 : 0;
+	return c;
+}
+
+int Sim::get_pairs(lfg_pair *out, int cap)
+{
+	std::vector<DPair> pairs(S_.npairs);
+	if (S_.npairs) LFG_CUDA(cudaMemcpyAsync(pairs.data(), S_.pairs, sizeof(DPair)*S_.npairs, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	int c = 0;
+	for (const DPair &q : pairs) {
+		if (!(q.flags & PF_INTER)) continue;
+		if (c < cap) {
+			lfg_pair &o = out[c];
+			std::memset(&o, 0, sizeof o);
+			o.p0 = q.p0; o.p1 = q.p1; o.z_offset = q.zoff;
+			o.contact_active = (q.flags & PF_CONTACT) ? 1 : 0;
+			o.state = q.state;
+			o.lub_active = (q.flags & PF_LUB) ? 1 : 0;
+			o.r = q.r; o.reduced_gap = q.gap;
+			for (int k = 0; k < 3; k++) {
+				o.nvec[k] = q.nvec[k]; o.rvec[k] = q.rvec[k]; o.disp_tan[k] = q.disp_tan[k];
+				o.f_spring_total[k] = q.fs_total[k]; o.rep_force[k] = q.rep_force[k];
+			}
+			o.lub_coeff = q.lub_coeff; o.log_lub_coeff = q.log_lub_coeff;
+		}
+		c++;
+	}
+	return c;
+}
+
+int Sim::particle_stress(int comp, double *out)
+{
+	static const int map[8] = {SC_GU_CONTACT, SC_GU_DASHPOT, SC_GU_HYDRO, SC_GU_REPULSION, SC_ME,
+	                           SC_XF_CONTACT, SC_XF_RATEINDEP, SC_XF_REPULSION};
+	if (comp < 0 || comp >= 8) return LFG_ERR_BAD_ARG;
+	int c = map[comp];
+	if (comp == 5 && S_.P.control == 1) c = SC_XF_RATEPROP;
+	LFG_CUDA(cudaMemcpyAsync(out, S_.sc+(size_t)c*6*S_.n, sizeof(double)*6*S_.n, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	return LFG_OK;
+}
+
+int Sim::velocity_component(int comp, double *out)
+{
+	if (comp < 0 || comp >= NFC) return LFG_ERR_BAD_ARG;
+	LFG_CUDA(cudaMemcpyAsync(out, S_.vc+(size_t)comp*6*S_.n, sizeof(double)*6*S_.n, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	return LFG_OK;
+}
+
+int Sim::set_contact(int p0, int p1, int state, const double *disp_tan)
+{
+	if (p0 > p1) std::swap(p0, p1);
+	std::vector<int> rp(S_.n+1);
+	LFG_CUDA(cudaMemcpyAsync(rp.data(), S_.row_ptr, sizeof(int)*(S_.n+1), cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	if (p0 < 0 || p1 >= S_.n) return LFG_ERR_BAD_ARG;
+	for (int t = rp[p0]; t < rp[p0+1]; t++) {
+		DPair q;
+		LFG_CUDA(cudaMemcpyAsync(&q, S_.pairs+t, sizeof q, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+		if (q.p1 != p1) continue;
+		for (int k = 0; k < 3; k++) q.disp_tan[k] = disp_tan[k];
+		if (state >= 0 && (q.flags & PF_CONTACT)) q.state = state;
+		LFG_CUDA(cudaMemcpyAsync(S_.pairs+t, &q, sizeof q, cudaMemcpyHostToDevice, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+		return LFG_OK;
+	}
+	return LFG_ERR_BAD_ARG;
+}
+
+void Sim::set_clock(double time, double strain, double dt, double rate, double maxv, double maxsv)
+{
+	first_time();
+	pull_clock();
+	DevClock K = *h_clock_;
+	K.time = time; K.strain = strain; K.dt = dt;
+	K.max_velocity = maxv; K.max_sliding_velocity = maxsv;
+	LFG_CUDA(cudaMemcpyAsync(S_.clock, &K, sizeof K, cudaMemcpyHostToDevice, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	phys_set_shear_rate(S_, rate, false, st_);
+	LFG_CUDA(cudaStreamSynchronize(st_));
+}
+
+void Sim::refresh()
+{
+	first_time();
+	pull_clock();
+	double msv = h_clock_->max_sliding_velocity;
+	phys_pairs_update(S_, 0, 1, true, st_);
+	pull_clock();
+	DevClock K = *h_clock_;
+	K.max_sliding_velocity = msv;
+	LFG_CUDA(cudaMemcpyAsync(S_.clock, &K, sizeof K, cudaMemcpyHostToDevice, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+}
+
+int Sim::assemble(double *dbl, int32_t *row, int32_t *col, double *odbl, int cap, int *nb_out)
+{
+	first_time();
+	phys_blocks(S_, solver_->d_dblocks(), solver_->d_odblocks(), st_);
+	LFG_CUDA(cudaStreamSynchronize(st_));
+	if (dbl) LFG_CUDA(cudaMemcpyAsync(dbl, solver_->d_dblocks(), sizeof(double)*15*S_.n, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	std::vector<DPair> pairs(S_.npairs);
+	std::vector<double> od(18*(size_t)S_.npairs);
+	if (S_.npairs) {
+		LFG_CUDA(cudaMemcpyAsync(pairs.data(), S_.pairs, sizeof(DPair)*S_.npairs, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+		LFG_CUDA(cudaMemcpyAsync(od.data(), solver_->d_odblocks(), sizeof(double)*18*S_.npairs, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	}
+	int c = 0;
+	const DevParams &P = S_.P;
+	for (int t = 0; t < S_.npairs; t++) {
+		const DPair &q = pairs[t];
+		if (!(q.flags & PF_INTER)) continue;
+		bool res = P.lub_on ? ((q.flags & PF_DASHPOT) || (q.flags & PF_LUB)) : (q.flags & PF_DASHPOT);
+		if (!res) continue;
+		if (c < cap) {
+			if (row) row[c] = q.p1;
+			if (col) col[c] = q.p0;
+			if (odbl) std::memcpy(odbl+18*(size_t)c, &od[18*(size_t)t], sizeof(double)*18);
+		}
+		c++;
+	}
+	if (nb_out) *nb_out = c;
+	return LFG_OK;
+}
+
+int Sim::force_component(int comp, double *out)
+{
+	if (comp < 0 || comp >= NFC) return LFG_ERR_BAD_ARG;
+	first_time();
+	phys_u_inf(S_, st_);
+	phys_force_components(S_, st_);
+	LFG_CUDA(cudaMemcpyAsync(out, S_.fc+(size_t)comp*6*S_.n, sizeof(double)*6*S_.n, cudaMemcpyDeviceToHost, st_));
+	LFG_CUDA(cudaStreamSynchronize(st_));
+	return LFG_OK;
+}
+
+void Sim::timing(lfg_sim_timing *o) const
+{
+	std::memset(o, 0, sizeof *o);
+	for (int k = 0; k < 8; k++) o->ms[k] = stage_ms_[k];
+	o->launches = last_launches_+2*(solver_->launches_factor()+solver_->launches_solve());
+	o->factor_flops = solver_->flops();
+	o->solve_bytes = 2.0*(double)solver_->nnz_L()*(opt_.precision == LFG_PREC_FP64 ? 8 : 4);
+}
+
+} // namespace lfg
+
+using namespace lfg;
+
+struct lfg_sim {
+	cudaStream_t stream = nullptr;
+	Sim *s = nullptr;
+	int device = 0;
+};
+
+#define SIM_GUARD_BEGIN try {
+#define SIM_GUARD_END                                                                   \
+	}                                                                                   \
+	catch (const lfg::Error &e) { return fail(st, e.code, e.info, e.msg.c_str()); }      \
+	catch (const std::bad_alloc &) { return fail(st, LFG_ERR_OOM, 0, "host allocation failed"); } \
+	catch (...) { return fail(st, LFG_ERR_CUDA, 0, "unexpected exception"); }
+
+static int sim_status(lfg_sim *h, lfg_status *st)
+{
+	if (h->s->error_code) {
+		int c = h->s->error_code;
+		int rc = fail(st, c, h->s->error_info, h->s->error_msg.c_str());
+		h->s->error_code = 0;
+		return rc;
+	}
+	return ok(st);
+}
+
+extern "C" {
+
+int lfg_sim_create(const lfg_params *p, const lfg_options *opt, int n, const double *pos, const double *radius,
+                   double lx, double ly, double lz, const double *le_disp, int ncs, const int32_t *cs_p0,
+                   const int32_t *cs_p1, const double *cs_disp_tan, lfg_sim **out, lfg_status *st)
+{
+	if (!p || !out || n <= 1 || !pos || !radius || lx <= 0 || lz <= 0 || ly < 0 || ncs < 0 ||
+	    (ncs > 0 && (!cs_p0 || !cs_p1 || !cs_disp_tan)))
+		return fail(st, LFG_ERR_BAD_ARG, 0, "bad arguments");
+	lfg_options o;
+	if (opt) o = *opt; else lfg_default_options(&o);
+	int rc = check_device(o.device, st);
+	if (rc) return rc;
+	lfg_sim *h = new (std::nothrow) lfg_sim();
+	if (!h) return fail(st, LFG_ERR_OOM, 0, "host allocation failed");
+	h->device = o.device;
+	try {
+		LFG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+		h->s = new Sim(*p, o, n, pos, radius, lx, ly, lz, le_disp, h->stream);
+		if (ncs) h->s->set_contacts(ncs, cs_p0, cs_p1, cs_disp_tan);   // System::setContacts
+		h->s->first_time();
+		*out = h;
+		return ok(st);
+	} catch (const lfg::Error &e) {
+		delete h->s;
+		if (h->stream) cudaStreamDestroy(h->stream);
+		delete h;
+		return fail(st, e.code, e.info, e.msg.c_str());
+	} catch (...) {
+		delete h->s;
+		if (h->stream) cudaStreamDestroy(h->stream);
+		delete h;
+		return fail(st, LFG_ERR_OOM, 0, "allocation failed");
+	}
+}
+
+int lfg_sim_advance(lfg_sim *h, double time_end, double strain_end, lfg_status *st)
+{
+	if (!h) return fail(st, LFG_ERR_BAD_ARG, 0, "null sim");
+	SIM_GUARD_BEGIN
+	cudaSetDevice(h->device);
+	h->s->advance(time_end, strain_end);
+	return sim_status(h, st);
+	SIM_GUARD_END
+}
+
+int lfg_sim_step(lfg_sim *h, int calc_stress, double time_end, double strain_end, lfg_status *st)
+{
+	if (!h) return fail(st, LFG_ERR_BAD_ARG, 0, "null sim");
+	SIM_GUARD_BEGIN
+	cudaSetDevice(h->device);
+	h->s->step(calc_stress, time_end, strain_end);
+	return sim_status(h, st);
+	SIM_GUARD_END
+}
+
+int lfg_sim_run(lfg_sim *h, int nsteps, double time_end, double strain_end, lfg_status *st)
+{
+	if (!h || nsteps < 0) return fail(st, LFG_ERR_BAD_ARG, 0, "bad arguments");
+	SIM_GUARD_BEGIN
+	cudaSetDevice(h->device);
+	for (int k = 0; k < nsteps; k++) {
+		h->s->step(0, time_end, strain_end);
+		if (h->s->error_code) break;
+	}
+	return sim_status(h, st);
+	SIM_GUARD_END
+}
+
+int lfg_sim_get_scalars(lfg_sim *h, lfg_sim_scalars *o)
+{
+	lfg_status *st = nullptr;
+	if (!h || !o) return LFG_ERR_BAD_ARG;
+	SIM_GUARD_BEGIN
+	h->s->scalars(o);
+	return LFG_OK;
+	SIM_GUARD_END
+}
+
+int lfg_sim_get_particles(lfg_sim *h, double *pos, double *vel, double *ang, double *na_vel, double *na_ang)
+{
+	lfg_status *st = nullptr;
+	if (!h) return LFG_ERR_BAD_ARG;
+	SIM_GUARD_BEGIN
+	h->s->particles(pos, vel, ang, na_vel, na_ang);
+	return LFG_OK;
+	SIM_GUARD_END
+}
+
+int lfg_sim_get_num_pairs(lfg_sim *h)
+{
+	if (!h) return -1;
+	try { return h->s->num_pairs(); } catch (...) { return -1; }
+}
+
+int lfg_sim_get_pairs(lfg_sim *h, lfg_pair *out, int cap)
+{
+	if (!h || (cap > 0 && !out)) return -1;
+	try { return h->s->get_pairs(out, cap); } catch (...) { return -1; }
+}
+
+int lfg_sim_get_particle_stress(lfg_sim *h, int comp, double *out)
+{
+	lfg_status *st = nullptr;
+	if (!h || !out) return LFG_ERR_BAD_ARG;
+	SIM_GUARD_BEGIN
+	return h->s->particle_stress(comp, out);
+	SIM_GUARD_END
+}
+
+int lfg_sim_get_velocity_component(lfg_sim *h, int comp, double *out)
+{
+	lfg_status *st = nullptr;
+	if (!h || !out) return LFG_ERR_BAD_ARG;
+	SIM_GUARD_BEGIN
+	return h->s->velocity_component(comp, out);
+	SIM_GUARD_END
+}
+
+int lfg_sim_set_contact(lfg_sim *h, int p0, int p1, int state, const double *disp_tan)
+{
+	lfg_status *st = nullptr;
+	if (!h || !disp_tan) return LFG_ERR_BAD_ARG;
+	SIM_GUARD_BEGIN
+	return h->s->set_contact(p0, p1, state, disp_tan);
+	SIM_GUARD_END
+}
+
+int lfg_sim_set_clock(lfg_sim *h, double time, double strain, double dt, double shear_rate, double maxv,
+                      double maxsv)
+{
+	lfg_status *st = nullptr;
+	if (!h) return LFG_ERR_BAD_ARG;
+	SIM_GUARD_BEGIN
+	h->s->set_clock(time, strain, dt, shear_rate, maxv, maxsv);
+	return LFG_OK;
+	SIM_GUARD_END
+}
+
+int lfg_sim_refresh(lfg_sim *h)
+{
+	lfg_status *st = nullptr;
+	if (!h) return LFG_ERR_BAD_ARG;
+	SIM_GUARD_BEGIN
+	h->s->refresh();
+	return LFG_OK;
+	SIM_GUARD_END
+}
+
+int lfg_sim_assemble(lfg_sim *h, double *dblocks, int32_t *od_row, int32_t *od_col, double *odblocks, int cap,
+                     int *nb_out)
+{
+	lfg_status *st = nullptr;
+	if (!h) return LFG_ERR_BAD_ARG;
+	SIM_GUARD_BEGIN
+	return h->s->assemble(dblocks, od_row, od_col, odblocks, cap, nb_out);
+	SIM_GUARD_END
+}
+
+int lfg_sim_force_component(lfg_sim *h, int comp, double *out)
+{
+	lfg_status *st = nullptr;
+	if (!h || !out) return LFG_ERR_BAD_ARG;
+	SIM_GUARD_BEGIN
+	return h->s->force_component(comp, out);
+	SIM_GUARD_END
+}
+
+int lfg_sim_get_timing(lfg_sim *h, lfg_sim_timing *o)
+{
+	if (!h || !o) return LFG_ERR_BAD_ARG;
+	h->s->timing(o);
+	return LFG_OK;
+}
+
+void lfg_sim_destroy(lfg_sim *h)
+{
+	if (!h) return;
+	cudaSetDevice(h->device);
+	delete h->s;
+	if (h->stream) cudaStreamDestroy(h->stream);
+	delete h;
+}
+
+} // extern "C"

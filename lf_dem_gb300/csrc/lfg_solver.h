@@ -33,6 +33,7 @@ public:
 	int launches_factor() const { return launches_factor_; }
 	int launches_solve() const { return launches_solve_; }
 	const lfg_options &options() const { return opt_; }
+	int *d_status() { return opt_.precision == LFG_PREC_FP64 ? F64_.status : F32_.status; }
 
 private:
 	struct GraphEntry {
