@@ -1,0 +1,331 @@
+#!/usr/bin/env python3
+"""Benchmark: particle-steps/s of LF_DEM's per-timestep hydrodynamic core on GB300.
+
+Workload (the metric's configuration): N = 4096 bidisperse spheres (radii 1 and
+1.4, equal volume shares), volume fraction 0.56, stress control sigma = 10
+critical-load units (friction_model 2), mu = 1, lubrication lambda = 1e-3,
+lub_max_gap 0.5, kn = 1e4, kt = 0.5 kn, seeded synthetic packing (there is no
+public dataset).  One step = one full predictor-corrector time step
+(2 assemblies, 2 factorisations, 2 x 4 right-hand-side solves, stresslets and
+shear-rate solve each half step).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+value        : particle-steps/s of the FP32 + FP64-refinement form, device time
+               (CUDA events on the engine's stream), state resident in HBM
+fp64_value   : the same for the plain FP64 form
+e2e          : through the C ABI with host buffers: create from host arrays
+               (H2D), K steps each followed by a D2H read of positions,
+               velocities and the stress tensor
+cpu_baseline : the CPU oracle (C restatement, OpenMP) on one step of the same
+               workload, on this machine's host cores
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+N_PART = 4096
+VF = 0.56
+SIGMA_CL = 10.0
+METRIC = "particle-steps/s at N=4096 phi=0.56, FP32+refine vs FP64 direct; p50/p99 latency"
+
+
+def workload_params():
+    return dict(kn=1e4, kt=5e3, mu_static=1.0, mu_dynamic=1.0, friction_model=2, critical_load=1.0,
+                repulsion_on=0, repulsion=0.0, repulsive_length=0.05, repulsive_max_length=-1.0,
+                lubrication_model=2, lub_reduce_parameter=1e-3, lub_max_gap=0.5, interaction_range=-1.0,
+                sd_coeff=1.0, contact_relaxation_time=1e-3, contact_relaxation_time_tan=-1.0, disp_max=1e-3,
+                dt=1e-4, dt_max=-1.0, dt_min=-1.0, fixed_dt=0, integration_method=1, control=1,
+                shear_rate=0.0, target_stress=SIGMA_CL / 6 / np.pi, Ehat=(0, 0, 0.5, 0, 0, 0),
+                Ohat=(0, 0.5, 0), init_strain_shear_rate_limit=0.0, init_shear_rate_limit=999.0, ft_max=0.0)
+
+
+def config(world):
+    return {"workload": f"3D stress-controlled critical-load model: N={N_PART} bidisperse 1:1.4, phi={VF}, "
+                        f"sigma={SIGMA_CL:g}cl, mu=1, lambda=1e-3, kn=1e4, predictor-corrector",
+            "n_particles": N_PART, "volume_fraction": VF, "control": "stress 10cl",
+            "parallelism": f"replicas x{world}" if world > 1 else "single suspension",
+            "l2": "inputs larger than L2 (fronts 0.8-1.7 GB per factorisation)"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), d.get("bf16_tflops_sustained", 1700.0), \
+            "measured"
+    except (OSError, ValueError):
+        return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+def run_engine(E, packing, precision, steps, warmup, device):
+    params = workload_params()
+    g = E.Sim(params, packing.position, packing.radius, packing.lx, packing.ly, packing.lz,
+              precision=precision, device=device)
+    g.run(warmup)
+    g.clear_step_times()
+    g.run(steps)
+    ms, kernels = g.step_times()
+    timing = g.timing()
+    sc = g.scalars()
+    g.close()
+    return ms, kernels, timing, sc
+
+
+def run_e2e(E, packing, precision, steps, device):
+    """Create from host arrays, K steps, each followed by a D2H read of the state."""
+    import ctypes as C
+    params = workload_params()
+    pos = np.ascontiguousarray(packing.position)
+    rad = np.ascontiguousarray(packing.radius)
+    t0 = time.perf_counter()
+    g = E.Sim(params, pos, rad, packing.lx, packing.ly, packing.lz, precision=precision, device=device)
+    L = E.load()
+    outp = np.zeros(3 * len(rad))
+    outv = np.zeros(3 * len(rad))
+    for _ in range(steps):
+        g.step()
+        L.lfg_sim_get_particles(g.h, outp.ctypes.data_as(C.c_void_p), outv.ctypes.data_as(C.c_void_p),
+                                None, None, None)
+        g.scalars()
+    t1 = time.perf_counter()
+    g.close()
+    n = len(rad)
+    return {"value": n * steps / (t1 - t0), "unit": "particle-steps/s",
+            "h2d_bytes_per_step": int((pos.nbytes + rad.nbytes) / steps),
+            "d2h_bytes_per_step": int(outp.nbytes + outv.nbytes + 8 * 6),
+            "note": "includes creation (H2D of the configuration, symbolic analysis, graph capture)"}
+
+
+def cpu_baseline(packing, nsteps=1):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build()
+    o = pyoracle.OracleSim(workload_params(), packing.position, packing.radius, packing.lx, packing.ly,
+                           packing.lz)
+    o.first_time()
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        o.step()
+    t1 = time.perf_counter()
+    return {"value": N_PART * nsteps / (t1 - t0), "unit": "particle-steps/s", "cores": pyoracle.num_threads(),
+            "kind": "port",
+            "sample": f"{nsteps} predictor-corrector step(s) of the N={N_PART} workload, "
+                      f"FP64 block Cholesky (minimum degree) with OpenMP, {t1 - t0:.1f} s"}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return world, rank, local, dist, torch
+    return world, rank, local, None, None
+
+
+def reference_arm(args):
+    world, rank, local, dist, torch = dist_setup()
+    if rank != 0:
+        return
+    from lf_dem_gb300 import packing as PK
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build()
+    p = PK.generate(N_PART, VF, seed=2000)
+    o = pyoracle.OracleSim(workload_params(), p.position, p.radius, p.lx, p.ly, p.lz)
+    o.first_time()
+    for _ in range(args.warmup):
+        o.step()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.step()
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    val = N_PART * args.steps / tot
+    line = {"metric": METRIC, "value": val, "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": config(1),
+            "p50_ms": 1e3 * float(np.percentile(times, 50)), "p99_ms": 1e3 * float(np.percentile(times, 99)),
+            "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": pyoracle.num_threads(),
+                             "kind": "port",
+                             "sample": f"{args.steps} full steps of the N={N_PART} workload on the CPU oracle "
+                                       "(C restatement of LF_DEM's step; reference C++ + CHOLMOD cannot be "
+                                       "built on this host)"},
+            "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 form")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling driver: FP32 form only, W + K steps, no measurement (for ncu)")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"], help="form used by --profile")
+    args = ap.parse_args()
+    if args.profile:
+        import lf_dem_gb300 as E
+        from lf_dem_gb300 import packing as PK
+        E.load()
+        pk = PK.generate(N_PART, VF, seed=2000)
+        prec = E.PREC_FP32_REFINE if args.precision == "fp32" else E.PREC_FP64
+        g = E.Sim(workload_params(), pk.position, pk.radius, pk.lx, pk.ly, pk.lz, precision=prec)
+        g.run(args.warmup)
+        g.run(args.steps)
+        ms, kern = g.step_times()
+        print(json.dumps({"profile_steps_ms": [float(x) for x in ms], "kernels": kern}))
+        return
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    world, rank, local, dist, torch = dist_setup()
+    import lf_dem_gb300 as E
+    from lf_dem_gb300 import build as B
+    from lf_dem_gb300 import packing as PK
+    if rank == 0 or world == 1:
+        B.build()
+    if dist is not None:
+        dist.barrier()
+    E.load()
+    rc, name, cc, nsm = E.device_info(local)
+    if rc != E.LFG_OK:
+        raise SystemExit(f"no sm_103 device (rank {rank}): {name} {cc}")
+    pk = PK.generate(N_PART, VF, seed=2000 + rank)
+    sampler = ClockSampler(local)
+    if dist is not None:
+        dist.barrier()
+    sampler.start()
+    ms32, kern32, tim32, sc32 = run_engine(E, pk, E.PREC_FP32_REFINE, args.steps, args.warmup, local)
+    clocks = sampler.stop()
+    total32 = float(np.sum(ms32)) / 1e3
+    if dist is not None:
+        t = torch.tensor([total32], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total32 = float(t.item())
+    value = N_PART * args.steps * world / total32
+    res = {}
+    if not args.no_fp64:
+        ms64, kern64, tim64, sc64 = run_engine(E, pk, E.PREC_FP64, max(3, args.steps // 2), args.warmup, local)
+        res["fp64_value"] = N_PART * len(ms64) * world / (float(np.sum(ms64)) / 1e3)
+        res["fp64_ms_per_step"] = float(np.mean(ms64))
+        res["fp64_p50_ms"] = float(np.percentile(ms64, 50))
+        res["fp64_p99_ms"] = float(np.percentile(ms64, 99))
+        res["fp64_stage_ms"] = dict(zip(["pairs", "assembly", "factor", "solve", "forces_stress", "move"],
+                                        tim64["ms"][:6]))
+    if rank != 0:
+        return
+    hbm, bf16, bf16s, src = measured_peaks()
+    # dominant kernel: the multifrontal factorisation (its launch sequence is a
+    # CUDA graph); algorithmic flops per factorisation / its device time
+    stage = dict(zip(["pairs", "assembly", "factor", "solve", "forces_stress", "move"], tim32["ms"][:6]))
+    fact_ms = stage["factor"] / 2.0   # two factorisations per step
+    achieved = tim32["factor_flops"] / (fact_ms * 1e-3) / 1e12 if fact_ms > 0 else 0.0
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            traffic = json.load(f).get("factor_fp32_bytes_per_factorisation")
+    except (OSError, ValueError):
+        pass
+    roof = {"bound": "tensor", "achieved": achieved, "peak": bf16s, "unit": "TFLOP/s",
+            "frac": achieved / bf16s, "traffic": traffic,
+            "kernel": "FP32 multifrontal factorisation (k_assemble/k_panel/k_update graph)",
+            "peak_source": f"bf16_tflops_sustained ({src}); the factorisation runs on FP32 CUDA cores"}
+    solve_ms = stage["solve"]
+    line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": float(np.mean(ms32)), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64refine", "data": "synthetic",
+            "config": config(world), "p50_ms": float(np.percentile(ms32, 50)),
+            "p99_ms": float(np.percentile(ms32, 99)), "stage_ms": stage, "gpu_launches": int(kern32),
+            "refine_iters": sc32["last_refine_iters"], "refine_residual": sc32["last_refine_residual"],
+            "symbolic_runs": sc32["n_symbolic_runs"], "roofline": roof, "clocks": clocks,
+            "device": name}
+    line.update(res)
+    iters = max(1, int(sc32["last_refine_iters"]))
+    solve_bytes_step = 2 * iters * tim32["solve_bytes"]   # predictor + corrector, one factor sweep per iteration
+    line["roofline_solve"] = {"bound": "hbm", "achieved": solve_bytes_step / max(solve_ms * 1e-3, 1e-12) / 1e9,
+                              "peak": hbm, "unit": "GB/s",
+                              "frac": solve_bytes_step / max(solve_ms * 1e-3, 1e-12) / 1e9 / hbm,
+                              "note": "factor bytes read by the triangular solves of one step / solve time"}
+    line["e2e"] = run_e2e(E, pk, E.PREC_FP32_REFINE, args.steps, local)
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(pk, 1)
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -97,7 +97,7 @@ typedef struct {
 	int device;             /* CUDA device ordinal */
 	double refine_tol;      /* relative residual target of the FP32 form (default 1e-12) */
 	int refine_max_iter;    /* default 30 */
-	double skin;            /* pair superset skin, units of (a_i+a_j)/2 (default 0.4) */
+	double skin;            /* pair superset skin, units of (a_i+a_j)/2 (default 0.15) */
 	int use_graphs;         /* capture factor/solve launch sequences in CUDA graphs (default 1) */
 	int leaf_size;          /* nested-dissection leaf size in particles (default 16) */
 	int pad_;
@@ -241,6 +241,12 @@ typedef struct {
 	double solve_bytes;      /* algorithmic bytes of one forward+backward solve, 1 RHS */
 } lfg_sim_timing;
 int lfg_sim_get_timing(lfg_sim *s, lfg_sim_timing *out);
+
+/* Device duration (ms, CUDA events on the simulation's stream) of every step
+ * since the last lfg_sim_clear_step_times; returns the number recorded and
+ * copies up to cap of them.  Also the number of kernels launched in them. */
+int lfg_sim_get_step_times(lfg_sim *s, double *ms, int cap, int64_t *kernels);
+void lfg_sim_clear_step_times(lfg_sim *s);
 
 void lfg_sim_destroy(lfg_sim *s);
 

@@ -101,7 +101,8 @@ EXPORTS = [
     "lfg_sim_create", "lfg_sim_advance", "lfg_sim_step", "lfg_sim_run", "lfg_sim_get_scalars",
     "lfg_sim_get_particles", "lfg_sim_get_num_pairs", "lfg_sim_get_pairs", "lfg_sim_get_particle_stress",
     "lfg_sim_get_velocity_component", "lfg_sim_set_contact", "lfg_sim_set_clock", "lfg_sim_refresh",
-    "lfg_sim_assemble", "lfg_sim_force_component", "lfg_sim_get_timing", "lfg_sim_destroy",
+    "lfg_sim_assemble", "lfg_sim_force_component", "lfg_sim_get_timing", "lfg_sim_get_step_times",
+    "lfg_sim_clear_step_times", "lfg_sim_destroy",
 ]
 
 _lib = None
@@ -156,6 +157,9 @@ def load(path: str | None = None):
         L.lfg_sim_assemble.argtypes = [vp, vp, vp, vp, vp, C.c_int, C.POINTER(C.c_int)]
         L.lfg_sim_force_component.argtypes = [vp, C.c_int, vp]
         L.lfg_sim_get_timing.argtypes = [vp, C.POINTER(SimTiming)]
+        L.lfg_sim_get_step_times.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_int64)]
+        L.lfg_sim_clear_step_times.argtypes = [vp]
+        L.lfg_sim_clear_step_times.restype = None
         L.lfg_sim_destroy.argtypes = [vp]
         L.lfg_sim_destroy.restype = None
     _lib = L
@@ -377,6 +381,17 @@ class Sim:
         out = np.zeros(6 * self.n)
         rc = load().lfg_sim_force_component(self.h, comp, _ptr(out))
         return None if rc else out.reshape(-1, 6)
+
+    def step_times(self):
+        L = load()
+        kern = C.c_int64()
+        n = L.lfg_sim_get_step_times(self.h, None, 0, C.byref(kern))
+        buf = np.zeros(max(n, 1))
+        L.lfg_sim_get_step_times(self.h, _ptr(buf), n, C.byref(kern))
+        return buf[:n].copy(), kern.value
+
+    def clear_step_times(self):
+        load().lfg_sim_clear_step_times(self.h)
 
     def timing(self) -> dict:
         t = SimTiming()

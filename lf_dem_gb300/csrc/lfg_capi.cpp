@@ -68,7 +68,7 @@ void lfg_default_options(lfg_options *o)
 	o->device = 0;
 	o->refine_tol = 1e-12;
 	o->refine_max_iter = 30;
-	o->skin = 0.4;
+	o->skin = 0.15;
 	o->use_graphs = 1;
 	o->leaf_size = 16;
 }

@@ -42,6 +42,8 @@ public:
 	int assemble(double *dbl, int32_t *row, int32_t *col, double *odbl, int cap, int *nb_out);
 	int force_component(int comp, double *out);
 	void timing(lfg_sim_timing *o) const;
+	std::vector<double> step_ms;
+	int64_t step_kernels = 0;
 	int error_code = 0, error_info = 0;
 	std::string error_msg;
 
@@ -71,6 +73,7 @@ private:
 	double stage_ms_[8] = {0};
 	int64_t launches_mark_ = 0;
 	int64_t last_launches_ = 0;
+	cudaEvent_t step_a_ = nullptr, step_b_ = nullptr;
 };
 
 static DevParams make_dev_params(const lfg_params &p, int n, double lx, double ly, double lz, double skin)
@@ -194,6 +197,8 @@ Sim::~Sim()
 	if (h_clock_) cudaFreeHost(h_clock_);
 	if (h_err_) cudaFreeHost(h_err_);
 	for (auto &e : evs_) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
+	if (step_a_) cudaEventDestroy(step_a_);
+	if (step_b_) cudaEventDestroy(step_b_);
 }
 
 // Build the pair superset at the current positions, carry the pair state of
@@ -333,7 +338,12 @@ void Sim::step(int calc_stress, double time_end, double strain_end)
 {
 	first_time();
 	ev_used_ = 0;
-	int64_t l0 = S_.launches;
+	int64_t l0 = S_.launches, k0 = solver_->kernels_launched();
+	if (!step_a_) {
+		LFG_CUDA(cudaEventCreate(&step_a_));
+		LFG_CUDA(cudaEventCreate(&step_b_));
+	}
+	LFG_CUDA(cudaEventRecord(step_a_, st_));
 	if (!prm_.fixed_dt) phys_adapt_dt(S_, time_end, strain_end, st_);
 	if (prm_.integration_method == 0) {
 		// System::timeEvolutionEulersMethod + timeStepMove (System.cpp:843-882, 1083-1122)
@@ -376,8 +386,15 @@ void Sim::step(int calc_stress, double time_end, double strain_end)
 	phys_pairs_update(S_, 1, 0, false, st_);
 	stage_end(0);
 	LFG_CUDA(cudaMemcpyAsync(h_err_, d_err_, sizeof(int), cudaMemcpyDeviceToHost, st_));
+	LFG_CUDA(cudaEventRecord(step_b_, st_));
 	pull_clock();
-	last_launches_ = S_.launches-l0;
+	last_launches_ = S_.launches-l0+(solver_->kernels_launched()-k0);
+	{
+		float ms = 0;
+		cudaEventElapsedTime(&ms, step_a_, step_b_);
+		step_ms.push_back(ms);
+		step_kernels += last_launches_;
+	}
 	for (int k = 0; k < 8; k++) stage_ms_[k] = 0;
 	for (size_t e = 0; e < ev_used_; e++) {
 		float ms = 0;
@@ -621,7 +638,7 @@ void Sim::timing(lfg_sim_timing *o) const
 {
 	std::memset(o, 0, sizeof *o);
 	for (int k = 0; k < 8; k++) o->ms[k] = stage_ms_[k];
-	o->launches = last_launches_+2*(solver_->launches_factor()+solver_->launches_solve());
+	o->launches = last_launches_;
 	o->factor_flops = solver_->flops();
 	o->solve_bytes = 2.0*(double)solver_->nnz_L()*(opt_.precision == LFG_PREC_FP64 ? 8 : 4);
 }
@@ -827,6 +844,22 @@ int lfg_sim_get_timing(lfg_sim *h, lfg_sim_timing *o)
 	if (!h || !o) return LFG_ERR_BAD_ARG;
 	h->s->timing(o);
 	return LFG_OK;
+}
+
+int lfg_sim_get_step_times(lfg_sim *h, double *ms, int cap, int64_t *kernels)
+{
+	if (!h) return -1;
+	int n = (int)h->s->step_ms.size();
+	for (int k = 0; k < n && k < cap && ms; k++) ms[k] = h->s->step_ms[k];
+	if (kernels) *kernels = h->s->step_kernels;
+	return n;
+}
+
+void lfg_sim_clear_step_times(lfg_sim *h)
+{
+	if (!h) return;
+	h->s->step_ms.clear();
+	h->s->step_kernels = 0;
 }
 
 void lfg_sim_destroy(lfg_sim *h)

@@ -113,10 +113,15 @@ void Solver::factorize_async()
 
 void Solver::run_graph(int kind, int k, const void *b, const void *x, const std::function<void()> &body)
 {
-	if (!opt_.use_graphs) { body(); return; }
+	if (!opt_.use_graphs) {
+		body();
+		kernels_ += kind == 0 ? launches_factor_ : launches_solve_+(kind == 2 ? 3 : 0);
+		return;
+	}
 	for (auto &g : graphs_) {
 		if (g.kind == kind && g.k == k && g.b == b && g.x == x) {
 			LFG_CUDA(cudaGraphLaunch(g.exec, st_));
+			kernels_ += g.nodes;
 			return;
 		}
 	}
@@ -131,10 +136,14 @@ void Solver::run_graph(int kind, int k, const void *b, const void *x, const std:
 	LFG_CUDA(cudaStreamEndCapture(st_, &graph));
 	GraphEntry e;
 	e.kind = kind; e.k = k; e.b = b; e.x = x;
+	size_t nn = 0;
+	LFG_CUDA(cudaGraphGetNodes(graph, nullptr, &nn));
+	e.nodes = (int64_t)nn;
 	LFG_CUDA(cudaGraphInstantiate(&e.exec, graph, 0));
 	cudaGraphDestroy(graph);
 	graphs_.push_back(e);
 	LFG_CUDA(cudaGraphLaunch(e.exec, st_));
+	kernels_ += e.nodes;
 }
 
 int Solver::check_factor(lfg_status *st)

@@ -32,6 +32,7 @@ public:
 	int64_t nnz_L() const { return S_.nnz_L; }
 	int launches_factor() const { return launches_factor_; }
 	int launches_solve() const { return launches_solve_; }
+	int64_t kernels_launched() const { return kernels_; }
 	const lfg_options &options() const { return opt_; }
 	int *d_status() { return opt_.precision == LFG_PREC_FP64 ? F64_.status : F32_.status; }
 
@@ -41,6 +42,7 @@ private:
 		const void *b = nullptr;
 		const void *x = nullptr;
 		cudaGraphExec_t exec = nullptr;
+		int64_t nodes = 0;
 	};
 	void run_graph(int kind, int k, const void *b, const void *x, const std::function<void()> &body);
 	void ensure_refine_ws(int k);
@@ -65,6 +67,7 @@ private:
 	int last_iters_ = 0;
 	double last_resid_ = 0;
 	int launches_factor_ = 0, launches_solve_ = 0;
+	int64_t kernels_ = 0;
 };
 
 } // namespace lfg

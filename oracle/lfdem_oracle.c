@@ -12,6 +12,18 @@
 #include <string.h>
 #include <stdint.h>
 #include "lfdem_oracle.h"
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+int lfo_num_threads(void)
+{
+#ifdef _OPENMP
+	return omp_get_max_threads();
+#else
+	return 1;
+#endif
+}
 
 #ifndef M_PI
 #define M_PI 3.14159265358979323846
@@ -1139,7 +1151,10 @@ static int bfact_factorize(bfact *f, const double *diag36, int nb, const int *ro
 				}
 			}
 		}
-		/* trailing update: A(r1,r2) -= L_r1k L_r2k^T for r1 >= r2 */
+		/* trailing update: A(r1,r2) -= L_r1k L_r2k^T for r1 >= r2; each t2
+		 * writes only column r2, so the loop runs in parallel */
+		int bad = 0;
+#pragma omp parallel for schedule(dynamic, 4) if (b-a > 16) reduction(|:bad)
 		for (int t2 = a; t2 < b; t2++) {
 			int r2 = f->rowidx[t2];
 			const double *L2 = &f->Lblk[(size_t)t2*36];
@@ -1155,7 +1170,7 @@ static int bfact_factorize(bfact *f, const double *diag36, int nb, const int *ro
 			for (int t1 = t2+1; t1 < b; t1++) {
 				int r1 = f->rowidx[t1];
 				while (p < pe && f->rowidx[p] < r1) p++;
-				if (p >= pe || f->rowidx[p] != r1) return -3;
+				if (p >= pe || f->rowidx[p] != r1) { bad = 1; break; }
 				double *T = &f->Lblk[(size_t)p*36];
 				const double *L1 = &f->Lblk[(size_t)t1*36];
 				for (int i = 0; i < 6; i++) for (int j = 0; j < 6; j++) {
@@ -1165,6 +1180,7 @@ static int bfact_factorize(bfact *f, const double *diag36, int nb, const int *ro
 				}
 			}
 		}
+		if (bad) return -3;
 	}
 	return 0;
 }

@@ -166,6 +166,9 @@ int lfo_force_component(lfo_sim *s, int comp, double *out);
 int lfo_bsr_solve(int nblk, const double *diag36, int nb, const int *row, const int *col,
                   const double *off36, int k, const double *b, double *x);
 
+/* Number of host threads the oracle's factorisation uses (OpenMP). */
+int lfo_num_threads(void);
+
 /* Block (compact -> dense 6x6 row-major) reconstructions of
  * StokesSolver.cpp:154-231 (rows of the lower block, columns of the column
  * particle). */

@@ -101,6 +101,7 @@ def lib():
         L.lfo_set_clock.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double,
                                     C.c_double, C.c_double, C.c_int]
         L.lfo_refresh.argtypes = [C.c_void_p]
+        L.lfo_num_threads.restype = C.c_int
         L.lfo_dblock_to_dense.argtypes = [dp, dp]
         L.lfo_odblock_to_dense.argtypes = [dp, dp]
         _lib = L
@@ -240,6 +241,10 @@ class OracleSim:
 
     def refresh(self):
         lib().lfo_refresh(self.h)
+
+
+def num_threads() -> int:
+    return lib().lfo_num_threads()
 
 
 def dblock_dense(d15):

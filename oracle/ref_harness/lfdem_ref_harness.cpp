@@ -41,6 +41,8 @@
 #include <vector>
 #include <csignal>
 #include <getopt.h>
+#include <unistd.h>
+#include <climits>
 #define private public
 #define protected public
 #include "Simulation.h"
@@ -172,12 +174,16 @@ int main(int argc, char **argv)
 		fprintf(stderr, "usage: %s CONF PARAMS r|s VALUE SUFFIX NSTEPS OUTDIR [CALC_STRESS] [STAGE]\n", argv[0]);
 		return 2;
 	}
-	std::string conf = argv[1], params = argv[2];
+	char buf[4096];
+	std::string conf = realpath(argv[1], buf) ? std::string(buf) : std::string(argv[1]);
+	std::string params = realpath(argv[2], buf) ? std::string(buf) : std::string(argv[2]);
 	bool stress = argv[3][0] == 's';
 	double value = atof(argv[4]);
 	std::string suffix = argv[5];
 	int nsteps = atoi(argv[6]);
-	std::string outdir = argv[7];
+	std::string outdir = realpath(argv[7], buf) ? std::string(buf) : std::string(argv[7]);
+	// the reference opens its output files in the working directory
+	if (chdir(outdir.c_str()) != 0) { perror("chdir"); return 2; }
 	int calc_stress = argc > 8 ? atoi(argv[8]) : 0;
 	int stage = argc > 9 ? atoi(argv[9]) : 1;
 
