@@ -28,11 +28,11 @@
 
 namespace lfg {
 
-enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4 };
+enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLAN_SYRK = 5 };
 
 template <typename T> struct Cfg;
 template <> struct Cfg<double> { static constexpr int NB = 32, TILE = 64, TPT = 4; };
-template <> struct Cfg<float>  { static constexpr int NB = 32, TILE = 128, TPT = 8; };
+template <> struct Cfg<float>  { static constexpr int NB = 64, TILE = 128, TPT = 8; };
 
 // ---------------------------------------------------------------------------
 // compact blocks -> dense (StokesSolver.cpp:154-231), m[r*6+c]
@@ -137,9 +137,14 @@ __global__ void k_scatter_od(int count, const int *__restrict__ list, const doub
 // one warp; rows owned by lanes i = lane + 32q.  Non-positive pivots are
 // replaced by 1 and reported through *fail (first column, global index + 1).
 // ---------------------------------------------------------------------------
+// row stride of the shared diagonal block: NB + 1 keeps the lanes (rows) of a
+// warp on distinct banks
+template <int NB> struct LdK { static constexpr int v = NB+1; };
+
 template <typename T, int NB>
 __device__ void warp_potrf(T *A, int w, int gcol0, int *fail)
 {
+	constexpr int LK = LdK<NB>::v;
 	int lane = threadIdx.x & 31;
 	for (int j = 0; j < w; j++) {
 		// s_i = A[i][j] - sum_{t<j} L[i][t] L[j][t] for i >= j
@@ -149,8 +154,8 @@ __device__ void warp_potrf(T *A, int w, int gcol0, int *fail)
 			int i = lane+32*q;
 			T s = 0;
 			if (i >= j && i < w) {
-				s = A[i*NB+j];
-				for (int t = 0; t < j; t++) s -= A[i*NB+t]*A[j*NB+t];
+				s = A[i*LK+j];
+				for (int t = 0; t < j; t++) s -= A[i*LK+t]*A[j*LK+t];
 			}
 			sv[q] = s;
 		}
@@ -164,8 +169,8 @@ __device__ void warp_potrf(T *A, int w, int gcol0, int *fail)
 #pragma unroll
 		for (int q = 0; q < (NB+31)/32; q++) {
 			int i = lane+32*q;
-			if (i == j) A[i*NB+j] = d;
-			else if (i > j && i < w) A[i*NB+j] = sv[q]/d;
+			if (i == j) A[i*LK+j] = d;
+			else if (i > j && i < w) A[i*LK+j] = sv[q]/d;
 		}
 		__syncwarp();
 	}
@@ -178,16 +183,16 @@ __global__ void __launch_bounds__(128) k_panel(const int4 *__restrict__ tasks, c
                                                const int64_t *__restrict__ sn_off, T *__restrict__ arena,
                                                int *fail)
 {
-	constexpr int NB = Cfg<T>::NB;
-	__shared__ T Lkk[NB*NB];
+	constexpr int NB = Cfg<T>::NB, LK = LdK<NB>::v;
+	__shared__ T Lkk[NB*LK];
 	int4 tk = tasks[blockIdx.x];
 	int s = tk.x, row0 = tk.y, k = tk.z, nrows = tk.w;
 	int n6 = 6*sn_n[s], ld = sn_ld[s];
 	int c0 = k*NB, w = min(NB, n6-c0);
 	T *base = arena+sn_off[s];
 	for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
-		int i = e/NB, j = e%NB;
-		Lkk[e] = (i < w && j <= i) ? base[(int64_t)(c0+j)*ld+c0+i] : T(0);
+		int i = e%NB, j = e/NB;   // consecutive threads read consecutive rows
+		Lkk[i*LK+j] = (i < w && j <= i) ? base[(int64_t)(c0+j)*ld+c0+i] : T(0);
 	}
 	__syncthreads();
 	if (threadIdx.x < 32) warp_potrf<T, NB>(Lkk, w, 6*sn_first[s]+c0, nullptr);
@@ -203,8 +208,8 @@ __global__ void __launch_bounds__(128) k_panel(const int4 *__restrict__ tasks, c
 			if (j < w) {
 				T v = x[j];
 #pragma unroll
-				for (int t = 0; t < NB; t++) if (t < j) v -= x[t]*Lkk[j*NB+t];
-				x[j] = v/Lkk[j*NB+j];
+				for (int t = 0; t < NB; t++) if (t < j) v -= x[t]*Lkk[j*LK+t];
+				x[j] = v/Lkk[j*LK+j];
 			}
 		}
 #pragma unroll
@@ -215,38 +220,41 @@ __global__ void __launch_bounds__(128) k_panel(const int4 *__restrict__ tasks, c
 // trailing update: CTA = one tile (sn, r0, c0, k); c0 == -1 writes the
 // factored diagonal block of panel k
 template <typename T>
-__global__ void __launch_bounds__(256) k_update(const int4 *__restrict__ tasks, const int *__restrict__ sn_first,
+__global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ tasks, const int *__restrict__ sn_first,
                                                 const int *__restrict__ sn_n, const int *__restrict__ sn_m,
                                                 const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
                                                 T *__restrict__ arena, int *fail)
 {
-	constexpr int NB = Cfg<T>::NB, TL = Cfg<T>::TILE, TPT = Cfg<T>::TPT;
+	constexpr int NB = Cfg<T>::NB, TL = Cfg<T>::TILE, TPT = Cfg<T>::TPT, LK = LdK<NB>::v;
 	constexpr int TD = TL/TPT; // threads per dimension (16)
-	__shared__ T As[NB][TL];
-	__shared__ T Bs[NB][TL];
+	extern __shared__ unsigned char smem_upd[];
+	T (*As)[TL] = reinterpret_cast<T (*)[TL]>(smem_upd);
+	T (*Bs)[TL] = reinterpret_cast<T (*)[TL]>(smem_upd+sizeof(T)*NB*TL);
 	int4 tk = tasks[blockIdx.x];
 	int s = tk.x, r0 = tk.y, cc0 = tk.z, k = tk.w;
 	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
 	int p0 = k*NB, w = min(NB, n6-p0), t0 = p0+w;
 	T *base = arena+sn_off[s];
 	if (cc0 < 0) {
-		T *Lkk = &As[0][0];  // NB*NB <= NB*TL
+		T *Lkk = &As[0][0];  // NB*(NB+1) <= 2*NB*TL (dynamic shared memory)
+		for (int e = threadIdx.x; e < NB*LK; e += blockDim.x) Lkk[e] = T(0);
+		__syncthreads();
 		for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
-			int i = e/NB, j = e%NB;
-			Lkk[e] = (i < w && j <= i) ? base[(int64_t)(p0+j)*ld+p0+i] : T(0);
+			int i = e%NB, j = e/NB;
+			Lkk[i*LK+j] = (i < w && j <= i) ? base[(int64_t)(p0+j)*ld+p0+i] : T(0);
 		}
 		__syncthreads();
 		if (threadIdx.x < 32) warp_potrf<T, NB>(Lkk, w, 6*sn_first[s]+p0, fail);
 		__syncthreads();
 		for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
-			int i = e/NB, j = e%NB;
-			if (i < w && j <= i) base[(int64_t)(p0+j)*ld+p0+i] = Lkk[e];
+			int i = e%NB, j = e/NB;
+			if (i < w && j <= i) base[(int64_t)(p0+j)*ld+p0+i] = Lkk[i*LK+j];
 		}
 		return;
 	}
 	bool extra = r0 >= F6;
 	int rlim = extra ? F6+t0 : F6;
-	int clim = extra ? n6 : F6;
+	int clim = n6;   // own columns only; the update matrix is k_syrk's
 	// load panel rows of the tile rows and tile columns
 	for (int e = threadIdx.x; e < NB*TL; e += blockDim.x) {
 		int t = e/TL, i = e%TL;
@@ -286,10 +294,94 @@ __global__ void __launch_bounds__(256) k_update(const int4 *__restrict__ tasks, 
 	}
 }
 
+
+// Schur complement of a supernode: U[r][c] -= sum_{t < 6n} L[r][t] L[c][t]
+// for 6n <= c <= r < 6F (tile (r0, c0) per CTA).  Deep-K loop over the
+// supernode's columns in chunks of KC, next chunk prefetched into registers
+// while the current one is multiplied from shared memory.
+template <typename T>
+__global__ void __launch_bounds__(256) k_syrk(const int4 *__restrict__ tasks, const int *__restrict__ sn_n,
+                                              const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
+                                              const int64_t *__restrict__ sn_off, T *__restrict__ arena)
+{
+	constexpr int TL = Cfg<T>::TILE, TPT = Cfg<T>::TPT, TD = TL/TPT;
+	constexpr int KC = 16;
+	constexpr int PER = KC*TL/256;   // elements of A (and of B) each thread loads per chunk
+	__shared__ T As[KC][TL];
+	__shared__ T Bs[KC][TL];
+	int4 tk = tasks[blockIdx.x];
+	int s = tk.x, r0 = tk.y, c0 = tk.z;
+	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
+	T *base = arena+sn_off[s];
+	int tx = threadIdx.x%TD, ty = threadIdx.x/TD;
+	T acc[TPT][TPT];
+#pragma unroll
+	for (int a = 0; a < TPT; a++)
+#pragma unroll
+		for (int b = 0; b < TPT; b++) acc[a][b] = 0;
+	T pa[PER], pb[PER];
+	auto load = [&](int t0) {
+#pragma unroll
+		for (int u = 0; u < PER; u++) {
+			int e = threadIdx.x+256*u;
+			int t = e/TL, i = e%TL;
+			int col = t0+t;
+			int ra = r0+i, rb = c0+i;
+			pa[u] = (col < n6 && ra < F6) ? base[(int64_t)col*ld+ra] : T(0);
+			pb[u] = (col < n6 && rb < F6) ? base[(int64_t)col*ld+rb] : T(0);
+		}
+	};
+	load(0);
+	for (int t0 = 0; t0 < n6; t0 += KC) {
+		__syncthreads();
+#pragma unroll
+		for (int u = 0; u < PER; u++) {
+			int e = threadIdx.x+256*u;
+			As[e/TL][e%TL] = pa[u];
+			Bs[e/TL][e%TL] = pb[u];
+		}
+		__syncthreads();
+		if (t0+KC < n6) load(t0+KC);
+#pragma unroll
+		for (int t = 0; t < KC; t++) {
+			T av[TPT], bv[TPT];
+#pragma unroll
+			for (int a = 0; a < TPT; a++) av[a] = As[t][tx+TD*a];
+#pragma unroll
+			for (int b = 0; b < TPT; b++) bv[b] = Bs[t][ty+TD*b];
+#pragma unroll
+			for (int a = 0; a < TPT; a++)
+#pragma unroll
+				for (int b = 0; b < TPT; b++) acc[a][b] += av[a]*bv[b];
+		}
+	}
+#pragma unroll
+	for (int b = 0; b < TPT; b++) {
+		int c = c0+ty+TD*b;
+		if (c >= F6) continue;
+#pragma unroll
+		for (int a = 0; a < TPT; a++) {
+			int r = r0+tx+TD*a;
+			if (r >= F6 || r < c) continue;
+			base[(int64_t)c*ld+r] -= acc[a][b];
+		}
+	}
+}
+
 // ---------------------------------------------------------------------------
 // allocation and launch
 // ---------------------------------------------------------------------------
 template <typename T> static void set_smem_limits(int maxn6);
+
+template <typename T> static size_t update_smem() { return 2*sizeof(T)*Cfg<T>::NB*Cfg<T>::TILE; }
+
+template <typename T> static void set_update_smem()
+{
+	static bool done = false;
+	if (done) return;
+	LFG_CUDA(cudaFuncSetAttribute(k_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)update_smem<T>()));
+	done = true;
+}
 
 template <typename T> void factor_alloc(DevFactor<T> &F, const DevSymbolic &D, int kmax)
 {
@@ -316,9 +408,8 @@ template <typename T> void factor_alloc(DevFactor<T> &F, const DevSymbolic &D, i
 		F.x_cap = xneed;
 	}
 	if (!F.status) LFG_CUDA(cudaMalloc((void **)&F.status, sizeof(int)*4));
-	if ((int64_t)sizeof(T)*4*D.max_n6 > 227*1024)
-		throw Error{LFG_ERR_BAD_ARG, 0, "supernode too wide for the shared-memory solve"};
 	set_smem_limits<T>(D.max_n6);
+	set_update_smem<T>();
 }
 
 template <typename T> void factor_free(DevFactor<T> &F)
@@ -361,8 +452,11 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 			                                    F.arena, F.status);
 			break;
 		case PLAN_UPDATE:
-			k_update<T><<<L.count, 256, 0, st>>>(D.tile_tasks+L.off, D.sn_first, D.sn_n, D.sn_m, D.sn_ld,
+			k_update<T><<<L.count, 256, update_smem<T>(), st>>>(D.tile_tasks+L.off, D.sn_first, D.sn_n, D.sn_m, D.sn_ld,
 			                                     D.sn_off, F.arena, F.status);
+			break;
+		case PLAN_SYRK:
+			k_syrk<T><<<L.count, 256, 0, st>>>(D.tile_tasks+L.off, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, F.arena);
 			break;
 		}
 		launches++;
@@ -396,170 +490,202 @@ __global__ void k_permute_out(int n, int k, const int *__restrict__ iperm, const
 	for (int r = 0; r < k; r++) x[(int64_t)r*6*n+t] = (double)xp[(int64_t)r*6*n+q];
 }
 
-// gather of the children's forward-update vectors into front row rloc
-template <typename T>
-__device__ inline T gather_w(int s, int rloc, int rr, int rhs, int64_t wstride, const int *child_off,
-                             const int *children, const int64_t *cinv_off, const int *cinv,
-                             const int *sn_n, const int64_t *sn_woff, const T *w)
+// Solve kernels.  Per level of the assembly tree, forward (leaves first):
+//   k_fwd_gather : v_top (own columns, in xp) += children's update vectors;
+//                  w_s (update rows) = children's update vectors
+//   k_fwd_y      : y = E^T v_top           (E = L11^-T, upper triangular)
+//   k_fwd_w      : w_s -= L21 y
+// backward (root first):
+//   k_bwd_z      : z = y - L21^T x[rows of s]
+//   k_bwd_x      : x = E z
+// Each CTA produces 32 outputs; for the row-oriented products (k_fwd_w,
+// k_bwd_x) its 8 warps split the column range and lanes own rows, so every
+// factor load is a coalesced 128-byte line; the column-oriented products
+// (k_fwd_y, k_bwd_z) use one warp per output column.  Sums over children and
+// warps run in a fixed order: results are bitwise reproducible.
+constexpr int SOLVE_OUT = 32;   // outputs per CTA
+constexpr int SOLVE_WARPS = 8;
+
+template <typename T, int K>
+__global__ void __launch_bounds__(256) k_fwd_gather(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
+                             const int *__restrict__ sn_n, const int *__restrict__ sn_m,
+                             const int *__restrict__ child_off, const int *__restrict__ children,
+                             const int64_t *__restrict__ cinv_off, const int *__restrict__ cinv,
+                             const int64_t *__restrict__ sn_woff, T *__restrict__ w, int64_t wstride,
+                             T *__restrict__ xp, int n6tot)
 {
-	T v = 0;
-	for (int q = child_off[s]; q < child_off[s+1]; q++) {
-		int ch = children[q];
-		int ic = cinv[cinv_off[ch]+rloc];
-		if (ic >= 0) v += w[rhs*wstride+sn_woff[ch]+6*(ic-sn_n[ch])+rr];
+	int s = lev_sn[blockIdx.y];
+	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s];
+	int r = blockIdx.x*blockDim.x+threadIdx.x;
+	if (r >= F6) return;
+	int ca = child_off[s], cz = child_off[s+1];
+	T acc[K];
+#pragma unroll
+	for (int q = 0; q < K; q++) acc[q] = 0;
+	int rb = r/6, rr = r%6;
+	for (int c = ca; c < cz; c++) {
+		int ch = children[c];
+		int ic = cinv[cinv_off[ch]+rb];
+		if (ic < 0) continue;
+		int64_t src = sn_woff[ch]+6*(ic-sn_n[ch])+rr;
+#pragma unroll
+		for (int q = 0; q < K; q++) acc[q] += w[q*wstride+src];
 	}
-	return v;
+	if (r < n6) {
+		int g = 6*sn_first[s]+r;
+#pragma unroll
+		for (int q = 0; q < K; q++) xp[(int64_t)q*n6tot+g] += acc[q];
+	} else {
+		int64_t d = sn_woff[s]+(r-n6);
+#pragma unroll
+		for (int q = 0; q < K; q++) w[q*wstride+d] = acc[q];
+	}
 }
 
-// forward part 1: y_s = E^T v_top, one warp per output column j
+// y_j = sum_{i <= j} E[i][j] v_i, one warp per column j
 template <typename T, int K>
-__global__ void k_fwd_y(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
+__global__ void __launch_bounds__(256) k_fwd_y(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
                         const int *__restrict__ sn_n, const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
-                        const int64_t *__restrict__ sn_off, const int *__restrict__ child_off,
-                        const int *__restrict__ children, const int64_t *__restrict__ cinv_off,
-                        const int *__restrict__ cinv, const int64_t *__restrict__ sn_woff,
-                        const T *__restrict__ arena, const T *__restrict__ w, int64_t wstride,
-                        const T *__restrict__ xp, T *__restrict__ yp, int n6tot, int chunk)
+                        const int64_t *__restrict__ sn_off, const T *__restrict__ arena,
+                        const T *__restrict__ xp, T *__restrict__ yp, int n6tot)
 {
-	extern __shared__ unsigned char smem_raw[];
-	T *v = reinterpret_cast<T *>(smem_raw);
 	int s = lev_sn[blockIdx.y];
 	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
-	int j0 = blockIdx.x*chunk;
-	if (j0 >= n6) return;
+	int warp = threadIdx.x/32, lane = threadIdx.x%32;
 	int f6 = 6*sn_first[s];
-	for (int i = threadIdx.x; i < n6; i += blockDim.x) {
-#pragma unroll
-		for (int r = 0; r < K; r++)
-			v[r*n6+i] = xp[(int64_t)r*n6tot+f6+i] +
-			            gather_w<T>(s, i/6, i%6, r, wstride, child_off, children, cinv_off, cinv, sn_n, sn_woff, w);
-	}
-	__syncthreads();
 	const T *E = arena+sn_off[s]+F6;
-	int warp = threadIdx.x/32, lane = threadIdx.x%32, nw = blockDim.x/32;
-	for (int j = j0+warp; j < min(n6, j0+chunk); j += nw) {
+	for (int j = blockIdx.x*SOLVE_OUT+warp; j < min(n6, (blockIdx.x+1)*SOLVE_OUT); j += SOLVE_WARPS) {
 		const T *col = E+(int64_t)j*ld;
 		T acc[K];
 #pragma unroll
-		for (int r = 0; r < K; r++) acc[r] = 0;
+		for (int q = 0; q < K; q++) acc[q] = 0;
 		for (int i = lane; i <= j; i += 32) {
 			T e = col[i];
 #pragma unroll
-			for (int r = 0; r < K; r++) acc[r] += e*v[r*n6+i];
+			for (int q = 0; q < K; q++) acc[q] += e*xp[(int64_t)q*n6tot+f6+i];
 		}
 #pragma unroll
-		for (int r = 0; r < K; r++) {
-			T a = acc[r];
+		for (int q = 0; q < K; q++) {
+			T a = acc[q];
 			for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-			if (lane == 0) yp[(int64_t)r*n6tot+f6+j] = a;
+			if (lane == 0) yp[(int64_t)q*n6tot+f6+j] = a;
 		}
 	}
 }
 
-// forward part 2: w_s = v_bottom - L21 y_s, one thread per update row
+// w_t -= sum_j L[n6+t][j] y_j: lanes own 32 consecutive rows, warps split j
 template <typename T, int K>
-__global__ void k_fwd_w(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
+__global__ void __launch_bounds__(256) k_fwd_w(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
                         const int *__restrict__ sn_n, const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
-                        const int64_t *__restrict__ sn_off, const int *__restrict__ child_off,
-                        const int *__restrict__ children, const int64_t *__restrict__ cinv_off,
-                        const int *__restrict__ cinv, const int64_t *__restrict__ sn_woff,
+                        const int64_t *__restrict__ sn_off, const int64_t *__restrict__ sn_woff,
                         const T *__restrict__ arena, T *__restrict__ w, int64_t wstride,
-                        const T *__restrict__ yp, int n6tot, int chunk)
+                        const T *__restrict__ yp, int n6tot)
 {
-	extern __shared__ unsigned char smem_raw[];
-	T *y = reinterpret_cast<T *>(smem_raw);
+	__shared__ T red[SOLVE_WARPS][K][32];
 	int s = lev_sn[blockIdx.y];
 	int n6 = 6*sn_n[s], m6 = 6*sn_m[s], ld = sn_ld[s];
-	int r0 = blockIdx.x*chunk;
-	if (r0 >= m6) return;
+	int t0 = blockIdx.x*32;
+	if (t0 >= m6) return;
+	int warp = threadIdx.x/32, lane = threadIdx.x%32;
+	int t = t0+lane;
 	int f6 = 6*sn_first[s];
-	for (int i = threadIdx.x; i < n6; i += blockDim.x)
+	const T *L = arena+sn_off[s]+n6;   // row n6 of column 0
+	T acc[K];
 #pragma unroll
-		for (int r = 0; r < K; r++) y[r*n6+i] = yp[(int64_t)r*n6tot+f6+i];
-	__syncthreads();
-	const T *L = arena+sn_off[s];
-	for (int t = r0+threadIdx.x; t < min(m6, r0+chunk); t += blockDim.x) {
-		int row = n6+t;
-		T acc[K];
+	for (int q = 0; q < K; q++) acc[q] = 0;
+	if (t < m6) {
+		for (int j = warp; j < n6; j += SOLVE_WARPS) {
+			T l = L[(int64_t)j*ld+t];
 #pragma unroll
-		for (int r = 0; r < K; r++)
-			acc[r] = gather_w<T>(s, row/6, row%6, r, wstride, child_off, children, cinv_off, cinv, sn_n, sn_woff, w);
-		for (int j = 0; j < n6; j++) {
-			T l = L[(int64_t)j*ld+row];
-#pragma unroll
-			for (int r = 0; r < K; r++) acc[r] -= l*y[r*n6+j];
+			for (int q = 0; q < K; q++) acc[q] += l*yp[(int64_t)q*n6tot+f6+j];
 		}
+	}
 #pragma unroll
-		for (int r = 0; r < K; r++) w[r*wstride+sn_woff[s]+t] = acc[r];
+	for (int q = 0; q < K; q++) red[warp][q][lane] = acc[q];
+	__syncthreads();
+	if (warp == 0 && t < m6) {
+		int64_t d = sn_woff[s]+t;
+#pragma unroll
+		for (int q = 0; q < K; q++) {
+			T a = 0;
+			for (int u = 0; u < SOLVE_WARPS; u++) a += red[u][q][lane];
+			w[q*wstride+d] -= a;
+		}
 	}
 }
 
-// backward part 1: z_s = y_s - L21^T x[rows], one warp per column j; z -> yp
+// z_j = y_j - sum_t L[n6+t][j] x[rows(t)], one warp per column j (z -> yp)
 template <typename T, int K>
-__global__ void k_bwd_z(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
+__global__ void __launch_bounds__(256) k_bwd_z(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
                         const int *__restrict__ sn_n, const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
                         const int64_t *__restrict__ sn_off, const int *__restrict__ sn_rows_off,
                         const int *__restrict__ rows, const T *__restrict__ arena, const T *__restrict__ xp,
-                        T *__restrict__ yp, int n6tot, int chunk)
+                        T *__restrict__ yp, int n6tot)
 {
 	int s = lev_sn[blockIdx.y];
 	int n6 = 6*sn_n[s], m6 = 6*sn_m[s], ld = sn_ld[s];
-	int j0 = blockIdx.x*chunk;
-	if (j0 >= n6) return;
+	if (m6 == 0) return;
+	int warp = threadIdx.x/32, lane = threadIdx.x%32;
 	int f6 = 6*sn_first[s];
-	const T *L = arena+sn_off[s];
+	const T *L = arena+sn_off[s]+n6;
 	const int *R = rows+sn_rows_off[s];
-	int warp = threadIdx.x/32, lane = threadIdx.x%32, nw = blockDim.x/32;
-	for (int j = j0+warp; j < min(n6, j0+chunk); j += nw) {
-		const T *col = L+(int64_t)j*ld+n6;
+	for (int j = blockIdx.x*SOLVE_OUT+warp; j < min(n6, (blockIdx.x+1)*SOLVE_OUT); j += SOLVE_WARPS) {
+		const T *col = L+(int64_t)j*ld;
 		T acc[K];
 #pragma unroll
-		for (int r = 0; r < K; r++) acc[r] = 0;
+		for (int q = 0; q < K; q++) acc[q] = 0;
 		for (int t = lane; t < m6; t += 32) {
 			T l = col[t];
 			int g = 6*R[t/6]+t%6;
 #pragma unroll
-			for (int r = 0; r < K; r++) acc[r] += l*xp[(int64_t)r*n6tot+g];
+			for (int q = 0; q < K; q++) acc[q] += l*xp[(int64_t)q*n6tot+g];
 		}
 #pragma unroll
-		for (int r = 0; r < K; r++) {
-			T a = acc[r];
+		for (int q = 0; q < K; q++) {
+			T a = acc[q];
 			for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-			if (lane == 0) yp[(int64_t)r*n6tot+f6+j] -= a;
+			if (lane == 0) yp[(int64_t)q*n6tot+f6+j] -= a;
 		}
 	}
 }
 
-// backward part 2: x_s = E z, one thread per row i (E upper triangular)
+// x_i = sum_{j >= i} E[i][j] z_j: lanes own 32 consecutive rows, warps split j
 template <typename T, int K>
-__global__ void k_bwd_x(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
+__global__ void __launch_bounds__(256) k_bwd_x(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
                         const int *__restrict__ sn_n, const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
                         const int64_t *__restrict__ sn_off, const T *__restrict__ arena,
-                        const T *__restrict__ yp, T *__restrict__ xp, int n6tot, int chunk)
+                        const T *__restrict__ yp, T *__restrict__ xp, int n6tot)
 {
-	extern __shared__ unsigned char smem_raw[];
-	T *z = reinterpret_cast<T *>(smem_raw);
+	__shared__ T red[SOLVE_WARPS][K][32];
 	int s = lev_sn[blockIdx.y];
 	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
-	int i0 = blockIdx.x*chunk;
+	int i0 = blockIdx.x*32;
 	if (i0 >= n6) return;
+	int warp = threadIdx.x/32, lane = threadIdx.x%32;
+	int i = i0+lane;
 	int f6 = 6*sn_first[s];
-	for (int i = threadIdx.x; i < n6; i += blockDim.x)
-#pragma unroll
-		for (int r = 0; r < K; r++) z[r*n6+i] = yp[(int64_t)r*n6tot+f6+i];
-	__syncthreads();
 	const T *E = arena+sn_off[s]+F6;
-	for (int i = i0+threadIdx.x; i < min(n6, i0+chunk); i += blockDim.x) {
-		T acc[K];
+	T acc[K];
 #pragma unroll
-		for (int r = 0; r < K; r++) acc[r] = 0;
-		for (int j = i; j < n6; j++) {
+	for (int q = 0; q < K; q++) acc[q] = 0;
+	if (i < n6) {
+		for (int j = i0+warp; j < n6; j += SOLVE_WARPS) {
+			if (j < i) continue;
 			T e = E[(int64_t)j*ld+i];
 #pragma unroll
-			for (int r = 0; r < K; r++) acc[r] += e*z[r*n6+j];
+			for (int q = 0; q < K; q++) acc[q] += e*yp[(int64_t)q*n6tot+f6+j];
 		}
+	}
 #pragma unroll
-		for (int r = 0; r < K; r++) xp[(int64_t)r*n6tot+f6+i] = acc[r];
+	for (int q = 0; q < K; q++) red[warp][q][lane] = acc[q];
+	__syncthreads();
+	if (warp == 0 && i < n6) {
+#pragma unroll
+		for (int q = 0; q < K; q++) {
+			T a = 0;
+			for (int u = 0; u < SOLVE_WARPS; u++) a += red[u][q][lane];
+			xp[(int64_t)q*n6tot+f6+i] = a;
+		}
 	}
 }
 
@@ -571,38 +697,39 @@ static int solve_k(DevFactor<T> &F, const DevSymbolic &D, const double *b, doubl
 	int64_t wstride = D.w_elems;
 	k_permute_in<T><<<(6*n+255)/256, 256, 0, st>>>(n, K, D.iperm, b, F.xp);
 	launches++;
-	const int CH = 256;  // outputs / rows per CTA
-	// forward: leaves -> root
 	for (int l = 0; l < D.nlevels; l++) {
 		int cnt = D.h_level_off[l+1]-D.h_level_off[l];
 		if (!cnt) continue;
-		int maxn6 = D.max_n6;
-		int gx = (std::max(maxn6, 1)+CH-1)/CH;
-		size_t sm = sizeof(T)*K*(size_t)maxn6;
-		dim3 g1(gx, cnt);
-		k_fwd_y<T, K><<<g1, 256, sm, st>>>(D.level_sn+D.h_level_off[l], D.sn_first, D.sn_n, D.sn_m, D.sn_ld,
-		                                    D.sn_off, D.child_off, D.children, D.cinv_off, D.cinv, D.sn_woff,
-		                                    F.arena, F.w, wstride, F.xp, F.yp, n6tot, CH);
-		int gxw = (D.max_F+CH-1)/CH;
-		dim3 g2(gxw, cnt);
-		k_fwd_w<T, K><<<g2, 256, sm, st>>>(D.level_sn+D.h_level_off[l], D.sn_first, D.sn_n, D.sn_m, D.sn_ld,
-		                                    D.sn_off, D.child_off, D.children, D.cinv_off, D.cinv, D.sn_woff,
-		                                    F.arena, F.w, wstride, F.yp, n6tot, CH);
+		const int *lev = D.level_sn+D.h_level_off[l];
+		int n6 = D.h_level_maxn6[l], m6 = D.h_level_maxm6[l];
+		dim3 g0((n6+m6+255)/256, cnt);
+		k_fwd_gather<T, K><<<g0, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.child_off, D.children, D.cinv_off,
+		                                        D.cinv, D.sn_woff, F.w, wstride, F.xp, n6tot);
+		dim3 g1((n6+SOLVE_OUT-1)/SOLVE_OUT, cnt);
+		k_fwd_y<T, K><<<g1, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, F.arena, F.xp, F.yp,
+		                                   n6tot);
 		launches += 2;
+		if (m6 > 0) {
+			dim3 g2((m6+31)/32, cnt);
+			k_fwd_w<T, K><<<g2, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, D.sn_woff, F.arena,
+			                                   F.w, wstride, F.yp, n6tot);
+			launches++;
+		}
 	}
-	// backward: root -> leaves
 	for (int l = D.nlevels-1; l >= 0; l--) {
 		int cnt = D.h_level_off[l+1]-D.h_level_off[l];
 		if (!cnt) continue;
-		int maxn6 = D.max_n6;
-		int gx = (std::max(maxn6, 1)+CH-1)/CH;
-		dim3 g(gx, cnt);
-		k_bwd_z<T, K><<<g, 256, 0, st>>>(D.level_sn+D.h_level_off[l], D.sn_first, D.sn_n, D.sn_m, D.sn_ld,
-		                                  D.sn_off, D.sn_rows_off, D.rows, F.arena, F.xp, F.yp, n6tot, CH);
-		size_t sm = sizeof(T)*K*(size_t)maxn6;
-		k_bwd_x<T, K><<<g, 256, sm, st>>>(D.level_sn+D.h_level_off[l], D.sn_first, D.sn_n, D.sn_m, D.sn_ld,
-		                                   D.sn_off, F.arena, F.yp, F.xp, n6tot, CH);
-		launches += 2;
+		const int *lev = D.level_sn+D.h_level_off[l];
+		int n6 = D.h_level_maxn6[l], m6 = D.h_level_maxm6[l];
+		dim3 g((n6+SOLVE_OUT-1)/SOLVE_OUT, cnt);
+		if (m6 > 0) {
+			k_bwd_z<T, K><<<g, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, D.sn_rows_off, D.rows,
+			                                  F.arena, F.xp, F.yp, n6tot);
+			launches++;
+		}
+		k_bwd_x<T, K><<<g, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, F.arena, F.yp, F.xp,
+		                                  n6tot);
+		launches++;
 	}
 	k_permute_out<T><<<(6*n+255)/256, 256, 0, st>>>(n, K, D.iperm, F.xp, x);
 	launches++;
@@ -611,27 +738,7 @@ static int solve_k(DevFactor<T> &F, const DevSymbolic &D, const double *b, doubl
 }
 
 template <typename T>
-static void set_smem_limits(int maxn6)
-{
-	static int done_for = -1;
-	size_t need = sizeof(T)*4*(size_t)maxn6;
-	if ((int)need <= done_for) return;
-	if (need > 48*1024) {
-		cudaFuncSetAttribute(k_fwd_y<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-		cudaFuncSetAttribute(k_fwd_y<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-		cudaFuncSetAttribute(k_fwd_y<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-		cudaFuncSetAttribute(k_fwd_y<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-		cudaFuncSetAttribute(k_fwd_w<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-		cudaFuncSetAttribute(k_fwd_w<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-		cudaFuncSetAttribute(k_fwd_w<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-		cudaFuncSetAttribute(k_fwd_w<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-		cudaFuncSetAttribute(k_bwd_x<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-		cudaFuncSetAttribute(k_bwd_x<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-		cudaFuncSetAttribute(k_bwd_x<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-		cudaFuncSetAttribute(k_bwd_x<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-	}
-	done_for = (int)need;
-}
+static void set_smem_limits(int) {}
 
 template <typename T>
 int factor_solve(DevFactor<T> &F, const DevSymbolic &D, int k, const double *b, double *x, cudaStream_t st)

@@ -99,6 +99,7 @@ struct DevSymbolic {
 	struct Launch { int kind; int level; int k; int64_t off; int count; };
 	std::vector<Launch> factor_plan;
 	std::vector<int> h_level_off, h_level_d_off, h_level_od_off;
+	std::vector<int> h_level_maxn6, h_level_maxm6;   // per-level maxima of 6n and 6m
 	std::vector<int64_t> h_col_task_off;
 	int64_t arena_elems = 0, w_elems = 0;
 	int max_F = 0;

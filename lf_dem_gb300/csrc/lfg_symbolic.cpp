@@ -391,7 +391,7 @@ void dev_symbolic_free(DevSymbolic &D)
 }
 
 // Launch kinds of the factor plan (interpreted by factor_numeric).
-enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4 };
+enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLAN_SYRK = 5 };
 
 void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb, int tile,
                          cudaStream_t st)
@@ -415,6 +415,13 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 	D.h_level_od_off = S.level_od_off;
 	D.max_n6 = 0;
 	for (int s = 0; s < S.nsn; s++) D.max_n6 = std::max(D.max_n6, 6*S.sn_n[s]);
+	D.h_level_maxn6.assign(S.nlevels, 0);
+	D.h_level_maxm6.assign(S.nlevels, 0);
+	for (int s = 0; s < S.nsn; s++) {
+		int l = S.sn_level[s];
+		D.h_level_maxn6[l] = std::max(D.h_level_maxn6[l], 6*S.sn_n[s]);
+		D.h_level_maxm6[l] = std::max(D.h_level_maxm6[l], 6*S.sn_m[s]);
+	}
 	// assembly column tasks, panel tasks and update tiles, level by level
 	std::vector<int> col_tasks;
 	std::vector<int4> panel_tasks, tile_tasks;
@@ -443,10 +450,11 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 				// panel rows: real [t0, F6), extra [F6, F6+t0)
 				for (int r = t0; r < F6; r += RC) panel_tasks.push_back(make_int4(s, r, k, std::min(RC, F6-r)));
 				for (int r = F6; r < F6+t0; r += RC) panel_tasks.push_back(make_int4(s, r, k, std::min(RC, F6+t0-r)));
-				// diagonal-block writer + trailing tiles
+				// diagonal-block writer + trailing tiles of the supernode's own
+				// columns (the update-matrix block is one SYRK after the panels)
 				tile_tasks.push_back(make_int4(s, k*panel_nb, -1, k));
 				for (int r = t0; r < F6; r += tile)
-					for (int c = t0; c <= r && c < F6; c += tile)
+					for (int c = t0; c <= r && c < n6; c += tile)
 						tile_tasks.push_back(make_int4(s, r, c, k));
 				for (int r = F6; r < F6+t0; r += tile)
 					for (int c = t0; c < n6; c += tile)
@@ -455,6 +463,17 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 			D.factor_plan.push_back({PLAN_PANEL, l, k, p0, (int)((int64_t)panel_tasks.size()-p0)});
 			D.factor_plan.push_back({PLAN_UPDATE, l, k, t0i, (int)((int64_t)tile_tasks.size()-t0i)});
 		}
+		// Schur complement U -= L21 L21^T, depth 6n, lower triangle of [6n, 6F)^2
+		int64_t s0 = (int64_t)tile_tasks.size();
+		for (int t = S.level_off[l]; t < S.level_off[l+1]; t++) {
+			int s = S.level_sn[t];
+			int n6 = 6*S.sn_n[s], F6 = n6+6*S.sn_m[s];
+			for (int r = n6; r < F6; r += tile)
+				for (int c = n6; c <= r; c += tile)
+					tile_tasks.push_back(make_int4(s, r, c, 0));
+		}
+		if ((int64_t)tile_tasks.size() > s0)
+			D.factor_plan.push_back({PLAN_SYRK, l, 0, s0, (int)((int64_t)tile_tasks.size()-s0)});
 	}
 	up(D.col_tasks, col_tasks, st);
 	up(D.panel_tasks, panel_tasks, st);

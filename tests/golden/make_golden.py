@@ -1,0 +1,113 @@
+#!/usr/bin/env python3
+"""Generate the golden fixtures in tests/golden/ by running LF_DEM's own C++
+(compiled from the reference sources into oracle/_ref by `make -C oracle ref`)
+on seeded packings, one time step at a time.
+
+Each fixture holds the resolved (non-dimensionalised) parameters, the
+configuration, and for every step: the state before the step, the reference's
+R_FU (lower CSC) and force / velocity / stress components at that state, and
+the state after the step.  The tests replay each step from the stored state
+with the CPU oracle and with the GPU engine and compare.
+
+usage: python tests/golden/make_golden.py   (needs the reference tree)
+"""
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+
+from lf_dem_gb300 import packing  # noqa: E402
+from refdump import read_records  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "lfdem_ref_harness")
+
+# Parameter files in LF_DEM's Parameter_File syntax (key = value; with unit
+# suffixes), resolved by the reference's own unit system inside the harness.
+CASES = {
+    "rate_n200": dict(n=200, vf=0.45, seed=101, control="r", value="1", suffix="r", steps=4, calc_stress=1,
+                      params="""
+lub_reduce_parameter = 1e-3;
+lub_max_gap = 0.5;
+kn = 1e4r;
+kt = 0.5kn;
+mu_static = 1;
+time_end = 2h;
+"""),
+    "stress_n200": dict(n=200, vf=0.5, seed=102, control="s", value="10", suffix="cl", steps=4, calc_stress=1,
+                        params="""
+lub_reduce_parameter = 1e-3;
+mu_static = 1;
+kn = 1e4cl;
+kt = 0.5kn;
+time_end = 5h;
+"""),
+    "rate_normal_n200": dict(n=200, vf=0.5, seed=103, control="r", value="2", suffix="r", steps=4,
+                             calc_stress=1, params="""
+lubrication_model = normal;
+friction_model = 0;
+lub_reduce_parameter = 1e-2;
+kn = 5e3r;
+repulsive_length = 0.02;
+contact_relaxation_time = 2e-3r;
+sd_coeff = 0.5;
+time_end = 1h;
+"""),
+}
+
+
+def run_case(name, c, workdir):
+    p = packing.generate(c["n"], c["vf"], seed=c["seed"])
+    conf = os.path.join(workdir, f"{name}.dat")
+    packing.write_conf(p, conf)
+    par = os.path.join(workdir, f"{name}_params.txt")
+    with open(par, "w") as f:
+        f.write(c["params"])
+    out = os.path.join(workdir, name)
+    os.makedirs(out, exist_ok=True)
+    r = subprocess.run([HARNESS, conf, par, c["control"], c["value"], c["suffix"], str(c["steps"]), out,
+                        str(c["calc_stress"]), "1"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"harness failed for {name}: {r.stderr[-2000:]}")
+    P = read_records(os.path.join(out, "params.bin"))
+    data = {"param_" + k: v for k, v in P.items()}
+    data["param_file"] = np.frombuffer(c["params"].encode(), dtype=np.uint8)
+    data["control_arg"] = np.frombuffer(f"-{c['control']} {c['value']}{c['suffix']}".encode(), dtype=np.uint8)
+    with open(conf) as f:
+        data["conf_file"] = np.frombuffer(f.read().encode(), dtype=np.uint8)
+    keep_pre = {"pre_position", "pre_shear_disp", "pre_time", "pre_strain", "pre_dt", "pre_shear_rate",
+                "pre_max_velocity", "pre_max_sliding_velocity", "pre_pairs_i", "pre_pairs_d"}
+    keep_post = {"post_position", "post_velocity", "post_ang_velocity", "post_na_velocity", "post_shear_rate",
+                 "post_dt", "post_strain", "post_time", "post_shear_disp", "post_pairs_i", "post_pairs_d",
+                 "post_total_stress", "post_max_velocity", "post_max_sliding_velocity"}
+    for k in range(c["steps"]):
+        R = read_records(os.path.join(out, f"step_{k:04d}.bin"))
+        last = k == c["steps"]-1
+        for key, v in R.items():
+            if key.endswith("pairs_d"):
+                v = v.reshape(-1, 20)[:, :16].reshape(-1)   # drop rvec / sliding velocity columns
+            if key in keep_pre or key in keep_post or (k == 0 and key.startswith("stage_")) or \
+                    (last and key.startswith("post_stress_")):
+                data[f"s{k}_{key}"] = v
+    data["nsteps"] = np.array([c["steps"]])
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **data)
+    return os.path.getsize(os.path.join(HERE, f"{name}.npz"))
+
+
+def main():
+    if not os.path.exists(HARNESS):
+        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+    with tempfile.TemporaryDirectory() as wd:
+        for name, c in CASES.items():
+            size = run_case(name, c, wd)
+            print(f"{name}: {size/1e3:.0f} kB")
+
+
+if __name__ == "__main__":
+    main()
