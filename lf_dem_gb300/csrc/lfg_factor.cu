@@ -29,10 +29,13 @@
 namespace lfg {
 
 enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLAN_SYRK = 5 };
+constexpr int PANEL_ROWS = 96;   // rows per panel task (must match the plan)
 
 template <typename T> struct Cfg;
-template <> struct Cfg<double> { static constexpr int NB = 32, TILE = 64, TPT = 4; };
-template <> struct Cfg<float>  { static constexpr int NB = 64, TILE = 128, TPT = 8; };
+// NB: panel width; TILE/TPT: trailing-update tile edge / outputs per thread
+// per dimension; STILE/STPT: the same for the deep-K Schur complement SYRK
+template <> struct Cfg<double> { static constexpr int NB = 32, TILE = 64, TPT = 4, STILE = 64, STPT = 4; };
+template <> struct Cfg<float>  { static constexpr int NB = 64, TILE = 64, TPT = 4, STILE = 128, STPT = 8; };
 
 // ---------------------------------------------------------------------------
 // compact blocks -> dense (StokesSolver.cpp:154-231), m[r*6+c]
@@ -176,44 +179,92 @@ __device__ void warp_potrf(T *A, int w, int gcol0, int *fail)
 	}
 }
 
-// panel: CTA (128 threads) = one task (sn, row0, k, nrows)
+// w x w Cholesky of a shared-memory block (A[i*LK+j], lower) by the whole
+// CTA, right-looking: every element's arithmetic is independent of the thread
+// count, so every CTA that factors the same block gets identical bits.
+template <typename T, int NB>
+__device__ void cta_potrf(T *A, int w, int gcol0, int *fail)
+{
+	constexpr int LK = LdK<NB>::v;
+	for (int j = 0; j < w; j++) {
+		if (threadIdx.x == 0) {
+			T d = A[j*LK+j];
+			if (!(d > T(0))) {
+				if (fail) atomicMin(fail, gcol0+j+1);
+				d = T(1);
+			}
+			A[j*LK+j] = sqrt(d);
+		}
+		__syncthreads();
+		T d = A[j*LK+j];
+		for (int i = j+1+threadIdx.x; i < w; i += blockDim.x) A[i*LK+j] /= d;
+		__syncthreads();
+		// trailing update, threads as a 16-wide 2-D grid over (row i, column l)
+		const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4, ny = blockDim.x >> 4;
+		for (int i = j+1+ty; i < w; i += ny) {
+			T aij = A[i*LK+j];
+			for (int l = j+1+tx; l <= i; l += 16) A[i*LK+l] -= aij*A[l*LK+j];
+		}
+		__syncthreads();
+	}
+}
+
+// panel: CTA (128 threads) = one task (sn, row0, k, nrows <= PANEL_ROWS).  The CTA factors
+// the diagonal block itself (the update kernel of the same step writes it
+// back), stages its rows in shared memory and solves x L_kk^T = a for each
+// row by 16-column blocks: independent accumulations over the solved blocks,
+// then a 16-step substitution inside the block.
 template <typename T>
 __global__ void __launch_bounds__(128) k_panel(const int4 *__restrict__ tasks, const int *__restrict__ sn_first,
                                                const int *__restrict__ sn_n, const int *__restrict__ sn_ld,
-                                               const int64_t *__restrict__ sn_off, T *__restrict__ arena,
-                                               int *fail)
+                                               const int64_t *__restrict__ sn_off, T *__restrict__ arena)
 {
 	constexpr int NB = Cfg<T>::NB, LK = LdK<NB>::v;
 	__shared__ T Lkk[NB*LK];
+	__shared__ T As[PANEL_ROWS*NB];   // the CTA's rows; column index XOR-swizzled by the row
+	                                  // so a warp's lanes (rows) fall on distinct banks
 	int4 tk = tasks[blockIdx.x];
 	int s = tk.x, row0 = tk.y, k = tk.z, nrows = tk.w;
 	int n6 = 6*sn_n[s], ld = sn_ld[s];
 	int c0 = k*NB, w = min(NB, n6-c0);
 	T *base = arena+sn_off[s];
+	for (int e = threadIdx.x; e < NB*LK; e += blockDim.x) Lkk[e] = T(0);
+	__syncthreads();
 	for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
-		int i = e%NB, j = e/NB;   // consecutive threads read consecutive rows
-		Lkk[i*LK+j] = (i < w && j <= i) ? base[(int64_t)(c0+j)*ld+c0+i] : T(0);
+		int i = e%NB, j = e/NB;
+		if (i < w && j <= i) Lkk[i*LK+j] = base[(int64_t)(c0+j)*ld+c0+i];
+	}
+	for (int e = threadIdx.x; e < PANEL_ROWS*NB; e += blockDim.x) {
+		int rr = e%PANEL_ROWS, j = e/PANEL_ROWS;   // coalesced over rows
+		As[rr*NB+(j ^ (rr & 31))] = (rr < nrows && j < w) ? base[(int64_t)(c0+j)*ld+row0+rr] : T(0);
 	}
 	__syncthreads();
-	if (threadIdx.x < 32) warp_potrf<T, NB>(Lkk, w, 6*sn_first[s]+c0, nullptr);
-	__syncthreads();
+	cta_potrf<T, NB>(Lkk, w, 0, nullptr);
 	int r = threadIdx.x;
-	if (r < nrows) {
-		int row = row0+r;
-		T x[NB];
+	if (r >= nrows || r >= PANEL_ROWS) return;
+	int row = row0+r;
+	T *a = As+r*NB;
+	const int sw = r & 31;
+	for (int jb = 0; jb < w; jb += 16) {
+		T x[16];
 #pragma unroll
-		for (int j = 0; j < NB; j++) x[j] = (j < w) ? base[(int64_t)(c0+j)*ld+row] : T(0);
+		for (int jj = 0; jj < 16; jj++) x[jj] = a[(jb+jj) ^ sw];
+		for (int t = 0; t < jb; t++) {
+			T xt = a[t ^ sw];
 #pragma unroll
-		for (int j = 0; j < NB; j++) {
-			if (j < w) {
-				T v = x[j];
-#pragma unroll
-				for (int t = 0; t < NB; t++) if (t < j) v -= x[t]*Lkk[j*LK+t];
-				x[j] = v/Lkk[j*LK+j];
-			}
+			for (int jj = 0; jj < 16; jj++) x[jj] -= xt*Lkk[(jb+jj)*LK+t];
 		}
 #pragma unroll
-		for (int j = 0; j < NB; j++) if (j < w) base[(int64_t)(c0+j)*ld+row] = x[j];
+		for (int jj = 0; jj < 16; jj++) {
+#pragma unroll
+			for (int u = 0; u < jj; u++) x[jj] -= x[u]*Lkk[(jb+jj)*LK+jb+u];
+			x[jj] = (jb+jj < w) ? x[jj]/Lkk[(jb+jj)*LK+jb+jj] : T(0);
+		}
+#pragma unroll
+		for (int jj = 0; jj < 16; jj++) {
+			a[(jb+jj) ^ sw] = x[jj];
+			if (jb+jj < w) base[(int64_t)(c0+jb+jj)*ld+row] = x[jj];
+		}
 	}
 }
 
@@ -225,7 +276,7 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
                                                 const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
                                                 T *__restrict__ arena, int *fail)
 {
-	constexpr int NB = Cfg<T>::NB, TL = Cfg<T>::TILE, TPT = Cfg<T>::TPT, LK = LdK<NB>::v;
+	constexpr int NB = Cfg<T>::NB, TL = Cfg<T>::TILE, TPT = Cfg<T>::TPT;
 	constexpr int TD = TL/TPT; // threads per dimension (16)
 	extern __shared__ unsigned char smem_upd[];
 	T (*As)[TL] = reinterpret_cast<T (*)[TL]>(smem_upd);
@@ -236,16 +287,16 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 	int p0 = k*NB, w = min(NB, n6-p0), t0 = p0+w;
 	T *base = arena+sn_off[s];
 	if (cc0 < 0) {
+		constexpr int LK = LdK<NB>::v;
 		T *Lkk = &As[0][0];  // NB*(NB+1) <= 2*NB*TL (dynamic shared memory)
 		for (int e = threadIdx.x; e < NB*LK; e += blockDim.x) Lkk[e] = T(0);
 		__syncthreads();
 		for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
 			int i = e%NB, j = e/NB;
-			Lkk[i*LK+j] = (i < w && j <= i) ? base[(int64_t)(p0+j)*ld+p0+i] : T(0);
+			if (i < w && j <= i) Lkk[i*LK+j] = base[(int64_t)(p0+j)*ld+p0+i];
 		}
 		__syncthreads();
-		if (threadIdx.x < 32) warp_potrf<T, NB>(Lkk, w, 6*sn_first[s]+p0, fail);
-		__syncthreads();
+		cta_potrf<T, NB>(Lkk, w, 6*sn_first[s]+p0, fail);
 		for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
 			int i = e%NB, j = e/NB;
 			if (i < w && j <= i) base[(int64_t)(p0+j)*ld+p0+i] = Lkk[i*LK+j];
@@ -304,7 +355,7 @@ __global__ void __launch_bounds__(256) k_syrk(const int4 *__restrict__ tasks, co
                                               const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
                                               const int64_t *__restrict__ sn_off, T *__restrict__ arena)
 {
-	constexpr int TL = Cfg<T>::TILE, TPT = Cfg<T>::TPT, TD = TL/TPT;
+	constexpr int TL = Cfg<T>::STILE, TPT = Cfg<T>::STPT, TD = TL/TPT;
 	constexpr int KC = 16;
 	constexpr int PER = KC*TL/256;   // elements of A (and of B) each thread loads per chunk
 	__shared__ T As[KC][TL];
@@ -372,6 +423,9 @@ __global__ void __launch_bounds__(256) k_syrk(const int4 *__restrict__ tasks, co
 // allocation and launch
 // ---------------------------------------------------------------------------
 template <typename T> static void set_smem_limits(int maxn6);
+template <typename T> static int &bwdz_cap_ref() { static int v = 48*1024; return v; }
+template <typename T> static int bwdz_smem_cap() { return bwdz_cap_ref<T>(); }
+
 
 template <typename T> static size_t update_smem() { return 2*sizeof(T)*Cfg<T>::NB*Cfg<T>::TILE; }
 
@@ -449,7 +503,7 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 			break;
 		case PLAN_PANEL:
 			k_panel<T><<<L.count, 128, 0, st>>>(D.panel_tasks+L.off, D.sn_first, D.sn_n, D.sn_ld, D.sn_off,
-			                                    F.arena, F.status);
+			                                    F.arena);
 			break;
 		case PLAN_UPDATE:
 			k_update<T><<<L.count, 256, update_smem<T>(), st>>>(D.tile_tasks+L.off, D.sn_first, D.sn_n, D.sn_m, D.sn_ld,
@@ -614,31 +668,54 @@ __global__ void __launch_bounds__(256) k_fwd_w(const int *__restrict__ lev_sn, c
 	}
 }
 
-// z_j = y_j - sum_t L[n6+t][j] x[rows(t)], one warp per column j (z -> yp)
+// z_j = y_j - sum_t L[n6+t][j] x[rows(t)], one warp per column j (z -> yp).
+// The CTA first gathers x at the supernode's rows into shared memory
+// (dynamic, K * 6m values) when it fits, otherwise reads them from global.
 template <typename T, int K>
 __global__ void __launch_bounds__(256) k_bwd_z(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
                         const int *__restrict__ sn_n, const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
                         const int64_t *__restrict__ sn_off, const int *__restrict__ sn_rows_off,
                         const int *__restrict__ rows, const T *__restrict__ arena, const T *__restrict__ xp,
-                        T *__restrict__ yp, int n6tot)
+                        T *__restrict__ yp, int n6tot, int smem_cap)
 {
+	extern __shared__ unsigned char smem_bz[];
+	T *xr = reinterpret_cast<T *>(smem_bz);
 	int s = lev_sn[blockIdx.y];
 	int n6 = 6*sn_n[s], m6 = 6*sn_m[s], ld = sn_ld[s];
 	if (m6 == 0) return;
+	int j0 = blockIdx.x*SOLVE_OUT;
+	if (j0 >= n6) return;
 	int warp = threadIdx.x/32, lane = threadIdx.x%32;
 	int f6 = 6*sn_first[s];
 	const T *L = arena+sn_off[s]+n6;
 	const int *R = rows+sn_rows_off[s];
-	for (int j = blockIdx.x*SOLVE_OUT+warp; j < min(n6, (blockIdx.x+1)*SOLVE_OUT); j += SOLVE_WARPS) {
+	bool staged = K*m6 <= smem_cap;
+	if (staged) {
+		for (int t = threadIdx.x; t < m6; t += blockDim.x) {
+			int g = 6*R[t/6]+t%6;
+#pragma unroll
+			for (int q = 0; q < K; q++) xr[q*m6+t] = xp[(int64_t)q*n6tot+g];
+		}
+		__syncthreads();
+	}
+	for (int j = j0+warp; j < min(n6, j0+SOLVE_OUT); j += SOLVE_WARPS) {
 		const T *col = L+(int64_t)j*ld;
 		T acc[K];
 #pragma unroll
 		for (int q = 0; q < K; q++) acc[q] = 0;
-		for (int t = lane; t < m6; t += 32) {
-			T l = col[t];
-			int g = 6*R[t/6]+t%6;
+		if (staged) {
+			for (int t = lane; t < m6; t += 32) {
+				T l = col[t];
 #pragma unroll
-			for (int q = 0; q < K; q++) acc[q] += l*xp[(int64_t)q*n6tot+g];
+				for (int q = 0; q < K; q++) acc[q] += l*xr[q*m6+t];
+			}
+		} else {
+			for (int t = lane; t < m6; t += 32) {
+				T l = col[t];
+				int g = 6*R[t/6]+t%6;
+#pragma unroll
+				for (int q = 0; q < K; q++) acc[q] += l*xp[(int64_t)q*n6tot+g];
+			}
 		}
 #pragma unroll
 		for (int q = 0; q < K; q++) {
@@ -723,8 +800,10 @@ static int solve_k(DevFactor<T> &F, const DevSymbolic &D, const double *b, doubl
 		int n6 = D.h_level_maxn6[l], m6 = D.h_level_maxm6[l];
 		dim3 g((n6+SOLVE_OUT-1)/SOLVE_OUT, cnt);
 		if (m6 > 0) {
-			k_bwd_z<T, K><<<g, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, D.sn_rows_off, D.rows,
-			                                  F.arena, F.xp, F.yp, n6tot);
+			size_t want = sizeof(T)*(size_t)K*m6;
+			size_t sm = want <= (size_t)bwdz_smem_cap<T>() ? want : 0;
+			k_bwd_z<T, K><<<g, 256, sm, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, D.sn_rows_off,
+			                                   D.rows, F.arena, F.xp, F.yp, n6tot, (int)(sm/sizeof(T)));
 			launches++;
 		}
 		k_bwd_x<T, K><<<g, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, F.arena, F.yp, F.xp,
@@ -737,8 +816,20 @@ static int solve_k(DevFactor<T> &F, const DevSymbolic &D, const double *b, doubl
 	return launches;
 }
 
+// allow k_bwd_z to stage up to 200 kB of gathered x in shared memory
 template <typename T>
-static void set_smem_limits(int) {}
+static void set_smem_limits(int)
+{
+	static bool done = false;
+	if (done) return;
+	const int cap = 200*1024;
+	LFG_CUDA(cudaFuncSetAttribute(k_bwd_z<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+	LFG_CUDA(cudaFuncSetAttribute(k_bwd_z<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+	LFG_CUDA(cudaFuncSetAttribute(k_bwd_z<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+	LFG_CUDA(cudaFuncSetAttribute(k_bwd_z<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+	bwdz_cap_ref<T>() = cap;
+	done = true;
+}
 
 template <typename T>
 int factor_solve(DevFactor<T> &F, const DevSymbolic &D, int k, const double *b, double *x, cudaStream_t st)
@@ -761,58 +852,77 @@ int factor_solve(DevFactor<T> &F, const DevSymbolic &D, int k, const double *b, 
 // ---------------------------------------------------------------------------
 // FP64 block residual r = b - A x (row-block gather, deterministic)
 // ---------------------------------------------------------------------------
-__global__ void k_residual(int n, int k, const double *__restrict__ dbl, const double *__restrict__ odbl,
-                           const int *__restrict__ od_row, const int *__restrict__ od_col,
-                           const int *__restrict__ lo_ptr, const int *__restrict__ lo_idx,
-                           const int *__restrict__ up_ptr, const int *__restrict__ up_idx,
-                           const double *__restrict__ b, const double *__restrict__ x, double *__restrict__ r)
+// Dense position r*6+c of a compact block: 0 = structural zero, otherwise
+// +-(index+1) into the compact storage.  DSYM is the full symmetric diagonal
+// block of the 15-value storage, ODENSE the 18-value off-diagonal block; both
+// follow d15_to_dense / od18_to_dense above.
+__constant__ signed char c_dsym[36] = {1, 2, 3, 0, 4, 5, 2, 6, 7, -4, 0, 8, 3, 7, 9, -5, -8, 0,
+                                       0, -4, -5, 10, 11, 12, 4, 0, -8, 11, 13, 14, 5, 8, 0, 12, 14, 15};
+__constant__ signed char c_odense[36] = {1, 2, 3, 0, -10, -11, 2, 6, 7, 10, 0, -15, 3, 7, 9, 11, 15, 0,
+                                         0, -4, -5, 12, 13, 14, 4, 0, -8, 13, 16, 17, 5, 8, 0, 14, 17, 18};
+
+__device__ inline void warp_expand(const double *src, const signed char *tab, double *m, int lane)
 {
-	int i = blockIdx.x*blockDim.x+threadIdx.x;
+	for (int p = lane; p < 36; p += 32) {
+		int t = tab[p];
+		m[p] = t == 0 ? 0.0 : (t > 0 ? src[t-1] : -src[-t-1]);
+	}
+	__syncwarp();
+}
+
+// r = b - A x, one warp per block row i: lane = 6 * rhs + a owns output entry
+// a of right-hand side rhs (up to 4 right-hand sides per pass).  Each block
+// is expanded once into the warp's shared 6x6 buffer.  Blocks are visited in
+// a fixed order (diagonal, row i's lower blocks, then its upper blocks), so
+// the result is reproducible.
+__global__ void __launch_bounds__(256) k_residual(int n, int k, const double *__restrict__ dbl,
+                           const double *__restrict__ odbl, const int *__restrict__ od_row,
+                           const int *__restrict__ od_col, const int *__restrict__ lo_ptr,
+                           const int *__restrict__ lo_idx, const int *__restrict__ up_ptr,
+                           const int *__restrict__ up_idx, const double *__restrict__ b,
+                           const double *__restrict__ x, double *__restrict__ r)
+{
+	__shared__ double sm[8][36];
+	int w = threadIdx.x/32, lane = threadIdx.x%32;
+	int i = blockIdx.x*8+w;
 	if (i >= n) return;
-	double m[36];
-	for (int rh = 0; rh < k; rh++) {
-		const double *xv = x+(int64_t)rh*6*n;
-		double acc[6];
-		d15_to_dense(dbl+15*(int64_t)i, m);
-		for (int a = 0; a < 6; a++) {
-			double s = 0;
-			for (int c = 0; c < 6; c++) {
-				double mv = (a >= c) ? m[a*6+c] : m[c*6+a];
-				s += mv*xv[6*i+c];
-			}
-			acc[a] = s;
-		}
-		// blocks in row i below the diagonal: (row i, col j<i) = M
+	double *m = sm[w];
+	for (int q0 = 0; q0 < k; q0 += 4) {
+		int q = q0+lane/6, a = lane%6;
+		bool act = lane < 24 && q < k;
+		const double *xv = x+(int64_t)(act ? q : 0)*6*n;
+		double acc = 0;
+		warp_expand(dbl+15*(int64_t)i, c_dsym, m, lane);
+		if (act)
+			for (int c = 0; c < 6; c++) acc += m[a*6+c]*xv[6*i+c];
 		for (int t = lo_ptr[i]; t < lo_ptr[i+1]; t++) {
 			int e = lo_idx[t];
-			int j = od_col[e];
-			od18_to_dense(odbl+18*(int64_t)e, m);
-			for (int a = 0; a < 6; a++) {
-				double s = 0;
-				for (int c = 0; c < 6; c++) s += m[a*6+c]*xv[6*j+c];
-				acc[a] += s;
+			__syncwarp();
+			warp_expand(odbl+18*(int64_t)e, c_odense, m, lane);
+			if (act) {
+				int j = od_col[e];
+				for (int c = 0; c < 6; c++) acc += m[a*6+c]*xv[6*j+c];
 			}
 		}
-		// blocks in row i above the diagonal: (row i, col j>i) = M(j,i)^T
 		for (int t = up_ptr[i]; t < up_ptr[i+1]; t++) {
 			int e = up_idx[t];
-			int j = od_row[e];
-			od18_to_dense(odbl+18*(int64_t)e, m);
-			for (int a = 0; a < 6; a++) {
-				double s = 0;
-				for (int c = 0; c < 6; c++) s += m[c*6+a]*xv[6*j+c];
-				acc[a] += s;
+			__syncwarp();
+			warp_expand(odbl+18*(int64_t)e, c_odense, m, lane);
+			if (act) {
+				int j = od_row[e];
+				for (int c = 0; c < 6; c++) acc += m[c*6+a]*xv[6*j+c];
 			}
 		}
-		for (int a = 0; a < 6; a++) r[(int64_t)rh*6*n+6*i+a] = b[(int64_t)rh*6*n+6*i+a]-acc[a];
+		if (act) r[(int64_t)q*6*n+6*i+a] = b[(int64_t)q*6*n+6*i+a]-acc;
+		__syncwarp();
 	}
 }
 
 void block_residual(const DevBlockMatrix &A, int k, const double *b, const double *x, double *r,
                     cudaStream_t st)
 {
-	k_residual<<<(A.n+127)/128, 128, 0, st>>>(A.n, k, A.dblocks, A.odblocks, A.od_row, A.od_col, A.lo_ptr,
-	                                          A.lo_idx, A.up_ptr, A.up_idx, b, x, r);
+	k_residual<<<(A.n+7)/8, 256, 0, st>>>(A.n, k, A.dblocks, A.odblocks, A.od_row, A.od_col, A.lo_ptr,
+	                                      A.lo_idx, A.up_ptr, A.up_idx, b, x, r);
 }
 
 __global__ void k_axpy(int64_t total, const double *__restrict__ d, double *__restrict__ x)
@@ -852,6 +962,8 @@ void residual_norms(int n6, int k, const double *r, const double *b, double *out
 }
 
 int factor_tile_size(int precision) { return precision == LFG_PREC_FP64 ? Cfg<double>::TILE : Cfg<float>::TILE; }
+int factor_syrk_tile_size(int precision) { return precision == LFG_PREC_FP64 ? Cfg<double>::STILE : Cfg<float>::STILE; }
+int factor_panel_rows() { return PANEL_ROWS; }
 int factor_panel_width(int precision) { return precision == LFG_PREC_FP64 ? Cfg<double>::NB : Cfg<float>::NB; }
 
 template void factor_alloc<double>(DevFactor<double> &, const DevSymbolic &, int);

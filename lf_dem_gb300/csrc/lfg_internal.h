@@ -111,9 +111,11 @@ struct DevSymbolic {
 // Tile edge and panel width the factor kernels use for a precision; the
 // launch plan built by dev_symbolic_upload must use the same values.
 int factor_tile_size(int precision);
+int factor_syrk_tile_size(int precision);
 int factor_panel_width(int precision);
+int factor_panel_rows();
 
-void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb, int tile,
+void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb, int tile, int syrk_tile,
                          cudaStream_t st);
 void dev_symbolic_free(DevSymbolic &D);
 

@@ -393,7 +393,7 @@ void dev_symbolic_free(DevSymbolic &D)
 // Launch kinds of the factor plan (interpreted by factor_numeric).
 enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLAN_SYRK = 5 };
 
-void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb, int tile,
+void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb, int tile, int syrk_tile,
                          cudaStream_t st)
 {
 	dev_symbolic_free(D);
@@ -425,7 +425,7 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 	// assembly column tasks, panel tasks and update tiles, level by level
 	std::vector<int> col_tasks;
 	std::vector<int4> panel_tasks, tile_tasks;
-	const int RC = 128;  // rows per panel task
+	const int RC = factor_panel_rows();  // rows per panel task
 	D.factor_plan.clear();
 	for (int l = 0; l < S.nlevels; l++) {
 		int64_t c0 = (int64_t)col_tasks.size()/2;
@@ -450,8 +450,9 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 				// panel rows: real [t0, F6), extra [F6, F6+t0)
 				for (int r = t0; r < F6; r += RC) panel_tasks.push_back(make_int4(s, r, k, std::min(RC, F6-r)));
 				for (int r = F6; r < F6+t0; r += RC) panel_tasks.push_back(make_int4(s, r, k, std::min(RC, F6+t0-r)));
-				// diagonal-block writer + trailing tiles of the supernode's own
-				// columns (the update-matrix block is one SYRK after the panels)
+				// diagonal-block writer + trailing tiles of the supernode's
+				// own columns (the update-matrix block is one SYRK after the
+				// panels)
 				tile_tasks.push_back(make_int4(s, k*panel_nb, -1, k));
 				for (int r = t0; r < F6; r += tile)
 					for (int c = t0; c <= r && c < n6; c += tile)
@@ -468,8 +469,8 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 		for (int t = S.level_off[l]; t < S.level_off[l+1]; t++) {
 			int s = S.level_sn[t];
 			int n6 = 6*S.sn_n[s], F6 = n6+6*S.sn_m[s];
-			for (int r = n6; r < F6; r += tile)
-				for (int c = n6; c <= r; c += tile)
+			for (int r = n6; r < F6; r += syrk_tile)
+				for (int c = n6; c <= r; c += syrk_tile)
 					tile_tasks.push_back(make_int4(s, r, c, 0));
 		}
 		if ((int64_t)tile_tasks.size() > s0)
