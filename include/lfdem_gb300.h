@@ -231,6 +231,30 @@ int lfg_sim_assemble(lfg_sim *s, double *dblocks, int32_t *od_row, int32_t *od_c
                      double *odblocks, int cap, int *nb_out);
 int lfg_sim_force_component(lfg_sim *s, int comp, double *out);
 
+/* Force component comp at the current state, like lfg_sim_force_component,
+ * written to DEVICE memory d_out (6n doubles on the simulation's device),
+ * allocating nothing: no cudaMalloc/cudaFree and no pinned staging.  This
+ * entry point has no counterpart in the reference (LF_DEM keeps no device
+ * memory).  It is for callers that may not allocate device memory while they
+ * run: an application that owns every device allocation through its own pool
+ * or arena, or one on a path where the implicit device synchronisation of
+ * cudaMalloc/cudaFree is not allowed.
+ *  - The per-pair intermediate goes to a fixed scratch in static device
+ *    memory with room for LFG_NOALLOC_MAX_PAIRS pair slots (48 doubles each,
+ *    12.6 MB per device).  A simulation whose candidate-pair list is longer
+ *    gets LFG_ERR_BAD_ARG; use lfg_sim_force_component there.
+ *  - Neither the scratch nor d_out needs to start at zero: every value read
+ *    is written earlier in the same call, and all 6n outputs are written.
+ *  - The first call on a device does set-up (it resolves the scratch's device
+ *    address with cudaGetSymbolAddress, with that device current); make that
+ *    first call before any stream capture.
+ *  - All calls on one device share the scratch.  Calls that overlap in time
+ *    (from several threads, or for several simulations on one device) race
+ *    and corrupt each other's results: the caller must serialise them.
+ * Returns when the result is in d_out. */
+#define LFG_NOALLOC_MAX_PAIRS 32768
+int lfg_sim_force_component_noalloc(lfg_sim *s, int comp, double *d_out, lfg_status *st);
+
 /* Timing of the last lfg_sim_run / lfg_sim_step, device milliseconds by stage
  * (0 pairs, 1 assembly, 2 factorisation, 3 solves, 4 forces+stress, 5 move)
  * and kernels launched. */

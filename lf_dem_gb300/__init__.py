@@ -102,7 +102,7 @@ EXPORTS = [
     "lfg_sim_get_particles", "lfg_sim_get_num_pairs", "lfg_sim_get_pairs", "lfg_sim_get_particle_stress",
     "lfg_sim_get_velocity_component", "lfg_sim_set_contact", "lfg_sim_set_clock", "lfg_sim_refresh",
     "lfg_sim_assemble", "lfg_sim_force_component", "lfg_sim_get_timing", "lfg_sim_get_step_times",
-    "lfg_sim_clear_step_times", "lfg_sim_destroy",
+    "lfg_sim_clear_step_times", "lfg_sim_destroy", "lfg_sim_force_component_noalloc",
 ]
 
 _lib = None
@@ -156,6 +156,7 @@ def load(path: str | None = None):
         L.lfg_sim_refresh.argtypes = [vp]
         L.lfg_sim_assemble.argtypes = [vp, vp, vp, vp, vp, C.c_int, C.POINTER(C.c_int)]
         L.lfg_sim_force_component.argtypes = [vp, C.c_int, vp]
+        L.lfg_sim_force_component_noalloc.argtypes = [vp, C.c_int, vp, pst]
         L.lfg_sim_get_timing.argtypes = [vp, C.POINTER(SimTiming)]
         L.lfg_sim_get_step_times.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_int64)]
         L.lfg_sim_clear_step_times.argtypes = [vp]
@@ -381,6 +382,13 @@ class Sim:
         out = np.zeros(6 * self.n)
         rc = load().lfg_sim_force_component(self.h, comp, _ptr(out))
         return None if rc else out.reshape(-1, 6)
+
+    def force_component_noalloc(self, comp: int, d_out: int):
+        """Force component comp into the device buffer at address d_out (6n
+        doubles) through the entry point that allocates nothing."""
+        st = Status()
+        rc = load().lfg_sim_force_component_noalloc(self.h, comp, C.c_void_p(d_out), C.byref(st))
+        _check(rc, st)
 
     def step_times(self):
         L = load()

@@ -10,6 +10,7 @@
 // Every per-particle sum is a gather over the pair list in a fixed order (no
 // floating-point atomics), so the engine is bitwise reproducible.
 #include <cstdio>
+#include <mutex>
 
 #include "lfg_physics.h"
 
@@ -1350,6 +1351,53 @@ void phys_force_components(DevSim &S, cudaStream_t st)
 		                                                         S.pair_scratch);
 	k_gather_pairs<<<blocks_for(S.n, 128), 128, 0, st>>>(S.n, NFC, 48, S.row_ptr, S.col_ptr, S.col_idx,
 	                                                     S.pair_scratch, S.fc);
+	S.launches += 2;
+}
+
+// ---------------------------------------------------------------------------
+// Force components into caller memory without allocating (backs
+// lfg_sim_force_component_noalloc).  Some callers may not allocate device
+// memory while they run: a host application that owns every device
+// allocation through its own pool, or one on a path where the implicit device
+// synchronisation of cudaMalloc/cudaFree is not allowed.  For them the
+// per-pair intermediate of k_pair_forces (48 doubles per pair slot) goes to a
+// fixed scratch in static device memory instead of DevSim::pair_scratch.
+// k_pair_forces writes all 48 values of every slot it covers before
+// k_gather_pairs reads them, so the scratch need not start at zero.  All
+// calls on one device share it: calls that overlap in time race.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) double g_noalloc_pair_scratch[(size_t)NOALLOC_MAX_PAIRS*48];
+
+static std::mutex g_noalloc_mu;
+static double *g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+
+double *noalloc_pair_scratch(int device)
+{
+	if (device < 0 || device >= NOALLOC_MAX_DEVICES)
+		throw Error{LFG_ERR_BAD_ARG, device, "device ordinal beyond the no-allocation scratch table"};
+	std::lock_guard<std::mutex> lock(g_noalloc_mu);
+	if (!g_noalloc_ptr[device]) {
+		// set-up, once per device, with that device current
+		void *p = nullptr;
+		cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_pair_scratch);
+		if (e != cudaSuccess)
+			throw Error{LFG_ERR_CUDA, (int)e,
+			            std::string("cudaGetSymbolAddress of the no-allocation scratch failed: ")+
+			            cudaGetErrorString(e)};
+		g_noalloc_ptr[device] = static_cast<double *>(p);
+	}
+	return g_noalloc_ptr[device];
+}
+
+void phys_force_component_into(DevSim &S, int comp, double *scr, double *out, cudaStream_t st)
+{
+	if (S.npairs > NOALLOC_MAX_PAIRS)
+		throw Error{LFG_ERR_BAD_ARG, S.npairs, "pair slots exceed the no-allocation scratch (32768)"};
+	if (S.npairs)
+		k_pair_forces<<<blocks_for(S.npairs, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst, S.u_inf,
+		                                                         scr);
+	k_gather_pairs<<<blocks_for(S.n, 128), 128, 0, st>>>(S.n, 1, 48, S.row_ptr, S.col_ptr, S.col_idx, scr+12*comp,
+	                                                     out);
 	S.launches += 2;
 }
 

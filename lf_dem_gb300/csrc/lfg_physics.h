@@ -104,6 +104,11 @@ void phys_pair_constants(DevSim &S, cudaStream_t st);
 void phys_pairs_update(DevSim &S, int mode, int in_predictor, bool zero_dt, cudaStream_t st);
 void phys_blocks(DevSim &S, double *d_dblocks, double *d_odblocks, cudaStream_t st);
 void phys_force_components(DevSim &S, cudaStream_t st);
+// force component comp into out (6n) through the static no-allocation scratch
+constexpr int NOALLOC_MAX_PAIRS = 32768;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+double *noalloc_pair_scratch(int device);
+void phys_force_component_into(DevSim &S, int comp, double *scr, double *out, cudaStream_t st);
 // divided = 1: one RHS per component (setSolverRHS); 0: their sum (addToSolverRHS)
 void phys_rhs(DevSim &S, int divided, cudaStream_t st);
 void phys_stresslets(DevSim &S, cudaStream_t st);

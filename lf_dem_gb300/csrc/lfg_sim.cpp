@@ -41,6 +41,7 @@ public:
 	void refresh();
 	int assemble(double *dbl, int32_t *row, int32_t *col, double *odbl, int cap, int *nb_out);
 	int force_component(int comp, double *out);
+	void force_component_noalloc(int comp, double *d_out, int device);
 	void timing(lfg_sim_timing *o) const;
 	std::vector<double> step_ms;
 	int64_t step_kernels = 0;
@@ -634,6 +635,22 @@ int Sim::force_component(int comp, double *out)
 	return LFG_OK;
 }
 
+// Same kernels and summation order as force_component, with the per-pair
+// intermediate in the static no-allocation scratch and the result written to
+// the caller's device buffer; nothing is allocated.
+void Sim::force_component_noalloc(int comp, double *d_out, int device)
+{
+	if (comp < 0 || comp >= NFC) throw Error{LFG_ERR_BAD_ARG, comp, "component must be 0..3"};
+	if (S_.npairs > NOALLOC_MAX_PAIRS)
+		throw Error{LFG_ERR_BAD_ARG, S_.npairs, "pair slots exceed the no-allocation scratch (32768)"};
+	double *scr = noalloc_pair_scratch(device);
+	first_time();
+	phys_u_inf(S_, st_);
+	phys_force_component_into(S_, comp, scr, d_out, st_);
+	LFG_CUDA(cudaGetLastError());
+	LFG_CUDA(cudaStreamSynchronize(st_));
+}
+
 void Sim::timing(lfg_sim_timing *o) const
 {
 	std::memset(o, 0, sizeof *o);
@@ -836,6 +853,22 @@ int lfg_sim_force_component(lfg_sim *h, int comp, double *out)
 	if (!h || !out) return LFG_ERR_BAD_ARG;
 	SIM_GUARD_BEGIN
 	return h->s->force_component(comp, out);
+	SIM_GUARD_END
+}
+
+int lfg_sim_force_component_noalloc(lfg_sim *h, int comp, double *d_out, lfg_status *st)
+{
+	if (!h || !d_out) return fail(st, LFG_ERR_BAD_ARG, 0, "null simulation or output");
+	SIM_GUARD_BEGIN
+	LFG_CUDA(cudaSetDevice(h->device));
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, d_out) != cudaSuccess ||
+	    !(a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == h->device))) {
+		cudaGetLastError();
+		return fail(st, LFG_ERR_BAD_ARG, 0, "d_out must be device memory on the simulation's device");
+	}
+	h->s->force_component_noalloc(comp, d_out, h->device);
+	return ok(st);
 	SIM_GUARD_END
 }
 
