@@ -5,7 +5,7 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["rate_n200", "stress_n200", "rate_normal_n200"]
+CASES = ["rate_n200", "stress_n200", "rate_normal_n200", "rate_2d_n200"]
 PARAM_KEYS = ["kn", "kt", "mu_static", "mu_dynamic", "critical_load", "ft_max", "friction_model", "repulsion_on",
               "repulsion", "repulsive_length", "repulsive_max_length", "lubrication_model", "lub_reduce_parameter",
               "lub_max_gap", "interaction_range", "sd_coeff", "contact_relaxation_time",

@@ -9,7 +9,7 @@ R_FU (lower CSC) and force / velocity / stress components at that state, and
 the state after the step.  The tests replay each step from the stored state
 with the CPU oracle and with the GPU engine and compare.
 
-usage: python tests/golden/make_golden.py   (needs the reference tree)
+usage: python tests/golden/make_golden.py [case ...]   (needs the reference tree)
 """
 import os
 import subprocess
@@ -59,11 +59,21 @@ contact_relaxation_time = 2e-3r;
 sd_coeff = 0.5;
 time_end = 1h;
 """),
+    # 2D monolayer (ly = 0 in the configuration): the reference's twodimension path
+    "rate_2d_n200": dict(n=200, vf=0.7, seed=104, control="r", value="1", suffix="r", steps=4, calc_stress=1,
+                         twodim=True, params="""
+lub_reduce_parameter = 1e-3;
+lub_max_gap = 0.5;
+kn = 1e4r;
+kt = 0.5kn;
+mu_static = 1;
+time_end = 2h;
+"""),
 }
 
 
 def run_case(name, c, workdir):
-    p = packing.generate(c["n"], c["vf"], seed=c["seed"])
+    p = packing.generate(c["n"], c["vf"], seed=c["seed"], twodim=c.get("twodim", False))
     conf = os.path.join(workdir, f"{name}.dat")
     packing.write_conf(p, conf)
     par = os.path.join(workdir, f"{name}_params.txt")
@@ -100,14 +110,16 @@ def run_case(name, c, workdir):
     return os.path.getsize(os.path.join(HERE, f"{name}.npz"))
 
 
-def main():
+def main(only=None):
     if not os.path.exists(HARNESS):
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
     with tempfile.TemporaryDirectory() as wd:
         for name, c in CASES.items():
+            if only and name not in only:
+                continue
             size = run_case(name, c, wd)
             print(f"{name}: {size/1e3:.0f} kB")
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or None)
