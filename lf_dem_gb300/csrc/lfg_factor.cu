@@ -15,10 +15,10 @@
 // Per level of the assembly tree (leaves first):
 //   assemble  : zero + gather children's update matrices (fixed child order),
 //   scatter   : add the compact D / OD blocks of the level's columns,
-//   panel k   : factor the k-th diagonal block (redundantly per CTA) and
-//               solve the rows below it (real rows and identity rows),
-//   update k  : trailing rank-w update of the lower triangle (tiles) and
-//               write-back of the factored diagonal block.
+//   diag k    : factor and invert the k-th diagonal block (one CTA per front),
+//   trsm k    : rows below it (real rows and identity rows) times Linv^T,
+//   update k  : trailing rank-w update of the front's own columns (tiles),
+//   syrk      : the update (Schur complement) matrix, one deep-K product.
 // Nothing uses atomics except the failure flag, so results are bitwise
 // reproducible run to run.
 #include <cstdio>
@@ -28,8 +28,9 @@
 
 namespace lfg {
 
-enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLAN_SYRK = 5 };
-constexpr int PANEL_ROWS = 96;   // rows per panel task (must match the plan)
+enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLAN_SYRK = 5,
+       PLAN_DIAG = 6 };
+constexpr int PANEL_ROWS = 128;  // rows per panel (k_trsm) task (must match the plan)
 
 template <typename T> struct Cfg;
 // NB: panel width; TILE/TPT: trailing-update tile edge / outputs per thread
@@ -136,140 +137,247 @@ __global__ void k_scatter_od(int count, const int *__restrict__ list, const doub
 }
 
 // ---------------------------------------------------------------------------
-// w x w Cholesky of a shared-memory block (row-major A[i*NB+j], lower), by
-// one warp; rows owned by lanes i = lane + 32q.  Non-positive pivots are
-// replaced by 1 and reported through *fail (first column, global index + 1).
+// diagonal block of panel k (k_diag): one CTA (128 threads) per front.  The
+// NB x NB block (NB = 32 or 64) is factored by 32 x 32 sub-blocks, each by
+// one warp holding its rows in registers (lane = row), then inverted:
+// Linv = L_kk^-1 (lower triangular).  k_diag writes L_kk back into the front
+// and Linv^T (row-major, NB x NB, zeros below the diagonal) to the front's
+// slot of the Linv workspace, so the rows below the block are solved by
+// k_trsm as a product with Linv^T.  Rows and columns past the panel width w
+// are padded with the identity.  A non-positive pivot is replaced by 1 and
+// reported through *fail (first global scalar column + 1).
 // ---------------------------------------------------------------------------
-// row stride of the shared diagonal block: NB + 1 keeps the lanes (rows) of a
-// warp on distinct banks
-template <int NB> struct LdK { static constexpr int v = NB+1; };
+constexpr unsigned FULL_MASK = 0xffffffffu;
 
-template <typename T, int NB>
-__device__ void warp_potrf(T *A, int w, int gcol0, int *fail)
-{
-	constexpr int LK = LdK<NB>::v;
-	int lane = threadIdx.x & 31;
-	for (int j = 0; j < w; j++) {
-		// s_i = A[i][j] - sum_{t<j} L[i][t] L[j][t] for i >= j
-		T sv[(NB+31)/32];
-#pragma unroll
-		for (int q = 0; q < (NB+31)/32; q++) {
-			int i = lane+32*q;
-			T s = 0;
-			if (i >= j && i < w) {
-				s = A[i*LK+j];
-				for (int t = 0; t < j; t++) s -= A[i*LK+t]*A[j*LK+t];
-			}
-			sv[q] = s;
-		}
-		T d = __shfl_sync(0xffffffffu, sv[j/32], j%32);
-		if (!(d > T(0))) {
-			if (lane == 0 && fail) atomicMin(fail, gcol0+j+1);
-			d = T(1);
-		}
-		d = sqrt(d);
-		__syncwarp();
-#pragma unroll
-		for (int q = 0; q < (NB+31)/32; q++) {
-			int i = lane+32*q;
-			if (i == j) A[i*LK+j] = d;
-			else if (i > j && i < w) A[i*LK+j] = sv[q]/d;
-		}
-		__syncwarp();
-	}
-}
+// Warp routines on 32 x 32 blocks in shared memory (row-major, stride ld),
+// one row or column per lane in registers, loops fully unrolled so every
+// register index is static.  Pivots use rsqrt and the triangular solves use
+// reciprocals of the diagonal (shuffled from the lane that owns it), so each
+// step's dependent chain is a shuffle, a multiply and the updates.
 
-// w x w Cholesky of a shared-memory block (A[i*LK+j], lower) by the whole
-// CTA, right-looking: every element's arithmetic is independent of the thread
-// count, so every CTA that factors the same block gets identical bits.
-template <typename T, int NB>
-__device__ void cta_potrf(T *A, int w, int gcol0, int *fail)
-{
-	constexpr int LK = LdK<NB>::v;
-	for (int j = 0; j < w; j++) {
-		if (threadIdx.x == 0) {
-			T d = A[j*LK+j];
-			if (!(d > T(0))) {
-				if (fail) atomicMin(fail, gcol0+j+1);
-				d = T(1);
-			}
-			A[j*LK+j] = sqrt(d);
-		}
-		__syncthreads();
-		T d = A[j*LK+j];
-		for (int i = j+1+threadIdx.x; i < w; i += blockDim.x) A[i*LK+j] /= d;
-		__syncthreads();
-		// trailing update, threads as a 16-wide 2-D grid over (row i, column l)
-		const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4, ny = blockDim.x >> 4;
-		for (int i = j+1+ty; i < w; i += ny) {
-			T aij = A[i*LK+j];
-			for (int l = j+1+tx; l <= i; l += 16) A[i*LK+l] -= aij*A[l*LK+j];
-		}
-		__syncthreads();
-	}
-}
-
-// panel: CTA (128 threads) = one task (sn, row0, k, nrows <= PANEL_ROWS).  The CTA factors
-// the diagonal block itself (the update kernel of the same step writes it
-// back), stages its rows in shared memory and solves x L_kk^T = a for each
-// row by 16-column blocks: independent accumulations over the solved blocks,
-// then a 16-step substitution inside the block.
+// Cholesky of S (lower part), lane = row; S's lower part becomes L and its
+// upper part zero
 template <typename T>
-__global__ void __launch_bounds__(128) k_panel(const int4 *__restrict__ tasks, const int *__restrict__ sn_first,
-                                               const int *__restrict__ sn_n, const int *__restrict__ sn_ld,
-                                               const int64_t *__restrict__ sn_off, T *__restrict__ arena)
+__device__ void warp_potrf32(T *S, int ld, int lane, int jlim, int gcol0, int *fail)
 {
-	constexpr int NB = Cfg<T>::NB, LK = LdK<NB>::v;
-	__shared__ T Lkk[NB*LK];
-	__shared__ T As[PANEL_ROWS*NB];   // the CTA's rows; column index XOR-swizzled by the row
-	                                  // so a warp's lanes (rows) fall on distinct banks
+	T a[32];
+#pragma unroll
+	for (int l = 0; l < 32; l++) a[l] = S[lane*ld+l];
+#pragma unroll
+	for (int j = 0; j < 32; j++) {
+		T djj = __shfl_sync(FULL_MASK, a[j], j);
+		if (!(djj > T(0))) {
+			if (lane == 0 && j < jlim && fail) atomicMin(fail, gcol0+j+1);
+			djj = T(1);
+		}
+		T rs = rsqrt(djj);
+		T lij = a[j]*rs;
+		a[j] = (lane == j) ? djj*rs : lij;
+#pragma unroll
+		for (int l = j+1; l < 32; l++) a[l] -= lij*__shfl_sync(FULL_MASK, lij, l);
+	}
+#pragma unroll
+	for (int l = 0; l < 32; l++) S[lane*ld+l] = (l <= lane) ? a[l] : T(0);
+	__syncwarp();
+}
+
+// X L^T = A for 32 rows (lane = row) of X (stride ldx), L lower (stride ldl);
+// X replaces A
+template <typename T>
+__device__ void warp_trsm32(T *X, int ldx, const T *L, int ldl, int lane)
+{
+	T rd = T(1)/L[lane*ldl+lane];
+	T x[32];
+#pragma unroll
+	for (int l = 0; l < 32; l++) x[l] = X[lane*ldx+l];
+#pragma unroll
+	for (int t = 0; t < 32; t++) {
+		x[t] *= __shfl_sync(FULL_MASK, rd, t);
+#pragma unroll
+		for (int l = t+1; l < 32; l++) x[l] -= x[t]*L[l*ldl+t];
+	}
+#pragma unroll
+	for (int l = 0; l < 32; l++) X[lane*ldx+l] = x[l];
+	__syncwarp();
+}
+
+// V = L^-1 (lower; lane = column), V row-major with stride ldv
+template <typename T>
+__device__ void warp_trtri32(const T *L, int ldl, T *V, int ldv, int lane)
+{
+	T rd = T(1)/L[lane*ldl+lane];
+	T y[32];
+#pragma unroll
+	for (int i = 0; i < 32; i++) y[i] = (i == lane) ? T(1) : T(0);
+#pragma unroll
+	for (int t = 0; t < 32; t++) {
+		y[t] *= __shfl_sync(FULL_MASK, rd, t);
+#pragma unroll
+		for (int i = t+1; i < 32; i++) y[i] -= L[i*ldl+t]*y[t];
+	}
+#pragma unroll
+	for (int i = 0; i < 32; i++) V[i*ldv+lane] = y[i];
+	__syncwarp();
+}
+
+// c8[q] = sum_{t < 32} A[i][t] B[t][c] for row i = tid / 4 and columns
+// c = tid % 4 + 4q (128 threads cover a 32 x 32 product); B[t][c] is read at
+// B[t*ldb_t + c*ldb_c]
+template <typename T>
+__device__ void cta_gemm32(T (&c8)[8], const T *A, int lda, const T *B, int ldb_t, int ldb_c)
+{
+	int i = threadIdx.x/4, c0 = threadIdx.x%4;
+#pragma unroll
+	for (int q = 0; q < 8; q++) c8[q] = T(0);
+#pragma unroll 8
+	for (int t = 0; t < 32; t++) {
+		T av = A[i*lda+t];
+#pragma unroll
+		for (int q = 0; q < 8; q++) c8[q] += av*B[t*ldb_t+(c0+4*q)*ldb_c];
+	}
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_diag(const int4 *__restrict__ tasks, const int *__restrict__ sn_first,
+                                              const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
+                                              T *__restrict__ arena, T *__restrict__ linv, int *fail)
+{
+	constexpr int NB = Cfg<T>::NB, LD = NB+1;
+	static_assert(NB == 32 || NB == 64, "panel width");
+	__shared__ T Ls[NB*LD];   // L, row-major
+	__shared__ T Vs[NB*LD];   // Linv, row-major
+	__shared__ T Ts[32*33];   // L21 Linv11 (NB = 64)
 	int4 tk = tasks[blockIdx.x];
-	int s = tk.x, row0 = tk.y, k = tk.z, nrows = tk.w;
-	int n6 = 6*sn_n[s], ld = sn_ld[s];
-	int c0 = k*NB, w = min(NB, n6-c0);
+	int s = tk.x, p0 = tk.y, w = tk.w;
+	int ld = sn_ld[s];
 	T *base = arena+sn_off[s];
-	for (int e = threadIdx.x; e < NB*LK; e += blockDim.x) Lkk[e] = T(0);
+	int gcol0 = 6*sn_first[s]+p0;
+	int warp = threadIdx.x/32, lane = threadIdx.x%32;
+	for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
+		int i = e%NB, j = e/NB;    // coalesced over i (column-major front)
+		T v = T(0);
+		if (j <= i) {
+			if (i < w) v = base[(int64_t)(p0+j)*ld+p0+i];
+			else if (i == j) v = T(1);
+		}
+		Ls[i*LD+j] = v;
+		Vs[i*LD+j] = T(0);
+	}
 	__syncthreads();
+	if (warp == 0) warp_potrf32<T>(Ls, LD, lane, w, gcol0, fail);
+	__syncthreads();
+	if (warp == 0) warp_trtri32<T>(Ls, LD, Vs, LD, lane);                        // Linv11
+	else if (NB == 64 && warp == 1) warp_trsm32<T>(Ls+32*LD, LD, Ls, LD, lane);   // L21 = A21 L11^-T
+	__syncthreads();
+	if (NB == 64) {
+		T c8[8], u8[8];
+		int i = threadIdx.x/4, c0 = threadIdx.x%4;
+		cta_gemm32<T>(c8, Ls+32*LD, LD, Vs, LD, 1);          // T1 = L21 Linv11
+		cta_gemm32<T>(u8, Ls+32*LD, LD, Ls+32*LD, 1, LD);     // L21 L21^T
+#pragma unroll
+		for (int q = 0; q < 8; q++) {
+			int c = c0+4*q;
+			Ts[i*33+c] = c8[q];
+			if (c <= i) Ls[(32+i)*LD+32+c] -= u8[q];
+		}
+		__syncthreads();
+		if (warp == 0) warp_potrf32<T>(Ls+32*LD+32, LD, lane, w-32, gcol0+32, fail);
+		__syncthreads();
+		if (warp == 0) warp_trtri32<T>(Ls+32*LD+32, LD, Vs+32*LD+32, LD, lane);   // Linv22
+		__syncthreads();
+		cta_gemm32<T>(c8, Vs+32*LD+32, LD, Ts, 33, 1);       // Linv22 T1
+#pragma unroll
+		for (int q = 0; q < 8; q++) Vs[(32+i)*LD+c0+4*q] = -c8[q];
+		__syncthreads();
+	}
+	T *vt = linv+(int64_t)s*NB*NB;
 	for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
 		int i = e%NB, j = e/NB;
-		if (i < w && j <= i) Lkk[i*LK+j] = base[(int64_t)(c0+j)*ld+c0+i];
+		if (j <= i && i < w) base[(int64_t)(p0+j)*ld+p0+i] = Ls[i*LD+j];
+		vt[j*NB+i] = Vs[i*LD+j];   // Linv^T[t = j][col = i]
 	}
+}
+
+// ---------------------------------------------------------------------------
+// rows below the diagonal block of panel k (k_trsm): X = A Linv_kk^T for up
+// to PANEL_ROWS rows per CTA (real rows [t0, 6F) and identity rows [6F,
+// 6F + t0)), in place.  256 threads: thread (g, r) computes rows r and r + 64
+// for two column chunks of width NB/8, chunks g and 7 - g (equal work, since
+// column j needs t <= j).  Linv^T sits in shared memory row-major, so a
+// chunk's coefficients for one t are one or two vector loads (a broadcast).
+// ---------------------------------------------------------------------------
+template <typename T> struct Vec2;
+template <> struct Vec2<float> { typedef float4 V; static constexpr int W = 4; };
+template <> struct Vec2<double> { typedef double2 V; static constexpr int W = 2; };
+
+template <typename T, int CW>
+__device__ inline void lds_chunk(const T *p, T (&v)[CW])
+{
+	typedef typename Vec2<T>::V V;
+	constexpr int W = Vec2<T>::W;
+	static_assert(CW % W == 0, "chunk width");
+#pragma unroll
+	for (int q = 0; q < CW/W; q++) {
+		V x = reinterpret_cast<const V *>(p)[q];
+		const T *xs = reinterpret_cast<const T *>(&x);
+#pragma unroll
+		for (int u = 0; u < W; u++) v[q*W+u] = xs[u];
+	}
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_trsm(const int4 *__restrict__ tasks, const int *__restrict__ sn_n,
+                                              const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
+                                              T *__restrict__ arena, const T *__restrict__ linv)
+{
+	constexpr int NB = Cfg<T>::NB, CW = NB/8;
+	__shared__ __align__(16) T Vt[NB*NB];
+	__shared__ T As[PANEL_ROWS*NB];   // row r, column t at r*NB + (t ^ (r & 31)): a warp's rows on distinct banks
+	static_assert(PANEL_ROWS == 128, "two rows per thread");
+	int4 tk = tasks[blockIdx.x];
+	int s = tk.x, row0 = tk.y, k = tk.z, nrows = tk.w;
+	int ld = sn_ld[s];
+	int p0 = k*NB;
+	int w = min(NB, 6*sn_n[s]-p0);   // panel width: columns p0 + w and later are not touched
+	T *base = arena+sn_off[s];
+	const T *vt = linv+(int64_t)s*NB*NB;
+	for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) Vt[e] = vt[e];
 	for (int e = threadIdx.x; e < PANEL_ROWS*NB; e += blockDim.x) {
-		int rr = e%PANEL_ROWS, j = e/PANEL_ROWS;   // coalesced over rows
-		As[rr*NB+(j ^ (rr & 31))] = (rr < nrows && j < w) ? base[(int64_t)(c0+j)*ld+row0+rr] : T(0);
+		int r = e%PANEL_ROWS, t = e/PANEL_ROWS;   // coalesced over rows
+		As[r*NB+(t ^ (r & 31))] = (r < nrows && t < w) ? base[(int64_t)(p0+t)*ld+row0+r] : T(0);
 	}
 	__syncthreads();
-	cta_potrf<T, NB>(Lkk, w, 0, nullptr);
-	int r = threadIdx.x;
-	if (r >= nrows || r >= PANEL_ROWS) return;
-	int row = row0+r;
-	T *a = As+r*NB;
-	const int sw = r & 31;
-	for (int jb = 0; jb < w; jb += 16) {
-		T x[16];
+	int g = threadIdx.x/64, r = threadIdx.x%64;
+	const T *a0 = As+r*NB, *a1 = As+(r+64)*NB;
+	const int sw = r & 31;   // rows r and r + 64 share the swizzle
 #pragma unroll
-		for (int jj = 0; jj < 16; jj++) x[jj] = a[(jb+jj) ^ sw];
-		for (int t = 0; t < jb; t++) {
-			T xt = a[t ^ sw];
+	for (int h = 0; h < 2; h++) {
+		int c = h ? 7-g : g;
+		int j0 = c*CW;
+		T x0[CW], x1[CW];
 #pragma unroll
-			for (int jj = 0; jj < 16; jj++) x[jj] -= xt*Lkk[(jb+jj)*LK+t];
+		for (int q = 0; q < CW; q++) x0[q] = x1[q] = T(0);
+		for (int t = 0; t < j0+CW; t++) {
+			T v[CW];
+			lds_chunk<T, CW>(Vt+t*NB+j0, v);
+			T u0 = a0[t ^ sw], u1 = a1[t ^ sw];
+#pragma unroll
+			for (int q = 0; q < CW; q++) {
+				x0[q] += u0*v[q];
+				x1[q] += u1*v[q];
+			}
 		}
 #pragma unroll
-		for (int jj = 0; jj < 16; jj++) {
-#pragma unroll
-			for (int u = 0; u < jj; u++) x[jj] -= x[u]*Lkk[(jb+jj)*LK+jb+u];
-			x[jj] = (jb+jj < w) ? x[jj]/Lkk[(jb+jj)*LK+jb+jj] : T(0);
-		}
-#pragma unroll
-		for (int jj = 0; jj < 16; jj++) {
-			a[(jb+jj) ^ sw] = x[jj];
-			if (jb+jj < w) base[(int64_t)(c0+jb+jj)*ld+row] = x[jj];
+		for (int q = 0; q < CW; q++) {
+			if (j0+q >= w) continue;
+			int64_t col = (int64_t)(p0+j0+q)*ld+row0;
+			if (r < nrows) base[col+r] = x0[q];
+			if (r+64 < nrows) base[col+r+64] = x1[q];
 		}
 	}
 }
 
-// trailing update: CTA = one tile (sn, r0, c0, k); c0 == -1 writes the
-// factored diagonal block of panel k
+// trailing update: CTA = one tile (sn, r0, c0, k) of the front's own columns
 template <typename T>
 __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ tasks, const int *__restrict__ sn_first,
                                                 const int *__restrict__ sn_n, const int *__restrict__ sn_m,
@@ -286,23 +394,6 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
 	int p0 = k*NB, w = min(NB, n6-p0), t0 = p0+w;
 	T *base = arena+sn_off[s];
-	if (cc0 < 0) {
-		constexpr int LK = LdK<NB>::v;
-		T *Lkk = &As[0][0];  // NB*(NB+1) <= 2*NB*TL (dynamic shared memory)
-		for (int e = threadIdx.x; e < NB*LK; e += blockDim.x) Lkk[e] = T(0);
-		__syncthreads();
-		for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
-			int i = e%NB, j = e/NB;
-			if (i < w && j <= i) Lkk[i*LK+j] = base[(int64_t)(p0+j)*ld+p0+i];
-		}
-		__syncthreads();
-		cta_potrf<T, NB>(Lkk, w, 6*sn_first[s]+p0, fail);
-		for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
-			int i = e%NB, j = e/NB;
-			if (i < w && j <= i) base[(int64_t)(p0+j)*ld+p0+i] = Lkk[i*LK+j];
-		}
-		return;
-	}
 	bool extra = r0 >= F6;
 	int rlim = extra ? F6+t0 : F6;
 	int clim = n6;   // own columns only; the update matrix is k_syrk's
@@ -461,6 +552,13 @@ template <typename T> void factor_alloc(DevFactor<T> &F, const DevSymbolic &D, i
 		LFG_CUDA(cudaMalloc((void **)&F.yp, sizeof(T)*xneed));
 		F.x_cap = xneed;
 	}
+	int64_t lneed = (int64_t)D.nsn*Cfg<T>::NB*Cfg<T>::NB;
+	if (F.linv_cap < lneed) {
+		if (F.linv) cudaFree(F.linv);
+		F.linv = nullptr;
+		LFG_CUDA(cudaMalloc((void **)&F.linv, sizeof(T)*lneed));
+		F.linv_cap = lneed;
+	}
 	if (!F.status) LFG_CUDA(cudaMalloc((void **)&F.status, sizeof(int)*4));
 	set_smem_limits<T>(D.max_n6);
 	set_update_smem<T>();
@@ -473,6 +571,7 @@ template <typename T> void factor_free(DevFactor<T> &F)
 	if (F.xp) cudaFree(F.xp);
 	if (F.yp) cudaFree(F.yp);
 	if (F.status) cudaFree(F.status);
+	if (F.linv) cudaFree(F.linv);
 	F = DevFactor<T>();
 }
 
@@ -501,9 +600,12 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 			                                                     D.od_br, D.od_bc, D.od_tr, D.sn_ld, D.sn_off,
 			                                                     F.arena);
 			break;
+		case PLAN_DIAG:
+			k_diag<T><<<L.count, 128, 0, st>>>(D.diag_tasks+L.off, D.sn_first, D.sn_ld, D.sn_off, F.arena, F.linv,
+			                                   F.status);
+			break;
 		case PLAN_PANEL:
-			k_panel<T><<<L.count, 128, 0, st>>>(D.panel_tasks+L.off, D.sn_first, D.sn_n, D.sn_ld, D.sn_off,
-			                                    F.arena);
+			k_trsm<T><<<L.count, 256, 0, st>>>(D.panel_tasks+L.off, D.sn_n, D.sn_ld, D.sn_off, F.arena, F.linv);
 			break;
 		case PLAN_UPDATE:
 			k_update<T><<<L.count, 256, update_smem<T>(), st>>>(D.tile_tasks+L.off, D.sn_first, D.sn_n, D.sn_m, D.sn_ld,

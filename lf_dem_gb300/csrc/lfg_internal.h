@@ -95,6 +95,7 @@ struct DevSymbolic {
 	int *col_tasks = nullptr;      // (sn, col) pairs for the assembly kernel
 	int4 *panel_tasks = nullptr;   // (sn, row0, k, nrows)
 	int4 *tile_tasks = nullptr;    // (sn, row0, col0, k)
+	int4 *diag_tasks = nullptr;    // (sn, col0, k, width) of each panel's diagonal block
 	// host-side launch plan
 	struct Launch { int kind; int level; int k; int64_t off; int count; };
 	std::vector<Launch> factor_plan;
@@ -124,7 +125,8 @@ template <typename T> struct DevFactor {
 	T *arena = nullptr;   // fronts
 	T *w = nullptr;       // forward-solve update vectors
 	T *xp = nullptr, *yp = nullptr; // permuted solve workspaces (k * 6n)
-	int64_t arena_cap = 0, w_cap = 0, x_cap = 0;
+	T *linv = nullptr;    // per supernode: Linv^T of its current panel's diagonal block
+	int64_t arena_cap = 0, w_cap = 0, x_cap = 0, linv_cap = 0;
 	int *status = nullptr; // device: first non-positive pivot column + 1 (0 = ok)
 };
 

@@ -3,8 +3,10 @@
 //
 // The matrix is R_FU in 6x6 blocks (one block row/column per particle).  The
 // ordering is a nested dissection of the block graph: recursive bisection
-// (coordinate median when particle positions are given, breadth-first level
-// sets otherwise) with the smaller one-sided vertex boundary as separator.
+// (coordinate cuts at several quantiles when particle positions are given,
+// breadth-first level sets otherwise).  With positions, the separator is the
+// minimum vertex cover of the cut edges (Koenig's theorem), about a third
+// fewer factorisation flops than a one-sided boundary.
 // The dissection tree is used directly as the multifrontal assembly tree:
 // each separator (and each leaf sub-domain) is one supernode whose columns are
 // contiguous in the ordering, and whose front is dense.  The row structure of
@@ -85,9 +87,88 @@ struct Dissector {
 		}
 	}
 
+	// Minimum vertex cover of the cut edges (edges between side 0 and side 1
+	// of S), by Koenig's theorem: maximum bipartite matching (augmenting
+	// paths), then the alternating-path labelling from the unmatched side-0
+	// vertices; cover = (side-0 vertices not reached) + (side-1 vertices
+	// reached).  Removing the cover disconnects the two sides.
+	std::vector<int> min_cover(const std::vector<int> &S, int st, const std::vector<int> &b0,
+	                           const std::vector<int> &b1)
+	{
+		int n0 = (int)b0.size(), n1 = (int)b1.size();
+		for (int t = 0; t < n0; t++) level[b0[t]] = t;
+		for (int t = 0; t < n1; t++) level[b1[t]] = t;
+		std::vector<int> eptr(n0+1, 0), eadj;
+		for (int t = 0; t < n0; t++) {
+			int v = b0[t];
+			for (int k = g.ptr[v]; k < g.ptr[v+1]; k++) {
+				int u = g.adj[k];
+				if (u < 0 || stamp[u] != st || side[u] != 1) continue;
+				eadj.push_back(level[u]);
+			}
+			eptr[t+1] = (int)eadj.size();
+		}
+		std::vector<int> m0(n0, -1), m1(n1, -1), seen(n1, -1);
+		std::vector<int> stk, it;
+		for (int r = 0; r < n0; r++) {
+			// iterative DFS for an augmenting path from r
+			stk.assign(1, r);
+			it.assign(1, eptr[r]);
+			std::vector<int> via;   // side-1 vertex taken at each depth
+			bool found = false;
+			while (!stk.empty() && !found) {
+				int x = stk.back();
+				int &k = it.back();
+				if (k == eptr[x+1]) { stk.pop_back(); it.pop_back(); if (!via.empty()) via.pop_back(); continue; }
+				int y = eadj[k++];
+				if (seen[y] == r) continue;
+				seen[y] = r;
+				if (m1[y] < 0) {
+					via.push_back(y);
+					found = true;
+				} else {
+					via.push_back(y);
+					stk.push_back(m1[y]);
+					it.push_back(eptr[m1[y]]);
+				}
+			}
+			if (found) {
+				// flip the path: stk[d] matched to via[d]
+				for (size_t d = 0; d < stk.size(); d++) {
+					m0[stk[d]] = via[d];
+					m1[via[d]] = stk[d];
+				}
+			}
+		}
+		std::vector<char> z0(n0, 0), z1(n1, 0);
+		std::vector<int> q;
+		for (int x = 0; x < n0; x++) if (m0[x] < 0) { z0[x] = 1; q.push_back(x); }
+		for (size_t h = 0; h < q.size(); h++) {
+			int x = q[h];
+			for (int k = eptr[x]; k < eptr[x+1]; k++) {
+				int y = eadj[k];
+				if (z1[y] || m0[x] == y) continue;
+				z1[y] = 1;
+				int x2 = m1[y];
+				if (x2 >= 0 && !z0[x2]) { z0[x2] = 1; q.push_back(x2); }
+			}
+		}
+		std::vector<int> cover;
+		for (int x = 0; x < n0; x++) if (!z0[x] && eptr[x+1] > eptr[x]) cover.push_back(b0[x]);
+		for (int y = 0; y < n1; y++) if (z1[y]) cover.push_back(b1[y]);
+		for (int v : b0) level[v] = -1;
+		for (int v : b1) level[v] = -1;
+		return cover;
+	}
+
+	// coordinate cuts along each axis at several quantiles; the separator is
+	// the minimum vertex cover of the cut edges; the cut with the smallest
+	// ratio |separator| / (|side 0| |side 1|) wins
 	std::vector<int> split_geometric(const std::vector<int> &S, int st)
 	{
+		static const double fracs[] = {0.5, 0.47, 0.53, 0.44, 0.56, 0.41, 0.59, 0.38, 0.62};
 		std::vector<int> best;
+		double best_cost = 0;
 		bool have = false;
 		std::vector<int> b0, b1;
 		std::vector<std::pair<double,int>> key(S.size());
@@ -95,16 +176,21 @@ struct Dissector {
 		for (int ax = 0; ax < 3; ax++) {
 			if (twod && ax == 1) continue;
 			for (size_t t = 0; t < S.size(); t++) key[t] = {pos[3*S[t]+ax], S[t]};
-			size_t mid = S.size()/2;
-			std::nth_element(key.begin(), key.begin()+mid, key.end());
-			for (size_t t = 0; t < S.size(); t++) side[key[t].second] = t < mid ? 0 : 1;
-			boundary(S, st, b0, b1);
-			const std::vector<int> &sep = b0.size() <= b1.size() ? b0 : b1;
-			if (!have || sep.size() < best.size()) {
-				best = sep;
-				have = true;
-				best_side.resize(S.size());
-				for (size_t t = 0; t < S.size(); t++) best_side[t] = side[S[t]];
+			std::sort(key.begin(), key.end());
+			for (double f : fracs) {
+				size_t mid = (size_t)(f*S.size());
+				if (mid == 0 || mid >= S.size()) continue;
+				for (size_t t = 0; t < S.size(); t++) side[key[t].second] = t < mid ? 0 : 1;
+				boundary(S, st, b0, b1);
+				std::vector<int> sep = min_cover(S, st, b0, b1);
+				double cost = (double)sep.size()/((double)mid*(double)(S.size()-mid));
+				if (!have || cost < best_cost) {
+					best = sep;
+					best_cost = cost;
+					have = true;
+					best_side.resize(S.size());
+					for (size_t t = 0; t < S.size(); t++) best_side[t] = side[S[t]];
+				}
 			}
 		}
 		for (size_t t = 0; t < S.size(); t++) side[S[t]] = best_side[t];
@@ -385,13 +471,14 @@ void dev_symbolic_free(DevSymbolic &D)
 	void *ptrs[] = {D.perm, D.iperm, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_rows_off, D.rows,
 	                D.sn_off, D.sn_woff, D.child_off, D.children, D.cinv_off, D.cinv, D.level_sn,
 	                D.d_sn, D.d_bc, D.od_sn, D.od_br, D.od_bc, D.od_tr, D.level_d, D.level_od,
-	                D.col_tasks, D.panel_tasks, D.tile_tasks};
+	                D.col_tasks, D.panel_tasks, D.tile_tasks, D.diag_tasks};
 	for (void *p : ptrs) if (p) cudaFree(p);
 	D = DevSymbolic();
 }
 
 // Launch kinds of the factor plan (interpreted by factor_numeric).
-enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLAN_SYRK = 5 };
+enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLAN_SYRK = 5,
+       PLAN_DIAG = 6 };
 
 void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb, int tile, int syrk_tile,
                          cudaStream_t st)
@@ -424,7 +511,7 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 	}
 	// assembly column tasks, panel tasks and update tiles, level by level
 	std::vector<int> col_tasks;
-	std::vector<int4> panel_tasks, tile_tasks;
+	std::vector<int4> panel_tasks, tile_tasks, diag_tasks;
 	const int RC = factor_panel_rows();  // rows per panel task
 	D.factor_plan.clear();
 	for (int l = 0; l < S.nlevels; l++) {
@@ -441,19 +528,19 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 		D.factor_plan.push_back({PLAN_SCATTER_OD, l, 0, S.level_od_off[l], S.level_od_off[l+1]-S.level_od_off[l]});
 		for (int k = 0; k < kmax; k++) {
 			int64_t p0 = (int64_t)panel_tasks.size(), t0i = (int64_t)tile_tasks.size();
+			int64_t d0 = (int64_t)diag_tasks.size();
 			for (int t = S.level_off[l]; t < S.level_off[l+1]; t++) {
 				int s = S.level_sn[t];
 				int n6 = 6*S.sn_n[s], F6 = n6+6*S.sn_m[s];
 				if (n6 <= k*panel_nb) continue;
 				int w = std::min(panel_nb, n6-k*panel_nb);
 				int t0 = k*panel_nb+w;
+				diag_tasks.push_back(make_int4(s, k*panel_nb, k, w));
 				// panel rows: real [t0, F6), extra [F6, F6+t0)
 				for (int r = t0; r < F6; r += RC) panel_tasks.push_back(make_int4(s, r, k, std::min(RC, F6-r)));
 				for (int r = F6; r < F6+t0; r += RC) panel_tasks.push_back(make_int4(s, r, k, std::min(RC, F6+t0-r)));
-				// diagonal-block writer + trailing tiles of the supernode's
-				// own columns (the update-matrix block is one SYRK after the
-				// panels)
-				tile_tasks.push_back(make_int4(s, k*panel_nb, -1, k));
+				// trailing tiles of the supernode's own columns (the
+				// update-matrix block is one SYRK after the panels)
 				for (int r = t0; r < F6; r += tile)
 					for (int c = t0; c <= r && c < n6; c += tile)
 						tile_tasks.push_back(make_int4(s, r, c, k));
@@ -461,6 +548,7 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 					for (int c = t0; c < n6; c += tile)
 						tile_tasks.push_back(make_int4(s, r, c, k));
 			}
+			D.factor_plan.push_back({PLAN_DIAG, l, k, d0, (int)((int64_t)diag_tasks.size()-d0)});
 			D.factor_plan.push_back({PLAN_PANEL, l, k, p0, (int)((int64_t)panel_tasks.size()-p0)});
 			D.factor_plan.push_back({PLAN_UPDATE, l, k, t0i, (int)((int64_t)tile_tasks.size()-t0i)});
 		}
@@ -479,6 +567,7 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 	up(D.col_tasks, col_tasks, st);
 	up(D.panel_tasks, panel_tasks, st);
 	up(D.tile_tasks, tile_tasks, st);
+	up(D.diag_tasks, diag_tasks, st);
 }
 
 } // namespace lfg
