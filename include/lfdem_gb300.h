@@ -177,6 +177,12 @@ int lfg_sim_step(lfg_sim *s, int calc_stress, double time_end, double strain_end
 /* nsteps steps without stress output (the throughput loop). */
 int lfg_sim_run(lfg_sim *s, int nsteps, double time_end, double strain_end, lfg_status *st);
 
+/* lfg_sim_advance in slices: at most max_steps loop steps of
+ * System::timeEvolution; when the end is reached, also the final
+ * stress-computing step, and *done = 1. */
+int lfg_sim_advance_partial(lfg_sim *s, double time_end, double strain_end, int max_steps, int *done,
+                            lfg_status *st);
+
 typedef struct {
 	double time, strain, shear_rate, dt;
 	double shear_disp[2];
@@ -273,6 +279,87 @@ int lfg_sim_get_step_times(lfg_sim *s, double *ms, int cap, int64_t *kernels);
 void lfg_sim_clear_step_times(lfg_sim *s);
 
 void lfg_sim_destroy(lfg_sim *s);
+
+/* Re-run the symbolic analysis of the current pattern with another
+ * nested-dissection leaf size (supernode size at the leaves). */
+int lfg_sim_set_leaf_size(lfg_sim *s, int leaf_size, lfg_status *st);
+/* Device bytes held by the simulation (fronts, pair records, vectors). */
+int64_t lfg_sim_device_bytes(lfg_sim *s);
+
+/* ------------------------------------------------------------------ */
+/* 3. Many suspensions on one GPU (a rheology sweep, and a server).    */
+/* These have no single counterpart in the reference, which runs one   */
+/* System per process; each suspension behaves exactly like one        */
+/* simulation of its own: the same results alone or together.        */
+/* ------------------------------------------------------------------ */
+
+/* Estimated device bytes of one suspension of n particles (phi 0.45-0.58)
+ * before it exists: the factor's front arena (~N^1.55) plus pair records. */
+int64_t lfg_footprint_estimate(int n, int precision);
+
+/* Batch: suspensions of uneven N advanced together; nthreads host workers
+ * (0: one per core, at most 16) step them in slices on their own streams. */
+typedef struct lfg_batch lfg_batch;
+int lfg_batch_create(int device, int nthreads, lfg_batch **out, lfg_status *st);
+/* Same arguments as lfg_sim_create (no contact states); *slot = its index. */
+int lfg_batch_add(lfg_batch *b, const lfg_params *p, const lfg_options *opt, int n, const double *pos,
+                  const double *radius, double lx, double ly, double lz, const double *le_disp, int *slot,
+                  lfg_status *st);
+int lfg_batch_size(const lfg_batch *b);
+/* The slot's simulation, for the lfg_sim_get_* calls (owned by the batch). */
+lfg_sim *lfg_batch_sim(lfg_batch *b, int slot);
+/* Every suspension nsteps steps (lfg_sim_run). */
+int lfg_batch_run(lfg_batch *b, int nsteps, lfg_status *st);
+/* Every suspension to its own strain_end[slot] (lfg_sim_advance). */
+int lfg_batch_advance(lfg_batch *b, const double *strain_end, lfg_status *st);
+/* Autotuner: per size class (half-octaves of N, precision), time `steps`
+ * steps of one member with each candidate leaf size and keep the fastest
+ * for the class (and for suspensions added later). */
+int lfg_batch_autotune(lfg_batch *b, const int *leaf_sizes, int count, int steps, lfg_status *st);
+/* The leaf size chosen for (n, precision), 0 if none. */
+int lfg_batch_tuned_leaf(const lfg_batch *b, int n, int precision);
+void lfg_batch_destroy(lfg_batch *b);
+
+/* Server: requests admitted while fewer than max_active run and their
+ * estimated footprint fits in hbm_budget_bytes next to the running ones
+ * (first fit in arrival order; one request always runs when nothing else
+ * does); each runs to strain_end on its own stream and worker thread, and
+ * newly arrived requests join as others finish. */
+typedef struct lfg_server lfg_server;
+typedef struct {
+	int64_t id;
+	const lfg_params *params;
+	const lfg_options *options;     /* may be NULL (defaults) */
+	int n;
+	const double *pos, *radius;     /* copied by lfg_server_submit */
+	double lx, ly, lz;
+	double strain_end;
+} lfg_request;
+typedef struct {
+	int64_t id;
+	int status, n;                  /* status: LFG_OK or the error code */
+	int64_t steps;
+	double t_submit, t_admit, t_done;   /* seconds since lfg_server_create */
+	double strain, shear_rate, viscosity, N1, N2;
+	int64_t footprint_est, footprint_bytes;
+	char msg[120];
+} lfg_result;
+typedef struct {
+	int64_t submitted, admitted;
+	int active, queued, peak_active, pad_;
+	int64_t reserved_bytes, peak_reserved_bytes, budget_bytes;
+} lfg_server_stats;
+int lfg_server_create(int device, int max_active, int64_t hbm_budget_bytes, lfg_server **out,
+                      lfg_status *st);
+int lfg_server_submit(lfg_server *s, const lfg_request *r, lfg_status *st);
+/* Copies up to cap finished results (each returned once); returns the count. */
+int lfg_server_poll(lfg_server *s, lfg_result *out, int cap);
+/* Until every submitted request has finished (timeout_s <= 0: no limit). */
+int lfg_server_wait(lfg_server *s, double timeout_s, lfg_status *st);
+/* Final positions (3n) of a finished request. */
+int lfg_server_final_positions(lfg_server *s, int64_t id, double *pos, int n);
+int lfg_server_get_stats(lfg_server *s, lfg_server_stats *out);
+void lfg_server_destroy(lfg_server *s);
 
 #ifdef __cplusplus
 }

@@ -88,6 +88,26 @@ class Pair(C.Structure):
     ]
 
 
+class Request(C.Structure):
+    _fields_ = [("id", C.c_int64), ("params", C.c_void_p), ("options", C.c_void_p), ("n", C.c_int),
+                ("pos", C.c_void_p), ("radius", C.c_void_p), ("lx", C.c_double), ("ly", C.c_double),
+                ("lz", C.c_double), ("strain_end", C.c_double)]
+
+
+class Result(C.Structure):
+    _fields_ = [("id", C.c_int64), ("status", C.c_int), ("n", C.c_int), ("steps", C.c_int64),
+                ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double),
+                ("strain", C.c_double), ("shear_rate", C.c_double), ("viscosity", C.c_double),
+                ("N1", C.c_double), ("N2", C.c_double), ("footprint_est", C.c_int64),
+                ("footprint_bytes", C.c_int64), ("msg", C.c_char * 120)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("admitted", C.c_int64), ("active", C.c_int), ("queued", C.c_int),
+                ("peak_active", C.c_int), ("pad_", C.c_int), ("reserved_bytes", C.c_int64),
+                ("peak_reserved_bytes", C.c_int64), ("budget_bytes", C.c_int64)]
+
+
 class SimTiming(C.Structure):
     _fields_ = [("ms", C.c_double * 8), ("launches", C.c_int64), ("factor_flops", C.c_double),
                 ("solve_bytes", C.c_double)]
@@ -103,6 +123,11 @@ EXPORTS = [
     "lfg_sim_get_velocity_component", "lfg_sim_set_contact", "lfg_sim_set_clock", "lfg_sim_refresh",
     "lfg_sim_assemble", "lfg_sim_force_component", "lfg_sim_get_timing", "lfg_sim_get_step_times",
     "lfg_sim_clear_step_times", "lfg_sim_destroy", "lfg_sim_force_component_noalloc",
+    "lfg_sim_advance_partial", "lfg_sim_set_leaf_size", "lfg_sim_device_bytes", "lfg_footprint_estimate",
+    "lfg_batch_create", "lfg_batch_add", "lfg_batch_size", "lfg_batch_sim", "lfg_batch_run", "lfg_batch_advance",
+    "lfg_batch_autotune", "lfg_batch_tuned_leaf", "lfg_batch_destroy",
+    "lfg_server_create", "lfg_server_submit", "lfg_server_poll", "lfg_server_wait", "lfg_server_final_positions",
+    "lfg_server_get_stats", "lfg_server_destroy",
 ]
 
 _lib = None
@@ -163,6 +188,32 @@ def load(path: str | None = None):
         L.lfg_sim_clear_step_times.restype = None
         L.lfg_sim_destroy.argtypes = [vp]
         L.lfg_sim_destroy.restype = None
+        L.lfg_sim_advance_partial.argtypes = [vp, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_int), pst]
+        L.lfg_sim_set_leaf_size.argtypes = [vp, C.c_int, pst]
+        L.lfg_sim_device_bytes.argtypes = [vp]
+        L.lfg_sim_device_bytes.restype = C.c_int64
+        L.lfg_footprint_estimate.argtypes = [C.c_int, C.c_int]
+        L.lfg_footprint_estimate.restype = C.c_int64
+        L.lfg_batch_create.argtypes = [C.c_int, C.c_int, C.POINTER(vp), pst]
+        L.lfg_batch_add.argtypes = [vp, C.POINTER(Params), C.POINTER(Options), C.c_int, vp, vp, C.c_double,
+                                    C.c_double, C.c_double, vp, C.POINTER(C.c_int), pst]
+        L.lfg_batch_size.argtypes = [vp]
+        L.lfg_batch_sim.argtypes = [vp, C.c_int]
+        L.lfg_batch_sim.restype = vp
+        L.lfg_batch_run.argtypes = [vp, C.c_int, pst]
+        L.lfg_batch_advance.argtypes = [vp, vp, pst]
+        L.lfg_batch_autotune.argtypes = [vp, vp, C.c_int, C.c_int, pst]
+        L.lfg_batch_tuned_leaf.argtypes = [vp, C.c_int, C.c_int]
+        L.lfg_batch_destroy.argtypes = [vp]
+        L.lfg_batch_destroy.restype = None
+        L.lfg_server_create.argtypes = [C.c_int, C.c_int, C.c_int64, C.POINTER(vp), pst]
+        L.lfg_server_submit.argtypes = [vp, C.POINTER(Request), pst]
+        L.lfg_server_poll.argtypes = [vp, C.POINTER(Result), C.c_int]
+        L.lfg_server_wait.argtypes = [vp, C.c_double, pst]
+        L.lfg_server_final_positions.argtypes = [vp, C.c_int64, vp, C.c_int]
+        L.lfg_server_get_stats.argtypes = [vp, C.POINTER(ServerStats)]
+        L.lfg_server_destroy.argtypes = [vp]
+        L.lfg_server_destroy.restype = None
     _lib = L
     return L
 
@@ -300,9 +351,19 @@ class Sim:
         _check(rc, st)
         self.h = h
 
+    @classmethod
+    def _borrowed(cls, handle, n):
+        """A view of a simulation owned by a Batch (not destroyed by close)."""
+        self = cls.__new__(cls)
+        self.h = C.c_void_p(handle)
+        self.n = n
+        self._owned = False
+        return self
+
     def close(self):
         if getattr(self, "h", None):
-            load().lfg_sim_destroy(self.h)
+            if getattr(self, "_owned", True):
+                load().lfg_sim_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -318,6 +379,13 @@ class Sim:
     def run(self, nsteps, time_end=-1.0, strain_end=1e9):
         st = Status()
         _check(load().lfg_sim_run(self.h, int(nsteps), time_end, strain_end, C.byref(st)), st)
+
+    def set_leaf_size(self, leaf):
+        st = Status()
+        _check(load().lfg_sim_set_leaf_size(self.h, int(leaf), C.byref(st)), st)
+
+    def device_bytes(self) -> int:
+        return int(load().lfg_sim_device_bytes(self.h))
 
     def advance(self, time_end=-1.0, strain_end=-1.0):
         st = Status()
@@ -406,3 +474,123 @@ class Sim:
         load().lfg_sim_get_timing(self.h, C.byref(t))
         return {"ms": list(t.ms), "launches": t.launches, "factor_flops": t.factor_flops,
                 "solve_bytes": t.solve_bytes}
+
+
+def footprint_estimate(n: int, precision: int = PREC_FP32_REFINE) -> int:
+    return int(load().lfg_footprint_estimate(int(n), int(precision)))
+
+
+class Batch:
+    """Many suspensions on one GPU (lfg_batch_*), stepped together."""
+
+    def __init__(self, device: int = 0, nthreads: int = 0):
+        L = load()
+        h = C.c_void_p()
+        st = Status()
+        _check(L.lfg_batch_create(device, nthreads, C.byref(h), C.byref(st)), st)
+        self.h = h
+        self.n = []
+        self._keep = []
+
+    def add(self, params: dict, position, radius, lx, ly, lz, precision: int = PREC_FP64, **opts) -> int:
+        L = load()
+        p = make_params(params)
+        o = default_options(precision=precision, **opts)
+        pos = np.ascontiguousarray(position, dtype=np.float64).reshape(-1)
+        rad = np.ascontiguousarray(radius, dtype=np.float64)
+        slot = C.c_int()
+        st = Status()
+        _check(L.lfg_batch_add(self.h, C.byref(p), C.byref(o), len(rad), _ptr(pos), _ptr(rad), lx, ly, lz, None,
+                               C.byref(slot), C.byref(st)), st)
+        self.n.append(len(rad))
+        return slot.value
+
+    def sim(self, slot: int) -> "Sim":
+        return Sim._borrowed(load().lfg_batch_sim(self.h, slot), self.n[slot])
+
+    def run(self, nsteps: int):
+        st = Status()
+        _check(load().lfg_batch_run(self.h, int(nsteps), C.byref(st)), st)
+
+    def advance(self, strain_end):
+        se = np.ascontiguousarray(strain_end, dtype=np.float64)
+        st = Status()
+        _check(load().lfg_batch_advance(self.h, _ptr(se), C.byref(st)), st)
+
+    def autotune(self, leaf_sizes=(8, 16, 32, 64), steps: int = 2):
+        ls = np.ascontiguousarray(leaf_sizes, dtype=np.int32)
+        st = Status()
+        _check(load().lfg_batch_autotune(self.h, _ptr(ls), len(ls), int(steps), C.byref(st)), st)
+
+    def tuned_leaf(self, n: int, precision: int) -> int:
+        return int(load().lfg_batch_tuned_leaf(self.h, int(n), int(precision)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().lfg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Request loop (lfg_server_*): admission by estimated factor footprint,
+    continuous batching, per-request timing."""
+
+    def __init__(self, max_active: int, hbm_budget_bytes: int, device: int = 0):
+        L = load()
+        h = C.c_void_p()
+        st = Status()
+        _check(L.lfg_server_create(device, int(max_active), int(hbm_budget_bytes), C.byref(h), C.byref(st)), st)
+        self.h = h
+        self._n = {}
+
+    def submit(self, rid: int, params: dict, position, radius, lx, ly, lz, strain_end: float,
+               precision: int = PREC_FP32_REFINE, **opts):
+        p = make_params(params)
+        o = default_options(precision=precision, **opts)
+        pos = np.ascontiguousarray(position, dtype=np.float64).reshape(-1)
+        rad = np.ascontiguousarray(radius, dtype=np.float64)
+        r = Request(id=rid, params=C.cast(C.pointer(p), C.c_void_p), options=C.cast(C.pointer(o), C.c_void_p),
+                    n=len(rad), pos=pos.ctypes.data, radius=rad.ctypes.data, lx=lx, ly=ly, lz=lz,
+                    strain_end=strain_end)
+        st = Status()
+        _check(load().lfg_server_submit(self.h, C.byref(r), C.byref(st)), st)   # copies the inputs
+        self._n[rid] = len(rad)
+
+    def poll(self, cap: int = 256):
+        buf = (Result * cap)()
+        k = load().lfg_server_poll(self.h, buf, cap)
+        return [buf[i] for i in range(k)]
+
+    def wait(self, timeout_s: float = 0.0):
+        st = Status()
+        _check(load().lfg_server_wait(self.h, float(timeout_s), C.byref(st)), st)
+
+    def final_positions(self, rid: int):
+        n = self._n[rid]
+        out = np.zeros(3 * n)
+        rc = load().lfg_server_final_positions(self.h, int(rid), _ptr(out), n)
+        if rc:
+            raise LFGError(rc, f"no final positions for request {rid}")
+        return out.reshape(-1, 3)
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        load().lfg_server_get_stats(self.h, C.byref(s))
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_ if k != "pad_"}
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().lfg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

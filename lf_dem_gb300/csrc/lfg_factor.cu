@@ -21,7 +21,9 @@
 //   syrk      : the update (Schur complement) matrix, one deep-K product.
 // Nothing uses atomics except the failure flag, so results are bitwise
 // reproducible run to run.
+#include <atomic>
 #include <cstdio>
+#include <mutex>
 #include <cuda_runtime.h>
 
 #include "lfg_internal.h"
@@ -514,7 +516,7 @@ __global__ void __launch_bounds__(256) k_syrk(const int4 *__restrict__ tasks, co
 // allocation and launch
 // ---------------------------------------------------------------------------
 template <typename T> static void set_smem_limits(int maxn6);
-template <typename T> static int &bwdz_cap_ref() { static int v = 48*1024; return v; }
+template <typename T> static std::atomic<int> &bwdz_cap_ref() { static std::atomic<int> v{48*1024}; return v; }
 template <typename T> static int bwdz_smem_cap() { return bwdz_cap_ref<T>(); }
 
 
@@ -522,10 +524,11 @@ template <typename T> static size_t update_smem() { return 2*sizeof(T)*Cfg<T>::N
 
 template <typename T> static void set_update_smem()
 {
-	static bool done = false;
-	if (done) return;
-	LFG_CUDA(cudaFuncSetAttribute(k_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)update_smem<T>()));
-	done = true;
+	static std::once_flag once;
+	std::call_once(once, [] {
+		LFG_CUDA(cudaFuncSetAttribute(k_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                              (int)update_smem<T>()));
+	});
 }
 
 template <typename T> void factor_alloc(DevFactor<T> &F, const DevSymbolic &D, int kmax)
@@ -922,15 +925,15 @@ static int solve_k(DevFactor<T> &F, const DevSymbolic &D, const double *b, doubl
 template <typename T>
 static void set_smem_limits(int)
 {
-	static bool done = false;
-	if (done) return;
-	const int cap = 200*1024;
-	LFG_CUDA(cudaFuncSetAttribute(k_bwd_z<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-	LFG_CUDA(cudaFuncSetAttribute(k_bwd_z<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-	LFG_CUDA(cudaFuncSetAttribute(k_bwd_z<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-	LFG_CUDA(cudaFuncSetAttribute(k_bwd_z<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-	bwdz_cap_ref<T>() = cap;
-	done = true;
+	static std::once_flag once;
+	std::call_once(once, [] {
+		const int cap = 200*1024;
+		LFG_CUDA(cudaFuncSetAttribute(k_bwd_z<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+		LFG_CUDA(cudaFuncSetAttribute(k_bwd_z<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+		LFG_CUDA(cudaFuncSetAttribute(k_bwd_z<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+		LFG_CUDA(cudaFuncSetAttribute(k_bwd_z<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+		bwdz_cap_ref<T>() = cap;
+	});
 }
 
 template <typename T>

@@ -30,6 +30,7 @@ public:
 	void first_time();
 	void step(int calc_stress, double time_end, double strain_end);
 	void advance(double time_end, double strain_end);
+	bool advance_partial(double time_end, double strain_end, int max_steps);
 	void scalars(lfg_sim_scalars *o);
 	void particles(double *pos, double *vel, double *ang, double *na_vel, double *na_ang);
 	int num_pairs();
@@ -43,6 +44,8 @@ public:
 	int force_component(int comp, double *out);
 	void force_component_noalloc(int comp, double *d_out, int device);
 	void timing(lfg_sim_timing *o) const;
+	void set_leaf_size(int leaf) { solver_->reanalyze(leaf); symbolic_runs_++; }
+	int64_t device_bytes() const;
 	std::vector<double> step_ms;
 	int64_t step_kernels = 0;
 	int error_code = 0, error_info = 0;
@@ -126,11 +129,12 @@ static DevParams make_dev_params(const lfg_params &p, int n, double lx, double l
 	return P;
 }
 
-template <typename V> static void dalloc(V *&p, size_t count)
+// zero-filled device allocation, ordered on the simulation's stream (no
+// device-wide synchronisation, so other suspensions keep running)
+template <typename V> static void dalloc(V *&p, size_t count, cudaStream_t st)
 {
 	LFG_CUDA(cudaMalloc((void **)&p, sizeof(V)*std::max<size_t>(count, 1)));
-	LFG_CUDA(cudaMemset(p, 0, sizeof(V)*std::max<size_t>(count, 1)));
-	LFG_CUDA(cudaDeviceSynchronize());
+	LFG_CUDA(cudaMemsetAsync(p, 0, sizeof(V)*std::max<size_t>(count, 1), st));
 }
 
 Sim::Sim(const lfg_params &p, const lfg_options &o, int n, const double *pos, const double *radius, double lx,
@@ -145,15 +149,15 @@ Sim::Sim(const lfg_params &p, const lfg_options &o, int n, const double *pos, co
 		throw Error{LFG_ERR_BAD_ARG, 0, "lub_max_gap must be smaller than 1 (System.cpp:340-346)"};
 	S_.n = n;
 	S_.P = make_dev_params(p, n, lx, ly, lz, o.skin);
-	dalloc(S_.clock, 1);
-	dalloc(S_.pos, 3*n); dalloc(S_.radius, n);
-	dalloc(S_.vel, 3*n); dalloc(S_.ang, 3*n); dalloc(S_.vel_pred, 3*n); dalloc(S_.ang_pred, 3*n);
-	dalloc(S_.u_inf, 3*n); dalloc(S_.na, 6*n);
-	dalloc(S_.vc, (size_t)NFC*6*n); dalloc(S_.fc, (size_t)NFC*6*n);
-	dalloc(S_.rhs, (size_t)NFC*6*n); dalloc(S_.sol, (size_t)NFC*6*n);
-	dalloc(S_.sc, (size_t)NSC*6*n); dalloc(S_.sc_tot, (size_t)NSC*6+12*(size_t)n);
-	dalloc(S_.row_ptr, n+1); dalloc(S_.col_ptr, n+1);
-	dalloc(d_err_, 1);
+	dalloc(S_.clock, 1, st_);
+	dalloc(S_.pos, 3*n, st_); dalloc(S_.radius, n, st_);
+	dalloc(S_.vel, 3*n, st_); dalloc(S_.ang, 3*n, st_); dalloc(S_.vel_pred, 3*n, st_); dalloc(S_.ang_pred, 3*n, st_);
+	dalloc(S_.u_inf, 3*n, st_); dalloc(S_.na, 6*n, st_);
+	dalloc(S_.vc, (size_t)NFC*6*n, st_); dalloc(S_.fc, (size_t)NFC*6*n, st_);
+	dalloc(S_.rhs, (size_t)NFC*6*n, st_); dalloc(S_.sol, (size_t)NFC*6*n, st_);
+	dalloc(S_.sc, (size_t)NSC*6*n, st_); dalloc(S_.sc_tot, (size_t)NSC*6+12*(size_t)n, st_);
+	dalloc(S_.row_ptr, n+1, st_); dalloc(S_.col_ptr, n+1, st_);
+	dalloc(d_err_, 1, st_);
 	LFG_CUDA(cudaMallocHost((void **)&h_clock_, sizeof(DevClock)));
 	LFG_CUDA(cudaMallocHost((void **)&h_err_, sizeof(int)));
 	LFG_CUDA(cudaMemcpyAsync(S_.pos, pos, sizeof(double)*3*n, cudaMemcpyHostToDevice, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
@@ -178,8 +182,8 @@ Sim::Sim(const lfg_params &p, const lfg_options &o, int n, const double *pos, co
 	S_.brute = (S_.ncx < 3 || S_.ncz < 3 || (!S_.P.twodim && S_.ncy < 3)) ? 1 : 0;
 	S_.csx = lx/S_.ncx; S_.csy = S_.P.twodim ? 1.0 : ly/S_.ncy; S_.csz = lz/S_.ncz;
 	int ncell = S_.ncx*S_.ncy*S_.ncz;
-	dalloc(S_.cell_of, n); dalloc(S_.cell_count, ncell); dalloc(S_.cell_start, ncell+1); dalloc(S_.cell_list, n);
-	dalloc(S_.cand_count, std::max(n, ncell)); dalloc(S_.cand_ptr, n+1);
+	dalloc(S_.cell_of, n, st_); dalloc(S_.cell_count, ncell, st_); dalloc(S_.cell_start, ncell+1, st_); dalloc(S_.cell_list, n, st_);
+	dalloc(S_.cand_count, std::max(n, ncell), st_); dalloc(S_.cand_ptr, n+1, st_);
 	solver_ = new Solver(n, opt_, st_);
 	h_pos_.assign(pos, pos+3*n);
 	rebuild_superset();
@@ -224,13 +228,13 @@ void Sim::rebuild_superset()
 		if (S_.pair_scratch) cudaFree(S_.pair_scratch);
 		if (S_.col_idx) cudaFree(S_.col_idx);
 		S_.pconst = nullptr; S_.blk_scratch = S_.pair_scratch = nullptr; S_.col_idx = nullptr;
-		dalloc(S_.pconst, S_.cap);
-		dalloc(S_.blk_scratch, (size_t)30*S_.cap);
-		dalloc(S_.pair_scratch, (size_t)12*NSC*S_.cap);
-		dalloc(S_.col_idx, S_.cap);
+		dalloc(S_.pconst, S_.cap, st_);
+		dalloc(S_.blk_scratch, (size_t)30*S_.cap, st_);
+		dalloc(S_.pair_scratch, (size_t)12*NSC*S_.cap, st_);
+		dalloc(S_.col_idx, S_.cap, st_);
 	}
 	DPair *fresh = nullptr;
-	dalloc(fresh, S_.cap);
+	dalloc(fresh, S_.cap, st_);
 	S_.pairs = fresh;
 	phys_merge_pairs(S_, old, old_row, old_n, st_);
 	LFG_CUDA(cudaMemcpyAsync(S_.row_ptr, S_.cand_ptr, sizeof(int)*(S_.n+1), cudaMemcpyDeviceToDevice, st_));
@@ -416,7 +420,15 @@ void Sim::check_error()
 
 void Sim::advance(double time_end, double strain_end)
 {
-	// System::timeEvolution loop and final stress step (System.cpp:1227-1279)
+	while (!advance_partial(time_end, strain_end, 1 << 30))
+		if (error_code) return;
+}
+
+// System::timeEvolution loop and final stress step (System.cpp:1227-1279),
+// resumable: at most max_steps loop steps; returns true once the end was
+// reached and the final stress-computing step has run
+bool Sim::advance_partial(double time_end, double strain_end, int max_steps)
+{
 	first_time();
 	pull_clock();
 	double adj = prm_.fixed_dt ? prm_.dt : 0;
@@ -425,11 +437,13 @@ void Sim::advance(double time_end, double strain_end)
 		if (h_clock_->time > te-1e-8 && te >= 0) return false;
 		return true;
 	};
-	while (keep(time_end-adj, strain_end-adj)) {
+	for (int k = 0; k < max_steps && keep(time_end-adj, strain_end-adj); k++) {
 		step(0, time_end, strain_end);
-		if (error_code) return;
+		if (error_code) return false;
 	}
+	if (keep(time_end-adj, strain_end-adj)) return false;
 	step(1, time_end, strain_end);
+	return error_code == 0;
 }
 
 void Sim::scalars(lfg_sim_scalars *o)
@@ -651,6 +665,19 @@ void Sim::force_component_noalloc(int comp, double *d_out, int device)
 	LFG_CUDA(cudaStreamSynchronize(st_));
 }
 
+// device memory held by this suspension: fronts (the dominant term), pair
+// records and their scratch, per-particle vectors, the compact R_FU values
+int64_t Sim::device_bytes() const
+{
+	lfg_solver_stats ss;
+	solver_->stats(&ss);
+	int64_t pair = sizeof(DPair)+sizeof(DPairConst)+sizeof(double)*(30+12*NSC)+2*sizeof(int);
+	int64_t part = sizeof(double)*(3*7+6*(1+4*NFC+NSC)+15)+sizeof(int)*8;
+	int64_t w = opt_.precision == LFG_PREC_FP64 ? 8 : 4;
+	int64_t sol = (int64_t)6*S_.n*4*w*4 + (int64_t)18*8*S_.cap;
+	return ss.front_bytes+(int64_t)S_.cap*pair+(int64_t)S_.n*part+sol;
+}
+
 void Sim::timing(lfg_sim_timing *o) const
 {
 	std::memset(o, 0, sizeof *o);
@@ -730,6 +757,18 @@ int lfg_sim_advance(lfg_sim *h, double time_end, double strain_end, lfg_status *
 	SIM_GUARD_BEGIN
 	cudaSetDevice(h->device);
 	h->s->advance(time_end, strain_end);
+	return sim_status(h, st);
+	SIM_GUARD_END
+}
+
+int lfg_sim_advance_partial(lfg_sim *h, double time_end, double strain_end, int max_steps, int *done,
+                            lfg_status *st)
+{
+	if (!h || max_steps < 0) return fail(st, LFG_ERR_BAD_ARG, 0, "bad arguments");
+	SIM_GUARD_BEGIN
+	cudaSetDevice(h->device);
+	bool d = h->s->advance_partial(time_end, strain_end, max_steps);
+	if (done) *done = d ? 1 : 0;
 	return sim_status(h, st);
 	SIM_GUARD_END
 }
@@ -870,6 +909,22 @@ int lfg_sim_force_component_noalloc(lfg_sim *h, int comp, double *d_out, lfg_sta
 	h->s->force_component_noalloc(comp, d_out, h->device);
 	return ok(st);
 	SIM_GUARD_END
+}
+
+int lfg_sim_set_leaf_size(lfg_sim *h, int leaf_size, lfg_status *st)
+{
+	if (!h || leaf_size < 1) return fail(st, LFG_ERR_BAD_ARG, leaf_size, "bad arguments");
+	SIM_GUARD_BEGIN
+	LFG_CUDA(cudaSetDevice(h->device));
+	h->s->set_leaf_size(leaf_size);
+	return ok(st);
+	SIM_GUARD_END
+}
+
+int64_t lfg_sim_device_bytes(lfg_sim *h)
+{
+	if (!h) return 0;
+	try { return h->s->device_bytes(); } catch (...) { return 0; }
 }
 
 int lfg_sim_get_timing(lfg_sim *h, lfg_sim_timing *o)

@@ -53,6 +53,10 @@ void Solver::set_pattern(int nb, const int32_t *row, const int32_t *col, const d
 		if (r[e] <= c[e] || r[e] >= n_ || c[e] < 0)
 			throw Error{LFG_ERR_BAD_ARG, e, "off-diagonal block must have n > row > col >= 0"};
 	nb_ = nb;
+	pat_r_ = r;
+	pat_c_ = c;
+	pat_pos_.assign(pos ? pos : nullptr, pos ? pos+3*(size_t)n_ : nullptr);
+	pat_box_[0] = lx; pat_box_[1] = ly; pat_box_[2] = lz;
 	symbolic_analyze(S_, n_, nb, r.data(), c.data(), pos, lx, ly, lz, opt_.leaf_size);
 	dev_symbolic_upload(D_, S_, nb, factor_panel_width(opt_.precision), factor_tile_size(opt_.precision),
 	                    factor_syrk_tile_size(opt_.precision), st_);
@@ -92,6 +96,17 @@ void Solver::set_pattern(int nb, const int32_t *row, const int32_t *col, const d
 	graphs_.clear();
 	analyzed_ = true;
 	symbolic_runs_++;
+}
+
+void Solver::reanalyze(int leaf_size)
+{
+	if (!analyzed_) throw Error{LFG_ERR_BAD_ARG, 0, "reanalyze before the first analysis"};
+	if (leaf_size < 1) throw Error{LFG_ERR_BAD_ARG, leaf_size, "leaf size must be positive"};
+	opt_.leaf_size = leaf_size;
+	std::vector<int32_t> r = pat_r_, c = pat_c_;
+	std::vector<double> pos = pat_pos_;
+	set_pattern(nb_, r.data(), c.data(), pos.empty() ? nullptr : pos.data(), pat_box_[0], pat_box_[1], pat_box_[2],
+	            false);
 }
 
 void Solver::set_values_host(const double *dblocks, const double *odblocks)

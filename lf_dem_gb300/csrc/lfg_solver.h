@@ -14,6 +14,9 @@ public:
 	void set_pattern(int nb, const int32_t *row, const int32_t *col, const double *pos, double lx,
 	                 double ly, double lz, bool device_ptrs);
 	void set_values_host(const double *dblocks, const double *odblocks);
+	// re-run the symbolic analysis of the current pattern with another
+	// nested-dissection leaf size (the batch autotuner's knob)
+	void reanalyze(int leaf_size);
 	// device arrays of the compact values (dblocks n x 15, odblocks nb x 18)
 	double *d_dblocks() { return A_.dblocks; }
 	double *d_odblocks() { return A_.odblocks; }
@@ -64,6 +67,9 @@ private:
 	double *hb_ = nullptr, *hx_ = nullptr;
 	int64_t hcap_ = 0;
 	std::vector<GraphEntry> graphs_;
+	std::vector<int32_t> pat_r_, pat_c_;   // the analysed pattern (for reanalyze)
+	std::vector<double> pat_pos_;
+	double pat_box_[3] = {0, 0, 0};
 	int last_iters_ = 0;
 	double last_resid_ = 0;
 	int launches_factor_ = 0, launches_solve_ = 0;
