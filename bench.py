@@ -10,6 +10,7 @@ public dataset).  One step = one full predictor-corrector time step
 shear-rate solve each half step).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+  python bench.py --workload sweep|serve     (the batched and serving forms)
 
 value        : particle-steps/s of the FP32 + FP64-refinement form, device time
                (CUDA events on the engine's stream), state resident in HBM
@@ -225,6 +226,128 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def _gen_packing(args):
+    from lf_dem_gb300 import packing as PK
+    n, vf, seed = args
+    return PK.generate(n, vf, seed=seed)
+
+
+def gen_packings(specs):
+    """Seeded packings, generated in a spawn pool before any GPU call."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(min(16, os.cpu_count() or 1)) as pool:
+        return pool.map(_gen_packing, specs)
+
+
+def rate_params(rate):
+    p = workload_params()
+    p.update(friction_model=1, critical_load=0.0, repulsion_on=1, repulsion=1.0, control=0, shear_rate=rate,
+             target_stress=0.0)
+    return p
+
+
+def stress_params(sigma_cl):
+    p = workload_params()
+    p.update(target_stress=sigma_cl / 6 / np.pi)
+    return p
+
+
+def bench_sweep(args):
+    """Batched rheology sweep: 64 independent 3D suspensions, N ~ U[256, 2048],
+    phi ~ U[0.45, 0.58], rate control with shear rates log-spaced 1e-2..1e2
+    (repulsive-force units), bidisperse 1:1.4, FP32 + refinement, advanced
+    together by one lfg_batch; leaf sizes picked by the autotuner.  Aggregate
+    particle-steps/s over K steps of every suspension, against the same batch
+    driven by one host thread (suspensions one after another)."""
+    rng = np.random.default_rng(4000)
+    m = args.count or 64
+    ns = rng.integers(256, 2049, size=m)
+    vfs = rng.uniform(0.45, 0.58, size=m)
+    rates = np.logspace(-2, 2, m)
+    packs = gen_packings([(int(n), float(v), 4000 + k) for k, (n, v) in enumerate(zip(ns, vfs))])
+    import lf_dem_gb300 as E
+    from lf_dem_gb300 import build as B
+    B.build()
+    E.load()
+    out = {}
+    for label, threads in (("concurrent", 16), ("one_thread", 1)):
+        b = E.Batch(nthreads=threads)
+        for p, r in zip(packs, rates):
+            b.add(rate_params(float(r)), p.position, p.radius, p.lx, p.ly, p.lz, precision=E.PREC_FP32_REFINE)
+        if label == "concurrent":
+            t0 = time.perf_counter()
+            b.autotune((8, 16, 32), steps=1)
+            out["autotune_s"] = time.perf_counter() - t0
+            out["tuned_leaf"] = {str(n): b.tuned_leaf(n, 1) for n in (256, 512, 1024, 2048)}
+        b.run(args.warmup)
+        t0 = time.perf_counter()
+        b.run(args.steps)
+        wall = time.perf_counter() - t0
+        out[label] = {"particle_steps_per_s": float(ns.sum()) * args.steps / wall, "wall_s": wall,
+                      "host_threads": threads}
+        b.close()
+    line = {"metric": "aggregate particle-steps/s, batched sweep", "workload": "sweep",
+            "value": out["concurrent"]["particle_steps_per_s"], "unit": "particle-steps/s",
+            "steps": args.steps, "warmup": args.warmup, "dtype": "f32+f64refine", "data": "synthetic",
+            "config": {"suspensions": m, "n_range": [256, 2048], "phi_range": [0.45, 0.58],
+                       "shear_rates": "log-spaced 1e-2..1e2 (repulsive-force units)", "control": "rate",
+                       "total_particles": int(ns.sum()),
+                       "note": "fixed step count per suspension instead of 2 strain units"},
+            **out}
+    line["speedup_vs_one_thread"] = out["concurrent"]["particle_steps_per_s"] / out["one_thread"]["particle_steps_per_s"]
+    print(json.dumps(line), flush=True)
+
+
+def bench_serve(args):
+    """Serving stream: R requests with Poisson arrivals (mean 50 ms), N
+    log-uniform in [200, 16384], phi ~ U[0.45, 0.58], stress control with sigma
+    log-uniform in [0.3, 100] cl, seeded packings, FP32 + refinement, each run
+    to a strain target; admission by estimated factor footprint.  Reports p50
+    / p99 time-to-strain (submit to done) and aggregate particle-steps/s."""
+    rng = np.random.default_rng(5000)
+    m = args.count or 48
+    ns = np.exp(rng.uniform(np.log(200), np.log(16384), size=m)).astype(int)
+    vfs = rng.uniform(0.45, 0.58, size=m)
+    sig = np.exp(rng.uniform(np.log(0.3), np.log(100.0), size=m))
+    arrivals = np.cumsum(rng.exponential(0.05, size=m))
+    packs = gen_packings([(int(n), float(v), 5000 + k) for k, (n, v) in enumerate(zip(ns, vfs))])
+    import lf_dem_gb300 as E
+    from lf_dem_gb300 import build as B
+    B.build()
+    E.load()
+    budget = int(args.hbm_budget_gb * 1e9)
+    srv = E.Server(max_active=args.max_active, hbm_budget_bytes=budget)
+    t0 = time.perf_counter()
+    for k in range(m):
+        delay = arrivals[k] - (time.perf_counter() - t0)
+        if delay > 0:
+            time.sleep(delay)
+        p = packs[k]
+        srv.submit(k, stress_params(float(sig[k])), p.position, p.radius, p.lx, p.ly, p.lz,
+                   strain_end=args.strain, precision=E.PREC_FP32_REFINE)
+    srv.wait()
+    res = srv.poll(cap=m + 8)
+    st = srv.stats()
+    srv.close()
+    bad = [r for r in res if r.status != 0]
+    tts = np.array([r.t_done - r.t_submit for r in res if r.status == 0])
+    queue = np.array([r.t_admit - r.t_submit for r in res if r.status == 0])
+    span = max(r.t_done for r in res) - min(r.t_submit for r in res)
+    psteps = sum(r.n * r.steps for r in res if r.status == 0)
+    line = {"metric": "time-to-strain p50/p99 and aggregate particle-steps/s, serving stream", "workload": "serve",
+            "value": float(psteps / span), "unit": "particle-steps/s",
+            "p50_time_to_strain_s": float(np.percentile(tts, 50)), "p99_time_to_strain_s": float(np.percentile(tts, 99)),
+            "p50_queue_s": float(np.percentile(queue, 50)), "p99_queue_s": float(np.percentile(queue, 99)),
+            "dtype": "f32+f64refine", "data": "synthetic", "failed": len(bad),
+            "config": {"requests": m, "arrivals": "Poisson, mean 50 ms", "n_range": [200, 16384],
+                       "phi_range": [0.45, 0.58], "sigma_cl_range": [0.3, 100], "strain_end": args.strain,
+                       "max_active": args.max_active, "hbm_budget_gb": args.hbm_budget_gb,
+                       "note": f"strain target {args.strain} instead of 1 strain unit"},
+            "server": st, "total_steps": int(sum(r.steps for r in res)), "span_s": span}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -236,7 +359,19 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="profiling driver: FP32 form only, W + K steps, no measurement (for ncu)")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"], help="form used by --profile")
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "sweep", "serve"],
+                    help="cfg2: the metric's workload (default); sweep / serve: the batched and serving forms")
+    ap.add_argument("--count", type=int, default=0, help="suspensions (sweep) or requests (serve)")
+    ap.add_argument("--strain", type=float, default=0.002, help="serve: strain target of each request")
+    ap.add_argument("--max-active", type=int, default=8, help="serve: concurrent requests")
+    ap.add_argument("--hbm-budget-gb", type=float, default=200.0, help="serve: device bytes for admission")
     args = ap.parse_args()
+    if args.workload == "sweep":
+        bench_sweep(args)
+        return
+    if args.workload == "serve":
+        bench_serve(args)
+        return
     if args.profile:
         import lf_dem_gb300 as E
         from lf_dem_gb300 import packing as PK
@@ -245,9 +380,12 @@ def main():
         prec = E.PREC_FP32_REFINE if args.precision == "fp32" else E.PREC_FP64
         g = E.Sim(workload_params(), pk.position, pk.radius, pk.lx, pk.ly, pk.lz, precision=prec)
         g.run(args.warmup)
+        g.clear_step_times()
         g.run(args.steps)
         ms, kern = g.step_times()
-        print(json.dumps({"profile_steps_ms": [float(x) for x in ms], "kernels": kern}))
+        t = g.timing()
+        print(json.dumps({"profile_steps_ms": [float(x) for x in ms], "kernels_in_timed_steps": kern,
+                          "factor_flops": t["factor_flops"], "solve_bytes": t["solve_bytes"]}))
         return
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
