@@ -179,17 +179,35 @@ def cpu_baseline(packing, nsteps=1):
                       f"FP64 block Cholesky (minimum degree) with OpenMP, {t1 - t0:.1f} s"}
 
 
-def dist_setup():
+def dist_setup(backend="nccl"):
+    """Ranks from the torchrun environment.  Each rank runs an independent
+    replica (one suspension per GPU); the process group only carries the
+    barrier and the max-over-ranks of the timed region."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
         return world, rank, local, dist, torch
     return world, rank, local, None, None
+
+
+def max_over_ranks(value, dist, torch, device):
+    """The slowest rank's time (weak scaling: every rank times its own replica)."""
+    if dist is None:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(n_particles, steps, world, slowest_s):
+    """Whole-job particle-steps/s: all ranks' particle-steps over the slowest rank's time."""
+    return n_particles * steps * world / slowest_s
 
 
 def reference_arm(args):
@@ -410,12 +428,8 @@ def main():
     sampler.start()
     ms32, kern32, tim32, sc32 = run_engine(E, pk, E.PREC_FP32_REFINE, args.steps, args.warmup, local)
     clocks = sampler.stop()
-    total32 = float(np.sum(ms32)) / 1e3
-    if dist is not None:
-        t = torch.tensor([total32], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total32 = float(t.item())
-    value = N_PART * args.steps * world / total32
+    total32 = max_over_ranks(float(np.sum(ms32)) / 1e3, dist, torch, f"cuda:{local}")
+    value = replica_value(N_PART, args.steps, world, total32)
     res = {}
     if not args.no_fp64:
         ms64, kern64, tim64, sc64 = run_engine(E, pk, E.PREC_FP64, max(3, args.steps // 2), args.warmup, local)
