@@ -33,12 +33,15 @@ namespace lfg {
 enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLAN_SYRK = 5,
        PLAN_DIAG = 6 };
 constexpr int PANEL_ROWS = 128;  // rows per panel (k_trsm) task (must match the plan)
+constexpr int SOLVE_WARPS = 8;
+constexpr int SOLVE_CB = 8;      // columns per CTA of the solve's column kernels
+constexpr int SOLVE_JC = 256;    // columns per chunk of the solve's row kernels
 
 template <typename T> struct Cfg;
 // NB: panel width; TILE/TPT: trailing-update tile edge / outputs per thread
 // per dimension; STILE/STPT: the same for the deep-K Schur complement SYRK
 template <> struct Cfg<double> { static constexpr int NB = 32, TILE = 64, TPT = 4, STILE = 64, STPT = 4; };
-template <> struct Cfg<float>  { static constexpr int NB = 64, TILE = 64, TPT = 4, STILE = 128, STPT = 8; };
+template <> struct Cfg<float>  { static constexpr int NB = 32, TILE = 64, TPT = 4, STILE = 128, STPT = 8; };
 
 // ---------------------------------------------------------------------------
 // compact blocks -> dense (StokesSolver.cpp:154-231), m[r*6+c]
@@ -515,9 +518,6 @@ __global__ void __launch_bounds__(256) k_syrk(const int4 *__restrict__ tasks, co
 // ---------------------------------------------------------------------------
 // allocation and launch
 // ---------------------------------------------------------------------------
-template <typename T> static void set_smem_limits(int maxn6);
-template <typename T> static std::atomic<int> &bwdz_cap_ref() { static std::atomic<int> v{48*1024}; return v; }
-template <typename T> static int bwdz_smem_cap() { return bwdz_cap_ref<T>(); }
 
 
 template <typename T> static size_t update_smem() { return 2*sizeof(T)*Cfg<T>::NB*Cfg<T>::TILE; }
@@ -562,8 +562,15 @@ template <typename T> void factor_alloc(DevFactor<T> &F, const DevSymbolic &D, i
 		LFG_CUDA(cudaMalloc((void **)&F.linv, sizeof(T)*lneed));
 		F.linv_cap = lneed;
 	}
+	F.pstride = std::max<int64_t>(D.w_elems, (int64_t)6*D.nblk);
+	int64_t pneed = (int64_t)kmax*((D.max_n6+SOLVE_JC-1)/SOLVE_JC)*F.pstride;
+	if (F.part_cap < pneed) {
+		if (F.part) cudaFree(F.part);
+		F.part = nullptr;
+		LFG_CUDA(cudaMalloc((void **)&F.part, sizeof(T)*pneed));
+		F.part_cap = pneed;
+	}
 	if (!F.status) LFG_CUDA(cudaMalloc((void **)&F.status, sizeof(int)*4));
-	set_smem_limits<T>(D.max_n6);
 	set_update_smem<T>();
 }
 
@@ -575,6 +582,7 @@ template <typename T> void factor_free(DevFactor<T> &F)
 	if (F.yp) cudaFree(F.yp);
 	if (F.status) cudaFree(F.status);
 	if (F.linv) cudaFree(F.linv);
+	if (F.part) cudaFree(F.part);
 	F = DevFactor<T>();
 }
 
@@ -662,8 +670,6 @@ __global__ void k_permute_out(int n, int k, const int *__restrict__ iperm, const
 // factor load is a coalesced 128-byte line; the column-oriented products
 // (k_fwd_y, k_bwd_z) use one warp per output column.  Sums over children and
 // warps run in a fixed order: results are bitwise reproducible.
-constexpr int SOLVE_OUT = 32;   // outputs per CTA
-constexpr int SOLVE_WARPS = 8;
 
 template <typename T, int K>
 __global__ void __launch_bounds__(256) k_fwd_gather(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
@@ -701,159 +707,104 @@ __global__ void __launch_bounds__(256) k_fwd_gather(const int *__restrict__ lev_
 	}
 }
 
-// y_j = sum_{i <= j} E[i][j] v_i, one warp per column j
-template <typename T, int K>
-__global__ void __launch_bounds__(256) k_fwd_y(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
-                        const int *__restrict__ sn_n, const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
-                        const int64_t *__restrict__ sn_off, const T *__restrict__ arena,
-                        const T *__restrict__ xp, T *__restrict__ yp, int n6tot)
+// Column products: one supernode per blockIdx.y, SOLVE_CB columns per
+// blockIdx.x; the 8 warps split the rows (each thread reads its row's
+// right-hand-side values once for all the CTA's columns) and the partial sums
+// meet in shared memory in a fixed order.
+//  MODE 0 (forward):  y_j  = sum_{i <= j} E[i][j] x_i      (E = L11^-T)
+//  MODE 1 (backward): z_j -= sum_t L21[t][j] x[rows(t)]    (z in yp)
+template <typename T, int K, int MODE>
+__global__ void __launch_bounds__(256) k_solve_cols(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
+                                                    const int *__restrict__ sn_n, const int *__restrict__ sn_m,
+                                                    const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
+                                                    const int *__restrict__ sn_rows_off,
+                                                    const int *__restrict__ rows, const T *__restrict__ arena,
+                                                    const T *__restrict__ xp, T *__restrict__ yp, int n6tot)
 {
-	int s = lev_sn[blockIdx.y];
-	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
-	int warp = threadIdx.x/32, lane = threadIdx.x%32;
-	int f6 = 6*sn_first[s];
-	const T *E = arena+sn_off[s]+F6;
-	for (int j = blockIdx.x*SOLVE_OUT+warp; j < min(n6, (blockIdx.x+1)*SOLVE_OUT); j += SOLVE_WARPS) {
-		const T *col = E+(int64_t)j*ld;
-		T acc[K];
-#pragma unroll
-		for (int q = 0; q < K; q++) acc[q] = 0;
-		for (int i = lane; i <= j; i += 32) {
-			T e = col[i];
-#pragma unroll
-			for (int q = 0; q < K; q++) acc[q] += e*xp[(int64_t)q*n6tot+f6+i];
-		}
-#pragma unroll
-		for (int q = 0; q < K; q++) {
-			T a = acc[q];
-			for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-			if (lane == 0) yp[(int64_t)q*n6tot+f6+j] = a;
-		}
-	}
-}
-
-// w_t -= sum_j L[n6+t][j] y_j: lanes own 32 consecutive rows, warps split j
-template <typename T, int K>
-__global__ void __launch_bounds__(256) k_fwd_w(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
-                        const int *__restrict__ sn_n, const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
-                        const int64_t *__restrict__ sn_off, const int64_t *__restrict__ sn_woff,
-                        const T *__restrict__ arena, T *__restrict__ w, int64_t wstride,
-                        const T *__restrict__ yp, int n6tot)
-{
-	__shared__ T red[SOLVE_WARPS][K][32];
+	__shared__ T red[SOLVE_WARPS][SOLVE_CB][K];
 	int s = lev_sn[blockIdx.y];
 	int n6 = 6*sn_n[s], m6 = 6*sn_m[s], ld = sn_ld[s];
-	int t0 = blockIdx.x*32;
-	if (t0 >= m6) return;
-	int warp = threadIdx.x/32, lane = threadIdx.x%32;
-	int t = t0+lane;
+	int j0 = blockIdx.x*SOLVE_CB;
+	if (j0 >= n6 || (MODE == 1 && m6 == 0)) return;
+	int jn = min(SOLVE_CB, n6-j0);
 	int f6 = 6*sn_first[s];
-	const T *L = arena+sn_off[s]+n6;   // row n6 of column 0
-	T acc[K];
-#pragma unroll
-	for (int q = 0; q < K; q++) acc[q] = 0;
-	if (t < m6) {
-		for (int j = warp; j < n6; j += SOLVE_WARPS) {
-			T l = L[(int64_t)j*ld+t];
-#pragma unroll
-			for (int q = 0; q < K; q++) acc[q] += l*yp[(int64_t)q*n6tot+f6+j];
-		}
-	}
-#pragma unroll
-	for (int q = 0; q < K; q++) red[warp][q][lane] = acc[q];
-	__syncthreads();
-	if (warp == 0 && t < m6) {
-		int64_t d = sn_woff[s]+t;
-#pragma unroll
-		for (int q = 0; q < K; q++) {
-			T a = 0;
-			for (int u = 0; u < SOLVE_WARPS; u++) a += red[u][q][lane];
-			w[q*wstride+d] -= a;
-		}
-	}
-}
-
-// z_j = y_j - sum_t L[n6+t][j] x[rows(t)], one warp per column j (z -> yp).
-// The CTA first gathers x at the supernode's rows into shared memory
-// (dynamic, K * 6m values) when it fits, otherwise reads them from global.
-template <typename T, int K>
-__global__ void __launch_bounds__(256) k_bwd_z(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
-                        const int *__restrict__ sn_n, const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
-                        const int64_t *__restrict__ sn_off, const int *__restrict__ sn_rows_off,
-                        const int *__restrict__ rows, const T *__restrict__ arena, const T *__restrict__ xp,
-                        T *__restrict__ yp, int n6tot, int smem_cap)
-{
-	extern __shared__ unsigned char smem_bz[];
-	T *xr = reinterpret_cast<T *>(smem_bz);
-	int s = lev_sn[blockIdx.y];
-	int n6 = 6*sn_n[s], m6 = 6*sn_m[s], ld = sn_ld[s];
-	if (m6 == 0) return;
-	int j0 = blockIdx.x*SOLVE_OUT;
-	if (j0 >= n6) return;
-	int warp = threadIdx.x/32, lane = threadIdx.x%32;
-	int f6 = 6*sn_first[s];
-	const T *L = arena+sn_off[s]+n6;
+	const T *M = arena+sn_off[s]+(MODE == 0 ? n6+m6 : n6)+(int64_t)j0*ld;
 	const int *R = rows+sn_rows_off[s];
-	bool staged = K*m6 <= smem_cap;
-	if (staged) {
-		for (int t = threadIdx.x; t < m6; t += blockDim.x) {
-			int g = 6*R[t/6]+t%6;
+	int nrow = MODE == 0 ? j0+jn : m6;
+	T acc[SOLVE_CB][K];
 #pragma unroll
-			for (int q = 0; q < K; q++) xr[q*m6+t] = xp[(int64_t)q*n6tot+g];
+	for (int c = 0; c < SOLVE_CB; c++)
+#pragma unroll
+		for (int q = 0; q < K; q++) acc[c][q] = 0;
+	for (int i = threadIdx.x; i < nrow; i += blockDim.x) {
+		int64_t g = MODE == 0 ? f6+i : 6*R[i/6]+i%6;
+		T v[K];
+#pragma unroll
+		for (int q = 0; q < K; q++) v[q] = xp[(int64_t)q*n6tot+g];
+#pragma unroll
+		for (int c = 0; c < SOLVE_CB; c++) {
+			if (c >= jn || (MODE == 0 && i > j0+c)) continue;
+			T e = M[(int64_t)c*ld+i];
+#pragma unroll
+			for (int q = 0; q < K; q++) acc[c][q] += e*v[q];
 		}
-		__syncthreads();
 	}
-	for (int j = j0+warp; j < min(n6, j0+SOLVE_OUT); j += SOLVE_WARPS) {
-		const T *col = L+(int64_t)j*ld;
-		T acc[K];
+	int warp = threadIdx.x/32, lane = threadIdx.x%32;
 #pragma unroll
-		for (int q = 0; q < K; q++) acc[q] = 0;
-		if (staged) {
-			for (int t = lane; t < m6; t += 32) {
-				T l = col[t];
-#pragma unroll
-				for (int q = 0; q < K; q++) acc[q] += l*xr[q*m6+t];
-			}
-		} else {
-			for (int t = lane; t < m6; t += 32) {
-				T l = col[t];
-				int g = 6*R[t/6]+t%6;
-#pragma unroll
-				for (int q = 0; q < K; q++) acc[q] += l*xp[(int64_t)q*n6tot+g];
-			}
-		}
+	for (int c = 0; c < SOLVE_CB; c++)
 #pragma unroll
 		for (int q = 0; q < K; q++) {
-			T a = acc[q];
+			T a = acc[c][q];
 			for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-			if (lane == 0) yp[(int64_t)q*n6tot+f6+j] -= a;
+			if (lane == 0) red[warp][c][q] = a;
+		}
+	__syncthreads();
+	if (threadIdx.x < SOLVE_CB*K) {
+		int c = threadIdx.x/K, q = threadIdx.x%K;
+		if (c < jn) {
+			T a = 0;
+			for (int u = 0; u < SOLVE_WARPS; u++) a += red[u][c][q];
+			T *o = yp+(int64_t)q*n6tot+f6+j0+c;
+			if (MODE == 0) *o = a;
+			else *o -= a;
 		}
 	}
 }
 
-// x_i = sum_{j >= i} E[i][j] z_j: lanes own 32 consecutive rows, warps split j
-template <typename T, int K>
-__global__ void __launch_bounds__(256) k_bwd_x(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
-                        const int *__restrict__ sn_n, const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
-                        const int64_t *__restrict__ sn_off, const T *__restrict__ arena,
-                        const T *__restrict__ yp, T *__restrict__ xp, int n6tot)
+// Row products: 32 rows per blockIdx.x (lanes), SOLVE_JC columns per
+// blockIdx.z (the 8 warps split them).  With one chunk the result is applied
+// directly; otherwise every chunk writes its partial sums (zeros for an empty
+// chunk) and k_solve_rowsum adds them in chunk order.
+//  MODE 0 (forward):  w_t -= sum_j L21[t][j] y_j        (t < 6m; w at sn_woff)
+//  MODE 1 (backward): x_i  = sum_{j >= i} E[i][j] z_j    (i < 6n; z in yp)
+template <typename T, int K, int MODE>
+__global__ void __launch_bounds__(256) k_solve_rows(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
+                                                    const int *__restrict__ sn_n, const int *__restrict__ sn_m,
+                                                    const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
+                                                    const int64_t *__restrict__ sn_woff, const T *__restrict__ arena,
+                                                    T *__restrict__ w, int64_t wstride, const T *__restrict__ yp,
+                                                    T *__restrict__ xp, int n6tot, T *__restrict__ part,
+                                                    int64_t pstride, int nchunk)
 {
 	__shared__ T red[SOLVE_WARPS][K][32];
 	int s = lev_sn[blockIdx.y];
-	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
-	int i0 = blockIdx.x*32;
-	if (i0 >= n6) return;
+	int n6 = 6*sn_n[s], m6 = 6*sn_m[s], ld = sn_ld[s];
+	int nrows = MODE == 0 ? m6 : n6;
+	int r0 = blockIdx.x*32;
+	if (r0 >= nrows) return;
 	int warp = threadIdx.x/32, lane = threadIdx.x%32;
-	int i = i0+lane;
 	int f6 = 6*sn_first[s];
-	const T *E = arena+sn_off[s]+F6;
+	int jlo = (MODE == 0 ? 0 : r0)+blockIdx.z*SOLVE_JC;
+	int jhi = min(n6, jlo+SOLVE_JC);
+	const T *M = arena+sn_off[s]+(MODE == 0 ? n6 : n6+m6);
+	int r = r0+lane;
 	T acc[K];
 #pragma unroll
 	for (int q = 0; q < K; q++) acc[q] = 0;
-	if (i < n6) {
-		for (int j = i0+warp; j < n6; j += SOLVE_WARPS) {
-			if (j < i) continue;
-			T e = E[(int64_t)j*ld+i];
+	if (r < nrows) {
+		for (int j = jlo+warp; j < jhi; j += SOLVE_WARPS) {
+			if (MODE == 1 && j < r) continue;
+			T e = M[(int64_t)j*ld+r];
 #pragma unroll
 			for (int q = 0; q < K; q++) acc[q] += e*yp[(int64_t)q*n6tot+f6+j];
 		}
@@ -861,13 +812,39 @@ __global__ void __launch_bounds__(256) k_bwd_x(const int *__restrict__ lev_sn, c
 #pragma unroll
 	for (int q = 0; q < K; q++) red[warp][q][lane] = acc[q];
 	__syncthreads();
-	if (warp == 0 && i < n6) {
+	if (warp == 0 && r < nrows) {
+		int64_t row = MODE == 0 ? sn_woff[s]+r : (int64_t)f6+r;
 #pragma unroll
 		for (int q = 0; q < K; q++) {
 			T a = 0;
 			for (int u = 0; u < SOLVE_WARPS; u++) a += red[u][q][lane];
-			xp[(int64_t)q*n6tot+f6+i] = a;
+			if (nchunk == 1) {
+				if (MODE == 0) w[q*wstride+row] -= a;
+				else xp[(int64_t)q*n6tot+row] = a;
+			} else {
+				part[((int64_t)q*nchunk+blockIdx.z)*pstride+row] = a;
+			}
 		}
+	}
+}
+
+template <typename T, int K, int MODE>
+__global__ void k_solve_rowsum(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
+                               const int *__restrict__ sn_n, const int *__restrict__ sn_m,
+                               const int64_t *__restrict__ sn_woff, T *__restrict__ w, int64_t wstride,
+                               T *__restrict__ xp, int n6tot, const T *__restrict__ part, int64_t pstride, int nchunk)
+{
+	int s = lev_sn[blockIdx.y];
+	int nrows = MODE == 0 ? 6*sn_m[s] : 6*sn_n[s];
+	int r = blockIdx.x*blockDim.x+threadIdx.x;
+	if (r >= nrows) return;
+	int64_t row = MODE == 0 ? sn_woff[s]+r : 6*(int64_t)sn_first[s]+r;
+#pragma unroll
+	for (int q = 0; q < K; q++) {
+		T a = 0;
+		for (int c = 0; c < nchunk; c++) a += part[((int64_t)q*nchunk+c)*pstride+row];
+		if (MODE == 0) w[q*wstride+row] -= a;
+		else xp[(int64_t)q*n6tot+row] = a;
 	}
 }
 
@@ -887,15 +864,23 @@ static int solve_k(DevFactor<T> &F, const DevSymbolic &D, const double *b, doubl
 		dim3 g0((n6+m6+255)/256, cnt);
 		k_fwd_gather<T, K><<<g0, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.child_off, D.children, D.cinv_off,
 		                                        D.cinv, D.sn_woff, F.w, wstride, F.xp, n6tot);
-		dim3 g1((n6+SOLVE_OUT-1)/SOLVE_OUT, cnt);
-		k_fwd_y<T, K><<<g1, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, F.arena, F.xp, F.yp,
-		                                   n6tot);
+		dim3 g1((n6+SOLVE_CB-1)/SOLVE_CB, cnt);
+		k_solve_cols<T, K, 0><<<g1, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, D.sn_rows_off,
+		                                          D.rows, F.arena, F.xp, F.yp, n6tot);
 		launches += 2;
 		if (m6 > 0) {
-			dim3 g2((m6+31)/32, cnt);
-			k_fwd_w<T, K><<<g2, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, D.sn_woff, F.arena,
-			                                   F.w, wstride, F.yp, n6tot);
+			int nch = (n6+SOLVE_JC-1)/SOLVE_JC;
+			dim3 g2((m6+31)/32, cnt, nch);
+			k_solve_rows<T, K, 0><<<g2, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, D.sn_woff,
+			                                          F.arena, F.w, wstride, F.yp, F.xp, n6tot, F.part, F.pstride,
+			                                          nch);
 			launches++;
+			if (nch > 1) {
+				dim3 g3((m6+255)/256, cnt);
+				k_solve_rowsum<T, K, 0><<<g3, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_woff, F.w, wstride,
+				                                            F.xp, n6tot, F.part, F.pstride, nch);
+				launches++;
+			}
 		}
 	}
 	for (int l = D.nlevels-1; l >= 0; l--) {
@@ -903,37 +888,28 @@ static int solve_k(DevFactor<T> &F, const DevSymbolic &D, const double *b, doubl
 		if (!cnt) continue;
 		const int *lev = D.level_sn+D.h_level_off[l];
 		int n6 = D.h_level_maxn6[l], m6 = D.h_level_maxm6[l];
-		dim3 g((n6+SOLVE_OUT-1)/SOLVE_OUT, cnt);
 		if (m6 > 0) {
-			size_t want = sizeof(T)*(size_t)K*m6;
-			size_t sm = want <= (size_t)bwdz_smem_cap<T>() ? want : 0;
-			k_bwd_z<T, K><<<g, 256, sm, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, D.sn_rows_off,
-			                                   D.rows, F.arena, F.xp, F.yp, n6tot, (int)(sm/sizeof(T)));
+			dim3 g((n6+SOLVE_CB-1)/SOLVE_CB, cnt);
+			k_solve_cols<T, K, 1><<<g, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off,
+			                                         D.sn_rows_off, D.rows, F.arena, F.xp, F.yp, n6tot);
 			launches++;
 		}
-		k_bwd_x<T, K><<<g, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, F.arena, F.yp, F.xp,
-		                                  n6tot);
+		int nch = (n6+SOLVE_JC-1)/SOLVE_JC;
+		dim3 g2((n6+31)/32, cnt, nch);
+		k_solve_rows<T, K, 1><<<g2, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, D.sn_woff,
+		                                          F.arena, F.w, wstride, F.yp, F.xp, n6tot, F.part, F.pstride, nch);
 		launches++;
+		if (nch > 1) {
+			dim3 g3((n6+255)/256, cnt);
+			k_solve_rowsum<T, K, 1><<<g3, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_woff, F.w, wstride, F.xp,
+			                                            n6tot, F.part, F.pstride, nch);
+			launches++;
+		}
 	}
 	k_permute_out<T><<<(6*n+255)/256, 256, 0, st>>>(n, K, D.iperm, F.xp, x);
 	launches++;
 	LFG_CUDA(cudaGetLastError());
 	return launches;
-}
-
-// allow k_bwd_z to stage up to 200 kB of gathered x in shared memory
-template <typename T>
-static void set_smem_limits(int)
-{
-	static std::once_flag once;
-	std::call_once(once, [] {
-		const int cap = 200*1024;
-		LFG_CUDA(cudaFuncSetAttribute(k_bwd_z<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-		LFG_CUDA(cudaFuncSetAttribute(k_bwd_z<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-		LFG_CUDA(cudaFuncSetAttribute(k_bwd_z<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-		LFG_CUDA(cudaFuncSetAttribute(k_bwd_z<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-		bwdz_cap_ref<T>() = cap;
-	});
 }
 
 template <typename T>

@@ -126,7 +126,9 @@ template <typename T> struct DevFactor {
 	T *w = nullptr;       // forward-solve update vectors
 	T *xp = nullptr, *yp = nullptr; // permuted solve workspaces (k * 6n)
 	T *linv = nullptr;    // per supernode: Linv^T of its current panel's diagonal block
-	int64_t arena_cap = 0, w_cap = 0, x_cap = 0, linv_cap = 0;
+	T *part = nullptr;    // solve: partial row sums per column chunk
+	int64_t pstride = 0;
+	int64_t arena_cap = 0, w_cap = 0, x_cap = 0, linv_cap = 0, part_cap = 0;
 	int *status = nullptr; // device: first non-positive pivot column + 1 (0 = ok)
 };
 
