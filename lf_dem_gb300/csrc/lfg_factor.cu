@@ -15,7 +15,8 @@
 // Per level of the assembly tree (leaves first):
 //   assemble  : zero + gather children's update matrices (fixed child order),
 //   scatter   : add the compact D / OD blocks of the level's columns,
-//   diag k    : factor and invert the k-th diagonal block (one CTA per front),
+//   diag      : factor and invert panel 0's diagonal block (one CTA per front);
+//               panel k + 1's is done inside update k by the tile that holds it,
 //   trsm k    : rows below it (real rows and identity rows) times Linv^T,
 //   update k  : trailing rank-w update of the front's own columns (tiles),
 //   syrk      : the update (Schur complement) matrix, one deep-K product.
@@ -242,21 +243,15 @@ __device__ void cta_gemm32(T (&c8)[8], const T *A, int lda, const T *B, int ldb_
 	}
 }
 
+// Factor and invert the NB x NB diagonal block at (p0, p0) of a front (width
+// w, identity-padded past it), with the calling CTA (>= 128 threads).  L_kk
+// goes back into the front, Linv_kk^T (row-major NB x NB) to vt.  Ls, Vs:
+// NB x (NB + 1) and Ts: 32 x 33 shared arrays of the caller.
 template <typename T>
-__global__ void __launch_bounds__(128) k_diag(const int4 *__restrict__ tasks, const int *__restrict__ sn_first,
-                                              const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
-                                              T *__restrict__ arena, T *__restrict__ linv, int *fail)
+__device__ void diag_block(T *base, int ld, int p0, int w, int gcol0, int *fail, T *Ls, T *Vs, T *Ts, T *vt)
 {
 	constexpr int NB = Cfg<T>::NB, LD = NB+1;
 	static_assert(NB == 32 || NB == 64, "panel width");
-	__shared__ T Ls[NB*LD];   // L, row-major
-	__shared__ T Vs[NB*LD];   // Linv, row-major
-	__shared__ T Ts[32*33];   // L21 Linv11 (NB = 64)
-	int4 tk = tasks[blockIdx.x];
-	int s = tk.x, p0 = tk.y, w = tk.w;
-	int ld = sn_ld[s];
-	T *base = arena+sn_off[s];
-	int gcol0 = 6*sn_first[s]+p0;
 	int warp = threadIdx.x/32, lane = threadIdx.x%32;
 	for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
 		int i = e%NB, j = e/NB;    // coalesced over i (column-major front)
@@ -275,32 +270,63 @@ __global__ void __launch_bounds__(128) k_diag(const int4 *__restrict__ tasks, co
 	else if (NB == 64 && warp == 1) warp_trsm32<T>(Ls+32*LD, LD, Ls, LD, lane);   // L21 = A21 L11^-T
 	__syncthreads();
 	if (NB == 64) {
+		bool act = threadIdx.x < 128;   // cta_gemm32 covers 32 x 32 with 128 threads
 		T c8[8], u8[8];
 		int i = threadIdx.x/4, c0 = threadIdx.x%4;
-		cta_gemm32<T>(c8, Ls+32*LD, LD, Vs, LD, 1);          // T1 = L21 Linv11
-		cta_gemm32<T>(u8, Ls+32*LD, LD, Ls+32*LD, 1, LD);     // L21 L21^T
+		if (act) {
+			cta_gemm32<T>(c8, Ls+32*LD, LD, Vs, LD, 1);          // T1 = L21 Linv11
+			cta_gemm32<T>(u8, Ls+32*LD, LD, Ls+32*LD, 1, LD);     // L21 L21^T
 #pragma unroll
-		for (int q = 0; q < 8; q++) {
-			int c = c0+4*q;
-			Ts[i*33+c] = c8[q];
-			if (c <= i) Ls[(32+i)*LD+32+c] -= u8[q];
+			for (int q = 0; q < 8; q++) {
+				int c = c0+4*q;
+				Ts[i*33+c] = c8[q];
+				if (c <= i) Ls[(32+i)*LD+32+c] -= u8[q];
+			}
 		}
 		__syncthreads();
 		if (warp == 0) warp_potrf32<T>(Ls+32*LD+32, LD, lane, w-32, gcol0+32, fail);
 		__syncthreads();
 		if (warp == 0) warp_trtri32<T>(Ls+32*LD+32, LD, Vs+32*LD+32, LD, lane);   // Linv22
 		__syncthreads();
-		cta_gemm32<T>(c8, Vs+32*LD+32, LD, Ts, 33, 1);       // Linv22 T1
+		if (act) {
+			cta_gemm32<T>(c8, Vs+32*LD+32, LD, Ts, 33, 1);       // Linv22 T1
 #pragma unroll
-		for (int q = 0; q < 8; q++) Vs[(32+i)*LD+c0+4*q] = -c8[q];
+			for (int q = 0; q < 8; q++) Vs[(32+i)*LD+c0+4*q] = -c8[q];
+		}
 		__syncthreads();
 	}
-	T *vt = linv+(int64_t)s*NB*NB;
 	for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
 		int i = e%NB, j = e/NB;
 		if (j <= i && i < w) base[(int64_t)(p0+j)*ld+p0+i] = Ls[i*LD+j];
 		vt[j*NB+i] = Vs[i*LD+j];   // Linv^T[t = j][col = i]
 	}
+}
+
+// Linv slot of supernode s for panel k: two slots per supernode, by the
+// parity of k, so the update launch of panel k can write panel k + 1's while
+// the panel-k solve of other fronts still reads panel k's
+template <typename T>
+__device__ inline T *linv_slot(T *linv, int nsn, int s, int k)
+{
+	constexpr int NB = Cfg<T>::NB;
+	return linv+((int64_t)(k & 1)*nsn+s)*NB*NB;
+}
+
+// diagonal block of panel 0 of every front of a level (later panels' blocks
+// are factored by the update launch of the previous panel)
+template <typename T>
+__global__ void __launch_bounds__(128) k_diag(const int4 *__restrict__ tasks, const int *__restrict__ sn_first,
+                                              const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
+                                              T *__restrict__ arena, T *__restrict__ linv, int nsn, int *fail)
+{
+	constexpr int NB = Cfg<T>::NB, LD = NB+1;
+	__shared__ T Ls[NB*LD];
+	__shared__ T Vs[NB*LD];
+	__shared__ T Ts[32*33];
+	int4 tk = tasks[blockIdx.x];
+	int s = tk.x, p0 = tk.y, k = tk.z, w = tk.w;
+	diag_block<T>(arena+sn_off[s], sn_ld[s], p0, w, 6*sn_first[s]+p0, fail, Ls, Vs, Ts,
+	              linv_slot<T>(linv, nsn, s, k));
 }
 
 // ---------------------------------------------------------------------------
@@ -333,7 +359,7 @@ __device__ inline void lds_chunk(const T *p, T (&v)[CW])
 template <typename T>
 __global__ void __launch_bounds__(256) k_trsm(const int4 *__restrict__ tasks, const int *__restrict__ sn_n,
                                               const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
-                                              T *__restrict__ arena, const T *__restrict__ linv)
+                                              T *__restrict__ arena, T *__restrict__ linv, int nsn)
 {
 	constexpr int NB = Cfg<T>::NB, CW = NB/8;
 	__shared__ __align__(16) T Vt[NB*NB];
@@ -345,7 +371,7 @@ __global__ void __launch_bounds__(256) k_trsm(const int4 *__restrict__ tasks, co
 	int p0 = k*NB;
 	int w = min(NB, 6*sn_n[s]-p0);   // panel width: columns p0 + w and later are not touched
 	T *base = arena+sn_off[s];
-	const T *vt = linv+(int64_t)s*NB*NB;
+	const T *vt = linv_slot<T>(linv, nsn, s, k);
 	for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) Vt[e] = vt[e];
 	for (int e = threadIdx.x; e < PANEL_ROWS*NB; e += blockDim.x) {
 		int r = e%PANEL_ROWS, t = e/PANEL_ROWS;   // coalesced over rows
@@ -382,12 +408,15 @@ __global__ void __launch_bounds__(256) k_trsm(const int4 *__restrict__ tasks, co
 	}
 }
 
-// trailing update: CTA = one tile (sn, r0, c0, k) of the front's own columns
+// trailing update: CTA = one tile (sn, r0, c0, k) of the front's own columns.
+// The tile at (t0, t0) holds panel k + 1's diagonal block: after its update it
+// factors and inverts that block (diag_block), so the next panel needs no
+// separate diagonal launch.
 template <typename T>
 __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ tasks, const int *__restrict__ sn_first,
                                                 const int *__restrict__ sn_n, const int *__restrict__ sn_m,
                                                 const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
-                                                T *__restrict__ arena, int *fail)
+                                                T *__restrict__ arena, T *__restrict__ linv, int nsn, int *fail)
 {
 	constexpr int NB = Cfg<T>::NB, TL = Cfg<T>::TILE, TPT = Cfg<T>::TPT;
 	constexpr int TD = TL/TPT; // threads per dimension (16)
@@ -438,6 +467,15 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 			if (!extra && r < c) continue;
 			base[(int64_t)c*ld+r] -= acc[a][b];
 		}
+	}
+	if (!extra && r0 == t0 && cc0 == t0) {
+		__syncthreads();   // this CTA's updates of the block are visible to all its threads
+		constexpr int LD = NB+1;
+		T *Ls = reinterpret_cast<T *>(smem_upd);
+		T *Vs = Ls+NB*LD;
+		T *Ts = Vs+NB*LD;
+		diag_block<T>(base, ld, t0, min(NB, n6-t0), 6*sn_first[s]+t0, fail, Ls, Vs, Ts,
+		              linv_slot<T>(linv, nsn, s, k+1));
 	}
 }
 
@@ -520,7 +558,12 @@ __global__ void __launch_bounds__(256) k_syrk(const int4 *__restrict__ tasks, co
 // ---------------------------------------------------------------------------
 
 
-template <typename T> static size_t update_smem() { return 2*sizeof(T)*Cfg<T>::NB*Cfg<T>::TILE; }
+template <typename T> static size_t update_smem()
+{
+	// the tile's two panels, or diag_block's Ls, Vs and Ts
+	constexpr int NB = Cfg<T>::NB;
+	return sizeof(T)*std::max(2*NB*Cfg<T>::TILE, 2*NB*(NB+1)+32*33);
+}
 
 template <typename T> static void set_update_smem()
 {
@@ -555,7 +598,7 @@ template <typename T> void factor_alloc(DevFactor<T> &F, const DevSymbolic &D, i
 		LFG_CUDA(cudaMalloc((void **)&F.yp, sizeof(T)*xneed));
 		F.x_cap = xneed;
 	}
-	int64_t lneed = (int64_t)D.nsn*Cfg<T>::NB*Cfg<T>::NB;
+	int64_t lneed = (int64_t)2*D.nsn*Cfg<T>::NB*Cfg<T>::NB;
 	if (F.linv_cap < lneed) {
 		if (F.linv) cudaFree(F.linv);
 		F.linv = nullptr;
@@ -613,14 +656,15 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 			break;
 		case PLAN_DIAG:
 			k_diag<T><<<L.count, 128, 0, st>>>(D.diag_tasks+L.off, D.sn_first, D.sn_ld, D.sn_off, F.arena, F.linv,
-			                                   F.status);
+			                                   D.nsn, F.status);
 			break;
 		case PLAN_PANEL:
-			k_trsm<T><<<L.count, 256, 0, st>>>(D.panel_tasks+L.off, D.sn_n, D.sn_ld, D.sn_off, F.arena, F.linv);
+			k_trsm<T><<<L.count, 256, 0, st>>>(D.panel_tasks+L.off, D.sn_n, D.sn_ld, D.sn_off, F.arena, F.linv,
+			                                   D.nsn);
 			break;
 		case PLAN_UPDATE:
-			k_update<T><<<L.count, 256, update_smem<T>(), st>>>(D.tile_tasks+L.off, D.sn_first, D.sn_n, D.sn_m, D.sn_ld,
-			                                     D.sn_off, F.arena, F.status);
+			k_update<T><<<L.count, 256, update_smem<T>(), st>>>(D.tile_tasks+L.off, D.sn_first, D.sn_n, D.sn_m,
+			                                                    D.sn_ld, D.sn_off, F.arena, F.linv, D.nsn, F.status);
 			break;
 		case PLAN_SYRK:
 			k_syrk<T><<<L.count, 256, 0, st>>>(D.tile_tasks+L.off, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, F.arena);

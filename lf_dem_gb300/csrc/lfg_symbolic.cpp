@@ -526,16 +526,25 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 		D.factor_plan.push_back({PLAN_ASSEMBLE, l, 0, c0, (int)((int64_t)col_tasks.size()/2-c0)});
 		D.factor_plan.push_back({PLAN_SCATTER_D, l, 0, S.level_d_off[l], S.level_d_off[l+1]-S.level_d_off[l]});
 		D.factor_plan.push_back({PLAN_SCATTER_OD, l, 0, S.level_od_off[l], S.level_od_off[l+1]-S.level_od_off[l]});
+		// diagonal blocks of panel 0 (later panels' are factored by the update
+		// launch of the panel before)
+		{
+			int64_t d0 = (int64_t)diag_tasks.size();
+			for (int t = S.level_off[l]; t < S.level_off[l+1]; t++) {
+				int s = S.level_sn[t];
+				int n6 = 6*S.sn_n[s];
+				if (n6 > 0) diag_tasks.push_back(make_int4(s, 0, 0, std::min(panel_nb, n6)));
+			}
+			D.factor_plan.push_back({PLAN_DIAG, l, 0, d0, (int)((int64_t)diag_tasks.size()-d0)});
+		}
 		for (int k = 0; k < kmax; k++) {
 			int64_t p0 = (int64_t)panel_tasks.size(), t0i = (int64_t)tile_tasks.size();
-			int64_t d0 = (int64_t)diag_tasks.size();
 			for (int t = S.level_off[l]; t < S.level_off[l+1]; t++) {
 				int s = S.level_sn[t];
 				int n6 = 6*S.sn_n[s], F6 = n6+6*S.sn_m[s];
 				if (n6 <= k*panel_nb) continue;
 				int w = std::min(panel_nb, n6-k*panel_nb);
 				int t0 = k*panel_nb+w;
-				diag_tasks.push_back(make_int4(s, k*panel_nb, k, w));
 				// panel rows: real [t0, F6), extra [F6, F6+t0)
 				for (int r = t0; r < F6; r += RC) panel_tasks.push_back(make_int4(s, r, k, std::min(RC, F6-r)));
 				for (int r = F6; r < F6+t0; r += RC) panel_tasks.push_back(make_int4(s, r, k, std::min(RC, F6+t0-r)));
@@ -548,7 +557,6 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 					for (int c = t0; c < n6; c += tile)
 						tile_tasks.push_back(make_int4(s, r, c, k));
 			}
-			D.factor_plan.push_back({PLAN_DIAG, l, k, d0, (int)((int64_t)diag_tasks.size()-d0)});
 			D.factor_plan.push_back({PLAN_PANEL, l, k, p0, (int)((int64_t)panel_tasks.size()-p0)});
 			D.factor_plan.push_back({PLAN_UPDATE, l, k, t0i, (int)((int64_t)tile_tasks.size()-t0i)});
 		}
