@@ -42,7 +42,7 @@ template <typename T> struct Cfg;
 // NB: panel width; TILE/TPT: trailing-update tile edge / outputs per thread
 // per dimension; STILE/STPT: the same for the deep-K Schur complement SYRK
 template <> struct Cfg<double> { static constexpr int NB = 32, TILE = 64, TPT = 4, STILE = 64, STPT = 4; };
-template <> struct Cfg<float>  { static constexpr int NB = 32, TILE = 64, TPT = 4, STILE = 128, STPT = 8; };
+template <> struct Cfg<float>  { static constexpr int NB = 64, TILE = 64, TPT = 4, STILE = 128, STPT = 8; };
 
 // ---------------------------------------------------------------------------
 // compact blocks -> dense (StokesSolver.cpp:154-231), m[r*6+c]
