@@ -23,6 +23,7 @@
 // Nothing uses atomics except the failure flag, so results are bitwise
 // reproducible run to run.
 #include <atomic>
+#include <type_traits>
 #include <cstdio>
 #include <mutex>
 #include <cuda_runtime.h>
@@ -554,6 +555,184 @@ __global__ void __launch_bounds__(256) k_syrk(const int4 *__restrict__ tasks, co
 }
 
 // ---------------------------------------------------------------------------
+// FP32 Schur complement on the tensor cores: k_syrk_tc.  tcgen05.mma
+// (kind::tf32) with a 3xTF32 split: x = hi + lo with hi the TF32 part of x
+// (the MMA reads only the upper 19 bits, so hi is x itself) and lo = x -
+// hi exactly, so A B^T ~ Ahi Bhi^T + Ahi Blo^T + Alo Bhi^T keeps FP32-level
+// accuracy for the refinement.  One CTA (256 threads) per 128 x 128 tile of
+// the update matrix; the accumulator lives in tensor memory (128 columns).
+// K is walked in chunks of 32 (one 128-byte row of TF32): the threads
+// transpose the chunk's column-major front data into K-major,
+// 128-byte-swizzled shared-memory tiles in a ring of 3 stages, one thread
+// issues 4 K-steps x 3 MMAs per chunk and commits them to the stage's
+// mbarrier, and staging of the next chunks overlaps the MMAs.  Every mbarrier
+// wait is bounded: on a timeout the CTA stops issuing, waits (bounded) for
+// what it issued, frees its tensor memory and records the timeout (status 0)
+// in *fail.
+// ---------------------------------------------------------------------------
+namespace umma {
+constexpr int M = 128, N = 128, KC = 32, STAGES = 3, THREADS = 256;
+constexpr int TILE_BYTES = M*KC*4;           // one operand part (16 KB)
+constexpr int STAGE_BYTES = 4*TILE_BYTES;    // A hi, A lo, B hi, B lo
+constexpr int SMEM_BYTES = STAGES*STAGE_BYTES+1024;
+constexpr uint32_t WAIT_LIMIT = 1u << 24;
+
+__device__ inline uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (stride byte offset), descriptor version 1
+__device__ inline uint64_t sdesc(uint32_t a)
+{
+	return (uint64_t)((a >> 4) & 0x3FFF) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+	       ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// instruction descriptor: D = F32, A = B = TF32, both K-major, N = 128, M = 128
+constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
+                           ((uint32_t)(M >> 4) << 24);
+
+__device__ inline float tf32_lo(float x) { return x-__uint_as_float(__float_as_uint(x) & 0xffffe000u); }
+
+__device__ inline bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+	for (uint32_t it = 0; it < WAIT_LIMIT; it++) {
+		uint32_t done;
+		asm volatile("{\n\t.reg .pred p;\n\t"
+		             "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+		             "selp.u32 %0, 1, 0, p;\n\t}\n"
+		             : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+		if (done) return true;
+	}
+	return false;
+}
+
+__device__ inline void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate)
+{
+	asm volatile("{\n\t.reg .pred p;\n\t"
+	             "setp.ne.b32 p, %4, 0;\n\t"
+	             "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n"
+	             :: "r"(tmem), "l"(a), "l"(b), "r"(IDESC), "r"(accumulate));
+}
+} // namespace umma
+
+__global__ void __launch_bounds__(umma::THREADS, 1) k_syrk_tc(const int4 *__restrict__ tasks,
+                                                              const int *__restrict__ sn_n,
+                                                              const int *__restrict__ sn_m,
+                                                              const int *__restrict__ sn_ld,
+                                                              const int64_t *__restrict__ sn_off,
+                                                              float *__restrict__ arena, int *fail)
+{
+	using namespace umma;
+	extern __shared__ unsigned char smem_tc[];
+	__shared__ __align__(8) uint64_t mbar[STAGES];
+	__shared__ uint32_t tmem_slot;
+	unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_tc)+1023) &
+	                                                      ~static_cast<uintptr_t>(1023));
+	int4 tk = tasks[blockIdx.x];
+	int s = tk.x, r0 = tk.y, c0 = tk.z;
+	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
+	float *base = arena+sn_off[s];
+	int tid = threadIdx.x, warp = tid/32, lane = tid%32;
+	if (warp == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+		             :: "r"(saddr(&tmem_slot)), "r"(N));
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+		asm volatile("tcgen05.fence::before_thread_sync;");
+	}
+	if (tid == 0) {
+		for (int q = 0; q < STAGES; q++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&mbar[q])));
+		asm volatile("fence.mbarrier_init.release.cluster;");
+	}
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;");
+	uint32_t tmem = tmem_slot;
+	int nchunk = (n6+KC-1)/KC;
+	uint32_t phase_bits = 0;   // bit q: parity expected at the next wait on stage q
+	bool ok = true;
+	int issued = 0;
+	// staging role: row m of both operands, K half h of the chunk
+	const int m = tid & (M-1), h = tid >> 7;
+	const int ra = r0+m, rb = c0+m;
+	const bool va = ra < F6, vb = rb < F6;
+	for (int ch = 0; ch < nchunk; ch++) {
+		int b = ch % STAGES;
+		if (ch >= STAGES) {
+			if (!mbar_wait(saddr(&mbar[b]), (phase_bits >> b) & 1u)) ok = false;
+			phase_bits ^= 1u << b;
+		}
+		if (!__syncthreads_and(ok)) { ok = false; break; }
+		unsigned char *stg = sm+b*STAGE_BYTES;
+		int tb = ch*KC+16*h;
+		float av[16], bv[16];
+#pragma unroll
+		for (int k = 0; k < 16; k++) {
+			int t = tb+k;
+			av[k] = (t < n6 && va) ? base[(int64_t)t*ld+ra] : 0.f;
+			bv[k] = (t < n6 && vb) ? base[(int64_t)t*ld+rb] : 0.f;
+		}
+#pragma unroll
+		for (int k = 0; k < 16; k++) {
+			int kk = 16*h+k;
+			uint32_t off = (uint32_t)((m >> 3)*1024+(m & 7)*128+((((kk >> 2) ^ (m & 7))) << 4)+((kk & 3) << 2));
+			*reinterpret_cast<float *>(stg+0*TILE_BYTES+off) = av[k];
+			*reinterpret_cast<float *>(stg+1*TILE_BYTES+off) = tf32_lo(av[k]);
+			*reinterpret_cast<float *>(stg+2*TILE_BYTES+off) = bv[k];
+			*reinterpret_cast<float *>(stg+3*TILE_BYTES+off) = tf32_lo(bv[k]);
+		}
+		asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+		__syncthreads();
+		if (tid == 0) {
+			asm volatile("tcgen05.fence::after_thread_sync;");
+			uint32_t sa = saddr(stg);
+#pragma unroll
+			for (int kk = 0; kk < KC/8; kk++) {
+				uint64_t ahi = sdesc(sa+0*TILE_BYTES+32*kk), alo = sdesc(sa+1*TILE_BYTES+32*kk);
+				uint64_t bhi = sdesc(sa+2*TILE_BYTES+32*kk), blo = sdesc(sa+3*TILE_BYTES+32*kk);
+				mma_tf32(tmem, ahi, bhi, (ch > 0 || kk > 0) ? 1u : 0u);
+				mma_tf32(tmem, ahi, blo, 1u);
+				mma_tf32(tmem, alo, bhi, 1u);
+			}
+			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+			             :: "r"(saddr(&mbar[b])) : "memory");
+		}
+		issued = ch+1;
+	}
+	// every issued MMA is complete once the last commit has arrived
+	if (issued > 0) {
+		int b = (issued-1) % STAGES;
+		if (!mbar_wait(saddr(&mbar[b]), (phase_bits >> b) & 1u)) ok = false;
+	}
+	asm volatile("tcgen05.fence::after_thread_sync;");
+	ok = __syncthreads_and(ok);
+	if (ok && issued == nchunk && nchunk > 0) {
+		// warp w reads TMEM lanes 32 (w % 4) .. +32 (rows) and columns 64 (w / 4) .. +64
+		int q = warp & 3, half = warp >> 2;
+		int r = r0+32*q+lane;
+#pragma unroll 1
+		for (int cb = 64*half; cb < 64*half+64; cb += 16) {
+			uint32_t v[16];
+			uint32_t ta = tmem+((uint32_t)(32*q) << 16)+(uint32_t)cb;
+			asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+			             "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+			             : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+			               "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+			               "=r"(v[14]), "=r"(v[15])
+			             : "r"(ta));
+			asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+			for (int j = 0; j < 16; j++) {
+				int c = c0+cb+j;
+				if (r < F6 && c < F6 && r >= c) base[(int64_t)c*ld+r] -= __uint_as_float(v[j]);
+			}
+		}
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;");
+	__syncthreads();
+	if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(N));
+	if (!ok && tid == 0 && fail) atomicMin(fail, 0);
+}
+
+// ---------------------------------------------------------------------------
 // allocation and launch
 // ---------------------------------------------------------------------------
 
@@ -571,6 +750,7 @@ template <typename T> static void set_update_smem()
 	std::call_once(once, [] {
 		LFG_CUDA(cudaFuncSetAttribute(k_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		                              (int)update_smem<T>()));
+		LFG_CUDA(cudaFuncSetAttribute(k_syrk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, umma::SMEM_BYTES));
 	});
 }
 
@@ -667,7 +847,12 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 			                                                    D.sn_ld, D.sn_off, F.arena, F.linv, D.nsn, F.status);
 			break;
 		case PLAN_SYRK:
-			k_syrk<T><<<L.count, 256, 0, st>>>(D.tile_tasks+L.off, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, F.arena);
+			if (std::is_same<T, float>::value)
+				k_syrk_tc<<<L.count, umma::THREADS, umma::SMEM_BYTES, st>>>(D.tile_tasks+L.off, D.sn_n, D.sn_m, D.sn_ld,
+				                                                   D.sn_off, reinterpret_cast<float *>(F.arena),
+				                                                   F.status);
+			else
+				k_syrk<T><<<L.count, 256, 0, st>>>(D.tile_tasks+L.off, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, F.arena);
 			break;
 		}
 		launches++;
