@@ -368,34 +368,57 @@ __global__ void k_candidates(DevParams P, CellView C, const DevClock *__restrict
 
 // every pair within the interaction range must be in the superset
 // (System::checkNewInteraction's test, System.cpp:1328-1373)
+// one thread per (particle i, neighbour cell): every pair (i, j > i) within
+// interaction range must be in the superset row of i
 __global__ void k_check_superset(DevParams P, CellView C, DevClock *__restrict__ clk,
                                  const double *__restrict__ pos, const double *__restrict__ radius,
                                  const int *__restrict__ row_ptr, const DPair *__restrict__ pairs)
 {
-	int i = blockIdx.x*blockDim.x+threadIdx.x;
-	if (i >= C.n) return;
+	const int ncell = P.twodim ? 9 : 27;
+	int64_t t = (int64_t)blockIdx.x*blockDim.x+threadIdx.x;
+	if (t >= (int64_t)C.n*ncell) return;
+	int i = (int)(t/ncell), q = (int)(t%ncell);
+	if (C.brute && q != 0) return;
 	const double *sd = clk->shear_disp;
 	v3 pi = ld3(pos+3*i);
 	double ri = radius[i];
 	int lo0 = row_ptr[i], hi0 = row_ptr[i+1];
-	bool missing = false;
-	for_neighbours(C, P, sd, i, pi, [&](int j) {
+	auto check = [&](int j) {
 		v3 d = vsub(ld3(pos+3*j), pi);
 		periodize_diff(P, sd, d);
 		double range = inter_range(P, ri, radius[j]);
 		if (vsq(d) < range*range) {
 			int lo = lo0, hi = hi0-1;
-			bool found = false;
 			while (lo <= hi) {
 				int m = (lo+hi) >> 1;
 				int pj = pairs[m].p1;
-				if (pj == j) { found = true; break; }
+				if (pj == j) return;
 				if (pj < j) lo = m+1; else hi = m-1;
 			}
-			if (!found) missing = true;
+			atomicOr(&clk->stale, 1);
 		}
-	});
-	if (missing) atomicOr(&clk->stale, 1);
+	};
+	if (C.brute) {
+		for (int j = i+1; j < C.n; j++) check(j);
+		return;
+	}
+	// the neighbour cell of index q, located as for_neighbours does
+	int dz = q/(P.twodim ? 3 : 9)-1;
+	int dy = P.twodim ? 0 : (q/3)%3-1;
+	int dx = q%3-1;
+	int zc = cell_coord(pi.z, P.lz, C.csz, C.ncz)+dz;
+	double sx = 0, sy = 0;
+	if (zc < 0) { zc += C.ncz; sx = sd[0]; sy = sd[1]; }
+	else if (zc >= C.ncz) { zc -= C.ncz; sx = -sd[0]; sy = -sd[1]; }
+	int xc = cell_coord(pi.x+sx, P.lx, C.csx, C.ncx);
+	int yy = P.twodim ? 0 : wrapc(cell_coord(pi.y+sy, P.ly, C.csy, C.ncy)+dy, C.ncy);
+	int xx = wrapc(xc+dx, C.ncx);
+	int cell = (zc*C.ncy+yy)*C.ncx+xx;
+	int s0 = C.start[cell], e0 = s0+C.count[cell];
+	for (int k = s0; k < e0; k++) {
+		int j = C.list[k];
+		if (j > i) check(j);
+	}
 }
 
 // ---------------------------------------------------------------------------
@@ -864,20 +887,15 @@ __global__ void k_gather_pairs(int n, int ncomp, int width, const int *__restric
                                const int *__restrict__ col_ptr, const int *__restrict__ col_idx,
                                const double *__restrict__ scr, double *__restrict__ out)
 {
-	int i = blockIdx.x*blockDim.x+threadIdx.x;
-	if (i >= n) return;
-	for (int c = 0; c < ncomp; c++) {
-		double a[6] = {0, 0, 0, 0, 0, 0};
-		for (int k = col_ptr[i]; k < col_ptr[i+1]; k++) {
-			const double *s = scr+width*(int64_t)col_idx[k]+12*c+6;
-			for (int e = 0; e < 6; e++) a[e] += s[e];
-		}
-		for (int t = row_ptr[i]; t < row_ptr[i+1]; t++) {
-			const double *s = scr+width*(int64_t)t+12*c;
-			for (int e = 0; e < 6; e++) a[e] += s[e];
-		}
-		for (int e = 0; e < 6; e++) out[(int64_t)c*6*n+6*i+e] = a[e];
-	}
+	// one thread per (particle, component, element): pairs with p1 == i first
+	// (ascending p0), then pairs with p0 == i (ascending p1)
+	int64_t t = (int64_t)blockIdx.x*blockDim.x+threadIdx.x;
+	if (t >= (int64_t)n*ncomp*6) return;
+	int e = (int)(t%6), c = (int)((t/6)%ncomp), i = (int)(t/(6*ncomp));
+	double a = 0;
+	for (int k = col_ptr[i]; k < col_ptr[i+1]; k++) a += scr[width*(int64_t)col_idx[k]+12*c+6+e];
+	for (int q = row_ptr[i]; q < row_ptr[i+1]; q++) a += scr[width*(int64_t)q+12*c+e];
+	out[(int64_t)c*6*n+6*i+e] = a;
 }
 
 // torque mask per component: contact (friction), dashpot (1), hydro (tangential), repulsion (0)
@@ -1311,7 +1329,8 @@ void phys_candidates(DevSim &S, cudaStream_t st, int *h_total)
 void phys_check_superset(DevSim &S, cudaStream_t st)
 {
 	CellView C = view(S);
-	k_check_superset<<<blocks_for(S.n, 128), 128, 0, st>>>(S.P, C, S.clock, S.pos, S.radius, S.row_ptr, S.pairs);
+	k_check_superset<<<blocks_for((S.P.twodim ? 9 : 27)*S.n, 256), 256, 0, st>>>(S.P, C, S.clock, S.pos, S.radius,
+	                                                                           S.row_ptr, S.pairs);
 	S.launches++;
 }
 
@@ -1349,7 +1368,7 @@ void phys_force_components(DevSim &S, cudaStream_t st)
 	if (S.npairs)
 		k_pair_forces<<<blocks_for(S.npairs, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst, S.u_inf,
 		                                                         S.pair_scratch);
-	k_gather_pairs<<<blocks_for(S.n, 128), 128, 0, st>>>(S.n, NFC, 48, S.row_ptr, S.col_ptr, S.col_idx,
+	k_gather_pairs<<<blocks_for(6*NFC*S.n, 256), 256, 0, st>>>(S.n, NFC, 48, S.row_ptr, S.col_ptr, S.col_idx,
 	                                                     S.pair_scratch, S.fc);
 	S.launches += 2;
 }
@@ -1396,7 +1415,7 @@ void phys_force_component_into(DevSim &S, int comp, double *scr, double *out, cu
 	if (S.npairs)
 		k_pair_forces<<<blocks_for(S.npairs, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst, S.u_inf,
 		                                                         scr);
-	k_gather_pairs<<<blocks_for(S.n, 128), 128, 0, st>>>(S.n, 1, 48, S.row_ptr, S.col_ptr, S.col_idx, scr+12*comp,
+	k_gather_pairs<<<blocks_for(6*S.n, 256), 256, 0, st>>>(S.n, 1, 48, S.row_ptr, S.col_ptr, S.col_idx, scr+12*comp,
 	                                                     out);
 	S.launches += 2;
 }
@@ -1417,7 +1436,7 @@ void phys_stresslets(DevSim &S, cudaStream_t st)
 	if (S.npairs)
 		k_pair_stress<<<blocks_for(S.npairs, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst, S.vc,
 		                                                         S.vel, S.ang, split, S.n, S.pair_scratch);
-	k_gather_pairs<<<blocks_for(S.n, 128), 128, 0, st>>>(S.n, NSC, 12*NSC, S.row_ptr, S.col_ptr, S.col_idx,
+	k_gather_pairs<<<blocks_for(6*NSC*S.n, 256), 256, 0, st>>>(S.n, NSC, 12*NSC, S.row_ptr, S.col_ptr, S.col_idx,
 	                                                     S.pair_scratch, S.sc);
 	k_stress_totals<<<NSC, 256, 0, st>>>(S.n, S.sc, S.sc_tot);
 	S.launches += 3;
