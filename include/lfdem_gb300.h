@@ -89,6 +89,8 @@ typedef struct {
 	double Ohat[3];
 	double init_strain_shear_rate_limit;
 	double init_shear_rate_limit;
+	double mu_rolling;               /* > 0 enables rolling friction (System.cpp:386-388) */
+	double kr;                       /* rolling spring constant (Contact.cpp:35-45) */
 } lfg_params;
 
 /* Engine options (not physics). */
@@ -225,6 +227,8 @@ int lfg_sim_get_velocity_component(lfg_sim *s, int comp, double *out);
  * tangential spring and friction state; set clocks; recompute every pair's
  * forces at the current positions with dt = 0 (System.cpp:1216-1226). */
 int lfg_sim_set_contact(lfg_sim *s, int p0, int p1, int state, const double *disp_tan);
+/* The rolling spring of that contact (contact_state.disp_rolling, Contact.h:150-162). */
+int lfg_sim_set_contact_rolling(lfg_sim *s, int p0, int p1, const double *disp_rolling);
 int lfg_sim_set_clock(lfg_sim *s, double time, double strain, double dt, double shear_rate,
                       double max_velocity, double max_sliding_velocity);
 int lfg_sim_refresh(lfg_sim *s);

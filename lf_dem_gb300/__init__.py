@@ -49,6 +49,7 @@ class Params(C.Structure):
         ("shear_rate", C.c_double), ("target_stress", C.c_double),
         ("Ehat", C.c_double * 6), ("Ohat", C.c_double * 3),
         ("init_strain_shear_rate_limit", C.c_double), ("init_shear_rate_limit", C.c_double),
+        ("mu_rolling", C.c_double), ("kr", C.c_double),
     ]
 
 
@@ -123,7 +124,7 @@ EXPORTS = [
     "lfg_sim_get_velocity_component", "lfg_sim_set_contact", "lfg_sim_set_clock", "lfg_sim_refresh",
     "lfg_sim_assemble", "lfg_sim_force_component", "lfg_sim_get_timing", "lfg_sim_get_step_times",
     "lfg_sim_clear_step_times", "lfg_sim_destroy", "lfg_sim_force_component_noalloc",
-    "lfg_sim_advance_partial", "lfg_sim_set_leaf_size", "lfg_sim_device_bytes", "lfg_footprint_estimate",
+    "lfg_sim_advance_partial", "lfg_sim_set_contact_rolling", "lfg_sim_set_leaf_size", "lfg_sim_device_bytes", "lfg_footprint_estimate",
     "lfg_batch_create", "lfg_batch_add", "lfg_batch_size", "lfg_batch_sim", "lfg_batch_run", "lfg_batch_advance",
     "lfg_batch_autotune", "lfg_batch_tuned_leaf", "lfg_batch_destroy",
     "lfg_server_create", "lfg_server_submit", "lfg_server_poll", "lfg_server_wait", "lfg_server_final_positions",
@@ -176,6 +177,7 @@ def load(path: str | None = None):
         L.lfg_sim_get_particle_stress.argtypes = [vp, C.c_int, vp]
         L.lfg_sim_get_velocity_component.argtypes = [vp, C.c_int, vp]
         L.lfg_sim_set_contact.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp]
+        L.lfg_sim_set_contact_rolling.argtypes = [vp, C.c_int, C.c_int, vp]
         L.lfg_sim_set_clock.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                         C.c_double]
         L.lfg_sim_refresh.argtypes = [vp]
@@ -428,6 +430,11 @@ class Sim:
         if rc:
             raise LFGError(rc, f"no pair ({p0},{p1})")
 
+    def set_contact_rolling(self, p0, p1, disp_rolling):
+        d = np.ascontiguousarray(disp_rolling, dtype=np.float64)
+        rc = load().lfg_sim_set_contact_rolling(self.h, int(p0), int(p1), _ptr(d))
+        if rc:
+            raise LFGError(rc, f"no pair ({p0}, {p1})")
     def set_clock(self, time, strain, dt, shear_rate, max_velocity, max_sliding_velocity):
         load().lfg_sim_set_clock(self.h, time, strain, dt, shear_rate, max_velocity, max_sliding_velocity)
 

@@ -164,6 +164,7 @@ __global__ void k_pair_constants(DevParams P, int np, const DPair *__restrict__ 
 	double ro_12 = (a0+a1)/2;
 	c.kn_s = ro_12*ro_12*P.kn;
 	c.kt_s = P.friction ? ro_12*P.kt : 0;
+	c.kr_s = (P.friction && P.rolling) ? ro_12*P.kr : 0;
 	c.rep_geo = a0*a1/(a0+a1);
 	// Lubrication::calcLubConstants
 	double r12 = ro/2;
@@ -445,6 +446,7 @@ __device__ void contact_activate(const DevParams &P, DPair &q)
 	if (P.friction) {
 		q.state = (P.friction_model == 2 || P.friction_model == 3) ? 1 : 2;
 		for (int k = 0; k < 3; k++) { q.disp_tan[k] = 0; q.prev_disp_tan[k] = 0; }
+		for (int k = 0; k < 3; k++) { q.disp_roll[k] = 0; q.prev_disp_roll[k] = 0; q.f_roll[k] = 0; }
 	} else {
 		q.state = 1;
 	}
@@ -457,7 +459,7 @@ __device__ void contact_deactivate(const DevParams &P, DPair &q)
 	q.fsn_norm = 0;
 	for (int k = 0; k < 3; k++) q.fs_total[k] = 0;
 	if (P.friction)
-		for (int k = 0; k < 3; k++) { q.disp_tan[k] = 0; q.fs_tan[k] = 0; }
+		for (int k = 0; k < 3; k++) { q.disp_tan[k] = 0; q.disp_roll[k] = 0; q.fs_tan[k] = 0; }
 }
 
 __device__ void lub_update(const DevParams &P, DPair &q, const DPairConst &c)
@@ -493,6 +495,16 @@ __device__ void friction_law(const DevParams &P, DPair &q, const DPairConst &c)
 		if (sq > sup*sup) { q.state = 3; sup = P.mu_d*q.normal_load; }
 		else q.state = 2;
 		if (q.state == 3) set_tan_norm(q, c, sqrt(sq), sup);
+		if (P.rolling) {
+			// Contact::setRollingForceNorm (Contact.cpp:283-305)
+			double sup_r = P.mu_r*q.normal_load;
+			double sq_r = vsq(ld3(q.f_roll));
+			if (sq_r > sup_r*sup_r) {
+				double sc = sup_r/sqrt(sq_r);
+				for (int k = 0; k < 3; k++) q.disp_roll[k] = sc*q.disp_roll[k];
+				for (int k = 0; k < 3; k++) q.f_roll[k] = c.kr_s*q.disp_roll[k];
+			}
+		}
 	} else if (fm == 2) {
 		double sup = q.fsn_norm-P.critical_load;
 		if (sup < 0) {
@@ -535,6 +547,7 @@ __device__ void contact_spring(const DevParams &P, DPair &q, const DPairConst &c
 		d = vsub(d, vscale(vdot(d, n), n));
 		st3(q.disp_tan, d);
 		st3(q.fs_tan, vscale(c.kt_s, d));
+		if (P.rolling) st3(q.f_roll, vscale(c.kr_s, ld3(q.disp_roll)));
 		friction_law(P, q, c);
 	}
 	if (q.state <= 1) st3(q.fs_total, fn);
@@ -554,6 +567,13 @@ __device__ void contact_increment(const DevParams &P, const DevClock &K, const d
 	q.rsv_sq = vsq(rsv);
 	if (in_predictor) for (int k = 0; k < 3; k++) q.prev_disp_tan[k] = q.disp_tan[k];
 	st3(q.disp_tan, vadd(ld3(q.prev_disp_tan), vscale(dt, rsv)));
+	if (P.rolling) {
+		// Contact::calcRollingVelocities + incrementRollingDisplacement (Contact.cpp:162-180)
+		double a_red = c.a0*c.a1/(c.a0+c.a1);
+		v3 rv = vscale(2*a_red, vcross(vsub(ld3(ang+3*q.p1), ld3(ang+3*q.p0)), n));
+		if (in_predictor) for (int k = 0; k < 3; k++) q.prev_disp_roll[k] = q.disp_roll[k];
+		st3(q.disp_roll, vadd(ld3(q.prev_disp_roll), vscale(dt, rv)));
+	}
 }
 
 __device__ void repulsion_force(const DevParams &P, DPair &q, const DPairConst &c)
@@ -833,8 +853,15 @@ __global__ void k_pair_forces(DevParams P, int np, const DevClock *__restrict__ 
 		st3(o+6, vneg(f));
 		if (q.state >= 2) {
 			v3 tq = vcross(n, ld3(q.fs_tan));
-			st3(o+3, vscale(c.a0, tq));
-			st3(o+9, vscale(c.a1, tq));
+			v3 t0 = vscale(c.a0, tq), t1 = vscale(c.a1, tq);
+			if (P.rolling) {
+				// Contact::addUpForceTorque (Contact.cpp:431-435): +a0 n x f_r on p0, -a1 n x f_r on p1
+				v3 tr = vcross(n, ld3(q.f_roll));
+				t0 = vadd(t0, vscale(c.a0, tr));
+				t1 = vsub(t1, vscale(c.a1, tr));
+			}
+			st3(o+3, t0);
+			st3(o+9, t1);
 		}
 	}
 	// dashpot R_FU U_inf (ContactDashpot::getRFU_Uinf, :426-441)

@@ -18,7 +18,8 @@ struct DevParams {
 	double target_stress, init_strain_limit, init_rate_limit;
 	double system_volume;
 	double skin;
-	int friction_model, friction, repulsiveforce, lub_on, tangential, twodim;
+	double mu_r, kr;                       // rolling friction (Contact.cpp:35-45, 283-305)
+	int friction_model, friction, rolling, repulsiveforce, lub_on, tangential, twodim;
 	int fixed_dt, control, integration_method, n;
 };
 
@@ -43,6 +44,7 @@ struct DPair {
 	double fs_total[3], fs_tan[3], fsn_norm, normal_load, rsv_sq;
 	double lub_coeff, log_lub_coeff;
 	double rep_force[3], rep_reduced;
+	double disp_roll[3], prev_disp_roll[3], f_roll[3];   // rolling spring (Contact.h:33-70)
 	int p0, p1, zoff, flags, state, pad_;
 };
 
@@ -52,7 +54,7 @@ enum { NLUB = 36, NDP = 16 };
 struct DPairConst {
 	double lc[NLUB];  // cXA cYA cYB cYC cXG cYG cYH cXM cYM (4 each)
 	double dc[NDP];   // dashpot XA YA YB YC (4 each)
-	double range, lub_range, a0, a1, ro, kn_s, kt_s, rep_geo;
+	double range, lub_range, a0, a1, ro, kn_s, kt_s, rep_geo, kr_s;
 };
 
 // Component slots.

@@ -37,7 +37,7 @@ public:
 	int get_pairs(lfg_pair *out, int cap);
 	int particle_stress(int comp, double *out);
 	int velocity_component(int comp, double *out);
-	int set_contact(int p0, int p1, int state, const double *disp_tan);
+	int set_contact(int p0, int p1, int state, const double *disp_tan, const double *disp_roll = nullptr);
 	void set_clock(double time, double strain, double dt, double rate, double maxv, double maxsv);
 	void refresh();
 	int assemble(double *dbl, int32_t *row, int32_t *col, double *odbl, int cap, int *nb_out);
@@ -90,6 +90,8 @@ static DevParams make_dev_params(const lfg_params &p, int n, double lx, double l
 	P.mu_s = P.friction ? p.mu_static : 0;
 	P.mu_d = p.mu_dynamic < 0 ? P.mu_s : p.mu_dynamic;
 	P.kn = p.kn; P.kt = p.kt;
+	P.rolling = p.mu_rolling > 0;
+	P.mu_r = p.mu_rolling; P.kr = p.kr;
 	P.critical_load = p.critical_load; P.ft_max = p.ft_max;
 	P.repulsiveforce = p.repulsion_on && p.repulsive_length > 0;
 	P.repulsion = p.repulsion; P.rep_len = p.repulsive_length; P.rep_max_len = p.repulsive_max_length;
@@ -145,6 +147,8 @@ Sim::Sim(const lfg_params &p, const lfg_options &o, int n, const double *pos, co
 		throw Error{LFG_ERR_BAD_ARG, p.friction_model, "unknown friction model"};
 	if (p.lubrication_model < 0 || p.lubrication_model > 2)
 		throw Error{LFG_ERR_BAD_ARG, p.lubrication_model, "unknown lubrication model"};
+	if (p.mu_rolling > 0 && p.friction_model == 0)
+		throw Error{LFG_ERR_BAD_ARG, 0, "rolling friction without sliding friction (System.cpp:386-391)"};
 	if (p.lubrication_model == 2 && p.lub_max_gap >= 1)
 		throw Error{LFG_ERR_BAD_ARG, 0, "lub_max_gap must be smaller than 1 (System.cpp:340-346)"};
 	S_.n = n;
@@ -566,7 +570,7 @@ int Sim::velocity_component(int comp, double *out)
 	return LFG_OK;
 }
 
-int Sim::set_contact(int p0, int p1, int state, const double *disp_tan)
+int Sim::set_contact(int p0, int p1, int state, const double *disp_tan, const double *disp_roll)
 {
 	if (p0 > p1) std::swap(p0, p1);
 	std::vector<int> rp(S_.n+1);
@@ -576,7 +580,8 @@ int Sim::set_contact(int p0, int p1, int state, const double *disp_tan)
 		DPair q;
 		LFG_CUDA(cudaMemcpyAsync(&q, S_.pairs+t, sizeof q, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
 		if (q.p1 != p1) continue;
-		for (int k = 0; k < 3; k++) q.disp_tan[k] = disp_tan[k];
+		if (disp_tan) for (int k = 0; k < 3; k++) q.disp_tan[k] = disp_tan[k];
+		if (disp_roll) for (int k = 0; k < 3; k++) q.disp_roll[k] = disp_roll[k];
 		if (state >= 0 && (q.flags & PF_CONTACT)) q.state = state;
 		LFG_CUDA(cudaMemcpyAsync(S_.pairs+t, &q, sizeof q, cudaMemcpyHostToDevice, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
 		return LFG_OK;
@@ -852,6 +857,15 @@ int lfg_sim_set_contact(lfg_sim *h, int p0, int p1, int state, const double *dis
 	if (!h || !disp_tan) return LFG_ERR_BAD_ARG;
 	SIM_GUARD_BEGIN
 	return h->s->set_contact(p0, p1, state, disp_tan);
+	SIM_GUARD_END
+}
+
+int lfg_sim_set_contact_rolling(lfg_sim *h, int p0, int p1, const double *disp_rolling)
+{
+	lfg_status *st = nullptr;
+	if (!h || !disp_rolling) return LFG_ERR_BAD_ARG;
+	SIM_GUARD_BEGIN
+	return h->s->set_contact(p0, p1, -1, nullptr, disp_rolling);
 	SIM_GUARD_END
 }
 

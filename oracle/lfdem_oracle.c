@@ -183,6 +183,8 @@ typedef struct {
 	int c_active, state;
 	double kn_s, kt_s, mu_s, mu_d;
 	v3 disp_tan, prev_disp_tan;
+	double kr_s, mu_r;                 /* rolling friction (Contact.cpp:35-45, 60-67) */
+	v3 disp_roll, prev_disp_roll, f_roll;
 	double fsn_norm, normal_load;
 	v3 fs_normal, fs_tan, fs_total;
 	double rsv_sq;
@@ -212,7 +214,7 @@ struct lfo_sim {
 	int np, twodim;
 	double lx, ly, lz, lx_half, ly_half, lz_half;
 	double system_volume;
-	int friction, lubrication, tangential, repulsiveforce, pairwise_resistance;
+	int friction, rolling, lubrication, tangential, repulsiveforce, pairwise_resistance;
 	int has_fc[NFC], fc_torque[NFC], fc_rate[NFC];
 	int has_sc[NSC], sc_rate[NSC], sc_group[NSC];
 	v3 *pos, *vel, *ang, *na_vel, *na_ang, *vel_pred, *ang_pred, *u_inf;
@@ -439,6 +441,9 @@ static void contact_activate(lfo_sim *s, opair *q)
 		else q->state = 2;
 		q->disp_tan = vzero();
 		q->prev_disp_tan = vzero();
+		q->disp_roll = vzero();
+		q->prev_disp_roll = vzero();
+		q->f_roll = vzero();
 	} else {
 		q->state = 1;
 	}
@@ -455,6 +460,7 @@ static void contact_deactivate(lfo_sim *s, opair *q)
 	q->fs_total = vzero();
 	if (s->friction) {
 		q->disp_tan = vzero();
+		q->disp_roll = vzero();
 		q->fs_tan = vzero();
 	}
 	q->dp_active = 0;
@@ -501,6 +507,10 @@ static int pair_create(lfo_sim *s, opair *q, int i, int j, double range)
 		q->kt_s = ro_12*s->p.kt;
 		q->mu_s = s->p.mu_static;
 		q->mu_d = s->p.mu_dynamic;
+		if (s->rolling) {
+			q->kr_s = ro_12*s->p.kr;
+			q->mu_r = s->p.mu_rolling;
+		}
 	}
 	if (dashpot_coeffs(s, q)) return -1;
 	if (q->gap <= 0) contact_activate(s, q);
@@ -537,6 +547,15 @@ static void friction_law(lfo_sim *s, opair *q)
 			q->state = 2;
 		}
 		if (q->state == 3) set_tan_norm(q, sqrt(sq_f_tan), supportable);
+		if (s->rolling) {
+			/* Contact::setRollingForceNorm, Contact.cpp:283-305 */
+			double sup_r = q->mu_r*q->normal_load;
+			double sq_f_roll = vsq(q->f_roll);
+			if (sq_f_roll > sup_r*sup_r) {
+				q->disp_roll = vscale(sup_r/sqrt(sq_f_roll), q->disp_roll);
+				q->f_roll = vscale(q->kr_s, q->disp_roll);
+			}
+		}
 	} else if (fm == 2) {
 		double supportable = q->fsn_norm-s->p.critical_load;
 		if (supportable < 0) {
@@ -595,6 +614,7 @@ static void contact_spring(lfo_sim *s, opair *q)
 	if (s->friction) {
 		q->disp_tan = vsub(q->disp_tan, vscale(vdot(q->disp_tan, q->nvec), q->nvec));
 		q->fs_tan = vscale(q->kt_s, q->disp_tan);
+		if (s->rolling) q->f_roll = vscale(q->kr_s, q->disp_roll);
 		friction_law(s, q);
 	}
 	if (q->state <= 1) q->fs_total = q->fs_normal;
@@ -613,6 +633,13 @@ static void contact_increment(lfo_sim *s, opair *q)
 	q->rsv_sq = vsq(rsv);
 	if (s->in_predictor) q->prev_disp_tan = q->disp_tan;
 	q->disp_tan = vadd(q->prev_disp_tan, vscale(s->dt, rsv));
+	if (s->rolling) {
+		/* Contact::calcRollingVelocities + incrementRollingDisplacement, Contact.cpp:162-180 */
+		double a_red = q->a0*q->a1/(q->a0+q->a1);
+		v3 rv = vscale(2*a_red, vcross(vsub(s->ang[q->p1], s->ang[q->p0]), q->nvec));
+		if (s->in_predictor) q->prev_disp_roll = q->disp_roll;
+		q->disp_roll = vadd(q->prev_disp_roll, vscale(s->dt, rv));
+	}
 }
 
 /* RepulsiveForce::calcReducedForceNorm + calcScaledForce,
@@ -1322,6 +1349,11 @@ static void force_component(lfo_sim *s, int comp, double *out)
 				v3 t = vcross(q->nvec, q->fs_tan);
 				addT(out, q->p0, vscale(q->a0, t));
 				addT(out, q->p1, vscale(q->a1, t));
+				if (s->rolling) {
+					v3 tr = vcross(q->nvec, q->f_roll);
+					addT(out, q->p0, vscale(q->a0, tr));
+					addT(out, q->p1, vneg(vscale(q->a1, tr)));
+				}
 			}
 		}
 	} else if (comp == FC_DASHPOT) {
@@ -1807,6 +1839,16 @@ int lfo_set_contact(lfo_sim *s, int p0, int p1, int state, const double *disp_ta
 	return 0;
 }
 
+/* rolling spring of an existing contact (contact_state.disp_rolling,
+ * Contact.h:150-162) */
+int lfo_set_contact_rolling(lfo_sim *s, int p0, int p1, const double *disp_rolling)
+{
+	int k = find_pair(s, p0, p1);
+	if (k < 0) return -1;
+	s->pairs[k].disp_roll = V(disp_rolling[0], disp_rolling[1], disp_rolling[2]);
+	return 0;
+}
+
 void lfo_set_clock(lfo_sim *s, double time, double strain, double dt, double shear_rate,
                    double max_velocity, double max_sliding_velocity, int firsttime_done)
 {
@@ -1873,6 +1915,7 @@ lfo_sim *lfo_create(const lfo_params *p, int np, const double *pos, const double
                     double lx, double ly, double lz, const double *le_disp,
                     int ncs, const int *cs_p0, const int *cs_p1, const double *cs_disp_tan)
 {
+	if (p->mu_rolling > 0 && p->friction_model == 0) return NULL;   /* System.cpp:386-391 */
 	lfo_sim *s = calloc(1, sizeof(lfo_sim));
 	s->p = *p;
 	s->np = np;
@@ -1884,6 +1927,7 @@ lfo_sim *lfo_create(const lfo_params *p, int np, const double *pos, const double
 	s->lubrication = p->lubrication_model != 0;
 	s->tangential = p->lubrication_model == 2;
 	s->friction = p->friction_model != 0;
+	s->rolling = p->mu_rolling > 0;
 	if (!s->friction) s->p.mu_static = 0;
 	if (s->p.mu_dynamic < 0) s->p.mu_dynamic = s->p.mu_static;
 	s->repulsiveforce = p->repulsion_on && p->repulsive_length > 0;

@@ -55,6 +55,8 @@ typedef struct {
 	double Ohat[3];
 	double init_strain_shear_rate_limit; /* System.cpp:90 default 0 */
 	double init_shear_rate_limit;        /* System.cpp:91 default 999 */
+	double mu_rolling;               /* > 0 enables rolling friction (System.cpp:386-388) */
+	double kr;                       /* rolling spring constant */
 } lfo_params;
 
 typedef struct lfo_sim lfo_sim;
@@ -118,6 +120,7 @@ void lfo_first_time(lfo_sim *s);
 /* Set the tangential spring and friction state of pair (p0,p1) (Contact.h
  * setState, :161-167).  Returns -1 if no such pair exists. */
 int lfo_set_contact(lfo_sim *s, int p0, int p1, int state, const double *disp_tan);
+int lfo_set_contact_rolling(lfo_sim *s, int p0, int p1, const double *disp_rolling);
 /* Set the clocks and rate (System::clk, shear_rate, dt, max velocities) and
  * mark the first-time set-up of timeEvolution as done or not. */
 void lfo_set_clock(lfo_sim *s, double time, double strain, double dt, double shear_rate,

@@ -41,6 +41,7 @@ class Params(C.Structure):
         ("shear_rate", C.c_double), ("target_stress", C.c_double),
         ("Ehat", C.c_double * 6), ("Ohat", C.c_double * 3),
         ("init_strain_shear_rate_limit", C.c_double), ("init_shear_rate_limit", C.c_double),
+        ("mu_rolling", C.c_double), ("kr", C.c_double),
     ]
 
 
@@ -98,6 +99,8 @@ def lib():
         L.lfo_bsr_solve.argtypes = [C.c_int, dp, C.c_int, ip, ip, dp, C.c_int, dp, dp]
         L.lfo_set_contact.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, dp]
         L.lfo_set_contact.restype = C.c_int
+        L.lfo_set_contact_rolling.argtypes = [C.c_void_p, C.c_int, C.c_int, dp]
+        L.lfo_set_contact_rolling.restype = C.c_int
         L.lfo_set_clock.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double,
                                     C.c_double, C.c_double, C.c_int]
         L.lfo_refresh.argtypes = [C.c_void_p]
@@ -235,6 +238,10 @@ class OracleSim:
         if st:
             raise RuntimeError(f"no pair ({p0},{p1}) in the oracle")
 
+    def set_contact_rolling(self, p0, p1, disp_rolling):
+        d = np.ascontiguousarray(disp_rolling, dtype=np.float64)
+        if lib().lfo_set_contact_rolling(self.h, int(p0), int(p1), d) != 0:
+            raise ValueError(f"no pair ({p0}, {p1})")
     def set_clock(self, time, strain, dt, shear_rate, max_velocity, max_sliding_velocity, firsttime_done=1):
         lib().lfo_set_clock(self.h, time, strain, dt, shear_rate, max_velocity, max_sliding_velocity,
                             int(firsttime_done))

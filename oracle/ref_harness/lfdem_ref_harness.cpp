@@ -83,7 +83,7 @@ static void dump_pairs(System &sys, const char *prefix)
 {
 	size_t n = sys.interaction.size();
 	std::vector<int> ip(n*6);
-	std::vector<double> dp(n*20);
+	std::vector<double> dp(n*23);
 	for (size_t k = 0; k < n; k++) {
 		Interaction &in = sys.interaction[k];
 		auto pr = in.get_par_num();
@@ -93,7 +93,7 @@ static void dump_pairs(System &sys, const char *prefix)
 		ip[6*k+3] = in.contact.getFrictionState();
 		ip[6*k+4] = sys.lubrication ? in.lubrication.is_active() : 0;
 		ip[6*k+5] = in.z_offset;
-		double *d = &dp[20*k];
+		double *d = &dp[23*k];
 		d[0] = in.separation_distance();
 		d[1] = in.get_reduced_gap();
 		d[2] = in.nvec.x; d[3] = in.nvec.y; d[4] = in.nvec.z;
@@ -105,6 +105,7 @@ static void dump_pairs(System &sys, const char *prefix)
 		d[13] = rf.x; d[14] = rf.y; d[15] = rf.z;
 		d[16] = in.rvec.x; d[17] = in.rvec.y; d[18] = in.rvec.z;
 		d[19] = in.contact.relative_surface_velocity_sqnorm;
+		d[20] = in.contact.disp_rolling.x; d[21] = in.contact.disp_rolling.y; d[22] = in.contact.disp_rolling.z;
 	}
 	std::string a = std::string(prefix)+"pairs_i", b = std::string(prefix)+"pairs_d";
 	puti(a.c_str(), ip.data(), ip.size());
@@ -225,6 +226,8 @@ int main(int argc, char **argv)
 		put("Ohat", oh, 3);
 		put1("init_strain_shear_rate_limit", sys.init_strain_shear_rate_limit);
 		put1("init_shear_rate_limit", sys.init_shear_rate_limit);
+		put1("mu_rolling", sys.rolling_friction ? p.mu_rolling : 0.0);
+		put1("kr", sys.rolling_friction ? p.kr : 0.0);
 		put1("lx", sys.get_lx()); put1("ly", sys.get_ly()); put1("lz", sys.get_lz());
 		put("radius", sys.radius.data(), sys.radius.size());
 		put_vec3("position0", sys.position);

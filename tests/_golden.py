@@ -5,13 +5,13 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["rate_n200", "stress_n200", "rate_normal_n200", "rate_2d_n200"]
+CASES = ["rate_n200", "stress_n200", "rate_normal_n200", "rate_2d_n200", "rolling_n200"]
 PARAM_KEYS = ["kn", "kt", "mu_static", "mu_dynamic", "critical_load", "ft_max", "friction_model", "repulsion_on",
               "repulsion", "repulsive_length", "repulsive_max_length", "lubrication_model", "lub_reduce_parameter",
               "lub_max_gap", "interaction_range", "sd_coeff", "contact_relaxation_time",
               "contact_relaxation_time_tan", "disp_max", "dt", "dt_max", "dt_min", "fixed_dt",
               "integration_method", "control", "shear_rate", "target_stress", "Ehat", "Ohat",
-              "init_strain_shear_rate_limit", "init_shear_rate_limit"]
+              "init_strain_shear_rate_limit", "init_shear_rate_limit", "mu_rolling", "kr"]
 
 
 def load(name):
@@ -21,6 +21,8 @@ def load(name):
 def params(F):
     d = {}
     for k in PARAM_KEYS:
+        if "param_" + k not in F:
+            continue
         v = F["param_" + k]
         d[k] = tuple(v) if k in ("Ehat", "Ohat") else float(v[0])
     # the reference resolved interaction_range = -1 to 2 + lub_max_gap and
@@ -35,7 +37,8 @@ def box(F):
 
 def pairs(F, k, when):
     pi = F[f"s{k}_{when}_pairs_i"].reshape(-1, 6)
-    pd = F[f"s{k}_{when}_pairs_d"].reshape(-1, 16)
+    raw = F[f"s{k}_{when}_pairs_d"]
+    pd = raw.reshape(len(pi), -1) if len(pi) else raw.reshape(0, 19)
     o = np.lexsort((pi[:, 1], pi[:, 0]))
     return pi[o], pd[o]
 
@@ -67,6 +70,8 @@ def restore(sim, F, k):
     for a, d in zip(pi, pd):
         if a[2]:  # contact active
             sim.set_contact(int(a[0]), int(a[1]), int(a[3]), d[5:8].copy())
+            if len(d) >= 19:
+                sim.set_contact_rolling(int(a[0]), int(a[1]), d[16:19].copy())
     sim.refresh()
     sim.set_clock(float(F[f"s{k}_pre_time"][0]), float(F[f"s{k}_pre_strain"][0]), float(F[f"s{k}_pre_dt"][0]),
                   float(F[f"s{k}_pre_shear_rate"][0]), float(F[f"s{k}_pre_max_velocity"][0]),

@@ -21,5 +21,10 @@ STRESS_PARAMS.update(friction_model=2, critical_load=1.0, repulsion_on=0, repuls
                      shear_rate=0.0, target_stress=10.0 / 6 / np.pi)
 
 
+# rolling friction on top of the rate-controlled set (Contact.cpp:162-180, 283-305)
+ROLLING_PARAMS = dict(RATE_PARAMS)
+ROLLING_PARAMS.update(mu_rolling=0.2, kr=5e3)
+
+
 def make_packing(n, vf, seed):
     return packing.generate(n, vf, seed=seed)

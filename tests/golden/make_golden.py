@@ -59,6 +59,18 @@ contact_relaxation_time = 2e-3r;
 sd_coeff = 0.5;
 time_end = 1h;
 """),
+    # rolling friction (mu_rolling > 0, Contact.cpp:162-180, 283-305, 431-435)
+    "rolling_n200": dict(n=200, vf=0.5, seed=105, control="r", value="1", suffix="r", steps=4, calc_stress=1,
+                         params="""
+lub_reduce_parameter = 1e-3;
+lub_max_gap = 0.5;
+kn = 1e4r;
+kt = 0.5kn;
+kr = 0.5kn;
+mu_static = 1;
+mu_rolling = 0.2;
+time_end = 2h;
+"""),
     # 2D monolayer (ly = 0 in the configuration): the reference's twodimension path
     "rate_2d_n200": dict(n=200, vf=0.7, seed=104, control="r", value="1", suffix="r", steps=4, calc_stress=1,
                          twodim=True, params="""
@@ -101,7 +113,10 @@ def run_case(name, c, workdir):
         last = k == c["steps"]-1
         for key, v in R.items():
             if key.endswith("pairs_d"):
-                v = v.reshape(-1, 20)[:, :16].reshape(-1)   # drop rvec / sliding velocity columns
+                # keep r, gap, n, disp_tan, f_spring_total, lub coefficients, repulsion and
+                # disp_rolling; drop rvec and the sliding velocity
+                v = v.reshape(-1, 23)
+                v = np.concatenate([v[:, :16], v[:, 20:23]], axis=1).reshape(-1)
             if key in keep_pre or key in keep_post or (k == 0 and key.startswith("stage_")) or \
                     (last and key.startswith("post_stress_")):
                 data[f"s{k}_{key}"] = v

@@ -4,7 +4,7 @@ velocities, pair list and contact states, stresslets) on seeded packings."""
 import numpy as np
 import pytest
 
-from _systems import RATE_PARAMS, STRESS_PARAMS, make_packing
+from _systems import RATE_PARAMS, ROLLING_PARAMS, STRESS_PARAMS, make_packing
 
 pytestmark = pytest.mark.gpu
 
@@ -45,7 +45,8 @@ def test_initial_pairs_and_blocks(oracle, engine, params):
 
 
 @pytest.mark.parametrize("params,n,vf,seed", [(RATE_PARAMS, 200, 0.45, 32), (STRESS_PARAMS, 200, 0.5, 33),
-                                              (RATE_PARAMS, 500, 0.5, 34)], ids=["rate200", "stress200", "rate500"])
+                                              (RATE_PARAMS, 500, 0.5, 34), (ROLLING_PARAMS, 300, 0.52, 35)],
+                         ids=["rate200", "stress200", "rate500", "rolling300"])
 def test_steps_match_oracle(oracle, engine, params, n, vf, seed):
     p, o, g = _make(oracle, engine, params, n, vf, seed)
     for k in range(4):
