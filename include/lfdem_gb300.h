@@ -93,6 +93,16 @@ typedef struct {
 	double kr;                       /* rolling spring constant (Contact.cpp:35-45) */
 } lfg_params;
 
+/* LF_DEM's Parameter_File (the text of the file) and command-line control
+ * ('r' with e.g. "1r" for `-r 1r`, 's' with e.g. "10cl" for `-s 10cl`)
+ * resolved by the reference's own rules (SimulationInit.cpp:156-1014:
+ * defaults, keyword parsing, unit suffixes, non-dimensionalisation; then
+ * System.cpp:348-414) into the flat parameters above.  time_end / strain_end
+ * are System::timeEvolution's arguments (the one not given is -1).  Brownian
+ * and cohesive forces are refused (LFG_ERR_BAD_ARG, message in st). */
+int lfg_config_resolve(const char *parameter_text, char control, const char *control_value,
+                       lfg_params *out, double *time_end, double *strain_end, lfg_status *st);
+
 /* Engine options (not physics). */
 typedef struct {
 	int precision;          /* LFG_PREC_* */

@@ -124,7 +124,7 @@ EXPORTS = [
     "lfg_sim_get_velocity_component", "lfg_sim_set_contact", "lfg_sim_set_clock", "lfg_sim_refresh",
     "lfg_sim_assemble", "lfg_sim_force_component", "lfg_sim_get_timing", "lfg_sim_get_step_times",
     "lfg_sim_clear_step_times", "lfg_sim_destroy", "lfg_sim_force_component_noalloc",
-    "lfg_sim_advance_partial", "lfg_sim_set_contact_rolling", "lfg_sim_set_leaf_size", "lfg_sim_device_bytes", "lfg_footprint_estimate",
+    "lfg_sim_advance_partial", "lfg_sim_set_contact_rolling", "lfg_config_resolve", "lfg_sim_set_leaf_size", "lfg_sim_device_bytes", "lfg_footprint_estimate",
     "lfg_batch_create", "lfg_batch_add", "lfg_batch_size", "lfg_batch_sim", "lfg_batch_run", "lfg_batch_advance",
     "lfg_batch_autotune", "lfg_batch_tuned_leaf", "lfg_batch_destroy",
     "lfg_server_create", "lfg_server_submit", "lfg_server_poll", "lfg_server_wait", "lfg_server_final_positions",
@@ -164,6 +164,8 @@ def load(path: str | None = None):
     L.lfg_solver_get_stats.argtypes = [vp, C.POINTER(SolverStats)]
     L.lfg_solver_destroy.argtypes = [vp]
     L.lfg_solver_destroy.restype = None
+    L.lfg_config_resolve.argtypes = [C.c_char_p, C.c_char, C.c_char_p, C.POINTER(Params), C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), pst]
     if hasattr(L, "lfg_sim_create"):
         L.lfg_sim_create.argtypes = [C.POINTER(Params), C.POINTER(Options), C.c_int, vp, vp, C.c_double,
                                      C.c_double, C.c_double, vp, C.c_int, vp, vp, vp, C.POINTER(vp), pst]
@@ -299,6 +301,23 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+
+def resolve_config(parameter_text: str, control: str, control_value: str):
+    """LF_DEM's Parameter_File + `-r value` / `-s value` resolved by the
+    reference's unit system (lfg_config_resolve): (parameter dict, time_end,
+    strain_end)."""
+    p = Params()
+    te, se = C.c_double(), C.c_double()
+    st = Status()
+    rc = load().lfg_config_resolve(parameter_text.encode(), control.encode(), control_value.encode(), C.byref(p),
+                                   C.byref(te), C.byref(se), C.byref(st))
+    _check(rc, st)
+    d = {}
+    for k, _ in Params._fields_:
+        v = getattr(p, k)
+        d[k] = tuple(v) if k in ("Ehat", "Ohat") else v
+    return d, te.value, se.value
 
 
 def make_params(d: dict) -> Params:
