@@ -103,6 +103,27 @@ typedef struct {
 int lfg_config_resolve(const char *parameter_text, char control, const char *control_value,
                        lfg_params *out, double *time_end, double *strain_end, lfg_status *st);
 
+/* LF_DEM's checkpoint files (Simulation::checkpoint, Simulation.cpp:602-611).
+ * Binary configuration conf_*.dat (Simulation.cpp:513-600, Configuration.h:
+ * 67-120): written in the labelled format 2; read in format 2 and in the old
+ * unlabelled format (unsigned-short contact particle numbers recognised as
+ * the reference does).  lfg_conf_read_binary: call with NULL arrays to get
+ * *np and *ncont, then with arrays of 3np (pos), np (radius), ncont (p0, p1)
+ * and 3ncont (disp_tan, disp_rolling); meta = vf, lx, ly, lz, le_disp x, y.
+ * State file chk_*.dat (States.cpp:9-66): format 1, strain, time, time in
+ * simulation units.  Host I/O only. */
+int lfg_conf_write_binary(const char *path, int np, double vf, double lx, double ly, double lz,
+                          const double *le_disp, const double *pos, const double *radius, int ncont,
+                          const int32_t *p0, const int32_t *p1, const double *disp_tan,
+                          const double *disp_rolling, lfg_status *st);
+int lfg_conf_read_binary(const char *path, int *np, int *ncont, int *format, double *meta, double *pos,
+                         double *radius, int32_t *p0, int32_t *p1, double *disp_tan, double *disp_rolling,
+                         lfg_status *st);
+int lfg_checkpoint_write(const char *path, double strain, double time, double time_in_simulation_units,
+                         lfg_status *st);
+int lfg_checkpoint_read(const char *path, double *strain, double *time, double *time_in_simulation_units,
+                        lfg_status *st);
+
 /* Engine options (not physics). */
 typedef struct {
 	int precision;          /* LFG_PREC_* */
@@ -239,6 +260,12 @@ int lfg_sim_get_velocity_component(lfg_sim *s, int comp, double *out);
 int lfg_sim_set_contact(lfg_sim *s, int p0, int p1, int state, const double *disp_tan);
 /* The rolling spring of that contact (contact_state.disp_rolling, Contact.h:150-162). */
 int lfg_sim_set_contact_rolling(lfg_sim *s, int p0, int p1, const double *disp_rolling);
+/* Active contacts and their springs (System::getContacts, System.cpp:306-320),
+ * sorted by (p0, p1): returns the count and copies up to cap of them
+ * (disp_tan, disp_rolling: 3 per contact; any array may be NULL); a negative
+ * value is an error code. */
+int lfg_sim_get_contact_states(lfg_sim *s, int32_t *p0, int32_t *p1, double *disp_tan,
+                               double *disp_rolling, int cap);
 int lfg_sim_set_clock(lfg_sim *s, double time, double strain, double dt, double shear_rate,
                       double max_velocity, double max_sliding_velocity);
 int lfg_sim_refresh(lfg_sim *s);

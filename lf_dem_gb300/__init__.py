@@ -124,7 +124,9 @@ EXPORTS = [
     "lfg_sim_get_velocity_component", "lfg_sim_set_contact", "lfg_sim_set_clock", "lfg_sim_refresh",
     "lfg_sim_assemble", "lfg_sim_force_component", "lfg_sim_get_timing", "lfg_sim_get_step_times",
     "lfg_sim_clear_step_times", "lfg_sim_destroy", "lfg_sim_force_component_noalloc",
-    "lfg_sim_advance_partial", "lfg_sim_set_contact_rolling", "lfg_config_resolve", "lfg_sim_set_leaf_size", "lfg_sim_device_bytes", "lfg_footprint_estimate",
+    "lfg_sim_advance_partial", "lfg_sim_set_contact_rolling", "lfg_config_resolve",
+    "lfg_sim_get_contact_states", "lfg_conf_write_binary", "lfg_conf_read_binary", "lfg_checkpoint_write",
+    "lfg_checkpoint_read", "lfg_sim_set_leaf_size", "lfg_sim_device_bytes", "lfg_footprint_estimate",
     "lfg_batch_create", "lfg_batch_add", "lfg_batch_size", "lfg_batch_sim", "lfg_batch_run", "lfg_batch_advance",
     "lfg_batch_autotune", "lfg_batch_tuned_leaf", "lfg_batch_destroy",
     "lfg_server_create", "lfg_server_submit", "lfg_server_poll", "lfg_server_wait", "lfg_server_final_positions",
@@ -164,6 +166,13 @@ def load(path: str | None = None):
     L.lfg_solver_get_stats.argtypes = [vp, C.POINTER(SolverStats)]
     L.lfg_solver_destroy.argtypes = [vp]
     L.lfg_solver_destroy.restype = None
+    L.lfg_conf_write_binary.argtypes = [C.c_char_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                        vp, vp, vp, C.c_int, vp, vp, vp, vp, pst]
+    L.lfg_conf_read_binary.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                       vp, vp, vp, vp, vp, vp, vp, pst]
+    L.lfg_checkpoint_write.argtypes = [C.c_char_p, C.c_double, C.c_double, C.c_double, pst]
+    L.lfg_checkpoint_read.argtypes = [C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                      C.POINTER(C.c_double), pst]
     L.lfg_config_resolve.argtypes = [C.c_char_p, C.c_char, C.c_char_p, C.POINTER(Params), C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), pst]
     if hasattr(L, "lfg_sim_create"):
@@ -180,6 +189,7 @@ def load(path: str | None = None):
         L.lfg_sim_get_velocity_component.argtypes = [vp, C.c_int, vp]
         L.lfg_sim_set_contact.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp]
         L.lfg_sim_set_contact_rolling.argtypes = [vp, C.c_int, C.c_int, vp]
+        L.lfg_sim_get_contact_states.argtypes = [vp, vp, vp, vp, vp, C.c_int]
         L.lfg_sim_set_clock.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                         C.c_double]
         L.lfg_sim_refresh.argtypes = [vp]
@@ -320,6 +330,56 @@ def resolve_config(parameter_text: str, control: str, control_value: str):
     return d, te.value, se.value
 
 
+def write_conf_binary(path, position, radius, lx, ly, lz, vf, le_disp=(0.0, 0.0), contacts=None):
+    """LF_DEM binary configuration (format 2).  contacts: (p0, p1, disp_tan,
+    disp_rolling) arrays or None."""
+    pos = np.ascontiguousarray(position, dtype=np.float64).reshape(-1)
+    rad = np.ascontiguousarray(radius, dtype=np.float64)
+    led = np.ascontiguousarray(le_disp, dtype=np.float64)
+    st = Status()
+    if contacts is not None and len(contacts[0]):
+        p0 = np.ascontiguousarray(contacts[0], dtype=np.int32)
+        p1 = np.ascontiguousarray(contacts[1], dtype=np.int32)
+        dt = np.ascontiguousarray(contacts[2], dtype=np.float64).reshape(-1)
+        dr = np.ascontiguousarray(contacts[3], dtype=np.float64).reshape(-1)
+        args = (len(p0), _ptr(p0), _ptr(p1), _ptr(dt), _ptr(dr))
+    else:
+        args = (0, None, None, None, None)
+    _check(load().lfg_conf_write_binary(str(path).encode(), len(rad), vf, lx, ly, lz, _ptr(led), _ptr(pos), _ptr(rad),
+                                        *args, C.byref(st)), st)
+
+
+def read_conf_binary(path):
+    """LF_DEM binary configuration -> dict(format, vf, lx, ly, lz, le_disp,
+    position, radius, p0, p1, disp_tan, disp_rolling)."""
+    L = load()
+    np_, nc, fmt = C.c_int(), C.c_int(), C.c_int()
+    st = Status()
+    _check(L.lfg_conf_read_binary(str(path).encode(), C.byref(np_), C.byref(nc), C.byref(fmt), None, None, None, None,
+                                  None, None, None, C.byref(st)), st)
+    n, k = np_.value, nc.value
+    meta, pos, rad = np.zeros(6), np.zeros(3 * n), np.zeros(n)
+    p0, p1 = np.zeros(max(k, 1), dtype=np.int32), np.zeros(max(k, 1), dtype=np.int32)
+    dt, dr = np.zeros(3 * max(k, 1)), np.zeros(3 * max(k, 1))
+    _check(L.lfg_conf_read_binary(str(path).encode(), C.byref(np_), C.byref(nc), C.byref(fmt), _ptr(meta), _ptr(pos),
+                                  _ptr(rad), _ptr(p0), _ptr(p1), _ptr(dt), _ptr(dr), C.byref(st)), st)
+    return dict(format=fmt.value, vf=meta[0], lx=meta[1], ly=meta[2], lz=meta[3], le_disp=tuple(meta[4:6]),
+                position=pos.reshape(-1, 3), radius=rad, p0=p0[:k], p1=p1[:k], disp_tan=dt[:3 * k].reshape(-1, 3),
+                disp_rolling=dr[:3 * k].reshape(-1, 3))
+
+
+def write_checkpoint(path, strain, time, time_in_simulation_units):
+    st = Status()
+    _check(load().lfg_checkpoint_write(str(path).encode(), strain, time, time_in_simulation_units, C.byref(st)), st)
+
+
+def read_checkpoint(path):
+    a, b, c = C.c_double(), C.c_double(), C.c_double()
+    st = Status()
+    _check(load().lfg_checkpoint_read(str(path).encode(), C.byref(a), C.byref(b), C.byref(c), C.byref(st)), st)
+    return a.value, b.value, c.value
+
+
 def make_params(d: dict) -> Params:
     """lfg_params from a dict of already non-dimensionalised values."""
     p = Params()
@@ -448,6 +508,17 @@ class Sim:
         rc = load().lfg_sim_set_contact(self.h, int(p0), int(p1), int(state), _ptr(d))
         if rc:
             raise LFGError(rc, f"no pair ({p0},{p1})")
+
+    def contact_states(self):
+        """Active contacts (p0, p1, disp_tan, disp_rolling), sorted by (p0, p1)."""
+        L = load()
+        k = L.lfg_sim_get_contact_states(self.h, None, None, None, None, 0)
+        if k < 0:
+            raise LFGError(-k, "contact states")
+        p0, p1 = np.zeros(max(k, 1), dtype=np.int32), np.zeros(max(k, 1), dtype=np.int32)
+        dt, dr = np.zeros(3 * max(k, 1)), np.zeros(3 * max(k, 1))
+        L.lfg_sim_get_contact_states(self.h, _ptr(p0), _ptr(p1), _ptr(dt), _ptr(dr), k)
+        return p0[:k], p1[:k], dt[:3 * k].reshape(-1, 3), dr[:3 * k].reshape(-1, 3)
 
     def set_contact_rolling(self, p0, p1, disp_rolling):
         d = np.ascontiguousarray(disp_rolling, dtype=np.float64)

@@ -35,6 +35,7 @@ public:
 	void particles(double *pos, double *vel, double *ang, double *na_vel, double *na_ang);
 	int num_pairs();
 	int get_pairs(lfg_pair *out, int cap);
+	int contact_states(int32_t *p0, int32_t *p1, double *dt, double *dr, int cap);
 	int particle_stress(int comp, double *out);
 	int velocity_component(int comp, double *out);
 	int set_contact(int p0, int p1, int state, const double *disp_tan, const double *disp_roll = nullptr);
@@ -526,6 +527,29 @@ int Sim::num_pairs()
 	return c;
 }
 
+// active contacts with their springs (System::getContacts, System.cpp:306-320),
+// sorted by (p0, p1)
+int Sim::contact_states(int32_t *p0, int32_t *p1, double *dt, double *dr, int cap)
+{
+	std::vector<DPair> pairs(S_.npairs);
+	if (S_.npairs) LFG_CUDA(cudaMemcpyAsync(pairs.data(), S_.pairs, sizeof(DPair)*S_.npairs, cudaMemcpyDeviceToHost, st_));
+	LFG_CUDA(cudaStreamSynchronize(st_));
+	int c = 0;
+	for (const DPair &q : pairs) {
+		if (!(q.flags & PF_INTER) || !(q.flags & PF_CONTACT)) continue;
+		if (c < cap) {
+			if (p0) p0[c] = q.p0;
+			if (p1) p1[c] = q.p1;
+			for (int k = 0; k < 3; k++) {
+				if (dt) dt[3*c+k] = q.disp_tan[k];
+				if (dr) dr[3*c+k] = q.disp_roll[k];
+			}
+		}
+		c++;
+	}
+	return c;
+}
+
 int Sim::get_pairs(lfg_pair *out, int cap)
 {
 	std::vector<DPair> pairs(S_.npairs);
@@ -858,6 +882,20 @@ int lfg_sim_set_contact(lfg_sim *h, int p0, int p1, int state, const double *dis
 	SIM_GUARD_BEGIN
 	return h->s->set_contact(p0, p1, state, disp_tan);
 	SIM_GUARD_END
+}
+
+int lfg_sim_get_contact_states(lfg_sim *h, int32_t *p0, int32_t *p1, double *disp_tan, double *disp_rolling,
+                               int cap)
+{
+	lfg_status *st = nullptr;
+	if (!h || cap < 0) return -LFG_ERR_BAD_ARG;
+	try {
+		cudaSetDevice(h->device);
+		return h->s->contact_states(p0, p1, disp_tan, disp_rolling, cap);
+	} catch (...) {
+		(void)st;
+		return -LFG_ERR_CUDA;
+	}
 }
 
 int lfg_sim_set_contact_rolling(lfg_sim *h, int p0, int p1, const double *disp_rolling)

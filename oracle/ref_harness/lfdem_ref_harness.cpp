@@ -46,6 +46,7 @@
 #define private public
 #define protected public
 #include "Simulation.h"
+#include "States.h"
 #undef private
 #undef protected
 
@@ -274,5 +275,9 @@ int main(int argc, char **argv)
 		}
 		fclose(g_out);
 	}
+	// checkpoint of the final state in the reference's own formats
+	// (Simulation::checkpoint, Simulation.cpp:602-611)
+	sim.outputConfigurationBinary(outdir+"/conf.bin");
+	State::outputStateBinary(outdir+"/chk.bin", sys);
 	return 0;
 }

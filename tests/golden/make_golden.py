@@ -121,6 +121,10 @@ def run_case(name, c, workdir):
                     (last and key.startswith("post_stress_")):
                 data[f"s{k}_{key}"] = v
     data["nsteps"] = np.array([c["steps"]])
+    # the reference's checkpoint of the final state (Simulation::checkpoint)
+    for fn, key in (("conf.bin", "conf_bin"), ("chk.bin", "chk_bin")):
+        with open(os.path.join(out, fn), "rb") as f:
+            data[key] = np.frombuffer(f.read(), dtype=np.uint8)
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **data)
     return os.path.getsize(os.path.join(HERE, f"{name}.npz"))
 
