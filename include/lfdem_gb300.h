@@ -258,7 +258,9 @@ int lfg_sim_get_velocity_component(lfg_sim *s, int comp, double *out);
  * tangential spring and friction state; set clocks; recompute every pair's
  * forces at the current positions with dt = 0 (System.cpp:1216-1226). */
 int lfg_sim_set_contact(lfg_sim *s, int p0, int p1, int state, const double *disp_tan);
-/* The rolling spring of that contact (contact_state.disp_rolling, Contact.h:150-162). */
+/* The rolling spring of that contact (contact_state.disp_rolling, Contact.h:150-162).
+ * On restart, set the rolling springs after lfg_sim_create and then call
+ * lfg_sim_refresh, so the first step starts from forces that include them. */
 int lfg_sim_set_contact_rolling(lfg_sim *s, int p0, int p1, const double *disp_rolling);
 /* Active contacts and their springs (System::getContacts, System.cpp:306-320),
  * sorted by (p0, p1): returns the count and copies up to cap of them

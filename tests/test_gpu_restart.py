@@ -33,6 +33,7 @@ def test_restart_from_checkpoint_matches_oracle(engine, oracle, tmp_path):
     for a, b, d in zip(c["p0"], c["p1"], c["disp_rolling"]):
         r.set_contact_rolling(int(a), int(b), d)
         o.set_contact_rolling(int(a), int(b), d)
+    r.refresh()   # creation already ran the first-time force update; redo it with the rolling springs
     o.first_time()
     for sim in (r, o):
         sim.set_clock(time, strain, sc["dt"], sc["shear_rate"], sc["max_velocity"], sc["max_sliding_velocity"])
