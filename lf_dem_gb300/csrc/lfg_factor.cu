@@ -33,7 +33,7 @@
 namespace lfg {
 
 enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLAN_SYRK = 5,
-       PLAN_DIAG = 6 };
+       PLAN_DIAG = 6, PLAN_SYRK_TC = 8 };
 constexpr int PANEL_ROWS = 128;  // rows per panel (k_trsm) task (must match the plan)
 constexpr int SOLVE_WARPS = 8;
 constexpr int SOLVE_CB = 8;      // columns per CTA of the solve's column kernels
@@ -615,45 +615,25 @@ __device__ inline void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t 
 }
 } // namespace umma
 
-__global__ void __launch_bounds__(umma::THREADS, 1) k_syrk_tc(const int4 *__restrict__ tasks,
-                                                              const int *__restrict__ sn_n,
-                                                              const int *__restrict__ sn_m,
-                                                              const int *__restrict__ sn_ld,
-                                                              const int64_t *__restrict__ sn_off,
-                                                              float *__restrict__ arena, int *fail)
+// One 128 x 128 tile C -= A B^T on the tensor cores, for the calling CTA
+// (umma::THREADS threads): rows r0 + [0, 128) of A and c0 + [0, 128) of B
+// taken from the front's columns [k0, k1) (A and B are rows of the same
+// column-major front), C[r][c] at base[c ld + r] for r < rlim, c < clim and,
+// when lower_only, r >= c.  tmem: this CTA's 128 accumulator columns; mbar:
+// its STAGES mbarriers (fresh: phase 0).  Returns false if a wait timed out.
+__device__ bool tc_tile_update(float *base, int ld, int r0, int c0, int k0, int k1, int rlim, int clim,
+                               bool lower_only, unsigned char *sm, uint64_t *mbar, uint32_t tmem)
 {
 	using namespace umma;
-	extern __shared__ unsigned char smem_tc[];
-	__shared__ __align__(8) uint64_t mbar[STAGES];
-	__shared__ uint32_t tmem_slot;
-	unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_tc)+1023) &
-	                                                      ~static_cast<uintptr_t>(1023));
-	int4 tk = tasks[blockIdx.x];
-	int s = tk.x, r0 = tk.y, c0 = tk.z;
-	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
-	float *base = arena+sn_off[s];
-	int tid = threadIdx.x, warp = tid/32, lane = tid%32;
-	if (warp == 0) {
-		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-		             :: "r"(saddr(&tmem_slot)), "r"(N));
-		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-		asm volatile("tcgen05.fence::before_thread_sync;");
-	}
-	if (tid == 0) {
-		for (int q = 0; q < STAGES; q++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&mbar[q])));
-		asm volatile("fence.mbarrier_init.release.cluster;");
-	}
-	__syncthreads();
-	asm volatile("tcgen05.fence::after_thread_sync;");
-	uint32_t tmem = tmem_slot;
-	int nchunk = (n6+KC-1)/KC;
+	const int tid = threadIdx.x, warp = tid/32, lane = tid%32;
+	int nchunk = (k1-k0+KC-1)/KC;
 	uint32_t phase_bits = 0;   // bit q: parity expected at the next wait on stage q
 	bool ok = true;
 	int issued = 0;
 	// staging role: row m of both operands, K half h of the chunk
 	const int m = tid & (M-1), h = tid >> 7;
 	const int ra = r0+m, rb = c0+m;
-	const bool va = ra < F6, vb = rb < F6;
+	const bool va = ra < rlim, vb = rb < clim;
 	for (int ch = 0; ch < nchunk; ch++) {
 		int b = ch % STAGES;
 		if (ch >= STAGES) {
@@ -662,13 +642,13 @@ __global__ void __launch_bounds__(umma::THREADS, 1) k_syrk_tc(const int4 *__rest
 		}
 		if (!__syncthreads_and(ok)) { ok = false; break; }
 		unsigned char *stg = sm+b*STAGE_BYTES;
-		int tb = ch*KC+16*h;
+		int tb = k0+ch*KC+16*h;
 		float av[16], bv[16];
 #pragma unroll
 		for (int k = 0; k < 16; k++) {
 			int t = tb+k;
-			av[k] = (t < n6 && va) ? base[(int64_t)t*ld+ra] : 0.f;
-			bv[k] = (t < n6 && vb) ? base[(int64_t)t*ld+rb] : 0.f;
+			av[k] = (t < k1 && va) ? base[(int64_t)t*ld+ra] : 0.f;
+			bv[k] = (t < k1 && vb) ? base[(int64_t)t*ld+rb] : 0.f;
 		}
 #pragma unroll
 		for (int k = 0; k < 16; k++) {
@@ -722,14 +702,60 @@ __global__ void __launch_bounds__(umma::THREADS, 1) k_syrk_tc(const int4 *__rest
 #pragma unroll
 			for (int j = 0; j < 16; j++) {
 				int c = c0+cb+j;
-				if (r < F6 && c < F6 && r >= c) base[(int64_t)c*ld+r] -= __uint_as_float(v[j]);
+				if (r < rlim && c < clim && (!lower_only || r >= c)) base[(int64_t)c*ld+r] -= __uint_as_float(v[j]);
 			}
 		}
 	}
 	asm volatile("tcgen05.fence::before_thread_sync;");
 	__syncthreads();
-	if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(N));
-	if (!ok && tid == 0 && fail) atomicMin(fail, 0);
+	return ok;
+}
+
+// tensor memory (128 columns) and the stage mbarriers of a tensor-core CTA
+__device__ inline uint32_t tc_setup(uint32_t *tmem_slot, uint64_t *mbar)
+{
+	using namespace umma;
+	if (threadIdx.x/32 == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+		             :: "r"(saddr(tmem_slot)), "r"(N));
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+		asm volatile("tcgen05.fence::before_thread_sync;");
+	}
+	if (threadIdx.x == 0) {
+		for (int q = 0; q < STAGES; q++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&mbar[q])));
+		asm volatile("fence.mbarrier_init.release.cluster;");
+	}
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;");
+	return *tmem_slot;
+}
+
+__device__ inline void tc_teardown(uint32_t tmem)
+{
+	if (threadIdx.x/32 == 0)
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(umma::N));
+}
+
+// Schur complement tile: U[r][c] -= sum_{t < 6n} L[r][t] L[c][t], lower part of [6n, 6F)^2
+__global__ void __launch_bounds__(umma::THREADS, 1) k_syrk_tc(const int4 *__restrict__ tasks,
+                                                              const int *__restrict__ sn_n,
+                                                              const int *__restrict__ sn_m,
+                                                              const int *__restrict__ sn_ld,
+                                                              const int64_t *__restrict__ sn_off,
+                                                              float *__restrict__ arena, int *fail)
+{
+	extern __shared__ unsigned char smem_tc[];
+	__shared__ __align__(8) uint64_t mbar[umma::STAGES];
+	__shared__ uint32_t tmem_slot;
+	unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_tc)+1023) &
+	                                                      ~static_cast<uintptr_t>(1023));
+	int4 tk = tasks[blockIdx.x];
+	int s = tk.x, r0 = tk.y, c0 = tk.z;
+	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
+	uint32_t tmem = tc_setup(&tmem_slot, mbar);
+	bool ok = tc_tile_update(arena+sn_off[s], ld, r0, c0, 0, n6, F6, F6, true, sm, mbar, tmem);
+	tc_teardown(tmem);
+	if (!ok && threadIdx.x == 0 && fail) atomicMin(fail, 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -847,12 +873,13 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 			                                                    D.sn_ld, D.sn_off, F.arena, F.linv, D.nsn, F.status);
 			break;
 		case PLAN_SYRK:
-			if (std::is_same<T, float>::value)
-				k_syrk_tc<<<L.count, umma::THREADS, umma::SMEM_BYTES, st>>>(D.tile_tasks+L.off, D.sn_n, D.sn_m, D.sn_ld,
-				                                                   D.sn_off, reinterpret_cast<float *>(F.arena),
-				                                                   F.status);
-			else
-				k_syrk<T><<<L.count, 256, 0, st>>>(D.tile_tasks+L.off, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, F.arena);
+			k_syrk<T><<<L.count, 256, 0, st>>>(D.tile_tasks+L.off, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, F.arena);
+			break;
+		case PLAN_SYRK_TC:
+			if (!std::is_same<T, float>::value) throw Error{LFG_ERR_BAD_ARG, 0, "tensor-core plan for FP64"};
+			k_syrk_tc<<<L.count, umma::THREADS, umma::SMEM_BYTES, st>>>(D.tile_tasks+L.off, D.sn_n, D.sn_m, D.sn_ld,
+			                                                           D.sn_off, reinterpret_cast<float *>(F.arena),
+			                                                           F.status);
 			break;
 		}
 		launches++;

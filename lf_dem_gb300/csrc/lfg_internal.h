@@ -117,7 +117,7 @@ int factor_panel_width(int precision);
 int factor_panel_rows();
 
 void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb, int tile, int syrk_tile,
-                         cudaStream_t st);
+                         bool tensor_cores, cudaStream_t st);
 void dev_symbolic_free(DevSymbolic &D);
 
 // Factor arenas and launchers (lfg_factor.cu).

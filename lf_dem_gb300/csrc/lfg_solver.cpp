@@ -59,7 +59,7 @@ void Solver::set_pattern(int nb, const int32_t *row, const int32_t *col, const d
 	pat_box_[0] = lx; pat_box_[1] = ly; pat_box_[2] = lz;
 	symbolic_analyze(S_, n_, nb, r.data(), c.data(), pos, lx, ly, lz, opt_.leaf_size);
 	dev_symbolic_upload(D_, S_, nb, factor_panel_width(opt_.precision), factor_tile_size(opt_.precision),
-	                    factor_syrk_tile_size(opt_.precision), st_);
+	                    factor_syrk_tile_size(opt_.precision), opt_.precision == LFG_PREC_FP32_REFINE, st_);
 	if (opt_.precision == LFG_PREC_FP64) factor_alloc(F64_, D_, 4);
 	else factor_alloc(F32_, D_, 4);
 	// block matrix pattern + row adjacency for the residual

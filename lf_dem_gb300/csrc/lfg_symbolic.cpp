@@ -478,10 +478,17 @@ void dev_symbolic_free(DevSymbolic &D)
 
 // Launch kinds of the factor plan (interpreted by factor_numeric).
 enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLAN_SYRK = 5,
-       PLAN_DIAG = 6 };
+       PLAN_DIAG = 6, PLAN_SYRK_TC = 8 };
+
+// levels whose largest front has at least this many pivot columns compute the
+// Schur complement on the tensor cores; below, the K loop is a few chunks and
+// the CUDA-core kernel is as fast.  (The in-front update of a panel step has
+// K = 64 only: on the tensor cores its tiles cost the same staging and
+// read-modify-write and ran slower, so it stays on the CUDA cores.)
+constexpr int TC_SYRK_MIN_N6 = 192;
 
 void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb, int tile, int syrk_tile,
-                         cudaStream_t st)
+                         bool tensor_cores, cudaStream_t st)
 {
 	dev_symbolic_free(D);
 	D.nblk = S.nblk; D.nsn = S.nsn; D.nlevels = S.nlevels; D.nb = nb;
@@ -570,7 +577,8 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 					tile_tasks.push_back(make_int4(s, r, c, 0));
 		}
 		if ((int64_t)tile_tasks.size() > s0)
-			D.factor_plan.push_back({PLAN_SYRK, l, 0, s0, (int)((int64_t)tile_tasks.size()-s0)});
+			D.factor_plan.push_back({tensor_cores && D.h_level_maxn6[l] >= TC_SYRK_MIN_N6 ? PLAN_SYRK_TC : PLAN_SYRK,
+			                         l, 0, s0, (int)((int64_t)tile_tasks.size()-s0)});
 	}
 	up(D.col_tasks, col_tasks, st);
 	up(D.panel_tasks, panel_tasks, st);
