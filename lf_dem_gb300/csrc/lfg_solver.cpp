@@ -209,15 +209,25 @@ int Solver::solve_device(int k, const double *b, double *x, lfg_status *st, bool
 	int64_t tot = (int64_t)6*n_*k;
 	LFG_CUDA(cudaMemsetAsync(ref_x_, 0, sizeof(double)*tot, st_));
 	LFG_CUDA(cudaMemcpyAsync(ref_r_, b, sizeof(double)*tot, cudaMemcpyDeviceToDevice, st_));
+	// One refinement iteration: d = (LL^T)^-1 r in FP32, x += d, r = b - A x in
+	// FP64.  The first launch runs as many iterations as the previous solve
+	// needed (captured together, one host check at the end), then one at a
+	// time until the tolerance is met.
+	auto iteration = [&]() {
+		launches_solve_ = factor_solve(F32_, D_, k, ref_r_, ref_d_, st_);
+		axpy_vec(n_, k, ref_d_, ref_x_, st_);
+		block_residual(A_, k, b, ref_x_, ref_r_, st_);
+	};
 	int it = 0;
 	double worst = 0;
-	for (it = 1; it <= opt_.refine_max_iter; it++) {
-		run_graph(2, k, b, nullptr, [&]() {
-			launches_solve_ = factor_solve(F32_, D_, k, ref_r_, ref_d_, st_);
-			axpy_vec(n_, k, ref_d_, ref_x_, st_);
-			block_residual(A_, k, b, ref_x_, ref_r_, st_);
+	int batch = std::max(1, std::min(pred_iters_, opt_.refine_max_iter));
+	while (it < opt_.refine_max_iter) {
+		int j = std::min(batch, opt_.refine_max_iter-it);
+		run_graph(2, k*64+j, b, nullptr, [&]() {
+			for (int q = 0; q < j; q++) iteration();
 			residual_norms(6*n_, k, ref_r_, b, d_norms_, st_);
 		});
+		it += j;
 		LFG_CUDA(cudaMemcpyAsync(h_norms_, d_norms_, sizeof(double)*2*k, cudaMemcpyDeviceToHost, st_));
 		LFG_CUDA(cudaStreamSynchronize(st_));
 		worst = 0;
@@ -227,8 +237,10 @@ int Solver::solve_device(int k, const double *b, double *x, lfg_status *st, bool
 			worst = std::max(worst, rb);
 		}
 		if (worst <= opt_.refine_tol) break;
+		batch = 1;
 	}
-	last_iters_ = std::min(it, opt_.refine_max_iter);
+	pred_iters_ = it;
+	last_iters_ = it;
 	last_resid_ = worst;
 	LFG_CUDA(cudaMemcpyAsync(x, ref_x_, sizeof(double)*tot, cudaMemcpyDeviceToDevice, st_));
 	if (st) { st->refine_iters = last_iters_; st->refine_residual = worst; }

@@ -71,6 +71,7 @@ private:
 	std::vector<double> pat_pos_;
 	double pat_box_[3] = {0, 0, 0};
 	int last_iters_ = 0;
+	int pred_iters_ = 2;   // refinement iterations launched together (the last solve's count)
 	double last_resid_ = 0;
 	int launches_factor_ = 0, launches_solve_ = 0;
 	int64_t kernels_ = 0;
