@@ -403,7 +403,8 @@ def main():
         ms, kern = g.step_times()
         t = g.timing()
         print(json.dumps({"profile_steps_ms": [float(x) for x in ms], "kernels_in_timed_steps": kern,
-                          "factor_flops": t["factor_flops"], "solve_bytes": t["solve_bytes"]}))
+                          "stage_ms": t["ms"], "factor_flops": t["factor_flops"],
+                          "solve_bytes": t["solve_bytes"]}))
         return
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

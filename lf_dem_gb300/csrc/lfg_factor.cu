@@ -75,6 +75,35 @@ __device__ inline void od18_to_dense(const double *o, double *m)
 // ---------------------------------------------------------------------------
 // assembly: one CTA per (supernode, scalar column)
 // ---------------------------------------------------------------------------
+// Programmatic dependent launch.  The factor and solve kernels are launched
+// with programmatic stream serialisation (launch_pdl) and call pdl_wait --
+// which returns once the previous launch has finished and its writes are
+// visible -- before their first access to data an earlier launch writes;
+// task lists and indices (written by the symbolic upload, before any of these
+// launches) may be read before it.  The solve phases also call pdl_trigger
+// first, so the next phase is scheduled as soon as all their CTAs run; the
+// factor kernels do not (their successors would sit resident next to the
+// diagonal-block CTA on the critical path: measured slower), so theirs start
+// when they finish, overlapping only the final flush.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args)
+{
+	cudaLaunchConfig_t cfg = {};
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	attr[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.gridDim = grid;
+	cfg.blockDim = block;
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = st;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	LFG_CUDA(cudaLaunchKernelEx(&cfg, kern, args...));
+}
+
 template <typename T>
 __global__ void k_assemble(const int *__restrict__ col_tasks, const int *__restrict__ sn_n,
                            const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
@@ -87,6 +116,7 @@ __global__ void k_assemble(const int *__restrict__ col_tasks, const int *__restr
 	T *col = arena+sn_off[s]+(int64_t)c*ld;
 	int cb = c/6, cr = c%6;
 	int ca = child_off[s], cz = child_off[s+1];
+	pdl_wait();
 	for (int r = c+threadIdx.x; r < F6; r += blockDim.x) {
 		int rb = r/6, rr = r%6;
 		T v = 0;
@@ -114,10 +144,11 @@ __global__ void k_scatter_d(int count, const int *__restrict__ list, const doubl
 	int t = blockIdx.x*blockDim.x+threadIdx.x;
 	if (t >= count) return;
 	int i = list[t];
-	double m[36];
-	d15_to_dense(dblocks+15*(int64_t)i, m);
 	int s = d_sn[i], b = d_bc[i], ld = sn_ld[s];
 	T *base = arena+sn_off[s];
+	pdl_wait();
+	double m[36];
+	d15_to_dense(dblocks+15*(int64_t)i, m);
 	for (int c = 0; c < 6; c++)
 		for (int r = c; r < 6; r++)
 			base[(int64_t)(6*b+c)*ld+6*b+r] += (T)m[r*6+c];
@@ -133,11 +164,12 @@ __global__ void k_scatter_od(int count, const int *__restrict__ list, const doub
 	int t = blockIdx.x*blockDim.x+threadIdx.x;
 	if (t >= count) return;
 	int e = list[t];
-	double m[36];
-	od18_to_dense(odblocks+18*(int64_t)e, m);
 	int s = od_sn[e], br = od_br[e], bc = od_bc[e], ld = sn_ld[s];
 	T *base = arena+sn_off[s];
 	bool tr = od_tr[e];
+	pdl_wait();
+	double m[36];
+	od18_to_dense(odblocks+18*(int64_t)e, m);
 	for (int c = 0; c < 6; c++)
 		for (int r = 0; r < 6; r++)
 			base[(int64_t)(6*bc+c)*ld+6*br+r] += (T)(tr ? m[c*6+r] : m[r*6+c]);
@@ -326,6 +358,7 @@ __global__ void __launch_bounds__(128) k_diag(const int4 *__restrict__ tasks, co
 	__shared__ T Ts[32*33];
 	int4 tk = tasks[blockIdx.x];
 	int s = tk.x, p0 = tk.y, k = tk.z, w = tk.w;
+	pdl_wait();
 	diag_block<T>(arena+sn_off[s], sn_ld[s], p0, w, 6*sn_first[s]+p0, fail, Ls, Vs, Ts,
 	              linv_slot<T>(linv, nsn, s, k));
 }
@@ -373,6 +406,7 @@ __global__ void __launch_bounds__(256) k_trsm(const int4 *__restrict__ tasks, co
 	int w = min(NB, 6*sn_n[s]-p0);   // panel width: columns p0 + w and later are not touched
 	T *base = arena+sn_off[s];
 	const T *vt = linv_slot<T>(linv, nsn, s, k);
+	pdl_wait();
 	for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) Vt[e] = vt[e];
 	for (int e = threadIdx.x; e < PANEL_ROWS*NB; e += blockDim.x) {
 		int r = e%PANEL_ROWS, t = e/PANEL_ROWS;   // coalesced over rows
@@ -432,6 +466,7 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 	bool extra = r0 >= F6;
 	int rlim = extra ? F6+t0 : F6;
 	int clim = n6;   // own columns only; the update matrix is k_syrk's
+	pdl_wait();
 	// load panel rows of the tile rows and tile columns
 	for (int e = threadIdx.x; e < NB*TL; e += blockDim.x) {
 		int t = e/TL, i = e%TL;
@@ -499,6 +534,7 @@ __global__ void __launch_bounds__(256) k_syrk(const int4 *__restrict__ tasks, co
 	int s = tk.x, r0 = tk.y, c0 = tk.z;
 	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
 	T *base = arena+sn_off[s];
+	pdl_wait();
 	int tx = threadIdx.x%TD, ty = threadIdx.x/TD;
 	T acc[TPT][TPT];
 #pragma unroll
@@ -752,6 +788,7 @@ __global__ void __launch_bounds__(umma::THREADS, 1) k_syrk_tc(const int4 *__rest
 	int4 tk = tasks[blockIdx.x];
 	int s = tk.x, r0 = tk.y, c0 = tk.z;
 	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
+	pdl_wait();   // before the tensor-memory allocation, too
 	uint32_t tmem = tc_setup(&tmem_slot, mbar);
 	bool ok = tc_tile_update(arena+sn_off[s], ld, r0, c0, 0, n6, F6, F6, true, sm, mbar, tmem);
 	tc_teardown(tmem);
@@ -848,38 +885,43 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 		if (L.count <= 0) continue;
 		switch (L.kind) {
 		case PLAN_ASSEMBLE:
-			k_assemble<T><<<L.count, 256, 0, st>>>(D.col_tasks+2*L.off, D.sn_n, D.sn_m, D.sn_ld, D.sn_off,
-			                                       D.child_off, D.children, D.cinv_off, D.cinv, F.arena);
+			launch_pdl(k_assemble<T>, L.count, 256, 0, st, (const int *)D.col_tasks+2*L.off, (const int *)D.sn_n,
+			           (const int *)D.sn_m, (const int *)D.sn_ld, (const int64_t *)D.sn_off,
+			           (const int *)D.child_off, (const int *)D.children, (const int64_t *)D.cinv_off,
+			           (const int *)D.cinv, F.arena);
 			break;
 		case PLAN_SCATTER_D:
-			k_scatter_d<T><<<(L.count+127)/128, 128, 0, st>>>(L.count, D.level_d+L.off, dbl, D.d_sn, D.d_bc,
-			                                                    D.sn_ld, D.sn_off, F.arena);
+			launch_pdl(k_scatter_d<T>, (L.count+127)/128, 128, 0, st, L.count, (const int *)D.level_d+L.off, dbl,
+			           (const int *)D.d_sn, (const int *)D.d_bc, (const int *)D.sn_ld, (const int64_t *)D.sn_off,
+			           F.arena);
 			break;
 		case PLAN_SCATTER_OD:
-			k_scatter_od<T><<<(L.count+127)/128, 128, 0, st>>>(L.count, D.level_od+L.off, odbl, D.od_sn,
-			                                                     D.od_br, D.od_bc, D.od_tr, D.sn_ld, D.sn_off,
-			                                                     F.arena);
+			launch_pdl(k_scatter_od<T>, (L.count+127)/128, 128, 0, st, L.count, (const int *)D.level_od+L.off, odbl,
+			           (const int *)D.od_sn, (const int *)D.od_br, (const int *)D.od_bc, (const int *)D.od_tr,
+			           (const int *)D.sn_ld, (const int64_t *)D.sn_off, F.arena);
 			break;
 		case PLAN_DIAG:
-			k_diag<T><<<L.count, 128, 0, st>>>(D.diag_tasks+L.off, D.sn_first, D.sn_ld, D.sn_off, F.arena, F.linv,
-			                                   D.nsn, F.status);
+			launch_pdl(k_diag<T>, L.count, 128, 0, st, (const int4 *)D.diag_tasks+L.off, (const int *)D.sn_first,
+			           (const int *)D.sn_ld, (const int64_t *)D.sn_off, F.arena, F.linv, D.nsn, F.status);
 			break;
 		case PLAN_PANEL:
-			k_trsm<T><<<L.count, 256, 0, st>>>(D.panel_tasks+L.off, D.sn_n, D.sn_ld, D.sn_off, F.arena, F.linv,
-			                                   D.nsn);
+			launch_pdl(k_trsm<T>, L.count, 256, 0, st, (const int4 *)D.panel_tasks+L.off, (const int *)D.sn_n,
+			           (const int *)D.sn_ld, (const int64_t *)D.sn_off, F.arena, F.linv, D.nsn);
 			break;
 		case PLAN_UPDATE:
-			k_update<T><<<L.count, 256, update_smem<T>(), st>>>(D.tile_tasks+L.off, D.sn_first, D.sn_n, D.sn_m,
-			                                                    D.sn_ld, D.sn_off, F.arena, F.linv, D.nsn, F.status);
+			launch_pdl(k_update<T>, L.count, 256, update_smem<T>(), st, (const int4 *)D.tile_tasks+L.off,
+			           (const int *)D.sn_first, (const int *)D.sn_n, (const int *)D.sn_m, (const int *)D.sn_ld,
+			           (const int64_t *)D.sn_off, F.arena, F.linv, D.nsn, F.status);
 			break;
 		case PLAN_SYRK:
-			k_syrk<T><<<L.count, 256, 0, st>>>(D.tile_tasks+L.off, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, F.arena);
+			launch_pdl(k_syrk<T>, L.count, 256, 0, st, (const int4 *)D.tile_tasks+L.off, (const int *)D.sn_n,
+			           (const int *)D.sn_m, (const int *)D.sn_ld, (const int64_t *)D.sn_off, F.arena);
 			break;
 		case PLAN_SYRK_TC:
 			if (!std::is_same<T, float>::value) throw Error{LFG_ERR_BAD_ARG, 0, "tensor-core plan for FP64"};
-			k_syrk_tc<<<L.count, umma::THREADS, umma::SMEM_BYTES, st>>>(D.tile_tasks+L.off, D.sn_n, D.sn_m, D.sn_ld,
-			                                                           D.sn_off, reinterpret_cast<float *>(F.arena),
-			                                                           F.status);
+			launch_pdl(k_syrk_tc, L.count, umma::THREADS, umma::SMEM_BYTES, st, (const int4 *)D.tile_tasks+L.off,
+			           (const int *)D.sn_n, (const int *)D.sn_m, (const int *)D.sn_ld, (const int64_t *)D.sn_off,
+			           reinterpret_cast<float *>(F.arena), F.status);
 			break;
 		}
 		launches++;
@@ -891,102 +933,90 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 // ---------------------------------------------------------------------------
 // solves (k <= 4 right-hand sides, RHS-major: v[r*6n + i])
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void k_permute_in(int n, int k, const int *__restrict__ iperm, const double *__restrict__ b,
-                             T *__restrict__ xp)
-{
-	int t = blockIdx.x*blockDim.x+threadIdx.x;
-	if (t >= 6*n) return;
-	int i = t/6, d = t%6;
-	int q = 6*iperm[i]+d;
-	for (int r = 0; r < k; r++) xp[(int64_t)r*6*n+q] = (T)b[(int64_t)r*6*n+t];
-}
+// Solve: forward (leaves first) and backward (root first) sweeps over the
+// levels of the assembly tree, for K <= 4 right-hand sides (RHS-major:
+// v[r*6n + i], permuted order).  Per level, forward:
+//   gather  : v_top (own columns, in xp) += children's update vectors;
+//             w_s (update rows) = children's update vectors
+//   cols 0  : y = E^T v_top            (E = L11^-T, upper triangular)
+//   rows 0  : w_s -= L21 y              (+ ordered sum of column chunks)
+// backward:
+//   cols 1  : z = y - L21^T x[rows of s]
+//   rows 1  : x = E z                   (+ ordered sum of column chunks)
+// A phase table built with the symbolic analysis lists the phases of a
+// sweep; each runs as one launch of k_solve_phase with one CTA per work
+// unit.  Column products take SOLVE_CB columns per unit (8 warps split the
+// rows), row products 32 rows x SOLVE_JC columns (lanes own rows, warps
+// split the columns).  Every sum runs in a fixed order: results are bitwise
+// reproducible.  (One persistent kernel with grid barriers between phases
+// was measured slower: the barriers cost more than the launch gaps.)
 
-template <typename T>
-__global__ void k_permute_out(int n, int k, const int *__restrict__ iperm, const T *__restrict__ xp,
-                              double *__restrict__ x)
-{
-	int t = blockIdx.x*blockDim.x+threadIdx.x;
-	if (t >= 6*n) return;
-	int i = t/6, d = t%6;
-	int q = 6*iperm[i]+d;
-	for (int r = 0; r < k; r++) x[(int64_t)r*6*n+t] = (double)xp[(int64_t)r*6*n+q];
-}
+// Solve phases read their indices and factor entries (constant during a
+// solve) before pdl_wait; every other access follows it.
 
-// Solve kernels.  Per level of the assembly tree, forward (leaves first):
-//   k_fwd_gather : v_top (own columns, in xp) += children's update vectors;
-//                  w_s (update rows) = children's update vectors
-//   k_fwd_y      : y = E^T v_top           (E = L11^-T, upper triangular)
-//   k_fwd_w      : w_s -= L21 y
-// backward (root first):
-//   k_bwd_z      : z = y - L21^T x[rows of s]
-//   k_bwd_x      : x = E z
-// Each CTA produces 32 outputs; for the row-oriented products (k_fwd_w,
-// k_bwd_x) its 8 warps split the column range and lanes own rows, so every
-// factor load is a coalesced 128-byte line; the column-oriented products
-// (k_fwd_y, k_bwd_z) use one warp per output column.  Sums over children and
-// warps run in a fixed order: results are bitwise reproducible.
+template <typename T> struct SolveArgs {
+	const int *lev_sn, *sn_first, *sn_n, *sn_m, *sn_ld, *sn_rows_off, *rows;
+	const int64_t *sn_off, *sn_woff, *cinv_off;
+	const int *child_off, *children, *cinv, *iperm;
+	const T *arena;
+	T *w, *xp, *yp, *part;
+	int64_t wstride, pstride;
+	int n, n6tot;
+	const double *b;
+	double *x;
+};
+
+template <typename T> struct SolveShared {
+	T red_c[SOLVE_WARPS][SOLVE_CB][4];
+	T red_r[SOLVE_WARPS][4][32];
+};
 
 template <typename T, int K>
-__global__ void __launch_bounds__(256) k_fwd_gather(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
-                             const int *__restrict__ sn_n, const int *__restrict__ sn_m,
-                             const int *__restrict__ child_off, const int *__restrict__ children,
-                             const int64_t *__restrict__ cinv_off, const int *__restrict__ cinv,
-                             const int64_t *__restrict__ sn_woff, T *__restrict__ w, int64_t wstride,
-                             T *__restrict__ xp, int n6tot)
+__device__ void unit_gather(const SolveArgs<T> &A, const int *lev, int bx, int by)
 {
-	int s = lev_sn[blockIdx.y];
-	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s];
-	int r = blockIdx.x*blockDim.x+threadIdx.x;
+	int s = lev[by];
+	int n6 = 6*A.sn_n[s], F6 = n6+6*A.sn_m[s];
+	int r = bx*blockDim.x+threadIdx.x;
 	if (r >= F6) return;
-	int ca = child_off[s], cz = child_off[s+1];
+	int ca = A.child_off[s], cz = A.child_off[s+1];
 	T acc[K];
 #pragma unroll
 	for (int q = 0; q < K; q++) acc[q] = 0;
 	int rb = r/6, rr = r%6;
+	pdl_wait();
 	for (int c = ca; c < cz; c++) {
-		int ch = children[c];
-		int ic = cinv[cinv_off[ch]+rb];
+		int ch = A.children[c];
+		int ic = A.cinv[A.cinv_off[ch]+rb];
 		if (ic < 0) continue;
-		int64_t src = sn_woff[ch]+6*(ic-sn_n[ch])+rr;
+		int64_t src = A.sn_woff[ch]+6*(ic-A.sn_n[ch])+rr;
 #pragma unroll
-		for (int q = 0; q < K; q++) acc[q] += w[q*wstride+src];
+		for (int q = 0; q < K; q++) acc[q] += A.w[q*A.wstride+src];
 	}
 	if (r < n6) {
-		int g = 6*sn_first[s]+r;
+		int g = 6*A.sn_first[s]+r;
 #pragma unroll
-		for (int q = 0; q < K; q++) xp[(int64_t)q*n6tot+g] += acc[q];
+		for (int q = 0; q < K; q++) A.xp[(int64_t)q*A.n6tot+g] += acc[q];
 	} else {
-		int64_t d = sn_woff[s]+(r-n6);
+		int64_t d = A.sn_woff[s]+(r-n6);
 #pragma unroll
-		for (int q = 0; q < K; q++) w[q*wstride+d] = acc[q];
+		for (int q = 0; q < K; q++) A.w[q*A.wstride+d] = acc[q];
 	}
 }
 
-// Column products: one supernode per blockIdx.y, SOLVE_CB columns per
-// blockIdx.x; the 8 warps split the rows (each thread reads its row's
-// right-hand-side values once for all the CTA's columns) and the partial sums
-// meet in shared memory in a fixed order.
-//  MODE 0 (forward):  y_j  = sum_{i <= j} E[i][j] x_i      (E = L11^-T)
-//  MODE 1 (backward): z_j -= sum_t L21[t][j] x[rows(t)]    (z in yp)
+// MODE 0: y_j = sum_{i <= j} E[i][j] x_i;  MODE 1: z_j -= sum_t L21[t][j] x[rows(t)]
 template <typename T, int K, int MODE>
-__global__ void __launch_bounds__(256) k_solve_cols(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
-                                                    const int *__restrict__ sn_n, const int *__restrict__ sn_m,
-                                                    const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
-                                                    const int *__restrict__ sn_rows_off,
-                                                    const int *__restrict__ rows, const T *__restrict__ arena,
-                                                    const T *__restrict__ xp, T *__restrict__ yp, int n6tot)
+__device__ void unit_cols(const SolveArgs<T> &A, const int *lev, int bx, int by, SolveShared<T> &sh)
 {
-	__shared__ T red[SOLVE_WARPS][SOLVE_CB][K];
-	int s = lev_sn[blockIdx.y];
-	int n6 = 6*sn_n[s], m6 = 6*sn_m[s], ld = sn_ld[s];
-	int j0 = blockIdx.x*SOLVE_CB;
+	int s = lev[by];
+	int n6 = 6*A.sn_n[s], m6 = 6*A.sn_m[s], ld = A.sn_ld[s];
+	int j0 = bx*SOLVE_CB;
 	if (j0 >= n6 || (MODE == 1 && m6 == 0)) return;
 	int jn = min(SOLVE_CB, n6-j0);
-	int f6 = 6*sn_first[s];
-	const T *M = arena+sn_off[s]+(MODE == 0 ? n6+m6 : n6)+(int64_t)j0*ld;
-	const int *R = rows+sn_rows_off[s];
+	int f6 = 6*A.sn_first[s];
+	const T *M = A.arena+A.sn_off[s]+(MODE == 0 ? n6+m6 : n6)+(int64_t)j0*ld;
+	const int *R = A.rows+A.sn_rows_off[s];
 	int nrow = MODE == 0 ? j0+jn : m6;
+	pdl_wait();
 	T acc[SOLVE_CB][K];
 #pragma unroll
 	for (int c = 0; c < SOLVE_CB; c++)
@@ -996,11 +1026,11 @@ __global__ void __launch_bounds__(256) k_solve_cols(const int *__restrict__ lev_
 		int64_t g = MODE == 0 ? f6+i : 6*R[i/6]+i%6;
 		T v[K];
 #pragma unroll
-		for (int q = 0; q < K; q++) v[q] = xp[(int64_t)q*n6tot+g];
+		for (int q = 0; q < K; q++) v[q] = A.xp[(int64_t)q*A.n6tot+g];
 #pragma unroll
 		for (int c = 0; c < SOLVE_CB; c++) {
 			if (c >= jn || (MODE == 0 && i > j0+c)) continue;
-			T e = M[(int64_t)c*ld+i];
+			T e = __ldg(&M[(int64_t)c*ld+i]);
 #pragma unroll
 			for (int q = 0; q < K; q++) acc[c][q] += e*v[q];
 		}
@@ -1012,160 +1042,187 @@ __global__ void __launch_bounds__(256) k_solve_cols(const int *__restrict__ lev_
 		for (int q = 0; q < K; q++) {
 			T a = acc[c][q];
 			for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-			if (lane == 0) red[warp][c][q] = a;
+			if (lane == 0) sh.red_c[warp][c][q] = a;
 		}
 	__syncthreads();
 	if (threadIdx.x < SOLVE_CB*K) {
 		int c = threadIdx.x/K, q = threadIdx.x%K;
 		if (c < jn) {
 			T a = 0;
-			for (int u = 0; u < SOLVE_WARPS; u++) a += red[u][c][q];
-			T *o = yp+(int64_t)q*n6tot+f6+j0+c;
+			for (int u = 0; u < SOLVE_WARPS; u++) a += sh.red_c[u][c][q];
+			T *o = A.yp+(int64_t)q*A.n6tot+f6+j0+c;
 			if (MODE == 0) *o = a;
 			else *o -= a;
 		}
 	}
 }
 
-// Row products: 32 rows per blockIdx.x (lanes), SOLVE_JC columns per
-// blockIdx.z (the 8 warps split them).  With one chunk the result is applied
-// directly; otherwise every chunk writes its partial sums (zeros for an empty
-// chunk) and k_solve_rowsum adds them in chunk order.
-//  MODE 0 (forward):  w_t -= sum_j L21[t][j] y_j        (t < 6m; w at sn_woff)
-//  MODE 1 (backward): x_i  = sum_{j >= i} E[i][j] z_j    (i < 6n; z in yp)
+// MODE 0: w_t -= sum_j L21[t][j] y_j;  MODE 1: x_i = sum_{j >= i} E[i][j] z_j
 template <typename T, int K, int MODE>
-__global__ void __launch_bounds__(256) k_solve_rows(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
-                                                    const int *__restrict__ sn_n, const int *__restrict__ sn_m,
-                                                    const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
-                                                    const int64_t *__restrict__ sn_woff, const T *__restrict__ arena,
-                                                    T *__restrict__ w, int64_t wstride, const T *__restrict__ yp,
-                                                    T *__restrict__ xp, int n6tot, T *__restrict__ part,
-                                                    int64_t pstride, int nchunk)
+__device__ void unit_rows(const SolveArgs<T> &A, const int *lev, int bx, int by, int bz, int nchunk,
+                          SolveShared<T> &sh)
 {
-	__shared__ T red[SOLVE_WARPS][K][32];
-	int s = lev_sn[blockIdx.y];
-	int n6 = 6*sn_n[s], m6 = 6*sn_m[s], ld = sn_ld[s];
+	int s = lev[by];
+	int n6 = 6*A.sn_n[s], m6 = 6*A.sn_m[s], ld = A.sn_ld[s];
 	int nrows = MODE == 0 ? m6 : n6;
-	int r0 = blockIdx.x*32;
+	int r0 = bx*32;
 	if (r0 >= nrows) return;
 	int warp = threadIdx.x/32, lane = threadIdx.x%32;
-	int f6 = 6*sn_first[s];
-	int jlo = (MODE == 0 ? 0 : r0)+blockIdx.z*SOLVE_JC;
+	int f6 = 6*A.sn_first[s];
+	int jlo = (MODE == 0 ? 0 : r0)+bz*SOLVE_JC;
 	int jhi = min(n6, jlo+SOLVE_JC);
-	const T *M = arena+sn_off[s]+(MODE == 0 ? n6 : n6+m6);
+	const T *M = A.arena+A.sn_off[s]+(MODE == 0 ? n6 : n6+m6);
 	int r = r0+lane;
+	pdl_wait();
 	T acc[K];
 #pragma unroll
 	for (int q = 0; q < K; q++) acc[q] = 0;
 	if (r < nrows) {
 		for (int j = jlo+warp; j < jhi; j += SOLVE_WARPS) {
 			if (MODE == 1 && j < r) continue;
-			T e = M[(int64_t)j*ld+r];
+			T e = __ldg(&M[(int64_t)j*ld+r]);
 #pragma unroll
-			for (int q = 0; q < K; q++) acc[q] += e*yp[(int64_t)q*n6tot+f6+j];
+			for (int q = 0; q < K; q++) acc[q] += e*A.yp[(int64_t)q*A.n6tot+f6+j];
 		}
 	}
 #pragma unroll
-	for (int q = 0; q < K; q++) red[warp][q][lane] = acc[q];
+	for (int q = 0; q < K; q++) sh.red_r[warp][q][lane] = acc[q];
 	__syncthreads();
 	if (warp == 0 && r < nrows) {
-		int64_t row = MODE == 0 ? sn_woff[s]+r : (int64_t)f6+r;
+		int64_t row = MODE == 0 ? A.sn_woff[s]+r : (int64_t)f6+r;
 #pragma unroll
 		for (int q = 0; q < K; q++) {
 			T a = 0;
-			for (int u = 0; u < SOLVE_WARPS; u++) a += red[u][q][lane];
+			for (int u = 0; u < SOLVE_WARPS; u++) a += sh.red_r[u][q][lane];
 			if (nchunk == 1) {
-				if (MODE == 0) w[q*wstride+row] -= a;
-				else xp[(int64_t)q*n6tot+row] = a;
+				if (MODE == 0) A.w[q*A.wstride+row] -= a;
+				else A.xp[(int64_t)q*A.n6tot+row] = a;
 			} else {
-				part[((int64_t)q*nchunk+blockIdx.z)*pstride+row] = a;
+				A.part[((int64_t)q*nchunk+bz)*A.pstride+row] = a;
 			}
 		}
 	}
 }
 
 template <typename T, int K, int MODE>
-__global__ void k_solve_rowsum(const int *__restrict__ lev_sn, const int *__restrict__ sn_first,
-                               const int *__restrict__ sn_n, const int *__restrict__ sn_m,
-                               const int64_t *__restrict__ sn_woff, T *__restrict__ w, int64_t wstride,
-                               T *__restrict__ xp, int n6tot, const T *__restrict__ part, int64_t pstride, int nchunk)
+__device__ void unit_rowsum(const SolveArgs<T> &A, const int *lev, int bx, int by, int nchunk)
 {
-	int s = lev_sn[blockIdx.y];
-	int nrows = MODE == 0 ? 6*sn_m[s] : 6*sn_n[s];
-	int r = blockIdx.x*blockDim.x+threadIdx.x;
+	int s = lev[by];
+	int nrows = MODE == 0 ? 6*A.sn_m[s] : 6*A.sn_n[s];
+	int r = bx*blockDim.x+threadIdx.x;
 	if (r >= nrows) return;
-	int64_t row = MODE == 0 ? sn_woff[s]+r : 6*(int64_t)sn_first[s]+r;
+	int64_t row = MODE == 0 ? A.sn_woff[s]+r : 6*(int64_t)A.sn_first[s]+r;
+	pdl_wait();
 #pragma unroll
 	for (int q = 0; q < K; q++) {
 		T a = 0;
-		for (int c = 0; c < nchunk; c++) a += part[((int64_t)q*nchunk+c)*pstride+row];
-		if (MODE == 0) w[q*wstride+row] -= a;
-		else xp[(int64_t)q*n6tot+row] = a;
+		for (int c = 0; c < nchunk; c++) a += A.part[((int64_t)q*nchunk+c)*A.pstride+row];
+		if (MODE == 0) A.w[q*A.wstride+row] -= a;
+		else A.xp[(int64_t)q*A.n6tot+row] = a;
 	}
+}
+
+template <typename T, int K>
+__device__ void unit_permute(const SolveArgs<T> &A, int bx, bool in)
+{
+	int t = bx*blockDim.x+threadIdx.x;
+	if (t >= 6*A.n) return;
+	int i = t/6, d = t%6;
+	int q = 6*A.iperm[i]+d;
+	pdl_wait();
+	if (in)
+		for (int r = 0; r < K; r++) A.xp[(int64_t)r*6*A.n+q] = (T)A.b[(int64_t)r*6*A.n+t];
+	else
+		for (int r = 0; r < K; r++) A.x[(int64_t)r*6*A.n+t] = (double)A.xp[(int64_t)r*6*A.n+q];
+}
+
+// one phase as its own launch: one CTA per work unit; one instantiation per
+// phase type, so each gets its own register budget
+template <typename T, int K, int TYPE>
+__global__ void __launch_bounds__(256) k_solve_phase(SolveArgs<T> A, SolvePhase ph)
+{
+	__shared__ SolveShared<T> sh;
+	pdl_trigger();
+	const int *lev = A.lev_sn+ph.lev_off;
+	int bx = blockIdx.x, by = blockIdx.y, bz = blockIdx.z;
+	if (TYPE == SP_PERM_IN) unit_permute<T, K>(A, bx, true);
+	if (TYPE == SP_GATHER) unit_gather<T, K>(A, lev, bx, by);
+	if (TYPE == SP_COLS0) unit_cols<T, K, 0>(A, lev, bx, by, sh);
+	if (TYPE == SP_ROWS0) unit_rows<T, K, 0>(A, lev, bx, by, bz, ph.nchunk, sh);
+	if (TYPE == SP_ROWSUM0) unit_rowsum<T, K, 0>(A, lev, bx, by, ph.nchunk);
+	if (TYPE == SP_COLS1) unit_cols<T, K, 1>(A, lev, bx, by, sh);
+	if (TYPE == SP_ROWS1) unit_rows<T, K, 1>(A, lev, bx, by, bz, ph.nchunk, sh);
+	if (TYPE == SP_ROWSUM1) unit_rowsum<T, K, 1>(A, lev, bx, by, ph.nchunk);
+	if (TYPE == SP_PERM_OUT) unit_permute<T, K>(A, bx, false);
+}
+
+template <typename T, int K>
+static void launch_phase(const SolveArgs<T> &A, const SolvePhase &p, cudaStream_t st)
+{
+	dim3 g(p.gx, p.gy, p.gz);
+	switch (p.type) {
+	case SP_PERM_IN: launch_pdl(k_solve_phase<T, K, SP_PERM_IN>, g, 256, 0, st, A, p); break;
+	case SP_GATHER: launch_pdl(k_solve_phase<T, K, SP_GATHER>, g, 256, 0, st, A, p); break;
+	case SP_COLS0: launch_pdl(k_solve_phase<T, K, SP_COLS0>, g, 256, 0, st, A, p); break;
+	case SP_ROWS0: launch_pdl(k_solve_phase<T, K, SP_ROWS0>, g, 256, 0, st, A, p); break;
+	case SP_ROWSUM0: launch_pdl(k_solve_phase<T, K, SP_ROWSUM0>, g, 256, 0, st, A, p); break;
+	case SP_COLS1: launch_pdl(k_solve_phase<T, K, SP_COLS1>, g, 256, 0, st, A, p); break;
+	case SP_ROWS1: launch_pdl(k_solve_phase<T, K, SP_ROWS1>, g, 256, 0, st, A, p); break;
+	case SP_ROWSUM1: launch_pdl(k_solve_phase<T, K, SP_ROWSUM1>, g, 256, 0, st, A, p); break;
+	default: launch_pdl(k_solve_phase<T, K, SP_PERM_OUT>, g, 256, 0, st, A, p); break;
+	}
+}
+
+// Phase table of one sweep (forward levels leaves first, backward levels
+// root first); the grid extents are those of the former per-phase launches.
+void solve_plan_build(DevSymbolic &D, cudaStream_t st)
+{
+	std::vector<SolvePhase> P;
+	auto add = [&](int type, int lev_off, int gx, int gy, int gz, int nchunk) {
+		P.push_back(SolvePhase{type, lev_off, gx, gy, gz, nchunk});
+	};
+	int n = D.nblk;
+	add(SP_PERM_IN, 0, (6*n+255)/256, 1, 1, 1);
+	for (int l = 0; l < D.nlevels; l++) {
+		int off = D.h_level_off[l], cnt = D.h_level_off[l+1]-off;
+		if (!cnt) continue;
+		int n6 = D.h_level_maxn6[l], m6 = D.h_level_maxm6[l];
+		add(SP_GATHER, off, (n6+m6+255)/256, cnt, 1, 1);
+		add(SP_COLS0, off, (n6+SOLVE_CB-1)/SOLVE_CB, cnt, 1, 1);
+		if (m6 > 0) {
+			int nch = (n6+SOLVE_JC-1)/SOLVE_JC;
+			add(SP_ROWS0, off, (m6+31)/32, cnt, nch, nch);
+			if (nch > 1) add(SP_ROWSUM0, off, (m6+255)/256, cnt, 1, nch);
+		}
+	}
+	for (int l = D.nlevels-1; l >= 0; l--) {
+		int off = D.h_level_off[l], cnt = D.h_level_off[l+1]-off;
+		if (!cnt) continue;
+		int n6 = D.h_level_maxn6[l], m6 = D.h_level_maxm6[l];
+		if (m6 > 0) add(SP_COLS1, off, (n6+SOLVE_CB-1)/SOLVE_CB, cnt, 1, 1);
+		int nch = (n6+SOLVE_JC-1)/SOLVE_JC;
+		add(SP_ROWS1, off, (n6+31)/32, cnt, nch, nch);
+		if (nch > 1) add(SP_ROWSUM1, off, (n6+255)/256, cnt, 1, nch);
+	}
+	add(SP_PERM_OUT, 0, (6*n+255)/256, 1, 1, 1);
+	D.h_solve_phases = P;
+	LFG_CUDA(cudaMalloc((void **)&D.solve_phases, sizeof(SolvePhase)*P.size()));
+	LFG_CUDA(cudaMemcpyAsync(D.solve_phases, P.data(), sizeof(SolvePhase)*P.size(), cudaMemcpyHostToDevice, st));
+	LFG_CUDA(cudaStreamSynchronize(st));
 }
 
 template <typename T, int K>
 static int solve_k(DevFactor<T> &F, const DevSymbolic &D, const double *b, double *x, cudaStream_t st)
 {
-	int n = D.nblk, n6tot = 6*n;
-	int launches = 0;
-	int64_t wstride = D.w_elems;
-	k_permute_in<T><<<(6*n+255)/256, 256, 0, st>>>(n, K, D.iperm, b, F.xp);
-	launches++;
-	for (int l = 0; l < D.nlevels; l++) {
-		int cnt = D.h_level_off[l+1]-D.h_level_off[l];
-		if (!cnt) continue;
-		const int *lev = D.level_sn+D.h_level_off[l];
-		int n6 = D.h_level_maxn6[l], m6 = D.h_level_maxm6[l];
-		dim3 g0((n6+m6+255)/256, cnt);
-		k_fwd_gather<T, K><<<g0, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.child_off, D.children, D.cinv_off,
-		                                        D.cinv, D.sn_woff, F.w, wstride, F.xp, n6tot);
-		dim3 g1((n6+SOLVE_CB-1)/SOLVE_CB, cnt);
-		k_solve_cols<T, K, 0><<<g1, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, D.sn_rows_off,
-		                                          D.rows, F.arena, F.xp, F.yp, n6tot);
-		launches += 2;
-		if (m6 > 0) {
-			int nch = (n6+SOLVE_JC-1)/SOLVE_JC;
-			dim3 g2((m6+31)/32, cnt, nch);
-			k_solve_rows<T, K, 0><<<g2, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, D.sn_woff,
-			                                          F.arena, F.w, wstride, F.yp, F.xp, n6tot, F.part, F.pstride,
-			                                          nch);
-			launches++;
-			if (nch > 1) {
-				dim3 g3((m6+255)/256, cnt);
-				k_solve_rowsum<T, K, 0><<<g3, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_woff, F.w, wstride,
-				                                            F.xp, n6tot, F.part, F.pstride, nch);
-				launches++;
-			}
-		}
-	}
-	for (int l = D.nlevels-1; l >= 0; l--) {
-		int cnt = D.h_level_off[l+1]-D.h_level_off[l];
-		if (!cnt) continue;
-		const int *lev = D.level_sn+D.h_level_off[l];
-		int n6 = D.h_level_maxn6[l], m6 = D.h_level_maxm6[l];
-		if (m6 > 0) {
-			dim3 g((n6+SOLVE_CB-1)/SOLVE_CB, cnt);
-			k_solve_cols<T, K, 1><<<g, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off,
-			                                         D.sn_rows_off, D.rows, F.arena, F.xp, F.yp, n6tot);
-			launches++;
-		}
-		int nch = (n6+SOLVE_JC-1)/SOLVE_JC;
-		dim3 g2((n6+31)/32, cnt, nch);
-		k_solve_rows<T, K, 1><<<g2, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_off, D.sn_woff,
-		                                          F.arena, F.w, wstride, F.yp, F.xp, n6tot, F.part, F.pstride, nch);
-		launches++;
-		if (nch > 1) {
-			dim3 g3((n6+255)/256, cnt);
-			k_solve_rowsum<T, K, 1><<<g3, 256, 0, st>>>(lev, D.sn_first, D.sn_n, D.sn_m, D.sn_woff, F.w, wstride, F.xp,
-			                                            n6tot, F.part, F.pstride, nch);
-			launches++;
-		}
-	}
-	k_permute_out<T><<<(6*n+255)/256, 256, 0, st>>>(n, K, D.iperm, F.xp, x);
-	launches++;
+	SolveArgs<T> A;
+	A.lev_sn = D.level_sn; A.sn_first = D.sn_first; A.sn_n = D.sn_n; A.sn_m = D.sn_m; A.sn_ld = D.sn_ld;
+	A.sn_rows_off = D.sn_rows_off; A.rows = D.rows; A.sn_off = D.sn_off; A.sn_woff = D.sn_woff;
+	A.cinv_off = D.cinv_off; A.child_off = D.child_off; A.children = D.children; A.cinv = D.cinv;
+	A.iperm = D.iperm; A.arena = F.arena; A.w = F.w; A.xp = F.xp; A.yp = F.yp; A.part = F.part;
+	A.wstride = D.w_elems; A.pstride = F.pstride; A.n = D.nblk; A.n6tot = 6*D.nblk; A.b = b; A.x = x;
+	for (const SolvePhase &p : D.h_solve_phases) launch_phase<T, K>(A, p, st);
 	LFG_CUDA(cudaGetLastError());
-	return launches;
+	return (int)D.h_solve_phases.size();
 }
 
 template <typename T>

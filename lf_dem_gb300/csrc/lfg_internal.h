@@ -78,6 +78,11 @@ void symbolic_analyze(Symbolic &S, int nblk, int nb, const int32_t *od_row,
 // ---------------------------------------------------------------------------
 // Device-side multifrontal factor (one precision per instance).
 // ---------------------------------------------------------------------------
+// One phase of a solve sweep: gx x gy x gz work units of one type over the
+// supernodes level_sn[lev_off ...] of one level (gy of them).
+enum { SP_PERM_IN, SP_GATHER, SP_COLS0, SP_ROWS0, SP_ROWSUM0, SP_COLS1, SP_ROWS1, SP_ROWSUM1, SP_PERM_OUT };
+struct SolvePhase { int type, lev_off, gx, gy, gz, nchunk; };
+
 struct DevSymbolic {
 	int nblk = 0, nsn = 0, nlevels = 0, nb = 0;
 	int *perm = nullptr, *iperm = nullptr;
@@ -96,6 +101,8 @@ struct DevSymbolic {
 	int4 *panel_tasks = nullptr;   // (sn, row0, k, nrows)
 	int4 *tile_tasks = nullptr;    // (sn, row0, col0, k)
 	int4 *diag_tasks = nullptr;    // (sn, col0, k, width) of each panel's diagonal block
+	SolvePhase *solve_phases = nullptr;   // phase table of a solve sweep
+	std::vector<SolvePhase> h_solve_phases;
 	// host-side launch plan
 	struct Launch { int kind; int level; int k; int64_t off; int count; };
 	std::vector<Launch> factor_plan;
@@ -119,6 +126,8 @@ int factor_panel_rows();
 void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb, int tile, int syrk_tile,
                          bool tensor_cores, cudaStream_t st);
 void dev_symbolic_free(DevSymbolic &D);
+// builds and uploads the phase table of the solve sweep (lfg_factor.cu)
+void solve_plan_build(DevSymbolic &D, cudaStream_t st);
 
 // Factor arenas and launchers (lfg_factor.cu).
 template <typename T> struct DevFactor {
@@ -129,7 +138,8 @@ template <typename T> struct DevFactor {
 	T *part = nullptr;    // solve: partial row sums per column chunk
 	int64_t pstride = 0;
 	int64_t arena_cap = 0, w_cap = 0, x_cap = 0, linv_cap = 0, part_cap = 0;
-	int *status = nullptr; // device: first non-positive pivot column + 1 (0 = ok)
+	int *status = nullptr; // device: first non-positive pivot column + 1; 0 = a bounded wait gave up;
+	                       // 0x7fffffff = ok
 };
 
 template <typename T> void factor_alloc(DevFactor<T> &F, const DevSymbolic &D, int kmax);

@@ -317,7 +317,6 @@ void Sim::compute_velocities(int calc_stress, int in_predictor)
 	stage_end(1);
 	stage_begin(2);
 	solver_->factorize_async();
-	phys_sticky_status(solver_->d_status(), d_err_, st_);
 	stage_end(2);
 	stage_begin(4);
 	phys_force_components(S_, st_);
@@ -327,6 +326,8 @@ void Sim::compute_velocities(int calc_stress, int in_predictor)
 	lfg_status st;
 	std::memset(&st, 0, sizeof st);
 	int rc = solver_->solve_device(divided ? NFC : 1, S_.rhs, divided ? S_.vc : S_.sol, &st, false);
+	// factor and solve status (a non-positive pivot, or a bounded wait that gave up)
+	phys_sticky_status(solver_->d_status(), d_err_, st_);
 	stage_end(3);
 	if (rc == LFG_ERR_NOT_CONVERGED) { error_code = rc; error_msg = st.msg; }
 	stage_begin(4);
@@ -416,7 +417,11 @@ void Sim::step(int calc_stress, double time_end, double strain_end)
 
 void Sim::check_error()
 {
-	if (*h_err_ != 0x7fffffff) {
+	if (*h_err_ == 0) {
+		error_code = LFG_ERR_TIMEOUT;
+		error_info = 0;
+		error_msg = "a bounded device wait in the resistance factorisation or solve gave up";
+	} else if (*h_err_ != 0x7fffffff) {
 		error_code = LFG_ERR_NOT_SPD;
 		error_info = *h_err_;
 		error_msg = "non-positive pivot in the resistance factorisation";

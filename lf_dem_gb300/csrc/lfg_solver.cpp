@@ -10,6 +10,7 @@
 #include "lfg_solver.h"
 
 namespace lfg {
+int fail(lfg_status *st, int code, int info, const char *msg);
 
 Solver::Solver(int n, const lfg_options &o, cudaStream_t st) : n_(n), opt_(o), st_(st)
 {
@@ -154,7 +155,14 @@ void Solver::run_graph(int kind, int k, const void *b, const void *x, const std:
 	e.kind = kind; e.k = k; e.b = b; e.x = x;
 	size_t nn = 0;
 	LFG_CUDA(cudaGraphGetNodes(graph, nullptr, &nn));
-	e.nodes = (int64_t)nn;
+	std::vector<cudaGraphNode_t> nodes(nn);
+	if (nn) LFG_CUDA(cudaGraphGetNodes(graph, nodes.data(), &nn));
+	e.nodes = 0;   // kernel nodes only (memsets and copies are not launches)
+	for (size_t q = 0; q < nn; q++) {
+		cudaGraphNodeType t;
+		LFG_CUDA(cudaGraphNodeGetType(nodes[q], &t));
+		if (t == cudaGraphNodeTypeKernel) e.nodes++;
+	}
 	LFG_CUDA(cudaGraphInstantiate(&e.exec, graph, 0));
 	cudaGraphDestroy(graph);
 	graphs_.push_back(e);
@@ -167,6 +175,7 @@ int Solver::check_factor(lfg_status *st)
 	int *dst = opt_.precision == LFG_PREC_FP64 ? F64_.status : F32_.status;
 	LFG_CUDA(cudaMemcpyAsync(h_status_, dst, sizeof(int), cudaMemcpyDeviceToHost, st_));
 	LFG_CUDA(cudaStreamSynchronize(st_));
+	if (*h_status_ == 0) return fail(st, LFG_ERR_TIMEOUT, 0, "a bounded device wait gave up");
 	if (*h_status_ != 0x7fffffff) {
 		int q = *h_status_-1;
 		int orig = S_.perm[q/6]*6+q%6;
@@ -268,7 +277,10 @@ int Solver::solve_host(int k, const double *rhs, double *x, lfg_status *st)
 	LFG_CUDA(cudaMemcpyAsync(hb_, rhs, sizeof(double)*tot, cudaMemcpyHostToDevice, st_));
 	int rc = solve_device(k, hb_, hx_, st, true);
 	LFG_CUDA(cudaMemcpyAsync(x, hx_, sizeof(double)*tot, cudaMemcpyDeviceToHost, st_));
+	int *dst = opt_.precision == LFG_PREC_FP64 ? F64_.status : F32_.status;
+	LFG_CUDA(cudaMemcpyAsync(h_status_+1, dst, sizeof(int), cudaMemcpyDeviceToHost, st_));
 	LFG_CUDA(cudaStreamSynchronize(st_));
+	if (h_status_[1] == 0) return fail(st, LFG_ERR_TIMEOUT, 0, "a bounded device wait gave up");
 	return rc;
 }
 
