@@ -492,16 +492,26 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 #pragma unroll
 			for (int b = 0; b < TPT; b++) acc[a][b] += av[a]*bv[b];
 	}
+	// all old values are loaded before the first store, so the loads overlap
+	// (a store between them would serialise them: the addresses may alias)
+	T old[TPT][TPT];
 #pragma unroll
 	for (int b = 0; b < TPT; b++) {
 		int c = cc0+ty+TD*b;
-		if (c >= clim) continue;
 #pragma unroll
 		for (int a = 0; a < TPT; a++) {
 			int r = r0+tx+TD*a;
-			if (r >= rlim) continue;
-			if (!extra && r < c) continue;
-			base[(int64_t)c*ld+r] -= acc[a][b];
+			bool in = c < clim && r < rlim && (extra || r >= c);
+			old[a][b] = in ? base[(int64_t)c*ld+r] : T(0);
+		}
+	}
+#pragma unroll
+	for (int b = 0; b < TPT; b++) {
+		int c = cc0+ty+TD*b;
+#pragma unroll
+		for (int a = 0; a < TPT; a++) {
+			int r = r0+tx+TD*a;
+			if (c < clim && r < rlim && (extra || r >= c)) base[(int64_t)c*ld+r] = old[a][b]-acc[a][b];
 		}
 	}
 	if (!extra && r0 == t0 && cc0 == t0) {
@@ -577,15 +587,24 @@ __global__ void __launch_bounds__(256) k_syrk(const int4 *__restrict__ tasks, co
 				for (int b = 0; b < TPT; b++) acc[a][b] += av[a]*bv[b];
 		}
 	}
+	// old values loaded before the stores (as in k_update)
+	T old[TPT][TPT];
 #pragma unroll
 	for (int b = 0; b < TPT; b++) {
 		int c = c0+ty+TD*b;
-		if (c >= F6) continue;
 #pragma unroll
 		for (int a = 0; a < TPT; a++) {
 			int r = r0+tx+TD*a;
-			if (r >= F6 || r < c) continue;
-			base[(int64_t)c*ld+r] -= acc[a][b];
+			old[a][b] = (c < F6 && r < F6 && r >= c) ? base[(int64_t)c*ld+r] : T(0);
+		}
+	}
+#pragma unroll
+	for (int b = 0; b < TPT; b++) {
+		int c = c0+ty+TD*b;
+#pragma unroll
+		for (int a = 0; a < TPT; a++) {
+			int r = r0+tx+TD*a;
+			if (c < F6 && r < F6 && r >= c) base[(int64_t)c*ld+r] = old[a][b]-acc[a][b];
 		}
 	}
 }
@@ -666,26 +685,31 @@ __device__ bool tc_tile_update(float *base, int ld, int r0, int c0, int k0, int 
 	uint32_t phase_bits = 0;   // bit q: parity expected at the next wait on stage q
 	bool ok = true;
 	int issued = 0;
-	// staging role: row m of both operands, K half h of the chunk
+	// staging role: row m of both operands, K half h of the chunk.  The global
+	// loads of chunk ch + 2 are issued right after chunk ch is staged, so two
+	// chunks of loads are in flight while the MMAs of earlier chunks run.
 	const int m = tid & (M-1), h = tid >> 7;
 	const int ra = r0+m, rb = c0+m;
 	const bool va = ra < rlim, vb = rb < clim;
-	for (int ch = 0; ch < nchunk; ch++) {
+	auto load = [&](int ch, float (&av)[16], float (&bv)[16]) {
+		int tb = k0+ch*KC+16*h;
+#pragma unroll
+		for (int k = 0; k < 16; k++) {
+			int t = tb+k;
+			av[k] = (ch < nchunk && t < k1 && va) ? base[(int64_t)t*ld+ra] : 0.f;
+			bv[k] = (ch < nchunk && t < k1 && vb) ? base[(int64_t)t*ld+rb] : 0.f;
+		}
+	};
+	// stage chunk ch (registers av, bv) into ring slot ch % STAGES and issue
+	// its MMAs; false once a wait has timed out
+	auto step = [&](int ch, float (&av)[16], float (&bv)[16]) -> bool {
 		int b = ch % STAGES;
 		if (ch >= STAGES) {
 			if (!mbar_wait(saddr(&mbar[b]), (phase_bits >> b) & 1u)) ok = false;
 			phase_bits ^= 1u << b;
 		}
-		if (!__syncthreads_and(ok)) { ok = false; break; }
+		if (!__syncthreads_and(ok)) { ok = false; return false; }
 		unsigned char *stg = sm+b*STAGE_BYTES;
-		int tb = k0+ch*KC+16*h;
-		float av[16], bv[16];
-#pragma unroll
-		for (int k = 0; k < 16; k++) {
-			int t = tb+k;
-			av[k] = (t < k1 && va) ? base[(int64_t)t*ld+ra] : 0.f;
-			bv[k] = (t < k1 && vb) ? base[(int64_t)t*ld+rb] : 0.f;
-		}
 #pragma unroll
 		for (int k = 0; k < 16; k++) {
 			int kk = 16*h+k;
@@ -695,6 +719,7 @@ __device__ bool tc_tile_update(float *base, int ld, int r0, int c0, int k0, int 
 			*reinterpret_cast<float *>(stg+2*TILE_BYTES+off) = bv[k];
 			*reinterpret_cast<float *>(stg+3*TILE_BYTES+off) = tf32_lo(bv[k]);
 		}
+		load(ch+2, av, bv);
 		asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 		__syncthreads();
 		if (tid == 0) {
@@ -712,6 +737,14 @@ __device__ bool tc_tile_update(float *base, int ld, int r0, int c0, int k0, int 
 			             :: "r"(saddr(&mbar[b])) : "memory");
 		}
 		issued = ch+1;
+		return true;
+	};
+	float a0[16], b0[16], a1[16], b1[16];
+	load(0, a0, b0);
+	load(1, a1, b1);
+	for (int ch = 0; ch < nchunk; ch += 2) {
+		if (!step(ch, a0, b0)) break;
+		if (ch+1 < nchunk && !step(ch+1, a1, b1)) break;
 	}
 	// every issued MMA is complete once the last commit has arrived
 	if (issued > 0) {
@@ -724,7 +757,15 @@ __device__ bool tc_tile_update(float *base, int ld, int r0, int c0, int k0, int 
 		// warp w reads TMEM lanes 32 (w % 4) .. +32 (rows) and columns 64 (w / 4) .. +64
 		int q = warp & 3, half = warp >> 2;
 		int r = r0+32*q+lane;
-#pragma unroll 1
+		// the thread's 64 old values, loaded before any store (the stores
+		// would otherwise serialise the loads: the addresses may alias)
+		float old[64];
+#pragma unroll
+		for (int j = 0; j < 64; j++) {
+			int c = c0+64*half+j;
+			old[j] = (r < rlim && c < clim && (!lower_only || r >= c)) ? base[(int64_t)c*ld+r] : 0.f;
+		}
+#pragma unroll
 		for (int cb = 64*half; cb < 64*half+64; cb += 16) {
 			uint32_t v[16];
 			uint32_t ta = tmem+((uint32_t)(32*q) << 16)+(uint32_t)cb;
@@ -738,7 +779,8 @@ __device__ bool tc_tile_update(float *base, int ld, int r0, int c0, int k0, int 
 #pragma unroll
 			for (int j = 0; j < 16; j++) {
 				int c = c0+cb+j;
-				if (r < rlim && c < clim && (!lower_only || r >= c)) base[(int64_t)c*ld+r] -= __uint_as_float(v[j]);
+				if (r < rlim && c < clim && (!lower_only || r >= c))
+					base[(int64_t)c*ld+r] = old[cb-64*half+j]-__uint_as_float(v[j]);
 			}
 		}
 	}
