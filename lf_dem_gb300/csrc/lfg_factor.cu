@@ -121,12 +121,13 @@ __global__ void k_assemble(const int *__restrict__ col_tasks, const int *__restr
 		int rb = r/6, rr = r%6;
 		T v = 0;
 		for (int q = ca; q < cz; q++) {
-			int ch = children[q];
-			const int *inv = cinv+cinv_off[ch];
-			int ir = inv[rb], ic = inv[cb];
+			int ch = __ldg(&children[q]);
+			const int *inv = cinv+__ldg(&cinv_off[ch]);
+			int ir = __ldg(&inv[rb]), ic = __ldg(&inv[cb]);
 			if (ir >= 0 && ic >= 0) {
-				int cld = sn_ld[ch];
-				v += arena[sn_off[ch]+(int64_t)(6*ic+cr)*cld+6*ir+rr];
+				int cld = __ldg(&sn_ld[ch]);
+				// child fronts are complete and not written here: read-only loads
+				v += __ldg(&arena[__ldg(&sn_off[ch])+(int64_t)(6*ic+cr)*cld+6*ir+rr]);
 			}
 		}
 		col[r] = v;
@@ -149,9 +150,17 @@ __global__ void k_scatter_d(int count, const int *__restrict__ list, const doubl
 	pdl_wait();
 	double m[36];
 	d15_to_dense(dblocks+15*(int64_t)i, m);
-	for (int c = 0; c < 6; c++)
-		for (int r = c; r < 6; r++)
-			base[(int64_t)(6*b+c)*ld+6*b+r] += (T)m[r*6+c];
+	// all 21 old values are loaded before the first store (a store between
+	// them would serialise the loads: the addresses may alias)
+	T old[21];
+#pragma unroll
+	for (int c = 0, e = 0; c < 6; c++)
+#pragma unroll
+		for (int r = c; r < 6; r++, e++) old[e] = base[(int64_t)(6*b+c)*ld+6*b+r];
+#pragma unroll
+	for (int c = 0, e = 0; c < 6; c++)
+#pragma unroll
+		for (int r = c; r < 6; r++, e++) base[(int64_t)(6*b+c)*ld+6*b+r] = old[e]+(T)m[r*6+c];
 }
 
 template <typename T>
@@ -170,9 +179,16 @@ __global__ void k_scatter_od(int count, const int *__restrict__ list, const doub
 	pdl_wait();
 	double m[36];
 	od18_to_dense(odblocks+18*(int64_t)e, m);
+	T old[36];
+#pragma unroll
 	for (int c = 0; c < 6; c++)
+#pragma unroll
+		for (int r = 0; r < 6; r++) old[6*c+r] = base[(int64_t)(6*bc+c)*ld+6*br+r];
+#pragma unroll
+	for (int c = 0; c < 6; c++)
+#pragma unroll
 		for (int r = 0; r < 6; r++)
-			base[(int64_t)(6*bc+c)*ld+6*br+r] += (T)(tr ? m[c*6+r] : m[r*6+c]);
+			base[(int64_t)(6*bc+c)*ld+6*br+r] = old[6*c+r]+(T)(tr ? m[c*6+r] : m[r*6+c]);
 }
 
 // ---------------------------------------------------------------------------
@@ -189,15 +205,131 @@ __global__ void k_scatter_od(int count, const int *__restrict__ list, const doub
 constexpr unsigned FULL_MASK = 0xffffffffu;
 
 // Warp routines on 32 x 32 blocks in shared memory (row-major, stride ld),
-// one row or column per lane in registers, loops fully unrolled so every
-// register index is static.  Pivots use rsqrt and the triangular solves use
-// reciprocals of the diagonal (shuffled from the lane that owns it), so each
-// step's dependent chain is a shuffle, a multiply and the updates.
+// one row or column per lane in registers.  The step loops are not unrolled
+// (the code stays small: it runs once per launch, so a fully unrolled body
+// would be fetched cold every time); register indices stay static because
+// every step shifts the lane's values down by one, so the current column is
+// always element 0.  Pivots use rsqrt and the triangular solves reciprocals
+// of the diagonal (shuffled from the lane that owns it).
+//
+// Lsh (32 x 32, 16-byte aligned): Lsh[32 j + q] = L[j + q][j] (zero past the
+// block), column j of L from the diagonal down, written by warp_potrf32 and
+// read by the solves with vector loads.
 
+// the 32 entries Lsh[32 j + q], q < 32
+template <typename T> __device__ inline void lsh_column(const T *Lsh, int j, T (&c)[32])
+{
+	if constexpr (sizeof(T) == 4) {
+		const float4 *p = reinterpret_cast<const float4 *>(Lsh+32*j);
+#pragma unroll
+		for (int u = 0; u < 8; u++) {
+			float4 v = p[u];
+			c[4*u] = v.x; c[4*u+1] = v.y; c[4*u+2] = v.z; c[4*u+3] = v.w;
+		}
+	} else {
+		const double2 *p = reinterpret_cast<const double2 *>(Lsh+32*j);
+#pragma unroll
+		for (int u = 0; u < 16; u++) {
+			double2 v = p[u];
+			c[2*u] = v.x; c[2*u+1] = v.y;
+		}
+	}
+}
+
+// v[q-1] = v[q] - f(c[q]) for 1 <= q < 32 - t, the live part of a step-t
+// shift; skips (warp-uniformly, in groups of 4) the entries past the block
+// (FP64 multiply-adds are scarce: the dead ones are not issued)
+template <typename T, typename F>
+__device__ inline void shift_update(T (&v)[32], int t, F f)
+{
+#pragma unroll
+	for (int g = 0; g < 8; g++) {
+		if (4*g <= 31-t) {
+#pragma unroll
+			for (int u = 0; u < 4; u++) {
+				int q = 4*g+u;
+				if (q >= 1) v[q-1] = v[q]-f(q);
+			}
+		}
+	}
+}
+
+// Cholesky of S (lower part), lane = row; S's lower part becomes L and its
+// upper part zero; Lsh receives L's columns
+template <typename T>
+__device__ void warp_potrf32(T *S, int ld, T *Lsh, int lane, int jlim, int gcol0, int *fail)
+{
+	T a[32];   // at step j: a[q] = S[lane][j + q]
+#pragma unroll
+	for (int l = 0; l < 32; l++) a[l] = S[lane*ld+l];
+#pragma unroll 1
+	for (int j = 0; j < 32; j++) {
+		T djj = __shfl_sync(FULL_MASK, a[0], j);
+		if (!(djj > T(0))) {
+			if (lane == 0 && j < jlim && fail) atomicMin(fail, gcol0+j+1);
+			djj = T(1);
+		}
+		T rs = rsqrt(djj);
+		T lij = a[0]*rs;
+		T v = lane > j ? lij : (lane == j ? djj*rs : T(0));
+		S[lane*ld+j] = v;
+		Lsh[32*j+((lane-j) & 31)] = lane >= j ? v : T(0);
+		__syncwarp();
+		T c[32];
+		lsh_column<T>(Lsh, j, c);
+		shift_update<T>(a, j, [&](int q) { return lij*c[q]; });
+	}
+	__syncwarp();
+}
+
+// X L^T = A for 32 rows (lane = row) of X (stride ldx), L lower (stride ldl,
+// columns in Lsh); X replaces A
+template <typename T>
+__device__ void warp_trsm32(T *X, int ldx, const T *L, int ldl, const T *Lsh, int lane)
+{
+	T rd = T(1)/L[lane*ldl+lane];
+	T x[32];   // at step t: x[q] = X[lane][t + q]
+#pragma unroll
+	for (int l = 0; l < 32; l++) x[l] = X[lane*ldx+l];
+#pragma unroll 1
+	for (int t = 0; t < 32; t++) {
+		T xt = x[0]*__shfl_sync(FULL_MASK, rd, t);
+		X[lane*ldx+t] = xt;
+		T c[32];
+		lsh_column<T>(Lsh, t, c);
+		shift_update<T>(x, t, [&](int q) { return xt*c[q]; });
+	}
+	__syncwarp();
+}
+
+// V = L^-1 (lower; lane = column), V row-major with stride ldv; L's columns
+// in Lsh
+template <typename T>
+__device__ void warp_trtri32(const T *L, int ldl, const T *Lsh, T *V, int ldv, int lane)
+{
+	T rd = T(1)/L[lane*ldl+lane];
+	T y[32];   // at step t: y[q] = V[t + q][lane]
+#pragma unroll
+	for (int i = 0; i < 32; i++) y[i] = (i == lane) ? T(1) : T(0);
+#pragma unroll 1
+	for (int t = 0; t < 32; t++) {
+		T yt = y[0]*__shfl_sync(FULL_MASK, rd, t);
+		V[t*ldv+lane] = yt;
+		T c[32];
+		lsh_column<T>(Lsh, t, c);
+		shift_update<T>(y, t, [&](int q) { return c[q]*yt; });
+	}
+	__syncwarp();
+}
+
+// Fully unrolled forms of the same three routines (lane = row or column,
+// every step's updates limited to the live entries), used for FP64: FP64
+// multiply-adds are scarce, so the shorter instruction stream beats the cost
+// of fetching the larger code cold; in FP32 the compact forms are faster.
 // Cholesky of S (lower part), lane = row; S's lower part becomes L and its
 // upper part zero
 template <typename T>
-__device__ void warp_potrf32(T *S, int ld, int lane, int jlim, int gcol0, int *fail)
+__device__ void warp_potrf32_unrolled(T *S, int ld, int lane, int jlim, int gcol0, int *fail)
 {
 	T a[32];
 #pragma unroll
@@ -223,7 +355,7 @@ __device__ void warp_potrf32(T *S, int ld, int lane, int jlim, int gcol0, int *f
 // X L^T = A for 32 rows (lane = row) of X (stride ldx), L lower (stride ldl);
 // X replaces A
 template <typename T>
-__device__ void warp_trsm32(T *X, int ldx, const T *L, int ldl, int lane)
+__device__ void warp_trsm32_unrolled(T *X, int ldx, const T *L, int ldl, int lane)
 {
 	T rd = T(1)/L[lane*ldl+lane];
 	T x[32];
@@ -242,7 +374,7 @@ __device__ void warp_trsm32(T *X, int ldx, const T *L, int ldl, int lane)
 
 // V = L^-1 (lower; lane = column), V row-major with stride ldv
 template <typename T>
-__device__ void warp_trtri32(const T *L, int ldl, T *V, int ldv, int lane)
+__device__ void warp_trtri32_unrolled(const T *L, int ldl, T *V, int ldv, int lane)
 {
 	T rd = T(1)/L[lane*ldl+lane];
 	T y[32];
@@ -258,6 +390,7 @@ __device__ void warp_trtri32(const T *L, int ldl, T *V, int ldv, int lane)
 	for (int i = 0; i < 32; i++) V[i*ldv+lane] = y[i];
 	__syncwarp();
 }
+
 
 // c8[q] = sum_{t < 32} A[i][t] B[t][c] for row i = tid / 4 and columns
 // c = tid % 4 + 4q (128 threads cover a 32 x 32 product); B[t][c] is read at
@@ -279,28 +412,51 @@ __device__ void cta_gemm32(T (&c8)[8], const T *A, int lda, const T *B, int ldb_
 // Factor and invert the NB x NB diagonal block at (p0, p0) of a front (width
 // w, identity-padded past it), with the calling CTA (>= 128 threads).  L_kk
 // goes back into the front, Linv_kk^T (row-major NB x NB) to vt.  Ls, Vs:
-// NB x (NB + 1) and Ts: 32 x 33 shared arrays of the caller.
+// NB x (NB + 1), Ts: 32 x 33 and Lsh: 2 x 32 x 32 (16-byte aligned) shared
+// arrays of the caller.
 template <typename T>
-__device__ void diag_block(T *base, int ld, int p0, int w, int gcol0, int *fail, T *Ls, T *Vs, T *Ts, T *vt)
+__device__ void diag_block(T *base, int ld, int p0, int w, int gcol0, int *fail, T *Ls, T *Vs, T *Ts, T *Lsh, T *vt)
 {
 	constexpr int NB = Cfg<T>::NB, LD = NB+1;
 	static_assert(NB == 32 || NB == 64, "panel width");
 	int warp = threadIdx.x/32, lane = threadIdx.x%32;
-	for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
-		int i = e%NB, j = e/NB;    // coalesced over i (column-major front)
-		T v = T(0);
-		if (j <= i) {
-			if (i < w) v = base[(int64_t)(p0+j)*ld+p0+i];
-			else if (i == j) v = T(1);
+	// batches of 16 loads per thread in flight, then their shared stores
+	for (int e0 = threadIdx.x; e0 < NB*NB; e0 += 16*blockDim.x) {
+		T v[16];
+#pragma unroll
+		for (int u = 0; u < 16; u++) {
+			int e = e0+u*blockDim.x;
+			int i = e%NB, j = e/NB;    // coalesced over i (column-major front)
+			v[u] = T(0);
+			if (e < NB*NB && j <= i) {
+				if (i < w) v[u] = base[(int64_t)(p0+j)*ld+p0+i];
+				else if (i == j) v[u] = T(1);
+			}
 		}
-		Ls[i*LD+j] = v;
-		Vs[i*LD+j] = T(0);
+#pragma unroll
+		for (int u = 0; u < 16; u++) {
+			int e = e0+u*blockDim.x;
+			if (e < NB*NB) {
+				int i = e%NB, j = e/NB;
+				Ls[i*LD+j] = v[u];
+				Vs[i*LD+j] = T(0);
+			}
+		}
 	}
 	__syncthreads();
-	if (warp == 0) warp_potrf32<T>(Ls, LD, lane, w, gcol0, fail);
+	constexpr bool unrolled = sizeof(T) == 8;
+	if (warp == 0) {
+		if constexpr (unrolled) warp_potrf32_unrolled<T>(Ls, LD, lane, w, gcol0, fail);
+		else warp_potrf32<T>(Ls, LD, Lsh, lane, w, gcol0, fail);
+	}
 	__syncthreads();
-	if (warp == 0) warp_trtri32<T>(Ls, LD, Vs, LD, lane);                        // Linv11
-	else if (NB == 64 && warp == 1) warp_trsm32<T>(Ls+32*LD, LD, Ls, LD, lane);   // L21 = A21 L11^-T
+	if (warp == 0) {                                                                   // Linv11
+		if constexpr (unrolled) warp_trtri32_unrolled<T>(Ls, LD, Vs, LD, lane);
+		else warp_trtri32<T>(Ls, LD, Lsh, Vs, LD, lane);
+	} else if (NB == 64 && warp == 1) {                                                // L21 = A21 L11^-T
+		if constexpr (unrolled) warp_trsm32_unrolled<T>(Ls+32*LD, LD, Ls, LD, lane);
+		else warp_trsm32<T>(Ls+32*LD, LD, Ls, LD, Lsh, lane);
+	}
 	__syncthreads();
 	if (NB == 64) {
 		bool act = threadIdx.x < 128;   // cta_gemm32 covers 32 x 32 with 128 threads
@@ -317,9 +473,15 @@ __device__ void diag_block(T *base, int ld, int p0, int w, int gcol0, int *fail,
 			}
 		}
 		__syncthreads();
-		if (warp == 0) warp_potrf32<T>(Ls+32*LD+32, LD, lane, w-32, gcol0+32, fail);
+		if (warp == 0) {
+			if constexpr (unrolled) warp_potrf32_unrolled<T>(Ls+32*LD+32, LD, lane, w-32, gcol0+32, fail);
+			else warp_potrf32<T>(Ls+32*LD+32, LD, Lsh+1024, lane, w-32, gcol0+32, fail);
+		}
 		__syncthreads();
-		if (warp == 0) warp_trtri32<T>(Ls+32*LD+32, LD, Vs+32*LD+32, LD, lane);   // Linv22
+		if (warp == 0) {                                                               // Linv22
+			if constexpr (unrolled) warp_trtri32_unrolled<T>(Ls+32*LD+32, LD, Vs+32*LD+32, LD, lane);
+			else warp_trtri32<T>(Ls+32*LD+32, LD, Lsh+1024, Vs+32*LD+32, LD, lane);
+		}
 		__syncthreads();
 		if (act) {
 			cta_gemm32<T>(c8, Vs+32*LD+32, LD, Ts, 33, 1);       // Linv22 T1
@@ -356,10 +518,11 @@ __global__ void __launch_bounds__(128) k_diag(const int4 *__restrict__ tasks, co
 	__shared__ T Ls[NB*LD];
 	__shared__ T Vs[NB*LD];
 	__shared__ T Ts[32*33];
+	__shared__ __align__(16) T Lsh[2*32*32];
 	int4 tk = tasks[blockIdx.x];
 	int s = tk.x, p0 = tk.y, k = tk.z, w = tk.w;
 	pdl_wait();
-	diag_block<T>(arena+sn_off[s], sn_ld[s], p0, w, 6*sn_first[s]+p0, fail, Ls, Vs, Ts,
+	diag_block<T>(arena+sn_off[s], sn_ld[s], p0, w, 6*sn_first[s]+p0, fail, Ls, Vs, Ts, Lsh,
 	              linv_slot<T>(linv, nsn, s, k));
 }
 
@@ -407,10 +570,27 @@ __global__ void __launch_bounds__(256) k_trsm(const int4 *__restrict__ tasks, co
 	T *base = arena+sn_off[s];
 	const T *vt = linv_slot<T>(linv, nsn, s, k);
 	pdl_wait();
-	for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) Vt[e] = vt[e];
-	for (int e = threadIdx.x; e < PANEL_ROWS*NB; e += blockDim.x) {
-		int r = e%PANEL_ROWS, t = e/PANEL_ROWS;   // coalesced over rows
-		As[r*NB+(t ^ (r & 31))] = (r < nrows && t < w) ? base[(int64_t)(p0+t)*ld+row0+r] : T(0);
+	// all of a thread's loads are issued before its shared stores (256
+	// threads: NB*NB/256 entries of Linv^T, PANEL_ROWS*NB/256 of the panel)
+	{
+		constexpr int PV = NB*NB/256, PA = PANEL_ROWS*NB/256;
+		T lv[PV], av[PA];
+#pragma unroll
+		for (int u = 0; u < PV; u++) lv[u] = vt[threadIdx.x+256*u];
+#pragma unroll
+		for (int u = 0; u < PA; u++) {
+			int e = threadIdx.x+256*u;
+			int r = e%PANEL_ROWS, t = e/PANEL_ROWS;   // coalesced over rows
+			av[u] = (r < nrows && t < w) ? base[(int64_t)(p0+t)*ld+row0+r] : T(0);
+		}
+#pragma unroll
+		for (int u = 0; u < PV; u++) Vt[threadIdx.x+256*u] = lv[u];
+#pragma unroll
+		for (int u = 0; u < PA; u++) {
+			int e = threadIdx.x+256*u;
+			int r = e%PANEL_ROWS, t = e/PANEL_ROWS;
+			As[r*NB+(t ^ (r & 31))] = av[u];
+		}
 	}
 	__syncthreads();
 	int g = threadIdx.x/64, r = threadIdx.x%64;
@@ -455,7 +635,7 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 {
 	constexpr int NB = Cfg<T>::NB, TL = Cfg<T>::TILE, TPT = Cfg<T>::TPT;
 	constexpr int TD = TL/TPT; // threads per dimension (16)
-	extern __shared__ unsigned char smem_upd[];
+	extern __shared__ __align__(16) unsigned char smem_upd[];
 	T (*As)[TL] = reinterpret_cast<T (*)[TL]>(smem_upd);
 	T (*Bs)[TL] = reinterpret_cast<T (*)[TL]>(smem_upd+sizeof(T)*NB*TL);
 	int4 tk = tasks[blockIdx.x];
@@ -468,11 +648,23 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 	int clim = n6;   // own columns only; the update matrix is k_syrk's
 	pdl_wait();
 	// load panel rows of the tile rows and tile columns
-	for (int e = threadIdx.x; e < NB*TL; e += blockDim.x) {
-		int t = e/TL, i = e%TL;
-		int ra = r0+i, rb = cc0+i;
-		As[t][i] = (t < w && ra < rlim) ? base[(int64_t)(p0+t)*ld+ra] : T(0);
-		Bs[t][i] = (t < w && rb < clim) ? base[(int64_t)(p0+t)*ld+rb] : T(0);
+	{
+		constexpr int PU = NB*TL/256;   // entries of each panel per thread, all loaded before the stores
+		T av[PU], bv[PU];
+#pragma unroll
+		for (int u = 0; u < PU; u++) {
+			int e = threadIdx.x+256*u;
+			int t = e/TL, i = e%TL;
+			int ra = r0+i, rb = cc0+i;
+			av[u] = (t < w && ra < rlim) ? base[(int64_t)(p0+t)*ld+ra] : T(0);
+			bv[u] = (t < w && rb < clim) ? base[(int64_t)(p0+t)*ld+rb] : T(0);
+		}
+#pragma unroll
+		for (int u = 0; u < PU; u++) {
+			int e = threadIdx.x+256*u;
+			As[e/TL][e%TL] = av[u];
+			Bs[e/TL][e%TL] = bv[u];
+		}
 	}
 	__syncthreads();
 	int tx = threadIdx.x%TD, ty = threadIdx.x/TD;
@@ -517,10 +709,11 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 	if (!extra && r0 == t0 && cc0 == t0) {
 		__syncthreads();   // this CTA's updates of the block are visible to all its threads
 		constexpr int LD = NB+1;
-		T *Ls = reinterpret_cast<T *>(smem_upd);
+		T *Lsh = reinterpret_cast<T *>(smem_upd);   // first: 16-byte aligned
+		T *Ls = Lsh+2*32*32;
 		T *Vs = Ls+NB*LD;
 		T *Ts = Vs+NB*LD;
-		diag_block<T>(base, ld, t0, min(NB, n6-t0), 6*sn_first[s]+t0, fail, Ls, Vs, Ts,
+		diag_block<T>(base, ld, t0, min(NB, n6-t0), 6*sn_first[s]+t0, fail, Ls, Vs, Ts, Lsh,
 		              linv_slot<T>(linv, nsn, s, k+1));
 	}
 }
@@ -710,14 +903,20 @@ __device__ bool tc_tile_update(float *base, int ld, int r0, int c0, int k0, int 
 		}
 		if (!__syncthreads_and(ok)) { ok = false; return false; }
 		unsigned char *stg = sm+b*STAGE_BYTES;
+		// 16-byte chunks (4 consecutive K): the 8 lanes of a quarter warp
+		// (consecutive m) land on 8 distinct rows and swizzled chunk columns,
+		// i.e. on all 32 banks
 #pragma unroll
-		for (int k = 0; k < 16; k++) {
-			int kk = 16*h+k;
-			uint32_t off = (uint32_t)((m >> 3)*1024+(m & 7)*128+((((kk >> 2) ^ (m & 7))) << 4)+((kk & 3) << 2));
-			*reinterpret_cast<float *>(stg+0*TILE_BYTES+off) = av[k];
-			*reinterpret_cast<float *>(stg+1*TILE_BYTES+off) = tf32_lo(av[k]);
-			*reinterpret_cast<float *>(stg+2*TILE_BYTES+off) = bv[k];
-			*reinterpret_cast<float *>(stg+3*TILE_BYTES+off) = tf32_lo(bv[k]);
+		for (int c4 = 0; c4 < 4; c4++) {
+			int ck = 4*h+c4;
+			uint32_t off = (uint32_t)((m >> 3)*1024+(m & 7)*128+((ck ^ (m & 7)) << 4));
+			const float *a = av+4*c4, *bq = bv+4*c4;
+			*reinterpret_cast<float4 *>(stg+0*TILE_BYTES+off) = make_float4(a[0], a[1], a[2], a[3]);
+			*reinterpret_cast<float4 *>(stg+1*TILE_BYTES+off) =
+				make_float4(tf32_lo(a[0]), tf32_lo(a[1]), tf32_lo(a[2]), tf32_lo(a[3]));
+			*reinterpret_cast<float4 *>(stg+2*TILE_BYTES+off) = make_float4(bq[0], bq[1], bq[2], bq[3]);
+			*reinterpret_cast<float4 *>(stg+3*TILE_BYTES+off) =
+				make_float4(tf32_lo(bq[0]), tf32_lo(bq[1]), tf32_lo(bq[2]), tf32_lo(bq[3]));
 		}
 		load(ch+2, av, bv);
 		asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -844,9 +1043,9 @@ __global__ void __launch_bounds__(umma::THREADS, 1) k_syrk_tc(const int4 *__rest
 
 template <typename T> static size_t update_smem()
 {
-	// the tile's two panels, or diag_block's Ls, Vs and Ts
+	// the tile's two panels, or diag_block's Lsh, Ls, Vs and Ts
 	constexpr int NB = Cfg<T>::NB;
-	return sizeof(T)*std::max(2*NB*Cfg<T>::TILE, 2*NB*(NB+1)+32*33);
+	return sizeof(T)*std::max(2*NB*Cfg<T>::TILE, 2*32*32+2*NB*(NB+1)+32*33);
 }
 
 template <typename T> static void set_update_smem()
