@@ -104,34 +104,68 @@ static void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t sme
 	LFG_CUDA(cudaLaunchKernelEx(&cfg, kern, args...));
 }
 
+// Column c of front s (rows [c, 6F) and, for own columns, the identity rows):
+// the sum over s's children, in child order, of their update-matrix entries
+// that land there.  Child-driven: for each child whose update contains
+// column c, its column is read contiguously (rows from the diagonal down)
+// and added into a shared-memory copy of the parent column through cfwd
+// (child update block -> parent front block; monotone, so the child's lower
+// triangle lands on the parent's).  The children's parameters are fetched
+// by one thread each, up to ASM_CHILDREN at a time.
+constexpr int ASM_CHILDREN = 32;
+
 template <typename T>
-__global__ void k_assemble(const int *__restrict__ col_tasks, const int *__restrict__ sn_n,
-                           const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
-                           const int64_t *__restrict__ sn_off, const int *__restrict__ child_off,
-                           const int *__restrict__ children, const int64_t *__restrict__ cinv_off,
-                           const int *__restrict__ cinv, T *__restrict__ arena)
+__global__ void __launch_bounds__(256) k_assemble(const int *__restrict__ col_tasks, const int *__restrict__ sn_n,
+                                                  const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
+                                                  const int64_t *__restrict__ sn_off,
+                                                  const int *__restrict__ child_off,
+                                                  const int *__restrict__ children,
+                                                  const int64_t *__restrict__ cinv_off,
+                                                  const int *__restrict__ cinv, const int *__restrict__ sn_rows_off,
+                                                  const int *__restrict__ cfwd, T *__restrict__ arena)
 {
+	extern __shared__ __align__(16) unsigned char smem_asm[];
+	T *buf = reinterpret_cast<T *>(smem_asm);   // buf[r - c], r in [c, 6F)
+	__shared__ int c_jc[ASM_CHILDREN], c_n6[ASM_CHILDREN], c_F6[ASM_CHILDREN], c_ld[ASM_CHILDREN],
+		c_ro[ASM_CHILDREN];
+	__shared__ int64_t c_off[ASM_CHILDREN];
 	int s = col_tasks[2*blockIdx.x], c = col_tasks[2*blockIdx.x+1];
 	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
 	T *col = arena+sn_off[s]+(int64_t)c*ld;
 	int cb = c/6, cr = c%6;
 	int ca = child_off[s], cz = child_off[s+1];
+	for (int r = c+threadIdx.x; r < F6; r += blockDim.x) buf[r-c] = T(0);
 	pdl_wait();
-	for (int r = c+threadIdx.x; r < F6; r += blockDim.x) {
-		int rb = r/6, rr = r%6;
-		T v = 0;
-		for (int q = ca; q < cz; q++) {
-			int ch = __ldg(&children[q]);
-			const int *inv = cinv+__ldg(&cinv_off[ch]);
-			int ir = __ldg(&inv[rb]), ic = __ldg(&inv[cb]);
-			if (ir >= 0 && ic >= 0) {
-				int cld = __ldg(&sn_ld[ch]);
-				// child fronts are complete and not written here: read-only loads
-				v += __ldg(&arena[__ldg(&sn_off[ch])+(int64_t)(6*ic+cr)*cld+6*ir+rr]);
-			}
+	for (int q0 = ca; q0 < cz; q0 += ASM_CHILDREN) {
+		int nq = min(ASM_CHILDREN, cz-q0);
+		__syncthreads();   // the previous chunk's parameters are no longer read
+		if (threadIdx.x < nq) {
+			int ch = children[q0+threadIdx.x];
+			int ic = cinv[cinv_off[ch]+cb];
+			c_jc[threadIdx.x] = ic < 0 ? -1 : 6*ic+cr;
+			c_n6[threadIdx.x] = 6*sn_n[ch];
+			c_F6[threadIdx.x] = 6*(sn_n[ch]+sn_m[ch]);
+			c_ld[threadIdx.x] = sn_ld[ch];
+			c_ro[threadIdx.x] = sn_rows_off[ch];
+			c_off[threadIdx.x] = sn_off[ch];
 		}
-		col[r] = v;
+		__syncthreads();
+		for (int u = 0; u < nq; u++) {
+			int jc = c_jc[u];
+			if (jc < 0) continue;   // uniform: column c is not in this child's update
+			int n6c = c_n6[u], F6c = c_F6[u];
+			// child fronts are complete and not written here: read-only loads
+			const T *src = arena+c_off[u]+(int64_t)jc*c_ld[u];
+			const int *fw = cfwd+c_ro[u];
+			for (int i = jc+threadIdx.x; i < F6c; i += blockDim.x) {
+				int pr = 6*__ldg(&fw[i/6-n6c/6])+i%6;
+				buf[pr-c] += __ldg(&src[i]);
+			}
+			__syncthreads();   // adds of one child complete before the next child's
+		}
 	}
+	__syncthreads();
+	for (int r = c+threadIdx.x; r < F6; r += blockDim.x) col[r] = buf[r-c];
 	if (c < n6)
 		for (int r = threadIdx.x; r < n6; r += blockDim.x) col[F6+r] = (r == c) ? T(1) : T(0);
 }
@@ -1048,6 +1082,21 @@ template <typename T> static size_t update_smem()
 	return sizeof(T)*std::max(2*NB*Cfg<T>::TILE, 2*32*32+2*NB*(NB+1)+32*33);
 }
 
+// assembly: one column of the largest front
+template <typename T> static size_t assemble_smem(const DevSymbolic &D) { return sizeof(T)*(size_t)D.max_F; }
+
+template <typename T> static void set_assemble_smem(const DevSymbolic &D)
+{
+	static std::mutex mu;
+	static size_t set = 48*1024;
+	size_t need = assemble_smem<T>(D);
+	std::lock_guard<std::mutex> g(mu);
+	if (need <= set) return;
+	if (need > 227*1024) throw Error{LFG_ERR_BAD_ARG, (int)D.max_F, "front too large for the assembly kernel"};
+	LFG_CUDA(cudaFuncSetAttribute(k_assemble<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+	set = need;
+}
+
 template <typename T> static void set_update_smem()
 {
 	static std::once_flag once;
@@ -1099,6 +1148,7 @@ template <typename T> void factor_alloc(DevFactor<T> &F, const DevSymbolic &D, i
 	}
 	if (!F.status) LFG_CUDA(cudaMalloc((void **)&F.status, sizeof(int)*4));
 	set_update_smem<T>();
+	set_assemble_smem<T>(D);
 }
 
 template <typename T> void factor_free(DevFactor<T> &F)
@@ -1126,10 +1176,10 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 		if (L.count <= 0) continue;
 		switch (L.kind) {
 		case PLAN_ASSEMBLE:
-			launch_pdl(k_assemble<T>, L.count, 256, 0, st, (const int *)D.col_tasks+2*L.off, (const int *)D.sn_n,
-			           (const int *)D.sn_m, (const int *)D.sn_ld, (const int64_t *)D.sn_off,
+			launch_pdl(k_assemble<T>, L.count, 256, assemble_smem<T>(D), st, (const int *)D.col_tasks+2*L.off,
+			           (const int *)D.sn_n, (const int *)D.sn_m, (const int *)D.sn_ld, (const int64_t *)D.sn_off,
 			           (const int *)D.child_off, (const int *)D.children, (const int64_t *)D.cinv_off,
-			           (const int *)D.cinv, F.arena);
+			           (const int *)D.cinv, (const int *)D.sn_rows_off, (const int *)D.cfwd, F.arena);
 			break;
 		case PLAN_SCATTER_D:
 			launch_pdl(k_scatter_d<T>, (L.count+127)/128, 128, 0, st, L.count, (const int *)D.level_d+L.off, dbl,

@@ -51,6 +51,8 @@ struct Symbolic {
 	std::vector<int> child_off, children;   // CSR over supernodes
 	std::vector<int64_t> cinv_off;
 	std::vector<int> cinv;
+	// cfwd[sn_rows_off[c] + t]: parent front block of child c's update block t
+	std::vector<int> cfwd;
 	// levels (0 = leaves)
 	int nlevels = 0;
 	std::vector<int> level_off, level_sn;   // CSR: supernodes of each level
@@ -92,6 +94,7 @@ struct DevSymbolic {
 	int *child_off = nullptr, *children = nullptr;
 	int64_t *cinv_off = nullptr;
 	int *cinv = nullptr;
+	int *cfwd = nullptr;
 	int *level_sn = nullptr;
 	int *d_sn = nullptr, *d_bc = nullptr;
 	int *od_sn = nullptr, *od_br = nullptr, *od_bc = nullptr, *od_tr = nullptr;

@@ -392,6 +392,7 @@ void symbolic_analyze(Symbolic &S, int n, int nb, const int32_t *od_row, const i
 		S.cinv_off[c+1] = S.cinv_off[c] + (p >= 0 ? S.sn_n[p]+S.sn_m[p] : 0);
 	}
 	S.cinv.assign(S.cinv_off[nsn], -1);
+	S.cfwd.assign(S.rows.size(), -1);
 	auto front_index = [&](int s, int q) -> int {
 		int f = S.sn_first[s];
 		if (q >= f && q < f+S.sn_n[s]) return q-f;
@@ -407,6 +408,7 @@ void symbolic_analyze(Symbolic &S, int n, int nb, const int32_t *od_row, const i
 			int fi = front_index(p, S.rows[S.sn_rows_off[c]+t]);
 			if (fi < 0) throw Error{LFG_ERR_BAD_ARG, 0, "symbolic: child row outside parent front"};
 			S.cinv[S.cinv_off[c]+fi] = S.sn_n[c]+t;
+			S.cfwd[S.sn_rows_off[c]+t] = fi;
 		}
 	}
 	// levels
@@ -469,7 +471,7 @@ template <typename V> static void up(V *&d, const std::vector<V> &h, cudaStream_
 void dev_symbolic_free(DevSymbolic &D)
 {
 	void *ptrs[] = {D.perm, D.iperm, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_rows_off, D.rows,
-	                D.sn_off, D.sn_woff, D.child_off, D.children, D.cinv_off, D.cinv, D.level_sn,
+	                D.sn_off, D.sn_woff, D.child_off, D.children, D.cinv_off, D.cinv, D.cfwd, D.level_sn,
 	                D.d_sn, D.d_bc, D.od_sn, D.od_br, D.od_bc, D.od_tr, D.level_d, D.level_od,
 	                D.col_tasks, D.panel_tasks, D.tile_tasks, D.diag_tasks, D.solve_phases};
 	for (void *p : ptrs) if (p) cudaFree(p);
@@ -499,7 +501,7 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 	up(D.sn_ld, S.sn_ld, st); up(D.sn_rows_off, S.sn_rows_off, st); up(D.rows, S.rows, st);
 	up(D.sn_off, S.sn_off, st); up(D.sn_woff, S.sn_woff, st);
 	up(D.child_off, S.child_off, st); up(D.children, S.children, st);
-	up(D.cinv_off, S.cinv_off, st); up(D.cinv, S.cinv, st);
+	up(D.cinv_off, S.cinv_off, st); up(D.cinv, S.cinv, st); up(D.cfwd, S.cfwd, st);
 	up(D.level_sn, S.level_sn, st);
 	up(D.d_sn, S.d_sn, st); up(D.d_bc, S.d_bc, st);
 	up(D.od_sn, S.od_sn, st); up(D.od_br, S.od_br, st); up(D.od_bc, S.od_bc, st); up(D.od_tr, S.od_tr, st);
