@@ -270,24 +270,6 @@ template <typename T> __device__ inline void lsh_column(const T *Lsh, int j, T (
 	}
 }
 
-// v[q-1] = v[q] - f(c[q]) for 1 <= q < 32 - t, the live part of a step-t
-// shift; skips (warp-uniformly, in groups of 4) the entries past the block
-// (FP64 multiply-adds are scarce: the dead ones are not issued)
-template <typename T, typename F>
-__device__ inline void shift_update(T (&v)[32], int t, F f)
-{
-#pragma unroll
-	for (int g = 0; g < 8; g++) {
-		if (4*g <= 31-t) {
-#pragma unroll
-			for (int u = 0; u < 4; u++) {
-				int q = 4*g+u;
-				if (q >= 1) v[q-1] = v[q]-f(q);
-			}
-		}
-	}
-}
-
 // Cholesky of S (lower part), lane = row; S's lower part becomes L and its
 // upper part zero; Lsh receives L's columns
 template <typename T>
@@ -311,7 +293,8 @@ __device__ void warp_potrf32(T *S, int ld, T *Lsh, int lane, int jlim, int gcol0
 		__syncwarp();
 		T c[32];
 		lsh_column<T>(Lsh, j, c);
-		shift_update<T>(a, j, [&](int q) { return lij*c[q]; });
+#pragma unroll
+		for (int q = 1; q < 32; q++) a[q-1] = a[q]-lij*c[q];   // entries past the block are dead
 	}
 	__syncwarp();
 }
@@ -331,7 +314,8 @@ __device__ void warp_trsm32(T *X, int ldx, const T *L, int ldl, const T *Lsh, in
 		X[lane*ldx+t] = xt;
 		T c[32];
 		lsh_column<T>(Lsh, t, c);
-		shift_update<T>(x, t, [&](int q) { return xt*c[q]; });
+#pragma unroll
+		for (int q = 1; q < 32; q++) x[q-1] = x[q]-xt*c[q];
 	}
 	__syncwarp();
 }
@@ -351,15 +335,17 @@ __device__ void warp_trtri32(const T *L, int ldl, const T *Lsh, T *V, int ldv, i
 		V[t*ldv+lane] = yt;
 		T c[32];
 		lsh_column<T>(Lsh, t, c);
-		shift_update<T>(y, t, [&](int q) { return c[q]*yt; });
+#pragma unroll
+		for (int q = 1; q < 32; q++) y[q-1] = y[q]-c[q]*yt;
 	}
 	__syncwarp();
 }
 
 // Fully unrolled forms of the same three routines (lane = row or column,
 // every step's updates limited to the live entries), used for FP64: FP64
-// multiply-adds are scarce, so the shorter instruction stream beats the cost
-// of fetching the larger code cold; in FP32 the compact forms are faster.
+// multiply-adds are scarce (the compact forms do twice as many, half of them
+// on dead entries), so the shorter arithmetic beats the cost of fetching the
+// larger code cold; in FP32 the compact forms are faster.
 // Cholesky of S (lower part), lane = row; S's lower part becomes L and its
 // upper part zero
 template <typename T>
@@ -448,12 +434,12 @@ __device__ void cta_gemm32(T (&c8)[8], const T *A, int lda, const T *B, int ldb_
 // goes back into the front, Linv_kk^T (row-major NB x NB) to vt.  Ls, Vs:
 // NB x (NB + 1), Ts: 32 x 33 and Lsh: 2 x 32 x 32 (16-byte aligned) shared
 // arrays of the caller.
+// diag_load: the block into Ls (lower part, identity-padded past w) and
+// zeros into Vs; diag_factor: the rest, from there
 template <typename T>
-__device__ void diag_block(T *base, int ld, int p0, int w, int gcol0, int *fail, T *Ls, T *Vs, T *Ts, T *Lsh, T *vt)
+__device__ void diag_load(const T *base, int ld, int p0, int w, T *Ls, T *Vs)
 {
 	constexpr int NB = Cfg<T>::NB, LD = NB+1;
-	static_assert(NB == 32 || NB == 64, "panel width");
-	int warp = threadIdx.x/32, lane = threadIdx.x%32;
 	// batches of 16 loads per thread in flight, then their shared stores
 	for (int e0 = threadIdx.x; e0 < NB*NB; e0 += 16*blockDim.x) {
 		T v[16];
@@ -477,7 +463,15 @@ __device__ void diag_block(T *base, int ld, int p0, int w, int gcol0, int *fail,
 			}
 		}
 	}
-	__syncthreads();
+}
+
+template <typename T>
+__device__ void diag_factor(T *base, int ld, int p0, int w, int gcol0, int *fail, T *Ls, T *Vs, T *Ts, T *Lsh,
+                            T *vt)
+{
+	constexpr int NB = Cfg<T>::NB, LD = NB+1;
+	static_assert(NB == 32 || NB == 64, "panel width");
+	int warp = threadIdx.x/32, lane = threadIdx.x%32;
 	constexpr bool unrolled = sizeof(T) == 8;
 	if (warp == 0) {
 		if constexpr (unrolled) warp_potrf32_unrolled<T>(Ls, LD, lane, w, gcol0, fail);
@@ -529,6 +523,14 @@ __device__ void diag_block(T *base, int ld, int p0, int w, int gcol0, int *fail,
 		if (j <= i && i < w) base[(int64_t)(p0+j)*ld+p0+i] = Ls[i*LD+j];
 		vt[j*NB+i] = Vs[i*LD+j];   // Linv^T[t = j][col = i]
 	}
+}
+
+template <typename T>
+__device__ void diag_block(T *base, int ld, int p0, int w, int gcol0, int *fail, T *Ls, T *Vs, T *Ts, T *Lsh, T *vt)
+{
+	diag_load<T>(base, ld, p0, w, Ls, Vs);
+	__syncthreads();
+	diag_factor<T>(base, ld, p0, w, gcol0, fail, Ls, Vs, Ts, Lsh, vt);
 }
 
 // Linv slot of supernode s for panel k: two slots per supernode, by the
@@ -659,8 +661,10 @@ __global__ void __launch_bounds__(256) k_trsm(const int4 *__restrict__ tasks, co
 
 // trailing update: CTA = one tile (sn, r0, c0, k) of the front's own columns.
 // The tile at (t0, t0) holds panel k + 1's diagonal block: after its update it
-// factors and inverts that block (diag_block), so the next panel needs no
-// separate diagonal launch.
+// factors and inverts that block (diag_factor), so the next panel needs no
+// separate diagonal launch.  (Solving panel k + 1's rows in this launch as
+// well -- column-t0 tiles waiting on a flag the diagonal CTA publishes, tasks
+// in ticket order -- was measured slower than the separate solve launch.)
 template <typename T>
 __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ tasks, const int *__restrict__ sn_first,
                                                 const int *__restrict__ sn_n, const int *__restrict__ sn_m,
@@ -680,7 +684,21 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 	bool extra = r0 >= F6;
 	int rlim = extra ? F6+t0 : F6;
 	int clim = n6;   // own columns only; the update matrix is k_syrk's
+	int tx = threadIdx.x%TD, ty = threadIdx.x/TD;
 	pdl_wait();
+	// the tile's old values, loaded first: their latency overlaps the panel
+	// loads and the products
+	T old[TPT][TPT];
+#pragma unroll
+	for (int b = 0; b < TPT; b++) {
+		int c = cc0+ty+TD*b;
+#pragma unroll
+		for (int a = 0; a < TPT; a++) {
+			int r = r0+tx+TD*a;
+			bool in = c < clim && r < rlim && (extra || r >= c);
+			old[a][b] = in ? base[(int64_t)c*ld+r] : T(0);
+		}
+	}
 	// load panel rows of the tile rows and tile columns
 	{
 		constexpr int PU = NB*TL/256;   // entries of each panel per thread, all loaded before the stores
@@ -701,7 +719,6 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 		}
 	}
 	__syncthreads();
-	int tx = threadIdx.x%TD, ty = threadIdx.x/TD;
 	T acc[TPT][TPT];
 #pragma unroll
 	for (int a = 0; a < TPT; a++)
@@ -718,37 +735,46 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 #pragma unroll
 			for (int b = 0; b < TPT; b++) acc[a][b] += av[a]*bv[b];
 	}
-	// all old values are loaded before the first store, so the loads overlap
-	// (a store between them would serialise them: the addresses may alias)
-	T old[TPT][TPT];
+	const bool diag = !extra && r0 == t0 && cc0 == t0;
+	constexpr int LD = NB+1;
+	T *Lsh = reinterpret_cast<T *>(smem_upd);   // diagonal-block work space (over As, Bs): Lsh first, 16-byte aligned
+	T *Ls = Lsh+2*32*32;
+	T *Vs = Ls+NB*LD;
+	T *Ts = Vs+NB*LD;
+	const int w1 = min(NB, n6-t0);   // width of panel k + 1
+	// With NB == TL the diagonal tile is panel k + 1's diagonal block: its
+	// entries in the block's rows go to Ls directly (diag_factor writes them
+	// back), the rows below it to the front.
+	const bool handoff = NB == TL && diag;
+	if (handoff) __syncthreads();   // As, Bs are no longer read
 #pragma unroll
 	for (int b = 0; b < TPT; b++) {
 		int c = cc0+ty+TD*b;
 #pragma unroll
 		for (int a = 0; a < TPT; a++) {
 			int r = r0+tx+TD*a;
-			bool in = c < clim && r < rlim && (extra || r >= c);
-			old[a][b] = in ? base[(int64_t)c*ld+r] : T(0);
+			T v = old[a][b]-acc[a][b];
+			if (handoff) {
+				int i = tx+TD*a, j = ty+TD*b;
+				if (i < NB && j < NB) {
+					T l = T(0);
+					if (j <= i) {
+						if (i < w1) l = v;
+						else if (i == j) l = T(1);
+					}
+					Ls[i*LD+j] = l;
+					Vs[i*LD+j] = T(0);
+				}
+				if (i < w1) continue;
+			}
+			if (c < clim && r < rlim && (extra || r >= c)) base[(int64_t)c*ld+r] = v;
 		}
 	}
-#pragma unroll
-	for (int b = 0; b < TPT; b++) {
-		int c = cc0+ty+TD*b;
-#pragma unroll
-		for (int a = 0; a < TPT; a++) {
-			int r = r0+tx+TD*a;
-			if (c < clim && r < rlim && (extra || r >= c)) base[(int64_t)c*ld+r] = old[a][b]-acc[a][b];
-		}
-	}
-	if (!extra && r0 == t0 && cc0 == t0) {
+	if (diag) {
 		__syncthreads();   // this CTA's updates of the block are visible to all its threads
-		constexpr int LD = NB+1;
-		T *Lsh = reinterpret_cast<T *>(smem_upd);   // first: 16-byte aligned
-		T *Ls = Lsh+2*32*32;
-		T *Vs = Ls+NB*LD;
-		T *Ts = Vs+NB*LD;
-		diag_block<T>(base, ld, t0, min(NB, n6-t0), 6*sn_first[s]+t0, fail, Ls, Vs, Ts, Lsh,
-		              linv_slot<T>(linv, nsn, s, k+1));
+		if (!handoff) diag_load<T>(base, ld, t0, w1, Ls, Vs);
+		__syncthreads();
+		diag_factor<T>(base, ld, t0, w1, 6*sn_first[s]+t0, fail, Ls, Vs, Ts, Lsh, linv_slot<T>(linv, nsn, s, k+1));
 	}
 }
 
@@ -1077,7 +1103,7 @@ __global__ void __launch_bounds__(umma::THREADS, 1) k_syrk_tc(const int4 *__rest
 
 template <typename T> static size_t update_smem()
 {
-	// the tile's two panels, or diag_block's Lsh, Ls, Vs and Ts
+	// the tile's two panels, or diag_factor's Lsh, Ls, Vs and Ts
 	constexpr int NB = Cfg<T>::NB;
 	return sizeof(T)*std::max(2*NB*Cfg<T>::TILE, 2*32*32+2*NB*(NB+1)+32*33);
 }
