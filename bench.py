@@ -24,6 +24,7 @@ cpu_baseline : the CPU oracle (C restatement, OpenMP) on one step of the same
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -63,8 +64,9 @@ def config(world):
 
 
 class ClockSampler:
-    """nvidia-smi clocks during the timed region."""
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi clocks every 20 ms; stop(window) keeps the samples whose own
+    timestamps fall inside the timed region (host wall-clock interval)."""
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -76,7 +78,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -87,30 +89,38 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
-    def stop(self):
+    def stop(self, window=None):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.05)   # the sample after the window's end
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         for ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
-            if len(f) < 9:
+            if len(f) < 10:
                 continue
             try:
-                sm.append(float(f[1]))
-                smax.append(float(f[2]))
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((ts, float(f[2]), float(f[3]), f[6:10]))
             except ValueError:
                 continue
-            for nm, v in zip(names, f[5:9]):
+        inside = [r for r in rows if window and window[0] <= r[0] <= window[1]]
+        use = inside if inside else rows
+        sm = [r[1] for r in use]
+        smax = [r[2] for r in use]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in use:
+            for nm, v in zip(names, r[3]):
                 if v.lower().startswith("active"):
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "window": "timed region" if inside else "whole run (no sample inside the timed region)"}
 
 
 def measured_peaks():
@@ -129,11 +139,14 @@ def run_engine(E, packing, precision, steps, warmup, device):
               precision=precision, device=device)
     g.run(warmup)
     g.clear_step_times()
+    t0 = time.time()
     g.run(steps)
+    t1 = time.time()
     ms, kernels = g.step_times()
     timing = g.timing()
     sc = g.scalars()
     g.close()
+    run_engine.window = (t0, t1)
     return ms, kernels, timing, sc
 
 
@@ -428,7 +441,7 @@ def main():
         dist.barrier()
     sampler.start()
     ms32, kern32, tim32, sc32 = run_engine(E, pk, E.PREC_FP32_REFINE, args.steps, args.warmup, local)
-    clocks = sampler.stop()
+    clocks = sampler.stop(run_engine.window)
     total32 = max_over_ranks(float(np.sum(ms32)) / 1e3, dist, torch, f"cuda:{local}")
     value = replica_value(N_PART, args.steps, world, total32)
     res = {}
