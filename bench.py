@@ -470,7 +470,9 @@ def main():
     roof = {"bound": "tensor", "achieved": achieved, "peak": bf16s, "unit": "TFLOP/s",
             "frac": achieved / bf16s, "traffic": traffic,
             "kernel": "FP32 multifrontal factorisation (k_assemble/k_panel/k_update graph)",
-            "peak_source": f"bf16_tflops_sustained ({src}); the factorisation runs on FP32 CUDA cores"}
+            "peak_source": f"bf16_tflops_sustained ({src}); the factorisation runs on FP32 CUDA cores",
+            # context: FP32 CUDA-core nominal peak, 152 SMs x 128 FMA/clk x 2 x 2.07 GHz
+            "fp32_simt_nominal_tflops": 80.5, "frac_of_fp32_simt_nominal": achieved / 80.5}
     solve_ms = stage["solve"]
     line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": float(np.mean(ms32)), "higher_is_better": True,
