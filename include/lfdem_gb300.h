@@ -103,6 +103,21 @@ typedef struct {
 int lfg_config_resolve(const char *parameter_text, char control, const char *control_value,
                        lfg_params *out, double *time_end, double *strain_end, lfg_status *st);
 
+/* The output side of the same resolution (SimulationInit.cpp:287-295,
+ * 392-402, 455-472): the output unit (the control value's scale), the factor
+ * from internal to output force units (Simulation::outputData's
+ * force_ratios[internal/output], Simulation.cpp:654-663), the control value's
+ * number (Simulation::input_rate / target_stress_input) and the output
+ * switches of the Parameter_File. */
+typedef struct {
+	char unit[32];
+	double internal_to_output;
+	double input_value;
+	int out_data_particle, out_data_interaction, origin_zero_flow, pad_;
+} lfg_output_units;
+int lfg_config_output(const char *parameter_text, char control, const char *control_value, lfg_output_units *out,
+                      lfg_status *st);
+
 /* LF_DEM's checkpoint files (Simulation::checkpoint, Simulation.cpp:602-611).
  * Binary configuration conf_*.dat (Simulation.cpp:513-600, Configuration.h:
  * 67-120): written in the labelled format 2; read in format 2 and in the old
@@ -322,6 +337,34 @@ int lfg_sim_get_step_times(lfg_sim *s, double *ms, int cap, int64_t *kernels);
 void lfg_sim_clear_step_times(lfg_sim *s);
 
 void lfg_sim_destroy(lfg_sim *s);
+
+/* LF_DEM's text output files for a simulation (Simulation::openOutputFiles,
+ * SimulationInit.cpp:1034-1074; Simulation::generateOutput with "data" and
+ * "config", Simulation.cpp:145-163): data_<name>.dat and st_<name>.dat
+ * (Simulation::outputData, Simulation.cpp:641-792), par_<name>.dat and
+ * int_<name>.dat (outputParFileTxt / outputIntFileTxt, Simulation.cpp:
+ * 884-1006), column for column, OutputData's format (OutputData.h:27-209).
+ * unit / internal_to_output / input_value as lfg_config_output gives them;
+ * version goes into the "# LF_DEM version" header line; volume_fraction into
+ * "# VF".  Existing files are an error unless force_overwrite.  Rows of int_
+ * are sorted by particle pair.  Simple shear, no walls (what the engine runs);
+ * pst_ (per-particle stress) is not written. */
+typedef struct lfg_output lfg_output;
+typedef struct {
+	const char *directory;          /* NULL or "": the working directory */
+	const char *simu_name;
+	const char *version;
+	const char *unit;
+	double internal_to_output;
+	double input_value;
+	double volume_fraction;
+	int out_data_particle, out_data_interaction, origin_zero_flow, diminish_output, force_overwrite;
+} lfg_output_config;
+int lfg_output_open(lfg_sim *s, const lfg_output_config *cfg, lfg_output **out, lfg_status *st);
+/* One output event at the current state: a data_ / st_ line, a par_ and an
+ * int_ block. */
+int lfg_output_write(lfg_output *o, lfg_status *st);
+void lfg_output_close(lfg_output *o);
 
 /* Re-run the symbolic analysis of the current pattern with another
  * nested-dissection leaf size (supernode size at the leaves). */

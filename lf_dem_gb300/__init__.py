@@ -32,6 +32,20 @@ class Status(C.Structure):
                 ("refine_residual", C.c_double), ("msg", C.c_char * 200)]
 
 
+class OutputUnits(C.Structure):
+    _fields_ = [("unit", C.c_char * 32), ("internal_to_output", C.c_double), ("input_value", C.c_double),
+                ("out_data_particle", C.c_int), ("out_data_interaction", C.c_int), ("origin_zero_flow", C.c_int),
+                ("pad_", C.c_int)]
+
+
+class OutputConfig(C.Structure):
+    _fields_ = [("directory", C.c_char_p), ("simu_name", C.c_char_p), ("version", C.c_char_p),
+                ("unit", C.c_char_p), ("internal_to_output", C.c_double), ("input_value", C.c_double),
+                ("volume_fraction", C.c_double), ("out_data_particle", C.c_int),
+                ("out_data_interaction", C.c_int), ("origin_zero_flow", C.c_int), ("diminish_output", C.c_int),
+                ("force_overwrite", C.c_int)]
+
+
 class Params(C.Structure):
     _fields_ = [
         ("kn", C.c_double), ("kt", C.c_double),
@@ -131,6 +145,7 @@ EXPORTS = [
     "lfg_batch_autotune", "lfg_batch_tuned_leaf", "lfg_batch_destroy",
     "lfg_server_create", "lfg_server_submit", "lfg_server_poll", "lfg_server_wait", "lfg_server_final_positions",
     "lfg_server_get_stats", "lfg_server_destroy",
+    "lfg_config_output", "lfg_output_open", "lfg_output_write", "lfg_output_close",
 ]
 
 _lib = None
@@ -175,10 +190,15 @@ def load(path: str | None = None):
                                       C.POINTER(C.c_double), pst]
     L.lfg_config_resolve.argtypes = [C.c_char_p, C.c_char, C.c_char_p, C.POINTER(Params), C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), pst]
+    L.lfg_config_output.argtypes = [C.c_char_p, C.c_char, C.c_char_p, C.POINTER(OutputUnits), pst]
     if hasattr(L, "lfg_sim_create"):
         L.lfg_sim_create.argtypes = [C.POINTER(Params), C.POINTER(Options), C.c_int, vp, vp, C.c_double,
                                      C.c_double, C.c_double, vp, C.c_int, vp, vp, vp, C.POINTER(vp), pst]
         L.lfg_sim_advance.argtypes = [vp, C.c_double, C.c_double, pst]
+        L.lfg_output_open.argtypes = [vp, C.POINTER(OutputConfig), C.POINTER(vp), pst]
+        L.lfg_output_write.argtypes = [vp, pst]
+        L.lfg_output_close.argtypes = [vp]
+        L.lfg_output_close.restype = None
         L.lfg_sim_step.argtypes = [vp, C.c_int, C.c_double, C.c_double, pst]
         L.lfg_sim_run.argtypes = [vp, C.c_int, C.c_double, C.c_double, pst]
         L.lfg_sim_get_scalars.argtypes = [vp, C.POINTER(SimScalars)]
@@ -328,6 +348,44 @@ def resolve_config(parameter_text: str, control: str, control_value: str):
         v = getattr(p, k)
         d[k] = tuple(v) if k in ("Ehat", "Ohat") else v
     return d, te.value, se.value
+
+
+def output_units(parameter_text: str, control: str, control_value: str) -> dict:
+    """Output unit, internal-to-output factor, control number and output
+    switches of a Parameter_File + control value (lfg_config_output)."""
+    u = OutputUnits()
+    st = Status()
+    _check(load().lfg_config_output(parameter_text.encode(), control.encode(), control_value.encode(), C.byref(u),
+                                    C.byref(st)), st)
+    return {"unit": u.unit.decode(), "internal_to_output": u.internal_to_output, "input_value": u.input_value,
+            "out_data_particle": u.out_data_particle, "out_data_interaction": u.out_data_interaction,
+            "origin_zero_flow": u.origin_zero_flow}
+
+
+class Output:
+    """LF_DEM's data_/st_/par_/int_ files for a Sim (lfg_output_*)."""
+
+    def __init__(self, sim, simu_name: str, units: dict, volume_fraction: float, directory: str = "",
+                 version: str = "lf_dem_gb300", diminish_output: bool = False, force_overwrite: bool = False):
+        L = load()
+        self._keep = [directory.encode(), simu_name.encode(), version.encode(), units["unit"].encode()]
+        cfg = OutputConfig(self._keep[0], self._keep[1], self._keep[2], self._keep[3],
+                           units["internal_to_output"], units["input_value"], volume_fraction,
+                           int(units.get("out_data_particle", 1)), int(units.get("out_data_interaction", 1)),
+                           int(units.get("origin_zero_flow", 1)), int(diminish_output), int(force_overwrite))
+        h = C.c_void_p()
+        st = Status()
+        _check(L.lfg_output_open(sim.h, C.byref(cfg), C.byref(h), C.byref(st)), st)
+        self.h = h
+
+    def write(self):
+        st = Status()
+        _check(load().lfg_output_write(self.h, C.byref(st)), st)
+
+    def close(self):
+        if self.h:
+            load().lfg_output_close(self.h)
+            self.h = None
 
 
 def write_conf_binary(path, position, radius, lx, ly, lz, vf, le_disp=(0.0, 0.0), contacts=None):

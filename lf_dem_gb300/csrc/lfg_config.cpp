@@ -287,6 +287,17 @@ public:
 				if (x.second.unit != uf && x.second.unit != "strain")
 					throw std::runtime_error("input value \""+x.first+"\" has an unknown unit \""+x.second.unit+"\"");
 		}
+		// every pairwise ratio of the resolved forces, both ways, in the same
+		// loop order (Simulation::buildFullSetOfForceRatios, SimulationInit.cpp:
+		// 136-153): the output converter reads force_ratios[internal/output]
+		std::map<std::string, double> forces;
+		for (const auto &x : input_values)
+			if (x.second.type == "force") forces[x.first] = *x.second.value;
+		for (const auto &f1 : forces)
+			for (const auto &f2 : forces) {
+				force_ratios[f2.first+'/'+f1.first] = f2.second/f1.second;
+				force_ratios[f1.first+'/'+f2.first] = 1/force_ratios[f2.first+'/'+f1.first];
+			}
 	}
 
 	void rate_controlled(double number, const std::string &scale)
@@ -399,6 +410,48 @@ extern "C" int lfg_config_resolve(const char *text, char control, const char *co
 		*out = o;
 		if (time_end) *time_end = te;
 		if (strain_end) *strain_end = se;
+		return ok(st);
+	} catch (const std::exception &e) {
+		return fail(st, LFG_ERR_BAD_ARG, 0, e.what());
+	}
+}
+
+// Output units and switches (Simulation::setupNonDimensionalization,
+// SimulationInit.cpp:287-295, 392-402, 455-472; Simulation::outputData's
+// force_ratios[internal/output], Simulation.cpp:654-663): the output unit is
+// the control value's scale; the internal one is "hydro" under rate
+// control (non-Brownian) and the stress's unit under stress control.
+extern "C" int lfg_config_output(const char *text, char control, const char *control_value, lfg_output_units *out,
+                                 lfg_status *st)
+{
+	if (!text || !control_value || !out || (control != 'r' && control != 's'))
+		return fail(st, LFG_ERR_BAD_ARG, 0, "bad arguments");
+	try {
+		Resolver R;
+		std::string num, suf;
+		if (!get_suffix(control_value, num, suf)) throw std::runtime_error("the control value needs a unit suffix");
+		double number = std::atof(num.c_str());
+		R.defaults(suf);
+		R.read(text);
+		R.tag_strain();
+		auto ln = R.longname.find(suf);
+		if (ln == R.longname.end()) throw std::runtime_error("unknown unit suffix "+suf);
+		const std::string scale = ln->second;
+		if (control == 'r') R.rate_controlled(number, scale);
+		else R.stress_controlled(number, scale);
+		const std::string internal = control == 'r' ? std::string("hydro") : scale;
+		auto it = R.force_ratios.find(internal+"/"+scale);
+		if (it == R.force_ratios.end())
+			throw std::runtime_error("cannot convert from \""+internal+"\" units to \""+scale+"\" units");
+		lfg_output_units u;
+		std::memset(&u, 0, sizeof u);
+		std::snprintf(u.unit, sizeof u.unit, "%s", scale.c_str());
+		u.internal_to_output = it->second;
+		u.input_value = number;
+		u.out_data_particle = R.p.out_data_particle;
+		u.out_data_interaction = R.p.out_data_interaction;
+		u.origin_zero_flow = R.p.origin_zero_flow;
+		*out = u;
 		return ok(st);
 	} catch (const std::exception &e) {
 		return fail(st, LFG_ERR_BAD_ARG, 0, e.what());

@@ -2,6 +2,7 @@
 // the CUDA translation units of the GB300 engine.  Not part of the C ABI.
 #pragma once
 
+#include <array>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -171,6 +172,23 @@ struct DevBlockMatrix {
 };
 void block_residual(const DevBlockMatrix &A, int k, const double *b, const double *x, double *r,
                     cudaStream_t st);
+
+// Everything the output writers read from a simulation (lfg_output.cpp),
+// gathered by sim_output_snapshot (lfg_sim.cpp) at the current state.
+struct OutputSnapshot {
+	int n = 0, twodim = 0, lubrication = 0, repulsion = 0, control = 0;
+	double lx = 0, ly = 0, lz = 0;
+	double time = 0, strain = 0, shear_rate = 0, avg_dt = 0, max_velocity = 0;
+	double shear_disp[2] = {0, 0}, shear_strain[3] = {0, 0, 0}, Einf[6] = {0}, vel_diff[3] = {0, 0, 0};
+	double kn = 0, kt = 0, kr = 0, interaction_range = 0;
+	double total_stress[6] = {0};
+	std::vector<std::string> groups;          // System::total_stress_groups, in key order
+	std::vector<std::array<double, 6>> group_stress;
+	std::vector<double> radius, pos, vel, ang, na, na_disp, angle;   // n, 3n, 3n, 3n, 6n, 3n, n
+	std::vector<double> pairs;                // OUT_W doubles per interaction, sorted by (p0, p1)
+	int out_w = 0;
+};
+
 void axpy_vec(int n, int k, const double *d, double *x, cudaStream_t st);
 // per-RHS squared norms of r and b, written to out[2k] (device)
 void residual_norms(int n6, int k, const double *r, const double *b, double *out, cudaStream_t st);

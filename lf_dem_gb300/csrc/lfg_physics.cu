@@ -615,6 +615,7 @@ __global__ void k_pairs_update(DevParams P, int np, DevClock *__restrict__ clk, 
 				memset(&q, 0, sizeof q);
 				q.p0 = p0; q.p1 = p1;
 				q.flags = PF_INTER;
+				for (int k = 0; k < 6; k++) q.xf_contact[k] = 0;   // a new Interaction (Contact.h)
 				pair_geometry(P, sd, pos, q, c);
 				if (q.gap <= 0) contact_activate(P, q);
 				lub_update(P, q, c);
@@ -971,7 +972,7 @@ __global__ void k_rate_split(int n, const DevParams P, const DevClock *__restric
 	for (int e = 0; e < 6; e++) { split[12*i+e] = pv[e]; split[12*i+6+e] = iv[e]; }
 }
 
-__global__ void k_pair_stress(DevParams P, int np, const DevClock *__restrict__ clk, const DPair *__restrict__ pairs,
+__global__ void k_pair_stress(DevParams P, int np, const DevClock *__restrict__ clk, DPair *__restrict__ pairs,
                               const DPairConst *__restrict__ pc, const double *__restrict__ vc,
                               const double *__restrict__ vel, const double *__restrict__ ang,
                               const double *__restrict__ split, int n, double *__restrict__ scr)
@@ -981,7 +982,7 @@ __global__ void k_pair_stress(DevParams P, int np, const DevClock *__restrict__ 
 	const int W = 12*NSC;
 	double *o = scr+W*(int64_t)t;
 	for (int k = 0; k < W; k++) o[k] = 0;
-	const DPair &q = pairs[t];
+	DPair &q = pairs[t];
 	if (!(q.flags & PF_INTER)) return;
 	const DPairConst &c = pc[t];
 	int i = q.p0, j = q.p1;
@@ -1039,6 +1040,7 @@ __global__ void k_pair_stress(DevParams P, int np, const DevClock *__restrict__ 
 			v3 F = vadd(ld3(q.fs_total), dashpot_force_p0(P, clk->vel_diff, q, c, ld3(vel+3*i), ld3(vel+3*j),
 			                                             ld3(ang+3*i), ld3(ang+3*j), true));
 			s2 XF = outer_sym(rv, F);
+			for (int e = 0; e < 6; e++) q.xf_contact[e] = XF.e[e];   // Contact::calcContactStress (Contact.cpp:439-450)
 			s2 a = sscale(c.a0/r_ij, XF), b = sscale(c.a1/r_ij, XF);
 			for (int e = 0; e < 6; e++) { o[12*SC_XF_CONTACT+e] = a.e[e]; o[12*SC_XF_CONTACT+6+e] = b.e[e]; }
 		}
@@ -1068,6 +1070,92 @@ __global__ void k_pair_stress(DevParams P, int np, const DevClock *__restrict__ 
 		s2 sc = sscale(0.5, outer_sym(rv, F));
 		for (int e = 0; e < 6; e++) { o[12*SC_XF_REPULSION+e] = sc.e[e]; o[12*SC_XF_REPULSION+6+e] = sc.e[e]; }
 	}
+}
+
+// Per-pair quantities of the output files (Simulation::outputData,
+// outputIntFileTxt: Simulation.cpp:641-809, 967-1006), at the current state.
+// Record of OUT_W doubles per superset pair:
+//   0 flags, 1 p0, 2 p1, 3 contact state, 4 reduced gap, 5-7 nvec,
+//   8-10 Lubrication::getTotalForce (Lubrication.cpp:659-690; non-affine
+//        velocities, the pair's current coefficients, + GE),
+//   11-13 Contact::getTotalForce (Contact.cpp:235-250; spring + dashpot with
+//        the total velocities; zero when not in contact),
+//   14 RepulsiveForce force_norm (RepulsiveForce.cpp:76-83),
+//   15-20 Contact::contact_stresslet_XF as last set (Contact.cpp:439-450),
+//   21 Contact::calcEnergy (Contact.cpp:469-485) when in contact,
+//   22 RepulsiveForce::calcEnergy (RepulsiveForce.cpp:133-150) with repulsion,
+//   23-25 disp_tan, 26-28 disp_rolling.
+__global__ void k_pair_output(DevParams P, int np, const DevClock *__restrict__ clk, const DPair *__restrict__ pairs,
+                              const DPairConst *__restrict__ pc, const double *__restrict__ vel,
+                              const double *__restrict__ ang, const double *__restrict__ na, double *__restrict__ out)
+{
+	int t = blockIdx.x*blockDim.x+threadIdx.x;
+	if (t >= np) return;
+	const DPair &q = pairs[t];
+	double *o = out+OUT_W*(int64_t)t;
+	for (int k = 0; k < OUT_W; k++) o[k] = 0;
+	o[0] = q.flags; o[1] = q.p0; o[2] = q.p1; o[3] = q.state; o[4] = q.gap;
+	if (!(q.flags & PF_INTER)) return;
+	const DPairConst &c = pc[t];
+	int i = q.p0, j = q.p1;
+	v3 n = ld3(q.nvec);
+	st3(o+5, n);
+	if (P.lub_on) {
+		double XA[4], YA[4], YB[4], XG[4], YG[4];
+		for (int k = 0; k < 4; k++) {
+			XA[k] = c.lc[CXA+k]*q.lub_coeff;
+			YA[k] = c.lc[CYA+k]*q.log_lub_coeff;
+			YB[k] = c.lc[CYB+k]*q.log_lub_coeff;
+			XG[k] = c.lc[CXG+k]*q.lub_coeff;
+			YG[k] = c.lc[CYG+k]*q.log_lub_coeff;
+		}
+		v3 vi = ld3(na+6*i), vj = ld3(na+6*j);
+		v3 f = vscale(-vdot(vadd(vscale(XA[0], vi), vscale(XA[1], vj)), n), n);
+		if (P.tangential) {
+			v3 oi = ld3(na+6*i+3), oj = ld3(na+6*j+3);
+			f = vadd(f, vsub(vscale(-YA[0], vsub(vi, vscale(vdot(n, vi), n))),
+			                 vscale(YA[1], vsub(vj, vscale(vdot(n, vj), n)))));
+			f = vadd(f, vsub(vscale(-YB[0], vcross(n, oi)), vscale(YB[2], vcross(n, oj))));
+		}
+		// GE_i (Lubrication::calcGE_squeeze / calcGE_squeeze_tangential)
+		double nnE = vdot(n, sdot(clk->Einf, n));
+		if (!P.tangential) {
+			double ci = (XG[0]+XG[2])*nnE;
+			f = vadd(f, V(ci*n.x, ci*n.y, ci*n.z));
+		} else {
+			double YG0_YG2 = YG[0]+YG[2];
+			double cGE_i = (XG[0]+XG[2]-2*YG0_YG2)*nnE;
+			v3 En = sdot(clk->Einf, n);
+			f = vadd(f, vadd(vscale(cGE_i, n), vscale(YG0_YG2*2, En)));
+		}
+		st3(o+8, f);
+	}
+	if (q.flags & PF_CONTACT) {
+		v3 F = vadd(ld3(q.fs_total), dashpot_force_p0(P, clk->vel_diff, q, c, ld3(vel+3*i), ld3(vel+3*j),
+		                                             ld3(ang+3*i), ld3(ang+3*j), true));
+		st3(o+11, F);
+		double overlap = -q.gap;
+		double e = 0.5*c.kn_s*overlap*overlap;
+		if (q.state >= 2) {
+			e += 0.5*c.kt_s*vsq(ld3(q.disp_tan));
+			if (P.rolling) e += 0.5*c.kr_s*vsq(ld3(q.disp_roll));
+		}
+		o[21] = e;
+	}
+	if (P.repulsiveforce) {
+		o[14] = P.repulsion*q.rep_reduced;
+		double gap = q.r-c.ro, e;
+		if (gap > 0) {
+			if (P.rep_max_len == -1) e = c.rep_geo*P.rep_len*exp(-gap/P.rep_len);
+			else e = c.rep_geo*P.rep_len*exp(-gap/P.rep_len)*0.5*(1+tanh(-(gap-P.rep_max_len)/1e-3));
+		} else {
+			e = c.rep_geo*P.rep_len*(1-gap);
+		}
+		o[22] = e;
+	}
+	for (int e = 0; e < 6; e++) o[15+e] = q.xf_contact[e];
+	st3(o+23, ld3(q.disp_tan));
+	st3(o+26, ld3(q.disp_roll));
 }
 
 // per-component totals over particles (fixed-order tree reduction)
@@ -1219,6 +1307,9 @@ __global__ void k_boxing(DevParams P, DevClock *clk)
 	v3 ez = sdot(K.Einf, V(0, 0, 1));
 	v3 inc = V(2*ez.x*K.dt, 2*ez.y*K.dt, 2*ez.z*K.dt);
 	for (int k = 0; k < 3; k++) K.shear_disp[k] += P.lz*(k == 0 ? inc.x : (k == 1 ? inc.y : inc.z));
+	K.shear_strain[0] += inc.x;
+	K.shear_strain[1] += inc.y;
+	K.shear_strain[2] += inc.z;
 	int m = (int)(K.shear_disp[0]/P.lx);
 	if (K.shear_disp[0] < 0) m--;
 	K.shear_disp[0] = K.shear_disp[0]-m*P.lx;
@@ -1230,23 +1321,35 @@ __global__ void k_boxing(DevParams P, DevClock *clk)
 }
 
 // System::displacement (System.cpp:2418-2443); corrector: the velocity
-// average of timeStepMoveCorrector (System.cpp:1164-1187) first
-__global__ void k_move(DevParams P, int n, int corrector, const DevClock *__restrict__ clk, double *__restrict__ pos,
+// average of timeStepMoveCorrector (System.cpp:1164-1187) first.  mode 0
+// (Euler) and 2 (corrector) then add na_velocity dt to na_disp (System.cpp:
+// 877, 981); in 2D the angle follows the y angular velocity (System.cpp:1113,
+// 1151, 1178).
+__global__ void k_move(DevParams P, int n, int mode, const DevClock *__restrict__ clk, double *__restrict__ pos,
                        double *__restrict__ vel, double *__restrict__ ang, const double *__restrict__ vel_pred,
-                       const double *__restrict__ ang_pred)
+                       const double *__restrict__ ang_pred, const double *__restrict__ na,
+                       double *__restrict__ na_disp, double *__restrict__ angle)
 {
 	int i = blockIdx.x*blockDim.x+threadIdx.x;
 	if (i >= n) return;
 	double dt = clk->dt;
 	v3 v = ld3(vel+3*i);
 	v3 dr;
-	if (corrector) {
+	if (mode == 2) {
 		v3 vp = ld3(vel_pred+3*i);
 		v = vscale(0.5, vadd(v, vp));
+		double wy = 0.5*(ang[3*i+1]+ang_pred[3*i+1]);
 		st3(ang+3*i, vscale(0.5, vadd(ld3(ang+3*i), ld3(ang_pred+3*i))));
 		dr = vscale(dt, vsub(v, vp));
+		if (P.twodim) angle[i] += (wy-ang_pred[3*i+1])*dt;
 	} else {
 		dr = vscale(dt, v);
+		if (P.twodim) angle[i] += ang[3*i+1]*dt;
+	}
+	if (mode != 1) {
+		na_disp[3*i+0] += na[6*i+0]*dt;
+		na_disp[3*i+1] += na[6*i+1]*dt;
+		na_disp[3*i+2] += na[6*i+2]*dt;
 	}
 	v3 p = vadd(ld3(pos+3*i), dr);
 	int zs = periodize(P, clk->shear_disp, p);
@@ -1516,9 +1619,18 @@ void phys_boxing(DevSim &S, cudaStream_t st)
 	S.launches++;
 }
 
-void phys_move(DevSim &S, int corrector, cudaStream_t st)
+void phys_pair_output(DevSim &S, double *out, cudaStream_t st)
 {
-	k_move<<<blocks_for(S.n, 128), 128, 0, st>>>(S.P, S.n, corrector, S.clock, S.pos, S.vel, S.ang, S.vel_pred, S.ang_pred);
+	if (!S.npairs) return;
+	k_pair_output<<<blocks_for(S.npairs, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst, S.vel, S.ang,
+	                                                         S.na, out);
+	S.launches++;
+}
+
+void phys_move(DevSim &S, int mode, cudaStream_t st)
+{
+	k_move<<<blocks_for(S.n, 128), 128, 0, st>>>(S.P, S.n, mode, S.clock, S.pos, S.vel, S.ang, S.vel_pred, S.ang_pred,
+	                                             S.na, S.na_disp, S.angle);
 	S.launches++;
 }
 

@@ -34,6 +34,7 @@ struct DevClock {
 	long long steps;
 	int stale;       // a pair within range is missing from the superset
 	int pad_;
+	double shear_strain[3];   // System::shear_strain: unwrapped sum of 2 Einf.ez dt (System.cpp:681-683)
 };
 
 // Pair state (one record per superset pair, sorted by (p0, p1)).
@@ -45,6 +46,7 @@ struct DPair {
 	double lub_coeff, log_lub_coeff;
 	double rep_force[3], rep_reduced;
 	double disp_roll[3], prev_disp_roll[3], f_roll[3];   // rolling spring (Contact.h:33-70)
+	double xf_contact[6];   // Contact::contact_stresslet_XF as of the last stress computation that set it
 	int p0, p1, zoff, flags, state, pad_;
 };
 
@@ -69,6 +71,8 @@ struct DevSim {
 	double *pos = nullptr, *radius = nullptr;
 	double *vel = nullptr, *ang = nullptr, *vel_pred = nullptr, *ang_pred = nullptr, *u_inf = nullptr;
 	double *na = nullptr;              // 6n
+	double *na_disp = nullptr;         // 3n: System::na_disp (System.cpp:877, 981)
+	double *angle = nullptr;           // n: System::angle (2D only, System.cpp:1113, 1151, 1178)
 	double *vc = nullptr;              // NFC x 6n
 	double *fc = nullptr;              // NFC x 6n
 	double *rhs = nullptr, *sol = nullptr;  // NFC x 6n
@@ -117,7 +121,11 @@ void phys_stresslets(DevSim &S, cudaStream_t st);
 void phys_shear_rate_from_stress(DevSim &S, cudaStream_t st);
 void phys_velocities(DevSim &S, int divided, int in_predictor, cudaStream_t st);
 void phys_adapt_dt(DevSim &S, double time_end, double strain_end, cudaStream_t st);
-void phys_move(DevSim &S, int corrector, cudaStream_t st);
+// mode 0: Euler move (then na_disp), 1: predictor move, 2: corrector move (then na_disp)
+void phys_move(DevSim &S, int mode, cudaStream_t st);
+// per-pair output record (OUT_W doubles per superset pair): see k_pair_output
+constexpr int OUT_W = 40;
+void phys_pair_output(DevSim &S, double *out, cudaStream_t st);
 void phys_boxing(DevSim &S, cudaStream_t st);
 void phys_save_pred(DevSim &S, cudaStream_t st);
 void phys_clear_sliding(DevSim &S, cudaStream_t st);

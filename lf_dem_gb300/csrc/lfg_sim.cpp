@@ -46,6 +46,7 @@ public:
 	void force_component_noalloc(int comp, double *d_out, int device);
 	void timing(lfg_sim_timing *o) const;
 	void set_leaf_size(int leaf) { solver_->reanalyze(leaf); symbolic_runs_++; }
+	void output_snapshot(OutputSnapshot &o);
 	int64_t device_bytes() const;
 	std::vector<double> step_ms;
 	int64_t step_kernels = 0;
@@ -70,6 +71,11 @@ private:
 	int *d_err_ = nullptr, *h_err_ = nullptr;
 	std::vector<double> h_pos_;
 	int symbolic_runs_ = 0;
+	// System::avg_dt: mean dt over the loop steps of the last timeEvolution
+	// (System.cpp:1234-1270); dt itself for a fixed time step (:609-611)
+	double avg_dt_ = 0, avg_dt_sum_ = 0;
+	int avg_dt_n_ = 0;
+	bool adv_running_ = false;
 	// stage timing
 	struct Ev { cudaEvent_t a, b; int stage; };
 	std::vector<Ev> evs_;
@@ -144,6 +150,7 @@ Sim::Sim(const lfg_params &p, const lfg_options &o, int n, const double *pos, co
          double ly, double lz, const double *le_disp, cudaStream_t st)
     : prm_(p), opt_(o), st_(st)
 {
+	avg_dt_ = p.fixed_dt ? p.dt : 0;
 	if (p.friction_model == 4 || p.friction_model < 0 || p.friction_model > 6)
 		throw Error{LFG_ERR_BAD_ARG, p.friction_model, "unknown friction model"};
 	if (p.lubrication_model < 0 || p.lubrication_model > 2)
@@ -158,6 +165,7 @@ Sim::Sim(const lfg_params &p, const lfg_options &o, int n, const double *pos, co
 	dalloc(S_.pos, 3*n, st_); dalloc(S_.radius, n, st_);
 	dalloc(S_.vel, 3*n, st_); dalloc(S_.ang, 3*n, st_); dalloc(S_.vel_pred, 3*n, st_); dalloc(S_.ang_pred, 3*n, st_);
 	dalloc(S_.u_inf, 3*n, st_); dalloc(S_.na, 6*n, st_);
+	dalloc(S_.na_disp, 3*n, st_); dalloc(S_.angle, n, st_);
 	dalloc(S_.vc, (size_t)NFC*6*n, st_); dalloc(S_.fc, (size_t)NFC*6*n, st_);
 	dalloc(S_.rhs, (size_t)NFC*6*n, st_); dalloc(S_.sol, (size_t)NFC*6*n, st_);
 	dalloc(S_.sc, (size_t)NSC*6*n, st_); dalloc(S_.sc_tot, (size_t)NSC*6+12*(size_t)n, st_);
@@ -199,7 +207,8 @@ Sim::Sim(const lfg_params &p, const lfg_options &o, int n, const double *pos, co
 Sim::~Sim()
 {
 	delete solver_;
-	void *p[] = {S_.clock, S_.pos, S_.radius, S_.vel, S_.ang, S_.vel_pred, S_.ang_pred, S_.u_inf, S_.na, S_.vc,
+	void *p[] = {S_.clock, S_.pos, S_.radius, S_.vel, S_.ang, S_.vel_pred, S_.ang_pred, S_.u_inf, S_.na, S_.na_disp,
+	             S_.angle, S_.vc,
 	             S_.fc, S_.rhs, S_.sol, S_.sc, S_.sc_tot, S_.pairs, S_.pconst, S_.row_ptr, S_.col_ptr, S_.col_idx,
 	             S_.blk_scratch, S_.pair_scratch, S_.cell_of, S_.cell_start, S_.cell_count, S_.cell_list,
 	             S_.cand_count, S_.cand_ptr, S_.cand, d_err_};
@@ -372,7 +381,7 @@ void Sim::step(int calc_stress, double time_end, double strain_end)
 		stage_begin(5);
 		if (!prm_.fixed_dt) phys_adapt_dt(S_, time_end, strain_end, st_);
 		phys_boxing(S_, st_);
-		phys_move(S_, 0, st_);
+		phys_move(S_, 1, st_);
 		stage_end(5);
 		stage_begin(0);
 		phys_pairs_update(S_, 0, 1, false, st_);
@@ -382,7 +391,7 @@ void Sim::step(int calc_stress, double time_end, double strain_end)
 		compute_velocities(calc_stress, 0);
 		if (calc_stress) { stage_begin(4); phys_stresslets(S_, st_); stage_end(4); }
 		stage_begin(5);
-		phys_move(S_, 1, st_);
+		phys_move(S_, 2, st_);
 		stage_end(5);
 	}
 	// checkNewInteraction: the superset must hold every pair within range
@@ -447,13 +456,101 @@ bool Sim::advance_partial(double time_end, double strain_end, int max_steps)
 		if (h_clock_->time > te-1e-8 && te >= 0) return false;
 		return true;
 	};
+	if (!adv_running_) {
+		adv_running_ = true;
+		avg_dt_sum_ = 0;
+		avg_dt_n_ = 0;
+	}
 	for (int k = 0; k < max_steps && keep(time_end-adj, strain_end-adj); k++) {
 		step(0, time_end, strain_end);
-		if (error_code) return false;
+		if (error_code) { adv_running_ = false; return false; }
+		avg_dt_sum_ += h_clock_->dt;
+		avg_dt_n_++;
 	}
 	if (keep(time_end-adj, strain_end-adj)) return false;
+	avg_dt_ = avg_dt_n_ > 0 ? avg_dt_sum_/avg_dt_n_ : h_clock_->dt;
+	adv_running_ = false;
 	step(1, time_end, strain_end);
 	return error_code == 0;
+}
+
+// The state the output writers read (Simulation::outputData,
+// outputParFileTxt, outputIntFileTxt: Simulation.cpp:641-1006).
+void Sim::output_snapshot(OutputSnapshot &o)
+{
+	lfg_sim_scalars sc;
+	scalars(&sc);   // pulls the clock
+	const DevClock &K = *h_clock_;
+	const DevParams &P = S_.P;
+	const int n = S_.n;
+	o.n = n;
+	o.twodim = P.twodim;
+	o.lubrication = P.lub_on;
+	o.repulsion = P.repulsiveforce;
+	o.control = P.control;
+	o.lx = P.lx; o.ly = P.ly; o.lz = P.lz;
+	o.time = K.time; o.strain = K.strain; o.shear_rate = K.shear_rate; o.avg_dt = avg_dt_;
+	o.max_velocity = K.max_velocity;
+	o.shear_disp[0] = K.shear_disp[0]; o.shear_disp[1] = K.shear_disp[1];
+	for (int k = 0; k < 3; k++) { o.shear_strain[k] = K.shear_strain[k]; o.vel_diff[k] = K.vel_diff[k]; }
+	for (int k = 0; k < 6; k++) o.Einf[k] = K.Einf[k];
+	o.kn = prm_.kn; o.kt = prm_.kt; o.kr = prm_.kr;
+	o.interaction_range = prm_.interaction_range == -1 ? 2+prm_.lub_max_gap : prm_.interaction_range;
+	// System::total_stress_groups (Stress.cpp:70-75, 342-358): the groups of
+	// the declared components; "hydro" always (E_inf term), "dashpot" with the
+	// velocity components (lubrication)
+	std::vector<double> tot(NSC*6);
+	LFG_CUDA(cudaMemcpyAsync(tot.data(), S_.sc_tot, sizeof(double)*6*NSC, cudaMemcpyDeviceToHost, st_));
+	LFG_CUDA(cudaStreamSynchronize(st_));
+	bool has[NSC] = {(bool)P.lub_on, (bool)P.lub_on, (bool)P.lub_on, (bool)P.lub_on,
+	                 P.lub_on && P.repulsiveforce, P.control == 0, P.control == 1, P.control == 1,
+	                 (bool)P.repulsiveforce};
+	const int group[NSC] = {2, 0, 1, 2, 3, 0, 0, 0, 3};
+	double g[4][6] = {{0}};
+	for (int c = 0; c < NSC; c++)
+		if (has[c]) for (int e = 0; e < 6; e++) g[group[c]][e] += tot[6*c+e];
+	for (int a = 0; a < 4; a++) for (int e = 0; e < 6; e++) g[a][e] /= P.system_volume;
+	for (int e = 0; e < 6; e++) g[2][e] += 2*K.Einf[e]/(6*M_PI);
+	const char *names[4] = {"contact", "dashpot", "hydro", "repulsion"};
+	const bool present[4] = {true, (bool)P.lub_on, true, (bool)P.repulsiveforce};
+	o.groups.clear();
+	o.group_stress.clear();
+	for (int a = 0; a < 4; a++) {
+		if (!present[a]) continue;
+		o.groups.push_back(names[a]);
+		std::array<double, 6> v;
+		for (int e = 0; e < 6; e++) v[e] = g[a][e];
+		o.group_stress.push_back(v);
+	}
+	// System::calcStress: total = sum of the groups in key order
+	for (int e = 0; e < 6; e++) o.total_stress[e] = 0;
+	for (const auto &v : o.group_stress)
+		for (int e = 0; e < 6; e++) o.total_stress[e] += v[e];
+	auto get = [&](std::vector<double> &h, const double *d, size_t cnt) {
+		h.resize(cnt);
+		if (cnt) LFG_CUDA(cudaMemcpyAsync(h.data(), d, sizeof(double)*cnt, cudaMemcpyDeviceToHost, st_));
+	};
+	get(o.radius, S_.radius, n);
+	get(o.pos, S_.pos, 3*(size_t)n);
+	get(o.vel, S_.vel, 3*(size_t)n);
+	get(o.ang, S_.ang, 3*(size_t)n);
+	get(o.na, S_.na, 6*(size_t)n);
+	get(o.na_disp, S_.na_disp, 3*(size_t)n);
+	get(o.angle, S_.angle, n);
+	o.out_w = OUT_W;
+	std::vector<double> all;
+	if (S_.npairs) {
+		static_assert(OUT_W <= 12*NSC, "pair scratch too small for the output records");
+		phys_pair_output(S_, S_.pair_scratch, st_);   // scratch holds 12*max(NFC, NSC) >= OUT_W doubles per pair
+		get(all, S_.pair_scratch, (size_t)OUT_W*S_.npairs);
+	}
+	LFG_CUDA(cudaStreamSynchronize(st_));
+	o.pairs.clear();
+	for (int t = 0; t < S_.npairs; t++) {
+		const double *r = all.data()+(size_t)OUT_W*t;
+		if (!((int)r[0] & PF_INTER)) continue;
+		o.pairs.insert(o.pairs.end(), r, r+OUT_W);
+	}
 }
 
 void Sim::scalars(lfg_sim_scalars *o)
@@ -748,6 +845,14 @@ static int sim_status(lfg_sim *h, lfg_status *st)
 	}
 	return ok(st);
 }
+
+namespace lfg {
+int sim_output_snapshot(lfg_sim *h, OutputSnapshot &o)
+{
+	h->s->output_snapshot(o);
+	return LFG_OK;
+}
+} // namespace lfg
 
 extern "C" {
 

@@ -238,6 +238,23 @@ int main(int argc, char **argv)
 		fclose(g_out);
 	}
 
+	// Output mode: with HARNESS_OUTPUT_DSTRAIN set, the reference's own
+	// System::timeEvolution runs to strains k * DSTRAIN (k = 1..NSTEPS), each
+	// followed by Simulation::generateOutput with "data" and "config"
+	// (Simulation.cpp:145-163), which writes data_/st_/par_/int_ into OUTDIR
+	// (the files Simulation::setupSimulation opened there).
+	if (const char *ods = getenv("HARNESS_OUTPUT_DSTRAIN")) {
+		double ds = atof(ods);
+		int counter = 0;
+		std::cout.setstate(std::ios_base::failbit);
+		for (int k = 1; k <= nsteps; k++) {
+			sys.timeEvolution(-1, k*ds);
+			std::set<std::string> ev = {"data", "config"};
+			sim.generateOutput(ev, counter);
+		}
+		std::cout.clear();
+		return 0;
+	}
 	// System::timeEvolution first-time block (System.cpp:1216-1226)
 	{
 		double dt_bak = sys.dt;

@@ -9,7 +9,7 @@ R_FU (lower CSC) and force / velocity / stress components at that state, and
 the state after the step.  The tests replay each step from the stored state
 with the CPU oracle and with the GPU engine and compare.
 
-usage: python tests/golden/make_golden.py [case ...]   (needs the reference tree)
+usage: python tests/golden/make_golden.py [case | writers_case ...]   (needs the reference tree)
 """
 import os
 import subprocess
@@ -129,15 +129,57 @@ def run_case(name, c, workdir):
     return os.path.getsize(os.path.join(HERE, f"{name}.npz"))
 
 
+# Output files: the reference advances to strains k * WRITER_DSTRAIN (k = 1,
+# 2) with its own System::timeEvolution and writes data_/st_/par_/int_
+# through Simulation::generateOutput (harness output mode).
+WRITER_CASES = ["rate_n200", "stress_n200", "rate_normal_n200", "rate_2d_n200"]
+WRITER_DSTRAIN = 1e-4
+WRITER_OUTPUTS = 2
+
+
+def run_writers(name, c, workdir):
+    p = packing.generate(c["n"], c["vf"], seed=c["seed"], twodim=c.get("twodim", False))
+    conf = os.path.join(workdir, f"w_{name}.dat")
+    packing.write_conf(p, conf)
+    par = os.path.join(workdir, f"w_{name}_params.txt")
+    with open(par, "w") as f:
+        f.write(c["params"])
+    out = os.path.join(workdir, "w_" + name)
+    os.makedirs(out, exist_ok=True)
+    env = dict(os.environ, HARNESS_OUTPUT_DSTRAIN=repr(WRITER_DSTRAIN))
+    r = subprocess.run([HARNESS, conf, par, c["control"], c["value"], c["suffix"], str(WRITER_OUTPUTS), out],
+                       capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        raise RuntimeError(f"harness (output mode) failed for {name}: {r.stderr[-2000:]}")
+    data = {"param_file": np.frombuffer(c["params"].encode(), dtype=np.uint8),
+            "control": np.frombuffer(c["control"].encode(), dtype=np.uint8),
+            "control_value": np.frombuffer((c["value"]+c["suffix"]).encode(), dtype=np.uint8),
+            "dstrain": np.array([WRITER_DSTRAIN]), "outputs": np.array([WRITER_OUTPUTS])}
+    with open(conf) as f:
+        data["conf_file"] = np.frombuffer(f.read().encode(), dtype=np.uint8)
+    for kind in ("data", "st", "par", "int"):
+        files = [f for f in os.listdir(out) if f.startswith(kind + "_") and f.endswith(".dat")]
+        assert len(files) == 1, (kind, files)
+        with open(os.path.join(out, files[0]), "rb") as f:
+            data[kind] = np.frombuffer(f.read(), dtype=np.uint8)
+    path = os.path.join(HERE, f"writers_{name}.npz")
+    np.savez_compressed(path, **data)
+    return os.path.getsize(path)
+
+
 def main(only=None):
     if not os.path.exists(HARNESS):
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
     with tempfile.TemporaryDirectory() as wd:
         for name, c in CASES.items():
-            if only and name not in only:
+            if only and name not in only and "writers_" + name not in only:
                 continue
-            size = run_case(name, c, wd)
-            print(f"{name}: {size/1e3:.0f} kB")
+            if not only or name in only:
+                size = run_case(name, c, wd)
+                print(f"{name}: {size/1e3:.0f} kB")
+            if name in WRITER_CASES and (not only or name in only or "writers_" + name in only):
+                size = run_writers(name, c, wd)
+                print(f"writers_{name}: {size/1e3:.0f} kB")
 
 
 if __name__ == "__main__":

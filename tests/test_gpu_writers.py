@@ -1,0 +1,161 @@
+"""LF_DEM's output files written by the engine (lfg_output_*) against the
+files the reference itself wrote (tests/golden/writers_*.npz: LF_DEM's own
+Simulation::generateOutput after System::timeEvolution to strains 1e-4 and
+2e-4 -- a few time steps -- run by the reference harness).
+
+Headers (the createDataHeader lines, "# data in <unit> units.", the column
+list, the snapshot headers' keys) must be identical.  Numbers are printed with
+6 significant digits by both; over a few steps two FP64 runs with different
+factorisation orderings agree to ~1e-10, so a printed value can differ only in
+its last digit, at a rounding boundary: relative 2e-5, absolute 1e-8 near
+zero.  (Over hundreds of steps the runs drift apart like any two dense-
+suspension trajectories -- sliding contacts sit exactly at the Coulomb limit
+and change state on last-bit differences -- which is why the fixtures stop
+early.)  int_ rows are matched by particle pair: the reference prints its
+interaction vector's order (creation history), the engine sorted pairs.
+"""
+import io
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from _golden import GOLDEN
+
+CASES = ["rate_n200", "stress_n200", "rate_normal_n200", "rate_2d_n200"]
+RTOL, ATOL = 2e-5, 1e-8
+
+
+def _load(case):
+    F = dict(np.load(os.path.join(GOLDEN, f"writers_{case}.npz")))
+    txt = {k: F[k].tobytes().decode() for k in ("param_file", "control", "control_value", "conf_file",
+                                                 "data", "st", "par", "int")}
+    return F, txt
+
+
+def _split(text):
+    """(header lines, [(block header lines, rows)]) of an output file."""
+    lines = text.splitlines()
+    head = []
+    i = 0
+    while i < len(lines) and (lines[i].startswith("#") or lines[i] == ""):
+        head.append(lines[i])
+        i += 1
+    blocks = []
+    cur_h, cur_r = [], []
+    for ln in lines[i:]:
+        if ln.startswith("#"):
+            if cur_r:
+                blocks.append((cur_h, cur_r))
+                cur_h, cur_r = [], []
+            cur_h.append(ln)
+        elif ln.strip():
+            cur_r.append(ln.split())
+    if cur_h or cur_r:
+        blocks.append((cur_h, cur_r))
+    return head, blocks
+
+
+def _close(a, b):
+    x, y = float(a), float(b)
+    return abs(x - y) <= ATOL + RTOL * max(abs(x), abs(y))
+
+
+def _rows_match(ra, rb, where):
+    assert len(ra) == len(rb), where
+    for ta, tb in zip(ra, rb):
+        assert len(ta) == len(tb), (where, ta, tb)
+        for u, v in zip(ta, tb):
+            assert _close(u, v), (where, ta, tb)
+
+
+def _header_match(ha, hb, where):
+    assert len(ha) == len(hb), where
+    for la, lb in zip(ha, hb):
+        if " : " in la:   # snapshot header: key exact, value numeric
+            ka, va = la.split(" : ")
+            kb, vb = lb.split(" : ")
+            assert ka == kb, where
+            assert _close(va, vb), (where, la, lb)
+        else:
+            assert la == lb, (where, la, lb)
+
+
+def _compare(kind, ref, got):
+    hr, br = _split(ref)
+    hg, bg = _split(got)
+    # the file header: data header + "# data in ... units." + column list
+    first_data = [ln for ln in hr if ln.startswith("#") and " : " not in ln]
+    first_got = [ln for ln in hg if ln.startswith("#") and " : " not in ln]
+    assert first_data == first_got, kind
+    if kind in ("data", "st"):
+        _rows_match([r for _, rows in br for r in rows], [r for _, rows in bg for r in rows], kind)
+        return
+    # par_/int_: the first block's snapshot header came with the file header
+    snap_r = [[ln for ln in hr if " : " in ln]] + [h for h, _ in br[1:]]
+    snap_g = [[ln for ln in hg if " : " in ln]] + [h for h, _ in bg[1:]]
+    assert len(br) == len(bg), kind
+    for k, ((_, rr), (_, rg)) in enumerate(zip(br, bg)):
+        _header_match(snap_r[k], snap_g[k], f"{kind} block {k}")
+        if kind == "int":
+            key = lambda r: (int(float(r[0])), int(float(r[1])))
+            rr = sorted(rr, key=key)
+            rg = sorted(rg, key=key)
+            assert [key(r) for r in rr] == [key(r) for r in rg], f"int block {k}: interaction sets differ"
+            # contact state 2 (non-sliding) vs 3 (sliding): a sliding spring is
+            # rescaled to exactly mu F_n (Contact.cpp:255-282), so with mu_s =
+            # mu_d the next |f_t|^2 > (mu F_n)^2 test compares equal values and
+            # the last bit decides; "frictional" (>= 2) and the forces agree
+            for rows in (rr, rg):
+                for r in rows:
+                    if r[2] == "3":
+                        r[2] = "2"
+        _rows_match(rr, rg, f"{kind} block {k}")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    """The built library without a device (the unit resolution is host code)."""
+    import lf_dem_gb300 as E
+    from lf_dem_gb300 import build as B
+    B.build()
+    E.load()
+    return E
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_output_units_match_reference_header(lib, case):
+    """lfg_config_output's unit = the reference's '# data in <unit> units.'  (CPU)"""
+    F, txt = _load(case)
+    u = lib.output_units(txt["param_file"], txt["control"], txt["control_value"])
+    line = [ln for ln in txt["data"].splitlines() if ln.startswith("# data in ")][0]
+    assert line == f"# data in {u['unit']} units."
+    assert u["internal_to_output"] > 0
+    assert u["out_data_particle"] == 1 and u["out_data_interaction"] == 1 and u["origin_zero_flow"] == 1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_output_files_match_reference(engine, case):
+    from lf_dem_gb300 import packing
+    F, txt = _load(case)
+    with tempfile.TemporaryDirectory() as d:
+        conf = os.path.join(d, "conf.dat")
+        with open(conf, "w") as f:
+            f.write(txt["conf_file"])
+        p = packing.read_conf(conf)
+        params, _, _ = engine.resolve_config(txt["param_file"], txt["control"], txt["control_value"])
+        units = engine.output_units(txt["param_file"], txt["control"], txt["control_value"])
+        g = engine.Sim(params, p.position, p.radius, p.lx, p.ly, p.lz, precision=engine.PREC_FP64)
+        out = engine.Output(g, "gpu", units, volume_fraction=p.vf, directory=d, version="reference-sources")
+        ds = float(F["dstrain"][0])
+        for k in range(1, int(F["outputs"][0]) + 1):
+            g.advance(strain_end=k * ds)
+            out.write()
+        out.close()
+        g.close()
+        for kind in ("data", "st", "par", "int"):
+            with open(os.path.join(d, f"{kind}_gpu.dat")) as f:
+                got = f.read()
+            _compare(kind, txt[kind], got)
