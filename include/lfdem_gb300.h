@@ -184,6 +184,13 @@ int lfg_solver_factorize(lfg_solver *s, lfg_status *st);
  * rhs and x are k x 6n host arrays (x may alias rhs). */
 int lfg_solver_solve(lfg_solver *s, int k, const double *rhs, double *x, lfg_status *st);
 
+/* x = L rhs for k right-hand sides (k x 6n host arrays, x must not alias rhs)
+ * with the current factor, L L^T = R in the caller's numbering:
+ * StokesSolver::compute_LTRHS (StokesSolver.cpp:627-669), used for the
+ * Brownian force.  L is this engine's factor (nested-dissection order); the
+ * reference's CHOLMOD L is another square root of R. */
+int lfg_solver_multiply_factor(lfg_solver *s, int k, const double *rhs, double *x, lfg_status *st);
+
 /* Device-pointer variant: rhs and x are k x 6n device arrays. */
 int lfg_solver_solve_device(lfg_solver *s, int k, const double *d_rhs, double *d_x,
                             lfg_status *st);

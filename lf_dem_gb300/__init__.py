@@ -145,7 +145,7 @@ EXPORTS = [
     "lfg_batch_autotune", "lfg_batch_tuned_leaf", "lfg_batch_destroy",
     "lfg_server_create", "lfg_server_submit", "lfg_server_poll", "lfg_server_wait", "lfg_server_final_positions",
     "lfg_server_get_stats", "lfg_server_destroy",
-    "lfg_config_output", "lfg_output_open", "lfg_output_write", "lfg_output_close",
+    "lfg_config_output", "lfg_output_open", "lfg_output_write", "lfg_output_close", "lfg_solver_multiply_factor",
 ]
 
 _lib = None
@@ -177,6 +177,7 @@ def load(path: str | None = None):
     L.lfg_solver_set_blocks.argtypes = [vp, vp, C.c_int, vp, vp, vp, C.c_int, vp, pst]
     L.lfg_solver_factorize.argtypes = [vp, pst]
     L.lfg_solver_solve.argtypes = [vp, C.c_int, vp, vp, pst]
+    L.lfg_solver_multiply_factor.argtypes = [vp, C.c_int, vp, vp, pst]
     L.lfg_solver_solve_device.argtypes = [vp, C.c_int, vp, vp, pst]
     L.lfg_solver_get_stats.argtypes = [vp, C.POINTER(SolverStats)]
     L.lfg_solver_destroy.argtypes = [vp]
@@ -305,6 +306,15 @@ class Solver:
         rc = load().lfg_solver_factorize(self.h, C.byref(st))
         self.last = st
         _check(rc, st)
+
+    def multiply_L(self, b):
+        """x = L b with the current factor (R = L L^T; lfg_solver_multiply_factor)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        k = b.size // (6 * self.n)
+        x = np.zeros_like(b)
+        st = Status()
+        _check(load().lfg_solver_multiply_factor(self.h, k, _ptr(b), _ptr(x), C.byref(st)), st)
+        return x
 
     def solve(self, b):
         b = np.ascontiguousarray(b, dtype=np.float64)

@@ -142,6 +142,17 @@ int lfg_solver_factorize(lfg_solver *h, lfg_status *st)
 	LFG_GUARD_END
 }
 
+int lfg_solver_multiply_factor(lfg_solver *h, int k, const double *rhs, double *x, lfg_status *st)
+{
+	if (!h || k < 0 || (k > 0 && (!rhs || !x))) return fail(st, LFG_ERR_BAD_ARG, 0, "bad arguments");
+	LFG_GUARD_BEGIN
+	cudaSetDevice(h->device);
+	int rc = h->s->multiply_host(k, rhs, x, st);
+	if (rc) return rc;
+	return ok(st);
+	LFG_GUARD_END
+}
+
 int lfg_solver_solve(lfg_solver *h, int k, const double *rhs, double *x, lfg_status *st)
 {
 	if (!h || k < 0 || (k > 0 && (!rhs || !x))) return fail(st, LFG_ERR_BAD_ARG, 0, "bad arguments");

@@ -1375,20 +1375,23 @@ __device__ void unit_cols(const SolveArgs<T> &A, const int *lev, int bx, int by,
 }
 
 // MODE 0: w_t -= sum_j L21[t][j] y_j;  MODE 1: x_i = sum_{j >= i} E[i][j] z_j
+// (product with L, y in yp): MODE 2: x_i += sum_{j <= i} L11[i][j] y_j;
+// MODE 3: w_t += sum_j L21[t][j] y_j
 template <typename T, int K, int MODE>
 __device__ void unit_rows(const SolveArgs<T> &A, const int *lev, int bx, int by, int bz, int nchunk,
                           SolveShared<T> &sh)
 {
+	constexpr bool UPD = MODE == 0 || MODE == 3;   // rows of the update block (w)
 	int s = lev[by];
 	int n6 = 6*A.sn_n[s], m6 = 6*A.sn_m[s], ld = A.sn_ld[s];
-	int nrows = MODE == 0 ? m6 : n6;
+	int nrows = UPD ? m6 : n6;
 	int r0 = bx*32;
 	if (r0 >= nrows) return;
 	int warp = threadIdx.x/32, lane = threadIdx.x%32;
 	int f6 = 6*A.sn_first[s];
-	int jlo = (MODE == 0 ? 0 : r0)+bz*SOLVE_JC;
+	int jlo = (MODE == 1 ? r0 : 0)+bz*SOLVE_JC;
 	int jhi = min(n6, jlo+SOLVE_JC);
-	const T *M = A.arena+A.sn_off[s]+(MODE == 0 ? n6 : n6+m6);
+	const T *M = A.arena+A.sn_off[s]+(UPD ? n6 : MODE == 1 ? n6+m6 : 0);
 	int r = r0+lane;
 	pdl_wait();
 	T acc[K];
@@ -1397,6 +1400,7 @@ __device__ void unit_rows(const SolveArgs<T> &A, const int *lev, int bx, int by,
 	if (r < nrows) {
 		for (int j = jlo+warp; j < jhi; j += SOLVE_WARPS) {
 			if (MODE == 1 && j < r) continue;
+			if (MODE == 2 && j > r) continue;
 			T e = __ldg(&M[(int64_t)j*ld+r]);
 #pragma unroll
 			for (int q = 0; q < K; q++) acc[q] += e*A.yp[(int64_t)q*A.n6tot+f6+j];
@@ -1406,13 +1410,15 @@ __device__ void unit_rows(const SolveArgs<T> &A, const int *lev, int bx, int by,
 	for (int q = 0; q < K; q++) sh.red_r[warp][q][lane] = acc[q];
 	__syncthreads();
 	if (warp == 0 && r < nrows) {
-		int64_t row = MODE == 0 ? A.sn_woff[s]+r : (int64_t)f6+r;
+		int64_t row = UPD ? A.sn_woff[s]+r : (int64_t)f6+r;
 #pragma unroll
 		for (int q = 0; q < K; q++) {
 			T a = 0;
 			for (int u = 0; u < SOLVE_WARPS; u++) a += sh.red_r[u][q][lane];
 			if (nchunk == 1) {
 				if (MODE == 0) A.w[q*A.wstride+row] -= a;
+				else if (MODE == 3) A.w[q*A.wstride+row] += a;
+				else if (MODE == 2) A.xp[(int64_t)q*A.n6tot+row] += a;
 				else A.xp[(int64_t)q*A.n6tot+row] = a;
 			} else {
 				A.part[((int64_t)q*nchunk+bz)*A.pstride+row] = a;
@@ -1424,30 +1430,40 @@ __device__ void unit_rows(const SolveArgs<T> &A, const int *lev, int bx, int by,
 template <typename T, int K, int MODE>
 __device__ void unit_rowsum(const SolveArgs<T> &A, const int *lev, int bx, int by, int nchunk)
 {
+	constexpr bool UPD = MODE == 0 || MODE == 3;
 	int s = lev[by];
-	int nrows = MODE == 0 ? 6*A.sn_m[s] : 6*A.sn_n[s];
+	int nrows = UPD ? 6*A.sn_m[s] : 6*A.sn_n[s];
 	int r = bx*blockDim.x+threadIdx.x;
 	if (r >= nrows) return;
-	int64_t row = MODE == 0 ? A.sn_woff[s]+r : 6*(int64_t)A.sn_first[s]+r;
+	int64_t row = UPD ? A.sn_woff[s]+r : 6*(int64_t)A.sn_first[s]+r;
 	pdl_wait();
 #pragma unroll
 	for (int q = 0; q < K; q++) {
 		T a = 0;
 		for (int c = 0; c < nchunk; c++) a += A.part[((int64_t)q*nchunk+c)*A.pstride+row];
 		if (MODE == 0) A.w[q*A.wstride+row] -= a;
+		else if (MODE == 3) A.w[q*A.wstride+row] += a;
+		else if (MODE == 2) A.xp[(int64_t)q*A.n6tot+row] += a;
 		else A.xp[(int64_t)q*A.n6tot+row] = a;
 	}
 }
 
+// in: b (permuted) into xp; in_y (product with L): b into yp and xp zeroed;
+// out: xp (unpermuted) into x
 template <typename T, int K>
-__device__ void unit_permute(const SolveArgs<T> &A, int bx, bool in)
+__device__ void unit_permute(const SolveArgs<T> &A, int bx, bool in, bool in_y = false)
 {
 	int t = bx*blockDim.x+threadIdx.x;
 	if (t >= 6*A.n) return;
 	int i = t/6, d = t%6;
 	int q = 6*A.iperm[i]+d;
 	pdl_wait();
-	if (in)
+	if (in_y) {
+		for (int r = 0; r < K; r++) {
+			A.yp[(int64_t)r*6*A.n+q] = (T)A.b[(int64_t)r*6*A.n+t];
+			A.xp[(int64_t)r*6*A.n+q] = T(0);
+		}
+	} else if (in)
 		for (int r = 0; r < K; r++) A.xp[(int64_t)r*6*A.n+q] = (T)A.b[(int64_t)r*6*A.n+t];
 	else
 		for (int r = 0; r < K; r++) A.x[(int64_t)r*6*A.n+t] = (double)A.xp[(int64_t)r*6*A.n+q];
@@ -1471,6 +1487,11 @@ __global__ void __launch_bounds__(256) k_solve_phase(SolveArgs<T> A, SolvePhase 
 	if (TYPE == SP_ROWS1) unit_rows<T, K, 1>(A, lev, bx, by, bz, ph.nchunk, sh);
 	if (TYPE == SP_ROWSUM1) unit_rowsum<T, K, 1>(A, lev, bx, by, ph.nchunk);
 	if (TYPE == SP_PERM_OUT) unit_permute<T, K>(A, bx, false);
+	if (TYPE == SP_PERM_IN_Y) unit_permute<T, K>(A, bx, true, true);
+	if (TYPE == SP_MUL_TOP) unit_rows<T, K, 2>(A, lev, bx, by, bz, ph.nchunk, sh);
+	if (TYPE == SP_MUL_TOPSUM) unit_rowsum<T, K, 2>(A, lev, bx, by, ph.nchunk);
+	if (TYPE == SP_MUL_UPD) unit_rows<T, K, 3>(A, lev, bx, by, bz, ph.nchunk, sh);
+	if (TYPE == SP_MUL_UPDSUM) unit_rowsum<T, K, 3>(A, lev, bx, by, ph.nchunk);
 }
 
 template <typename T, int K>
@@ -1486,6 +1507,11 @@ static void launch_phase(const SolveArgs<T> &A, const SolvePhase &p, cudaStream_
 	case SP_COLS1: launch_pdl(k_solve_phase<T, K, SP_COLS1>, g, 256, 0, st, A, p); break;
 	case SP_ROWS1: launch_pdl(k_solve_phase<T, K, SP_ROWS1>, g, 256, 0, st, A, p); break;
 	case SP_ROWSUM1: launch_pdl(k_solve_phase<T, K, SP_ROWSUM1>, g, 256, 0, st, A, p); break;
+	case SP_PERM_IN_Y: launch_pdl(k_solve_phase<T, K, SP_PERM_IN_Y>, g, 256, 0, st, A, p); break;
+	case SP_MUL_TOP: launch_pdl(k_solve_phase<T, K, SP_MUL_TOP>, g, 256, 0, st, A, p); break;
+	case SP_MUL_TOPSUM: launch_pdl(k_solve_phase<T, K, SP_MUL_TOPSUM>, g, 256, 0, st, A, p); break;
+	case SP_MUL_UPD: launch_pdl(k_solve_phase<T, K, SP_MUL_UPD>, g, 256, 0, st, A, p); break;
+	case SP_MUL_UPDSUM: launch_pdl(k_solve_phase<T, K, SP_MUL_UPDSUM>, g, 256, 0, st, A, p); break;
 	default: launch_pdl(k_solve_phase<T, K, SP_PERM_OUT>, g, 256, 0, st, A, p); break;
 	}
 }
@@ -1523,13 +1549,33 @@ void solve_plan_build(DevSymbolic &D, cudaStream_t st)
 	}
 	add(SP_PERM_OUT, 0, (6*n+255)/256, 1, 1, 1);
 	D.h_solve_phases = P;
-	LFG_CUDA(cudaMalloc((void **)&D.solve_phases, sizeof(SolvePhase)*P.size()));
-	LFG_CUDA(cudaMemcpyAsync(D.solve_phases, P.data(), sizeof(SolvePhase)*P.size(), cudaMemcpyHostToDevice, st));
-	LFG_CUDA(cudaStreamSynchronize(st));
+	// product y = P^T L P b (compute_LTRHS): per level leaves first, gather
+	// the children's update vectors, x_top += L11 b_top, w += L21 b_top
+	std::vector<SolvePhase> M;
+	P.swap(M);
+	add(SP_PERM_IN_Y, 0, (6*n+255)/256, 1, 1, 1);
+	for (int l = 0; l < D.nlevels; l++) {
+		int off = D.h_level_off[l], cnt = D.h_level_off[l+1]-off;
+		if (!cnt) continue;
+		int n6 = D.h_level_maxn6[l], m6 = D.h_level_maxm6[l];
+		int nch = (n6+SOLVE_JC-1)/SOLVE_JC;
+		add(SP_GATHER, off, (n6+m6+255)/256, cnt, 1, 1);
+		add(SP_MUL_TOP, off, (n6+31)/32, cnt, nch, nch);
+		if (nch > 1) add(SP_MUL_TOPSUM, off, (n6+255)/256, cnt, 1, nch);
+		if (m6 > 0) {
+			add(SP_MUL_UPD, off, (m6+31)/32, cnt, nch, nch);
+			if (nch > 1) add(SP_MUL_UPDSUM, off, (m6+255)/256, cnt, 1, nch);
+		}
+	}
+	add(SP_PERM_OUT, 0, (6*n+255)/256, 1, 1, 1);
+	D.h_mul_phases = P;
+	P.swap(M);
+	(void)st;
 }
 
 template <typename T, int K>
-static int solve_k(DevFactor<T> &F, const DevSymbolic &D, const double *b, double *x, cudaStream_t st)
+static int solve_k(DevFactor<T> &F, const DevSymbolic &D, const std::vector<SolvePhase> &phases,
+                   const double *b, double *x, cudaStream_t st)
 {
 	SolveArgs<T> A;
 	A.lev_sn = D.level_sn; A.sn_first = D.sn_first; A.sn_n = D.sn_n; A.sn_m = D.sn_m; A.sn_ld = D.sn_ld;
@@ -1537,13 +1583,14 @@ static int solve_k(DevFactor<T> &F, const DevSymbolic &D, const double *b, doubl
 	A.cinv_off = D.cinv_off; A.child_off = D.child_off; A.children = D.children; A.cinv = D.cinv;
 	A.iperm = D.iperm; A.arena = F.arena; A.w = F.w; A.xp = F.xp; A.yp = F.yp; A.part = F.part;
 	A.wstride = D.w_elems; A.pstride = F.pstride; A.n = D.nblk; A.n6tot = 6*D.nblk; A.b = b; A.x = x;
-	for (const SolvePhase &p : D.h_solve_phases) launch_phase<T, K>(A, p, st);
+	for (const SolvePhase &p : phases) launch_phase<T, K>(A, p, st);
 	LFG_CUDA(cudaGetLastError());
-	return (int)D.h_solve_phases.size();
+	return (int)phases.size();
 }
 
 template <typename T>
-int factor_solve(DevFactor<T> &F, const DevSymbolic &D, int k, const double *b, double *x, cudaStream_t st)
+static int run_sweeps(DevFactor<T> &F, const DevSymbolic &D, const std::vector<SolvePhase> &ph, int k,
+                      const double *b, double *x, cudaStream_t st)
 {
 	int launches = 0;
 	for (int r0 = 0; r0 < k; r0 += 4) {
@@ -1551,13 +1598,27 @@ int factor_solve(DevFactor<T> &F, const DevSymbolic &D, int k, const double *b, 
 		const double *bb = b+(int64_t)r0*6*D.nblk;
 		double *xx = x+(int64_t)r0*6*D.nblk;
 		switch (kk) {
-		case 1: launches += solve_k<T, 1>(F, D, bb, xx, st); break;
-		case 2: launches += solve_k<T, 2>(F, D, bb, xx, st); break;
-		case 3: launches += solve_k<T, 3>(F, D, bb, xx, st); break;
-		default: launches += solve_k<T, 4>(F, D, bb, xx, st); break;
+		case 1: launches += solve_k<T, 1>(F, D, ph, bb, xx, st); break;
+		case 2: launches += solve_k<T, 2>(F, D, ph, bb, xx, st); break;
+		case 3: launches += solve_k<T, 3>(F, D, ph, bb, xx, st); break;
+		default: launches += solve_k<T, 4>(F, D, ph, bb, xx, st); break;
 		}
 	}
 	return launches;
+}
+
+template <typename T>
+int factor_solve(DevFactor<T> &F, const DevSymbolic &D, int k, const double *b, double *x, cudaStream_t st)
+{
+	return run_sweeps(F, D, D.h_solve_phases, k, b, x, st);
+}
+
+// y = L b with the factor (R = L L^T in the caller's order): StokesSolver::
+// compute_LTRHS (StokesSolver.cpp:627-669) for the Brownian force
+template <typename T>
+int factor_multiply(DevFactor<T> &F, const DevSymbolic &D, int k, const double *b, double *x, cudaStream_t st)
+{
+	return run_sweeps(F, D, D.h_mul_phases, k, b, x, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -1683,6 +1744,10 @@ template void factor_free<double>(DevFactor<double> &);
 template void factor_free<float>(DevFactor<float> &);
 template int factor_numeric<double>(DevFactor<double> &, const DevSymbolic &, const double *, const double *, cudaStream_t);
 template int factor_numeric<float>(DevFactor<float> &, const DevSymbolic &, const double *, const double *, cudaStream_t);
+template int factor_multiply<double>(DevFactor<double> &, const DevSymbolic &, int, const double *, double *,
+                                     cudaStream_t);
+template int factor_multiply<float>(DevFactor<float> &, const DevSymbolic &, int, const double *, double *,
+                                    cudaStream_t);
 template int factor_solve<double>(DevFactor<double> &, const DevSymbolic &, int, const double *, double *, cudaStream_t);
 template int factor_solve<float>(DevFactor<float> &, const DevSymbolic &, int, const double *, double *, cudaStream_t);
 

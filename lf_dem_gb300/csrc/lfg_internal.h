@@ -83,7 +83,8 @@ void symbolic_analyze(Symbolic &S, int nblk, int nb, const int32_t *od_row,
 // ---------------------------------------------------------------------------
 // One phase of a solve sweep: gx x gy x gz work units of one type over the
 // supernodes level_sn[lev_off ...] of one level (gy of them).
-enum { SP_PERM_IN, SP_GATHER, SP_COLS0, SP_ROWS0, SP_ROWSUM0, SP_COLS1, SP_ROWS1, SP_ROWSUM1, SP_PERM_OUT };
+enum { SP_PERM_IN, SP_GATHER, SP_COLS0, SP_ROWS0, SP_ROWSUM0, SP_COLS1, SP_ROWS1, SP_ROWSUM1, SP_PERM_OUT,
+       SP_PERM_IN_Y, SP_MUL_TOP, SP_MUL_TOPSUM, SP_MUL_UPD, SP_MUL_UPDSUM };
 struct SolvePhase { int type, lev_off, gx, gy, gz, nchunk; };
 
 struct DevSymbolic {
@@ -105,8 +106,8 @@ struct DevSymbolic {
 	int4 *panel_tasks = nullptr;   // (sn, row0, k, nrows)
 	int4 *tile_tasks = nullptr;    // (sn, row0, col0, k)
 	int4 *diag_tasks = nullptr;    // (sn, col0, k, width) of each panel's diagonal block
-	SolvePhase *solve_phases = nullptr;   // phase table of a solve sweep
-	std::vector<SolvePhase> h_solve_phases;
+	std::vector<SolvePhase> h_solve_phases;   // phase table of a solve sweep
+	std::vector<SolvePhase> h_mul_phases;     // ... of the product with L
 	// host-side launch plan
 	struct Launch { int kind; int level; int k; int64_t off; int count; };
 	std::vector<Launch> factor_plan;
@@ -159,6 +160,10 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *d_dblock
 template <typename T>
 int factor_solve(DevFactor<T> &F, const DevSymbolic &D, int k, const double *b, double *x,
                  cudaStream_t st);
+// x = P^T L P b (k vectors; x may not alias b)
+template <typename T>
+int factor_multiply(DevFactor<T> &F, const DevSymbolic &D, int k, const double *b, double *x,
+                    cudaStream_t st);
 
 // y = A x for the compact block matrix (FP64), k vectors, and r = b - A x.
 // Lower/upper adjacency lists for the per-block-row gather.

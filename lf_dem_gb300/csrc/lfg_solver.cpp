@@ -264,6 +264,36 @@ int Solver::solve_device(int k, const double *b, double *x, lfg_status *st, bool
 	return LFG_OK;
 }
 
+// StokesSolver::compute_LTRHS (StokesSolver.cpp:627-669): the Brownian
+// force's L psi, with this factor's L (any L with L L^T = R gives the same
+// statistics; the reference's CHOLMOD factor is another one)
+void Solver::multiply_device(int k, const double *b, double *x)
+{
+	if (k <= 0) return;
+	run_graph(3, k, b, x, [&]() {
+		if (opt_.precision == LFG_PREC_FP64) factor_multiply(F64_, D_, k, b, x, st_);
+		else factor_multiply(F32_, D_, k, b, x, st_);
+	});
+}
+
+int Solver::multiply_host(int k, const double *rhs, double *x, lfg_status *st)
+{
+	int64_t tot = (int64_t)6*n_*k;
+	if (hcap_ < tot) {
+		if (hb_) cudaFree(hb_);
+		if (hx_) cudaFree(hx_);
+		LFG_CUDA(cudaMalloc((void **)&hb_, sizeof(double)*tot));
+		LFG_CUDA(cudaMalloc((void **)&hx_, sizeof(double)*tot));
+		hcap_ = tot;
+	}
+	LFG_CUDA(cudaMemcpyAsync(hb_, rhs, sizeof(double)*tot, cudaMemcpyHostToDevice, st_));
+	multiply_device(k, hb_, hx_);
+	LFG_CUDA(cudaMemcpyAsync(x, hx_, sizeof(double)*tot, cudaMemcpyDeviceToHost, st_));
+	LFG_CUDA(cudaStreamSynchronize(st_));
+	(void)st;
+	return LFG_OK;
+}
+
 int Solver::solve_host(int k, const double *rhs, double *x, lfg_status *st)
 {
 	int64_t tot = (int64_t)6*n_*k;

@@ -24,6 +24,9 @@ public:
 	int check_factor(lfg_status *st);
 	int solve_device(int k, const double *b, double *x, lfg_status *st, bool sync_check);
 	int solve_host(int k, const double *rhs, double *x, lfg_status *st);
+	// x = L b (R = L L^T, caller's order) with the current factor: device / host
+	void multiply_device(int k, const double *b, double *x);
+	int multiply_host(int k, const double *b, double *x, lfg_status *st);
 	void stats(lfg_solver_stats *o) const;
 	bool analyzed() const { return analyzed_; }
 	int n() const { return n_; }

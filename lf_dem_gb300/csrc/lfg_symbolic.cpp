@@ -473,7 +473,7 @@ void dev_symbolic_free(DevSymbolic &D)
 	void *ptrs[] = {D.perm, D.iperm, D.sn_first, D.sn_n, D.sn_m, D.sn_ld, D.sn_rows_off, D.rows,
 	                D.sn_off, D.sn_woff, D.child_off, D.children, D.cinv_off, D.cinv, D.cfwd, D.level_sn,
 	                D.d_sn, D.d_bc, D.od_sn, D.od_br, D.od_bc, D.od_tr, D.level_d, D.level_od,
-	                D.col_tasks, D.panel_tasks, D.tile_tasks, D.diag_tasks, D.solve_phases};
+	                D.col_tasks, D.panel_tasks, D.tile_tasks, D.diag_tasks};
 	for (void *p : ptrs) if (p) cudaFree(p);
 	D = DevSymbolic();
 }

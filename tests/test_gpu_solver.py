@@ -59,3 +59,37 @@ def test_not_spd_reported(oracle, engine):
     with pytest.raises(engine.LFGError) as ei:
         s.factorize()
     assert ei.value.code == engine.LFG_ERR_NOT_SPD
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-11), (1, 2e-6)], ids=["fp64", "fp32"])
+def test_multiply_L_is_a_square_root(oracle, engine, precision, tol):
+    """lfg_solver_multiply_factor (StokesSolver::compute_LTRHS): x = L b with
+    L L^T = R.  The engine's L is its own (nested-dissection) square root, so
+    the checks are the identities every square root satisfies: L L^T = R
+    column by column, and (L a)^T R^-1 (L b) = a^T b."""
+    import _golden as G
+    n = 60
+    p, o, d15, r, c, o18 = _assembled(oracle, n, 0.45, 21)
+    R = G.dense_from_blocks(oracle, d15, r, c, o18, n)
+    s = engine.Solver(n, precision)
+    s.set_blocks(d15, r, c, o18, True, positions=p.position)
+    s.factorize()
+    m = 6 * n
+    Lm = np.zeros((m, m))
+    for j0 in range(0, m, 4):
+        E = np.zeros((4, m))
+        for q in range(4):
+            if j0 + q < m:
+                E[q, j0 + q] = 1.0
+        Y = s.multiply_L(E)
+        for q in range(4):
+            if j0 + q < m:
+                Lm[:, j0 + q] = Y[q]
+    rel = np.abs(Lm @ Lm.T - R).max() / np.abs(R).max()
+    assert rel < tol, rel
+    rng = np.random.default_rng(5)
+    a = rng.standard_normal((2, m))
+    y = s.multiply_L(a)
+    x = np.linalg.solve(R, y.T).T
+    lhs = y[0] @ x[1]
+    assert abs(lhs - a[0] @ a[1]) < 50 * tol * np.abs(a[0]) @ np.abs(a[1])
