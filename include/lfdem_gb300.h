@@ -91,6 +91,10 @@ typedef struct {
 	double init_shear_rate_limit;
 	double mu_rolling;               /* > 0 enables rolling friction (System.cpp:386-388) */
 	double kr;                       /* rolling spring constant (Contact.cpp:35-45) */
+	double brownian;                 /* > 0: Brownian force with kT = brownian (internal units;
+	                                    System::setBrownianForceToParticle, System.cpp:1665-1710):
+	                                    rate control, predictor-corrector, fixed dt */
+	uint64_t seed;                   /* random stream of the Brownian force (Philox4x32-10) */
 } lfg_params;
 
 /* LF_DEM's Parameter_File (the text of the file) and command-line control
@@ -344,6 +348,11 @@ int lfg_sim_get_step_times(lfg_sim *s, double *ms, int cap, int64_t *kernels);
 void lfg_sim_clear_step_times(lfg_sim *s);
 
 void lfg_sim_destroy(lfg_sim *s);
+
+/* Test and restart hook (Brownian runs): the next step's predictor uses this
+ * Brownian force (6n host doubles, (F, T) per particle) instead of drawing
+ * one -- the force a reference run drew, for a step-by-step comparison. */
+int lfg_sim_set_brownian_force(lfg_sim *s, const double *fb, lfg_status *st);
 
 /* LF_DEM's text output files for a simulation (Simulation::openOutputFiles,
  * SimulationInit.cpp:1034-1074; Simulation::generateOutput with "data" and

@@ -63,7 +63,7 @@ class Params(C.Structure):
         ("shear_rate", C.c_double), ("target_stress", C.c_double),
         ("Ehat", C.c_double * 6), ("Ohat", C.c_double * 3),
         ("init_strain_shear_rate_limit", C.c_double), ("init_shear_rate_limit", C.c_double),
-        ("mu_rolling", C.c_double), ("kr", C.c_double),
+        ("mu_rolling", C.c_double), ("kr", C.c_double), ("brownian", C.c_double), ("seed", C.c_uint64),
     ]
 
 
@@ -146,6 +146,7 @@ EXPORTS = [
     "lfg_server_create", "lfg_server_submit", "lfg_server_poll", "lfg_server_wait", "lfg_server_final_positions",
     "lfg_server_get_stats", "lfg_server_destroy",
     "lfg_config_output", "lfg_output_open", "lfg_output_write", "lfg_output_close", "lfg_solver_multiply_factor",
+    "lfg_sim_set_brownian_force",
 ]
 
 _lib = None
@@ -196,6 +197,7 @@ def load(path: str | None = None):
         L.lfg_sim_create.argtypes = [C.POINTER(Params), C.POINTER(Options), C.c_int, vp, vp, C.c_double,
                                      C.c_double, C.c_double, vp, C.c_int, vp, vp, vp, C.POINTER(vp), pst]
         L.lfg_sim_advance.argtypes = [vp, C.c_double, C.c_double, pst]
+        L.lfg_sim_set_brownian_force.argtypes = [vp, vp, pst]
         L.lfg_output_open.argtypes = [vp, C.POINTER(OutputConfig), C.POINTER(vp), pst]
         L.lfg_output_write.argtypes = [vp, pst]
         L.lfg_output_close.argtypes = [vp]
@@ -593,6 +595,12 @@ class Sim:
         rc = load().lfg_sim_set_contact_rolling(self.h, int(p0), int(p1), _ptr(d))
         if rc:
             raise LFGError(rc, f"no pair ({p0}, {p1})")
+    def set_brownian_force(self, fb):
+        """The Brownian force (6n) the next predictor uses instead of a draw."""
+        f = np.ascontiguousarray(fb, dtype=np.float64)
+        st = Status()
+        _check(load().lfg_sim_set_brownian_force(self.h, _ptr(f), C.byref(st)), st)
+
     def set_clock(self, time, strain, dt, shear_rate, max_velocity, max_sliding_velocity):
         load().lfg_sim_set_clock(self.h, time, strain, dt, shear_rate, max_velocity, max_sliding_velocity)
 

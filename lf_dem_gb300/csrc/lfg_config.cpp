@@ -313,8 +313,14 @@ public:
 		*input_values[scale].value = 1/number;
 		force_ratios[scale+"/hydro"] = *input_values[scale].value;
 		resolve("hydro");
-		if (force_ratios.count("hydro/brownian") || force_ratios.count("brownian/brownian"))
-			throw std::runtime_error("Brownian forces are not supported by this engine");
+		// setUnitScaleRateControlled (SimulationInit.cpp:380-402): with a
+		// Brownian force the internal unit stays hydro above Pe_switch; below
+		// it the reference switches to Brownian units with time-averaged
+		// stresses, which this engine does not run
+		if (force_ratios.count("hydro/brownian") || force_ratios.count("brownian/brownian")) {
+			if (!(force_ratios["hydro/brownian"] > p.Pe_switch))
+				throw std::runtime_error("Brownian-dominated runs (Pe <= Pe_switch) are not supported by this engine");
+		}
 		for (auto &x : input_values) change_unit(x.second, "hydro");
 	}
 
@@ -362,8 +368,12 @@ extern "C" int lfg_config_resolve(const char *text, char control, const char *co
 		Params &p = R.p;
 		R.repulsiveforce = R.input_values.count("repulsion") > 0;
 		R.critical_load_on = R.input_values.count("critical_load") > 0;
-		if (R.input_values.count("cohesion") || R.input_values.count("brownian"))
-			throw std::runtime_error("cohesion and Brownian forces are not supported by this engine");
+		if (R.input_values.count("cohesion")) throw std::runtime_error("cohesion is not supported by this engine");
+		const bool brownian = R.input_values.count("brownian") > 0;
+		if (brownian && control != 'r')
+			throw std::runtime_error("stress-controlled Brownian runs are not supported by this engine");
+		if (brownian && p.integration_method != 1)
+			throw std::runtime_error("Brownian simulation needs to use the Predictor-Corrector method.");
 		if (R.input_values.count("hydro")) R.shear_rate = *R.input_values["hydro"].value;
 		if (R.critical_load_on) p.friction_model = 2;
 		// resolveTimeOrStrainParameters
@@ -407,6 +417,8 @@ extern "C" int lfg_config_resolve(const char *text, char control, const char *co
 		o.init_strain_shear_rate_limit = 0;
 		o.init_shear_rate_limit = 999;
 		o.mu_rolling = p.mu_rolling; o.kr = p.kr;
+		o.brownian = brownian ? p.brownian : 0;   // kT in hydro units (exportForceAmplitudes)
+		o.seed = 0;
 		*out = o;
 		if (time_end) *time_end = te;
 		if (strain_end) *strain_end = se;

@@ -629,10 +629,17 @@ __global__ void k_pairs_update(DevParams P, int np, DevClock *__restrict__ clk, 
 				if (q.flags & PF_CONTACT) contact_deactivate(P, q);
 				q.flags = 0;   // interaction removed (System.cpp:1395-1400)
 			} else {
+				// Interaction::updateContactState (Interaction.cpp:199-235)
+				q.flags &= ~PF_CHANGED;
+				const bool mark = in_predictor && P.brownian_on;
 				if (q.flags & PF_CONTACT) {
-					if (q.gap > 0) contact_deactivate(P, q);
+					if (q.gap > 0) {
+						contact_deactivate(P, q);
+						if (mark) q.flags |= PF_CHANGED;
+					}
 				} else if (q.gap <= 0) {
 					contact_activate(P, q);
+					if (mark) q.flags |= PF_CHANGED;
 				}
 				if (q.flags & PF_CONTACT) contact_spring(P, q, c);
 				lub_update(P, q, c);
@@ -765,7 +772,13 @@ __global__ void k_pair_blocks(DevParams P, int np, const DPair *__restrict__ pai
 	} else {
 		const DPairConst &c = pc[t];
 		v3 n = ld3(q.nvec);
-		if (q.flags & PF_DASHPOT) {
+		// Interaction::RFU_ODBlock / RFU_DBlocks (Interaction.cpp:247-300): in the
+		// corrector of a Brownian step, a pair whose contact opened or closed in
+		// the predictor keeps the resistance it had before (lubrication for a
+		// new contact, the dashpot for a broken one)
+		const bool dp = q.flags & PF_DASHPOT, ch = q.flags & PF_CHANGED;
+		const bool use_dashpot = !P.lub_on ? dp : (dp ? !ch : ch);
+		if (use_dashpot) {
 			const double *D = c.dc;
 			if (P.dp_tan_coeff > 0) full_blocks(D+DXA, D+DYA, D+DYB, D+DYC, n, true, od, b0, b1);
 			else xa_blocks(D[DXA+0], D[DXA+1], D[DXA+3], n, od, b0, b1);
@@ -932,15 +945,18 @@ __global__ void k_rhs(DevParams P, int n, int divided, const double *__restrict_
 	int t = blockIdx.x*blockDim.x+threadIdx.x;
 	if (t >= 6*n) return;
 	int d = t%6;
-	bool has[NFC] = {true, true, (bool)P.lub_on, (bool)P.repulsiveforce};
-	bool tq[NFC] = {(bool)P.friction, true, (bool)P.tangential, false};
+	bool has[NFC] = {true, true, (bool)P.lub_on, (bool)P.repulsiveforce, (bool)P.brownian_on};
+	bool tq[NFC] = {(bool)P.friction, true, (bool)P.tangential, false, true};
+	const int order[NFC] = {FC_BROWNIAN, FC_CONTACT, FC_DASHPOT, FC_HYDRO, FC_REPULSION};
 	if (divided) {
 		for (int c = 0; c < NFC; c++)
 			rhs[(int64_t)c*6*n+t] = (!has[c] || (d >= 3 && !tq[c])) ? 0.0 : fc[(int64_t)c*6*n+t];
 	} else {
 		double s = 0;
-		for (int c = 0; c < NFC; c++)
+		for (int u = 0; u < NFC; u++) {
+			int c = order[u];
 			if (has[c] && (d < 3 || tq[c])) s += fc[(int64_t)c*6*n+t];
+		}
 		rhs[t] = s;
 	}
 }
@@ -957,8 +973,8 @@ __global__ void k_rate_split(int n, const DevParams P, const DevClock *__restric
 	int i = blockIdx.x*blockDim.x+threadIdx.x;
 	if (i >= n) return;
 	double pv[6] = {0, 0, 0, 0, 0, 0}, iv[6] = {0, 0, 0, 0, 0, 0};
-	bool has[NFC] = {true, true, (bool)P.lub_on, (bool)P.repulsiveforce};
-	bool prop[NFC] = {false, true, true, false};
+	bool has[NFC] = {true, true, (bool)P.lub_on, (bool)P.repulsiveforce, false};
+	bool prop[NFC] = {false, true, true, false, false};
 	for (int c = 0; c < NFC; c++) {
 		if (!has[c]) continue;
 		const double *v = vc+(int64_t)c*6*n+6*i;
@@ -998,7 +1014,7 @@ __global__ void k_pair_stress(DevParams P, int np, const DevClock *__restrict__ 
 		}
 		s2 nn = outer(nv);
 		// GU per velocity component (Lubrication::addGUStresslet)
-		bool has[NFC] = {true, true, (bool)P.lub_on, (bool)P.repulsiveforce};
+		bool has[NFC] = {true, true, (bool)P.lub_on, (bool)P.repulsiveforce, (bool)P.brownian_on};
 		for (int cc = 0; cc < NFC; cc++) {
 			if (!has[cc]) continue;
 			const double *v = vc+(int64_t)cc*6*n;
@@ -1016,7 +1032,7 @@ __global__ void k_pair_stress(DevParams P, int np, const DevClock *__restrict__ 
 				sadd_to(Si, sscale(-2, saddv(sscale(YM[0], t2i), sscale(YM[1], t2j))));
 				sadd_to(Sj, sscale(-2, saddv(sscale(YM[2], t2i), sscale(YM[3], t2j))));
 			}
-			int slot = SC_GU_CONTACT+cc;
+			int slot = sc_gu_slot(cc);
 			for (int e = 0; e < 6; e++) { o[12*slot+e] = Si.e[e]; o[12*slot+6+e] = Sj.e[e]; }
 		}
 		// ME (Lubrication::addMEStresslet)
@@ -1193,7 +1209,7 @@ __global__ void k_set_rate(DevParams P, DevClock *clk, double rate) { set_rate(P
 __global__ void k_shear_rate(DevParams P, DevClock *clk, const double *__restrict__ tot, int has_mask)
 {
 	DevClock &K = *clk;
-	const int rate_of[NSC] = {1, 0, 1, 1, 0, 2, 0, 1, 0};  // 0 indep 1 prop 2 dependent
+	const int rate_of[NSC] = {1, 0, 1, 1, 0, 2, 0, 1, 0, 0, 0};  // 0 indep 1 prop 2 dependent
 	double prop[6] = {0, 0, 0, 0, 0, 0}, indep[6] = {0, 0, 0, 0, 0, 0};
 	for (int c = 0; c < NSC; c++) {
 		if (!(has_mask & (1 << c))) continue;
@@ -1221,20 +1237,28 @@ __global__ void k_velocities(DevParams P, int n, int divided, int stress_ctl, in
 	double sq = 0;
 	if (i < n) {
 		double v[6];
+		// System::sumUpVelocityComponents in map order (brownian first);
+		// 2D Brownian: rushWorkFor2DBrownian (System.cpp:2394-2416) on the
+		// Brownian component (divided) or the total
+		bool rush = P.brownian_on && P.twodim;
 		if (divided) {
-			bool has[NFC] = {true, true, (bool)P.lub_on, (bool)P.repulsiveforce};
-			bool prop[NFC] = {false, true, true, false};
+			bool has[NFC] = {true, true, (bool)P.lub_on, (bool)P.repulsiveforce, (bool)P.brownian_on};
+			bool prop[NFC] = {false, true, true, false, false};
+			const int order[NFC] = {FC_BROWNIAN, FC_CONTACT, FC_DASHPOT, FC_HYDRO, FC_REPULSION};
 			double rate = clk->shear_rate;
 			for (int e = 0; e < 6; e++) v[e] = 0;
-			for (int c = 0; c < NFC; c++) {
+			for (int u = 0; u < NFC; u++) {
+				int c = order[u];
 				if (!has[c]) continue;
 				double *x = vc+(int64_t)c*6*n+6*i;
 				if (stress_ctl && prop[c])
 					for (int e = 0; e < 6; e++) x[e] *= rate;
+				if (rush && c == FC_BROWNIAN) { x[1] = 0; x[3] = 0; x[5] = 0; }
 				for (int e = 0; e < 6; e++) v[e] += x[e];
 			}
 		} else {
 			for (int e = 0; e < 6; e++) v[e] = sol[6*i+e];
+			if (rush) { v[1] = 0; v[3] = 0; v[5] = 0; }
 		}
 		for (int e = 0; e < 6; e++) na[6*i+e] = v[e];
 		sq = v[0]*v[0]+v[1]*v[1]+v[2]*v[2];
@@ -1498,8 +1522,8 @@ void phys_force_components(DevSim &S, cudaStream_t st)
 	if (S.npairs)
 		k_pair_forces<<<blocks_for(S.npairs, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst, S.u_inf,
 		                                                         S.pair_scratch);
-	k_gather_pairs<<<blocks_for(6*NFC*S.n, 256), 256, 0, st>>>(S.n, NFC, 48, S.row_ptr, S.col_ptr, S.col_idx,
-	                                                     S.pair_scratch, S.fc);
+	k_gather_pairs<<<blocks_for(6*NPFC*S.n, 256), 256, 0, st>>>(S.n, NPFC, 12*NPFC, S.row_ptr, S.col_ptr,
+	                                                      S.col_idx, S.pair_scratch, S.fc);
 	S.launches += 2;
 }
 
@@ -1556,7 +1580,68 @@ void phys_rhs(DevSim &S, int divided, cudaStream_t st)
 	S.launches++;
 }
 
-void phys_stresslets(DevSim &S, cudaStream_t st)
+// System::calcStressPerParticle's Brownian part (Stress.cpp:270-286): every
+// component is reset first, so the predictor keeps a copy of the Brownian GU
+// stress in brownian_predictor, and the corrector halves its own Brownian GU
+// stress with the (just reset, zero) predictor copy
+__global__ void k_brownian_stress(int n6, int in_predictor, double *__restrict__ sc)
+{
+	int t = blockIdx.x*blockDim.x+threadIdx.x;
+	if (t >= n6) return;
+	double *b = sc+(int64_t)SC_GU_BROWNIAN*n6, *bp = sc+(int64_t)SC_BROWNIAN_PRED*n6;
+	if (in_predictor) bp[t] = b[t];
+	else b[t] = 0.5*(b[t]-bp[t]);
+}
+
+// Standard normal deviates for the Brownian force: Philox4x32-10 (Salmon,
+// Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC11),
+// counter (thread, draw), key = seed; Box-Muller on the two pairs of each
+// 4-word output.  Thread t writes psi[4t .. 4t+3].
+__device__ inline void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1)
+{
+	for (int r = 0; r < 10; r++) {
+		uint32_t hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u*c[0];
+		uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u*c[2];
+		uint32_t n0 = hi1^c[1]^k0, n1 = lo1, n2 = hi0^c[3]^k1, n3 = lo0;
+		c[0] = n0; c[1] = n1; c[2] = n2; c[3] = n3;
+		k0 += 0x9E3779B9u;
+		k1 += 0xBB67AE85u;
+	}
+}
+
+__global__ void k_brownian_psi(int n6, uint32_t k0, uint32_t k1, uint32_t d0, uint32_t d1, double amp,
+                               double *__restrict__ psi)
+{
+	int t = blockIdx.x*blockDim.x+threadIdx.x;
+	if (4*t >= n6) return;
+	uint32_t c[4] = {(uint32_t)t, d0, d1, 0x4C464744u};
+	philox4x32_10(c, k0, k1);
+	double z[4];
+	for (int h = 0; h < 2; h++) {
+		// u1 in (0, 1], u2 in [0, 1)
+		double u1 = ((double)c[2*h]+1.0)*2.3283064365386963e-10;
+		double u2 = (double)c[2*h+1]*2.3283064365386963e-10;
+		double r = sqrt(-2.0*log(u1));
+		double sn, cs;
+		sincospi(2.0*u2, &sn, &cs);
+		z[2*h] = r*cs;
+		z[2*h+1] = r*sn;
+	}
+	for (int q = 0; q < 4; q++)
+		if (4*t+q < n6) psi[4*t+q] = amp*z[q];
+}
+
+void phys_brownian_psi(DevSim &S, unsigned long long seed, unsigned long long draw, double amp, double *psi,
+                       cudaStream_t st)
+{
+	int n6 = 6*S.n;
+	int threads = (n6+3)/4;
+	k_brownian_psi<<<blocks_for(threads, 256), 256, 0, st>>>(n6, (uint32_t)seed, (uint32_t)(seed >> 32),
+	                                                          (uint32_t)draw, (uint32_t)(draw >> 32), amp, psi);
+	S.launches++;
+}
+
+void phys_stresslets(DevSim &S, int in_predictor, cudaStream_t st)
 {
 	double *split = S.sc_tot+6*NSC;  // n x 12 region after the totals
 	if (S.P.control == 1) {
@@ -1568,6 +1653,10 @@ void phys_stresslets(DevSim &S, cudaStream_t st)
 		                                                         S.vel, S.ang, split, S.n, S.pair_scratch);
 	k_gather_pairs<<<blocks_for(6*NSC*S.n, 256), 256, 0, st>>>(S.n, NSC, 12*NSC, S.row_ptr, S.col_ptr, S.col_idx,
 	                                                     S.pair_scratch, S.sc);
+	if (S.P.brownian_on) {
+		k_brownian_stress<<<blocks_for(6*S.n, 256), 256, 0, st>>>(6*S.n, in_predictor, S.sc);
+		S.launches++;
+	}
 	k_stress_totals<<<NSC, 256, 0, st>>>(S.n, S.sc, S.sc_tot);
 	S.launches += 3;
 }
@@ -1581,7 +1670,9 @@ static int sc_mask(const DevParams &P)
 		m |= 1 << SC_GU_DASHPOT;
 		m |= 1 << SC_GU_HYDRO;
 		if (P.repulsiveforce) m |= 1 << SC_GU_REPULSION;
+		if (P.brownian_on) m |= 1 << SC_GU_BROWNIAN;
 	}
+	if (P.brownian_on) m |= 1 << SC_BROWNIAN_PRED;
 	if (P.control == 0) m |= 1 << SC_XF_CONTACT;
 	else m |= (1 << SC_XF_RATEPROP) | (1 << SC_XF_RATEINDEP);
 	if (P.repulsiveforce) m |= 1 << SC_XF_REPULSION;

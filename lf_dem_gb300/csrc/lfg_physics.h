@@ -19,7 +19,8 @@ struct DevParams {
 	double system_volume;
 	double skin;
 	double mu_r, kr;                       // rolling friction (Contact.cpp:35-45, 283-305)
-	int friction_model, friction, rolling, repulsiveforce, lub_on, tangential, twodim;
+	double brownian;                       // kT in internal units (0: no Brownian force)
+	int friction_model, friction, rolling, repulsiveforce, lub_on, tangential, twodim, brownian_on;
 	int fixed_dt, control, integration_method, n;
 };
 
@@ -38,7 +39,9 @@ struct DevClock {
 };
 
 // Pair state (one record per superset pair, sorted by (p0, p1)).
-enum { PF_INTER = 1, PF_CONTACT = 2, PF_LUB = 4, PF_DASHPOT = 8 };
+// PF_CHANGED: the contact opened or closed in the predictor's update of a
+// Brownian step (Interaction::contact_state_changed_after_predictor)
+enum { PF_INTER = 1, PF_CONTACT = 2, PF_LUB = 4, PF_DASHPOT = 8, PF_CHANGED = 16 };
 struct DPair {
 	double rvec[3], nvec[3], r, gap;
 	double disp_tan[3], prev_disp_tan[3];
@@ -60,9 +63,17 @@ struct DPairConst {
 };
 
 // Component slots.
-enum { FC_CONTACT = 0, FC_DASHPOT = 1, FC_HYDRO = 2, FC_REPULSION = 3, NFC = 4 };
+// The pair-force components come first (NPFC of them, gathered from the
+// pair scratch); the Brownian force (System::setBrownianForceToParticle) is
+// generated per particle.  Sums over components run in the reference's
+// std::map order: brownian, contact, dashpot, hydro, repulsion.
+enum { FC_CONTACT = 0, FC_DASHPOT = 1, FC_HYDRO = 2, FC_REPULSION = 3, FC_BROWNIAN = 4, NFC = 5 };
+constexpr int NPFC = 4;
 enum { SC_ME = 0, SC_GU_CONTACT, SC_GU_DASHPOT, SC_GU_HYDRO, SC_GU_REPULSION,
-       SC_XF_CONTACT, SC_XF_RATEINDEP, SC_XF_RATEPROP, SC_XF_REPULSION, NSC };
+       SC_XF_CONTACT, SC_XF_RATEINDEP, SC_XF_RATEPROP, SC_XF_REPULSION,
+       SC_GU_BROWNIAN, SC_BROWNIAN_PRED, NSC };
+// GU stress slot of force component c
+__host__ __device__ inline int sc_gu_slot(int c) { return c == FC_BROWNIAN ? SC_GU_BROWNIAN : SC_GU_CONTACT+c; }
 
 struct DevSim {
 	int n = 0;
@@ -117,7 +128,12 @@ double *noalloc_pair_scratch(int device);
 void phys_force_component_into(DevSim &S, int comp, double *scr, double *out, cudaStream_t st);
 // divided = 1: one RHS per component (setSolverRHS); 0: their sum (addToSolverRHS)
 void phys_rhs(DevSim &S, int divided, cudaStream_t st);
-void phys_stresslets(DevSim &S, cudaStream_t st);
+// in_predictor: the Brownian stress of the mid-point scheme (Stress.cpp:270-286)
+void phys_stresslets(DevSim &S, int in_predictor, cudaStream_t st);
+// psi: amp * standard normal deviates (6n), Philox4x32-10 keyed by seed,
+// counter draw (one draw per Brownian force)
+void phys_brownian_psi(DevSim &S, unsigned long long seed, unsigned long long draw, double amp, double *psi,
+                       cudaStream_t st);
 void phys_shear_rate_from_stress(DevSim &S, cudaStream_t st);
 void phys_velocities(DevSim &S, int divided, int in_predictor, cudaStream_t st);
 void phys_adapt_dt(DevSim &S, double time_end, double strain_end, cudaStream_t st);

@@ -47,6 +47,7 @@ public:
 	void timing(lfg_sim_timing *o) const;
 	void set_leaf_size(int leaf) { solver_->reanalyze(leaf); symbolic_runs_++; }
 	void output_snapshot(OutputSnapshot &o);
+	void set_brownian_force(const double *fb);
 	int64_t device_bytes() const;
 	std::vector<double> step_ms;
 	int64_t step_kernels = 0;
@@ -71,6 +72,11 @@ private:
 	int *d_err_ = nullptr, *h_err_ = nullptr;
 	std::vector<double> h_pos_;
 	int symbolic_runs_ = 0;
+	// Brownian force: draws so far, psi work vector, a force given for the
+	// next predictor (set_brownian_force)
+	unsigned long long brownian_draws_ = 0;
+	double *psi_ = nullptr;
+	bool fb_given_ = false;
 	// System::avg_dt: mean dt over the loop steps of the last timeEvolution
 	// (System.cpp:1234-1270); dt itself for a fixed time step (:609-611)
 	double avg_dt_ = 0, avg_dt_sum_ = 0;
@@ -99,6 +105,8 @@ static DevParams make_dev_params(const lfg_params &p, int n, double lx, double l
 	P.kn = p.kn; P.kt = p.kt;
 	P.rolling = p.mu_rolling > 0;
 	P.mu_r = p.mu_rolling; P.kr = p.kr;
+	P.brownian_on = p.brownian > 0;
+	P.brownian = p.brownian;
 	P.critical_load = p.critical_load; P.ft_max = p.ft_max;
 	P.repulsiveforce = p.repulsion_on && p.repulsive_length > 0;
 	P.repulsion = p.repulsion; P.rep_len = p.repulsive_length; P.rep_max_len = p.repulsive_max_length;
@@ -166,6 +174,7 @@ Sim::Sim(const lfg_params &p, const lfg_options &o, int n, const double *pos, co
 	dalloc(S_.vel, 3*n, st_); dalloc(S_.ang, 3*n, st_); dalloc(S_.vel_pred, 3*n, st_); dalloc(S_.ang_pred, 3*n, st_);
 	dalloc(S_.u_inf, 3*n, st_); dalloc(S_.na, 6*n, st_);
 	dalloc(S_.na_disp, 3*n, st_); dalloc(S_.angle, n, st_);
+	if (p.brownian > 0) dalloc(psi_, 6*n, st_);
 	dalloc(S_.vc, (size_t)NFC*6*n, st_); dalloc(S_.fc, (size_t)NFC*6*n, st_);
 	dalloc(S_.rhs, (size_t)NFC*6*n, st_); dalloc(S_.sol, (size_t)NFC*6*n, st_);
 	dalloc(S_.sc, (size_t)NSC*6*n, st_); dalloc(S_.sc_tot, (size_t)NSC*6+12*(size_t)n, st_);
@@ -208,7 +217,7 @@ Sim::~Sim()
 {
 	delete solver_;
 	void *p[] = {S_.clock, S_.pos, S_.radius, S_.vel, S_.ang, S_.vel_pred, S_.ang_pred, S_.u_inf, S_.na, S_.na_disp,
-	             S_.angle, S_.vc,
+	             S_.angle, psi_, S_.vc,
 	             S_.fc, S_.rhs, S_.sol, S_.sc, S_.sc_tot, S_.pairs, S_.pconst, S_.row_ptr, S_.col_ptr, S_.col_idx,
 	             S_.blk_scratch, S_.pair_scratch, S_.cell_of, S_.cell_start, S_.cell_count, S_.cell_list,
 	             S_.cand_count, S_.cand_ptr, S_.cand, d_err_};
@@ -329,19 +338,32 @@ void Sim::compute_velocities(int calc_stress, int in_predictor)
 	stage_end(2);
 	stage_begin(4);
 	phys_force_components(S_, st_);
+	if (S_.P.brownian_on && in_predictor) {
+		// System::setBrownianForceToParticle: F_B = L (sqrt(2 kT/dt) psi) with
+		// the factor of this configuration, drawn in the predictor only (the
+		// corrector keeps it)
+		double *fb = S_.fc+(size_t)FC_BROWNIAN*6*S_.n;
+		if (fb_given_) {
+			fb_given_ = false;
+		} else {
+			phys_brownian_psi(S_, prm_.seed, brownian_draws_++, std::sqrt(2*prm_.brownian/prm_.dt), psi_, st_);
+			solver_->multiply_device(1, psi_, fb);
+		}
+	}
 	phys_rhs(S_, divided, st_);
 	stage_end(4);
 	stage_begin(3);
 	lfg_status st;
 	std::memset(&st, 0, sizeof st);
-	int rc = solver_->solve_device(divided ? NFC : 1, S_.rhs, divided ? S_.vc : S_.sol, &st, false);
+	int nrhs = S_.P.brownian_on ? NFC : NPFC;   // the Brownian component is the last
+	int rc = solver_->solve_device(divided ? nrhs : 1, S_.rhs, divided ? S_.vc : S_.sol, &st, false);
 	// factor and solve status (a non-positive pivot, or a bounded wait that gave up)
 	phys_sticky_status(solver_->d_status(), d_err_, st_);
 	stage_end(3);
 	if (rc == LFG_ERR_NOT_CONVERGED) { error_code = rc; error_msg = st.msg; }
 	stage_begin(4);
 	if (divided && stress_ctl) {
-		phys_stresslets(S_, st_);
+		phys_stresslets(S_, in_predictor, st_);
 		phys_shear_rate_from_stress(S_, st_);
 	}
 	phys_velocities(S_, divided, in_predictor, st_);
@@ -364,11 +386,11 @@ void Sim::step(int calc_stress, double time_end, double strain_end)
 		LFG_CUDA(cudaEventCreate(&step_b_));
 	}
 	LFG_CUDA(cudaEventRecord(step_a_, st_));
-	if (!prm_.fixed_dt) phys_adapt_dt(S_, time_end, strain_end, st_);
+	if (!prm_.fixed_dt && !S_.P.brownian_on) phys_adapt_dt(S_, time_end, strain_end, st_);
 	if (prm_.integration_method == 0) {
 		// System::timeEvolutionEulersMethod + timeStepMove (System.cpp:843-882, 1083-1122)
 		compute_velocities(calc_stress, 1);
-		if (calc_stress) { stage_begin(4); phys_stresslets(S_, st_); stage_end(4); }
+		if (calc_stress) { stage_begin(4); phys_stresslets(S_, 1, st_); stage_end(4); }
 		stage_begin(5);
 		if (!prm_.fixed_dt) phys_adapt_dt(S_, time_end, strain_end, st_);
 		phys_boxing(S_, st_);
@@ -377,9 +399,10 @@ void Sim::step(int calc_stress, double time_end, double strain_end)
 	} else {
 		// predictor (System.cpp:888-930, 1124-1162)
 		compute_velocities(calc_stress, 1);
-		if (calc_stress) { stage_begin(4); phys_stresslets(S_, st_); stage_end(4); }
+		if (calc_stress) { stage_begin(4); phys_stresslets(S_, 1, st_); stage_end(4); }
 		stage_begin(5);
-		if (!prm_.fixed_dt) phys_adapt_dt(S_, time_end, strain_end, st_);
+		// no adaptive time step with Brownian forces (System.cpp:1129, 1243)
+		if (!prm_.fixed_dt && !S_.P.brownian_on) phys_adapt_dt(S_, time_end, strain_end, st_);
 		phys_boxing(S_, st_);
 		phys_move(S_, 1, st_);
 		stage_end(5);
@@ -389,7 +412,7 @@ void Sim::step(int calc_stress, double time_end, double strain_end)
 		phys_save_pred(S_, st_);
 		// corrector (System.cpp:931-983, 1164-1187)
 		compute_velocities(calc_stress, 0);
-		if (calc_stress) { stage_begin(4); phys_stresslets(S_, st_); stage_end(4); }
+		if (calc_stress) { stage_begin(4); phys_stresslets(S_, 0, st_); stage_end(4); }
 		stage_begin(5);
 		phys_move(S_, 2, st_);
 		stage_end(5);
@@ -474,6 +497,15 @@ bool Sim::advance_partial(double time_end, double strain_end, int max_steps)
 	return error_code == 0;
 }
 
+void Sim::set_brownian_force(const double *fb)
+{
+	if (!S_.P.brownian_on) throw Error{LFG_ERR_BAD_ARG, 0, "the simulation has no Brownian force"};
+	LFG_CUDA(cudaMemcpyAsync(S_.fc+(size_t)FC_BROWNIAN*6*S_.n, fb, sizeof(double)*6*S_.n, cudaMemcpyHostToDevice,
+	                         st_));
+	LFG_CUDA(cudaStreamSynchronize(st_));
+	fb_given_ = true;
+}
+
 // The state the output writers read (Simulation::outputData,
 // outputParFileTxt, outputIntFileTxt: Simulation.cpp:641-1006).
 void Sim::output_snapshot(OutputSnapshot &o)
@@ -504,22 +536,25 @@ void Sim::output_snapshot(OutputSnapshot &o)
 	LFG_CUDA(cudaStreamSynchronize(st_));
 	bool has[NSC] = {(bool)P.lub_on, (bool)P.lub_on, (bool)P.lub_on, (bool)P.lub_on,
 	                 P.lub_on && P.repulsiveforce, P.control == 0, P.control == 1, P.control == 1,
-	                 (bool)P.repulsiveforce};
-	const int group[NSC] = {2, 0, 1, 2, 3, 0, 0, 0, 3};
-	double g[4][6] = {{0}};
+	                 (bool)P.repulsiveforce, P.lub_on && P.brownian_on, (bool)P.brownian_on};
+	// groups: 0 contact, 1 dashpot, 2 hydro, 3 repulsion, 4 brownian
+	const int group[NSC] = {2, 0, 1, 2, 3, 0, 0, 0, 3, 4, 4};
+	double g[5][6] = {{0}};
 	for (int c = 0; c < NSC; c++)
 		if (has[c]) for (int e = 0; e < 6; e++) g[group[c]][e] += tot[6*c+e];
-	for (int a = 0; a < 4; a++) for (int e = 0; e < 6; e++) g[a][e] /= P.system_volume;
+	for (int a = 0; a < 5; a++) for (int e = 0; e < 6; e++) g[a][e] /= P.system_volume;
 	for (int e = 0; e < 6; e++) g[2][e] += 2*K.Einf[e]/(6*M_PI);
-	const char *names[4] = {"contact", "dashpot", "hydro", "repulsion"};
-	const bool present[4] = {true, (bool)P.lub_on, true, (bool)P.repulsiveforce};
+	// key order of System::total_stress_groups
+	const char *names[5] = {"brownian", "contact", "dashpot", "hydro", "repulsion"};
+	const int idx[5] = {4, 0, 1, 2, 3};
+	const bool present[5] = {(bool)P.brownian_on, true, (bool)P.lub_on, true, (bool)P.repulsiveforce};
 	o.groups.clear();
 	o.group_stress.clear();
-	for (int a = 0; a < 4; a++) {
+	for (int a = 0; a < 5; a++) {
 		if (!present[a]) continue;
 		o.groups.push_back(names[a]);
 		std::array<double, 6> v;
-		for (int e = 0; e < 6; e++) v[e] = g[a][e];
+		for (int e = 0; e < 6; e++) v[e] = g[idx[a]][e];
 		o.group_stress.push_back(v);
 	}
 	// System::calcStress: total = sum of the groups in key order
@@ -569,15 +604,17 @@ void Sim::scalars(lfg_sim_scalars *o)
 	const DevParams &P = S_.P;
 	bool has[NSC] = {(bool)P.lub_on, (bool)P.lub_on, (bool)P.lub_on, (bool)P.lub_on,
 	                 P.lub_on && P.repulsiveforce, P.control == 0, P.control == 1, P.control == 1,
-	                 (bool)P.repulsiveforce};
-	const int group[NSC] = {2, 0, 1, 2, 3, 0, 0, 0, 3};
-	double g[4][6] = {{0}};
+	                 (bool)P.repulsiveforce, P.lub_on && P.brownian_on, (bool)P.brownian_on};
+	// groups: 0 contact, 1 dashpot, 2 hydro, 3 repulsion, 4 brownian
+	const int group[NSC] = {2, 0, 1, 2, 3, 0, 0, 0, 3, 4, 4};
+	double g[5][6] = {{0}};
 	for (int c = 0; c < NSC; c++)
 		if (has[c]) for (int e = 0; e < 6; e++) g[group[c]][e] += tot[6*c+e];
 	double inv = 1.0/P.system_volume;
-	for (int a = 0; a < 4; a++) for (int e = 0; e < 6; e++) g[a][e] *= inv;
+	for (int a = 0; a < 5; a++) for (int e = 0; e < 6; e++) g[a][e] *= inv;
 	for (int e = 0; e < 6; e++) g[2][e] += 2*K.Einf[e]/(6*M_PI);
-	for (int e = 0; e < 6; e++) o->total_stress[e] = g[0][e]+g[1][e]+g[2][e]+g[3][e];
+	// in the groups' key order (brownian, contact, dashpot, hydro, repulsion)
+	for (int e = 0; e < 6; e++) o->total_stress[e] = g[4][e]+g[0][e]+g[1][e]+g[2][e]+g[3][e];
 	const double *E = K.Einf;
 	double EE = E[0]*E[0]+2*E[1]*E[1]+2*E[2]*E[2]+2*E[3]*E[3]+E[4]*E[4]+E[5]*E[5];
 	if (K.shear_rate != 0 && EE != 0) {
@@ -680,9 +717,9 @@ int Sim::get_pairs(lfg_pair *out, int cap)
 
 int Sim::particle_stress(int comp, double *out)
 {
-	static const int map[8] = {SC_GU_CONTACT, SC_GU_DASHPOT, SC_GU_HYDRO, SC_GU_REPULSION, SC_ME,
-	                           SC_XF_CONTACT, SC_XF_RATEINDEP, SC_XF_REPULSION};
-	if (comp < 0 || comp >= 8) return LFG_ERR_BAD_ARG;
+	static const int map[10] = {SC_GU_CONTACT, SC_GU_DASHPOT, SC_GU_HYDRO, SC_GU_REPULSION, SC_ME,
+	                            SC_XF_CONTACT, SC_XF_RATEINDEP, SC_XF_REPULSION, SC_GU_BROWNIAN, SC_BROWNIAN_PRED};
+	if (comp < 0 || comp >= 10) return LFG_ERR_BAD_ARG;
 	int c = map[comp];
 	if (comp == 5 && S_.P.control == 1) c = SC_XF_RATEPROP;
 	LFG_CUDA(cudaMemcpyAsync(out, S_.sc+(size_t)c*6*S_.n, sizeof(double)*6*S_.n, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
@@ -863,6 +900,9 @@ int lfg_sim_create(const lfg_params *p, const lfg_options *opt, int n, const dou
 	if (!p || !out || n <= 1 || !pos || !radius || lx <= 0 || lz <= 0 || ly < 0 || ncs < 0 ||
 	    (ncs > 0 && (!cs_p0 || !cs_p1 || !cs_disp_tan)))
 		return fail(st, LFG_ERR_BAD_ARG, 0, "bad arguments");
+	if (p->brownian > 0 && (p->integration_method != 1 || p->control != 0))
+		return fail(st, LFG_ERR_BAD_ARG, 0,
+		            "Brownian forces need the predictor-corrector method and rate control (System.cpp:423-436)");
 	lfg_options o;
 	if (opt) o = *opt; else lfg_default_options(&o);
 	int rc = check_device(o.device, st);
@@ -973,6 +1013,15 @@ int lfg_sim_get_particle_stress(lfg_sim *h, int comp, double *out)
 	if (!h || !out) return LFG_ERR_BAD_ARG;
 	SIM_GUARD_BEGIN
 	return h->s->particle_stress(comp, out);
+	SIM_GUARD_END
+}
+
+int lfg_sim_set_brownian_force(lfg_sim *h, const double *fb, lfg_status *st)
+{
+	if (!h || !fb) return fail(st, LFG_ERR_BAD_ARG, 0, "bad arguments");
+	SIM_GUARD_BEGIN
+	h->s->set_brownian_force(fb);
+	return ok(st);
 	SIM_GUARD_END
 }
 

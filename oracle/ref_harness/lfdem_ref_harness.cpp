@@ -229,6 +229,7 @@ int main(int argc, char **argv)
 		put1("init_shear_rate_limit", sys.init_shear_rate_limit);
 		put1("mu_rolling", sys.rolling_friction ? p.mu_rolling : 0.0);
 		put1("kr", sys.rolling_friction ? p.kr : 0.0);
+		put1("brownian", sys.brownian ? p.brownian : 0.0);
 		put1("lx", sys.get_lx()); put1("ly", sys.get_ly()); put1("lz", sys.get_lz());
 		put("radius", sys.radius.data(), sys.radius.size());
 		put_vec3("position0", sys.position);
@@ -280,11 +281,24 @@ int main(int argc, char **argv)
 			dump_components(sys, "stage_");
 			dump_scalars(sys, "stage_");
 		}
-		if (!sys.p.fixed_dt) sys.adaptTimeStep(time_end, strain_end);
+		// System::timeEvolution's loop (System.cpp:1243-1245): no adaptive step
+		// with Brownian forces
+		if (!sys.brownian && !sys.p.fixed_dt) sys.adaptTimeStep(time_end, strain_end);
 		if (sys.p.integration_method == 0) sys.timeEvolutionEulersMethod(calc_stress, time_end, strain_end);
 		else sys.timeEvolutionPredictorCorrectorMethod(calc_stress, time_end, strain_end);
 		dump_scalars(sys, "post_");
 		dump_pairs(sys, "post_");
+		if (sys.brownian) {
+			// the Brownian force of this step (drawn in the predictor, kept for
+			// the corrector: System::setBrownianForceToParticle)
+			const auto &fcb = sys.force_components["brownian"];
+			std::vector<double> fb(6*(size_t)sys.np);
+			for (int i = 0; i < sys.np; i++) {
+				fb[6*i] = fcb.force[i].x; fb[6*i+1] = fcb.force[i].y; fb[6*i+2] = fcb.force[i].z;
+				fb[6*i+3] = fcb.torque[i].x; fb[6*i+4] = fcb.torque[i].y; fb[6*i+5] = fcb.torque[i].z;
+			}
+			put("post_brownian_force", fb.data(), fb.size());
+		}
 		if (calc_stress) {
 			dump_components(sys, "post_");
 			sys.calcStress();

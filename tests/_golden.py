@@ -6,12 +6,16 @@ import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["rate_n200", "stress_n200", "rate_normal_n200", "rate_2d_n200", "rolling_n200"]
+# Brownian runs: the reference draws its Brownian force from a clock-seeded
+# generator; each step's force is recorded and replayed (the CPU oracle has
+# no Brownian path, so these are engine-only)
+BROWNIAN_CASES = ["brownian_n200"]
 PARAM_KEYS = ["kn", "kt", "mu_static", "mu_dynamic", "critical_load", "ft_max", "friction_model", "repulsion_on",
               "repulsion", "repulsive_length", "repulsive_max_length", "lubrication_model", "lub_reduce_parameter",
               "lub_max_gap", "interaction_range", "sd_coeff", "contact_relaxation_time",
               "contact_relaxation_time_tan", "disp_max", "dt", "dt_max", "dt_min", "fixed_dt",
               "integration_method", "control", "shear_rate", "target_stress", "Ehat", "Ohat",
-              "init_strain_shear_rate_limit", "init_shear_rate_limit", "mu_rolling", "kr"]
+              "init_strain_shear_rate_limit", "init_shear_rate_limit", "mu_rolling", "kr", "brownian"]
 
 
 def load(name):

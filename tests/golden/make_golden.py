@@ -71,6 +71,18 @@ mu_static = 1;
 mu_rolling = 0.2;
 time_end = 2h;
 """),
+    # Brownian force at Pe = 1000 (hydro internal units, fixed dt, mid-point
+    # predictor-corrector; System.cpp:888-983, 1665-1710, Stress.cpp:270-286);
+    # the harness records each step's Brownian force
+    "brownian_n200": dict(n=200, vf=0.45, seed=106, control="r", value="1000", suffix="b", steps=6, calc_stress=1,
+                          params="""
+lub_reduce_parameter = 1e-3;
+lub_max_gap = 0.5;
+kn = 1e4h;
+kt = 0.5kn;
+mu_static = 1;
+time_end = 1h;
+"""),
     # 2D monolayer (ly = 0 in the configuration): the reference's twodimension path
     "rate_2d_n200": dict(n=200, vf=0.7, seed=104, control="r", value="1", suffix="r", steps=4, calc_stress=1,
                          twodim=True, params="""
@@ -107,7 +119,7 @@ def run_case(name, c, workdir):
                 "pre_max_velocity", "pre_max_sliding_velocity", "pre_pairs_i", "pre_pairs_d"}
     keep_post = {"post_position", "post_velocity", "post_ang_velocity", "post_na_velocity", "post_shear_rate",
                  "post_dt", "post_strain", "post_time", "post_shear_disp", "post_pairs_i", "post_pairs_d",
-                 "post_total_stress", "post_max_velocity", "post_max_sliding_velocity"}
+                 "post_total_stress", "post_max_velocity", "post_max_sliding_velocity", "post_brownian_force"}
     for k in range(c["steps"]):
         R = read_records(os.path.join(out, f"step_{k:04d}.bin"))
         last = k == c["steps"]-1

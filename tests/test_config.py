@@ -20,7 +20,7 @@ def E():
     return E
 
 
-@pytest.mark.parametrize("name", G.CASES)
+@pytest.mark.parametrize("name", G.CASES+G.BROWNIAN_CASES)
 def test_resolved_parameters_match_reference(E, name):
     F = G.load(name)
     text = bytes(F["param_file"]).decode()

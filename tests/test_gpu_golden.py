@@ -57,3 +57,38 @@ def test_steps_match_reference(engine, name, precision, tol):
         ts = F[f"s{k}_post_total_stress"]
         assert np.abs(s["total_stress"] - ts).max() <= tol * np.abs(ts).max(), k
         g.close()
+
+
+@pytest.mark.parametrize("name", G.BROWNIAN_CASES)
+@pytest.mark.parametrize("precision,tol", [(0, 1e-9), (1, 1e-8)], ids=["fp64", "fp32refine"])
+def test_brownian_steps_match_reference(engine, name, precision, tol):
+    """Mid-point (predictor-corrector) steps with the Brownian force the
+    reference drew for that step (System::timeEvolutionPredictorCorrectorMethod,
+    System.cpp:888-983; the force is reused in the corrector; fixed dt; the
+    Banchio-Brady stress of Stress.cpp:270-286)."""
+    F = G.load(name)
+    skip = G.removal_steps(F)
+    assert len(skip) < int(F["nsteps"][0]) - 2, "too few steps without an interaction removal"
+    for k in range(int(F["nsteps"][0])):
+        g = _make(engine, F, k, precision)
+        g.set_brownian_force(F[f"s{k}_post_brownian_force"])
+        g.step(calc_stress=True)
+        pi, _ = G.pairs(F, k, "post")
+        pg = g.pairs()
+        assert np.array_equal(np.stack([pg["p0"], pg["p1"]], 1), pi[:, :2]), k
+        if k in skip:
+            continue   # the reference's swap-removal side effect (see _golden.removal_steps)
+        assert np.array_equal(pg["contact_active"], pi[:, 2]), k
+        s = g.scalars()
+        for key in ("dt", "strain"):
+            ref = float(F[f"s{k}_post_{key}"][0])
+            assert abs(s[key] - ref) <= tol * abs(ref), (k, key)
+        p = g.particles()
+        for ours, theirs in (("pos", "position"), ("vel", "velocity"), ("ang", "ang_velocity"),
+                             ("na_vel", "na_velocity")):
+            ref = F[f"s{k}_post_{theirs}"].reshape(-1, 3)
+            err = np.abs(p[ours] - ref).max() / np.abs(ref).max()
+            assert err <= tol, (k, ours, err)
+        ts = F[f"s{k}_post_total_stress"]
+        assert np.abs(s["total_stress"] - ts).max() <= tol * np.abs(ts).max(), k
+        g.close()
