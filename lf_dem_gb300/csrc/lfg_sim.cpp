@@ -339,9 +339,9 @@ void Sim::compute_velocities(int calc_stress, int in_predictor)
 	stage_begin(4);
 	phys_force_components(S_, st_);
 	if (S_.P.brownian_on && in_predictor) {
-		// System::setBrownianForceToParticle: F_B = L (sqrt(2 kT/dt) psi) with
-		// the factor of this configuration, drawn in the predictor only (the
-		// corrector keeps it)
+		// System::setBrownianForceToParticle (System.cpp:1665-1710): F_B =
+		// L (sqrt(2 kT/dt) psi) with the factor of this configuration, drawn
+		// in the predictor only (the corrector keeps it)
 		double *fb = S_.fc+(size_t)FC_BROWNIAN*6*S_.n;
 		if (fb_given_) {
 			fb_given_ = false;
