@@ -1172,6 +1172,17 @@ template <typename T> void factor_alloc(DevFactor<T> &F, const DevSymbolic &D, i
 		LFG_CUDA(cudaMalloc((void **)&F.part, sizeof(T)*pneed));
 		F.part_cap = pneed;
 	}
+	int64_t tneed = 1;
+	for (const auto *tab : {&D.h_solve_phases, &D.h_mul_phases})
+		for (const SolvePhase &p : *tab)
+			if (p.nchunk > 1) tneed = std::max<int64_t>(tneed, (int64_t)p.gx*p.gy);
+	if (F.tally_cap < tneed) {
+		if (F.tally) cudaFree(F.tally);
+		F.tally = nullptr;
+		LFG_CUDA(cudaMalloc((void **)&F.tally, sizeof(int)*tneed));
+		LFG_CUDA(cudaMemset(F.tally, 0, sizeof(int)*tneed));
+		F.tally_cap = tneed;
+	}
 	if (!F.status) LFG_CUDA(cudaMalloc((void **)&F.status, sizeof(int)*4));
 	set_update_smem<T>();
 	set_assemble_smem<T>(D);
@@ -1186,6 +1197,7 @@ template <typename T> void factor_free(DevFactor<T> &F)
 	if (F.status) cudaFree(F.status);
 	if (F.linv) cudaFree(F.linv);
 	if (F.part) cudaFree(F.part);
+	if (F.tally) cudaFree(F.tally);
 	F = DevFactor<T>();
 }
 
@@ -1264,8 +1276,9 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 // sweep; each runs as one launch of k_solve_phase with one CTA per work
 // unit.  Column products take SOLVE_CB columns per unit (8 warps split the
 // rows), row products 32 rows x SOLVE_JC columns (lanes own rows, warps
-// split the columns).  Every sum runs in a fixed order: results are bitwise
-// reproducible.  (One persistent kernel with grid barriers between phases
+// split the columns; the last chunk of a row block to finish, found with a
+// per-block counter, adds the chunks' partial sums).  Every sum runs in a
+// fixed order: results are bitwise reproducible.  (One persistent kernel with grid barriers between phases
 // was measured slower: the barriers cost more than the launch gaps.)
 
 // Solve phases read their indices and factor entries (constant during a
@@ -1277,6 +1290,7 @@ template <typename T> struct SolveArgs {
 	const int *child_off, *children, *cinv, *iperm;
 	const T *arena;
 	T *w, *xp, *yp, *part;
+	int *tally;
 	int64_t wstride, pstride;
 	int n, n6tot;
 	const double *b;
@@ -1286,6 +1300,7 @@ template <typename T> struct SolveArgs {
 template <typename T> struct SolveShared {
 	T red_c[SOLVE_WARPS][SOLVE_CB][4];
 	T red_r[SOLVE_WARPS][4][32];
+	int last;
 };
 
 template <typename T, int K>
@@ -1321,9 +1336,16 @@ __device__ void unit_gather(const SolveArgs<T> &A, const int *lev, int bx, int b
 }
 
 // MODE 0: y_j = sum_{i <= j} E[i][j] x_i;  MODE 1: z_j -= sum_t L21[t][j] x[rows(t)]
+// The row loop takes SolveUnroll<T>::U rows of a thread per batch: all their loads are
+// issued before the first multiply-add (the phases are latency-bound, one
+// round trip per batch instead of per row); each thread still adds its rows
+// in increasing order.
+template <typename T> struct SolveUnroll { static constexpr int U = sizeof(T) == 4 ? 4 : 2; };
+
 template <typename T, int K, int MODE>
 __device__ void unit_cols(const SolveArgs<T> &A, const int *lev, int bx, int by, SolveShared<T> &sh)
 {
+	constexpr int U = SolveUnroll<T>::U;
 	int s = lev[by];
 	int n6 = 6*A.sn_n[s], m6 = 6*A.sn_m[s], ld = A.sn_ld[s];
 	int j0 = bx*SOLVE_CB;
@@ -1339,17 +1361,33 @@ __device__ void unit_cols(const SolveArgs<T> &A, const int *lev, int bx, int by,
 	for (int c = 0; c < SOLVE_CB; c++)
 #pragma unroll
 		for (int q = 0; q < K; q++) acc[c][q] = 0;
-	for (int i = threadIdx.x; i < nrow; i += blockDim.x) {
-		int64_t g = MODE == 0 ? f6+i : 6*R[i/6]+i%6;
-		T v[K];
+	for (int i0 = threadIdx.x; i0 < nrow; i0 += U*blockDim.x) {
+		int64_t g[U];
 #pragma unroll
-		for (int q = 0; q < K; q++) v[q] = A.xp[(int64_t)q*A.n6tot+g];
+		for (int u = 0; u < U; u++) {
+			int i = i0+u*blockDim.x;
+			g[u] = i >= nrow ? -1 : MODE == 0 ? f6+i : 6*R[i/6]+i%6;
+		}
+		T v[U][K], e[U][SOLVE_CB];
 #pragma unroll
-		for (int c = 0; c < SOLVE_CB; c++) {
-			if (c >= jn || (MODE == 0 && i > j0+c)) continue;
-			T e = __ldg(&M[(int64_t)c*ld+i]);
+		for (int u = 0; u < U; u++) {
+			int i = i0+u*blockDim.x;
 #pragma unroll
-			for (int q = 0; q < K; q++) acc[c][q] += e*v[q];
+			for (int q = 0; q < K; q++) v[u][q] = g[u] < 0 ? T(0) : A.xp[(int64_t)q*A.n6tot+g[u]];
+#pragma unroll
+			for (int c = 0; c < SOLVE_CB; c++)
+				e[u][c] = (g[u] < 0 || c >= jn || (MODE == 0 && i > j0+c)) ? T(0) : __ldg(&M[(int64_t)c*ld+i]);
+		}
+#pragma unroll
+		for (int u = 0; u < U; u++) {
+			if (g[u] < 0) continue;
+			int i = i0+u*blockDim.x;
+#pragma unroll
+			for (int c = 0; c < SOLVE_CB; c++) {
+				if (c >= jn || (MODE == 0 && i > j0+c)) continue;
+#pragma unroll
+				for (int q = 0; q < K; q++) acc[c][q] += e[u][c]*v[u][q];
+			}
 		}
 	}
 	int warp = threadIdx.x/32, lane = threadIdx.x%32;
@@ -1372,6 +1410,16 @@ __device__ void unit_cols(const SolveArgs<T> &A, const int *lev, int bx, int by,
 			else *o -= a;
 		}
 	}
+}
+
+// a row product's result for row `row` of right-hand side q
+template <typename T, int MODE>
+__device__ inline void rows_apply(const SolveArgs<T> &A, int q, int64_t row, T a)
+{
+	if (MODE == 0) A.w[q*A.wstride+row] -= a;
+	else if (MODE == 3) A.w[q*A.wstride+row] += a;
+	else if (MODE == 2) A.xp[(int64_t)q*A.n6tot+row] += a;
+	else A.xp[(int64_t)q*A.n6tot+row] = a;
 }
 
 // MODE 0: w_t -= sum_j L21[t][j] y_j;  MODE 1: x_i = sum_{j >= i} E[i][j] z_j
@@ -1398,12 +1446,26 @@ __device__ void unit_rows(const SolveArgs<T> &A, const int *lev, int bx, int by,
 #pragma unroll
 	for (int q = 0; q < K; q++) acc[q] = 0;
 	if (r < nrows) {
-		for (int j = jlo+warp; j < jhi; j += SOLVE_WARPS) {
-			if (MODE == 1 && j < r) continue;
-			if (MODE == 2 && j > r) continue;
-			T e = __ldg(&M[(int64_t)j*ld+r]);
+		// RU columns of a warp per batch, loads first (see unit_cols)
+		constexpr int RU = 2*SolveUnroll<T>::U;
+		for (int j0 = jlo+warp; j0 < jhi; j0 += RU*SOLVE_WARPS) {
+			T e[RU], y[RU][K];
 #pragma unroll
-			for (int q = 0; q < K; q++) acc[q] += e*A.yp[(int64_t)q*A.n6tot+f6+j];
+			for (int u = 0; u < RU; u++) {
+				// unmasked by the triangle: column j < n6 of a front is
+				// allocated down to its last row (the masked product skips it)
+				int j = j0+u*SOLVE_WARPS;
+				e[u] = j < jhi ? __ldg(&M[(int64_t)j*ld+r]) : T(0);
+#pragma unroll
+				for (int q = 0; q < K; q++) y[u][q] = j < jhi ? A.yp[(int64_t)q*A.n6tot+f6+j] : T(0);
+			}
+#pragma unroll
+			for (int u = 0; u < RU; u++) {
+				int j = j0+u*SOLVE_WARPS;
+				if (j >= jhi || (MODE == 1 && j < r) || (MODE == 2 && j > r)) continue;
+#pragma unroll
+				for (int q = 0; q < K; q++) acc[q] += e[u]*y[u][q];
+			}
 		}
 	}
 #pragma unroll
@@ -1415,37 +1477,31 @@ __device__ void unit_rows(const SolveArgs<T> &A, const int *lev, int bx, int by,
 		for (int q = 0; q < K; q++) {
 			T a = 0;
 			for (int u = 0; u < SOLVE_WARPS; u++) a += sh.red_r[u][q][lane];
-			if (nchunk == 1) {
-				if (MODE == 0) A.w[q*A.wstride+row] -= a;
-				else if (MODE == 3) A.w[q*A.wstride+row] += a;
-				else if (MODE == 2) A.xp[(int64_t)q*A.n6tot+row] += a;
-				else A.xp[(int64_t)q*A.n6tot+row] = a;
-			} else {
-				A.part[((int64_t)q*nchunk+bz)*A.pstride+row] = a;
-			}
+			if (nchunk == 1) rows_apply<T, MODE>(A, q, row, a);
+			else A.part[((int64_t)q*nchunk+bz)*A.pstride+row] = a;
 		}
 	}
-}
-
-template <typename T, int K, int MODE>
-__device__ void unit_rowsum(const SolveArgs<T> &A, const int *lev, int bx, int by, int nchunk)
-{
-	constexpr bool UPD = MODE == 0 || MODE == 3;
-	int s = lev[by];
-	int nrows = UPD ? 6*A.sn_m[s] : 6*A.sn_n[s];
-	int r = bx*blockDim.x+threadIdx.x;
-	if (r >= nrows) return;
-	int64_t row = UPD ? A.sn_woff[s]+r : 6*(int64_t)A.sn_first[s]+r;
-	pdl_wait();
+	if (nchunk == 1) return;
+	// The chunk that completes this row block adds the chunks' partial sums
+	// in chunk order (the same sum a separate launch would form).  The
+	// fence orders each chunk's partial stores before its count.
+	__threadfence();
+	__syncthreads();
+	int *cnt = A.tally+(int64_t)by*gridDim.x+bx;
+	if (threadIdx.x == 0) sh.last = atomicAdd(cnt, 1) == nchunk-1;
+	__syncthreads();
+	if (!sh.last) return;
+	__threadfence();
+	if (warp == 0 && r < nrows) {
+		int64_t row = UPD ? A.sn_woff[s]+r : (int64_t)f6+r;
 #pragma unroll
-	for (int q = 0; q < K; q++) {
-		T a = 0;
-		for (int c = 0; c < nchunk; c++) a += A.part[((int64_t)q*nchunk+c)*A.pstride+row];
-		if (MODE == 0) A.w[q*A.wstride+row] -= a;
-		else if (MODE == 3) A.w[q*A.wstride+row] += a;
-		else if (MODE == 2) A.xp[(int64_t)q*A.n6tot+row] += a;
-		else A.xp[(int64_t)q*A.n6tot+row] = a;
+		for (int q = 0; q < K; q++) {
+			T a = 0;
+			for (int c = 0; c < nchunk; c++) a += __ldcg(&A.part[((int64_t)q*nchunk+c)*A.pstride+row]);
+			rows_apply<T, MODE>(A, q, row, a);
+		}
 	}
+	if (threadIdx.x == 0) *cnt = 0;   // ready for the next row-product phase
 }
 
 // in: b (permuted) into xp; in_y (product with L): b into yp and xp zeroed;
@@ -1482,16 +1538,12 @@ __global__ void __launch_bounds__(256) k_solve_phase(SolveArgs<T> A, SolvePhase 
 	if (TYPE == SP_GATHER) unit_gather<T, K>(A, lev, bx, by);
 	if (TYPE == SP_COLS0) unit_cols<T, K, 0>(A, lev, bx, by, sh);
 	if (TYPE == SP_ROWS0) unit_rows<T, K, 0>(A, lev, bx, by, bz, ph.nchunk, sh);
-	if (TYPE == SP_ROWSUM0) unit_rowsum<T, K, 0>(A, lev, bx, by, ph.nchunk);
 	if (TYPE == SP_COLS1) unit_cols<T, K, 1>(A, lev, bx, by, sh);
 	if (TYPE == SP_ROWS1) unit_rows<T, K, 1>(A, lev, bx, by, bz, ph.nchunk, sh);
-	if (TYPE == SP_ROWSUM1) unit_rowsum<T, K, 1>(A, lev, bx, by, ph.nchunk);
 	if (TYPE == SP_PERM_OUT) unit_permute<T, K>(A, bx, false);
 	if (TYPE == SP_PERM_IN_Y) unit_permute<T, K>(A, bx, true, true);
 	if (TYPE == SP_MUL_TOP) unit_rows<T, K, 2>(A, lev, bx, by, bz, ph.nchunk, sh);
-	if (TYPE == SP_MUL_TOPSUM) unit_rowsum<T, K, 2>(A, lev, bx, by, ph.nchunk);
 	if (TYPE == SP_MUL_UPD) unit_rows<T, K, 3>(A, lev, bx, by, bz, ph.nchunk, sh);
-	if (TYPE == SP_MUL_UPDSUM) unit_rowsum<T, K, 3>(A, lev, bx, by, ph.nchunk);
 }
 
 template <typename T, int K>
@@ -1503,15 +1555,11 @@ static void launch_phase(const SolveArgs<T> &A, const SolvePhase &p, cudaStream_
 	case SP_GATHER: launch_pdl(k_solve_phase<T, K, SP_GATHER>, g, 256, 0, st, A, p); break;
 	case SP_COLS0: launch_pdl(k_solve_phase<T, K, SP_COLS0>, g, 256, 0, st, A, p); break;
 	case SP_ROWS0: launch_pdl(k_solve_phase<T, K, SP_ROWS0>, g, 256, 0, st, A, p); break;
-	case SP_ROWSUM0: launch_pdl(k_solve_phase<T, K, SP_ROWSUM0>, g, 256, 0, st, A, p); break;
 	case SP_COLS1: launch_pdl(k_solve_phase<T, K, SP_COLS1>, g, 256, 0, st, A, p); break;
 	case SP_ROWS1: launch_pdl(k_solve_phase<T, K, SP_ROWS1>, g, 256, 0, st, A, p); break;
-	case SP_ROWSUM1: launch_pdl(k_solve_phase<T, K, SP_ROWSUM1>, g, 256, 0, st, A, p); break;
 	case SP_PERM_IN_Y: launch_pdl(k_solve_phase<T, K, SP_PERM_IN_Y>, g, 256, 0, st, A, p); break;
 	case SP_MUL_TOP: launch_pdl(k_solve_phase<T, K, SP_MUL_TOP>, g, 256, 0, st, A, p); break;
-	case SP_MUL_TOPSUM: launch_pdl(k_solve_phase<T, K, SP_MUL_TOPSUM>, g, 256, 0, st, A, p); break;
 	case SP_MUL_UPD: launch_pdl(k_solve_phase<T, K, SP_MUL_UPD>, g, 256, 0, st, A, p); break;
-	case SP_MUL_UPDSUM: launch_pdl(k_solve_phase<T, K, SP_MUL_UPDSUM>, g, 256, 0, st, A, p); break;
 	default: launch_pdl(k_solve_phase<T, K, SP_PERM_OUT>, g, 256, 0, st, A, p); break;
 	}
 }
@@ -1535,7 +1583,6 @@ void solve_plan_build(DevSymbolic &D, cudaStream_t st)
 		if (m6 > 0) {
 			int nch = (n6+SOLVE_JC-1)/SOLVE_JC;
 			add(SP_ROWS0, off, (m6+31)/32, cnt, nch, nch);
-			if (nch > 1) add(SP_ROWSUM0, off, (m6+255)/256, cnt, 1, nch);
 		}
 	}
 	for (int l = D.nlevels-1; l >= 0; l--) {
@@ -1545,7 +1592,6 @@ void solve_plan_build(DevSymbolic &D, cudaStream_t st)
 		if (m6 > 0) add(SP_COLS1, off, (n6+SOLVE_CB-1)/SOLVE_CB, cnt, 1, 1);
 		int nch = (n6+SOLVE_JC-1)/SOLVE_JC;
 		add(SP_ROWS1, off, (n6+31)/32, cnt, nch, nch);
-		if (nch > 1) add(SP_ROWSUM1, off, (n6+255)/256, cnt, 1, nch);
 	}
 	add(SP_PERM_OUT, 0, (6*n+255)/256, 1, 1, 1);
 	D.h_solve_phases = P;
@@ -1561,10 +1607,8 @@ void solve_plan_build(DevSymbolic &D, cudaStream_t st)
 		int nch = (n6+SOLVE_JC-1)/SOLVE_JC;
 		add(SP_GATHER, off, (n6+m6+255)/256, cnt, 1, 1);
 		add(SP_MUL_TOP, off, (n6+31)/32, cnt, nch, nch);
-		if (nch > 1) add(SP_MUL_TOPSUM, off, (n6+255)/256, cnt, 1, nch);
 		if (m6 > 0) {
 			add(SP_MUL_UPD, off, (m6+31)/32, cnt, nch, nch);
-			if (nch > 1) add(SP_MUL_UPDSUM, off, (m6+255)/256, cnt, 1, nch);
 		}
 	}
 	add(SP_PERM_OUT, 0, (6*n+255)/256, 1, 1, 1);
@@ -1581,7 +1625,7 @@ static int solve_k(DevFactor<T> &F, const DevSymbolic &D, const std::vector<Solv
 	A.lev_sn = D.level_sn; A.sn_first = D.sn_first; A.sn_n = D.sn_n; A.sn_m = D.sn_m; A.sn_ld = D.sn_ld;
 	A.sn_rows_off = D.sn_rows_off; A.rows = D.rows; A.sn_off = D.sn_off; A.sn_woff = D.sn_woff;
 	A.cinv_off = D.cinv_off; A.child_off = D.child_off; A.children = D.children; A.cinv = D.cinv;
-	A.iperm = D.iperm; A.arena = F.arena; A.w = F.w; A.xp = F.xp; A.yp = F.yp; A.part = F.part;
+	A.iperm = D.iperm; A.arena = F.arena; A.w = F.w; A.xp = F.xp; A.yp = F.yp; A.part = F.part; A.tally = F.tally;
 	A.wstride = D.w_elems; A.pstride = F.pstride; A.n = D.nblk; A.n6tot = 6*D.nblk; A.b = b; A.x = x;
 	for (const SolvePhase &p : phases) launch_phase<T, K>(A, p, st);
 	LFG_CUDA(cudaGetLastError());

@@ -83,8 +83,8 @@ void symbolic_analyze(Symbolic &S, int nblk, int nb, const int32_t *od_row,
 // ---------------------------------------------------------------------------
 // One phase of a solve sweep: gx x gy x gz work units of one type over the
 // supernodes level_sn[lev_off ...] of one level (gy of them).
-enum { SP_PERM_IN, SP_GATHER, SP_COLS0, SP_ROWS0, SP_ROWSUM0, SP_COLS1, SP_ROWS1, SP_ROWSUM1, SP_PERM_OUT,
-       SP_PERM_IN_Y, SP_MUL_TOP, SP_MUL_TOPSUM, SP_MUL_UPD, SP_MUL_UPDSUM };
+enum { SP_PERM_IN, SP_GATHER, SP_COLS0, SP_ROWS0, SP_COLS1, SP_ROWS1, SP_PERM_OUT, SP_PERM_IN_Y, SP_MUL_TOP,
+       SP_MUL_UPD };
 struct SolvePhase { int type, lev_off, gx, gy, gz, nchunk; };
 
 struct DevSymbolic {
@@ -141,8 +141,9 @@ template <typename T> struct DevFactor {
 	T *xp = nullptr, *yp = nullptr; // permuted solve workspaces (k * 6n)
 	T *linv = nullptr;    // per supernode: Linv^T of its current panel's diagonal block
 	T *part = nullptr;    // solve: partial row sums per column chunk
+	int *tally = nullptr; // solve: chunks done per row block of a row-product phase (0 between phases)
 	int64_t pstride = 0;
-	int64_t arena_cap = 0, w_cap = 0, x_cap = 0, linv_cap = 0, part_cap = 0;
+	int64_t arena_cap = 0, w_cap = 0, x_cap = 0, linv_cap = 0, part_cap = 0, tally_cap = 0;
 	int *status = nullptr; // device: first non-positive pivot column + 1; 0 = a bounded wait gave up;
 	                       // 0x7fffffff = ok
 };
