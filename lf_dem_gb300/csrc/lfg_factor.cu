@@ -239,16 +239,22 @@ __global__ void k_scatter_od(int count, const int *__restrict__ list, const doub
 constexpr unsigned FULL_MASK = 0xffffffffu;
 
 // Warp routines on 32 x 32 blocks in shared memory (row-major, stride ld),
-// one row or column per lane in registers.  The step loops are not unrolled
-// (the code stays small: it runs once per launch, so a fully unrolled body
-// would be fetched cold every time); register indices stay static because
-// every step shifts the lane's values down by one, so the current column is
-// always element 0.  Pivots use rsqrt and the triangular solves reciprocals
-// of the diagonal (shuffled from the lane that owns it).
+// one row or column per lane in registers.  The step loops are not fully
+// unrolled (the code stays small: it runs once per launch, so a fully
+// unrolled body would be fetched cold every time); register indices stay
+// static because every step shifts the lane's values down by one, so the
+// current column is always element 0.
 //
-// Lsh (32 x 32, 16-byte aligned): Lsh[32 j + q] = L[j + q][j] (zero past the
-// block), column j of L from the diagonal down, written by warp_potrf32 and
-// read by the solves with vector loads.
+// Lsh (32 x 32, 16-byte aligned): Lsh[32 j + q] = L[j + q][j] for q >= 1
+// (zero past the block) and Lsh[32 j] = 1 / L[j][j] (the pivot's rsqrt),
+// column j of L from the diagonal down, written by warp_potrf32 and read by
+// the solves with vector loads.
+//
+// The steps are latency chains; each routine keeps only what the next step
+// needs on the chain: warp_potrf32 takes the next pivot's row entry by
+// shuffle and starts the next pivot's shuffle before the column arrives
+// through Lsh; the solves take the reciprocal from Lsh (no shuffle, no
+// division) and load two columns per iteration ahead of their updates.
 
 // the 32 entries Lsh[32 j + q], q < 32
 template <typename T> __device__ inline void lsh_column(const T *Lsh, int j, T (&c)[32])
@@ -278,65 +284,86 @@ __device__ void warp_potrf32(T *S, int ld, T *Lsh, int lane, int jlim, int gcol0
 	T a[32];   // at step j: a[q] = S[lane][j + q]
 #pragma unroll
 	for (int l = 0; l < 32; l++) a[l] = S[lane*ld+l];
+	T djj = __shfl_sync(FULL_MASK, a[0], 0);
+	if (!(djj > T(0))) {
+		if (lane == 0 && jlim > 0 && fail) atomicMin(fail, gcol0+1);
+		djj = T(1);
+	}
+	T rs = rsqrt(djj);
 #pragma unroll 1
 	for (int j = 0; j < 32; j++) {
-		T djj = __shfl_sync(FULL_MASK, a[0], j);
-		if (!(djj > T(0))) {
-			if (lane == 0 && j < jlim && fail) atomicMin(fail, gcol0+j+1);
-			djj = T(1);
-		}
-		T rs = rsqrt(djj);
 		T lij = a[0]*rs;
-		T v = lane > j ? lij : (lane == j ? djj*rs : T(0));
-		S[lane*ld+j] = v;
-		Lsh[32*j+((lane-j) & 31)] = lane >= j ? v : T(0);
+		S[lane*ld+j] = lane > j ? lij : (lane == j ? djj*rs : T(0));
+		Lsh[32*j+((lane-j) & 31)] = lane > j ? lij : (lane == j ? rs : T(0));
 		__syncwarp();
 		T c[32];
-		lsh_column<T>(Lsh, j, c);
+		lsh_column<T>(Lsh, j, c);   // in flight during the next pivot's chain
+		// the next pivot (its entry of column j by shuffle, its check and
+		// rsqrt) ahead of this column's updates
+		T a0 = a[1]-lij*__shfl_sync(FULL_MASK, lij, (j+1) & 31);
+		T dn = __shfl_sync(FULL_MASK, a0, (j+1) & 31);
+		bool bad = !(dn > T(0));
+		if (bad && lane == 0 && j+1 < 32 && j+1 < jlim && fail) atomicMin(fail, gcol0+j+2);
+		dn = bad ? T(1) : dn;
+		T rsn = rsqrt(dn);
+		a[0] = a0;
 #pragma unroll
-		for (int q = 1; q < 32; q++) a[q-1] = a[q]-lij*c[q];   // entries past the block are dead
+		for (int q = 2; q < 32; q++) a[q-1] = a[q]-lij*c[q];   // entries past the block are dead
+		djj = dn;
+		rs = rsn;
 	}
 	__syncwarp();
 }
 
-// X L^T = A for 32 rows (lane = row) of X (stride ldx), L lower (stride ldl,
-// columns in Lsh); X replaces A
+// X L^T = A for 32 rows (lane = row) of X (stride ldx), L lower given by its
+// columns in Lsh; X replaces A.  Columns alternate between two register
+// buffers, each loaded one step before its use.
 template <typename T>
-__device__ void warp_trsm32(T *X, int ldx, const T *L, int ldl, const T *Lsh, int lane)
+__device__ void warp_trsm32(T *X, int ldx, const T *Lsh, int lane)
 {
-	T rd = T(1)/L[lane*ldl+lane];
 	T x[32];   // at step t: x[q] = X[lane][t + q]
 #pragma unroll
 	for (int l = 0; l < 32; l++) x[l] = X[lane*ldx+l];
+	T c[32], d[32];
+	lsh_column<T>(Lsh, 0, c);
 #pragma unroll 1
-	for (int t = 0; t < 32; t++) {
-		T xt = x[0]*__shfl_sync(FULL_MASK, rd, t);
+	for (int t = 0; t < 32; t += 2) {
+		lsh_column<T>(Lsh, t+1, d);
+		T xt = x[0]*c[0];
 		X[lane*ldx+t] = xt;
-		T c[32];
-		lsh_column<T>(Lsh, t, c);
 #pragma unroll
 		for (int q = 1; q < 32; q++) x[q-1] = x[q]-xt*c[q];
+		lsh_column<T>(Lsh, (t+2) & 31, c);   // after the last pair: column 0 again, unused
+		xt = x[0]*d[0];
+		X[lane*ldx+t+1] = xt;
+#pragma unroll
+		for (int q = 1; q < 32; q++) x[q-1] = x[q]-xt*d[q];
 	}
 	__syncwarp();
 }
 
 // V = L^-1 (lower; lane = column), V row-major with stride ldv; L's columns
-// in Lsh
+// in Lsh (loaded as in warp_trsm32)
 template <typename T>
-__device__ void warp_trtri32(const T *L, int ldl, const T *Lsh, T *V, int ldv, int lane)
+__device__ void warp_trtri32(const T *Lsh, T *V, int ldv, int lane)
 {
-	T rd = T(1)/L[lane*ldl+lane];
 	T y[32];   // at step t: y[q] = V[t + q][lane]
 #pragma unroll
 	for (int i = 0; i < 32; i++) y[i] = (i == lane) ? T(1) : T(0);
+	T c[32], d[32];
+	lsh_column<T>(Lsh, 0, c);
 #pragma unroll 1
-	for (int t = 0; t < 32; t++) {
-		T yt = y[0]*__shfl_sync(FULL_MASK, rd, t);
+	for (int t = 0; t < 32; t += 2) {
+		lsh_column<T>(Lsh, t+1, d);
+		T yt = y[0]*c[0];
 		V[t*ldv+lane] = yt;
-		T c[32];
-		lsh_column<T>(Lsh, t, c);
 #pragma unroll
 		for (int q = 1; q < 32; q++) y[q-1] = y[q]-c[q]*yt;
+		lsh_column<T>(Lsh, (t+2) & 31, c);
+		yt = y[0]*d[0];
+		V[(t+1)*ldv+lane] = yt;
+#pragma unroll
+		for (int q = 1; q < 32; q++) y[q-1] = y[q]-d[q]*yt;
 	}
 	__syncwarp();
 }
@@ -413,12 +440,12 @@ __device__ void warp_trtri32_unrolled(const T *L, int ldl, T *V, int ldv, int la
 
 
 // c8[q] = sum_{t < 32} A[i][t] B[t][c] for row i = tid / 4 and columns
-// c = tid % 4 + 4q (128 threads cover a 32 x 32 product); B[t][c] is read at
-// B[t*ldb_t + c*ldb_c]
+// c = tid % 4 + 4q (128 threads, tid < 128, cover a 32 x 32 product);
+// B[t][c] is read at B[t*ldb_t + c*ldb_c]
 template <typename T>
-__device__ void cta_gemm32(T (&c8)[8], const T *A, int lda, const T *B, int ldb_t, int ldb_c)
+__device__ void cta_gemm32(T (&c8)[8], const T *A, int lda, const T *B, int ldb_t, int ldb_c, int tid)
 {
-	int i = threadIdx.x/4, c0 = threadIdx.x%4;
+	int i = tid/4, c0 = tid%4;
 #pragma unroll
 	for (int q = 0; q < 8; q++) c8[q] = T(0);
 #pragma unroll 8
@@ -480,19 +507,33 @@ __device__ void diag_factor(T *base, int ld, int p0, int w, int gcol0, int *fail
 	__syncthreads();
 	if (warp == 0) {                                                                   // Linv11
 		if constexpr (unrolled) warp_trtri32_unrolled<T>(Ls, LD, Vs, LD, lane);
-		else warp_trtri32<T>(Ls, LD, Lsh, Vs, LD, lane);
+		else warp_trtri32<T>(Lsh, Vs, LD, lane);
 	} else if (NB == 64 && warp == 1) {                                                // L21 = A21 L11^-T
 		if constexpr (unrolled) warp_trsm32_unrolled<T>(Ls+32*LD, LD, Ls, LD, lane);
-		else warp_trsm32<T>(Ls+32*LD, LD, Ls, LD, Lsh, lane);
+		else warp_trsm32<T>(Ls+32*LD, LD, Lsh, lane);
 	}
 	__syncthreads();
 	if (NB == 64) {
 		bool act = threadIdx.x < 128;   // cta_gemm32 covers 32 x 32 with 128 threads
 		T c8[8], u8[8];
 		int i = threadIdx.x/4, c0 = threadIdx.x%4;
-		if (act) {
-			cta_gemm32<T>(c8, Ls+32*LD, LD, Vs, LD, 1);          // T1 = L21 Linv11
-			cta_gemm32<T>(u8, Ls+32*LD, LD, Ls+32*LD, 1, LD);     // L21 L21^T
+		if (blockDim.x >= 256) {
+			// the two products side by side: L21 L21^T (on the chain to the
+			// next pivot block) by threads 0-127, T1 by threads 128-255
+			int t2 = threadIdx.x-128;
+			if (act) {
+				cta_gemm32<T>(u8, Ls+32*LD, LD, Ls+32*LD, 1, LD, threadIdx.x);
+#pragma unroll
+				for (int q = 0; q < 8; q++)
+					if (c0+4*q <= i) Ls[(32+i)*LD+32+c0+4*q] -= u8[q];
+			} else if (t2 < 128) {
+				cta_gemm32<T>(c8, Ls+32*LD, LD, Vs, LD, 1, t2);
+#pragma unroll
+				for (int q = 0; q < 8; q++) Ts[(t2/4)*33+t2%4+4*q] = c8[q];
+			}
+		} else if (act) {
+			cta_gemm32<T>(c8, Ls+32*LD, LD, Vs, LD, 1, threadIdx.x);          // T1 = L21 Linv11
+			cta_gemm32<T>(u8, Ls+32*LD, LD, Ls+32*LD, 1, LD, threadIdx.x);     // L21 L21^T
 #pragma unroll
 			for (int q = 0; q < 8; q++) {
 				int c = c0+4*q;
@@ -508,20 +549,37 @@ __device__ void diag_factor(T *base, int ld, int p0, int w, int gcol0, int *fail
 		__syncthreads();
 		if (warp == 0) {                                                               // Linv22
 			if constexpr (unrolled) warp_trtri32_unrolled<T>(Ls+32*LD+32, LD, Vs+32*LD+32, LD, lane);
-			else warp_trtri32<T>(Ls+32*LD+32, LD, Lsh+1024, Vs+32*LD+32, LD, lane);
+			else warp_trtri32<T>(Lsh+1024, Vs+32*LD+32, LD, lane);
 		}
 		__syncthreads();
 		if (act) {
-			cta_gemm32<T>(c8, Vs+32*LD+32, LD, Ts, 33, 1);       // Linv22 T1
+			cta_gemm32<T>(c8, Vs+32*LD+32, LD, Ts, 33, 1, threadIdx.x);       // Linv22 T1
 #pragma unroll
 			for (int q = 0; q < 8; q++) Vs[(32+i)*LD+c0+4*q] = -c8[q];
 		}
 		__syncthreads();
 	}
-	for (int e = threadIdx.x; e < NB*NB; e += blockDim.x) {
-		int i = e%NB, j = e/NB;
-		if (j <= i && i < w) base[(int64_t)(p0+j)*ld+p0+i] = Ls[i*LD+j];
-		vt[j*NB+i] = Vs[i*LD+j];   // Linv^T[t = j][col = i]
+	// batches of 8 elements per thread: shared loads first, then the stores
+	for (int e0 = threadIdx.x; e0 < NB*NB; e0 += 8*blockDim.x) {
+		T lv[8], vv[8];
+#pragma unroll
+		for (int u = 0; u < 8; u++) {
+			int e = e0+u*blockDim.x;
+			if (e < NB*NB) {
+				int i = e%NB, j = e/NB;
+				lv[u] = Ls[i*LD+j];
+				vv[u] = Vs[i*LD+j];
+			}
+		}
+#pragma unroll
+		for (int u = 0; u < 8; u++) {
+			int e = e0+u*blockDim.x;
+			if (e < NB*NB) {
+				int i = e%NB, j = e/NB;
+				if (j <= i && i < w) base[(int64_t)(p0+j)*ld+p0+i] = lv[u];
+				vt[j*NB+i] = vv[u];   // Linv^T[t = j][col = i]
+			}
+		}
 	}
 }
 
