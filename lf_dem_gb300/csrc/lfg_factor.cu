@@ -81,8 +81,10 @@ __device__ inline void od18_to_dense(const double *o, double *m)
 // visible -- before their first access to data an earlier launch writes;
 // task lists and indices (written by the symbolic upload, before any of these
 // launches) may be read before it.  The solve phases also call pdl_trigger
-// first, so the next phase is scheduled as soon as all their CTAs run; the
-// factor kernels do not (their successors would sit resident next to the
+// first, so the next phase is scheduled as soon as all their CTAs run, and so
+// does the panel solve k_trsm (a short launch: the next update's CTAs, the
+// diagonal tiles first, are resident when it completes).  The other factor
+// kernels do not (their successors would sit resident next to the
 // diagonal-block CTA on the critical path: measured slower), so theirs start
 // when they finish, overlapping only the final flush.
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
@@ -663,6 +665,7 @@ __global__ void __launch_bounds__(256) k_trsm(const int4 *__restrict__ tasks, co
 	int w = min(NB, 6*sn_n[s]-p0);   // panel width: columns p0 + w and later are not touched
 	T *base = arena+sn_off[s];
 	const T *vt = linv_slot<T>(linv, nsn, s, k);
+	pdl_trigger();   // the next update's CTAs wait resident while this short launch runs
 	pdl_wait();
 	// all of a thread's loads are issued before its shared stores (256
 	// threads: NB*NB/256 entries of Linv^T, PANEL_ROWS*NB/256 of the panel)

@@ -548,6 +548,16 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 		}
 		for (int k = 0; k < kmax; k++) {
 			int64_t p0 = (int64_t)panel_tasks.size(), t0i = (int64_t)tile_tasks.size();
+			// every front's diagonal tile first: its CTA factors the next
+			// panel's diagonal block (the launch's critical path), so it is
+			// dispatched in the first wave
+			for (int t = S.level_off[l]; t < S.level_off[l+1]; t++) {
+				int s = S.level_sn[t];
+				int n6 = 6*S.sn_n[s];
+				if (n6 <= k*panel_nb) continue;
+				int t0 = k*panel_nb+std::min(panel_nb, n6-k*panel_nb);
+				if (t0 < n6) tile_tasks.push_back(make_int4(s, t0, t0, k));
+			}
 			for (int t = S.level_off[l]; t < S.level_off[l+1]; t++) {
 				int s = S.level_sn[t];
 				int n6 = 6*S.sn_n[s], F6 = n6+6*S.sn_m[s];
@@ -561,7 +571,7 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 				// update-matrix block is one SYRK after the panels)
 				for (int r = t0; r < F6; r += tile)
 					for (int c = t0; c <= r && c < n6; c += tile)
-						tile_tasks.push_back(make_int4(s, r, c, k));
+						if (r != t0 || c != t0) tile_tasks.push_back(make_int4(s, r, c, k));
 				for (int r = F6; r < F6+t0; r += tile)
 					for (int c = t0; c < n6; c += tile)
 						tile_tasks.push_back(make_int4(s, r, c, k));
