@@ -34,7 +34,7 @@ namespace lfg {
 
 enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLAN_SYRK = 5,
        PLAN_DIAG = 6, PLAN_SYRK_TC = 8 };
-constexpr int PANEL_ROWS = 128;  // rows per panel (k_trsm) task (must match the plan)
+constexpr int PANEL_ROWS = 64;   // rows per panel (k_trsm) task (must match the plan)
 constexpr int SOLVE_WARPS = 8;
 constexpr int SOLVE_CB = 8;      // columns per CTA of the solve's column kernels
 constexpr int SOLVE_JC = 256;    // columns per chunk of the solve's row kernels
@@ -625,9 +625,9 @@ __global__ void __launch_bounds__(128) k_diag(const int4 *__restrict__ tasks, co
 // ---------------------------------------------------------------------------
 // rows below the diagonal block of panel k (k_trsm): X = A Linv_kk^T for up
 // to PANEL_ROWS rows per CTA (real rows [t0, 6F) and identity rows [6F,
-// 6F + t0)), in place.  256 threads: thread (g, r) computes rows r and r + 64
-// for two column chunks of width NB/8, chunks g and 7 - g (equal work, since
-// column j needs t <= j).  Linv^T sits in shared memory row-major, so a
+// 6F + t0)), in place.  256 threads: thread (g, r) computes row r for two
+// column chunks of width NB/8, chunks g and 7 - g (equal work, since column
+// j needs t <= j).  Linv^T sits in shared memory row-major, so a
 // chunk's coefficients for one t are one or two vector loads (a broadcast).
 // ---------------------------------------------------------------------------
 template <typename T> struct Vec2;
@@ -657,7 +657,7 @@ __global__ void __launch_bounds__(256) k_trsm(const int4 *__restrict__ tasks, co
 	constexpr int NB = Cfg<T>::NB, CW = NB/8;
 	__shared__ __align__(16) T Vt[NB*NB];
 	__shared__ T As[PANEL_ROWS*NB];   // row r, column t at r*NB + (t ^ (r & 31)): a warp's rows on distinct banks
-	static_assert(PANEL_ROWS == 128, "two rows per thread");
+	static_assert(PANEL_ROWS == 64, "one row per thread");
 	int4 tk = tasks[blockIdx.x];
 	int s = tk.x, row0 = tk.y, k = tk.z, nrows = tk.w;
 	int ld = sn_ld[s];
@@ -690,32 +690,30 @@ __global__ void __launch_bounds__(256) k_trsm(const int4 *__restrict__ tasks, co
 		}
 	}
 	__syncthreads();
+	// thread: row r, column chunks g and 7 - g (equal work per thread:
+	// chunk c has (c + 1) CW terms per entry)
 	int g = threadIdx.x/64, r = threadIdx.x%64;
-	const T *a0 = As+r*NB, *a1 = As+(r+64)*NB;
-	const int sw = r & 31;   // rows r and r + 64 share the swizzle
+	const T *a0 = As+r*NB;
+	const int sw = r & 31;
 #pragma unroll
 	for (int h = 0; h < 2; h++) {
 		int c = h ? 7-g : g;
 		int j0 = c*CW;
-		T x0[CW], x1[CW];
+		T x0[CW];
 #pragma unroll
-		for (int q = 0; q < CW; q++) x0[q] = x1[q] = T(0);
+		for (int q = 0; q < CW; q++) x0[q] = T(0);
+#pragma unroll 4
 		for (int t = 0; t < j0+CW; t++) {
 			T v[CW];
 			lds_chunk<T, CW>(Vt+t*NB+j0, v);
-			T u0 = a0[t ^ sw], u1 = a1[t ^ sw];
+			T u0 = a0[t ^ sw];
 #pragma unroll
-			for (int q = 0; q < CW; q++) {
-				x0[q] += u0*v[q];
-				x1[q] += u1*v[q];
-			}
+			for (int q = 0; q < CW; q++) x0[q] += u0*v[q];
 		}
 #pragma unroll
 		for (int q = 0; q < CW; q++) {
 			if (j0+q >= w) continue;
-			int64_t col = (int64_t)(p0+j0+q)*ld+row0;
-			if (r < nrows) base[col+r] = x0[q];
-			if (r+64 < nrows) base[col+r+64] = x1[q];
+			if (r < nrows) base[(int64_t)(p0+j0+q)*ld+row0+r] = x0[q];
 		}
 	}
 }
