@@ -1340,8 +1340,12 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 // fixed order: results are bitwise reproducible.  (One persistent kernel with grid barriers between phases
 // was measured slower: the barriers cost more than the launch gaps.)
 
-// Solve phases read their indices and factor entries (constant during a
-// solve) before pdl_wait; every other access follows it.
+// Solve phases read their indices and the first batch of their factor
+// entries before pdl_wait, overlapping the previous phase: the factor is
+// complete before the second phase starts (the first phase does not trigger
+// early and waits for the factorisation, whether both run as graphs or as
+// plain launches in one stream) and constant during the solve; every other
+// access follows the wait.
 
 template <typename T> struct SolveArgs {
 	const int *lev_sn, *sn_first, *sn_n, *sn_m, *sn_ld, *sn_rows_off, *rows;
@@ -1370,18 +1374,35 @@ __device__ void unit_gather(const SolveArgs<T> &A, const int *lev, int bx, int b
 	int r = bx*blockDim.x+threadIdx.x;
 	if (r >= F6) return;
 	int ca = A.child_off[s], cz = A.child_off[s+1];
+	int rb = r/6, rr = r%6;
+	// the first children's source positions (symbolic) before the wait
+	constexpr int CPRE = 4;
+	int64_t src[CPRE];
+#pragma unroll
+	for (int c = 0; c < CPRE; c++) {
+		src[c] = -1;
+		if (ca+c < cz) {
+			int ch = A.children[ca+c];
+			int ic = A.cinv[A.cinv_off[ch]+rb];
+			if (ic >= 0) src[c] = A.sn_woff[ch]+6*(ic-A.sn_n[ch])+rr;
+		}
+	}
 	T acc[K];
 #pragma unroll
 	for (int q = 0; q < K; q++) acc[q] = 0;
-	int rb = r/6, rr = r%6;
 	pdl_wait();
-	for (int c = ca; c < cz; c++) {
+#pragma unroll
+	for (int c = 0; c < CPRE; c++)
+		if (src[c] >= 0)
+#pragma unroll
+			for (int q = 0; q < K; q++) acc[q] += A.w[q*A.wstride+src[c]];
+	for (int c = ca+CPRE; c < cz; c++) {
 		int ch = A.children[c];
 		int ic = A.cinv[A.cinv_off[ch]+rb];
 		if (ic < 0) continue;
-		int64_t src = A.sn_woff[ch]+6*(ic-A.sn_n[ch])+rr;
+		int64_t sc = A.sn_woff[ch]+6*(ic-A.sn_n[ch])+rr;
 #pragma unroll
-		for (int q = 0; q < K; q++) acc[q] += A.w[q*A.wstride+src];
+		for (int q = 0; q < K; q++) acc[q] += A.w[q*A.wstride+sc];
 	}
 	if (r < n6) {
 		int g = 6*A.sn_first[s]+r;
@@ -1401,6 +1422,22 @@ __device__ void unit_gather(const SolveArgs<T> &A, const int *lev, int bx, int b
 // in increasing order.
 template <typename T> struct SolveUnroll { static constexpr int U = sizeof(T) == 4 ? 4 : 2; };
 
+// one batch of a column product's rows: their positions (g < 0 past the
+// rows) and factor entries
+template <typename T, int U, int MODE>
+__device__ __forceinline__ void cols_batch(int i0, int nrow, int f6, const int *R, const T *M, int ld, int j0, int jn,
+                                           int64_t (&g)[U], T (&e)[U][SOLVE_CB])
+{
+#pragma unroll
+	for (int u = 0; u < U; u++) {
+		int i = i0+u*blockDim.x;
+		g[u] = i >= nrow ? -1 : MODE == 0 ? f6+i : 6*R[i/6]+i%6;
+#pragma unroll
+		for (int c = 0; c < SOLVE_CB; c++)
+			e[u][c] = (i >= nrow || c >= jn || (MODE == 0 && i > j0+c)) ? T(0) : __ldg(&M[(int64_t)c*ld+i]);
+	}
+}
+
 template <typename T, int K, int MODE>
 __device__ void unit_cols(const SolveArgs<T> &A, const int *lev, int bx, int by, SolveShared<T> &sh)
 {
@@ -1414,29 +1451,21 @@ __device__ void unit_cols(const SolveArgs<T> &A, const int *lev, int bx, int by,
 	const T *M = A.arena+A.sn_off[s]+(MODE == 0 ? n6+m6 : n6)+(int64_t)j0*ld;
 	const int *R = A.rows+A.sn_rows_off[s];
 	int nrow = MODE == 0 ? j0+jn : m6;
-	pdl_wait();
 	T acc[SOLVE_CB][K];
 #pragma unroll
 	for (int c = 0; c < SOLVE_CB; c++)
 #pragma unroll
 		for (int q = 0; q < K; q++) acc[c][q] = 0;
+	int64_t g[U];
+	T e[U][SOLVE_CB];
+	cols_batch<T, U, MODE>(threadIdx.x, nrow, f6, R, M, ld, j0, jn, g, e);   // before the wait
+	pdl_wait();
 	for (int i0 = threadIdx.x; i0 < nrow; i0 += U*blockDim.x) {
-		int64_t g[U];
+		T v[U][K];
 #pragma unroll
-		for (int u = 0; u < U; u++) {
-			int i = i0+u*blockDim.x;
-			g[u] = i >= nrow ? -1 : MODE == 0 ? f6+i : 6*R[i/6]+i%6;
-		}
-		T v[U][K], e[U][SOLVE_CB];
-#pragma unroll
-		for (int u = 0; u < U; u++) {
-			int i = i0+u*blockDim.x;
+		for (int u = 0; u < U; u++)
 #pragma unroll
 			for (int q = 0; q < K; q++) v[u][q] = g[u] < 0 ? T(0) : A.xp[(int64_t)q*A.n6tot+g[u]];
-#pragma unroll
-			for (int c = 0; c < SOLVE_CB; c++)
-				e[u][c] = (g[u] < 0 || c >= jn || (MODE == 0 && i > j0+c)) ? T(0) : __ldg(&M[(int64_t)c*ld+i]);
-		}
 #pragma unroll
 		for (int u = 0; u < U; u++) {
 			if (g[u] < 0) continue;
@@ -1448,6 +1477,8 @@ __device__ void unit_cols(const SolveArgs<T> &A, const int *lev, int bx, int by,
 				for (int q = 0; q < K; q++) acc[c][q] += e[u][c]*v[u][q];
 			}
 		}
+		int i1 = i0+U*blockDim.x;
+		if (i1 < nrow) cols_batch<T, U, MODE>(i1, nrow, f6, R, M, ld, j0, jn, g, e);
 	}
 	int warp = threadIdx.x/32, lane = threadIdx.x%32;
 #pragma unroll
@@ -1500,21 +1531,28 @@ __device__ void unit_rows(const SolveArgs<T> &A, const int *lev, int bx, int by,
 	int jhi = min(n6, jlo+SOLVE_JC);
 	const T *M = A.arena+A.sn_off[s]+(UPD ? n6 : MODE == 1 ? n6+m6 : 0);
 	int r = r0+lane;
-	pdl_wait();
 	T acc[K];
 #pragma unroll
 	for (int q = 0; q < K; q++) acc[q] = 0;
+	// RU columns of a warp per batch, the factor entries of the first batch
+	// before the wait, loads ahead of the multiply-adds (see unit_cols).
+	// Unmasked by the triangle: column j < n6 of a front is allocated down
+	// to its last row (the masked product skips it).
+	constexpr int RU = 2*SolveUnroll<T>::U;
+	T e[RU];
+	int jb = jlo+warp;
+#pragma unroll
+	for (int u = 0; u < RU; u++) {
+		int j = jb+u*SOLVE_WARPS;
+		e[u] = (r < nrows && j < jhi) ? __ldg(&M[(int64_t)j*ld+r]) : T(0);
+	}
+	pdl_wait();
 	if (r < nrows) {
-		// RU columns of a warp per batch, loads first (see unit_cols)
-		constexpr int RU = 2*SolveUnroll<T>::U;
-		for (int j0 = jlo+warp; j0 < jhi; j0 += RU*SOLVE_WARPS) {
-			T e[RU], y[RU][K];
+		for (int j0 = jb; j0 < jhi; j0 += RU*SOLVE_WARPS) {
+			T y[RU][K];
 #pragma unroll
 			for (int u = 0; u < RU; u++) {
-				// unmasked by the triangle: column j < n6 of a front is
-				// allocated down to its last row (the masked product skips it)
 				int j = j0+u*SOLVE_WARPS;
-				e[u] = j < jhi ? __ldg(&M[(int64_t)j*ld+r]) : T(0);
 #pragma unroll
 				for (int q = 0; q < K; q++) y[u][q] = j < jhi ? A.yp[(int64_t)q*A.n6tot+f6+j] : T(0);
 			}
@@ -1525,6 +1563,13 @@ __device__ void unit_rows(const SolveArgs<T> &A, const int *lev, int bx, int by,
 #pragma unroll
 				for (int q = 0; q < K; q++) acc[q] += e[u]*y[u][q];
 			}
+			int j1 = j0+RU*SOLVE_WARPS;
+			if (j1 < jhi)
+#pragma unroll
+				for (int u = 0; u < RU; u++) {
+					int j = j1+u*SOLVE_WARPS;
+					e[u] = j < jhi ? __ldg(&M[(int64_t)j*ld+r]) : T(0);
+				}
 		}
 	}
 #pragma unroll
@@ -1590,7 +1635,10 @@ template <typename T, int K, int TYPE>
 __global__ void __launch_bounds__(256) k_solve_phase(SolveArgs<T> A, SolvePhase ph)
 {
 	__shared__ SolveShared<T> sh;
-	pdl_trigger();
+	// The first phase (permutation in) lets the next one start only when it
+	// has finished, i.e. after the factorisation it waits for: the later
+	// phases read factor entries before their wait.
+	if (TYPE != SP_PERM_IN && TYPE != SP_PERM_IN_Y) pdl_trigger();
 	const int *lev = A.lev_sn+ph.lev_off;
 	int bx = blockIdx.x, by = blockIdx.y, bz = blockIdx.z;
 	if (TYPE == SP_PERM_IN) unit_permute<T, K>(A, bx, true);
