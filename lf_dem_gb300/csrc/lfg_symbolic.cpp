@@ -14,9 +14,14 @@
 // structures, restricted to later columns -- every such row belongs to an
 // ancestor, so a child's update matrix always fits in its parent's front.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
+#include <exception>
+#include <memory>
+#include <mutex>
 #include <numeric>
 #include <queue>
+#include <thread>
 
 #include "lfg_internal.h"
 
@@ -60,31 +65,58 @@ struct TNode {
 	std::vector<int> kids;
 };
 
+// work arrays of the separator search (one set per thread); side and level
+// are indexed by vertex (a candidate cut's labelling and ranks)
+struct CoverWork {
+	std::vector<int> eptr, eadj, m0, m1, seen, stk, it, via, q, side, level;
+	std::vector<char> z0, z1;
+	void reserve(int n)
+	{
+		if ((int)side.size() < n) {
+			side.assign(n, 0);
+			level.assign(n, -1);
+		}
+	}
+};
+
+// the best cut along one axis
+struct AxisCut {
+	bool have = false;
+	double cost = 0;
+	int mid = 0;
+	std::vector<int> sep;
+	std::vector<std::pair<double,int>> key;   // S sorted along the axis
+};
+
+// The two halves of a cut are dissected by separate threads near the top of
+// the tree: they touch disjoint vertex sets of side[], level[] and stamp[]
+// (stamp[] is also read for the neighbours of a set, hence relaxed atomics),
+// and node ids are only labels (the tree and its postorder come from the
+// kids lists), so the result does not depend on the thread schedule.
 struct Dissector {
 	const Graph &g;
 	const double *pos;
 	bool twod;
 	int leaf;
 	std::vector<TNode> nodes;
-	std::vector<int> stamp, side, level;
-	int cur = 0;
+	std::mutex nodes_mu;
+	std::unique_ptr<std::atomic<int>[]> stamp;
+	std::vector<int> side, level;
+	std::atomic<int> cur{0};
 
 	Dissector(const Graph &g_, const double *pos_, bool twod_, int leaf_, int n)
-	    : g(g_), pos(pos_), twod(twod_), leaf(leaf_), stamp(n, -1), side(n, 0), level(n, -1) {}
-
-	// one-sided vertex separator for the current side[] labelling of S
-	void boundary(const std::vector<int> &S, int st, std::vector<int> &b0, std::vector<int> &b1)
+	    : g(g_), pos(pos_), twod(twod_), leaf(leaf_), stamp(new std::atomic<int>[n]), side(n, 0), level(n, -1)
 	{
-		b0.clear(); b1.clear();
-		for (int v : S) {
-			bool cross = false;
-			for (int k = g.ptr[v]; k < g.ptr[v+1]; k++) {
-				int u = g.adj[k];
-				if (u < 0 || stamp[u] != st) continue;
-				if (side[u] != side[v]) { cross = true; break; }
-			}
-			if (cross) (side[v] == 0 ? b0 : b1).push_back(v);
-		}
+		for (int i = 0; i < n; i++) stamp[i].store(-1, std::memory_order_relaxed);
+	}
+
+	bool in(int u, int st) const { return u >= 0 && stamp[u].load(std::memory_order_relaxed) == st; }
+
+	int add_node(TNode &&t)
+	{
+		std::lock_guard<std::mutex> lk(nodes_mu);
+		nodes.push_back(std::move(t));
+		return (int)nodes.size()-1;
 	}
 
 	// Minimum vertex cover of the cut edges (edges between side 0 and side 1
@@ -92,29 +124,44 @@ struct Dissector {
 	// paths), then the alternating-path labelling from the unmatched side-0
 	// vertices; cover = (side-0 vertices not reached) + (side-1 vertices
 	// reached).  Removing the cover disconnects the two sides.
-	std::vector<int> min_cover(const std::vector<int> &S, int st, const std::vector<int> &b0,
-	                           const std::vector<int> &b1)
+	std::vector<int> min_cover(int st, const std::vector<int> &b0, const std::vector<int> &b1, CoverWork &w)
 	{
+		auto &eptr = w.eptr, &eadj = w.eadj, &m0 = w.m0, &m1 = w.m1, &seen = w.seen, &stk = w.stk, &it = w.it;
+		auto &via = w.via, &q = w.q, &side = w.side, &level = w.level;
+		auto &z0 = w.z0, &z1 = w.z1;
 		int n0 = (int)b0.size(), n1 = (int)b1.size();
 		for (int t = 0; t < n0; t++) level[b0[t]] = t;
 		for (int t = 0; t < n1; t++) level[b1[t]] = t;
-		std::vector<int> eptr(n0+1, 0), eadj;
+		eptr.assign(n0+1, 0);
+		eadj.clear();
 		for (int t = 0; t < n0; t++) {
 			int v = b0[t];
 			for (int k = g.ptr[v]; k < g.ptr[v+1]; k++) {
 				int u = g.adj[k];
-				if (u < 0 || stamp[u] != st || side[u] != 1) continue;
+				if (!in(u, st) || side[u] != 1) continue;
 				eadj.push_back(level[u]);
 			}
 			eptr[t+1] = (int)eadj.size();
 		}
-		std::vector<int> m0(n0, -1), m1(n1, -1), seen(n1, -1);
-		std::vector<int> stk, it;
+		m0.assign(n0, -1);
+		m1.assign(n1, -1);
+		seen.assign(n1, -1);
+		// greedy start (each side-0 vertex takes its first free neighbour);
+		// augmenting paths then extend it to a maximum matching
+		for (int x = 0; x < n0; x++)
+			for (int k = eptr[x]; k < eptr[x+1]; k++)
+				if (m1[eadj[k]] < 0) {
+					m0[x] = eadj[k];
+					m1[eadj[k]] = x;
+					break;
+				}
+		// via: side-1 vertex taken at each depth of the search
 		for (int r = 0; r < n0; r++) {
+			if (m0[r] >= 0) continue;
 			// iterative DFS for an augmenting path from r
 			stk.assign(1, r);
 			it.assign(1, eptr[r]);
-			std::vector<int> via;   // side-1 vertex taken at each depth
+			via.clear();
 			bool found = false;
 			while (!stk.empty() && !found) {
 				int x = stk.back();
@@ -140,8 +187,9 @@ struct Dissector {
 				}
 			}
 		}
-		std::vector<char> z0(n0, 0), z1(n1, 0);
-		std::vector<int> q;
+		z0.assign(n0, 0);
+		z1.assign(n1, 0);
+		q.clear();
 		for (int x = 0; x < n0; x++) if (m0[x] < 0) { z0[x] = 1; q.push_back(x); }
 		for (size_t h = 0; h < q.size(); h++) {
 			int x = q[h];
@@ -163,38 +211,97 @@ struct Dissector {
 
 	// coordinate cuts along each axis at several quantiles; the separator is
 	// the minimum vertex cover of the cut edges; the cut with the smallest
-	// ratio |separator| / (|side 0| |side 1|) wins
-	std::vector<int> split_geometric(const std::vector<int> &S, int st)
+	// ratio |separator| / (|side 0| |side 1|) wins (the first one, in axis
+	// then quantile order, among equals)
+	void cut_axis(int ax, const std::vector<int> &S, int st, CoverWork &w, AxisCut &out)
 	{
 		static const double fracs[] = {0.5, 0.47, 0.53, 0.44, 0.56, 0.41, 0.59, 0.38, 0.62};
-		std::vector<int> best;
-		double best_cost = 0;
-		bool have = false;
+		auto &side = w.side, &level = w.level;
 		std::vector<int> b0, b1;
 		std::vector<std::pair<double,int>> key(S.size());
-		std::vector<int> best_side;
-		for (int ax = 0; ax < 3; ax++) {
-			if (twod && ax == 1) continue;
-			for (size_t t = 0; t < S.size(); t++) key[t] = {pos[3*S[t]+ax], S[t]};
-			std::sort(key.begin(), key.end());
-			for (double f : fracs) {
-				size_t mid = (size_t)(f*S.size());
-				if (mid == 0 || mid >= S.size()) continue;
-				for (size_t t = 0; t < S.size(); t++) side[key[t].second] = t < mid ? 0 : 1;
-				boundary(S, st, b0, b1);
-				std::vector<int> sep = min_cover(S, st, b0, b1);
-				double cost = (double)sep.size()/((double)mid*(double)(S.size()-mid));
-				if (!have || cost < best_cost) {
-					best = sep;
-					best_cost = cost;
-					have = true;
-					best_side.resize(S.size());
-					for (size_t t = 0; t < S.size(); t++) best_side[t] = side[S[t]];
-				}
+		// each vertex's rank along the axis and the lowest and highest rank
+		// of its neighbours in S: the boundary of a cut at rank mid (side 0 =
+		// rank < mid) is read off without walking the adjacency again
+		std::vector<int> rk(S.size()), lo(S.size()), hi(S.size());
+		for (size_t t = 0; t < S.size(); t++) key[t] = {pos[3*S[t]+ax], S[t]};
+		std::sort(key.begin(), key.end());
+		for (size_t t = 0; t < S.size(); t++) level[key[t].second] = (int)t;   // rank (scratch)
+		for (size_t t = 0; t < S.size(); t++) {
+			int v = S[t];
+			rk[t] = level[v];
+			int a = INT32_MAX, b = -1;
+			for (int k = g.ptr[v]; k < g.ptr[v+1]; k++) {
+				int u = g.adj[k];
+				if (!in(u, st)) continue;
+				a = std::min(a, level[u]);
+				b = std::max(b, level[u]);
+			}
+			lo[t] = a;
+			hi[t] = b;
+		}
+		for (int v : S) level[v] = -1;
+		for (double f : fracs) {
+			int mid = (int)(f*S.size());
+			if (mid == 0 || mid >= (int)S.size()) continue;
+			for (size_t t = 0; t < S.size(); t++) side[key[t].second] = (int)t < mid ? 0 : 1;
+			b0.clear(); b1.clear();
+			for (size_t t = 0; t < S.size(); t++) {
+				if (rk[t] < mid) { if (hi[t] >= mid) b0.push_back(S[t]); }
+				else if (lo[t] < mid) b1.push_back(S[t]);
+			}
+			std::vector<int> sep = min_cover(st, b0, b1, w);
+			double cost = (double)sep.size()/((double)mid*(double)(S.size()-mid));
+			if (!out.have || cost < out.cost) {
+				out.have = true;
+				out.cost = cost;
+				out.mid = mid;
+				out.sep = std::move(sep);
 			}
 		}
-		for (size_t t = 0; t < S.size(); t++) side[S[t]] = best_side[t];
-		return best;
+		if (out.have) out.key = std::move(key);
+	}
+
+	std::vector<int> split_geometric(const std::vector<int> &S, int st, CoverWork &w)
+	{
+		int n = (int)side.size();
+		std::vector<int> axes = twod ? std::vector<int>{0, 2} : std::vector<int>{0, 1, 2};
+		std::vector<AxisCut> cut(axes.size());
+		w.reserve(n);
+		if (S.size() >= 1024) {
+			// large sets: the axes on separate threads, each with its own
+			// labelling and rank arrays
+			std::vector<CoverWork> wk(axes.size()-1);
+			std::vector<std::exception_ptr> err(axes.size(), nullptr);
+			std::vector<std::thread> th;
+			for (size_t a = 1; a < axes.size(); a++)
+				th.emplace_back([&, a] {
+					try {
+						wk[a-1].reserve(n);
+						cut_axis(axes[a], S, st, wk[a-1], cut[a]);
+					} catch (...) {
+						err[a] = std::current_exception();
+					}
+				});
+			try {
+				cut_axis(axes[0], S, st, w, cut[0]);
+			} catch (...) {
+				err[0] = std::current_exception();
+			}
+			for (auto &t : th) t.join();
+			for (auto &e : err) if (e) std::rethrow_exception(e);
+		} else {
+			for (size_t a = 0; a < axes.size(); a++) cut_axis(axes[a], S, st, w, cut[a]);
+		}
+		int b = -1;
+		for (size_t a = 0; a < axes.size(); a++)
+			if (cut[a].have && (b < 0 || cut[a].cost < cut[b].cost)) b = (int)a;
+		if (b < 0) {   // (sets of one vertex do not reach this)
+			for (int v : S) side[v] = 0;
+			return {};
+		}
+		const AxisCut &c = cut[b];
+		for (size_t t = 0; t < S.size(); t++) side[c.key[t].second] = (int)t < c.mid ? 0 : 1;
+		return c.sep;
 	}
 
 	// breadth-first level structure from a pseudo-peripheral vertex; the
@@ -210,7 +317,7 @@ struct Dissector {
 				int v = q.front(); q.pop(); order.push_back(v);
 				for (int k = g.ptr[v]; k < g.ptr[v+1]; k++) {
 					int u = g.adj[k];
-					if (u < 0 || stamp[u] != st || level[u] >= 0) continue;
+					if (!in(u, st) || level[u] >= 0) continue;
 					level[u] = level[v]+1;
 					q.push(u);
 				}
@@ -238,16 +345,12 @@ struct Dissector {
 		return sep;
 	}
 
-	std::vector<int> dissect(std::vector<int> S)
+	std::vector<int> dissect(std::vector<int> S, int depth, CoverWork &w)
 	{
-		if ((int)S.size() <= leaf) {
-			nodes.push_back(TNode{S, {}});
-			return {(int)nodes.size()-1};
-		}
+		if ((int)S.size() <= leaf) return {add_node(TNode{S, {}})};
 		int st = cur++;
-		for (int v : S) stamp[v] = st;
-		std::vector<int> sep = pos ? split_geometric(S, st) : split_bfs(S, st);
-		std::vector<char> insep;
+		for (int v : S) stamp[v].store(st, std::memory_order_relaxed);
+		std::vector<int> sep = pos ? split_geometric(S, st, w) : split_bfs(S, st);
 		for (int v : sep) side[v] = 2;
 		std::vector<int> L, R;
 		for (int v : S) {
@@ -257,11 +360,26 @@ struct Dissector {
 		std::vector<int> roots;
 		if (L.size() == S.size() || R.size() == S.size()) {
 			// no progress (should not happen); make a leaf
-			nodes.push_back(TNode{S, {}});
-			return {(int)nodes.size()-1};
+			return {add_node(TNode{S, {}})};
 		}
-		std::vector<int> kl = L.empty() ? std::vector<int>{} : dissect(L);
-		std::vector<int> kr = R.empty() ? std::vector<int>{} : dissect(R);
+		std::vector<int> kl, kr;
+		if (depth < 4 && L.size() >= 256 && R.size() >= 256) {
+			std::exception_ptr err;
+			std::thread t([&] {
+				try {
+					CoverWork wl;
+					kl = dissect(L, depth+1, wl);
+				} catch (...) {
+					err = std::current_exception();
+				}
+			});
+			kr = dissect(R, depth+1, w);
+			t.join();
+			if (err) std::rethrow_exception(err);
+		} else {
+			if (!L.empty()) kl = dissect(L, depth+1, w);
+			if (!R.empty()) kr = dissect(R, depth+1, w);
+		}
 		if (sep.empty()) {
 			roots = kl;
 			roots.insert(roots.end(), kr.begin(), kr.end());
@@ -271,8 +389,7 @@ struct Dissector {
 		nd.cols = sep;
 		nd.kids = kl;
 		nd.kids.insert(nd.kids.end(), kr.begin(), kr.end());
-		nodes.push_back(nd);
-		return {(int)nodes.size()-1};
+		return {add_node(std::move(nd))};
 	}
 };
 
@@ -288,7 +405,8 @@ void symbolic_analyze(Symbolic &S, int n, int nb, const int32_t *od_row, const i
 	Dissector D(g, pos, ly == 0, std::max(1, leaf_size), n);
 	std::vector<int> all(n);
 	std::iota(all.begin(), all.end(), 0);
-	std::vector<int> roots = D.dissect(all);
+	CoverWork work;
+	std::vector<int> roots = D.dissect(all, 0, work);
 
 	// postorder numbering of tree nodes -> supernodes
 	std::vector<int> post;                 // tree node ids in postorder
