@@ -278,6 +278,17 @@ template <typename T> __device__ inline void lsh_column(const T *Lsh, int j, T (
 	}
 }
 
+// pivot reciprocal square root: the hardware approximation for FP32 (the
+// FP32 factor is refined in FP64 anyway; no denormal handling on the chain),
+// the library rsqrt for FP64
+__device__ __forceinline__ float pivot_rsqrt(float x)
+{
+	float r;
+	asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+	return r;
+}
+__device__ __forceinline__ double pivot_rsqrt(double x) { return rsqrt(x); }
+
 // Cholesky of S (lower part), lane = row; S's lower part becomes L and its
 // upper part zero; Lsh receives L's columns
 template <typename T>
@@ -291,7 +302,7 @@ __device__ void warp_potrf32(T *S, int ld, T *Lsh, int lane, int jlim, int gcol0
 		if (lane == 0 && jlim > 0 && fail) atomicMin(fail, gcol0+1);
 		djj = T(1);
 	}
-	T rs = rsqrt(djj);
+	T rs = pivot_rsqrt(djj);
 #pragma unroll 1
 	for (int j = 0; j < 32; j++) {
 		T lij = a[0]*rs;
@@ -307,7 +318,7 @@ __device__ void warp_potrf32(T *S, int ld, T *Lsh, int lane, int jlim, int gcol0
 		bool bad = !(dn > T(0));
 		if (bad && lane == 0 && j+1 < 32 && j+1 < jlim && fail) atomicMin(fail, gcol0+j+2);
 		dn = bad ? T(1) : dn;
-		T rsn = rsqrt(dn);
+		T rsn = pivot_rsqrt(dn);
 		a[0] = a0;
 #pragma unroll
 		for (int q = 2; q < 32; q++) a[q-1] = a[q]-lij*c[q];   // entries past the block are dead
