@@ -253,10 +253,11 @@ constexpr unsigned FULL_MASK = 0xffffffffu;
 // the solves with vector loads.
 //
 // The steps are latency chains; each routine keeps only what the next step
-// needs on the chain: warp_potrf32 takes the next pivot's row entry by
-// shuffle and starts the next pivot's shuffle before the column arrives
-// through Lsh; the solves take the reciprocal from Lsh (no shuffle, no
-// division) and load two columns per iteration ahead of their updates.
+// needs on the chain: in warp_potrf32 the next pivot's lane updates its
+// own diagonal entry and broadcasts it, and its rsqrt is issued before the
+// column updates, which wait for Lsh; the solves take the reciprocal from
+// Lsh (no shuffle, no division) and load two columns per iteration ahead of
+// their updates.
 
 // the 32 entries Lsh[32 j + q], q < 32
 template <typename T> __device__ inline void lsh_column(const T *Lsh, int j, T (&c)[32])
@@ -306,22 +307,20 @@ __device__ void warp_potrf32(T *S, int ld, T *Lsh, int lane, int jlim, int gcol0
 #pragma unroll 1
 	for (int j = 0; j < 32; j++) {
 		T lij = a[0]*rs;
+		// the next pivot first: lane j + 1 updates its own diagonal entry with
+		// its own L[j + 1][j] and broadcasts it (one shuffle on the chain)
+		T dn = __shfl_sync(FULL_MASK, a[1]-lij*lij, (j+1) & 31);
 		S[lane*ld+j] = lane > j ? lij : (lane == j ? djj*rs : T(0));
 		Lsh[32*j+((lane-j) & 31)] = lane > j ? lij : (lane == j ? rs : T(0));
 		__syncwarp();
 		T c[32];
-		lsh_column<T>(Lsh, j, c);   // in flight during the next pivot's chain
-		// the next pivot (its entry of column j by shuffle, its check and
-		// rsqrt) ahead of this column's updates
-		T a0 = a[1]-lij*__shfl_sync(FULL_MASK, lij, (j+1) & 31);
-		T dn = __shfl_sync(FULL_MASK, a0, (j+1) & 31);
+		lsh_column<T>(Lsh, j, c);   // in flight during the pivot's check and rsqrt
 		bool bad = !(dn > T(0));
 		if (bad && lane == 0 && j+1 < 32 && j+1 < jlim && fail) atomicMin(fail, gcol0+j+2);
 		dn = bad ? T(1) : dn;
 		T rsn = pivot_rsqrt(dn);
-		a[0] = a0;
 #pragma unroll
-		for (int q = 2; q < 32; q++) a[q-1] = a[q]-lij*c[q];   // entries past the block are dead
+		for (int q = 1; q < 32; q++) a[q-1] = a[q]-lij*c[q];   // entries past the block are dead
 		djj = dn;
 		rs = rsn;
 	}
