@@ -993,30 +993,34 @@ __global__ void k_pair_stress(DevParams P, int np, const DevClock *__restrict__ 
                               const double *__restrict__ vel, const double *__restrict__ ang,
                               const double *__restrict__ split, int n, double *__restrict__ scr)
 {
-	int t = blockIdx.x*blockDim.x+threadIdx.x;
-	if (t >= np) return;
-	const int W = 12*NSC;
-	double *o = scr+W*(int64_t)t;
-	for (int k = 0; k < W; k++) o[k] = 0;
+	// one thread per (stresslet slot, pair), slot-major (a warp's pairs share
+	// the slot's branch): it writes the slot's 12 values (the pair's p0 and p1
+	// parts), zero where the slot does not apply
+	int64_t tt = (int64_t)blockIdx.x*blockDim.x+threadIdx.x;
+	if (tt >= (int64_t)np*NSC) return;
+	int t = (int)(tt%np), slot = (int)(tt/np);
+	double *o = scr+12*NSC*(int64_t)t+12*slot;
+	s2 Si = szero(), Sj = szero();
 	DPair &q = pairs[t];
-	if (!(q.flags & PF_INTER)) return;
-	const DPairConst &c = pc[t];
-	int i = q.p0, j = q.p1;
-	v3 nv = ld3(q.nvec);
-	s2 Si, Sj;
-	if (P.lub_on && (q.flags & PF_LUB)) {
-		double XG[4], YG[4], XM[4], YM[4];
-		for (int k = 0; k < 4; k++) {
-			XG[k] = c.lc[CXG+k]*q.lub_coeff;
-			YG[k] = c.lc[CYG+k]*q.log_lub_coeff;
-			XM[k] = c.lc[CXM+k]*q.lub_coeff;
-			YM[k] = c.lc[CYM+k]*q.log_lub_coeff;
-		}
-		s2 nn = outer(nv);
-		// GU per velocity component (Lubrication::addGUStresslet)
+	const int flags = q.flags;
+	if (flags & PF_INTER) {
+		const DPairConst &c = pc[t];
+		int i = q.p0, j = q.p1;
+		v3 nv = ld3(q.nvec);
+		const bool lub = P.lub_on && (flags & PF_LUB);
+		int cc = -1;   // force component of a GU slot
+		for (int u = 0; u < NFC; u++)
+			if (sc_gu_slot(u) == slot) cc = u;
 		bool has[NFC] = {true, true, (bool)P.lub_on, (bool)P.repulsiveforce, (bool)P.brownian_on};
-		for (int cc = 0; cc < NFC; cc++) {
-			if (!has[cc]) continue;
+		if (lub && cc >= 0 && has[cc]) {
+			// GU of one velocity component (Lubrication::addGUStresslet)
+			double XG[4], YG[4], YM[4];
+			for (int k = 0; k < 4; k++) {
+				XG[k] = c.lc[CXG+k]*q.lub_coeff;
+				YG[k] = c.lc[CYG+k]*q.log_lub_coeff;
+				YM[k] = c.lc[CYM+k]*q.log_lub_coeff;
+			}
+			s2 nn = outer(nv);
 			const double *v = vc+(int64_t)cc*6*n;
 			v3 vi = ld3(v+6*i), vj = ld3(v+6*j), oi = ld3(v+6*i+3), oj = ld3(v+6*j+3);
 			double nvi = vdot(nv, vi), nvj = vdot(nv, vj);
@@ -1032,60 +1036,65 @@ __global__ void k_pair_stress(DevParams P, int np, const DevClock *__restrict__ 
 				sadd_to(Si, sscale(-2, saddv(sscale(YM[0], t2i), sscale(YM[1], t2j))));
 				sadd_to(Sj, sscale(-2, saddv(sscale(YM[2], t2i), sscale(YM[3], t2j))));
 			}
-			int slot = sc_gu_slot(cc);
-			for (int e = 0; e < 6; e++) { o[12*slot+e] = Si.e[e]; o[12*slot+6+e] = Sj.e[e]; }
+		} else if (lub && slot == SC_ME) {
+			// ME (Lubrication::addMEStresslet)
+			double XM[4], YM[4];
+			for (int k = 0; k < 4; k++) {
+				XM[k] = c.lc[CXM+k]*q.lub_coeff;
+				YM[k] = c.lc[CYM+k]*q.log_lub_coeff;
+			}
+			s2 nn = outer(nv);
+			double nnE = vdot(nv, sdot(clk->Einf, nv));
+			double coeff = 1.5*nnE;
+			Si = sscale(coeff*(XM[0]+XM[1]), nn);
+			Sj = sscale(coeff*(XM[2]+XM[3]), nn);
+			if (P.tangential) {
+				v3 En = sdot(clk->Einf, nv);
+				s2 T = sscale(2, ssub(outer_sym(nv, En), sscale(nnE, nn)));
+				sadd_to(Si, sscale(YM[0]+YM[1], T));
+				sadd_to(Sj, sscale(YM[2]+YM[3], T));
+			}
+		} else if (slot == SC_XF_CONTACT || slot == SC_XF_RATEINDEP || slot == SC_XF_RATEPROP) {
+			v3 rv = ld3(q.rvec);
+			double r_ij = c.a0+c.a1;
+			if (P.control == 0) {
+				if (slot == SC_XF_CONTACT && (flags & PF_CONTACT)) {
+					// Contact::addUpStress with total velocities
+					v3 F = vadd(ld3(q.fs_total), dashpot_force_p0(P, clk->vel_diff, q, c, ld3(vel+3*i),
+					                                             ld3(vel+3*j), ld3(ang+3*i), ld3(ang+3*j), true));
+					s2 XF = outer_sym(rv, F);
+					for (int e = 0; e < 6; e++) q.xf_contact[e] = XF.e[e];   // Contact::calcContactStress (Contact.cpp:439-450)
+					Si = sscale(c.a0/r_ij, XF);
+					Sj = sscale(c.a1/r_ij, XF);
+				}
+			} else if (slot == SC_XF_RATEINDEP) {
+				if (flags & PF_CONTACT) {
+					s2 sp = outer_sym(rv, ld3(q.fs_total));
+					sadd_to(Si, sscale(c.a0/r_ij, sp));
+					sadd_to(Sj, sscale(c.a1/r_ij, sp));
+				}
+				if (flags & PF_DASHPOT) {
+					const double *si = split+12*i, *sj = split+12*j;
+					s2 ri = outer_sym(rv, dashpot_force_p0(P, clk->vel_diff, q, c, ld3(si+6), ld3(sj+6), ld3(si+9),
+					                                       ld3(sj+9), false));
+					sadd_to(Si, sscale(c.a0/r_ij, ri));
+					sadd_to(Sj, sscale(c.a1/r_ij, ri));
+				}
+			} else if (slot == SC_XF_RATEPROP && (flags & PF_DASHPOT)) {
+				const double *si = split+12*i, *sj = split+12*j;
+				s2 rp = outer_sym(rv, dashpot_force_p0(P, clk->vel_diff, q, c, ld3(si), ld3(sj), ld3(si+3), ld3(sj+3),
+				                                       true));
+				sadd_to(Si, sscale(c.a0/r_ij, rp));
+				sadd_to(Sj, sscale(c.a1/r_ij, rp));
+			}
+		} else if (slot == SC_XF_REPULSION && P.repulsiveforce) {
+			v3 rv = ld3(q.rvec);
+			v3 F = vscale(-(P.repulsion*q.rep_reduced), nv);
+			Si = sscale(0.5, outer_sym(rv, F));
+			Sj = Si;
 		}
-		// ME (Lubrication::addMEStresslet)
-		double nnE = vdot(nv, sdot(clk->Einf, nv));
-		double coeff = 1.5*nnE;
-		Si = sscale(coeff*(XM[0]+XM[1]), nn);
-		Sj = sscale(coeff*(XM[2]+XM[3]), nn);
-		if (P.tangential) {
-			v3 En = sdot(clk->Einf, nv);
-			s2 T = sscale(2, ssub(outer_sym(nv, En), sscale(nnE, nn)));
-			sadd_to(Si, sscale(YM[0]+YM[1], T));
-			sadd_to(Sj, sscale(YM[2]+YM[3], T));
-		}
-		for (int e = 0; e < 6; e++) { o[12*SC_ME+e] = Si.e[e]; o[12*SC_ME+6+e] = Sj.e[e]; }
 	}
-	v3 rv = ld3(q.rvec);
-	double r_ij = c.a0+c.a1;
-	if (P.control == 0) {
-		if (q.flags & PF_CONTACT) {
-			// Contact::addUpStress with total velocities
-			v3 F = vadd(ld3(q.fs_total), dashpot_force_p0(P, clk->vel_diff, q, c, ld3(vel+3*i), ld3(vel+3*j),
-			                                             ld3(ang+3*i), ld3(ang+3*j), true));
-			s2 XF = outer_sym(rv, F);
-			for (int e = 0; e < 6; e++) q.xf_contact[e] = XF.e[e];   // Contact::calcContactStress (Contact.cpp:439-450)
-			s2 a = sscale(c.a0/r_ij, XF), b = sscale(c.a1/r_ij, XF);
-			for (int e = 0; e < 6; e++) { o[12*SC_XF_CONTACT+e] = a.e[e]; o[12*SC_XF_CONTACT+6+e] = b.e[e]; }
-		}
-	} else {
-		s2 pi_ = szero(), pj_ = szero(), ii_ = szero(), ij_ = szero();
-		if (q.flags & PF_CONTACT) {
-			s2 sp = outer_sym(rv, ld3(q.fs_total));
-			sadd_to(ii_, sscale(c.a0/r_ij, sp));
-			sadd_to(ij_, sscale(c.a1/r_ij, sp));
-		}
-		if (q.flags & PF_DASHPOT) {
-			const double *si = split+12*i, *sj = split+12*j;
-			s2 rp = outer_sym(rv, dashpot_force_p0(P, clk->vel_diff, q, c, ld3(si), ld3(sj), ld3(si+3), ld3(sj+3), true));
-			sadd_to(pi_, sscale(c.a0/r_ij, rp));
-			sadd_to(pj_, sscale(c.a1/r_ij, rp));
-			s2 ri = outer_sym(rv, dashpot_force_p0(P, clk->vel_diff, q, c, ld3(si+6), ld3(sj+6), ld3(si+9), ld3(sj+9), false));
-			sadd_to(ii_, sscale(c.a0/r_ij, ri));
-			sadd_to(ij_, sscale(c.a1/r_ij, ri));
-		}
-		for (int e = 0; e < 6; e++) {
-			o[12*SC_XF_RATEPROP+e] = pi_.e[e]; o[12*SC_XF_RATEPROP+6+e] = pj_.e[e];
-			o[12*SC_XF_RATEINDEP+e] = ii_.e[e]; o[12*SC_XF_RATEINDEP+6+e] = ij_.e[e];
-		}
-	}
-	if (P.repulsiveforce) {
-		v3 F = vscale(-(P.repulsion*q.rep_reduced), nv);
-		s2 sc = sscale(0.5, outer_sym(rv, F));
-		for (int e = 0; e < 6; e++) { o[12*SC_XF_REPULSION+e] = sc.e[e]; o[12*SC_XF_REPULSION+6+e] = sc.e[e]; }
-	}
+	for (int e = 0; e < 6; e++) { o[e] = Si.e[e]; o[6+e] = Sj.e[e]; }
 }
 
 // Per-pair quantities of the output files (Simulation::outputData,
@@ -1649,8 +1658,8 @@ void phys_stresslets(DevSim &S, int in_predictor, cudaStream_t st)
 		S.launches++;
 	}
 	if (S.npairs)
-		k_pair_stress<<<blocks_for(S.npairs, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst, S.vc,
-		                                                         S.vel, S.ang, split, S.n, S.pair_scratch);
+		k_pair_stress<<<blocks_for(S.npairs*NSC, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst, S.vc,
+		                                                             S.vel, S.ang, split, S.n, S.pair_scratch);
 	k_gather_pairs<<<blocks_for(6*NSC*S.n, 256), 256, 0, st>>>(S.n, NSC, 12*NSC, S.row_ptr, S.col_ptr, S.col_idx,
 	                                                     S.pair_scratch, S.sc);
 	if (S.P.brownian_on) {
