@@ -150,6 +150,26 @@ def run_engine(E, packing, precision, steps, warmup, device):
     return ms, kernels, timing, sc
 
 
+def fp32_accuracy(E, packing, device):
+    """One step of the FP32+refine form against the FP64 form from the same
+    state (same workload): max relative differences of the velocities, the
+    angular velocities and the total stress, with the refinement's counts."""
+    params = workload_params()
+    out = {}
+    for prec in (E.PREC_FP64, E.PREC_FP32_REFINE):
+        g = E.Sim(params, packing.position, packing.radius, packing.lx, packing.ly, packing.lz,
+                  precision=prec, device=device)
+        g.step(calc_stress=True)
+        out[prec] = (g.particles(), g.scalars())
+        g.close()
+    (p64, s64), (p32, s32) = out[E.PREC_FP64], out[E.PREC_FP32_REFINE]
+    rel = lambda a, b: float(np.abs(np.asarray(a) - np.asarray(b)).max() / np.abs(np.asarray(b)).max())
+    return {"vel": rel(p32["vel"], p64["vel"]), "ang": rel(p32["ang"], p64["ang"]),
+            "total_stress": rel(s32["total_stress"], s64["total_stress"]),
+            "refine_iters": int(s32["last_refine_iters"]), "refine_residual": float(s32["last_refine_residual"]),
+            "note": "one predictor-corrector step from the same state, FP32 factor + FP64 refinement vs FP64 factor"}
+
+
 def run_e2e(E, packing, precision, steps, device):
     """Create from host arrays, K steps, each followed by a D2H read of the state."""
     import ctypes as C
@@ -453,6 +473,8 @@ def main():
         res["fp64_p99_ms"] = float(np.percentile(ms64, 99))
         res["fp64_stage_ms"] = dict(zip(["pairs", "assembly", "factor", "solve", "forces_stress", "move"],
                                         tim64["ms"][:6]))
+        if rank == 0:
+            res["fp32_vs_fp64"] = fp32_accuracy(E, pk, local)
     if rank != 0:
         return
     hbm, bf16, bf16s, src = measured_peaks()
