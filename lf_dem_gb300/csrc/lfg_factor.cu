@@ -32,8 +32,8 @@
 
 namespace lfg {
 
-enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLAN_SYRK = 5,
-       PLAN_DIAG = 6, PLAN_SYRK_TC = 8 };
+enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER = 1, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLAN_SYRK = 5, PLAN_DIAG = 6,
+       PLAN_SYRK_TC = 8 };
 constexpr int PANEL_ROWS = 64;   // rows per panel (k_trsm) task (must match the plan)
 constexpr int SOLVE_WARPS = 8;
 constexpr int SOLVE_CB = 8;      // columns per CTA of the solve's column kernels
@@ -172,59 +172,55 @@ __global__ void __launch_bounds__(256) k_assemble(const int *__restrict__ col_ta
 		for (int r = threadIdx.x; r < n6; r += blockDim.x) col[F6+r] = (r == c) ? T(1) : T(0);
 }
 
+// R_FU blocks of one level added into its fronts, one thread per block: the
+// level's diagonal blocks (threads < nd), then its off-diagonal blocks.  The
+// two kinds never share a front entry (an off-diagonal block joins two
+// different particles), so one launch adds both.
 template <typename T>
-__global__ void k_scatter_d(int count, const int *__restrict__ list, const double *__restrict__ dblocks,
-                            const int *__restrict__ d_sn, const int *__restrict__ d_bc,
-                            const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
-                            T *__restrict__ arena)
+__global__ void k_scatter(int nd, int nod, const int *__restrict__ dlist, const int *__restrict__ odlist,
+                          const double *__restrict__ dblocks, const double *__restrict__ odblocks,
+                          const int *__restrict__ d_sn, const int *__restrict__ d_bc, const int *__restrict__ od_sn,
+                          const int *__restrict__ od_br, const int *__restrict__ od_bc, const int *__restrict__ od_tr,
+                          const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off, T *__restrict__ arena)
 {
 	int t = blockIdx.x*blockDim.x+threadIdx.x;
-	if (t >= count) return;
-	int i = list[t];
-	int s = d_sn[i], b = d_bc[i], ld = sn_ld[s];
-	T *base = arena+sn_off[s];
-	pdl_wait();
+	if (t >= nd+nod) return;
 	double m[36];
-	d15_to_dense(dblocks+15*(int64_t)i, m);
-	// all 21 old values are loaded before the first store (a store between
-	// them would serialise the loads: the addresses may alias)
-	T old[21];
+	if (t < nd) {
+		int i = dlist[t];
+		int s = d_sn[i], b = d_bc[i], ld = sn_ld[s];
+		T *base = arena+sn_off[s];
+		pdl_wait();
+		d15_to_dense(dblocks+15*(int64_t)i, m);
+		// all 21 old values are loaded before the first store (a store between
+		// them would serialise the loads: the addresses may alias)
+		T old[21];
 #pragma unroll
-	for (int c = 0, e = 0; c < 6; c++)
+		for (int c = 0, e = 0; c < 6; c++)
 #pragma unroll
-		for (int r = c; r < 6; r++, e++) old[e] = base[(int64_t)(6*b+c)*ld+6*b+r];
+			for (int r = c; r < 6; r++, e++) old[e] = base[(int64_t)(6*b+c)*ld+6*b+r];
 #pragma unroll
-	for (int c = 0, e = 0; c < 6; c++)
+		for (int c = 0, e = 0; c < 6; c++)
 #pragma unroll
-		for (int r = c; r < 6; r++, e++) base[(int64_t)(6*b+c)*ld+6*b+r] = old[e]+(T)m[r*6+c];
-}
-
-template <typename T>
-__global__ void k_scatter_od(int count, const int *__restrict__ list, const double *__restrict__ odblocks,
-                             const int *__restrict__ od_sn, const int *__restrict__ od_br,
-                             const int *__restrict__ od_bc, const int *__restrict__ od_tr,
-                             const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
-                             T *__restrict__ arena)
-{
-	int t = blockIdx.x*blockDim.x+threadIdx.x;
-	if (t >= count) return;
-	int e = list[t];
-	int s = od_sn[e], br = od_br[e], bc = od_bc[e], ld = sn_ld[s];
-	T *base = arena+sn_off[s];
-	bool tr = od_tr[e];
-	pdl_wait();
-	double m[36];
-	od18_to_dense(odblocks+18*(int64_t)e, m);
-	T old[36];
+			for (int r = c; r < 6; r++, e++) base[(int64_t)(6*b+c)*ld+6*b+r] = old[e]+(T)m[r*6+c];
+	} else {
+		int e = odlist[t-nd];
+		int s = od_sn[e], br = od_br[e], bc = od_bc[e], ld = sn_ld[s];
+		T *base = arena+sn_off[s];
+		bool tr = od_tr[e];
+		pdl_wait();
+		od18_to_dense(odblocks+18*(int64_t)e, m);
+		T old[36];
 #pragma unroll
-	for (int c = 0; c < 6; c++)
+		for (int c = 0; c < 6; c++)
 #pragma unroll
-		for (int r = 0; r < 6; r++) old[6*c+r] = base[(int64_t)(6*bc+c)*ld+6*br+r];
+			for (int r = 0; r < 6; r++) old[6*c+r] = base[(int64_t)(6*bc+c)*ld+6*br+r];
 #pragma unroll
-	for (int c = 0; c < 6; c++)
+		for (int c = 0; c < 6; c++)
 #pragma unroll
-		for (int r = 0; r < 6; r++)
-			base[(int64_t)(6*bc+c)*ld+6*br+r] = old[6*c+r]+(T)(tr ? m[c*6+r] : m[r*6+c]);
+			for (int r = 0; r < 6; r++)
+				base[(int64_t)(6*bc+c)*ld+6*br+r] = old[6*c+r]+(T)(tr ? m[c*6+r] : m[r*6+c]);
+	}
 }
 
 // ---------------------------------------------------------------------------
@@ -1288,16 +1284,15 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 			           (const int *)D.child_off, (const int *)D.children, (const int64_t *)D.cinv_off,
 			           (const int *)D.cinv, (const int *)D.sn_rows_off, (const int *)D.cfwd, F.arena);
 			break;
-		case PLAN_SCATTER_D:
-			launch_pdl(k_scatter_d<T>, (L.count+127)/128, 128, 0, st, L.count, (const int *)D.level_d+L.off, dbl,
-			           (const int *)D.d_sn, (const int *)D.d_bc, (const int *)D.sn_ld, (const int64_t *)D.sn_off,
-			           F.arena);
-			break;
-		case PLAN_SCATTER_OD:
-			launch_pdl(k_scatter_od<T>, (L.count+127)/128, 128, 0, st, L.count, (const int *)D.level_od+L.off, odbl,
+		case PLAN_SCATTER: {
+			int d0 = D.h_level_d_off[L.level], nd = D.h_level_d_off[L.level+1]-d0;
+			int o0 = D.h_level_od_off[L.level], nod = D.h_level_od_off[L.level+1]-o0;
+			launch_pdl(k_scatter<T>, (nd+nod+127)/128, 128, 0, st, nd, nod, (const int *)D.level_d+d0,
+			           (const int *)D.level_od+o0, dbl, odbl, (const int *)D.d_sn, (const int *)D.d_bc,
 			           (const int *)D.od_sn, (const int *)D.od_br, (const int *)D.od_bc, (const int *)D.od_tr,
 			           (const int *)D.sn_ld, (const int64_t *)D.sn_off, F.arena);
 			break;
+		}
 		case PLAN_DIAG:
 			launch_pdl(k_diag<T>, L.count, 128, 0, st, (const int4 *)D.diag_tasks+L.off, (const int *)D.sn_first,
 			           (const int *)D.sn_ld, (const int64_t *)D.sn_off, F.arena, F.linv, D.nsn, F.status);

@@ -597,8 +597,8 @@ void dev_symbolic_free(DevSymbolic &D)
 }
 
 // Launch kinds of the factor plan (interpreted by factor_numeric).
-enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER_D = 1, PLAN_SCATTER_OD = 2, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLAN_SYRK = 5,
-       PLAN_DIAG = 6, PLAN_SYRK_TC = 8 };
+enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER = 1, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLAN_SYRK = 5, PLAN_DIAG = 6,
+       PLAN_SYRK_TC = 8 };
 
 // levels whose largest front has at least this many pivot columns compute the
 // Schur complement on the tensor cores; below, the K loop is a few chunks and
@@ -651,8 +651,10 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 			kmax = std::max(kmax, (6*S.sn_n[s]+panel_nb-1)/panel_nb);
 		}
 		D.factor_plan.push_back({PLAN_ASSEMBLE, l, 0, c0, (int)((int64_t)col_tasks.size()/2-c0)});
-		D.factor_plan.push_back({PLAN_SCATTER_D, l, 0, S.level_d_off[l], S.level_d_off[l+1]-S.level_d_off[l]});
-		D.factor_plan.push_back({PLAN_SCATTER_OD, l, 0, S.level_od_off[l], S.level_od_off[l+1]-S.level_od_off[l]});
+		// one launch for the level's diagonal and off-diagonal blocks (ranges
+		// from h_level_d_off / h_level_od_off)
+		D.factor_plan.push_back({PLAN_SCATTER, l, 0, 0,
+		                         (S.level_d_off[l+1]-S.level_d_off[l])+(S.level_od_off[l+1]-S.level_od_off[l])});
 		// diagonal blocks of panel 0 (later panels' are factored by the update
 		// launch of the panel before)
 		{
