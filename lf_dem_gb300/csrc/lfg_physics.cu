@@ -806,24 +806,19 @@ __global__ void k_dblocks(DevParams P, int n, const double *__restrict__ radius,
                           const int *__restrict__ col_ptr, const int *__restrict__ col_idx,
                           const double *__restrict__ bscr, double *__restrict__ dbl)
 {
-	int i = blockIdx.x*blockDim.x+threadIdx.x;
-	if (i >= n) return;
-	double d[15];
-	for (int k = 0; k < 15; k++) d[k] = 0;
+	// one thread per (particle, entry of its 15-value block): the pairs'
+	// contributions to that entry in the reference's order (p1 == i first,
+	// then p0 == i); adjacent threads read adjacent entries of a record
+	int64_t tt = (int64_t)blockIdx.x*blockDim.x+threadIdx.x;
+	if (tt >= 15*(int64_t)n) return;
+	int i = (int)(tt/15), e = (int)(tt%15);
 	double a = radius[i];
-	double FU = P.sd_coeff*a;
-	double TW = P.sd_coeff*pow(a, 3)*4.0/3;
-	d[0] = FU; d[5] = FU; d[8] = FU;
-	d[9] = TW; d[12] = TW; d[14] = TW;
-	for (int k = col_ptr[i]; k < col_ptr[i+1]; k++) {
-		const double *b1 = bscr+30*(int64_t)col_idx[k]+15;
-		for (int e = 0; e < 15; e++) d[e] += b1[e];
-	}
-	for (int t = row_ptr[i]; t < row_ptr[i+1]; t++) {
-		const double *b0 = bscr+30*(int64_t)t;
-		for (int e = 0; e < 15; e++) d[e] += b0[e];
-	}
-	for (int k = 0; k < 15; k++) dbl[15*(int64_t)i+k] = d[k];
+	double d = 0;
+	if (e == 0 || e == 5 || e == 8) d = P.sd_coeff*a;
+	else if (e == 9 || e == 12 || e == 14) d = P.sd_coeff*pow(a, 3)*4.0/3;
+	for (int k = col_ptr[i]; k < col_ptr[i+1]; k++) d += bscr[30*(int64_t)col_idx[k]+15+e];
+	for (int t = row_ptr[i]; t < row_ptr[i+1]; t++) d += bscr[30*(int64_t)t+e];
+	dbl[15*(int64_t)i+e] = d;
 }
 
 // ---------------------------------------------------------------------------
@@ -852,19 +847,26 @@ __global__ void k_pair_forces(DevParams P, int np, const DevClock *__restrict__ 
                               const DPairConst *__restrict__ pc, const double *__restrict__ u_inf,
                               double *__restrict__ scr)
 {
-	int t = blockIdx.x*blockDim.x+threadIdx.x;
-	if (t >= np) return;
+	// one thread per (force component, pair), component-major (a warp's pairs
+	// share the component's branch): it writes the component's 12 values (the
+	// pair's p0 and p1 force and torque), zero where it does not apply
+	int64_t tt = (int64_t)blockIdx.x*blockDim.x+threadIdx.x;
+	if (tt >= (int64_t)np*NPFC) return;
+	int t = (int)(tt%np), comp = (int)(tt/np);
+	double ov[12];
+	for (int k = 0; k < 12; k++) ov[k] = 0;
 	const DPair &q = pairs[t];
-	double *o = scr+48*(int64_t)t;
-	for (int k = 0; k < 48; k++) o[k] = 0;
-	if (!(q.flags & PF_INTER)) return;
+	if (!(q.flags & PF_INTER)) {
+		for (int k = 0; k < 12; k++) scr[48*(int64_t)t+12*comp+k] = 0;
+		return;
+	}
 	const DPairConst &c = pc[t];
 	v3 n = ld3(q.nvec);
 	// contact (Contact::addUpForceTorque, Contact.cpp:419-437)
-	if (q.flags & PF_CONTACT) {
+	if (comp == FC_CONTACT && (q.flags & PF_CONTACT)) {
 		v3 f = ld3(q.fs_total);
-		st3(o+0, f);
-		st3(o+6, vneg(f));
+		st3(ov+0, f);
+		st3(ov+6, vneg(f));
 		if (q.state >= 2) {
 			v3 tq = vcross(n, ld3(q.fs_tan));
 			v3 t0 = vscale(c.a0, tq), t1 = vscale(c.a1, tq);
@@ -874,23 +876,23 @@ __global__ void k_pair_forces(DevParams P, int np, const DevClock *__restrict__ 
 				t0 = vadd(t0, vscale(c.a0, tr));
 				t1 = vsub(t1, vscale(c.a1, tr));
 			}
-			st3(o+3, t0);
-			st3(o+9, t1);
+			st3(ov+3, t0);
+			st3(ov+9, t1);
 		}
 	}
 	// dashpot R_FU U_inf (ContactDashpot::getRFU_Uinf, :426-441)
-	if ((q.flags & PF_CONTACT) && (q.flags & PF_DASHPOT)) {
+	if (comp == FC_DASHPOT && (q.flags & PF_CONTACT) && (q.flags & PF_DASHPOT)) {
 		v3 om = V(clk->Omega[0], clk->Omega[1], clk->Omega[2]);
 		v3 f0 = dashpot_force_p0(P, clk->vel_diff, q, c, ld3(u_inf+3*q.p0), ld3(u_inf+3*q.p1), om, om, true);
 		v3 t0 = vzero();
 		if (P.dp_tan_coeff > 0) t0 = vscale(c.a0, vcross(n, f0));
-		st3(o+12, f0);
-		st3(o+15, t0);
-		st3(o+18, vneg(f0));
-		st3(o+21, vscale(c.a1/c.a0, t0));
+		st3(ov+0, f0);
+		st3(ov+3, t0);
+		st3(ov+6, vneg(f0));
+		st3(ov+9, vscale(c.a1/c.a0, t0));
 	}
 	// hydro (Lubrication::calcGEHE_squeeze_tangential / calcGE_squeeze, :332-403)
-	if (P.lub_on && (q.flags & PF_LUB)) {
+	if (comp == FC_HYDRO && P.lub_on && (q.flags & PF_LUB)) {
 		double XG[4], YG[4], YH[4];
 		for (int k = 0; k < 4; k++) {
 			XG[k] = c.lc[CXG+k]*q.lub_coeff;
@@ -900,27 +902,28 @@ __global__ void k_pair_forces(DevParams P, int np, const DevClock *__restrict__ 
 		double nnE = vdot(n, sdot(clk->Einf, n));
 		if (!P.tangential) {
 			double ci = (XG[0]+XG[2])*nnE, cj = (XG[1]+XG[3])*nnE;
-			st3(o+24, V(ci*n.x, ci*n.y, ci*n.z));
-			st3(o+30, V(cj*n.x, cj*n.y, cj*n.z));
+			st3(ov+0, V(ci*n.x, ci*n.y, ci*n.z));
+			st3(ov+6, V(cj*n.x, cj*n.y, cj*n.z));
 		} else {
 			double YG0_YG2 = YG[0]+YG[2], YG1_YG3 = YG[1]+YG[3];
 			double cGE_i = (XG[0]+XG[2]-2*YG0_YG2)*nnE;
 			double cGE_j = (XG[1]+XG[3]-2*YG1_YG3)*nnE;
 			double cHE_i = YH[0]+YH[2], cHE_j = YH[1]+YH[3];
 			v3 En = sdot(clk->Einf, n);
-			st3(o+24, vadd(vscale(cGE_i, n), vscale(YG0_YG2*2, En)));
-			st3(o+30, vadd(vscale(cGE_j, n), vscale(YG1_YG3*2, En)));
+			st3(ov+0, vadd(vscale(cGE_i, n), vscale(YG0_YG2*2, En)));
+			st3(ov+6, vadd(vscale(cGE_j, n), vscale(YG1_YG3*2, En)));
 			v3 nExn = vcross(En, n);
-			st3(o+27, vscale(-2*cHE_i, nExn));
-			st3(o+33, vscale(-2*cHE_j, nExn));
+			st3(ov+3, vscale(-2*cHE_i, nExn));
+			st3(ov+9, vscale(-2*cHE_j, nExn));
 		}
 	}
 	// repulsion (RepulsiveForce::addUpForce, :101-105)
-	if (P.repulsiveforce) {
+	if (comp == FC_REPULSION && P.repulsiveforce) {
 		v3 f = ld3(q.rep_force);
-		st3(o+36, f);
-		st3(o+42, vneg(f));
+		st3(ov+0, f);
+		st3(ov+6, vneg(f));
 	}
+	for (int k = 0; k < 12; k++) scr[48*(int64_t)t+12*comp+k] = ov[k];
 }
 
 // per particle gather: components c with stride 12 in scratch of width W
@@ -1521,7 +1524,7 @@ void phys_blocks(DevSim &S, double *dbl, double *odbl, cudaStream_t st)
 {
 	if (S.npairs)
 		k_pair_blocks<<<blocks_for(S.npairs, 128), 128, 0, st>>>(S.P, S.npairs, S.pairs, S.pconst, odbl, S.blk_scratch);
-	k_dblocks<<<blocks_for(S.n, 128), 128, 0, st>>>(S.P, S.n, S.radius, S.row_ptr, S.col_ptr, S.col_idx,
+	k_dblocks<<<blocks_for(15*(int64_t)S.n, 128), 128, 0, st>>>(S.P, S.n, S.radius, S.row_ptr, S.col_ptr, S.col_idx,
 	                                                S.blk_scratch, dbl);
 	S.launches += 2;
 }
@@ -1529,8 +1532,8 @@ void phys_blocks(DevSim &S, double *dbl, double *odbl, cudaStream_t st)
 void phys_force_components(DevSim &S, cudaStream_t st)
 {
 	if (S.npairs)
-		k_pair_forces<<<blocks_for(S.npairs, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst, S.u_inf,
-		                                                         S.pair_scratch);
+		k_pair_forces<<<blocks_for((int64_t)S.npairs*NPFC, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst,
+		                                                                       S.u_inf, S.pair_scratch);
 	k_gather_pairs<<<blocks_for(6*NPFC*S.n, 256), 256, 0, st>>>(S.n, NPFC, 12*NPFC, S.row_ptr, S.col_ptr,
 	                                                      S.col_idx, S.pair_scratch, S.fc);
 	S.launches += 2;
@@ -1576,8 +1579,8 @@ void phys_force_component_into(DevSim &S, int comp, double *scr, double *out, cu
 	if (S.npairs > NOALLOC_MAX_PAIRS)
 		throw Error{LFG_ERR_BAD_ARG, S.npairs, "pair slots exceed the no-allocation scratch (32768)"};
 	if (S.npairs)
-		k_pair_forces<<<blocks_for(S.npairs, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst, S.u_inf,
-		                                                         scr);
+		k_pair_forces<<<blocks_for((int64_t)S.npairs*NPFC, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst,
+		                                                                       S.u_inf, scr);
 	k_gather_pairs<<<blocks_for(6*S.n, 256), 256, 0, st>>>(S.n, 1, 48, S.row_ptr, S.col_ptr, S.col_idx, scr+12*comp,
 	                                                     out);
 	S.launches += 2;
