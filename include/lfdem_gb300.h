@@ -147,8 +147,8 @@ int lfg_checkpoint_read(const char *path, double *strain, double *time, double *
 typedef struct {
 	int precision;          /* LFG_PREC_* */
 	int device;             /* CUDA device ordinal */
-	double refine_tol;      /* relative residual target of the FP32 form (default 1e-9: two
-	                           iterations, velocities within ~1e-11 of the FP64 form) */
+	double refine_tol;      /* relative residual target of the FP32 form (default 2e-10: two
+	                           iterations at N=4096, velocities within ~1e-11 of the FP64 form) */
 	int refine_max_iter;    /* default 30 */
 	double skin;            /* pair superset skin, units of (a_i+a_j)/2 (default 0.15) */
 	int use_graphs;         /* capture factor/solve launch sequences in CUDA graphs (default 1) */

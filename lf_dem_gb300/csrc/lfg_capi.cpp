@@ -66,7 +66,7 @@ void lfg_default_options(lfg_options *o)
 	std::memset(o, 0, sizeof *o);
 	o->precision = LFG_PREC_FP64;
 	o->device = 0;
-	o->refine_tol = 1e-9;
+	o->refine_tol = 2e-10;
 	o->refine_max_iter = 30;
 	o->skin = 0.15;
 	o->use_graphs = 1;

@@ -35,7 +35,7 @@ def test_default_options(lib):
     import lf_dem_gb300 as E
     E._lib = None
     o = E.default_options()
-    assert o.precision == E.PREC_FP64 and o.use_graphs == 1 and o.refine_tol == 1e-9
+    assert o.precision == E.PREC_FP64 and o.use_graphs == 1 and o.refine_tol == 2e-10
 
 
 def test_no_device_reports_cleanly(lib):

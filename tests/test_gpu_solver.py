@@ -39,7 +39,7 @@ def test_fp64_solve_matches_oracle(oracle, engine, n, vf, seed):
 @pytest.mark.parametrize("n,vf,seed", [(500, 0.5, 13)])
 def test_fp32_refine_matches_oracle(oracle, engine, n, vf, seed, refine_tol, bound):
     """FP32 factor + FP64 refinement against the oracle's FP64 solve: with a
-    tight tolerance to the FP64 form's accuracy, with the default one (1e-9
+    tight tolerance to the FP64 form's accuracy, with the default one (2e-10
     relative residual) within the 1e-8 target."""
     p, o, d15, r, c, o18 = _assembled(oracle, n, vf, seed)
     rng = np.random.default_rng(seed)
@@ -53,7 +53,7 @@ def test_fp32_refine_matches_oracle(oracle, engine, n, vf, seed, refine_tol, bou
     rel = np.abs(x - x_ref).max() / np.abs(x_ref).max()
     assert rel < bound, rel
     assert s.last.refine_iters >= 1
-    assert s.last.refine_residual <= (refine_tol or 1e-9)
+    assert s.last.refine_residual <= (refine_tol or 2e-10)
 
 
 def test_not_spd_reported(oracle, engine):
