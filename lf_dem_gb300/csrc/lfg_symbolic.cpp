@@ -601,12 +601,13 @@ enum { PLAN_ASSEMBLE = 0, PLAN_SCATTER = 1, PLAN_PANEL = 3, PLAN_UPDATE = 4, PLA
        PLAN_SYRK_TC = 8 };
 
 // levels whose largest front has at least this many pivot columns compute the
-// Schur complement on the tensor cores (measured faster down to 6n = 64 at
-// N = 4096; the CUDA-core kernel takes the smallest levels).  (The in-front
+// Schur complement on the tensor cores: all of them in FP32 (at N = 4096 the
+// tensor-core kernel was faster down to 6n = 64 and no slower below); FP64
+// uses the CUDA-core kernel.  (The in-front
 // update of a panel step has K = 64 only: on the tensor cores its tiles cost
 // the same staging and read-modify-write and ran slower, so it stays on the
 // CUDA cores.)
-constexpr int TC_SYRK_MIN_N6 = 64;
+constexpr int TC_SYRK_MIN_N6 = 0;
 
 void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb, int tile, int syrk_tile,
                          bool tensor_cores, cudaStream_t st)
