@@ -1866,27 +1866,41 @@ void axpy_vec(int n, int k, const double *d, double *x, cudaStream_t st)
 }
 
 // per-RHS sums of squares of r and b, single CTA per RHS (fixed order)
-__global__ void k_norms(int n6, const double *__restrict__ r, const double *__restrict__ b, double *out)
+// squared norms of r and b per right-hand side (one CTA of 1024 threads each;
+// a fixed reduction order: per thread, then warps by shuffles, then warps)
+__global__ void __launch_bounds__(1024) k_norms(int n6, const double *__restrict__ r, const double *__restrict__ b,
+                                                double *out)
 {
-	__shared__ double sr[256], sb[256];
+	__shared__ double sr[32], sb[32];
 	int rh = blockIdx.x;
 	double a = 0, c = 0;
-	for (int i = threadIdx.x; i < n6; i += 256) {
+#pragma unroll 4
+	for (int i = threadIdx.x; i < n6; i += blockDim.x) {
 		double u = r[(int64_t)rh*n6+i], v = b[(int64_t)rh*n6+i];
-		a += u*u; c += v*v;
+		a += u*u;
+		c += v*v;
 	}
-	sr[threadIdx.x] = a; sb[threadIdx.x] = c;
+	for (int o = 16; o > 0; o >>= 1) {
+		a += __shfl_down_sync(FULL_MASK, a, o);
+		c += __shfl_down_sync(FULL_MASK, c, o);
+	}
+	int w = threadIdx.x/32, l = threadIdx.x%32;
+	if (l == 0) { sr[w] = a; sb[w] = c; }
 	__syncthreads();
-	for (int o = 128; o > 0; o >>= 1) {
-		if (threadIdx.x < o) { sr[threadIdx.x] += sr[threadIdx.x+o]; sb[threadIdx.x] += sb[threadIdx.x+o]; }
-		__syncthreads();
+	if (w == 0) {
+		a = l < (int)blockDim.x/32 ? sr[l] : 0.0;
+		c = l < (int)blockDim.x/32 ? sb[l] : 0.0;
+		for (int o = 16; o > 0; o >>= 1) {
+			a += __shfl_down_sync(FULL_MASK, a, o);
+			c += __shfl_down_sync(FULL_MASK, c, o);
+		}
+		if (l == 0) { out[2*rh] = a; out[2*rh+1] = c; }
 	}
-	if (threadIdx.x == 0) { out[2*rh] = sr[0]; out[2*rh+1] = sb[0]; }
 }
 
 void residual_norms(int n6, int k, const double *r, const double *b, double *out, cudaStream_t st)
 {
-	k_norms<<<k, 256, 0, st>>>(n6, r, b, out);
+	k_norms<<<k, 1024, 0, st>>>(n6, r, b, out);
 }
 
 int factor_tile_size(int precision) { return precision == LFG_PREC_FP64 ? Cfg<double>::TILE : Cfg<float>::TILE; }

@@ -1187,22 +1187,30 @@ __global__ void k_pair_output(DevParams P, int np, const DevClock *__restrict__ 
 }
 
 // per-component totals over particles (fixed-order tree reduction)
-__global__ void k_stress_totals(int n, const double *__restrict__ sc, double *__restrict__ tot)
+// per stresslet component, the sum over particles (one CTA of 1024 threads
+// each; a fixed reduction order: per thread, then warps by shuffles, then
+// warps)
+__global__ void __launch_bounds__(1024) k_stress_totals(int n, const double *__restrict__ sc,
+                                                        double *__restrict__ tot)
 {
-	__shared__ double red[256][6];
+	__shared__ double red[32][6];
 	int c = blockIdx.x;
 	double a[6] = {0, 0, 0, 0, 0, 0};
 	for (int i = threadIdx.x; i < n; i += blockDim.x)
 		for (int e = 0; e < 6; e++) a[e] += sc[(int64_t)c*6*n+6*i+e];
-	for (int e = 0; e < 6; e++) red[threadIdx.x][e] = a[e];
+	for (int o = 16; o > 0; o >>= 1)
+		for (int e = 0; e < 6; e++) a[e] += __shfl_down_sync(0xffffffffu, a[e], o);
+	int w = threadIdx.x/32, l = threadIdx.x%32;
+	if (l == 0)
+		for (int e = 0; e < 6; e++) red[w][e] = a[e];
 	__syncthreads();
-	for (int o = blockDim.x/2; o > 0; o >>= 1) {
-		if (threadIdx.x < o)
-			for (int e = 0; e < 6; e++) red[threadIdx.x][e] += red[threadIdx.x+o][e];
-		__syncthreads();
+	if (w == 0) {
+		for (int e = 0; e < 6; e++) a[e] = l < (int)blockDim.x/32 ? red[l][e] : 0.0;
+		for (int o = 16; o > 0; o >>= 1)
+			for (int e = 0; e < 6; e++) a[e] += __shfl_down_sync(0xffffffffu, a[e], o);
+		if (l == 0)
+			for (int e = 0; e < 6; e++) tot[6*c+e] = a[e];
 	}
-	if (threadIdx.x == 0)
-		for (int e = 0; e < 6; e++) tot[6*c+e] = red[0][e];
 }
 
 __device__ void set_rate(const DevParams &P, DevClock &K, double rate)
@@ -1669,7 +1677,7 @@ void phys_stresslets(DevSim &S, int in_predictor, cudaStream_t st)
 		k_brownian_stress<<<blocks_for(6*S.n, 256), 256, 0, st>>>(6*S.n, in_predictor, S.sc);
 		S.launches++;
 	}
-	k_stress_totals<<<NSC, 256, 0, st>>>(S.n, S.sc, S.sc_tot);
+	k_stress_totals<<<NSC, 1024, 0, st>>>(S.n, S.sc, S.sc_tot);
 	S.launches += 3;
 }
 
