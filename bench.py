@@ -491,8 +491,12 @@ def main():
         pass
     roof = {"bound": "tensor", "achieved": achieved, "peak": bf16s, "unit": "TFLOP/s",
             "frac": achieved / bf16s, "traffic": traffic,
-            "kernel": "FP32 multifrontal factorisation (k_assemble/k_panel/k_update graph)",
-            "peak_source": f"bf16_tflops_sustained ({src}); the factorisation runs on FP32 CUDA cores",
+            "traffic_source": "profile-derived: DRAM bytes of the factorisation kernels per factorisation, "
+                              "from the ncu launch list in profiles/ (not measured in this run)",
+            "kernel": "FP32 multifrontal factorisation graph: k_assemble, k_scatter, k_diag, k_trsm, k_update "
+                      "(CUDA cores) and k_syrk_tc (Schur complements, tcgen05 3xTF32)",
+            "peak_source": f"bf16_tflops_sustained ({src}); the panel steps run on FP32 CUDA cores, "
+                           "the Schur complements on the tensor cores",
             # context: FP32 CUDA-core nominal peak, 152 SMs x 128 FMA/clk x 2 x 2.07 GHz
             "fp32_simt_nominal_tflops": 80.5, "frac_of_fp32_simt_nominal": achieved / 80.5}
     solve_ms = stage["solve"]

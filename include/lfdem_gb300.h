@@ -307,17 +307,19 @@ int lfg_sim_assemble(lfg_sim *s, double *dblocks, int32_t *od_row, int32_t *od_c
                      double *odblocks, int cap, int *nb_out);
 int lfg_sim_force_component(lfg_sim *s, int comp, double *out);
 
-/* Force component comp at the current state, like lfg_sim_force_component,
- * written to DEVICE memory d_out (6n doubles on the simulation's device),
+/* Pair-force component comp (0 contact, 1 dashpot, 2 hydro, 3 repulsion; 4,
+ * the Brownian force, is refused with LFG_ERR_BAD_ARG) at the current state,
+ * like lfg_sim_force_component, written to DEVICE memory d_out (6n doubles on
+ * the simulation's device),
  * allocating nothing: no cudaMalloc/cudaFree and no pinned staging.  This
  * entry point has no counterpart in the reference (LF_DEM keeps no device
  * memory).  It is for callers that may not allocate device memory while they
  * run: an application that owns every device allocation through its own pool
  * or arena, or one on a path where the implicit device synchronisation of
  * cudaMalloc/cudaFree is not allowed.
- *  - The per-pair intermediate goes to a fixed scratch in static device
- *    memory with room for LFG_NOALLOC_MAX_PAIRS pair slots (48 doubles each,
- *    12.6 MB per device).  A simulation whose candidate-pair list is longer
+ *  - The per-pair intermediate of the requested component goes to a fixed
+ *    scratch in static device memory with room for LFG_NOALLOC_MAX_PAIRS
+ *    pair slots (12 doubles each, 3.1 MB per device).  A simulation whose candidate-pair list is longer
  *    gets LFG_ERR_BAD_ARG; use lfg_sim_force_component there.
  *  - Neither the scratch nor d_out needs to start at zero: every value read
  *    is written earlier in the same call, and all 6n outputs are written.

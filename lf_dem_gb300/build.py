@@ -8,7 +8,9 @@ a reduced gap of exactly 0).
 from __future__ import annotations
 
 import concurrent.futures as cf
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -18,6 +20,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "liblfdem_gb300.so")
+STAMP = os.path.join(LIBDIR, "liblfdem_gb300.fingerprint")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NO_FMAD = {"lfg_physics.cu"}
 
@@ -51,14 +54,34 @@ def _compile(src: str, verbose: bool) -> str:
     return obj
 
 
+def _fingerprint(srcs) -> str:
+    """Hash of everything the library is built from: the sources, the public
+    header, this recipe, the compiler's version and the host architecture.  A
+    library is reused only when its recorded fingerprint equals this one, so a
+    copy built elsewhere (another machine, older sources) is always rebuilt."""
+    h = hashlib.sha256()
+    files = [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC))]
+    files += [os.path.join(HERE, "..", "include", "lfdem_gb300.h"), os.path.abspath(__file__)]
+    for f in files:
+        h.update(os.path.basename(f).encode())
+        with open(f, "rb") as fh:
+            h.update(fh.read())
+    ver = subprocess.run([_nvcc(), "--version"], capture_output=True, text=True).stdout
+    h.update(ver.encode())
+    h.update(platform.machine().encode())
+    h.update(" ".join(ARCH).encode())
+    return h.hexdigest()
+
+
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = sources()
-    newest_src = max(os.path.getmtime(os.path.join(CSRC, s)) for s in os.listdir(CSRC))
-    newest_src = max(newest_src, os.path.getmtime(os.path.join(HERE, "..", "include", "lfdem_gb300.h")))
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) > newest_src:
-        return LIB
+    fp = _fingerprint(srcs)
+    if not force and os.path.exists(LIB) and os.path.exists(STAMP):
+        with open(STAMP) as f:
+            if f.read().strip() == fp:
+                return LIB
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
     tmp = LIB + ".tmp"
@@ -67,6 +90,9 @@ def build(verbose: bool = False, force: bool = False) -> str:
     if out.returncode != 0:
         raise RuntimeError("link failed:\n" + out.stderr)
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as f:
+        f.write(fp + "\n")
+    sys.stderr.write(f"lf_dem_gb300: built {LIB} ({platform.machine()}, {len(srcs)} sources)\n")
     return LIB
 
 

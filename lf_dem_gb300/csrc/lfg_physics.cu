@@ -842,22 +842,24 @@ __device__ v3 dashpot_force_p0(const DevParams &P, const double *vel_diff, const
 	return f;
 }
 
-// per pair: 4 components x (F0, T0, F1, T1)
+// per pair: 4 components x (F0, T0, F1, T1) (only < 0, 48 values per pair),
+// or the one component `only` (12 values per pair)
 __global__ void k_pair_forces(DevParams P, int np, const DevClock *__restrict__ clk, const DPair *__restrict__ pairs,
                               const DPairConst *__restrict__ pc, const double *__restrict__ u_inf,
-                              double *__restrict__ scr)
+                              double *__restrict__ scr, int only)
 {
 	// one thread per (force component, pair), component-major (a warp's pairs
 	// share the component's branch): it writes the component's 12 values (the
 	// pair's p0 and p1 force and torque), zero where it does not apply
 	int64_t tt = (int64_t)blockIdx.x*blockDim.x+threadIdx.x;
-	if (tt >= (int64_t)np*NPFC) return;
-	int t = (int)(tt%np), comp = (int)(tt/np);
+	if (tt >= (int64_t)np*(only < 0 ? NPFC : 1)) return;
+	int t = (int)(tt%np), comp = only < 0 ? (int)(tt/np) : only;
+	double *dst = only < 0 ? scr+48*(int64_t)t+12*comp : scr+12*(int64_t)t;
 	double ov[12];
 	for (int k = 0; k < 12; k++) ov[k] = 0;
 	const DPair &q = pairs[t];
 	if (!(q.flags & PF_INTER)) {
-		for (int k = 0; k < 12; k++) scr[48*(int64_t)t+12*comp+k] = 0;
+		for (int k = 0; k < 12; k++) dst[k] = 0;
 		return;
 	}
 	const DPairConst &c = pc[t];
@@ -923,7 +925,7 @@ __global__ void k_pair_forces(DevParams P, int np, const DevClock *__restrict__ 
 		st3(ov+0, f);
 		st3(ov+6, vneg(f));
 	}
-	for (int k = 0; k < 12; k++) scr[48*(int64_t)t+12*comp+k] = ov[k];
+	for (int k = 0; k < 12; k++) dst[k] = ov[k];
 }
 
 // per particle gather: components c with stride 12 in scratch of width W
@@ -1541,7 +1543,7 @@ void phys_force_components(DevSim &S, cudaStream_t st)
 {
 	if (S.npairs)
 		k_pair_forces<<<blocks_for((int64_t)S.npairs*NPFC, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst,
-		                                                                       S.u_inf, S.pair_scratch);
+		                                                                       S.u_inf, S.pair_scratch, -1);
 	k_gather_pairs<<<blocks_for(6*NPFC*S.n, 256), 256, 0, st>>>(S.n, NPFC, 12*NPFC, S.row_ptr, S.col_ptr,
 	                                                      S.col_idx, S.pair_scratch, S.fc);
 	S.launches += 2;
@@ -1553,13 +1555,14 @@ void phys_force_components(DevSim &S, cudaStream_t st)
 // memory while they run: a host application that owns every device
 // allocation through its own pool, or one on a path where the implicit device
 // synchronisation of cudaMalloc/cudaFree is not allowed.  For them the
-// per-pair intermediate of k_pair_forces (48 doubles per pair slot) goes to a
-// fixed scratch in static device memory instead of DevSim::pair_scratch.
-// k_pair_forces writes all 48 values of every slot it covers before
-// k_gather_pairs reads them, so the scratch need not start at zero.  All
-// calls on one device share it: calls that overlap in time race.
+// per-pair intermediate of k_pair_forces, computed for the requested
+// component only (12 doubles per pair slot), goes to a fixed scratch in static
+// device memory instead of DevSim::pair_scratch.  k_pair_forces writes all 12
+// values of every slot it covers before k_gather_pairs reads them, so the
+// scratch need not start at zero.  All calls on one device share it: calls
+// that overlap in time race.
 // ---------------------------------------------------------------------------
-static __device__ __align__(256) double g_noalloc_pair_scratch[(size_t)NOALLOC_MAX_PAIRS*48];
+static __device__ __align__(256) double g_noalloc_pair_scratch[(size_t)NOALLOC_MAX_PAIRS*12];
 
 static std::mutex g_noalloc_mu;
 static double *g_noalloc_ptr[NOALLOC_MAX_DEVICES];
@@ -1584,13 +1587,14 @@ double *noalloc_pair_scratch(int device)
 
 void phys_force_component_into(DevSim &S, int comp, double *scr, double *out, cudaStream_t st)
 {
+	if (comp < 0 || comp >= NPFC)
+		throw Error{LFG_ERR_BAD_ARG, comp, "pair-force component must be 0..3"};
 	if (S.npairs > NOALLOC_MAX_PAIRS)
 		throw Error{LFG_ERR_BAD_ARG, S.npairs, "pair slots exceed the no-allocation scratch (32768)"};
 	if (S.npairs)
-		k_pair_forces<<<blocks_for((int64_t)S.npairs*NPFC, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst,
-		                                                                       S.u_inf, scr);
-	k_gather_pairs<<<blocks_for(6*S.n, 256), 256, 0, st>>>(S.n, 1, 48, S.row_ptr, S.col_ptr, S.col_idx, scr+12*comp,
-	                                                     out);
+		k_pair_forces<<<blocks_for((int64_t)S.npairs, 128), 128, 0, st>>>(S.P, S.npairs, S.clock, S.pairs, S.pconst,
+		                                                                  S.u_inf, scr, comp);
+	k_gather_pairs<<<blocks_for(6*S.n, 256), 256, 0, st>>>(S.n, 1, 12, S.row_ptr, S.col_ptr, S.col_idx, scr, out);
 	S.launches += 2;
 }
 

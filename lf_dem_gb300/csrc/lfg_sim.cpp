@@ -822,7 +822,9 @@ int Sim::force_component(int comp, double *out)
 // the caller's device buffer; nothing is allocated.
 void Sim::force_component_noalloc(int comp, double *d_out, int device)
 {
-	if (comp < 0 || comp >= NFC) throw Error{LFG_ERR_BAD_ARG, comp, "component must be 0..3"};
+	// the pair-force components only: the Brownian one (FC_BROWNIAN) is not a
+	// sum over pairs and has no slot in the scratch
+	if (comp < 0 || comp >= NPFC) throw Error{LFG_ERR_BAD_ARG, comp, "component must be 0..3"};
 	if (S_.npairs > NOALLOC_MAX_PAIRS)
 		throw Error{LFG_ERR_BAD_ARG, S_.npairs, "pair slots exceed the no-allocation scratch (32768)"};
 	double *scr = noalloc_pair_scratch(device);

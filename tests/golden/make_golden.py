@@ -9,7 +9,7 @@ R_FU (lower CSC) and force / velocity / stress components at that state, and
 the state after the step.  The tests replay each step from the stored state
 with the CPU oracle and with the GPU engine and compare.
 
-usage: python tests/golden/make_golden.py [case | writers_case ...]   (needs the reference tree)
+usage: LFDEM_REF=<LF_DEM source dir> make -C oracle ref && python tests/golden/make_golden.py [case | writers_case ...]
 """
 import os
 import subprocess

@@ -55,6 +55,15 @@ def test_noalloc_force_components_match(engine, params, vf, seed):
         host = np.zeros(6 * n)
         with pytest.raises(engine.LFGError):
             g.force_component_noalloc(0, host.ctypes.data)
+        # only the pair-force components 0..3 have a scratch slot: the Brownian
+        # component (4) and out-of-range values are refused, the output untouched
+        assert rt.cudaMemset(dptr, 0, nbytes) == 0
+        for bad in (4, 5, -1):
+            with pytest.raises(engine.LFGError):
+                g.force_component_noalloc(bad, dptr.value)
+        got = np.empty(6 * n)
+        assert rt.cudaMemcpy(got.ctypes.data, dptr, nbytes, 2) == 0
+        assert not got.any()
     finally:
         rt.cudaFree(dptr)
         g.close()
