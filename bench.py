@@ -18,8 +18,11 @@ fp64_value   : the same for the plain FP64 form
 e2e          : through the C ABI with host buffers: create from host arrays
                (H2D), K steps each followed by a D2H read of positions,
                velocities and the stress tensor
-cpu_baseline : the CPU oracle (C restatement, OpenMP) on one step of the same
-               workload, on this machine's host cores
+cpu_baseline : the CPU oracle (C restatement, OpenMP) on three steps of the
+               same workload on this machine's host cores, plus one step on
+               one thread; its first step is the reference of the accuracy
+               figures (fp32_vs_oracle, fp64_vs_oracle: velocities, angular
+               velocities, contact forces, stress, viscosity, N1, N2)
 """
 from __future__ import annotations
 
@@ -150,24 +153,48 @@ def run_engine(E, packing, precision, steps, warmup, device):
     return ms, kernels, timing, sc
 
 
-def fp32_accuracy(E, packing, device):
-    """One step of the FP32+refine form against the FP64 form from the same
-    state (same workload): max relative differences of the velocities, the
-    angular velocities and the total stress, with the refinement's counts."""
+def _step_record(part, sc, pairs):
+    return {"vel": part["vel"], "ang": part["ang"], "total_stress": sc["total_stress"],
+            "viscosity": sc["viscosity"], "N1": sc["N1"], "N2": sc["N2"],
+            "keys": np.stack([pairs["p0"], pairs["p1"]], 1), "contact_force": np.asarray(pairs["f_spring_total"])}
+
+
+def _errors(a, b):
+    """Largest relative differences of record a against record b (each
+    relative to the largest magnitude of b's quantity)."""
+    rel = lambda x, y: float(np.abs(np.asarray(x) - np.asarray(y)).max() / max(np.abs(np.asarray(y)).max(), 1e-300))
+    out = {k: rel(a[k], b[k]) for k in ("vel", "ang", "total_stress", "viscosity", "N1", "N2")}
+    out["contact_force"] = rel(a["contact_force"], b["contact_force"]) if np.array_equal(a["keys"], b["keys"]) \
+        else None
+    out["pair_list_identical"] = bool(np.array_equal(a["keys"], b["keys"]))
+    return out
+
+
+def accuracy(E, packing, device, oracle_ref=None):
+    """One predictor-corrector step with stresses from the packing, in the
+    FP32 + refinement and the FP64 forms: largest relative differences of the
+    velocities, angular velocities, contact forces, total stress, viscosity,
+    N1 and N2 against the CPU oracle's step from the same state (when given)
+    and between the two forms, with the refinement's counts."""
     params = workload_params()
-    out = {}
+    rec = {}
     for prec in (E.PREC_FP64, E.PREC_FP32_REFINE):
         g = E.Sim(params, packing.position, packing.radius, packing.lx, packing.ly, packing.lz,
                   precision=prec, device=device)
         g.step(calc_stress=True)
-        out[prec] = (g.particles(), g.scalars())
+        rec[prec] = (_step_record(g.particles(), g.scalars(), g.pairs()), g.scalars())
         g.close()
-    (p64, s64), (p32, s32) = out[E.PREC_FP64], out[E.PREC_FP32_REFINE]
-    rel = lambda a, b: float(np.abs(np.asarray(a) - np.asarray(b)).max() / np.abs(np.asarray(b)).max())
-    return {"vel": rel(p32["vel"], p64["vel"]), "ang": rel(p32["ang"], p64["ang"]),
-            "total_stress": rel(s32["total_stress"], s64["total_stress"]),
-            "refine_iters": int(s32["last_refine_iters"]), "refine_residual": float(s32["last_refine_residual"]),
-            "note": "one predictor-corrector step from the same state, FP32 factor + FP64 refinement vs FP64 factor"}
+    (r64, _), (r32, s32) = rec[E.PREC_FP64], rec[E.PREC_FP32_REFINE]
+    out = {"fp32_vs_fp64": dict(_errors(r32, r64), refine_iters=int(s32["last_refine_iters"]),
+                                refine_residual=float(s32["last_refine_residual"]),
+                                note="one predictor-corrector step from the same state, FP32 factor + FP64 "
+                                     "refinement vs FP64 factor")}
+    if oracle_ref is not None:
+        out["fp32_vs_oracle"] = dict(_errors(r32, oracle_ref),
+                                     note="one step from the packing against the CPU oracle (FP64)")
+        out["fp64_vs_oracle"] = dict(_errors(r64, oracle_ref),
+                                     note="one step from the packing against the CPU oracle (FP64)")
+    return out
 
 
 def run_e2e(E, packing, precision, steps, device):
@@ -195,21 +222,72 @@ def run_e2e(E, packing, precision, steps, device):
             "note": "includes creation (H2D of the configuration, symbolic analysis, graph capture)"}
 
 
-def cpu_baseline(packing, nsteps=1):
+def cpu_baseline(packing, nsteps=3, one_thread=True):
+    """The CPU oracle on this machine's host cores: nsteps predictor-corrector
+    steps of the workload from the packing with all OpenMP threads (the first
+    one with stresses; its result is the accuracy reference), then one step on
+    one thread.  Returns (baseline record, the first step's result)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     pyoracle.build()
+    cores = pyoracle.num_threads()
     o = pyoracle.OracleSim(workload_params(), packing.position, packing.radius, packing.lx, packing.ly,
                            packing.lz)
     o.first_time()
     t0 = time.perf_counter()
-    for _ in range(nsteps):
-        o.step()
+    o.step(calc_stress=True)
     t1 = time.perf_counter()
-    return {"value": N_PART * nsteps / (t1 - t0), "unit": "particle-steps/s", "cores": pyoracle.num_threads(),
-            "kind": "port",
-            "sample": f"{nsteps} predictor-corrector step(s) of the N={N_PART} workload, "
-                      f"FP64 block Cholesky (minimum degree) with OpenMP, {t1 - t0:.1f} s"}
+    ref = _step_record(o.particles(), o.scalars(), o.pairs())
+    for _ in range(nsteps - 1):
+        o.step()
+    t2 = time.perf_counter()
+    fs = pyoracle.factor_stats(o)
+    steps_s = [t1 - t0, (t2 - t1) / max(nsteps - 1, 1)]
+    rec = {"value": N_PART * nsteps / (t2 - t0), "unit": "particle-steps/s", "cores": cores, "kind": "port",
+           "sample": f"{nsteps} predictor-corrector steps of the N={N_PART} workload from the packing, "
+                     f"{t2 - t0:.1f} s, FP64 block Cholesky (minimum degree on 6x6 blocks, right-looking, "
+                     f"OpenMP trailing update); first step with stresses {steps_s[0]:.2f} s",
+           "factor_flops_per_factorisation": fs["factor_flops"],
+           "factor_gflops": fs["factor_flops"] * fs["factorisations"] / max(fs["factor_s"], 1e-12) / 1e9,
+           "factor_s_per_factorisation": fs["factor_s"] / max(fs["factorisations"], 1),
+           "analyze_s_per_factorisation": fs["analyze_s"] / max(fs["factorisations"], 1),
+           "cpu": _cpu_model()}
+    del o
+    if one_thread:
+        pyoracle.set_num_threads(1)
+        o1 = pyoracle.OracleSim(workload_params(), packing.position, packing.radius, packing.lx, packing.ly,
+                                packing.lz)
+        o1.first_time()
+        t0 = time.perf_counter()
+        o1.step()
+        t1 = time.perf_counter()
+        fs1 = pyoracle.factor_stats(o1)
+        rec["one_thread"] = {"value": N_PART / (t1 - t0), "unit": "particle-steps/s", "cores": 1,
+                             "sample": f"1 predictor-corrector step, {t1 - t0:.1f} s",
+                             "factor_gflops": fs1["factor_flops"] * fs1["factorisations"] /
+                             max(fs1["factor_s"], 1e-12) / 1e9}
+        del o1
+        pyoracle.set_num_threads(cores)
+    return rec, ref
+
+
+ARM_PARTS = {"0xd4f": "Arm Neoverse V2", "0xd40": "Arm Neoverse V1", "0xd0c": "Arm Neoverse N1",
+             "0xd49": "Arm Neoverse N2"}
+
+
+def _cpu_model():
+    try:
+        with open("/proc/cpuinfo") as f:
+            txt = f.read()
+        for key in ("model name", "Model name", "CPU part"):
+            for ln in txt.splitlines():
+                if ln.startswith(key):
+                    v = ln.split(":", 1)[1].strip()
+                    return f"{ARM_PARTS.get(v, v)} ({os.cpu_count()} logical CPUs)"
+    except OSError:
+        pass
+    import platform
+    return f"{platform.machine()} ({os.cpu_count()} logical CPUs)"
 
 
 def dist_setup(backend="nccl"):
@@ -263,6 +341,7 @@ def reference_arm(args):
         times.append(time.perf_counter() - t0)
     tot = sum(times)
     val = N_PART * args.steps / tot
+    fs = pyoracle.factor_stats(o)
     line = {"metric": METRIC, "value": val, "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
@@ -272,7 +351,10 @@ def reference_arm(args):
                              "kind": "port",
                              "sample": f"{args.steps} full steps of the N={N_PART} workload on the CPU oracle "
                                        "(C restatement of LF_DEM's step; reference C++ + CHOLMOD cannot be "
-                                       "built on this host)"},
+                                       "built on this host)",
+                             "factor_flops_per_factorisation": fs["factor_flops"],
+                             "factor_gflops": fs["factor_flops"] * fs["factorisations"] /
+                             max(fs["factor_s"], 1e-12) / 1e9, "cpu": _cpu_model()},
             "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -473,8 +555,6 @@ def main():
         res["fp64_p99_ms"] = float(np.percentile(ms64, 99))
         res["fp64_stage_ms"] = dict(zip(["pairs", "assembly", "factor", "solve", "forces_stress", "move"],
                                         tim64["ms"][:6]))
-        if rank == 0:
-            res["fp32_vs_fp64"] = fp32_accuracy(E, pk, local)
     if rank != 0:
         return
     hbm, bf16, bf16s, src = measured_peaks()
@@ -516,8 +596,11 @@ def main():
                               "frac": solve_bytes_step / max(solve_ms * 1e-3, 1e-12) / 1e9 / hbm,
                               "note": "factor bytes read by the triangular solves of one step / solve time"}
     line["e2e"] = run_e2e(E, pk, E.PREC_FP32_REFINE, args.steps, local)
+    oracle_ref = None
     if not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(pk, 1)
+        line["cpu_baseline"], oracle_ref = cpu_baseline(pk)
+    if not args.no_fp64:
+        line.update(accuracy(E, pk, local, oracle_ref))
     print(json.dumps(line), flush=True)
 
 

@@ -25,6 +25,15 @@ int lfo_num_threads(void)
 #endif
 }
 
+void lfo_set_num_threads(int n)
+{
+#ifdef _OPENMP
+	if (n > 0) omp_set_num_threads(n);
+#else
+	(void)n;
+#endif
+}
+
 #ifndef M_PI
 #define M_PI 3.14159265358979323846
 #endif
@@ -237,6 +246,9 @@ struct lfo_sim {
 	/* solver */
 	void *fact;
 	double rate_prop_shearstress, rate_indep_shearstress;
+	/* factorisation statistics (baseline reporting): count, ordering flops
+	 * of the last one, wall seconds of analysis and numeric phases */
+	long long n_factor; double last_factor_flops, analyze_s, factor_s;
 };
 
 /* ------------------------------------------------------------------ */
@@ -1274,6 +1286,28 @@ int lfo_bsr_solve(int nblk, const double *diag36, int nb, const int *row, const 
 
 /* assemble -> dense blocks -> analyse + factorise (StokesSolver::
  * matrixFillingDone / factorizeResistanceMatrix, StokesSolver.cpp:937-978) */
+/* algorithmic flops of a factorisation with this ordering: every block
+ * column is 6 scalar columns with 6c rows below them (c off-diagonal
+ * blocks), counted as n^3/3 + n^2 m + n m^2 with n = 6, m = 6c */
+static double bfact_flops(const bfact *f)
+{
+	double fl = 0;
+	for (int k = 0; k < f->n; k++) {
+		double m = 6.0*(f->colptr[k+1]-f->colptr[k]);
+		fl += 72.0+36.0*m+6.0*m*m;
+	}
+	return fl;
+}
+
+static double wall_s(void)
+{
+#ifdef _OPENMP
+	return omp_get_wtime();
+#else
+	return 0.0;
+#endif
+}
+
 static int factorize_current(lfo_sim *s)
 {
 	int n = s->np;
@@ -1282,8 +1316,15 @@ static int factorize_current(lfo_sim *s)
 	for (int i = 0; i < n; i++) lfo_dblock_to_dense(&s->dblocks[i*15], &diag36[i*36]);
 	for (int e = 0; e < s->nod; e++) lfo_odblock_to_dense(&s->odblocks[e*18], &off36[e*36]);
 	if (s->fact) { bfact_free(s->fact); s->fact = NULL; }
+	double t0 = wall_s();
 	bfact *f = bfact_analyze(n, s->nod, s->odrow, s->odcol);
+	double t1 = wall_s();
 	int st = f ? bfact_factorize(f, diag36, s->nod, s->odrow, s->odcol, off36) : -1;
+	double t2 = wall_s();
+	s->n_factor++;
+	s->analyze_s += t1-t0;
+	s->factor_s += t2-t1;
+	if (f) s->last_factor_flops = bfact_flops(f);
 	free(diag36); free(off36);
 	s->fact = f;
 	return st;
@@ -2051,4 +2092,12 @@ int lfo_get_velocity_component(const lfo_sim *s, int comp, double *out)
 	if (comp < 0 || comp >= NFC || !s->has_fc[comp]) return -1;
 	memcpy(out, s->vc[comp], sizeof(double)*6*s->np);
 	return 0;
+}
+
+void lfo_factor_stats(const lfo_sim *s, double *out4)
+{
+	out4[0] = (double)s->n_factor;
+	out4[1] = s->last_factor_flops;
+	out4[2] = s->analyze_s;
+	out4[3] = s->factor_s;
 }

@@ -171,6 +171,14 @@ int lfo_bsr_solve(int nblk, const double *diag36, int nb, const int *row, const 
 
 /* Number of host threads the oracle's factorisation uses (OpenMP). */
 int lfo_num_threads(void);
+void lfo_set_num_threads(int n);   /* OpenMP threads of later parallel regions */
+
+/* Factorisation statistics for baseline reporting: out4 = {factorisations so
+ * far, algorithmic flops of the last one (sum over block columns of
+ * n^3/3 + n^2 m + n m^2 with n = 6, m = 6 x its off-diagonal blocks), wall
+ * seconds spent in ordering + symbolic analysis, wall seconds in the numeric
+ * factorisation}. */
+void lfo_factor_stats(const lfo_sim *s, double *out4);
 
 /* Block (compact -> dense 6x6 row-major) reconstructions of
  * StokesSolver.cpp:154-231 (rows of the lower block, columns of the column

@@ -105,6 +105,8 @@ def lib():
                                     C.c_double, C.c_double, C.c_int]
         L.lfo_refresh.argtypes = [C.c_void_p]
         L.lfo_num_threads.restype = C.c_int
+        L.lfo_set_num_threads.argtypes = [C.c_int]
+        L.lfo_factor_stats.argtypes = [C.c_void_p, C.c_void_p]
         L.lfo_dblock_to_dense.argtypes = [dp, dp]
         L.lfo_odblock_to_dense.argtypes = [dp, dp]
         _lib = L
@@ -248,6 +250,20 @@ class OracleSim:
 
     def refresh(self):
         lib().lfo_refresh(self.h)
+
+
+def factor_stats(sim) -> dict:
+    """Factorisations so far, the last one's ordering flops, seconds in the
+    ordering + symbolic analysis and in the numeric factorisation."""
+    out = np.zeros(4)
+    lib().lfo_factor_stats(sim.h, out.ctypes.data)
+    return {"factorisations": int(out[0]), "factor_flops": float(out[1]), "analyze_s": float(out[2]),
+            "factor_s": float(out[3])}
+
+
+def set_num_threads(n: int) -> None:
+    """OpenMP threads of the oracle's later parallel regions."""
+    lib().lfo_set_num_threads(int(n))
 
 
 def num_threads() -> int:
