@@ -10,6 +10,7 @@ public dataset).  One step = one full predictor-corrector time step
 shear-rate solve each half step).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+  python bench.py --workload cfg3            (the 2D monolayer, N=8192)
   python bench.py --workload sweep|serve     (the batched and serving forms)
 
 value        : particle-steps/s of the FP32 + FP64-refinement form, device time
@@ -432,6 +433,93 @@ def bench_sweep(args):
     print(json.dumps(line), flush=True)
 
 
+def monolayer_params():
+    """2D monolayer: rate control 1r (repulsive-force units), kn = 1e4,
+    kt = 0.5 kn, mu = 1, lambda = 1e-3, lub_max_gap 0.5, no Brownian force."""
+    return rate_params(1.0)
+
+
+def _state_of(g):
+    """Everything a restart needs: positions, Lees-Edwards offset, contact
+    springs and the clock."""
+    sc = g.scalars()
+    c0, c1, dtan, _ = g.contact_states()
+    return {"pos": g.particles()["pos"].copy(), "le": tuple(sc["shear_disp"]),
+            "contacts": [(int(a), int(b), d) for a, b, d in zip(c0, c1, dtan)],
+            "clock": (sc["time"], sc["strain"], sc["dt"], sc["shear_rate"], sc["max_velocity"],
+                      sc["max_sliding_velocity"])}
+
+
+def bench_cfg3(args):
+    """2D monolayer: N = 8192 bidisperse discs (1:1.4, equal area shares),
+    areal fraction 0.78, rate control 1r, seeded packing.  The FP32 +
+    refinement form with 3 unknowns per particle (in-plane x, z translation,
+    y rotation) is timed over K steps; every 100 steps (from the first) the
+    run's state is handed to an FP64 engine with LF_DEM's 6x6 blocks and to
+    a fresh FP32 one with 3 unknowns, both advance one step from it, and the
+    largest relative velocity / stress differences are reported (the FP64
+    check, outside the timed steps).  The same K steps are also timed with 6x6
+    blocks in FP32 + refinement for comparison."""
+    import lf_dem_gb300 as E
+    from lf_dem_gb300 import build as B
+    from lf_dem_gb300 import packing as PK
+    n = args.count or 8192
+    pk = PK.generate(n, 0.78, seed=3000, twodim=True)
+    B.build()
+    E.load()
+    prm = monolayer_params()
+    out = {}
+    for label, dof in (("dof3", 3), ("dof6", 6)):
+        g = E.Sim(prm, pk.position, pk.radius, pk.lx, pk.ly, pk.lz, precision=E.PREC_FP32_REFINE, dof_2d=dof)
+        g.run(args.warmup)
+        g.clear_step_times()
+        checks = []
+        ms_all = []
+        done = 0
+        while done < args.steps:
+            if dof == 3 and done % 100 == 0:
+                # the FP64 check: both forms advance one step from the run's state
+                st = _state_of(g)
+                res = {}
+                for prec, d in ((E.PREC_FP64, 6), (E.PREC_FP32_REFINE, 3)):
+                    h = E.Sim(prm, st["pos"], pk.radius, pk.lx, pk.ly, pk.lz, le_disp=st["le"],
+                              contacts=st["contacts"], precision=prec, dof_2d=d)
+                    h.set_clock(*st["clock"])
+                    h.step(calc_stress=True)
+                    res[prec] = (h.particles(), h.scalars())
+                    h.close()
+                (p64, s64), (p32, s32) = res[E.PREC_FP64], res[E.PREC_FP32_REFINE]
+                rel = lambda a, b: float(np.abs(np.asarray(a) - np.asarray(b)).max() /
+                                         max(np.abs(np.asarray(b)).max(), 1e-300))
+                checks.append({"step": done, "strain": float(st["clock"][1]), "vel": rel(p32["vel"], p64["vel"]),
+                               "ang": rel(p32["ang"], p64["ang"]),
+                               "total_stress": rel(s32["total_stress"], s64["total_stress"])})
+            k = min(args.steps - done, 100 - done % 100)
+            g.run(k)
+            ms, kern = g.step_times()
+            g.clear_step_times()
+            ms_all.extend(list(ms))
+            done += k
+        tim = g.timing()
+        sc = g.scalars()
+        out[label] = {"particle_steps_per_s": n * len(ms_all) / (float(np.sum(ms_all)) / 1e3),
+                      "ms_per_step": float(np.mean(ms_all)), "p50_ms": float(np.percentile(ms_all, 50)),
+                      "p99_ms": float(np.percentile(ms_all, 99)), "factor_flops": tim["factor_flops"],
+                      "refine_iters": int(sc["last_refine_iters"]), "strain_reached": float(sc["strain"])}
+        if checks:
+            out[label]["fp64_checks"] = checks
+        g.close()
+    line = {"metric": "particle-steps/s, 2D monolayer N=8192 areal phi=0.78, FP32+refine (3 unknowns per particle) "
+                      "with an FP64 check every 100 steps", "workload": "cfg3",
+            "value": out["dof3"]["particle_steps_per_s"], "unit": "particle-steps/s", "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": out["dof3"]["ms_per_step"], "higher_is_better": True,
+            "dtype": "f32+f64refine", "data": "synthetic",
+            "config": {"n_particles": n, "areal_fraction": 0.78, "control": "rate 1r", "twodim": True,
+                       "note": "fixed step count instead of 3 strain units; device time per step (CUDA events)"},
+            **out, "speedup_dof3_vs_dof6": out["dof3"]["particle_steps_per_s"] / out["dof6"]["particle_steps_per_s"]}
+    print(json.dumps(line), flush=True)
+
+
 def bench_serve(args):
     """Serving stream: R requests with Poisson arrivals (mean 50 ms), N
     log-uniform in [200, 16384], phi ~ U[0.45, 0.58], stress control with sigma
@@ -492,13 +580,17 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="profiling driver: FP32 form only, W + K steps, no measurement (for ncu)")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"], help="form used by --profile")
-    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "sweep", "serve"],
-                    help="cfg2: the metric's workload (default); sweep / serve: the batched and serving forms")
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg3", "sweep", "serve"],
+                    help="cfg2: the metric's workload (default); cfg3: the 2D monolayer; "
+                         "sweep / serve: the batched and serving forms")
     ap.add_argument("--count", type=int, default=0, help="suspensions (sweep) or requests (serve)")
     ap.add_argument("--strain", type=float, default=0.002, help="serve: strain target of each request")
     ap.add_argument("--max-active", type=int, default=8, help="serve: concurrent requests")
     ap.add_argument("--hbm-budget-gb", type=float, default=200.0, help="serve: device bytes for admission")
     args = ap.parse_args()
+    if args.workload == "cfg3":
+        bench_cfg3(args)
+        return
     if args.workload == "sweep":
         bench_sweep(args)
         return

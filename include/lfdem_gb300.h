@@ -153,7 +153,12 @@ typedef struct {
 	double skin;            /* pair superset skin, units of (a_i+a_j)/2 (default 0.15) */
 	int use_graphs;         /* capture factor/solve launch sequences in CUDA graphs (default 1) */
 	int leaf_size;          /* nested-dissection leaf size in particles (default 16) */
-	int pad_;
+	int dof_2d;             /* unknowns per particle of a 2D run (ly = 0) without Brownian force:
+	                           3 (default) solves only the in-plane x, z translation and y rotation,
+	                           which the 6x6 blocks of a monolayer decouple exactly from the others
+	                           (their out-of-plane velocities are 0); 6 keeps LF_DEM's 6x6 blocks
+	                           (System.cpp:478-491, StokesSolver.cpp:87-100).  3D and Brownian runs
+	                           always use 6. */
 } lfg_options;
 
 void lfg_default_options(lfg_options *opt);
@@ -166,7 +171,13 @@ int lfg_device_info(int device, char *name, int name_len, int *sm_major, int *sm
 /* ------------------------------------------------------------------ */
 typedef struct lfg_solver lfg_solver;
 
-/* StokesSolver::init (StokesSolver.cpp:77-106): n_mobile particles, dof 6. */
+/* StokesSolver::init (StokesSolver.cpp:77-106): n_mobile particles, dof 6;
+ * or dof 3 for a 2D system (ly = 0), whose 6x6 blocks couple the in-plane
+ * unknowns (x, z translation, y rotation: components 0, 2, 4) only among
+ * themselves: the solver then factors those alone.  Blocks, right-hand sides
+ * and solutions keep LF_DEM's 6-per-particle layout either way; with dof 3
+ * the other components of a right-hand side are not read and those of a
+ * solution are 0.  LF_DEM itself has no 3-unknown variant. */
 int lfg_solver_create(int n_mobile, int dof, const lfg_options *opt, lfg_solver **out,
                       lfg_status *st);
 

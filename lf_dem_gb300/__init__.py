@@ -70,7 +70,7 @@ class Params(C.Structure):
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("refine_tol", C.c_double),
                 ("refine_max_iter", C.c_int), ("pad0_", C.c_int), ("skin", C.c_double),
-                ("use_graphs", C.c_int), ("leaf_size", C.c_int), ("pad_", C.c_int), ("pad2_", C.c_int)]
+                ("use_graphs", C.c_int), ("leaf_size", C.c_int), ("dof_2d", C.c_int), ("pad2_", C.c_int)]
 
 
 class SolverStats(C.Structure):
@@ -282,13 +282,14 @@ def _ptr(a: np.ndarray):
 class Solver:
     """Device resistance solver (lfg_solver_*): the StokesSolver linear algebra."""
 
-    def __init__(self, n: int, precision: int = PREC_FP64, **opts):
+    def __init__(self, n: int, precision: int = PREC_FP64, dof: int = 6, **opts):
         L = load()
         self.n = n
+        self.dof = dof
         self.opt = default_options(precision=precision, **opts)
         h = C.c_void_p()
         st = Status()
-        _check(L.lfg_solver_create(n, 6, C.byref(self.opt), C.byref(h), C.byref(st)), st)
+        _check(L.lfg_solver_create(n, dof, C.byref(self.opt), C.byref(h), C.byref(st)), st)
         self.h = h
         self.last = st
 

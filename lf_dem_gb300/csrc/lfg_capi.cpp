@@ -71,6 +71,7 @@ void lfg_default_options(lfg_options *o)
 	o->skin = 0.15;
 	o->use_graphs = 1;
 	o->leaf_size = 16;
+	o->dof_2d = 3;
 }
 
 int lfg_device_info(int device, char *name, int name_len, int *sm_major, int *sm_minor, int *sm_count)
@@ -89,7 +90,7 @@ int lfg_device_info(int device, char *name, int name_len, int *sm_major, int *sm
 int lfg_solver_create(int n_mobile, int dof, const lfg_options *opt, lfg_solver **out, lfg_status *st)
 {
 	if (!out || n_mobile <= 0) return fail(st, LFG_ERR_BAD_ARG, 0, "bad arguments");
-	if (dof != 6) return fail(st, LFG_ERR_BAD_ARG, dof, "only 6 degrees of freedom per particle are supported");
+	if (dof != 6 && dof != 3) return fail(st, LFG_ERR_BAD_ARG, dof, "degrees of freedom per particle must be 6 or 3");
 	lfg_options o;
 	if (opt) o = *opt; else lfg_default_options(&o);
 	if (o.precision != LFG_PREC_FP64 && o.precision != LFG_PREC_FP32_REFINE)
@@ -101,7 +102,7 @@ int lfg_solver_create(int n_mobile, int dof, const lfg_options *opt, lfg_solver 
 	h = new lfg_solver();
 	h->device = o.device;
 	LFG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
-	h->s = new Solver(n_mobile, o, h->stream);
+	h->s = new Solver(n_mobile, o, h->stream, dof);
 	*out = h;
 	return ok(st);
 	}

@@ -90,6 +90,11 @@ __device__ inline void od18_to_dense(const double *o, double *m)
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
+// Scalar index r of a front or vector with dof unknowns per particle (6, or
+// 3 for the in-plane part of a 2D system): its particle (block) and component.
+__device__ __forceinline__ int bdiv(int r, int dof) { return dof == 6 ? r/6 : r/3; }
+__device__ __forceinline__ int bmod(int r, int dof) { return dof == 6 ? r%6 : r%3; }
+
 template <typename... KArgs, typename... Args>
 static void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args)
 {
@@ -124,7 +129,7 @@ __global__ void __launch_bounds__(256) k_assemble(const int *__restrict__ col_ta
                                                   const int *__restrict__ children,
                                                   const int64_t *__restrict__ cinv_off,
                                                   const int *__restrict__ cinv, const int *__restrict__ sn_rows_off,
-                                                  const int *__restrict__ cfwd, T *__restrict__ arena)
+                                                  const int *__restrict__ cfwd, T *__restrict__ arena, int dof)
 {
 	extern __shared__ __align__(16) unsigned char smem_asm[];
 	T *buf = reinterpret_cast<T *>(smem_asm);   // buf[r - c], r in [c, 6F)
@@ -132,9 +137,9 @@ __global__ void __launch_bounds__(256) k_assemble(const int *__restrict__ col_ta
 		c_ro[ASM_CHILDREN];
 	__shared__ int64_t c_off[ASM_CHILDREN];
 	int s = col_tasks[2*blockIdx.x], c = col_tasks[2*blockIdx.x+1];
-	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
+	int n6 = dof*sn_n[s], F6 = n6+dof*sn_m[s], ld = sn_ld[s];
 	T *col = arena+sn_off[s]+(int64_t)c*ld;
-	int cb = c/6, cr = c%6;
+	int cb = bdiv(c, dof), cr = bmod(c, dof);
 	int ca = child_off[s], cz = child_off[s+1];
 	for (int r = c+threadIdx.x; r < F6; r += blockDim.x) buf[r-c] = T(0);
 	pdl_wait();
@@ -144,9 +149,9 @@ __global__ void __launch_bounds__(256) k_assemble(const int *__restrict__ col_ta
 		if (threadIdx.x < nq) {
 			int ch = children[q0+threadIdx.x];
 			int ic = cinv[cinv_off[ch]+cb];
-			c_jc[threadIdx.x] = ic < 0 ? -1 : 6*ic+cr;
-			c_n6[threadIdx.x] = 6*sn_n[ch];
-			c_F6[threadIdx.x] = 6*(sn_n[ch]+sn_m[ch]);
+			c_jc[threadIdx.x] = ic < 0 ? -1 : dof*ic+cr;
+			c_n6[threadIdx.x] = sn_n[ch];   // in particles
+			c_F6[threadIdx.x] = dof*(sn_n[ch]+sn_m[ch]);
 			c_ld[threadIdx.x] = sn_ld[ch];
 			c_ro[threadIdx.x] = sn_rows_off[ch];
 			c_off[threadIdx.x] = sn_off[ch];
@@ -155,12 +160,12 @@ __global__ void __launch_bounds__(256) k_assemble(const int *__restrict__ col_ta
 		for (int u = 0; u < nq; u++) {
 			int jc = c_jc[u];
 			if (jc < 0) continue;   // uniform: column c is not in this child's update
-			int n6c = c_n6[u], F6c = c_F6[u];
+			int nbc = c_n6[u], F6c = c_F6[u];
 			// child fronts are complete and not written here: read-only loads
 			const T *src = arena+c_off[u]+(int64_t)jc*c_ld[u];
 			const int *fw = cfwd+c_ro[u];
 			for (int i = jc+threadIdx.x; i < F6c; i += blockDim.x) {
-				int pr = 6*__ldg(&fw[i/6-n6c/6])+i%6;
+				int pr = dof*__ldg(&fw[bdiv(i, dof)-nbc])+bmod(i, dof);
 				buf[pr-c] += __ldg(&src[i]);
 			}
 			__syncthreads();   // adds of one child complete before the next child's
@@ -181,11 +186,51 @@ __global__ void k_scatter(int nd, int nod, const int *__restrict__ dlist, const 
                           const double *__restrict__ dblocks, const double *__restrict__ odblocks,
                           const int *__restrict__ d_sn, const int *__restrict__ d_bc, const int *__restrict__ od_sn,
                           const int *__restrict__ od_br, const int *__restrict__ od_bc, const int *__restrict__ od_tr,
-                          const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off, T *__restrict__ arena)
+                          const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off, T *__restrict__ arena,
+                          int dof)
 {
 	int t = blockIdx.x*blockDim.x+threadIdx.x;
 	if (t >= nd+nod) return;
 	double m[36];
+	if (dof == 3) {
+		// in-plane part of a 2D system: unknowns x, z translation and y
+		// rotation, components 0, 2, 4 of the 6x6 block
+		if (t < nd) {
+			int i = dlist[t];
+			int s = d_sn[i], b = d_bc[i], ld = sn_ld[s];
+			T *base = arena+sn_off[s];
+			pdl_wait();
+			d15_to_dense(dblocks+15*(int64_t)i, m);
+			T old[6];
+#pragma unroll
+			for (int c = 0, e = 0; c < 3; c++)
+#pragma unroll
+				for (int r = c; r < 3; r++, e++) old[e] = base[(int64_t)(3*b+c)*ld+3*b+r];
+#pragma unroll
+			for (int c = 0, e = 0; c < 3; c++)
+#pragma unroll
+				for (int r = c; r < 3; r++, e++) base[(int64_t)(3*b+c)*ld+3*b+r] = old[e]+(T)m[(2*r)*6+2*c];
+		} else {
+			int e = odlist[t-nd];
+			int s = od_sn[e], br = od_br[e], bc = od_bc[e], ld = sn_ld[s];
+			T *base = arena+sn_off[s];
+			bool tr = od_tr[e];
+			pdl_wait();
+			od18_to_dense(odblocks+18*(int64_t)e, m);
+			T old[9];
+#pragma unroll
+			for (int c = 0; c < 3; c++)
+#pragma unroll
+				for (int r = 0; r < 3; r++) old[3*c+r] = base[(int64_t)(3*bc+c)*ld+3*br+r];
+#pragma unroll
+			for (int c = 0; c < 3; c++)
+#pragma unroll
+				for (int r = 0; r < 3; r++)
+					base[(int64_t)(3*bc+c)*ld+3*br+r] =
+						old[3*c+r]+(T)(tr ? m[(2*c)*6+2*r] : m[(2*r)*6+2*c]);
+		}
+		return;
+	}
 	if (t < nd) {
 		int i = dlist[t];
 		int s = d_sn[i], b = d_bc[i], ld = sn_ld[s];
@@ -614,7 +659,7 @@ __device__ inline T *linv_slot(T *linv, int nsn, int s, int k)
 template <typename T>
 __global__ void __launch_bounds__(128) k_diag(const int4 *__restrict__ tasks, const int *__restrict__ sn_first,
                                               const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
-                                              T *__restrict__ arena, T *__restrict__ linv, int nsn, int *fail)
+                                              T *__restrict__ arena, T *__restrict__ linv, int nsn, int *fail, int dof)
 {
 	constexpr int NB = Cfg<T>::NB, LD = NB+1;
 	__shared__ T Ls[NB*LD];
@@ -624,7 +669,7 @@ __global__ void __launch_bounds__(128) k_diag(const int4 *__restrict__ tasks, co
 	int4 tk = tasks[blockIdx.x];
 	int s = tk.x, p0 = tk.y, k = tk.z, w = tk.w;
 	pdl_wait();
-	diag_block<T>(arena+sn_off[s], sn_ld[s], p0, w, 6*sn_first[s]+p0, fail, Ls, Vs, Ts, Lsh,
+	diag_block<T>(arena+sn_off[s], sn_ld[s], p0, w, dof*sn_first[s]+p0, fail, Ls, Vs, Ts, Lsh,
 	              linv_slot<T>(linv, nsn, s, k));
 }
 
@@ -658,7 +703,7 @@ __device__ inline void lds_chunk(const T *p, T (&v)[CW])
 template <typename T>
 __global__ void __launch_bounds__(256) k_trsm(const int4 *__restrict__ tasks, const int *__restrict__ sn_n,
                                               const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
-                                              T *__restrict__ arena, T *__restrict__ linv, int nsn)
+                                              T *__restrict__ arena, T *__restrict__ linv, int nsn, int dof)
 {
 	constexpr int NB = Cfg<T>::NB, CW = NB/8;
 	__shared__ __align__(16) T Vt[NB*NB];
@@ -668,7 +713,7 @@ __global__ void __launch_bounds__(256) k_trsm(const int4 *__restrict__ tasks, co
 	int s = tk.x, row0 = tk.y, k = tk.z, nrows = tk.w;
 	int ld = sn_ld[s];
 	int p0 = k*NB;
-	int w = min(NB, 6*sn_n[s]-p0);   // panel width: columns p0 + w and later are not touched
+	int w = min(NB, dof*sn_n[s]-p0);   // panel width: columns p0 + w and later are not touched
 	T *base = arena+sn_off[s];
 	const T *vt = linv_slot<T>(linv, nsn, s, k);
 	pdl_trigger();   // the next update's CTAs wait resident while this short launch runs
@@ -734,7 +779,8 @@ template <typename T>
 __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ tasks, const int *__restrict__ sn_first,
                                                 const int *__restrict__ sn_n, const int *__restrict__ sn_m,
                                                 const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
-                                                T *__restrict__ arena, T *__restrict__ linv, int nsn, int *fail)
+                                                T *__restrict__ arena, T *__restrict__ linv, int nsn, int *fail,
+                                                int dof)
 {
 	constexpr int NB = Cfg<T>::NB, TL = Cfg<T>::TILE, TPT = Cfg<T>::TPT;
 	constexpr int TD = TL/TPT; // threads per dimension (16)
@@ -743,7 +789,7 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 	T (*Bs)[TL] = reinterpret_cast<T (*)[TL]>(smem_upd+sizeof(T)*NB*TL);
 	int4 tk = tasks[blockIdx.x];
 	int s = tk.x, r0 = tk.y, cc0 = tk.z, k = tk.w;
-	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
+	int n6 = dof*sn_n[s], F6 = n6+dof*sn_m[s], ld = sn_ld[s];
 	int p0 = k*NB, w = min(NB, n6-p0), t0 = p0+w;
 	T *base = arena+sn_off[s];
 	bool extra = r0 >= F6;
@@ -839,7 +885,7 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 		__syncthreads();   // this CTA's updates of the block are visible to all its threads
 		if (!handoff) diag_load<T>(base, ld, t0, w1, Ls, Vs);
 		__syncthreads();
-		diag_factor<T>(base, ld, t0, w1, 6*sn_first[s]+t0, fail, Ls, Vs, Ts, Lsh, linv_slot<T>(linv, nsn, s, k+1));
+		diag_factor<T>(base, ld, t0, w1, dof*sn_first[s]+t0, fail, Ls, Vs, Ts, Lsh, linv_slot<T>(linv, nsn, s, k+1));
 	}
 }
 
@@ -851,7 +897,7 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 template <typename T>
 __global__ void __launch_bounds__(256) k_syrk(const int4 *__restrict__ tasks, const int *__restrict__ sn_n,
                                               const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
-                                              const int64_t *__restrict__ sn_off, T *__restrict__ arena)
+                                              const int64_t *__restrict__ sn_off, T *__restrict__ arena, int dof)
 {
 	constexpr int TL = Cfg<T>::STILE, TPT = Cfg<T>::STPT, TD = TL/TPT;
 	constexpr int KC = 16;
@@ -860,7 +906,7 @@ __global__ void __launch_bounds__(256) k_syrk(const int4 *__restrict__ tasks, co
 	__shared__ T Bs[KC][TL];
 	int4 tk = tasks[blockIdx.x];
 	int s = tk.x, r0 = tk.y, c0 = tk.z;
-	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
+	int n6 = dof*sn_n[s], F6 = n6+dof*sn_m[s], ld = sn_ld[s];
 	T *base = arena+sn_off[s];
 	pdl_wait();
 	int tx = threadIdx.x%TD, ty = threadIdx.x/TD;
@@ -1144,7 +1190,7 @@ __global__ void __launch_bounds__(umma::THREADS, 1) k_syrk_tc(const int4 *__rest
                                                               const int *__restrict__ sn_m,
                                                               const int *__restrict__ sn_ld,
                                                               const int64_t *__restrict__ sn_off,
-                                                              float *__restrict__ arena, int *fail)
+                                                              float *__restrict__ arena, int *fail, int dof)
 {
 	extern __shared__ unsigned char smem_tc[];
 	__shared__ __align__(8) uint64_t mbar[umma::STAGES];
@@ -1153,7 +1199,7 @@ __global__ void __launch_bounds__(umma::THREADS, 1) k_syrk_tc(const int4 *__rest
 	                                                      ~static_cast<uintptr_t>(1023));
 	int4 tk = tasks[blockIdx.x];
 	int s = tk.x, r0 = tk.y, c0 = tk.z;
-	int n6 = 6*sn_n[s], F6 = n6+6*sn_m[s], ld = sn_ld[s];
+	int n6 = dof*sn_n[s], F6 = n6+dof*sn_m[s], ld = sn_ld[s];
 	pdl_wait();   // before the tensor-memory allocation, too
 	uint32_t tmem = tc_setup(&tmem_slot, mbar);
 	bool ok = tc_tile_update(arena+sn_off[s], ld, r0, c0, 0, n6, F6, F6, true, sm, mbar, tmem);
@@ -1282,7 +1328,7 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 			launch_pdl(k_assemble<T>, L.count, 256, assemble_smem<T>(D), st, (const int *)D.col_tasks+2*L.off,
 			           (const int *)D.sn_n, (const int *)D.sn_m, (const int *)D.sn_ld, (const int64_t *)D.sn_off,
 			           (const int *)D.child_off, (const int *)D.children, (const int64_t *)D.cinv_off,
-			           (const int *)D.cinv, (const int *)D.sn_rows_off, (const int *)D.cfwd, F.arena);
+			           (const int *)D.cinv, (const int *)D.sn_rows_off, (const int *)D.cfwd, F.arena, D.dof);
 			break;
 		case PLAN_SCATTER: {
 			int d0 = D.h_level_d_off[L.level], nd = D.h_level_d_off[L.level+1]-d0;
@@ -1290,31 +1336,31 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 			launch_pdl(k_scatter<T>, (nd+nod+127)/128, 128, 0, st, nd, nod, (const int *)D.level_d+d0,
 			           (const int *)D.level_od+o0, dbl, odbl, (const int *)D.d_sn, (const int *)D.d_bc,
 			           (const int *)D.od_sn, (const int *)D.od_br, (const int *)D.od_bc, (const int *)D.od_tr,
-			           (const int *)D.sn_ld, (const int64_t *)D.sn_off, F.arena);
+			           (const int *)D.sn_ld, (const int64_t *)D.sn_off, F.arena, D.dof);
 			break;
 		}
 		case PLAN_DIAG:
 			launch_pdl(k_diag<T>, L.count, 128, 0, st, (const int4 *)D.diag_tasks+L.off, (const int *)D.sn_first,
-			           (const int *)D.sn_ld, (const int64_t *)D.sn_off, F.arena, F.linv, D.nsn, F.status);
+			           (const int *)D.sn_ld, (const int64_t *)D.sn_off, F.arena, F.linv, D.nsn, F.status, D.dof);
 			break;
 		case PLAN_PANEL:
 			launch_pdl(k_trsm<T>, L.count, 256, 0, st, (const int4 *)D.panel_tasks+L.off, (const int *)D.sn_n,
-			           (const int *)D.sn_ld, (const int64_t *)D.sn_off, F.arena, F.linv, D.nsn);
+			           (const int *)D.sn_ld, (const int64_t *)D.sn_off, F.arena, F.linv, D.nsn, D.dof);
 			break;
 		case PLAN_UPDATE:
 			launch_pdl(k_update<T>, L.count, 256, update_smem<T>(), st, (const int4 *)D.tile_tasks+L.off,
 			           (const int *)D.sn_first, (const int *)D.sn_n, (const int *)D.sn_m, (const int *)D.sn_ld,
-			           (const int64_t *)D.sn_off, F.arena, F.linv, D.nsn, F.status);
+			           (const int64_t *)D.sn_off, F.arena, F.linv, D.nsn, F.status, D.dof);
 			break;
 		case PLAN_SYRK:
 			launch_pdl(k_syrk<T>, L.count, 256, 0, st, (const int4 *)D.tile_tasks+L.off, (const int *)D.sn_n,
-			           (const int *)D.sn_m, (const int *)D.sn_ld, (const int64_t *)D.sn_off, F.arena);
+			           (const int *)D.sn_m, (const int *)D.sn_ld, (const int64_t *)D.sn_off, F.arena, D.dof);
 			break;
 		case PLAN_SYRK_TC:
 			if (!std::is_same<T, float>::value) throw Error{LFG_ERR_BAD_ARG, 0, "tensor-core plan for FP64"};
 			launch_pdl(k_syrk_tc, L.count, umma::THREADS, umma::SMEM_BYTES, st, (const int4 *)D.tile_tasks+L.off,
 			           (const int *)D.sn_n, (const int *)D.sn_m, (const int *)D.sn_ld, (const int64_t *)D.sn_off,
-			           reinterpret_cast<float *>(F.arena), F.status);
+			           reinterpret_cast<float *>(F.arena), F.status, D.dof);
 			break;
 		}
 		launches++;
@@ -1360,7 +1406,7 @@ template <typename T> struct SolveArgs {
 	T *w, *xp, *yp, *part;
 	int *tally;
 	int64_t wstride, pstride;
-	int n, n6tot;
+	int n, n6tot, dof;   // particles, scalar unknowns (dof n), unknowns per particle
 	const double *b;
 	double *x;
 };
@@ -1375,11 +1421,12 @@ template <typename T, int K>
 __device__ void unit_gather(const SolveArgs<T> &A, const int *lev, int bx, int by)
 {
 	int s = lev[by];
-	int n6 = 6*A.sn_n[s], F6 = n6+6*A.sn_m[s];
+	const int dof = A.dof;
+	int n6 = dof*A.sn_n[s], F6 = n6+dof*A.sn_m[s];
 	int r = bx*blockDim.x+threadIdx.x;
 	if (r >= F6) return;
 	int ca = A.child_off[s], cz = A.child_off[s+1];
-	int rb = r/6, rr = r%6;
+	int rb = bdiv(r, dof), rr = bmod(r, dof);
 	// the first children's source positions (symbolic) before the wait
 	constexpr int CPRE = 4;
 	int64_t src[CPRE];
@@ -1389,7 +1436,7 @@ __device__ void unit_gather(const SolveArgs<T> &A, const int *lev, int bx, int b
 		if (ca+c < cz) {
 			int ch = A.children[ca+c];
 			int ic = A.cinv[A.cinv_off[ch]+rb];
-			if (ic >= 0) src[c] = A.sn_woff[ch]+6*(ic-A.sn_n[ch])+rr;
+			if (ic >= 0) src[c] = A.sn_woff[ch]+dof*(ic-A.sn_n[ch])+rr;
 		}
 	}
 	T acc[K];
@@ -1405,12 +1452,12 @@ __device__ void unit_gather(const SolveArgs<T> &A, const int *lev, int bx, int b
 		int ch = A.children[c];
 		int ic = A.cinv[A.cinv_off[ch]+rb];
 		if (ic < 0) continue;
-		int64_t sc = A.sn_woff[ch]+6*(ic-A.sn_n[ch])+rr;
+		int64_t sc = A.sn_woff[ch]+dof*(ic-A.sn_n[ch])+rr;
 #pragma unroll
 		for (int q = 0; q < K; q++) acc[q] += A.w[q*A.wstride+sc];
 	}
 	if (r < n6) {
-		int g = 6*A.sn_first[s]+r;
+		int g = dof*A.sn_first[s]+r;
 #pragma unroll
 		for (int q = 0; q < K; q++) A.xp[(int64_t)q*A.n6tot+g] += acc[q];
 	} else {
@@ -1431,12 +1478,12 @@ template <typename T> struct SolveUnroll { static constexpr int U = sizeof(T) ==
 // rows) and factor entries
 template <typename T, int U, int MODE>
 __device__ __forceinline__ void cols_batch(int i0, int nrow, int f6, const int *R, const T *M, int ld, int j0, int jn,
-                                           int64_t (&g)[U], T (&e)[U][SOLVE_CB])
+                                           int dof, int64_t (&g)[U], T (&e)[U][SOLVE_CB])
 {
 #pragma unroll
 	for (int u = 0; u < U; u++) {
 		int i = i0+u*blockDim.x;
-		g[u] = i >= nrow ? -1 : MODE == 0 ? f6+i : 6*R[i/6]+i%6;
+		g[u] = i >= nrow ? -1 : MODE == 0 ? f6+i : dof*R[bdiv(i, dof)]+bmod(i, dof);
 #pragma unroll
 		for (int c = 0; c < SOLVE_CB; c++)
 			e[u][c] = (i >= nrow || c >= jn || (MODE == 0 && i > j0+c)) ? T(0) : __ldg(&M[(int64_t)c*ld+i]);
@@ -1448,11 +1495,12 @@ __device__ void unit_cols(const SolveArgs<T> &A, const int *lev, int bx, int by,
 {
 	constexpr int U = SolveUnroll<T>::U;
 	int s = lev[by];
-	int n6 = 6*A.sn_n[s], m6 = 6*A.sn_m[s], ld = A.sn_ld[s];
+	const int dof = A.dof;
+	int n6 = dof*A.sn_n[s], m6 = dof*A.sn_m[s], ld = A.sn_ld[s];
 	int j0 = bx*SOLVE_CB;
 	if (j0 >= n6 || (MODE == 1 && m6 == 0)) return;
 	int jn = min(SOLVE_CB, n6-j0);
-	int f6 = 6*A.sn_first[s];
+	int f6 = dof*A.sn_first[s];
 	const T *M = A.arena+A.sn_off[s]+(MODE == 0 ? n6+m6 : n6)+(int64_t)j0*ld;
 	const int *R = A.rows+A.sn_rows_off[s];
 	int nrow = MODE == 0 ? j0+jn : m6;
@@ -1463,7 +1511,7 @@ __device__ void unit_cols(const SolveArgs<T> &A, const int *lev, int bx, int by,
 		for (int q = 0; q < K; q++) acc[c][q] = 0;
 	int64_t g[U];
 	T e[U][SOLVE_CB];
-	cols_batch<T, U, MODE>(threadIdx.x, nrow, f6, R, M, ld, j0, jn, g, e);   // before the wait
+	cols_batch<T, U, MODE>(threadIdx.x, nrow, f6, R, M, ld, j0, jn, dof, g, e);   // before the wait
 	pdl_wait();
 	for (int i0 = threadIdx.x; i0 < nrow; i0 += U*blockDim.x) {
 		T v[U][K];
@@ -1483,7 +1531,7 @@ __device__ void unit_cols(const SolveArgs<T> &A, const int *lev, int bx, int by,
 			}
 		}
 		int i1 = i0+U*blockDim.x;
-		if (i1 < nrow) cols_batch<T, U, MODE>(i1, nrow, f6, R, M, ld, j0, jn, g, e);
+		if (i1 < nrow) cols_batch<T, U, MODE>(i1, nrow, f6, R, M, ld, j0, jn, dof, g, e);
 	}
 	int warp = threadIdx.x/32, lane = threadIdx.x%32;
 #pragma unroll
@@ -1526,12 +1574,13 @@ __device__ void unit_rows(const SolveArgs<T> &A, const int *lev, int bx, int by,
 {
 	constexpr bool UPD = MODE == 0 || MODE == 3;   // rows of the update block (w)
 	int s = lev[by];
-	int n6 = 6*A.sn_n[s], m6 = 6*A.sn_m[s], ld = A.sn_ld[s];
+	const int dof = A.dof;
+	int n6 = dof*A.sn_n[s], m6 = dof*A.sn_m[s], ld = A.sn_ld[s];
 	int nrows = UPD ? m6 : n6;
 	int r0 = bx*32;
 	if (r0 >= nrows) return;
 	int warp = threadIdx.x/32, lane = threadIdx.x%32;
-	int f6 = 6*A.sn_first[s];
+	int f6 = dof*A.sn_first[s];
 	int jlo = (MODE == 1 ? r0 : 0)+bz*SOLVE_JC;
 	int jhi = min(n6, jlo+SOLVE_JC);
 	const T *M = A.arena+A.sn_off[s]+(UPD ? n6 : MODE == 1 ? n6+m6 : 0);
@@ -1614,24 +1663,34 @@ __device__ void unit_rows(const SolveArgs<T> &A, const int *lev, int bx, int by,
 }
 
 // in: b (permuted) into xp; in_y (product with L): b into yp and xp zeroed;
-// out: xp (unpermuted) into x
+// out: xp (unpermuted) into x.  b and x keep 6 values per particle; with
+// dof 3 only components 0, 2, 4 (x, z translation, y rotation) are unknowns:
+// the others of b are not read and those of x are written as 0.
 template <typename T, int K>
 __device__ void unit_permute(const SolveArgs<T> &A, int bx, bool in, bool in_y = false)
 {
 	int t = bx*blockDim.x+threadIdx.x;
 	if (t >= 6*A.n) return;
 	int i = t/6, d = t%6;
-	int q = 6*A.iperm[i]+d;
+	const int64_t n6 = A.n6tot;
+	int q;
+	if (A.dof == 6) q = 6*A.iperm[i]+d;
+	else q = (d & 1) ? -1 : 3*A.iperm[i]+d/2;
 	pdl_wait();
+	if (q < 0) {
+		if (!in && !in_y)
+			for (int r = 0; r < K; r++) A.x[(int64_t)r*6*A.n+t] = 0.0;
+		return;
+	}
 	if (in_y) {
 		for (int r = 0; r < K; r++) {
-			A.yp[(int64_t)r*6*A.n+q] = (T)A.b[(int64_t)r*6*A.n+t];
-			A.xp[(int64_t)r*6*A.n+q] = T(0);
+			A.yp[(int64_t)r*n6+q] = (T)A.b[(int64_t)r*6*A.n+t];
+			A.xp[(int64_t)r*n6+q] = T(0);
 		}
 	} else if (in)
-		for (int r = 0; r < K; r++) A.xp[(int64_t)r*6*A.n+q] = (T)A.b[(int64_t)r*6*A.n+t];
+		for (int r = 0; r < K; r++) A.xp[(int64_t)r*n6+q] = (T)A.b[(int64_t)r*6*A.n+t];
 	else
-		for (int r = 0; r < K; r++) A.x[(int64_t)r*6*A.n+t] = (double)A.xp[(int64_t)r*6*A.n+q];
+		for (int r = 0; r < K; r++) A.x[(int64_t)r*6*A.n+t] = (double)A.xp[(int64_t)r*n6+q];
 }
 
 // one phase as its own launch: one CTA per work unit; one instantiation per
@@ -1738,7 +1797,8 @@ static int solve_k(DevFactor<T> &F, const DevSymbolic &D, const std::vector<Solv
 	A.sn_rows_off = D.sn_rows_off; A.rows = D.rows; A.sn_off = D.sn_off; A.sn_woff = D.sn_woff;
 	A.cinv_off = D.cinv_off; A.child_off = D.child_off; A.children = D.children; A.cinv = D.cinv;
 	A.iperm = D.iperm; A.arena = F.arena; A.w = F.w; A.xp = F.xp; A.yp = F.yp; A.part = F.part; A.tally = F.tally;
-	A.wstride = D.w_elems; A.pstride = F.pstride; A.n = D.nblk; A.n6tot = 6*D.nblk; A.b = b; A.x = x;
+	A.wstride = D.w_elems; A.pstride = F.pstride; A.n = D.nblk; A.n6tot = D.dof*D.nblk; A.dof = D.dof;
+	A.b = b; A.x = x;
 	for (const SolvePhase &p : phases) launch_phase<T, K>(A, p, st);
 	LFG_CUDA(cudaGetLastError());
 	return (int)phases.size();
@@ -1808,7 +1868,7 @@ __global__ void __launch_bounds__(256) k_residual(int n, int k, const double *__
                            const int *__restrict__ od_col, const int *__restrict__ lo_ptr,
                            const int *__restrict__ lo_idx, const int *__restrict__ up_ptr,
                            const int *__restrict__ up_idx, const double *__restrict__ b,
-                           const double *__restrict__ x, double *__restrict__ r)
+                           const double *__restrict__ x, double *__restrict__ r, int dof)
 {
 	__shared__ double sm[8][36];
 	int w = threadIdx.x/32, lane = threadIdx.x%32;
@@ -1841,7 +1901,9 @@ __global__ void __launch_bounds__(256) k_residual(int n, int k, const double *__
 				for (int c = 0; c < 6; c++) acc += m[c*6+a]*xv[6*j+c];
 			}
 		}
-		if (act) r[(int64_t)q*6*n+6*i+a] = b[(int64_t)q*6*n+6*i+a]-acc;
+		// dof 3: only components 0, 2, 4 are unknowns of the system (the
+		// out-of-plane ones are neither solved nor part of the residual)
+		if (act) r[(int64_t)q*6*n+6*i+a] = (dof == 3 && (a & 1)) ? 0.0 : b[(int64_t)q*6*n+6*i+a]-acc;
 		__syncwarp();
 	}
 }
@@ -1850,7 +1912,7 @@ void block_residual(const DevBlockMatrix &A, int k, const double *b, const doubl
                     cudaStream_t st)
 {
 	k_residual<<<(A.n+7)/8, 256, 0, st>>>(A.n, k, A.dblocks, A.odblocks, A.od_row, A.od_col, A.lo_ptr,
-	                                      A.lo_idx, A.up_ptr, A.up_idx, b, x, r);
+	                                      A.lo_idx, A.up_ptr, A.up_idx, b, x, r, A.dof);
 }
 
 __global__ void k_axpy(int64_t total, const double *__restrict__ d, double *__restrict__ x)

@@ -36,7 +36,8 @@ struct Error {
 // assembly tree).  Computed on the host, mirrored to the device.
 // ---------------------------------------------------------------------------
 struct Symbolic {
-	int nblk = 0;                 // particles (6x6 blocks)
+	int nblk = 0;                 // particles (dof x dof blocks)
+	int dof = 6;                  // scalar unknowns per particle: 6, or 3 for the in-plane part of a 2D system
 	std::vector<int> perm;        // perm[k] = particle at permuted position k
 	std::vector<int> iperm;       // iperm[particle] = permuted position
 	// supernodes, in postorder (children before parents)
@@ -74,9 +75,11 @@ struct Symbolic {
 // Build the symbolic analysis.  od_row/od_col: nb lower off-diagonal blocks
 // (the pattern).  pos (3 * nblk, may be null) drives a geometric nested
 // dissection; otherwise a breadth-first level-set dissection is used.
+// dof: scalar unknowns per particle (6; 3 for the in-plane x, z translation
+// and y rotation of a 2D system); it scales the front sizes only.
 void symbolic_analyze(Symbolic &S, int nblk, int nb, const int32_t *od_row,
                       const int32_t *od_col, const double *pos, double lx, double ly, double lz,
-                      int leaf_size);
+                      int leaf_size, int dof = 6);
 
 // ---------------------------------------------------------------------------
 // Device-side multifrontal factor (one precision per instance).
@@ -89,6 +92,7 @@ struct SolvePhase { int type, lev_off, gx, gy, gz, nchunk; };
 
 struct DevSymbolic {
 	int nblk = 0, nsn = 0, nlevels = 0, nb = 0;
+	int dof = 6;                   // scalar unknowns per particle (6 or 3)
 	int *perm = nullptr, *iperm = nullptr;
 	int *sn_first = nullptr, *sn_n = nullptr, *sn_m = nullptr, *sn_ld = nullptr;
 	int *sn_rows_off = nullptr, *rows = nullptr;
@@ -112,7 +116,7 @@ struct DevSymbolic {
 	struct Launch { int kind; int level; int k; int64_t off; int count; };
 	std::vector<Launch> factor_plan;
 	std::vector<int> h_level_off, h_level_d_off, h_level_od_off;
-	std::vector<int> h_level_maxn6, h_level_maxm6;   // per-level maxima of 6n and 6m
+	std::vector<int> h_level_maxn6, h_level_maxm6;   // per-level maxima of dof n and dof m (scalar)
 	std::vector<int64_t> h_col_task_off;
 	int64_t arena_elems = 0, w_elems = 0;
 	int max_F = 0;
@@ -170,6 +174,7 @@ int factor_multiply(DevFactor<T> &F, const DevSymbolic &D, int k, const double *
 // Lower/upper adjacency lists for the per-block-row gather.
 struct DevBlockMatrix {
 	int n = 0, nb = 0;
+	int dof = 6;                 // unknowns per particle of the solved system (6, or 3: components 0, 2, 4)
 	double *dblocks = nullptr;   // n x 15
 	double *odblocks = nullptr;  // nb x 18
 	int *od_row = nullptr, *od_col = nullptr;

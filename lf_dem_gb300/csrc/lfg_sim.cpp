@@ -206,7 +206,10 @@ Sim::Sim(const lfg_params &p, const lfg_options &o, int n, const double *pos, co
 	int ncell = S_.ncx*S_.ncy*S_.ncz;
 	dalloc(S_.cell_of, n, st_); dalloc(S_.cell_count, ncell, st_); dalloc(S_.cell_start, ncell+1, st_); dalloc(S_.cell_list, n, st_);
 	dalloc(S_.cand_count, std::max(n, ncell), st_); dalloc(S_.cand_ptr, n+1, st_);
-	solver_ = new Solver(n, opt_, st_);
+	// a monolayer's in-plane unknowns (x, z, rotation about y) decouple from
+	// the others: solve them alone unless asked for LF_DEM's 6x6 blocks
+	int dof = (S_.P.twodim && !S_.P.brownian_on && o.dof_2d != 6) ? 3 : 6;
+	solver_ = new Solver(n, opt_, st_, dof);
 	h_pos_.assign(pos, pos+3*n);
 	rebuild_superset();
 	// System::setupGenericConfiguration -> checkNewInteraction (System.cpp:517-519)

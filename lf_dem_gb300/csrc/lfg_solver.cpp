@@ -12,9 +12,11 @@
 namespace lfg {
 int fail(lfg_status *st, int code, int info, const char *msg);
 
-Solver::Solver(int n, const lfg_options &o, cudaStream_t st) : n_(n), opt_(o), st_(st)
+Solver::Solver(int n, const lfg_options &o, cudaStream_t st, int dof) : n_(n), dof_(dof), opt_(o), st_(st)
 {
+	if (dof != 6 && dof != 3) throw Error{LFG_ERR_BAD_ARG, dof, "degrees of freedom per particle must be 6 or 3"};
 	A_.n = n;
+	A_.dof = dof;
 	LFG_CUDA(cudaMalloc((void **)&A_.dblocks, sizeof(double)*15*(size_t)std::max(n, 1)));
 	LFG_CUDA(cudaMalloc((void **)&A_.lo_ptr, sizeof(int)*(n+1)));
 	LFG_CUDA(cudaMalloc((void **)&A_.up_ptr, sizeof(int)*(n+1)));
@@ -58,7 +60,7 @@ void Solver::set_pattern(int nb, const int32_t *row, const int32_t *col, const d
 	pat_c_ = c;
 	pat_pos_.assign(pos ? pos : nullptr, pos ? pos+3*(size_t)n_ : nullptr);
 	pat_box_[0] = lx; pat_box_[1] = ly; pat_box_[2] = lz;
-	symbolic_analyze(S_, n_, nb, r.data(), c.data(), pos, lx, ly, lz, opt_.leaf_size);
+	symbolic_analyze(S_, n_, nb, r.data(), c.data(), pos, lx, ly, lz, opt_.leaf_size, dof_);
 	dev_symbolic_upload(D_, S_, nb, factor_panel_width(opt_.precision), factor_tile_size(opt_.precision),
 	                    factor_syrk_tile_size(opt_.precision), opt_.precision == LFG_PREC_FP32_REFINE, st_);
 	if (opt_.precision == LFG_PREC_FP64) factor_alloc(F64_, D_, 4);
@@ -178,7 +180,9 @@ int Solver::check_factor(lfg_status *st)
 	if (*h_status_ == 0) return fail(st, LFG_ERR_TIMEOUT, 0, "a bounded device wait gave up");
 	if (*h_status_ != 0x7fffffff) {
 		int q = *h_status_-1;
-		int orig = S_.perm[q/6]*6+q%6;
+		// scalar column of the caller's 6-per-particle numbering (dof 3:
+		// components 0, 2, 4)
+		int orig = dof_ == 6 ? S_.perm[q/6]*6+q%6 : S_.perm[q/3]*6+2*(q%3);
 		if (st) {
 			st->code = LFG_ERR_NOT_SPD;
 			st->info = orig+1;

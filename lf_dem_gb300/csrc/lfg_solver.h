@@ -8,7 +8,10 @@ namespace lfg {
 
 class Solver {
 public:
-	Solver(int n, const lfg_options &o, cudaStream_t st);
+	// dof: 6, or 3 for the in-plane unknowns (x, z translation, y rotation)
+	// of a 2D system; right-hand sides and solutions keep 6 values per
+	// particle either way
+	Solver(int n, const lfg_options &o, cudaStream_t st, int dof = 6);
 	~Solver();
 	// pattern of the lower off-diagonal blocks; re-runs the symbolic analysis
 	void set_pattern(int nb, const int32_t *row, const int32_t *col, const double *pos, double lx,
@@ -30,6 +33,7 @@ public:
 	void stats(lfg_solver_stats *o) const;
 	bool analyzed() const { return analyzed_; }
 	int n() const { return n_; }
+	int dof() const { return dof_; }
 	int nb() const { return nb_; }
 	int symbolic_runs() const { return symbolic_runs_; }
 	int last_iters() const { return last_iters_; }
@@ -53,7 +57,7 @@ private:
 	void run_graph(int kind, int k, const void *b, const void *x, const std::function<void()> &body);
 	void ensure_refine_ws(int k);
 
-	int n_ = 0, nb_ = 0;
+	int n_ = 0, nb_ = 0, dof_ = 6;
 	lfg_options opt_;
 	cudaStream_t st_;
 	Symbolic S_;

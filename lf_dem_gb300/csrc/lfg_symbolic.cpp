@@ -396,11 +396,13 @@ struct Dissector {
 } // namespace
 
 void symbolic_analyze(Symbolic &S, int n, int nb, const int32_t *od_row, const int32_t *od_col,
-                      const double *pos, double lx, double ly, double lz, int leaf_size)
+                      const double *pos, double lx, double ly, double lz, int leaf_size, int dof)
 {
 	(void)lx; (void)lz;
+	if (dof != 6 && dof != 3) throw Error{LFG_ERR_BAD_ARG, dof, "degrees of freedom per particle must be 6 or 3"};
 	S = Symbolic();
 	S.nblk = n;
+	S.dof = dof;
 	Graph g = build_graph(n, nb, od_row, od_col);
 	Dissector D(g, pos, ly == 0, std::max(1, leaf_size), n);
 	std::vector<int> all(n);
@@ -489,7 +491,7 @@ void symbolic_analyze(Symbolic &S, int n, int nb, const int32_t *od_row, const i
 	int64_t off = 0, woff = 0;
 	S.max_F = 0; S.nnz_L = 0; S.flops = 0;
 	for (int s = 0; s < nsn; s++) {
-		int n6 = 6*S.sn_n[s], m6 = 6*S.sn_m[s], F6 = n6+m6;
+		int n6 = dof*S.sn_n[s], m6 = dof*S.sn_m[s], F6 = n6+m6;
 		S.sn_ld[s] = F6+n6;
 		S.sn_off[s] = off;
 		off += (int64_t)S.sn_ld[s]*F6;
@@ -614,6 +616,8 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 {
 	dev_symbolic_free(D);
 	D.nblk = S.nblk; D.nsn = S.nsn; D.nlevels = S.nlevels; D.nb = nb;
+	const int dof = S.dof;
+	D.dof = dof;
 	D.arena_elems = S.arena_elems; D.w_elems = S.w_elems; D.max_F = S.max_F;
 	D.flops = S.flops; D.nnz_L = S.nnz_L;
 	up(D.perm, S.perm, st); up(D.iperm, S.iperm, st);
@@ -630,13 +634,13 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 	D.h_level_d_off = S.level_d_off;
 	D.h_level_od_off = S.level_od_off;
 	D.max_n6 = 0;
-	for (int s = 0; s < S.nsn; s++) D.max_n6 = std::max(D.max_n6, 6*S.sn_n[s]);
+	for (int s = 0; s < S.nsn; s++) D.max_n6 = std::max(D.max_n6, dof*S.sn_n[s]);
 	D.h_level_maxn6.assign(S.nlevels, 0);
 	D.h_level_maxm6.assign(S.nlevels, 0);
 	for (int s = 0; s < S.nsn; s++) {
 		int l = S.sn_level[s];
-		D.h_level_maxn6[l] = std::max(D.h_level_maxn6[l], 6*S.sn_n[s]);
-		D.h_level_maxm6[l] = std::max(D.h_level_maxm6[l], 6*S.sn_m[s]);
+		D.h_level_maxn6[l] = std::max(D.h_level_maxn6[l], dof*S.sn_n[s]);
+		D.h_level_maxm6[l] = std::max(D.h_level_maxm6[l], dof*S.sn_m[s]);
 	}
 	// assembly column tasks, panel tasks and update tiles, level by level
 	std::vector<int> col_tasks;
@@ -648,9 +652,9 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 		int kmax = 0;
 		for (int t = S.level_off[l]; t < S.level_off[l+1]; t++) {
 			int s = S.level_sn[t];
-			int F6 = 6*(S.sn_n[s]+S.sn_m[s]);
+			int F6 = dof*(S.sn_n[s]+S.sn_m[s]);
 			for (int c = 0; c < F6; c++) { col_tasks.push_back(s); col_tasks.push_back(c); }
-			kmax = std::max(kmax, (6*S.sn_n[s]+panel_nb-1)/panel_nb);
+			kmax = std::max(kmax, (dof*S.sn_n[s]+panel_nb-1)/panel_nb);
 		}
 		D.factor_plan.push_back({PLAN_ASSEMBLE, l, 0, c0, (int)((int64_t)col_tasks.size()/2-c0)});
 		// one launch for the level's diagonal and off-diagonal blocks (ranges
@@ -663,7 +667,7 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 			int64_t d0 = (int64_t)diag_tasks.size();
 			for (int t = S.level_off[l]; t < S.level_off[l+1]; t++) {
 				int s = S.level_sn[t];
-				int n6 = 6*S.sn_n[s];
+				int n6 = dof*S.sn_n[s];
 				if (n6 > 0) diag_tasks.push_back(make_int4(s, 0, 0, std::min(panel_nb, n6)));
 			}
 			D.factor_plan.push_back({PLAN_DIAG, l, 0, d0, (int)((int64_t)diag_tasks.size()-d0)});
@@ -675,14 +679,14 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 			// dispatched in the first wave
 			for (int t = S.level_off[l]; t < S.level_off[l+1]; t++) {
 				int s = S.level_sn[t];
-				int n6 = 6*S.sn_n[s];
+				int n6 = dof*S.sn_n[s];
 				if (n6 <= k*panel_nb) continue;
 				int t0 = k*panel_nb+std::min(panel_nb, n6-k*panel_nb);
 				if (t0 < n6) tile_tasks.push_back(make_int4(s, t0, t0, k));
 			}
 			for (int t = S.level_off[l]; t < S.level_off[l+1]; t++) {
 				int s = S.level_sn[t];
-				int n6 = 6*S.sn_n[s], F6 = n6+6*S.sn_m[s];
+				int n6 = dof*S.sn_n[s], F6 = n6+dof*S.sn_m[s];
 				if (n6 <= k*panel_nb) continue;
 				int w = std::min(panel_nb, n6-k*panel_nb);
 				int t0 = k*panel_nb+w;
@@ -705,7 +709,7 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 		int64_t s0 = (int64_t)tile_tasks.size();
 		for (int t = S.level_off[l]; t < S.level_off[l+1]; t++) {
 			int s = S.level_sn[t];
-			int n6 = 6*S.sn_n[s], F6 = n6+6*S.sn_m[s];
+			int n6 = dof*S.sn_n[s], F6 = n6+dof*S.sn_m[s];
 			for (int r = n6; r < F6; r += syrk_tile)
 				for (int c = n6; c <= r; c += syrk_tile)
 					tile_tasks.push_back(make_int4(s, r, c, 0));
