@@ -352,6 +352,13 @@ typedef struct {
 	int64_t launches;
 	double factor_flops;     /* algorithmic flops of one factorisation */
 	double solve_bytes;      /* algorithmic bytes of one forward+backward solve, 1 RHS */
+	double rebuild_ms;       /* host wall time of the pair-superset rebuilds since the last
+	                            lfg_sim_clear_step_times: candidate pairs, symbolic analysis
+	                            (cholmod_analyze's counterpart, StokesSolver.cpp:955-962) and
+	                            upload, plus the capture of the new factorisation and solve
+	                            graphs after them */
+	int rebuilds;            /* number of those rebuilds */
+	int pad_;
 } lfg_sim_timing;
 int lfg_sim_get_timing(lfg_sim *s, lfg_sim_timing *out);
 
@@ -435,6 +442,37 @@ int lfg_batch_autotune(lfg_batch *b, const int *leaf_sizes, int count, int steps
 /* The leaf size chosen for (n, precision), 0 if none. */
 int lfg_batch_tuned_leaf(const lfg_batch *b, int n, int precision);
 void lfg_batch_destroy(lfg_batch *b);
+
+/* Fused batch: the suspensions advance in lockstep through ONE joint
+ * factorisation and solve of the block-diagonal system of all of them (the
+ * assembly trees merged level by level from the leaves), so each launch of
+ * the factorisation and of the solve serves every suspension; each half step
+ * is a CUDA graph (the suspensions' own kernels on parallel branches) that
+ * is captured once per joint analysis and replayed.  The FP32 refinement
+ * stops when every suspension's own relative residual meets the tolerance.
+ * Each suspension's results are those it gets alone, to the solve's
+ * tolerance (1e-10 relative in FP64, 1e-8 with FP32 + refinement).  The
+ * host waits three times per step (after each solve and after the
+ * corrector's superset check); a pattern change of any suspension redoes
+ * its analysis and the joint one.  Same calls as a batch: lfg_batch_add
+ * (predictor-corrector, no Brownian force, all 3D or all 2D; the options'
+ * precision is replaced by the batch's), lfg_batch_run, lfg_batch_advance
+ * (lockstep until each suspension reaches its strain, the finished ones
+ * waiting, then one stress-computing step of all), lfg_batch_autotune (the
+ * leaf size of all suspensions, timed on the fused step), lfg_batch_sim (to
+ * read a suspension's state; it cannot step on its own). */
+int lfg_batch_create_fused(int device, int precision, lfg_batch **out, lfg_status *st);
+
+/* Counters of a batch: kernels launched so far (graph kernel nodes counted
+ * per replay), joint analyses (fused), factorisation flops of the joint
+ * system (fused), refinement iterations of the last solve (fused FP32). */
+typedef struct {
+	int64_t kernels;
+	int joint_analyses, last_refine_iters;
+	double factor_flops;
+	int fused, pad_;
+} lfg_batch_stats;
+int lfg_batch_get_stats(const lfg_batch *b, lfg_batch_stats *out);
 
 /* Server: requests admitted while fewer than max_active run and their
  * estimated footprint fits in hbm_budget_bytes next to the running ones

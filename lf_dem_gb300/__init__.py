@@ -123,9 +123,14 @@ class ServerStats(C.Structure):
                 ("peak_reserved_bytes", C.c_int64), ("budget_bytes", C.c_int64)]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("kernels", C.c_int64), ("joint_analyses", C.c_int), ("last_refine_iters", C.c_int),
+                ("factor_flops", C.c_double), ("fused", C.c_int), ("pad_", C.c_int)]
+
+
 class SimTiming(C.Structure):
     _fields_ = [("ms", C.c_double * 8), ("launches", C.c_int64), ("factor_flops", C.c_double),
-                ("solve_bytes", C.c_double)]
+                ("solve_bytes", C.c_double), ("rebuild_ms", C.c_double), ("rebuilds", C.c_int), ("pad_", C.c_int)]
 
 
 # Every extern "C" symbol declared in include/lfdem_gb300.h.
@@ -142,7 +147,8 @@ EXPORTS = [
     "lfg_sim_get_contact_states", "lfg_conf_write_binary", "lfg_conf_read_binary", "lfg_checkpoint_write",
     "lfg_checkpoint_read", "lfg_sim_set_leaf_size", "lfg_sim_device_bytes", "lfg_footprint_estimate",
     "lfg_batch_create", "lfg_batch_add", "lfg_batch_size", "lfg_batch_sim", "lfg_batch_run", "lfg_batch_advance",
-    "lfg_batch_autotune", "lfg_batch_tuned_leaf", "lfg_batch_destroy",
+    "lfg_batch_autotune", "lfg_batch_tuned_leaf", "lfg_batch_destroy", "lfg_batch_create_fused",
+    "lfg_batch_get_stats",
     "lfg_server_create", "lfg_server_submit", "lfg_server_poll", "lfg_server_wait", "lfg_server_final_positions",
     "lfg_server_get_stats", "lfg_server_destroy",
     "lfg_config_output", "lfg_output_open", "lfg_output_write", "lfg_output_close", "lfg_solver_multiply_factor",
@@ -243,6 +249,8 @@ def load(path: str | None = None):
         L.lfg_batch_tuned_leaf.argtypes = [vp, C.c_int, C.c_int]
         L.lfg_batch_destroy.argtypes = [vp]
         L.lfg_batch_destroy.restype = None
+        L.lfg_batch_create_fused.argtypes = [C.c_int, C.c_int, C.POINTER(vp), pst]
+        L.lfg_batch_get_stats.argtypes = [vp, C.POINTER(BatchStats)]
         L.lfg_server_create.argtypes = [C.c_int, C.c_int, C.c_int64, C.POINTER(vp), pst]
         L.lfg_server_submit.argtypes = [vp, C.POINTER(Request), pst]
         L.lfg_server_poll.argtypes = [vp, C.POINTER(Result), C.c_int]
@@ -647,7 +655,7 @@ class Sim:
         t = SimTiming()
         load().lfg_sim_get_timing(self.h, C.byref(t))
         return {"ms": list(t.ms), "launches": t.launches, "factor_flops": t.factor_flops,
-                "solve_bytes": t.solve_bytes}
+                "solve_bytes": t.solve_bytes, "rebuild_ms": t.rebuild_ms, "rebuilds": t.rebuilds}
 
 
 def footprint_estimate(n: int, precision: int = PREC_FP32_REFINE) -> int:
@@ -657,11 +665,17 @@ def footprint_estimate(n: int, precision: int = PREC_FP32_REFINE) -> int:
 class Batch:
     """Many suspensions on one GPU (lfg_batch_*), stepped together."""
 
-    def __init__(self, device: int = 0, nthreads: int = 0):
+    def __init__(self, device: int = 0, nthreads: int = 0, fused: bool = False, precision: int = PREC_FP32_REFINE):
+        """fused: lockstep through one joint factorisation and solve
+        (lfg_batch_create_fused, all suspensions in `precision`); otherwise
+        each suspension on its own stream, driven by nthreads host workers."""
         L = load()
         h = C.c_void_p()
         st = Status()
-        _check(L.lfg_batch_create(device, nthreads, C.byref(h), C.byref(st)), st)
+        if fused:
+            _check(L.lfg_batch_create_fused(device, precision, C.byref(h), C.byref(st)), st)
+        else:
+            _check(L.lfg_batch_create(device, nthreads, C.byref(h), C.byref(st)), st)
         self.h = h
         self.n = []
         self._keep = []
@@ -698,6 +712,11 @@ class Batch:
 
     def tuned_leaf(self, n: int, precision: int) -> int:
         return int(load().lfg_batch_tuned_leaf(self.h, int(n), int(precision)))
+
+    def stats(self) -> dict:
+        s = BatchStats()
+        load().lfg_batch_get_stats(self.h, C.byref(s))
+        return {k: getattr(s, k) for k, _ in BatchStats._fields_ if k != "pad_"}
 
     def close(self):
         if getattr(self, "h", None):

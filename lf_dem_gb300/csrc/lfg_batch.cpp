@@ -121,6 +121,8 @@ int size_class(int n, int precision) { return 2*(int)std::lround(2*std::log2((do
 struct lfg_batch {
 	int device = 0;
 	int nthreads = 1;
+	FusedGroup *fused = nullptr;     // lockstep through one joint solver (lfg_batch_create_fused)
+	int fused_precision = 0;
 	std::vector<lfg_sim *> sims;
 	std::vector<int> n, precision;
 	std::map<int, int> tuned_leaf;   // size class -> leaf size
@@ -158,6 +160,30 @@ int lfg_batch_create(int device, int nthreads, lfg_batch **out, lfg_status *st)
 	}
 }
 
+int lfg_batch_create_fused(int device, int precision, lfg_batch **out, lfg_status *st)
+{
+	if (!out) return fail(st, LFG_ERR_BAD_ARG, 0, "null output");
+	if (precision != LFG_PREC_FP64 && precision != LFG_PREC_FP32_REFINE)
+		return fail(st, LFG_ERR_BAD_ARG, precision, "unknown precision");
+	int rc = check_device(device, st);
+	if (rc) return rc;
+	lfg_batch *b = nullptr;
+	try {
+		b = new lfg_batch();
+		b->device = device;
+		b->fused_precision = precision;
+		b->fused = fused_create(device, precision);
+		*out = b;
+		return ok(st);
+	} catch (const Error &e) {
+		delete b;
+		return fail(st, e.code, e.info, e.msg.c_str());
+	} catch (...) {
+		delete b;
+		return fail(st, LFG_ERR_OOM, 0, "allocation failed");
+	}
+}
+
 int lfg_batch_add(lfg_batch *b, const lfg_params *p, const lfg_options *opt, int n, const double *pos,
                   const double *radius, double lx, double ly, double lz, const double *le_disp, int *slot,
                   lfg_status *st)
@@ -166,10 +192,12 @@ int lfg_batch_add(lfg_batch *b, const lfg_params *p, const lfg_options *opt, int
 	lfg_options o;
 	if (opt) o = *opt; else lfg_default_options(&o);
 	o.device = b->device;
+	if (b->fused) o.precision = b->fused_precision;
 	auto it = b->tuned_leaf.find(size_class(n, o.precision));
 	if (it != b->tuned_leaf.end()) o.leaf_size = it->second;
 	lfg_sim *s = nullptr;
-	int rc = lfg_sim_create(p, &o, n, pos, radius, lx, ly, lz, le_disp, 0, nullptr, nullptr, nullptr, &s, st);
+	int rc = b->fused ? fused_add(b->fused, p, &o, n, pos, radius, lx, ly, lz, le_disp, &s, st)
+	                  : lfg_sim_create(p, &o, n, pos, radius, lx, ly, lz, le_disp, 0, nullptr, nullptr, nullptr, &s, st);
 	if (rc) return rc;
 	b->sims.push_back(s);
 	b->n.push_back(n);
@@ -217,9 +245,24 @@ static int batch_drive(lfg_batch *b, const std::function<int(int, bool *, lfg_st
 	return ok(st);
 }
 
+// the fused group's calls, errors as status codes
+static int fused_call(lfg_batch *b, const std::function<void()> &f, lfg_status *st)
+{
+	try {
+		cudaSetDevice(b->device);
+		f();
+		return ok(st);
+	} catch (const Error &e) {
+		return fail(st, e.code, e.info, e.msg.c_str());
+	} catch (const std::bad_alloc &) {
+		return fail(st, LFG_ERR_OOM, 0, "host allocation failed");
+	}
+}
+
 int lfg_batch_run(lfg_batch *b, int nsteps, lfg_status *st)
 {
 	if (!b || nsteps < 0) return fail(st, LFG_ERR_BAD_ARG, 0, "bad arguments");
+	if (b->fused) return fused_call(b, [&] { fused_run(b->fused, nsteps); }, st);
 	std::vector<int> left(b->sims.size(), nsteps);
 	const int slice = 2;
 	return batch_drive(b, [&](int slot, bool *done, lfg_status *s) {
@@ -234,6 +277,7 @@ int lfg_batch_run(lfg_batch *b, int nsteps, lfg_status *st)
 int lfg_batch_advance(lfg_batch *b, const double *strain_end, lfg_status *st)
 {
 	if (!b || !strain_end) return fail(st, LFG_ERR_BAD_ARG, 0, "bad arguments");
+	if (b->fused) return fused_call(b, [&] { fused_advance(b->fused, strain_end); }, st);
 	const int slice = 2;
 	return batch_drive(b, [&](int slot, bool *done, lfg_status *s) {
 		int d = 0;
@@ -249,6 +293,26 @@ int lfg_batch_advance(lfg_batch *b, const double *strain_end, lfg_status *st)
 int lfg_batch_autotune(lfg_batch *b, const int *leaf_sizes, int count, int steps, lfg_status *st)
 {
 	if (!b || !leaf_sizes || count <= 0 || steps <= 0) return fail(st, LFG_ERR_BAD_ARG, 0, "bad arguments");
+	if (b->fused) {
+		// one leaf size for the joint system: time the fused step with each
+		// (after a step that captures its graphs), keep the fastest
+		double best = 1e300;
+		int best_leaf = leaf_sizes[0];
+		for (int c = 0; c < count; c++) {
+			int rc = fused_call(b, [&] {
+				fused_set_leaf_size(b->fused, leaf_sizes[c]);
+				fused_run(b->fused, 1);
+				cudaDeviceSynchronize();
+				auto t0 = std::chrono::steady_clock::now();
+				fused_run(b->fused, steps);
+				double t = now_s(t0);
+				if (t < best) { best = t; best_leaf = leaf_sizes[c]; }
+			}, st);
+			if (rc) return rc;
+		}
+		for (size_t i = 0; i < b->sims.size(); i++) b->tuned_leaf[size_class(b->n[i], b->precision[i])] = best_leaf;
+		return fused_call(b, [&] { fused_set_leaf_size(b->fused, best_leaf); }, st);
+	}
 	std::map<int, std::vector<int>> classes;
 	for (int i = 0; i < (int)b->sims.size(); i++) classes[size_class(b->n[i], b->precision[i])].push_back(i);
 	for (auto &kv : classes) {
@@ -286,10 +350,31 @@ int lfg_batch_tuned_leaf(const lfg_batch *b, int n, int precision)
 	return it == b->tuned_leaf.end() ? 0 : it->second;
 }
 
+int lfg_batch_get_stats(const lfg_batch *b, lfg_batch_stats *out)
+{
+	if (!b || !out) return LFG_ERR_BAD_ARG;
+	std::memset(out, 0, sizeof *out);
+	out->fused = b->fused != nullptr;
+	if (b->fused) {
+		fused_stats(b->fused, &out->kernels, &out->joint_analyses, &out->factor_flops, &out->last_refine_iters);
+	} else {
+		for (lfg_sim *s : b->sims) {
+			lfg_sim_timing t;
+			if (lfg_sim_get_timing(s, &t) == LFG_OK) out->factor_flops += t.factor_flops;
+			double ms;
+			int64_t k = 0;
+			lfg_sim_get_step_times(s, &ms, 0, &k);
+			out->kernels += k;
+		}
+	}
+	return LFG_OK;
+}
+
 void lfg_batch_destroy(lfg_batch *b)
 {
 	if (!b) return;
 	delete b->pool;
+	if (b->fused) fused_destroy(b->fused);   // before its members: it refers to them
 	for (lfg_sim *s : b->sims) lfg_sim_destroy(s);
 	delete b;
 }

@@ -1930,14 +1930,18 @@ void axpy_vec(int n, int k, const double *d, double *x, cudaStream_t st)
 // per-RHS sums of squares of r and b, single CTA per RHS (fixed order)
 // squared norms of r and b per right-hand side (one CTA of 1024 threads each;
 // a fixed reduction order: per thread, then warps by shuffles, then warps)
+// squared norms of r and b per right-hand side and segment: segment q of a
+// right-hand side is entries [seg[q], seg[q+1]) (one segment, [0, n6), when
+// seg is null); out[2 (rh nseg + q)] = |r|^2, then |b|^2
 __global__ void __launch_bounds__(1024) k_norms(int n6, const double *__restrict__ r, const double *__restrict__ b,
-                                                double *out)
+                                                const int *__restrict__ seg, double *out)
 {
 	__shared__ double sr[32], sb[32];
-	int rh = blockIdx.x;
+	int rh = blockIdx.x, q = blockIdx.y, nseg = gridDim.y;
+	int lo = seg ? seg[q] : 0, hi = seg ? seg[q+1] : n6;
 	double a = 0, c = 0;
 #pragma unroll 4
-	for (int i = threadIdx.x; i < n6; i += blockDim.x) {
+	for (int i = lo+threadIdx.x; i < hi; i += blockDim.x) {
 		double u = r[(int64_t)rh*n6+i], v = b[(int64_t)rh*n6+i];
 		a += u*u;
 		c += v*v;
@@ -1956,13 +1960,14 @@ __global__ void __launch_bounds__(1024) k_norms(int n6, const double *__restrict
 			a += __shfl_down_sync(FULL_MASK, a, o);
 			c += __shfl_down_sync(FULL_MASK, c, o);
 		}
-		if (l == 0) { out[2*rh] = a; out[2*rh+1] = c; }
+		if (l == 0) { out[2*(rh*nseg+q)] = a; out[2*(rh*nseg+q)+1] = c; }
 	}
 }
 
-void residual_norms(int n6, int k, const double *r, const double *b, double *out, cudaStream_t st)
+void residual_norms(int n6, int k, const double *r, const double *b, double *out, cudaStream_t st,
+                    const int *seg, int nseg)
 {
-	k_norms<<<k, 1024, 0, st>>>(n6, r, b, out);
+	k_norms<<<dim3(k, seg ? nseg : 1), 1024, 0, st>>>(n6, r, b, seg, out);
 }
 
 int factor_tile_size(int precision) { return precision == LFG_PREC_FP64 ? Cfg<double>::TILE : Cfg<float>::TILE; }

@@ -81,6 +81,11 @@ void symbolic_analyze(Symbolic &S, int nblk, int nb, const int32_t *od_row,
                       const int32_t *od_col, const double *pos, double lx, double ly, double lz,
                       int leaf_size, int dof = 6);
 
+// The joint analysis of independent systems (the block-diagonal matrix of
+// all of them): parts concatenated, levels of their assembly trees merged
+// from the leaves.
+void symbolic_concat(Symbolic &J, const std::vector<const Symbolic *> &parts);
+
 // ---------------------------------------------------------------------------
 // Device-side multifrontal factor (one precision per instance).
 // ---------------------------------------------------------------------------
@@ -200,8 +205,25 @@ struct OutputSnapshot {
 	int out_w = 0;
 };
 
+// Fused batch (lfg_sim.cpp): suspensions stepping in lockstep through one
+// joint solver.  fused_add creates a member simulation (owned by the caller,
+// destroyed with lfg_sim_destroy after the group).
+class FusedGroup;
+FusedGroup *fused_create(int device, int precision);
+void fused_destroy(FusedGroup *g);
+int fused_add(FusedGroup *g, const lfg_params *p, const lfg_options *opt, int n, const double *pos,
+              const double *radius, double lx, double ly, double lz, const double *le_disp, lfg_sim **out,
+              lfg_status *st);
+void fused_run(FusedGroup *g, int nsteps);
+void fused_advance(FusedGroup *g, const double *strain_end);
+void fused_set_leaf_size(FusedGroup *g, int leaf);
+void fused_stats(const FusedGroup *g, int64_t *kernels, int *joint_runs, double *flops, int *iters);
+
 void axpy_vec(int n, int k, const double *d, double *x, cudaStream_t st);
-// per-RHS squared norms of r and b, written to out[2k] (device)
-void residual_norms(int n6, int k, const double *r, const double *b, double *out, cudaStream_t st);
+// per-RHS squared norms of r and b, written to out[2k] (device); with a
+// segment table seg (nseg + 1 offsets into each right-hand side, device), per
+// right-hand side and segment: out[2 (rh nseg + q)]
+void residual_norms(int n6, int k, const double *r, const double *b, double *out, cudaStream_t st,
+                    const int *seg = nullptr, int nseg = 1);
 
 } // namespace lfg

@@ -11,6 +11,8 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <functional>
+#include <map>
 #include <new>
 
 #include "lfg_physics.h"
@@ -23,8 +25,10 @@ int check_device(int device, lfg_status *st);
 
 class Sim {
 public:
+	// fused: a member of a fused batch (its solver only analyses the pattern;
+	// the batch's joint solver factors and solves)
 	Sim(const lfg_params &p, const lfg_options &o, int n, const double *pos, const double *radius, double lx,
-	    double ly, double lz, const double *le_disp, cudaStream_t st);
+	    double ly, double lz, const double *le_disp, cudaStream_t st, bool fused = false);
 	~Sim();
 	void set_contacts(int ncs, const int32_t *p0, const int32_t *p1, const double *dt);
 	void first_time();
@@ -51,11 +55,46 @@ public:
 	int64_t device_bytes() const;
 	std::vector<double> step_ms;
 	int64_t step_kernels = 0;
+	double rebuild_ms_ = 0;   // host wall time of superset rebuilds (see lfg_sim_timing)
+	int rebuilds_ = 0;
+	double capture_mark_ = 0; // the solver's graph-capture time at the last clear
+	void clear_timing() { step_ms.clear(); step_kernels = 0; rebuild_ms_ = 0; rebuilds_ = 0;
+	                      capture_mark_ = solver_->capture_ms(); }
 	int error_code = 0, error_info = 0;
 	std::string error_msg;
 
-private:
+	// stages of a step (see compute_velocities); used by step() and by the
+	// lockstep driver of a fused batch
+	void pc_pre_solve(double *dbl, double *odbl);
+	int pc_forces_rhs(int calc_stress, int in_predictor, double **rhs, double **sol);
+	void pc_post_solve(int calc_stress, int in_predictor);
+	void pc_move_predictor(int calc_stress, double time_end, double strain_end, bool timed);
+	void pc_move_corrector(int calc_stress, bool timed);
+	void superset_check_launch();
 	void rebuild_superset();
+	DevSim &dev() { return S_; }
+	DevClock *host_clock() { return h_clock_; }
+	void pull_clock_public() { pull_clock(); }
+	// the clock's copy to the host (pinned), ordered on this stream
+	void queue_clock_copy()
+	{
+		LFG_CUDA(cudaMemcpyAsync(h_clock_, S_.clock, sizeof(DevClock), cudaMemcpyDeviceToHost, st_));
+	}
+	// right-hand sides solved for in a half step and where they and their
+	// solutions live (as pc_forces_rhs, without launching anything)
+	int rhs_count(int calc_stress, double **rhs, double **sol)
+	{
+		int divided = (calc_stress || prm_.control == 1) ? 1 : 0;
+		*rhs = S_.rhs;
+		*sol = divided ? S_.vc : S_.sol;
+		return divided ? (S_.P.brownian_on ? NFC : NPFC) : 1;
+	}
+	Solver *solver() { return solver_; }
+	const lfg_params &params() const { return prm_; }
+	bool fused_ = false;      // member of a fused batch: no own factor, no own step
+	cudaStream_t stream() const { return st_; }
+
+private:
 	void compute_velocities(int calc_stress, int in_predictor);
 	void check_error();
 	void pull_clock();
@@ -155,8 +194,8 @@ template <typename V> static void dalloc(V *&p, size_t count, cudaStream_t st)
 }
 
 Sim::Sim(const lfg_params &p, const lfg_options &o, int n, const double *pos, const double *radius, double lx,
-         double ly, double lz, const double *le_disp, cudaStream_t st)
-    : prm_(p), opt_(o), st_(st)
+         double ly, double lz, const double *le_disp, cudaStream_t st, bool fused)
+    : fused_(fused), prm_(p), opt_(o), st_(st)
 {
 	avg_dt_ = p.fixed_dt ? p.dt : 0;
 	if (p.friction_model == 4 || p.friction_model < 0 || p.friction_model > 6)
@@ -209,7 +248,7 @@ Sim::Sim(const lfg_params &p, const lfg_options &o, int n, const double *pos, co
 	// a monolayer's in-plane unknowns (x, z, rotation about y) decouple from
 	// the others: solve them alone unless asked for LF_DEM's 6x6 blocks
 	int dof = (S_.P.twodim && !S_.P.brownian_on && o.dof_2d != 6) ? 3 : 6;
-	solver_ = new Solver(n, opt_, st_, dof);
+	solver_ = new Solver(n, opt_, st_, dof, fused);
 	h_pos_.assign(pos, pos+3*n);
 	rebuild_superset();
 	// System::setupGenericConfiguration -> checkNewInteraction (System.cpp:517-519)
@@ -326,25 +365,31 @@ void Sim::stage_end(int)
 	cur_stage_ = -1;
 }
 
-void Sim::compute_velocities(int calc_stress, int in_predictor)
+// Stages of a step, shared by step() (with this suspension's own solver) and
+// the lockstep driver of a fused batch (one joint solver for all its
+// suspensions, FusedGroup below).
+
+// System::computeVelocities (System.cpp:2273-2319) up to the factorisation:
+// the shear rate set to 1 under stress control, u_inf, the R_FU blocks
+// (into dbl / odbl)
+void Sim::pc_pre_solve(double *dbl, double *odbl)
 {
-	// System::computeVelocities (System.cpp:2273-2319)
-	bool stress_ctl = prm_.control == 1;
-	int divided = (calc_stress || stress_ctl) ? 1 : 0;
-	stage_begin(1);
-	if (stress_ctl) phys_set_shear_rate(S_, 1.0, false, st_);
+	if (prm_.control == 1) phys_set_shear_rate(S_, 1.0, false, st_);
 	phys_u_inf(S_, st_);
-	phys_blocks(S_, solver_->d_dblocks(), solver_->d_odblocks(), st_);
-	stage_end(1);
-	stage_begin(2);
-	solver_->factorize_async();
-	stage_end(2);
-	stage_begin(4);
+	phys_blocks(S_, dbl, odbl, st_);
+}
+
+// the force components and the right-hand sides; returns how many of them
+// are solved for and where they and the solutions live
+int Sim::pc_forces_rhs(int calc_stress, int in_predictor, double **rhs, double **sol)
+{
+	int divided = (calc_stress || prm_.control == 1) ? 1 : 0;
 	phys_force_components(S_, st_);
 	if (S_.P.brownian_on && in_predictor) {
 		// System::setBrownianForceToParticle (System.cpp:1665-1710): F_B =
 		// L (sqrt(2 kT/dt) psi) with the factor of this configuration, drawn
 		// in the predictor only (the corrector keeps it)
+		if (fused_) throw Error{LFG_ERR_BAD_ARG, 0, "Brownian forces in a fused batch"};
 		double *fb = S_.fc+(size_t)FC_BROWNIAN*6*S_.n;
 		if (fb_given_) {
 			fb_given_ = false;
@@ -354,22 +399,80 @@ void Sim::compute_velocities(int calc_stress, int in_predictor)
 		}
 	}
 	phys_rhs(S_, divided, st_);
+	int nrhs = S_.P.brownian_on ? NFC : NPFC;   // the Brownian component is the last
+	*rhs = S_.rhs;
+	*sol = divided ? S_.vc : S_.sol;
+	return divided ? nrhs : 1;
+}
+
+// after the solve: stress control's stresslets and shear rate, velocities
+void Sim::pc_post_solve(int calc_stress, int in_predictor)
+{
+	int divided = (calc_stress || prm_.control == 1) ? 1 : 0;
+	if (divided && prm_.control == 1) {
+		phys_stresslets(S_, in_predictor, st_);
+		phys_shear_rate_from_stress(S_, st_);
+	}
+	phys_velocities(S_, divided, in_predictor, st_);
+}
+
+// the predictor's move (System::timeStepMovePredictor, System.cpp:1124-1162)
+// and the interaction update at the moved positions
+void Sim::pc_move_predictor(int calc_stress, double time_end, double strain_end, bool timed)
+{
+	if (calc_stress) { if (timed) stage_begin(4); phys_stresslets(S_, 1, st_); if (timed) stage_end(4); }
+	if (timed) stage_begin(5);
+	// no adaptive time step with Brownian forces (System.cpp:1129, 1243)
+	if (!prm_.fixed_dt && !S_.P.brownian_on) phys_adapt_dt(S_, time_end, strain_end, st_);
+	phys_boxing(S_, st_);
+	phys_move(S_, 1, st_);
+	if (timed) { stage_end(5); stage_begin(0); }
+	phys_pairs_update(S_, 0, 1, false, st_);
+	if (timed) stage_end(0);
+	phys_save_pred(S_, st_);
+}
+
+// the corrector's move (System::timeStepMoveCorrector, System.cpp:1164-1187)
+void Sim::pc_move_corrector(int calc_stress, bool timed)
+{
+	if (calc_stress) { if (timed) stage_begin(4); phys_stresslets(S_, 0, st_); if (timed) stage_end(4); }
+	if (timed) stage_begin(5);
+	phys_move(S_, 2, st_);
+	if (timed) stage_end(5);
+}
+
+// checkNewInteraction: does the superset still hold every pair within range?
+// (the flag is read on the host)
+void Sim::superset_check_launch()
+{
+	LFG_CUDA(cudaMemsetAsync(&S_.clock->stale, 0, sizeof(int), st_));
+	phys_cells(S_, 0, st_);
+	phys_check_superset(S_, st_);
+}
+
+void Sim::compute_velocities(int calc_stress, int in_predictor)
+{
+	// System::computeVelocities (System.cpp:2273-2319)
+	stage_begin(1);
+	pc_pre_solve(solver_->d_dblocks(), solver_->d_odblocks());
+	stage_end(1);
+	stage_begin(2);
+	solver_->factorize_async();
+	stage_end(2);
+	stage_begin(4);
+	double *rhs = nullptr, *sol = nullptr;
+	int k = pc_forces_rhs(calc_stress, in_predictor, &rhs, &sol);
 	stage_end(4);
 	stage_begin(3);
 	lfg_status st;
 	std::memset(&st, 0, sizeof st);
-	int nrhs = S_.P.brownian_on ? NFC : NPFC;   // the Brownian component is the last
-	int rc = solver_->solve_device(divided ? nrhs : 1, S_.rhs, divided ? S_.vc : S_.sol, &st, false);
+	int rc = solver_->solve_device(k, rhs, sol, &st, false);
 	// factor and solve status (a non-positive pivot, or a bounded wait that gave up)
 	phys_sticky_status(solver_->d_status(), d_err_, st_);
 	stage_end(3);
 	if (rc == LFG_ERR_NOT_CONVERGED) { error_code = rc; error_msg = st.msg; }
 	stage_begin(4);
-	if (divided && stress_ctl) {
-		phys_stresslets(S_, in_predictor, st_);
-		phys_shear_rate_from_stress(S_, st_);
-	}
-	phys_velocities(S_, divided, in_predictor, st_);
+	pc_post_solve(calc_stress, in_predictor);
 	stage_end(4);
 }
 
@@ -381,6 +484,7 @@ void Sim::pull_clock()
 
 void Sim::step(int calc_stress, double time_end, double strain_end)
 {
+	if (fused_) throw Error{LFG_ERR_BAD_ARG, 0, "a suspension of a fused batch steps with its batch"};
 	first_time();
 	ev_used_ = 0;
 	int64_t l0 = S_.launches, k0 = solver_->kernels_launched();
@@ -402,32 +506,23 @@ void Sim::step(int calc_stress, double time_end, double strain_end)
 	} else {
 		// predictor (System.cpp:888-930, 1124-1162)
 		compute_velocities(calc_stress, 1);
-		if (calc_stress) { stage_begin(4); phys_stresslets(S_, 1, st_); stage_end(4); }
-		stage_begin(5);
-		// no adaptive time step with Brownian forces (System.cpp:1129, 1243)
-		if (!prm_.fixed_dt && !S_.P.brownian_on) phys_adapt_dt(S_, time_end, strain_end, st_);
-		phys_boxing(S_, st_);
-		phys_move(S_, 1, st_);
-		stage_end(5);
-		stage_begin(0);
-		phys_pairs_update(S_, 0, 1, false, st_);
-		stage_end(0);
-		phys_save_pred(S_, st_);
+		pc_move_predictor(calc_stress, time_end, strain_end, true);
 		// corrector (System.cpp:931-983, 1164-1187)
 		compute_velocities(calc_stress, 0);
-		if (calc_stress) { stage_begin(4); phys_stresslets(S_, 0, st_); stage_end(4); }
-		stage_begin(5);
-		phys_move(S_, 2, st_);
-		stage_end(5);
+		pc_move_corrector(calc_stress, true);
 	}
 	// checkNewInteraction: the superset must hold every pair within range
 	stage_begin(0);
-	LFG_CUDA(cudaMemsetAsync(&S_.clock->stale, 0, sizeof(int), st_));
-	phys_cells(S_, 0, st_);
-	phys_check_superset(S_, st_);
+	superset_check_launch();
 	stage_end(0);
 	pull_clock();
-	if (h_clock_->stale) rebuild_superset();
+	if (h_clock_->stale) {
+		auto t0 = std::chrono::steady_clock::now();
+		rebuild_superset();
+		LFG_CUDA(cudaStreamSynchronize(st_));
+		rebuild_ms_ += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now()-t0).count();
+		rebuilds_++;
+	}
 	stage_begin(0);
 	phys_pairs_update(S_, 1, 0, false, st_);
 	stage_end(0);
@@ -858,7 +953,360 @@ void Sim::timing(lfg_sim_timing *o) const
 	o->launches = last_launches_;
 	o->factor_flops = solver_->flops();
 	o->solve_bytes = 2.0*(double)solver_->nnz_L()*(opt_.precision == LFG_PREC_FP64 ? 8 : 4);
+	o->rebuild_ms = rebuild_ms_+(solver_->capture_ms()-capture_mark_);
+	o->rebuilds = rebuilds_;
 }
+
+
+// ---------------------------------------------------------------------------
+// Fused batch: independent suspensions advanced in lockstep through one joint
+// solver.  The joint system is the block-diagonal matrix of all of them
+// (symbolic_concat): every factorisation and solve launch serves every
+// suspension, level by level of the merged assembly forest.  Each half step
+// runs as CUDA graphs captured once per joint analysis: the suspensions'
+// own kernels on parallel branches (one stream each), joined before the
+// joint factorisation and solve.  The host synchronises three times per step:
+// after each of the two solves (the FP32 refinement's convergence test, per
+// suspension) and after the corrector (the pair supersets' staleness).
+// Predictor-corrector steps only, no Brownian force; all suspensions share
+// the precision and the number of unknowns per particle.
+// ---------------------------------------------------------------------------
+class FusedGroup {
+public:
+	FusedGroup(int device, int precision) : device_(device), prec_(precision)
+	{
+		LFG_CUDA(cudaSetDevice(device));
+		LFG_CUDA(cudaStreamCreateWithFlags(&main_, cudaStreamNonBlocking));
+		LFG_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
+		LFG_CUDA(cudaMallocHost((void **)&h_status_, sizeof(int)));
+	}
+	~FusedGroup()
+	{
+		clear_graphs();
+		delete joint_;
+		for (cudaEvent_t e : join_) cudaEventDestroy(e);
+		if (fork_) cudaEventDestroy(fork_);
+		if (d_rhs_) cudaFree(d_rhs_);
+		if (d_sol_) cudaFree(d_sol_);
+		if (h_status_) cudaFreeHost(h_status_);
+		if (main_) cudaStreamDestroy(main_);
+	}
+	void add(Sim *s)
+	{
+		const lfg_params &p = s->params();
+		if (p.integration_method != 1) throw Error{LFG_ERR_BAD_ARG, 0, "a fused batch needs the predictor-corrector method"};
+		if (p.brownian > 0) throw Error{LFG_ERR_BAD_ARG, 0, "a fused batch takes no Brownian forces"};
+		if (!sims_.empty() && s->solver()->dof() != sims_[0]->solver()->dof())
+			throw Error{LFG_ERR_BAD_ARG, 0, "a fused batch needs one kind of system (all 3D or all 2D)"};
+		sims_.push_back(s);
+		cudaEvent_t e;
+		LFG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+		join_.push_back(e);
+		dirty_ = true;
+	}
+	int size() const { return (int)sims_.size(); }
+	// nsteps lockstep steps of every suspension (no stress output)
+	void run(int nsteps)
+	{
+		std::vector<double> te(sims_.size(), -1.0), se(sims_.size(), 1e300);
+		std::vector<char> act(sims_.size(), 1);
+		for (int k = 0; k < nsteps; k++) step(0, te, se, act);
+	}
+	// System::timeEvolution of every suspension to its own strain: lockstep
+	// steps while any suspension is short of its target (the others wait,
+	// unchanged), then one stress-computing step of all of them
+	void advance(const double *strain_end)
+	{
+		std::vector<double> te(sims_.size(), -1.0), se(strain_end, strain_end+sims_.size());
+		for (;;) {
+			std::vector<char> act(sims_.size(), 0);
+			bool any = false;
+			for (size_t i = 0; i < sims_.size(); i++) {
+				sims_[i]->pull_clock_public();
+				act[i] = sims_[i]->host_clock()->strain <= se[i]-1e-8;
+				any = any || act[i];
+			}
+			if (!any) break;
+			step(0, te, se, act);
+		}
+		std::vector<char> all(sims_.size(), 1);
+		step(1, te, se, all);
+	}
+	int64_t kernels() const { return kernels_; }
+	int symbolic_joint_runs() const { return joint_runs_; }
+	double factor_flops() const { return joint_ ? joint_->flops() : 0; }
+	int last_refine_iters() const { return last_iters_; }
+	// nested-dissection leaf size of every suspension (the autotuner's knob)
+	void set_leaf_size(int leaf)
+	{
+		for (Sim *s : sims_) s->set_leaf_size(leaf);
+		dirty_ = true;
+	}
+
+private:
+	void clear_graphs()
+	{
+		for (auto &g : graphs_) if (g.second) cudaGraphExecDestroy(g.second);
+		graphs_.clear();
+	}
+	// the joint analysis: after additions and pattern changes
+	void build_joint()
+	{
+		std::vector<const Symbolic *> parts;
+		std::vector<int32_t> row, col;
+		pbase_.assign(sims_.size()+1, 0);
+		obase_.assign(sims_.size()+1, 0);
+		for (size_t i = 0; i < sims_.size(); i++) {
+			const Solver *v = sims_[i]->solver();
+			parts.push_back(&v->symbolic());
+			for (size_t e = 0; e < v->pattern_rows().size(); e++) {
+				row.push_back(pbase_[i]+v->pattern_rows()[e]);
+				col.push_back(pbase_[i]+v->pattern_cols()[e]);
+			}
+			pbase_[i+1] = pbase_[i]+v->n();
+			obase_[i+1] = obase_[i]+(int)v->pattern_rows().size();
+		}
+		Symbolic J;
+		symbolic_concat(J, parts);
+		int ntot = pbase_.back();
+		if (!joint_ || joint_->n() != ntot) {
+			delete joint_;
+			joint_ = nullptr;
+			lfg_options o;
+			lfg_default_options(&o);
+			o.precision = prec_;
+			o.device = device_;
+			o.use_graphs = 0;   // the group captures the joint launches in its own graphs
+			joint_ = new Solver(ntot, o, main_, sims_[0]->solver()->dof());
+			if (d_rhs_) cudaFree(d_rhs_);
+			if (d_sol_) cudaFree(d_sol_);
+			d_rhs_ = d_sol_ = nullptr;
+			// right-hand sides every suspension does not use stay zero
+			LFG_CUDA(cudaMalloc((void **)&d_rhs_, sizeof(double)*6*(size_t)ntot*NPFC));
+			LFG_CUDA(cudaMalloc((void **)&d_sol_, sizeof(double)*6*(size_t)ntot*NPFC));
+			LFG_CUDA(cudaMemsetAsync(d_rhs_, 0, sizeof(double)*6*(size_t)ntot*NPFC, main_));
+			LFG_CUDA(cudaMemsetAsync(d_sol_, 0, sizeof(double)*6*(size_t)ntot*NPFC, main_));
+		}
+		joint_->install(std::move(J), (int)row.size(), row.data(), col.data());
+		joint_->set_segments(pbase_);
+		joint_->reserve_refine(NPFC);   // no allocation inside the captured segments
+		clear_graphs();
+		joint_runs_++;
+		dirty_ = false;
+	}
+	void fork()
+	{
+		LFG_CUDA(cudaEventRecord(fork_, main_));
+		for (Sim *s : sims_) LFG_CUDA(cudaStreamWaitEvent(s->stream(), fork_, 0));
+	}
+	void join()
+	{
+		for (size_t i = 0; i < sims_.size(); i++) {
+			LFG_CUDA(cudaEventRecord(join_[i], sims_[i]->stream()));
+			LFG_CUDA(cudaStreamWaitEvent(main_, join_[i], 0));
+		}
+	}
+	// the suspensions' right-hand sides into the joint one (6 n_i values of
+	// each of their k_i right-hand sides at offset 6 pbase_i), and back
+	void gather(size_t i, int k, const double *rhs)
+	{
+		int n6 = 6*sims_[i]->solver()->n(), N6 = 6*pbase_.back();
+		LFG_CUDA(cudaMemcpy2DAsync(d_rhs_+6*(size_t)pbase_[i], sizeof(double)*N6, rhs, sizeof(double)*n6,
+		                           sizeof(double)*n6, k, cudaMemcpyDeviceToDevice, sims_[i]->stream()));
+	}
+	void scatter(size_t i, int k, double *sol)
+	{
+		int n6 = 6*sims_[i]->solver()->n(), N6 = 6*pbase_.back();
+		LFG_CUDA(cudaMemcpy2DAsync(sol, sizeof(double)*n6, d_sol_+6*(size_t)pbase_[i], sizeof(double)*N6,
+		                           sizeof(double)*n6, k, cudaMemcpyDeviceToDevice, sims_[i]->stream()));
+	}
+	// launches of one graph segment: captured on first use, then replayed
+	void segment(int key, const std::function<void()> &body)
+	{
+		auto it = graphs_.find(key);
+		if (it == graphs_.end()) {
+			cudaGraph_t g;
+			LFG_CUDA(cudaStreamBeginCapture(main_, cudaStreamCaptureModeThreadLocal));
+			try {
+				body();
+			} catch (...) {
+				cudaStreamEndCapture(main_, &g);
+				throw;
+			}
+			LFG_CUDA(cudaStreamEndCapture(main_, &g));
+			size_t nn = 0;
+			LFG_CUDA(cudaGraphGetNodes(g, nullptr, &nn));
+			std::vector<cudaGraphNode_t> nodes(nn);
+			if (nn) LFG_CUDA(cudaGraphGetNodes(g, nodes.data(), &nn));
+			int64_t kn = 0;
+			for (size_t q = 0; q < nn; q++) {
+				cudaGraphNodeType t;
+				LFG_CUDA(cudaGraphNodeGetType(nodes[q], &t));
+				if (t == cudaGraphNodeTypeKernel) kn++;
+			}
+			cudaGraphExec_t ex;
+			LFG_CUDA(cudaGraphInstantiate(&ex, g, 0));
+			cudaGraphDestroy(g);
+			it = graphs_.emplace(key, ex).first;
+			graph_kernels_[key] = kn;
+		}
+		LFG_CUDA(cudaGraphLaunch(it->second, main_));
+		kernels_ += graph_kernels_[key];
+	}
+	// one half step's solve: launched in a graph segment (refinement
+	// iterations as many as the last solve needed), completed here
+	void solve_finish(int k)
+	{
+		if (prec_ == LFG_PREC_FP64) return;
+		int it = iters_planned_;
+		double worst = joint_->refine_worst(k);
+		lfg_options o;
+		lfg_default_options(&o);
+		while (!(worst <= o.refine_tol) && it < o.refine_max_iter) {
+			joint_->refine_iterations(k, d_rhs_, 1);
+			kernels_ += joint_->launches_solve()+3;   // sweeps, x += d, residual, norms
+			it++;
+			worst = joint_->refine_worst(k);
+		}
+		lfg_status st;
+		std::memset(&st, 0, sizeof st);
+		int rc = joint_->refine_finish(k, d_sol_, it, worst, &st);
+		last_iters_ = it;
+		joint_->set_pred_iters(it);
+		if (rc) throw Error{rc, it, st.msg};
+	}
+	void solve_launch(int k)
+	{
+		if (prec_ == LFG_PREC_FP64) {
+			joint_->solve_device(k, d_rhs_, d_sol_, nullptr, false);
+			return;
+		}
+		joint_->refine_begin(k, d_rhs_);
+		joint_->refine_iterations(k, d_rhs_, iters_planned_);
+	}
+	void step(int calc_stress, const std::vector<double> &te, const std::vector<double> &se,
+	          const std::vector<char> &act)
+	{
+		cudaSetDevice(device_);
+		if (dirty_) build_joint();
+		std::vector<double> key_args(te);
+		key_args.insert(key_args.end(), se.begin(), se.end());
+		for (char a : act) key_args.push_back(a);
+		if (key_args != graph_args_) { clear_graphs(); graph_args_ = key_args; }
+		const size_t m = sims_.size();
+		std::vector<int> k(m, 1);
+		std::vector<double *> rhs(m, nullptr), sol(m, nullptr);
+		const int kmax = kmax_of(calc_stress, act);
+		double *dbl = joint_->d_dblocks(), *odbl = joint_->d_odblocks();
+		if (prec_ != LFG_PREC_FP64) iters_planned_ = std::max(1, joint_->pred_iters());
+		const int ip = iters_planned_;
+		auto forces = [&](int in_pred) {
+			fork();
+			for (size_t i = 0; i < m; i++) {
+				if (!act[i]) continue;
+				k[i] = sims_[i]->pc_forces_rhs(calc_stress, in_pred, &rhs[i], &sol[i]);
+				gather(i, k[i], rhs[i]);
+			}
+			join();
+		};
+		// predictor: time step, blocks, joint factorisation, forces, solve
+		segment(key(0, calc_stress, ip), [&]() {
+			fork();
+			for (size_t i = 0; i < m; i++) {
+				if (!act[i]) continue;
+				Sim *s = sims_[i];
+				if (!s->params().fixed_dt) phys_adapt_dt(s->dev(), te[i], se[i], s->stream());
+				s->pc_pre_solve(dbl+15*(size_t)pbase_[i], odbl+18*(size_t)obase_[i]);
+			}
+			join();
+			joint_->factorize_async();
+			forces(1);
+			solve_launch(kmax);
+		});
+		solve_finish(kmax);
+		// predictor's velocities and move, corrector's blocks, factorisation, solve
+		segment(key(1, calc_stress, ip), [&]() {
+			fork();
+			for (size_t i = 0; i < m; i++) {
+				if (!act[i]) continue;
+				Sim *s = sims_[i];
+				double *r = nullptr, *x = nullptr;
+				int ki = s->rhs_count(calc_stress, &r, &x);
+				scatter(i, ki, x);
+				s->pc_post_solve(calc_stress, 1);
+				s->pc_move_predictor(calc_stress, te[i], se[i], false);
+				s->pc_pre_solve(dbl+15*(size_t)pbase_[i], odbl+18*(size_t)obase_[i]);
+			}
+			join();
+			joint_->factorize_async();
+			forces(0);
+			solve_launch(kmax);
+		});
+		solve_finish(kmax);
+		// corrector's velocities and move, the supersets' check, clocks to the host
+		segment(key(2, calc_stress, ip), [&]() {
+			fork();
+			for (size_t i = 0; i < m; i++) {
+				if (!act[i]) continue;
+				Sim *s = sims_[i];
+				double *r = nullptr, *x = nullptr;
+				int ki = s->rhs_count(calc_stress, &r, &x);
+				scatter(i, ki, x);
+				s->pc_post_solve(calc_stress, 0);
+				s->pc_move_corrector(calc_stress, false);
+				s->superset_check_launch();
+				s->queue_clock_copy();
+			}
+			join();
+			LFG_CUDA(cudaMemcpyAsync(h_status_, joint_->d_status(), sizeof(int), cudaMemcpyDeviceToHost, main_));
+		});
+		LFG_CUDA(cudaStreamSynchronize(main_));
+		if (*h_status_ == 0) throw Error{LFG_ERR_TIMEOUT, 0, "a bounded device wait in the joint factorisation gave up"};
+		if (*h_status_ != 0x7fffffff) throw Error{LFG_ERR_NOT_SPD, *h_status_, "non-positive pivot in the joint factorisation"};
+		bool changed = false;
+		for (size_t i = 0; i < m; i++) {
+			if (!act[i] || !sims_[i]->host_clock()->stale) continue;
+			sims_[i]->rebuild_superset();
+			changed = true;
+		}
+		if (changed) { build_joint(); graph_args_.clear(); }
+		segment(key(3, calc_stress, ip), [&]() {
+			fork();
+			for (size_t i = 0; i < m; i++)
+				if (act[i]) phys_pairs_update(sims_[i]->dev(), 1, 0, false, sims_[i]->stream());
+			join();
+		});
+		LFG_CUDA(cudaStreamSynchronize(main_));
+	}
+	int kmax_of(int calc_stress, const std::vector<char> &act)
+	{
+		int km = 1;
+		for (size_t i = 0; i < sims_.size(); i++) {
+			if (!act[i]) continue;
+			double *r, *x;
+			km = std::max(km, sims_[i]->rhs_count(calc_stress, &r, &x));
+		}
+		return km;
+	}
+	static int key(int seg, int calc_stress, int iters) { return (iters*2+calc_stress)*4+seg; }
+
+	int device_, prec_;
+	cudaStream_t main_ = nullptr;
+	cudaEvent_t fork_ = nullptr;
+	std::vector<cudaEvent_t> join_;
+	std::vector<Sim *> sims_;
+	std::vector<int> pbase_, obase_;
+	Solver *joint_ = nullptr;
+	double *d_rhs_ = nullptr, *d_sol_ = nullptr;
+	int *h_status_ = nullptr;
+	std::map<int, cudaGraphExec_t> graphs_;
+	std::map<int, int64_t> graph_kernels_;
+	std::vector<double> graph_args_;
+	bool dirty_ = true;
+	int iters_planned_ = 2, last_iters_ = 0;
+	int joint_runs_ = 0;
+	int64_t kernels_ = 0;
+};
 
 } // namespace lfg
 
@@ -898,9 +1346,22 @@ int sim_output_snapshot(lfg_sim *h, OutputSnapshot &o)
 
 extern "C" {
 
+static int sim_new(const lfg_params *p, const lfg_options *opt, int n, const double *pos, const double *radius,
+                   double lx, double ly, double lz, const double *le_disp, int ncs, const int32_t *cs_p0,
+                   const int32_t *cs_p1, const double *cs_disp_tan, lfg_sim **out, lfg_status *st, bool fused);
+
 int lfg_sim_create(const lfg_params *p, const lfg_options *opt, int n, const double *pos, const double *radius,
                    double lx, double ly, double lz, const double *le_disp, int ncs, const int32_t *cs_p0,
                    const int32_t *cs_p1, const double *cs_disp_tan, lfg_sim **out, lfg_status *st)
+{
+	return sim_new(p, opt, n, pos, radius, lx, ly, lz, le_disp, ncs, cs_p0, cs_p1, cs_disp_tan, out, st, false);
+}
+
+} // extern "C"
+
+static int sim_new(const lfg_params *p, const lfg_options *opt, int n, const double *pos, const double *radius,
+                   double lx, double ly, double lz, const double *le_disp, int ncs, const int32_t *cs_p0,
+                   const int32_t *cs_p1, const double *cs_disp_tan, lfg_sim **out, lfg_status *st, bool fused)
 {
 	if (!p || !out || n <= 1 || !pos || !radius || lx <= 0 || lz <= 0 || ly < 0 || ncs < 0 ||
 	    (ncs > 0 && (!cs_p0 || !cs_p1 || !cs_disp_tan)))
@@ -917,7 +1378,7 @@ int lfg_sim_create(const lfg_params *p, const lfg_options *opt, int n, const dou
 	h->device = o.device;
 	try {
 		LFG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
-		h->s = new Sim(*p, o, n, pos, radius, lx, ly, lz, le_disp, h->stream);
+		h->s = new Sim(*p, o, n, pos, radius, lx, ly, lz, le_disp, h->stream, fused);
 		if (ncs) h->s->set_contacts(ncs, cs_p0, cs_p1, cs_disp_tan);   // System::setContacts
 		h->s->first_time();
 		*out = h;
@@ -934,6 +1395,38 @@ int lfg_sim_create(const lfg_params *p, const lfg_options *opt, int n, const dou
 		return fail(st, LFG_ERR_OOM, 0, "allocation failed");
 	}
 }
+
+namespace lfg {
+FusedGroup *fused_create(int device, int precision) { return new FusedGroup(device, precision); }
+void fused_destroy(FusedGroup *g) { delete g; }
+int fused_add(FusedGroup *g, const lfg_params *p, const lfg_options *opt, int n, const double *pos,
+              const double *radius, double lx, double ly, double lz, const double *le_disp, lfg_sim **out,
+              lfg_status *st)
+{
+	int rc = sim_new(p, opt, n, pos, radius, lx, ly, lz, le_disp, 0, nullptr, nullptr, nullptr, out, st, true);
+	if (rc) return rc;
+	try {
+		g->add((*out)->s);
+	} catch (const Error &e) {
+		lfg_sim_destroy(*out);
+		*out = nullptr;
+		return fail(st, e.code, e.info, e.msg.c_str());
+	}
+	return ok(st);
+}
+void fused_run(FusedGroup *g, int nsteps) { g->run(nsteps); }
+void fused_advance(FusedGroup *g, const double *strain_end) { g->advance(strain_end); }
+void fused_set_leaf_size(FusedGroup *g, int leaf) { g->set_leaf_size(leaf); }
+void fused_stats(const FusedGroup *g, int64_t *kernels, int *joint_runs, double *flops, int *iters)
+{
+	*kernels = g->kernels();
+	*joint_runs = g->symbolic_joint_runs();
+	*flops = g->factor_flops();
+	*iters = g->last_refine_iters();
+}
+} // namespace lfg
+
+extern "C" {
 
 int lfg_sim_advance(lfg_sim *h, double time_end, double strain_end, lfg_status *st)
 {
@@ -1162,8 +1655,7 @@ int lfg_sim_get_step_times(lfg_sim *h, double *ms, int cap, int64_t *kernels)
 void lfg_sim_clear_step_times(lfg_sim *h)
 {
 	if (!h) return;
-	h->s->step_ms.clear();
-	h->s->step_kernels = 0;
+	h->s->clear_timing();
 }
 
 void lfg_sim_destroy(lfg_sim *h)

@@ -4,6 +4,7 @@
 // multifrontal factorisation in FP64 or FP32, solves with k right-hand sides,
 // FP64 iterative refinement for the FP32 form.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 
@@ -12,7 +13,8 @@
 namespace lfg {
 int fail(lfg_status *st, int code, int info, const char *msg);
 
-Solver::Solver(int n, const lfg_options &o, cudaStream_t st, int dof) : n_(n), dof_(dof), opt_(o), st_(st)
+Solver::Solver(int n, const lfg_options &o, cudaStream_t st, int dof, bool analysis_only)
+    : n_(n), dof_(dof), analysis_only_(analysis_only), opt_(o), st_(st)
 {
 	if (dof != 6 && dof != 3) throw Error{LFG_ERR_BAD_ARG, dof, "degrees of freedom per particle must be 6 or 3"};
 	A_.n = n;
@@ -31,7 +33,7 @@ Solver::~Solver()
 	factor_free(F64_);
 	factor_free(F32_);
 	void *p[] = {A_.dblocks, A_.odblocks, A_.od_row, A_.od_col, A_.lo_ptr, A_.lo_idx, A_.up_ptr, A_.up_idx,
-	             d_norms_, ref_x_, ref_r_, ref_d_, hb_, hx_};
+	             d_norms_, ref_x_, ref_r_, ref_d_, hb_, hx_, d_seg_};
 	for (void *q : p) if (q) cudaFree(q);
 	if (h_norms_) cudaFreeHost(h_norms_);
 	if (h_status_) cudaFreeHost(h_status_);
@@ -61,6 +63,31 @@ void Solver::set_pattern(int nb, const int32_t *row, const int32_t *col, const d
 	pat_pos_.assign(pos ? pos : nullptr, pos ? pos+3*(size_t)n_ : nullptr);
 	pat_box_[0] = lx; pat_box_[1] = ly; pat_box_[2] = lz;
 	symbolic_analyze(S_, n_, nb, r.data(), c.data(), pos, lx, ly, lz, opt_.leaf_size, dof_);
+	if (analysis_only_) {
+		analyzed_ = true;
+		symbolic_runs_++;
+		return;
+	}
+	upload(r, c);
+}
+
+// A symbolic analysis made elsewhere (a joint analysis of several
+// suspensions) for the pattern (row, col): upload and allocate as set_pattern.
+void Solver::install(Symbolic &&S, int nb, const int32_t *row, const int32_t *col)
+{
+	if (S.nblk != n_ || S.dof != dof_) throw Error{LFG_ERR_BAD_ARG, S.nblk, "symbolic analysis of another system"};
+	std::vector<int32_t> r(row, row+nb), c(col, col+nb);
+	nb_ = nb;
+	pat_r_ = r;
+	pat_c_ = c;
+	pat_pos_.clear();
+	S_ = std::move(S);
+	upload(r, c);
+}
+
+void Solver::upload(const std::vector<int32_t> &r, const std::vector<int32_t> &c)
+{
+	const int nb = nb_;
 	dev_symbolic_upload(D_, S_, nb, factor_panel_width(opt_.precision), factor_tile_size(opt_.precision),
 	                    factor_syrk_tile_size(opt_.precision), opt_.precision == LFG_PREC_FP32_REFINE, st_);
 	if (opt_.precision == LFG_PREC_FP64) factor_alloc(F64_, D_, 4);
@@ -144,6 +171,7 @@ void Solver::run_graph(int kind, int k, const void *b, const void *x, const std:
 			return;
 		}
 	}
+	auto t0 = std::chrono::steady_clock::now();
 	cudaGraph_t graph;
 	LFG_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
 	try {
@@ -168,6 +196,7 @@ void Solver::run_graph(int kind, int k, const void *b, const void *x, const std:
 	LFG_CUDA(cudaGraphInstantiate(&e.exec, graph, 0));
 	cudaGraphDestroy(graph);
 	graphs_.push_back(e);
+	capture_ms_ += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now()-t0).count();
 	LFG_CUDA(cudaGraphLaunch(e.exec, st_));
 	kernels_ += e.nodes;
 }
@@ -218,42 +247,64 @@ int Solver::solve_device(int k, const double *b, double *x, lfg_status *st, bool
 		last_resid_ = 0;
 		return LFG_OK;
 	}
-	ensure_refine_ws(k);
-	int64_t tot = (int64_t)6*n_*k;
-	LFG_CUDA(cudaMemsetAsync(ref_x_, 0, sizeof(double)*tot, st_));
-	LFG_CUDA(cudaMemcpyAsync(ref_r_, b, sizeof(double)*tot, cudaMemcpyDeviceToDevice, st_));
-	// One refinement iteration: d = (LL^T)^-1 r in FP32, x += d, r = b - A x in
-	// FP64.  The first launch runs as many iterations as the previous solve
-	// needed (captured together, one host check at the end), then one at a
-	// time until the tolerance is met.
-	auto iteration = [&]() {
-		launches_solve_ = factor_solve(F32_, D_, k, ref_r_, ref_d_, st_);
-		axpy_vec(n_, k, ref_d_, ref_x_, st_);
-		block_residual(A_, k, b, ref_x_, ref_r_, st_);
-	};
+	refine_begin(k, b);
 	int it = 0;
 	double worst = 0;
 	int batch = std::max(1, std::min(pred_iters_, opt_.refine_max_iter));
 	while (it < opt_.refine_max_iter) {
 		int j = std::min(batch, opt_.refine_max_iter-it);
-		run_graph(2, k*64+j, b, nullptr, [&]() {
-			for (int q = 0; q < j; q++) iteration();
-			residual_norms(6*n_, k, ref_r_, b, d_norms_, st_);
-		});
+		run_graph(2, k*64+j, b, nullptr, [&]() { refine_iterations(k, b, j); });
 		it += j;
-		LFG_CUDA(cudaMemcpyAsync(h_norms_, d_norms_, sizeof(double)*2*k, cudaMemcpyDeviceToHost, st_));
-		LFG_CUDA(cudaStreamSynchronize(st_));
-		worst = 0;
-		for (int r = 0; r < k; r++) {
-			double rb = h_norms_[2*r+1] > 0 ? std::sqrt(h_norms_[2*r]/h_norms_[2*r+1]) : std::sqrt(h_norms_[2*r]);
-			if (!(rb == rb)) rb = INFINITY;
-			worst = std::max(worst, rb);
-		}
+		worst = refine_worst(k);
 		if (worst <= opt_.refine_tol) break;
 		batch = 1;
 	}
 	pred_iters_ = it;
-	last_iters_ = it;
+	return refine_finish(k, x, it, worst, st);
+}
+
+// FP32 refinement in pieces.  refine_begin: x = 0, r = b.  refine_iterations:
+// j times { d = (L L^T)_32^-1 r in FP32; x += d; r = b - A x in FP64 }, then
+// the squared norms of r and b per right-hand side (and per segment); these
+// only launch work, so a caller may capture them in its own graph.
+// refine_worst: waits and returns the largest relative residual.
+// refine_finish: copies x out and records the counts.
+void Solver::refine_begin(int k, const double *b)
+{
+	ensure_refine_ws(k);
+	int64_t tot = (int64_t)6*n_*k;
+	LFG_CUDA(cudaMemsetAsync(ref_x_, 0, sizeof(double)*tot, st_));
+	LFG_CUDA(cudaMemcpyAsync(ref_r_, b, sizeof(double)*tot, cudaMemcpyDeviceToDevice, st_));
+}
+
+void Solver::refine_iterations(int k, const double *b, int j)
+{
+	for (int q = 0; q < j; q++) {
+		launches_solve_ = factor_solve(F32_, D_, k, ref_r_, ref_d_, st_);
+		axpy_vec(n_, k, ref_d_, ref_x_, st_);
+		block_residual(A_, k, b, ref_x_, ref_r_, st_);
+	}
+	residual_norms(6*n_, k, ref_r_, b, d_norms_, st_, seg_.empty() ? nullptr : d_seg_, (int)seg_.size()-1);
+}
+
+double Solver::refine_worst(int k)
+{
+	int nseg = seg_.empty() ? 1 : (int)seg_.size()-1;
+	LFG_CUDA(cudaMemcpyAsync(h_norms_, d_norms_, sizeof(double)*2*k*nseg, cudaMemcpyDeviceToHost, st_));
+	LFG_CUDA(cudaStreamSynchronize(st_));
+	double worst = 0;
+	for (int r = 0; r < k*nseg; r++) {
+		double rb = h_norms_[2*r+1] > 0 ? std::sqrt(h_norms_[2*r]/h_norms_[2*r+1]) : std::sqrt(h_norms_[2*r]);
+		if (!(rb == rb)) rb = INFINITY;
+		worst = std::max(worst, rb);
+	}
+	return worst;
+}
+
+int Solver::refine_finish(int k, double *x, int iters, double worst, lfg_status *st)
+{
+	int64_t tot = (int64_t)6*n_*k;
+	last_iters_ = iters;
 	last_resid_ = worst;
 	LFG_CUDA(cudaMemcpyAsync(x, ref_x_, sizeof(double)*tot, cudaMemcpyDeviceToDevice, st_));
 	if (st) { st->refine_iters = last_iters_; st->refine_residual = worst; }
@@ -264,8 +315,30 @@ int Solver::solve_device(int k, const double *b, double *x, lfg_status *st, bool
 		}
 		return LFG_ERR_NOT_CONVERGED;
 	}
-	(void)sync_check;
 	return LFG_OK;
+}
+
+// Per-suspension segments of a joint system (particle offsets, nseg + 1):
+// the refinement's convergence test takes the largest relative residual over
+// the segments, so every suspension meets the tolerance on its own.
+void Solver::set_segments(const std::vector<int> &particle_off)
+{
+	seg_.resize(particle_off.size());
+	for (size_t q = 0; q < particle_off.size(); q++) seg_[q] = 6*particle_off[q];
+	if (d_seg_) cudaFree(d_seg_);
+	d_seg_ = nullptr;
+	LFG_CUDA(cudaMalloc((void **)&d_seg_, sizeof(int)*std::max<size_t>(seg_.size(), 1)));
+	LFG_CUDA(cudaMemcpyAsync(d_seg_, seg_.data(), sizeof(int)*seg_.size(), cudaMemcpyHostToDevice, st_));
+	size_t need = 2*8*std::max<size_t>(seg_.size(), 2);
+	if (need > norms_cap_) {
+		cudaFreeHost(h_norms_);
+		cudaFree(d_norms_);
+		h_norms_ = nullptr; d_norms_ = nullptr;
+		LFG_CUDA(cudaMallocHost((void **)&h_norms_, sizeof(double)*need));
+		LFG_CUDA(cudaMalloc((void **)&d_norms_, sizeof(double)*need));
+		norms_cap_ = need;
+	}
+	LFG_CUDA(cudaStreamSynchronize(st_));
 }
 
 // StokesSolver::compute_LTRHS (StokesSolver.cpp:627-669): the Brownian

@@ -578,6 +578,97 @@ void symbolic_analyze(Symbolic &S, int n, int nb, const int32_t *od_row, const i
 	}
 }
 
+// Joint analysis of independent systems: the block-diagonal matrix of all of
+// them, whose assembly forest is the union of their trees.  Each part's
+// particles, supernodes, rows, fronts, update vectors and off-diagonal blocks
+// follow the previous parts'; level l of the forest holds every part's level
+// l (levels count from the leaves), so one launch per level and stage serves
+// all parts.
+void symbolic_concat(Symbolic &J, const std::vector<const Symbolic *> &parts)
+{
+	J = Symbolic();
+	if (parts.empty()) throw Error{LFG_ERR_BAD_ARG, 0, "joint analysis of no system"};
+	J.dof = parts[0]->dof;
+	for (const Symbolic *P : parts) {
+		if (P->dof != J.dof) throw Error{LFG_ERR_BAD_ARG, P->dof, "joint analysis of systems with different dof"};
+		J.nlevels = std::max(J.nlevels, P->nlevels);
+	}
+	int B = 0, SB = 0, RB = 0, CHB = 0, OB = 0;
+	int64_t AB = 0, WB = 0, CB = 0;
+	for (const Symbolic *P : parts) {
+		for (int k = 0; k < P->nblk; k++) {
+			J.perm.push_back(B+P->perm[k]);
+			J.iperm.push_back(B+P->iperm[k]);
+		}
+		for (int q = 0; q < P->nsn; q++) {
+			J.sn_first.push_back(B+P->sn_first[q]);
+			J.sn_n.push_back(P->sn_n[q]);
+			J.sn_m.push_back(P->sn_m[q]);
+			J.sn_parent.push_back(P->sn_parent[q] >= 0 ? SB+P->sn_parent[q] : -1);
+			J.sn_level.push_back(P->sn_level[q]);
+			J.sn_rows_off.push_back(RB+P->sn_rows_off[q]);
+			J.sn_off.push_back(AB+P->sn_off[q]);
+			J.sn_ld.push_back(P->sn_ld[q]);
+			J.sn_woff.push_back(WB+P->sn_woff[q]);
+			J.child_off.push_back(CHB+P->child_off[q]);
+			J.cinv_off.push_back(CB+P->cinv_off[q]);
+		}
+		for (int r : P->rows) J.rows.push_back(B+r);
+		J.cfwd.insert(J.cfwd.end(), P->cfwd.begin(), P->cfwd.end());
+		for (int c : P->children) J.children.push_back(SB+c);
+		J.cinv.insert(J.cinv.end(), P->cinv.begin(), P->cinv.end());
+		for (int i = 0; i < P->nblk; i++) {
+			J.d_sn.push_back(SB+P->d_sn[i]);
+			J.d_bc.push_back(P->d_bc[i]);
+		}
+		for (size_t e = 0; e < P->od_sn.size(); e++) {
+			J.od_sn.push_back(SB+P->od_sn[e]);
+			J.od_br.push_back(P->od_br[e]);
+			J.od_bc.push_back(P->od_bc[e]);
+			J.od_tr.push_back(P->od_tr[e]);
+		}
+		J.max_F = std::max(J.max_F, P->max_F);
+		J.nnz_L += P->nnz_L;
+		J.flops += P->flops;
+		B += P->nblk;
+		SB += P->nsn;
+		RB += (int)P->rows.size();
+		CHB += (int)P->children.size();
+		OB += (int)P->od_sn.size();
+		AB += P->arena_elems;
+		WB += P->w_elems;
+		CB += P->cinv_off[P->nsn];
+	}
+	J.nblk = B;
+	J.nsn = SB;
+	J.sn_rows_off.push_back(RB);
+	J.child_off.push_back(CHB);
+	J.cinv_off.push_back(CB);
+	J.arena_elems = AB;
+	J.w_elems = std::max<int64_t>(WB, 1);
+	// levels: every part's level l, parts in order
+	J.level_off.assign(J.nlevels+1, 0);
+	J.level_d_off.assign(J.nlevels+1, 0);
+	J.level_od_off.assign(J.nlevels+1, 0);
+	for (int l = 0; l < J.nlevels; l++) {
+		int sb = 0, b = 0, ob = 0;
+		for (const Symbolic *P : parts) {
+			if (l < P->nlevels) {
+				for (int t = P->level_off[l]; t < P->level_off[l+1]; t++) J.level_sn.push_back(sb+P->level_sn[t]);
+				for (int t = P->level_d_off[l]; t < P->level_d_off[l+1]; t++) J.level_d.push_back(b+P->level_d[t]);
+				for (int t = P->level_od_off[l]; t < P->level_od_off[l+1]; t++)
+					J.level_od.push_back(ob+P->level_od[t]);
+			}
+			sb += P->nsn;
+			b += P->nblk;
+			ob += (int)P->od_sn.size();
+		}
+		J.level_off[l+1] = (int)J.level_sn.size();
+		J.level_d_off[l+1] = (int)J.level_d.size();
+		J.level_od_off[l+1] = (int)J.level_od.size();
+	}
+}
+
 // ---------------------------------------------------------------------------
 // device mirror + launch plan
 // ---------------------------------------------------------------------------
