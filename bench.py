@@ -171,6 +171,37 @@ def _errors(a, b):
     return out
 
 
+def pattern_changes(E, packing, device, steps):
+    """A longer run of the FP32 + refinement form from the packing, long
+    enough for the pair superset to run out of skin: how often the pattern of
+    R_FU changes (superset rebuild + symbolic analysis, cholmod_analyze's
+    counterpart), what one rebuild costs on the host (including the capture
+    of the new factorisation and solve graphs), and the throughput with those
+    rebuilds folded in: particle-steps / host wall-clock time of the whole
+    run."""
+    params = workload_params()
+    g = E.Sim(params, packing.position, packing.radius, packing.lx, packing.ly, packing.lz,
+              precision=E.PREC_FP32_REFINE, device=device)
+    g.run(3)
+    g.clear_step_times()
+    s0 = g.scalars()["strain"]
+    t0 = time.perf_counter()
+    g.run(steps)
+    wall = time.perf_counter() - t0
+    ms, _ = g.step_times()
+    tim = g.timing()
+    sc = g.scalars()
+    g.close()
+    r = tim["rebuilds"]
+    return {"steps": steps, "strain_covered": float(sc["strain"] - s0), "rebuilds": r,
+            "steps_per_rebuild": steps / r if r else None,
+            "rebuild_host_ms_total": tim["rebuild_ms"], "rebuild_host_ms_mean": tim["rebuild_ms"] / r if r else None,
+            "device_ms_per_step": float(np.mean(ms)), "wall_ms_per_step": 1e3 * wall / steps,
+            "value_amortised": N_PART * steps / wall, "unit": "particle-steps/s",
+            "note": "host wall clock over the whole run, rebuilds (candidate pairs, symbolic analysis, "
+                    "upload, graph capture) included"}
+
+
 def accuracy(E, packing, device, oracle_ref=None):
     """One predictor-corrector step with stresses from the packing, in the
     FP32 + refinement and the FP64 forms: largest relative differences of the
@@ -232,6 +263,7 @@ def cpu_baseline(packing, nsteps=3, one_thread=True):
     import pyoracle
     pyoracle.build()
     cores = pyoracle.num_threads()
+    method = _cpu_factorisation(pyoracle)
     o = pyoracle.OracleSim(workload_params(), packing.position, packing.radius, packing.lx, packing.ly,
                            packing.lz)
     o.first_time()
@@ -246,8 +278,8 @@ def cpu_baseline(packing, nsteps=3, one_thread=True):
     steps_s = [t1 - t0, (t2 - t1) / max(nsteps - 1, 1)]
     rec = {"value": N_PART * nsteps / (t2 - t0), "unit": "particle-steps/s", "cores": cores, "kind": "port",
            "sample": f"{nsteps} predictor-corrector steps of the N={N_PART} workload from the packing, "
-                     f"{t2 - t0:.1f} s, FP64 block Cholesky (minimum degree on 6x6 blocks, right-looking, "
-                     f"OpenMP trailing update); first step with stresses {steps_s[0]:.2f} s",
+                     f"{t2 - t0:.1f} s; first step with stresses {steps_s[0]:.2f} s",
+           "factorisation": method,
            "factor_flops_per_factorisation": fs["factor_flops"],
            "factor_gflops": fs["factor_flops"] * fs["factorisations"] / max(fs["factor_s"], 1e-12) / 1e9,
            "factor_s_per_factorisation": fs["factor_s"] / max(fs["factorisations"], 1),
@@ -274,6 +306,16 @@ def cpu_baseline(packing, nsteps=3, one_thread=True):
 
 ARM_PARTS = {"0xd4f": "Arm Neoverse V2", "0xd40": "Arm Neoverse V1", "0xd0c": "Arm Neoverse N1",
              "0xd49": "Arm Neoverse N2"}
+
+
+def _cpu_factorisation(pyoracle):
+    """The CPU oracle's factorisation for the baseline: supernodal with dense
+    BLAS-3 kernels (CHOLMOD's method) when scipy's BLAS/LAPACK is present."""
+    if pyoracle.use_blas():
+        return ("FP64 supernodal multifrontal Cholesky (minimum-degree ordering on the 6x6 blocks, relaxed "
+                "supernodes), dense kernels dpotrf/dtrsm/dsyrk/dgemm from scipy's OpenBLAS, small fronts in "
+                "parallel with OpenMP")
+    return "FP64 block Cholesky (minimum degree on 6x6 blocks, right-looking, OpenMP trailing update)"
 
 
 def _cpu_model():
@@ -330,6 +372,7 @@ def reference_arm(args):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     pyoracle.build()
+    method = _cpu_factorisation(pyoracle)
     p = PK.generate(N_PART, VF, seed=2000)
     o = pyoracle.OracleSim(workload_params(), p.position, p.radius, p.lx, p.ly, p.lz)
     o.first_time()
@@ -353,6 +396,7 @@ def reference_arm(args):
                              "sample": f"{args.steps} full steps of the N={N_PART} workload on the CPU oracle "
                                        "(C restatement of LF_DEM's step; reference C++ + CHOLMOD cannot be "
                                        "built on this host)",
+                             "factorisation": method,
                              "factor_flops_per_factorisation": fs["factor_flops"],
                              "factor_gflops": fs["factor_flops"] * fs["factorisations"] /
                              max(fs["factor_s"], 1e-12) / 1e9, "cpu": _cpu_model()},
@@ -390,10 +434,12 @@ def stress_params(sigma_cl):
 def bench_sweep(args):
     """Batched rheology sweep: 64 independent 3D suspensions, N ~ U[256, 2048],
     phi ~ U[0.45, 0.58], rate control with shear rates log-spaced 1e-2..1e2
-    (repulsive-force units), bidisperse 1:1.4, FP32 + refinement, advanced
-    together by one lfg_batch; leaf sizes picked by the autotuner.  Aggregate
-    particle-steps/s over K steps of every suspension, against the same batch
-    driven by one host thread (suspensions one after another)."""
+    (repulsive-force units), bidisperse 1:1.4, FP32 + refinement.  Three ways
+    to advance them K steps each, aggregate particle-steps/s over host wall
+    time: fused (one joint factorisation and solve per half step for all of
+    them, each half step a captured CUDA graph; leaf size picked by the
+    autotuner on the fused step), concurrent (each on its own stream, 16 host
+    workers) and one host thread (one after another)."""
     rng = np.random.default_rng(4000)
     m = args.count or 64
     ns = rng.integers(256, 2049, size=m)
@@ -405,31 +451,45 @@ def bench_sweep(args):
     B.build()
     E.load()
     out = {}
-    for label, threads in (("concurrent", 16), ("one_thread", 1)):
-        b = E.Batch(nthreads=threads)
+    for label, threads in (("fused", 0), ("concurrent", 16), ("one_thread", 1)):
+        if label == "fused":
+            b = E.Batch(fused=True, precision=E.PREC_FP32_REFINE)
+        else:
+            b = E.Batch(nthreads=threads)
+        t0 = time.perf_counter()
         for p, r in zip(packs, rates):
             b.add(rate_params(float(r)), p.position, p.radius, p.lx, p.ly, p.lz, precision=E.PREC_FP32_REFINE)
-        if label == "concurrent":
+        create_s = time.perf_counter() - t0
+        rec = {"create_s": create_s}
+        if label != "one_thread":
             t0 = time.perf_counter()
             b.autotune((8, 16, 32), steps=1)
-            out["autotune_s"] = time.perf_counter() - t0
-            out["tuned_leaf"] = {str(n): b.tuned_leaf(n, 1) for n in (256, 512, 1024, 2048)}
+            rec["autotune_s"] = time.perf_counter() - t0
+            rec["tuned_leaf"] = {str(n): b.tuned_leaf(n, 1) for n in (256, 512, 1024, 2048)}
         b.run(args.warmup)
+        k0 = b.stats()["kernels"]
         t0 = time.perf_counter()
         b.run(args.steps)
         wall = time.perf_counter() - t0
-        out[label] = {"particle_steps_per_s": float(ns.sum()) * args.steps / wall, "wall_s": wall,
-                      "host_threads": threads}
+        st = b.stats()
+        rec.update({"particle_steps_per_s": float(ns.sum()) * args.steps / wall, "wall_s": wall,
+                    "host_threads": threads if label != "fused" else 1,
+                    "kernels_per_batch_step": (st["kernels"] - k0) / args.steps})
+        if label == "fused":
+            rec.update({"joint_factor_gflop": st["factor_flops"] / 1e9, "joint_analyses": st["joint_analyses"],
+                        "refine_iters": st["last_refine_iters"]})
+        out[label] = rec
         b.close()
     line = {"metric": "aggregate particle-steps/s, batched sweep", "workload": "sweep",
-            "value": out["concurrent"]["particle_steps_per_s"], "unit": "particle-steps/s",
+            "value": out["fused"]["particle_steps_per_s"], "unit": "particle-steps/s",
             "steps": args.steps, "warmup": args.warmup, "dtype": "f32+f64refine", "data": "synthetic",
             "config": {"suspensions": m, "n_range": [256, 2048], "phi_range": [0.45, 0.58],
                        "shear_rates": "log-spaced 1e-2..1e2 (repulsive-force units)", "control": "rate",
                        "total_particles": int(ns.sum()),
-                       "note": "fixed step count per suspension instead of 2 strain units"},
+                       "note": "fixed step count per suspension instead of 2 strain units; host wall time"},
             **out}
-    line["speedup_vs_one_thread"] = out["concurrent"]["particle_steps_per_s"] / out["one_thread"]["particle_steps_per_s"]
+    line["fused_vs_concurrent"] = out["fused"]["particle_steps_per_s"] / out["concurrent"]["particle_steps_per_s"]
+    line["fused_vs_one_thread"] = out["fused"]["particle_steps_per_s"] / out["one_thread"]["particle_steps_per_s"]
     print(json.dumps(line), flush=True)
 
 
@@ -584,6 +644,8 @@ def main():
                     help="cfg2: the metric's workload (default); cfg3: the 2D monolayer; "
                          "sweep / serve: the batched and serving forms")
     ap.add_argument("--count", type=int, default=0, help="suspensions (sweep) or requests (serve)")
+    ap.add_argument("--long-steps", type=int, default=400,
+                    help="steps of the run that counts pattern changes (0: skip)")
     ap.add_argument("--strain", type=float, default=0.002, help="serve: strain target of each request")
     ap.add_argument("--max-active", type=int, default=8, help="serve: concurrent requests")
     ap.add_argument("--hbm-budget-gb", type=float, default=200.0, help="serve: device bytes for admission")
@@ -688,6 +750,8 @@ def main():
                               "frac": solve_bytes_step / max(solve_ms * 1e-3, 1e-12) / 1e9 / hbm,
                               "note": "factor bytes read by the triangular solves of one step / solve time"}
     line["e2e"] = run_e2e(E, pk, E.PREC_FP32_REFINE, args.steps, local)
+    if args.long_steps > 0:
+        line["pattern_changes"] = pattern_changes(E, pk, local, args.long_steps)
     oracle_ref = None
     if not args.no_cpu:
         line["cpu_baseline"], oracle_ref = cpu_baseline(pk)

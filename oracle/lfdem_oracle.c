@@ -1054,7 +1054,13 @@ static void bfact_free(bfact *f)
 static int popcount64(uint64_t x) { return __builtin_popcountll(x); }
 
 /* symbolic: minimum degree with elimination-graph bitsets */
+static bfact *bfact_analyze_ex(int n, int nb, const int *row, const int *col, int numeric);
 static bfact *bfact_analyze(int n, int nb, const int *row, const int *col)
+{
+	return bfact_analyze_ex(n, nb, row, col, 1);
+}
+
+static bfact *bfact_analyze_ex(int n, int nb, const int *row, const int *col, int numeric)
 {
 	int W = (n+63)/64;
 	uint64_t *adj = calloc((size_t)n*W, sizeof(uint64_t));
@@ -1123,8 +1129,10 @@ static bfact *bfact_analyze(int n, int nb, const int *row, const int *col)
 			f->rowidx[u+1] = x;
 		}
 	}
-	f->Lblk = calloc((size_t)(used > 0 ? used : 1)*36, sizeof(double));
-	f->Ldiag = calloc((size_t)n*36, sizeof(double));
+	if (numeric) {
+		f->Lblk = calloc((size_t)(used > 0 ? used : 1)*36, sizeof(double));
+		f->Ldiag = calloc((size_t)n*36, sizeof(double));
+	}
 	free(adj); free(elim); free(deg); free(rows_orig); free(cstart); free(nb_set); free(done);
 	return f;
 }
@@ -1270,6 +1278,386 @@ static void bfact_solve(const bfact *f, const double *b, double *x, double *w)
 	for (int k = 0; k < n; k++) memcpy(&x[f->perm[k]*6], &w[k*6], 6*sizeof(double));
 }
 
+/* ------------------------------------------------------------------ */
+/* Supernodal multifrontal factorisation with dense BLAS-3 kernels: the   */
+/* method of CHOLMOD's supernodal cholmod_factorize / cholmod_solve2,     */
+/* which LF_DEM calls (StokesSolver.cpp:671-703, 950-978).  Same ordering */
+/* and column structure as the block factorisation above (minimum degree  */
+/* on the 6x6 blocks); consecutive columns whose structures nest form a   */
+/* supernode (a fundamental supernode), factored as a dense front:        */
+/*   front = A's entries + the children's update matrices (extend-add);   */
+/*   L11 = chol(F11) (dpotrf), L21 = F21 L11^-T (dtrsm),                   */
+/*   update = F22 - L21 L21^T (dsyrk), passed to the parent.               */
+/* The dense kernels come from the caller (lfo_set_blas: LAPACK dpotrf,   */
+/* BLAS dtrsm, dsyrk, dgemm, Fortran calling convention, e.g. scipy's     */
+/* OpenBLAS).  Levels of the supernode tree with many fronts run them in  */
+/* parallel (OpenMP, one BLAS thread each); the top levels run one front  */
+/* at a time with every BLAS thread.  Without lfo_set_blas the block      */
+/* factorisation is used.                                                 */
+/* ------------------------------------------------------------------ */
+typedef void (*potrf_fn)(const char *, const int *, double *, const int *, int *);
+typedef void (*trsm_fn)(const char *, const char *, const char *, const char *, const int *, const int *,
+                        const double *, const double *, const int *, double *, const int *);
+typedef void (*syrk_fn)(const char *, const char *, const int *, const int *, const double *, const double *,
+                        const int *, const double *, double *, const int *);
+typedef void (*gemm_fn)(const char *, const char *, const int *, const int *, const int *, const double *,
+                        const double *, const int *, const double *, const int *, const double *, double *,
+                        const int *);
+typedef void (*threads_fn)(int);
+static struct {
+	potrf_fn potrf; trsm_fn trsm; syrk_fn syrk; gemm_fn gemm; threads_fn set_threads;
+	int threads;
+} g_blas;
+
+void lfo_set_blas(void *potrf, void *trsm, void *syrk, void *gemm, void *set_threads, int threads)
+{
+	g_blas.potrf = (potrf_fn)potrf;
+	g_blas.trsm = (trsm_fn)trsm;
+	g_blas.syrk = (syrk_fn)syrk;
+	g_blas.gemm = (gemm_fn)gemm;
+	g_blas.set_threads = (threads_fn)set_threads;
+	g_blas.threads = threads > 0 ? threads : 1;
+}
+
+int lfo_blas_ready(void) { return g_blas.potrf && g_blas.trsm && g_blas.syrk && g_blas.gemm; }
+
+static void blas_threads(int t)
+{
+	if (g_blas.set_threads) g_blas.set_threads(t);
+}
+
+typedef struct {
+	bfact *sym;            /* ordering and block column structures */
+	int nsn;
+	int *first, *width;    /* supernode: first eliminated block column, width in blocks */
+	int *rows_off;         /* below-diagonal block rows of supernode q: sym->rowidx[rows_off[q] ..] */
+	int *nrows;
+	int *parent;           /* supernode parent, -1 at a root */
+	int *child_off, *child;
+	int *level, nlevels, *level_off, *level_sn;
+	double **L;            /* 6F x 6w, column-major, ld 6F (F = w + nrows) */
+	double **U;            /* update matrices (6 nrows)^2, freed by the parent */
+	/* A's off-diagonal blocks by lower eliminated column */
+	int *acol_ptr, *arow, *aidx, *atr;
+} snfact;
+
+static void sn_free(snfact *f)
+{
+	if (!f) return;
+	for (int q = 0; q < f->nsn; q++) { free(f->L ? f->L[q] : NULL); free(f->U ? f->U[q] : NULL); }
+	free(f->L); free(f->U);
+	free(f->first); free(f->width); free(f->rows_off); free(f->nrows); free(f->parent);
+	free(f->child_off); free(f->child); free(f->level); free(f->level_off); free(f->level_sn);
+	free(f->acol_ptr); free(f->arow); free(f->aidx); free(f->atr);
+	bfact_free(f->sym);
+	free(f);
+}
+
+static snfact *sn_analyze(int n, int nb, const int *row, const int *col)
+{
+	bfact *b = bfact_analyze_ex(n, nb, row, col, 0);
+	if (!b) return NULL;
+	snfact *f = calloc(1, sizeof(snfact));
+	f->sym = b;
+	int *sn_of = malloc(sizeof(int)*(n > 0 ? n : 1));
+	f->first = malloc(sizeof(int)*(n+1));
+	f->width = malloc(sizeof(int)*(n+1));
+	int q = -1;
+	for (int k = 0; k < n; k++) {
+		int cnt = b->colptr[k+1]-b->colptr[k];
+		int merge = 0;
+		if (k > 0) {
+			int pc = b->colptr[k]-b->colptr[k-1];
+			/* column k-1's structure is {k} plus column k's: nested */
+			merge = pc == cnt+1 && pc > 0 && b->rowidx[b->colptr[k-1]] == k;
+		}
+		if (!merge) { q++; f->first[q] = k; f->width[q] = 0; }
+		f->width[q]++;
+		sn_of[k] = q;
+	}
+	int nsn = q+1;
+	/* relaxed amalgamation (CHOLMOD's rule, cholmod_super.c defaults nrelax
+	 * 4/16/48, zrelax 0.8/0.1/0.05): a supernode whose parent is the next
+	 * one merges into it when the dense front adds few explicit zeros */
+	{
+		int *par = malloc(sizeof(int)*(nsn > 0 ? nsn : 1));
+		int *nr = malloc(sizeof(int)*(nsn > 0 ? nsn : 1));
+		for (q = 0; q < nsn; q++) {
+			int last = f->first[q]+f->width[q]-1;
+			nr[q] = b->colptr[last+1]-b->colptr[last];
+			par[q] = nr[q] > 0 ? sn_of[b->rowidx[b->colptr[last]]] : -1;
+		}
+		int out = 0;
+		double extra_acc = 0;   /* explicit zeros already merged into the supernode being built */
+		for (q = 0; q < nsn; q++) {
+			int p = q+1;
+			if (p < nsn && par[q] == p) {
+				double wq = f->width[q], wp = f->width[p], mq = nr[q], mp = nr[p];
+				double w = wq+wp;
+				double nnz = w*(w+1)/2+w*mp;
+				double extra = extra_acc+wq*(wp+mp-mq);
+				double z = extra/nnz, cols = 6*w;
+				int merge = cols <= 4*6 || (cols <= 16*6 && z < 0.8) || (cols <= 48*6 && z < 0.1) || z < 0.05;
+				if (merge) {
+					f->first[p] = f->first[q];
+					f->width[p] += f->width[q];
+					extra_acc = extra;
+					continue;
+				}
+			}
+			f->first[out] = f->first[q];
+			f->width[out] = f->width[q];
+			out++;
+			extra_acc = 0;
+		}
+		nsn = out;
+		for (q = 0; q < nsn; q++)
+			for (int k = f->first[q]; k < f->first[q]+f->width[q]; k++) sn_of[k] = q;
+		free(par);
+		free(nr);
+	}
+	f->nsn = nsn;
+	f->rows_off = malloc(sizeof(int)*(nsn+1));
+	f->nrows = malloc(sizeof(int)*(nsn+1));
+	f->parent = malloc(sizeof(int)*(nsn+1));
+	for (q = 0; q < nsn; q++) {
+		int last = f->first[q]+f->width[q]-1;
+		f->rows_off[q] = b->colptr[last];
+		f->nrows[q] = b->colptr[last+1]-b->colptr[last];
+		f->parent[q] = f->nrows[q] > 0 ? sn_of[b->rowidx[b->colptr[last]]] : -1;
+	}
+	f->child_off = calloc(nsn+1, sizeof(int));
+	f->child = malloc(sizeof(int)*(nsn > 0 ? nsn : 1));
+	for (q = 0; q < nsn; q++) if (f->parent[q] >= 0) f->child_off[f->parent[q]+1]++;
+	for (q = 0; q < nsn; q++) f->child_off[q+1] += f->child_off[q];
+	{
+		int *fill = malloc(sizeof(int)*(nsn+1));
+		memcpy(fill, f->child_off, sizeof(int)*(nsn+1));
+		for (q = 0; q < nsn; q++) if (f->parent[q] >= 0) f->child[fill[f->parent[q]]++] = q;
+		free(fill);
+	}
+	/* levels from the leaves (children have lower numbers) */
+	f->level = calloc(nsn+1, sizeof(int));
+	f->nlevels = 0;
+	for (q = 0; q < nsn; q++) {
+		int l = 0;
+		for (int c = f->child_off[q]; c < f->child_off[q+1]; c++)
+			if (f->level[f->child[c]]+1 > l) l = f->level[f->child[c]]+1;
+		f->level[q] = l;
+		if (l+1 > f->nlevels) f->nlevels = l+1;
+	}
+	f->level_off = calloc(f->nlevels+1, sizeof(int));
+	f->level_sn = malloc(sizeof(int)*(nsn > 0 ? nsn : 1));
+	for (q = 0; q < nsn; q++) f->level_off[f->level[q]+1]++;
+	for (int l = 0; l < f->nlevels; l++) f->level_off[l+1] += f->level_off[l];
+	{
+		int *fill = malloc(sizeof(int)*(f->nlevels+1));
+		memcpy(fill, f->level_off, sizeof(int)*(f->nlevels+1));
+		for (q = 0; q < nsn; q++) f->level_sn[fill[f->level[q]]++] = q;
+		free(fill);
+	}
+	/* A's off-diagonal blocks by their lower eliminated column */
+	f->acol_ptr = calloc(n+1, sizeof(int));
+	f->arow = malloc(sizeof(int)*(nb > 0 ? nb : 1));
+	f->aidx = malloc(sizeof(int)*(nb > 0 ? nb : 1));
+	f->atr = malloc(sizeof(int)*(nb > 0 ? nb : 1));
+	for (int e = 0; e < nb; e++) {
+		int pi = b->iperm[row[e]], pj = b->iperm[col[e]];
+		f->acol_ptr[(pi < pj ? pi : pj)+1]++;
+	}
+	for (int k = 0; k < n; k++) f->acol_ptr[k+1] += f->acol_ptr[k];
+	{
+		int *fill = malloc(sizeof(int)*(n+1));
+		memcpy(fill, f->acol_ptr, sizeof(int)*(n+1));
+		for (int e = 0; e < nb; e++) {
+			int pi = b->iperm[row[e]], pj = b->iperm[col[e]];
+			int lo = pi < pj ? pi : pj, hi = pi < pj ? pj : pi;
+			int t = fill[lo]++;
+			f->arow[t] = hi;
+			f->aidx[t] = e;
+			f->atr[t] = pi < pj;   /* the stored block is the transpose of the lower one */
+		}
+		free(fill);
+	}
+	f->L = calloc(nsn, sizeof(double *));
+	f->U = calloc(nsn, sizeof(double *));
+	free(sn_of);
+	return f;
+}
+
+/* one front: assemble, factor, update; fpos is a per-thread block -> front
+ * position map (entries of other fronts are never read) */
+static int sn_front(snfact *f, int q, const double *diag36, const double *off36, int *fpos)
+{
+	bfact *b = f->sym;
+	int w = f->width[q], m = f->nrows[q], F = w+m, k0 = f->first[q];
+	int nf = 6*F, n6 = 6*w, m6 = 6*m;
+	/* large fronts are assembled by all threads (outside the parallel
+	 * levels); every column is touched by one thread only */
+	int par = nf > 600;
+#ifdef _OPENMP
+	if (omp_in_parallel()) par = 0;
+#endif
+	double *A = malloc(sizeof(double)*(size_t)nf*nf);
+	if (!A) return -4;
+#pragma omp parallel for schedule(static) if (par)
+	for (int c = 0; c < nf; c++) memset(&A[(size_t)c*nf], 0, sizeof(double)*nf);
+	for (int j = 0; j < w; j++) fpos[k0+j] = j;
+	for (int t = 0; t < m; t++) fpos[b->rowidx[f->rows_off[q]+t]] = w+t;
+	/* A's blocks of the supernode's columns (lower part) */
+	for (int j = 0; j < w; j++) {
+		int k = k0+j;
+		const double *D = &diag36[(size_t)b->perm[k]*36];
+		for (int c = 0; c < 6; c++)
+			for (int r = c; r < 6; r++) A[(size_t)(6*j+c)*nf+6*j+r] += D[r*6+c];
+		for (int t = f->acol_ptr[k]; t < f->acol_ptr[k+1]; t++) {
+			int fr = fpos[f->arow[t]];
+			const double *B = &off36[(size_t)f->aidx[t]*36];
+			for (int c = 0; c < 6; c++)
+				for (int r = 0; r < 6; r++)
+					A[(size_t)(6*j+c)*nf+6*fr+r] += f->atr[t] ? B[c*6+r] : B[r*6+c];
+		}
+	}
+	/* extend-add of the children's update matrices */
+	for (int cc = f->child_off[q]; cc < f->child_off[q+1]; cc++) {
+		int c = f->child[cc];
+		int mc = f->nrows[c], mc6 = 6*mc;
+		double *Uc = f->U[c];
+		const int *rc = &b->rowidx[f->rows_off[c]];
+#pragma omp parallel for schedule(dynamic, 8) if (par)
+		for (int bj = 0; bj < mc; bj++) {
+			int pj = fpos[rc[bj]];
+			for (int bi = bj; bi < mc; bi++) {
+				int pi = fpos[rc[bi]];
+				for (int c6 = 0; c6 < 6; c6++)
+					for (int r6 = (bi == bj ? c6 : 0); r6 < 6; r6++)
+						A[(size_t)(6*pj+c6)*nf+6*pi+r6] += Uc[(size_t)(6*bj+c6)*mc6+6*bi+r6];
+			}
+		}
+		free(Uc);
+		f->U[c] = NULL;
+	}
+	int info = 0;
+	g_blas.potrf("L", &n6, A, &nf, &info);
+	if (info > 0) { free(A); return 6*k0+info; }
+	if (m > 0) {
+		const double one = 1.0, mone = -1.0;
+		g_blas.trsm("R", "L", "T", "N", &m6, &n6, &one, A, &nf, A+n6, &nf);
+		g_blas.syrk("L", "N", &m6, &n6, &mone, A+n6, &nf, &one, A+(size_t)n6*nf+n6, &nf);
+		double *U = malloc(sizeof(double)*(size_t)m6*m6);
+#pragma omp parallel for schedule(static) if (par)
+		for (int c = 0; c < m6; c++) memcpy(&U[(size_t)c*m6], &A[(size_t)(n6+c)*nf+n6], sizeof(double)*m6);
+		f->U[q] = U;
+	}
+	/* keep the supernode's columns (L11 over L21) */
+	double *L = malloc(sizeof(double)*(size_t)nf*n6);
+#pragma omp parallel for schedule(static) if (par)
+	for (int c = 0; c < n6; c++) memcpy(&L[(size_t)c*nf], &A[(size_t)c*nf], sizeof(double)*nf);
+	free(A);
+	f->L[q] = L;
+	return 0;
+}
+
+static int sn_factorize(snfact *f, const double *diag36, const double *off36)
+{
+	int n = f->sym->n;
+	int nthr = lfo_num_threads();
+	int bad = 0;
+	int *fpos_all = malloc(sizeof(int)*(size_t)n*(nthr > 0 ? nthr : 1));
+	for (int l = 0; l < f->nlevels && !bad; l++) {
+		int a = f->level_off[l], z = f->level_off[l+1];
+		if (z-a >= 2*nthr && nthr > 1) {
+			/* many fronts: one per thread, single-threaded BLAS */
+			blas_threads(1);
+#pragma omp parallel for schedule(dynamic, 1) reduction(|:bad)
+			for (int t = a; t < z; t++) {
+				int tid = 0;
+#ifdef _OPENMP
+				tid = omp_get_thread_num();
+#endif
+				int st = sn_front(f, f->level_sn[t], diag36, off36, fpos_all+(size_t)tid*n);
+				if (st) bad |= 1;
+			}
+			blas_threads(g_blas.threads);
+		} else {
+			blas_threads(g_blas.threads);
+			for (int t = a; t < z && !bad; t++) {
+				int st = sn_front(f, f->level_sn[t], diag36, off36, fpos_all);
+				if (st) bad = 1;
+			}
+		}
+	}
+	free(fpos_all);
+	return bad ? -5 : 0;
+}
+
+/* x = A^-1 b for k right-hand sides (6n each) */
+static void sn_solve(const snfact *f, int k, const double *b, double *x)
+{
+	const bfact *s = f->sym;
+	int n = s->n, n6t = 6*n;
+	double *y = malloc(sizeof(double)*(size_t)n6t*k);
+	for (int r = 0; r < k; r++)
+		for (int kk = 0; kk < n; kk++) memcpy(&y[(size_t)r*n6t+6*kk], &b[(size_t)r*n6t+6*s->perm[kk]], 6*sizeof(double));
+	int cap = 0;
+	double *tmp = NULL;
+	const double one = 1.0, mone = -1.0;
+	blas_threads(g_blas.threads);
+	/* forward: L y = b */
+	for (int q = 0; q < f->nsn; q++) {
+		int w = f->width[q], m = f->nrows[q], nf = 6*(w+m), n6 = 6*w, m6 = 6*m;
+		double *yq = y+6*(size_t)f->first[q];
+		g_blas.trsm("L", "L", "N", "N", &n6, &k, &one, f->L[q], &nf, yq, &n6t);
+		if (!m) continue;
+		if (cap < m6*k) { free(tmp); cap = m6*k; tmp = malloc(sizeof(double)*cap); }
+		const int *rr = &s->rowidx[f->rows_off[q]];
+		for (int r = 0; r < k; r++)
+			for (int t = 0; t < m; t++)
+				memcpy(&tmp[(size_t)r*m6+6*t], &y[(size_t)r*n6t+6*rr[t]], 6*sizeof(double));
+		g_blas.gemm("N", "N", &m6, &k, &n6, &mone, f->L[q]+n6, &nf, yq, &n6t, &one, tmp, &m6);
+		for (int r = 0; r < k; r++)
+			for (int t = 0; t < m; t++)
+				memcpy(&y[(size_t)r*n6t+6*rr[t]], &tmp[(size_t)r*m6+6*t], 6*sizeof(double));
+	}
+	/* backward: L^T x = y */
+	for (int q = f->nsn-1; q >= 0; q--) {
+		int w = f->width[q], m = f->nrows[q], nf = 6*(w+m), n6 = 6*w, m6 = 6*m;
+		double *yq = y+6*(size_t)f->first[q];
+		if (m) {
+			if (cap < m6*k) { free(tmp); cap = m6*k; tmp = malloc(sizeof(double)*cap); }
+			const int *rr = &s->rowidx[f->rows_off[q]];
+			for (int r = 0; r < k; r++)
+				for (int t = 0; t < m; t++)
+					memcpy(&tmp[(size_t)r*m6+6*t], &y[(size_t)r*n6t+6*rr[t]], 6*sizeof(double));
+			g_blas.gemm("T", "N", &n6, &k, &m6, &mone, f->L[q]+n6, &nf, tmp, &m6, &one, yq, &n6t);
+		}
+		g_blas.trsm("L", "L", "T", "N", &n6, &k, &one, f->L[q], &nf, yq, &n6t);
+	}
+	for (int r = 0; r < k; r++)
+		for (int kk = 0; kk < n; kk++) memcpy(&x[(size_t)r*n6t+6*s->perm[kk]], &y[(size_t)r*n6t+6*kk], 6*sizeof(double));
+	free(tmp);
+	free(y);
+}
+
+/* the factor a system holds: the block factorisation or the supernodal one */
+typedef struct { bfact *b; snfact *sn; } factor_t;
+
+static void fact_free(void *p)
+{
+	factor_t *f = p;
+	if (!f) return;
+	bfact_free(f->b);
+	sn_free(f->sn);
+	free(f);
+}
+
+static void fact_solve(const void *p, const double *b, double *x, double *w)
+{
+	const factor_t *f = p;
+	if (f->sn) sn_solve(f->sn, 1, b, x);
+	else bfact_solve(f->b, b, x, w);
+}
+
 int lfo_bsr_solve(int nblk, const double *diag36, int nb, const int *row, const int *col,
                   const double *off36, int k, const double *b, double *x)
 {
@@ -1315,18 +1703,28 @@ static int factorize_current(lfo_sim *s)
 	double *off36 = malloc(sizeof(double)*36*(s->nod > 0 ? s->nod : 1));
 	for (int i = 0; i < n; i++) lfo_dblock_to_dense(&s->dblocks[i*15], &diag36[i*36]);
 	for (int e = 0; e < s->nod; e++) lfo_odblock_to_dense(&s->odblocks[e*18], &off36[e*36]);
-	if (s->fact) { bfact_free(s->fact); s->fact = NULL; }
-	double t0 = wall_s();
-	bfact *f = bfact_analyze(n, s->nod, s->odrow, s->odcol);
-	double t1 = wall_s();
-	int st = f ? bfact_factorize(f, diag36, s->nod, s->odrow, s->odcol, off36) : -1;
-	double t2 = wall_s();
+	if (s->fact) { fact_free(s->fact); s->fact = NULL; }
+	factor_t *F = calloc(1, sizeof(factor_t));
+	double t0 = wall_s(), t1, t2;
+	int st;
+	if (lfo_blas_ready()) {
+		F->sn = sn_analyze(n, s->nod, s->odrow, s->odcol);
+		t1 = wall_s();
+		st = F->sn ? sn_factorize(F->sn, diag36, off36) : -1;
+		t2 = wall_s();
+		if (F->sn) s->last_factor_flops = bfact_flops(F->sn->sym);
+	} else {
+		F->b = bfact_analyze(n, s->nod, s->odrow, s->odcol);
+		t1 = wall_s();
+		st = F->b ? bfact_factorize(F->b, diag36, s->nod, s->odrow, s->odcol, off36) : -1;
+		t2 = wall_s();
+		if (F->b) s->last_factor_flops = bfact_flops(F->b);
+	}
 	s->n_factor++;
 	s->analyze_s += t1-t0;
 	s->factor_s += t2-t1;
-	if (f) s->last_factor_flops = bfact_flops(f);
 	free(diag36); free(off36);
-	s->fact = f;
+	s->fact = F;
 	return st;
 }
 
@@ -1345,7 +1743,7 @@ int lfo_solve_assembled(lfo_sim *s, int k, const double *b, double *x)
 	int st = factorize_current(s);
 	if (st) return st;
 	double *w = malloc(sizeof(double)*6*s->np);
-	for (int r = 0; r < k; r++) bfact_solve(s->fact, &b[(size_t)r*6*s->np], &x[(size_t)r*6*s->np], w);
+	for (int r = 0; r < k; r++) fact_solve(s->fact, &b[(size_t)r*6*s->np], &x[(size_t)r*6*s->np], w);
 	free(w);
 	return 0;
 }
@@ -1511,7 +1909,7 @@ static int compute_velocities(lfo_sim *s, int divided)
 			if (!s->has_fc[c]) continue;
 			force_component(s, c, s->fc_force[c]);
 			rhs_set(s, c, s->fc_force[c], rhs);
-			bfact_solve(s->fact, rhs, s->vc[c], w);
+			fact_solve(s->fact, rhs, s->vc[c], w);
 		}
 		if (s->p.control == 1) {
 			/* System::computeShearRate, System.cpp:2017-2055 */
@@ -1558,7 +1956,7 @@ static int compute_velocities(lfo_sim *s, int divided)
 			force_component(s, c, s->fc_force[c]);
 			rhs_add(s, c, s->fc_force[c], rhs);
 		}
-		bfact_solve(s->fact, rhs, x, w);
+		fact_solve(s->fact, rhs, x, w);
 		for (int i = 0; i < n; i++) {
 			s->na_vel[i] = V(x[6*i], x[6*i+1], x[6*i+2]);
 			s->na_ang[i] = V(x[6*i+3], x[6*i+4], x[6*i+5]);
@@ -2010,7 +2408,7 @@ void lfo_destroy(lfo_sim *s)
 	for (int c = 0; c < NFC; c++) { free(s->fc_force[c]); free(s->vc[c]); }
 	for (int c = 0; c < NSC; c++) free(s->sc[c]);
 	free(s->pairs); free(s->dblocks); free(s->odrow); free(s->odcol); free(s->odblocks);
-	bfact_free(s->fact);
+	fact_free(s->fact);
 	free(s);
 }
 

@@ -180,6 +180,15 @@ void lfo_set_num_threads(int n);   /* OpenMP threads of later parallel regions *
  * factorisation}. */
 void lfo_factor_stats(const lfo_sim *s, double *out4);
 
+/* Dense kernels for the supernodal factorisation (the method of CHOLMOD's
+ * supernodal factorisation, which the reference calls): LAPACK dpotrf and
+ * BLAS dtrsm, dsyrk, dgemm with the Fortran calling convention (32-bit
+ * integers), and optionally the BLAS library's thread-count setter and the
+ * thread count to use for the large fronts.  Once set, every later
+ * factorisation is supernodal; without them the block factorisation runs. */
+void lfo_set_blas(void *potrf, void *trsm, void *syrk, void *gemm, void *set_threads, int threads);
+int lfo_blas_ready(void);
+
 /* Block (compact -> dense 6x6 row-major) reconstructions of
  * StokesSolver.cpp:154-231 (rows of the lower block, columns of the column
  * particle). */

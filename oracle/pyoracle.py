@@ -106,6 +106,8 @@ def lib():
         L.lfo_refresh.argtypes = [C.c_void_p]
         L.lfo_num_threads.restype = C.c_int
         L.lfo_set_num_threads.argtypes = [C.c_int]
+        L.lfo_set_blas.argtypes = [C.c_void_p] * 5 + [C.c_int]
+        L.lfo_blas_ready.restype = C.c_int
         L.lfo_factor_stats.argtypes = [C.c_void_p, C.c_void_p]
         L.lfo_dblock_to_dense.argtypes = [dp, dp]
         L.lfo_odblock_to_dense.argtypes = [dp, dp]
@@ -259,6 +261,53 @@ def factor_stats(sim) -> dict:
     lib().lfo_factor_stats(sim.h, out.ctypes.data)
     return {"factorisations": int(out[0]), "factor_flops": float(out[1]), "analyze_s": float(out[2]),
             "factor_s": float(out[3])}
+
+
+def _capsule_ptr(capsule) -> int:
+    get_name = C.pythonapi.PyCapsule_GetName
+    get_name.restype = C.c_char_p
+    get_name.argtypes = [C.py_object]
+    get_ptr = C.pythonapi.PyCapsule_GetPointer
+    get_ptr.restype = C.c_void_p
+    get_ptr.argtypes = [C.py_object, C.c_char_p]
+    return get_ptr(capsule, get_name(capsule))
+
+
+def use_blas(threads: int = 0) -> bool:
+    """Switch the oracle's factorisation to the supernodal one with dense
+    BLAS-3 kernels (the method of CHOLMOD's supernodal factorisation), taking
+    dpotrf, dtrsm, dsyrk and dgemm from scipy's BLAS/LAPACK (Fortran
+    interface, through scipy.linalg.cython_blas / cython_lapack) and the
+    OpenBLAS thread setter of scipy's bundled OpenBLAS when there is one.
+    threads: BLAS threads for the large fronts (0: the OpenMP thread count).
+    Returns False when scipy is not available (the block factorisation stays)."""
+    try:
+        import scipy.linalg.cython_blas as cb
+        import scipy.linalg.cython_lapack as cl
+    except ImportError:
+        return False
+    potrf = _capsule_ptr(cl.__pyx_capi__["dpotrf"])
+    trsm = _capsule_ptr(cb.__pyx_capi__["dtrsm"])
+    syrk = _capsule_ptr(cb.__pyx_capi__["dsyrk"])
+    gemm = _capsule_ptr(cb.__pyx_capi__["dgemm"])
+    setter = None
+    import glob
+    import scipy
+    libdir = os.path.join(os.path.dirname(os.path.dirname(scipy.__file__)), "scipy.libs")
+    for path in sorted(glob.glob(os.path.join(libdir, "*openblas*.so*"))):
+        try:
+            blas = C.CDLL(path)
+        except OSError:
+            continue
+        for name in ("scipy_openblas_set_num_threads", "openblas_set_num_threads"):
+            fn = getattr(blas, name, None)
+            if fn is not None:
+                setter = C.cast(fn, C.c_void_p).value
+                break
+        if setter:
+            break
+    lib().lfo_set_blas(potrf, trsm, syrk, gemm, setter, int(threads) if threads > 0 else num_threads())
+    return bool(lib().lfo_blas_ready())
 
 
 def set_num_threads(n: int) -> None:
