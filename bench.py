@@ -288,6 +288,8 @@ def cpu_baseline(packing, nsteps=3, one_thread=True):
     del o
     if one_thread:
         pyoracle.set_num_threads(1)
+        if pyoracle.lib().lfo_blas_ready():
+            pyoracle.use_blas(threads=1)   # the BLAS library's threads too
         o1 = pyoracle.OracleSim(workload_params(), packing.position, packing.radius, packing.lx, packing.ly,
                                 packing.lz)
         o1.first_time()
@@ -301,6 +303,8 @@ def cpu_baseline(packing, nsteps=3, one_thread=True):
                              max(fs1["factor_s"], 1e-12) / 1e9}
         del o1
         pyoracle.set_num_threads(cores)
+        if pyoracle.lib().lfo_blas_ready():
+            pyoracle.use_blas(threads=cores)
     return rec, ref
 
 
@@ -451,7 +455,10 @@ def bench_sweep(args):
     B.build()
     E.load()
     out = {}
-    for label, threads in (("fused", 0), ("concurrent", 16), ("one_thread", 1)):
+    modes = (("fused", 0), ("concurrent", 16), ("one_thread", 1))
+    if getattr(args, "sweep_modes", None):
+        modes = tuple(m for m in modes if m[0] in args.sweep_modes)
+    for label, threads in modes:
         if label == "fused":
             b = E.Batch(fused=True, precision=E.PREC_FP32_REFINE)
         else:
@@ -488,9 +495,10 @@ def bench_sweep(args):
                        "total_particles": int(ns.sum()),
                        "note": "fixed step count per suspension instead of 2 strain units; host wall time"},
             **out}
-    line["fused_vs_concurrent"] = out["fused"]["particle_steps_per_s"] / out["concurrent"]["particle_steps_per_s"]
-    line["fused_vs_one_thread"] = out["fused"]["particle_steps_per_s"] / out["one_thread"]["particle_steps_per_s"]
-    print(json.dumps(line), flush=True)
+    for other in ("concurrent", "one_thread"):
+        if other in out:
+            line[f"fused_vs_{other}"] = out["fused"]["particle_steps_per_s"] / out[other]["particle_steps_per_s"]
+    return line
 
 
 def monolayer_params():
@@ -577,7 +585,7 @@ def bench_cfg3(args):
             "config": {"n_particles": n, "areal_fraction": 0.78, "control": "rate 1r", "twodim": True,
                        "note": "fixed step count instead of 3 strain units; device time per step (CUDA events)"},
             **out, "speedup_dof3_vs_dof6": out["dof3"]["particle_steps_per_s"] / out["dof6"]["particle_steps_per_s"]}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def bench_serve(args):
@@ -637,6 +645,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 form")
+    ap.add_argument("--no-others", action="store_true",
+                    help="skip the short cfg3 (2D monolayer) and sweep measurements of the default run")
     ap.add_argument("--profile", action="store_true",
                     help="profiling driver: FP32 form only, W + K steps, no measurement (for ncu)")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"], help="form used by --profile")
@@ -651,10 +661,10 @@ def main():
     ap.add_argument("--hbm-budget-gb", type=float, default=200.0, help="serve: device bytes for admission")
     args = ap.parse_args()
     if args.workload == "cfg3":
-        bench_cfg3(args)
+        print(json.dumps(bench_cfg3(args)), flush=True)
         return
     if args.workload == "sweep":
-        bench_sweep(args)
+        print(json.dumps(bench_sweep(args)), flush=True)
         return
     if args.workload == "serve":
         bench_serve(args)
@@ -757,6 +767,16 @@ def main():
         line["cpu_baseline"], oracle_ref = cpu_baseline(pk)
     if not args.no_fp64:
         line.update(accuracy(E, pk, local, oracle_ref))
+    if not args.no_others:
+        # the other configured workloads, short: the 2D monolayer (cfg3) and
+        # the batched sweep (cfg4, fused and concurrent)
+        import copy
+        a3 = copy.copy(args)
+        a3.steps, a3.warmup, a3.count = 200, 3, 0
+        line["cfg3"] = bench_cfg3(a3)
+        a4 = copy.copy(args)
+        a4.steps, a4.warmup, a4.count, a4.sweep_modes = 5, 3, 0, ("fused", "concurrent")
+        line["sweep"] = bench_sweep(a4)
     print(json.dumps(line), flush=True)
 
 

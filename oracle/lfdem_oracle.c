@@ -1492,12 +1492,9 @@ static int sn_front(snfact *f, int q, const double *diag36, const double *off36,
 	bfact *b = f->sym;
 	int w = f->width[q], m = f->nrows[q], F = w+m, k0 = f->first[q];
 	int nf = 6*F, n6 = 6*w, m6 = 6*m;
-	/* large fronts are assembled by all threads (outside the parallel
-	 * levels); every column is touched by one thread only */
-	int par = nf > 600;
-#ifdef _OPENMP
-	if (omp_in_parallel()) par = 0;
-#endif
+	/* the copies run on one thread: OpenMP threads next to the BLAS
+	 * library's own (spinning) threads were measured slower */
+	const int par = 0;
 	double *A = malloc(sizeof(double)*(size_t)nf*nf);
 	if (!A) return -4;
 #pragma omp parallel for schedule(static) if (par)
