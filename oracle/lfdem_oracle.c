@@ -1655,6 +1655,43 @@ static void fact_solve(const void *p, const double *b, double *x, double *w)
 	else bfact_solve(f->b, b, x, w);
 }
 
+/* A factor of a block matrix on its own (the reference harness's CHOLMOD
+ * stand-in): supernodal when the BLAS kernels are set, block otherwise. */
+struct lfo_factor { factor_t f; int n; };
+
+lfo_factor *lfo_factor_create(int nblk, const double *diag36, int nb, const int *row, const int *col,
+                              const double *off36, int *status)
+{
+	lfo_factor *h = calloc(1, sizeof(lfo_factor));
+	h->n = nblk;
+	int st;
+	if (lfo_blas_ready()) {
+		h->f.sn = sn_analyze(nblk, nb, row, col);
+		st = h->f.sn ? sn_factorize(h->f.sn, diag36, off36) : -1;
+	} else {
+		h->f.b = bfact_analyze(nblk, nb, row, col);
+		st = h->f.b ? bfact_factorize(h->f.b, diag36, nb, row, col, off36) : -1;
+	}
+	if (status) *status = st;
+	return h;
+}
+
+void lfo_factor_solve(const lfo_factor *h, int k, const double *b, double *x)
+{
+	if (h->f.sn) { sn_solve(h->f.sn, k, b, x); return; }
+	double *w = malloc(sizeof(double)*6*(size_t)h->n);
+	for (int r = 0; r < k; r++) bfact_solve(h->f.b, &b[(size_t)r*6*h->n], &x[(size_t)r*6*h->n], w);
+	free(w);
+}
+
+void lfo_factor_free(lfo_factor *h)
+{
+	if (!h) return;
+	bfact_free(h->f.b);
+	sn_free(h->f.sn);
+	free(h);
+}
+
 int lfo_bsr_solve(int nblk, const double *diag36, int nb, const int *row, const int *col,
                   const double *off36, int k, const double *b, double *x)
 {

@@ -189,6 +189,16 @@ void lfo_factor_stats(const lfo_sim *s, double *out4);
 void lfo_set_blas(void *potrf, void *trsm, void *syrk, void *gemm, void *set_threads, int threads);
 int lfo_blas_ready(void);
 
+/* A factor of an SPD block matrix on its own (6x6 blocks: diag36 n x 36
+ * row-major, nb lower off-diagonal blocks (row > col) off36 row-major):
+ * supernodal when the BLAS kernels are set, block otherwise; *status 0 or
+ * the failing column + 1.  Solve: k right-hand sides of 6n. */
+typedef struct lfo_factor lfo_factor;
+lfo_factor *lfo_factor_create(int nblk, const double *diag36, int nb, const int *row, const int *col,
+                              const double *off36, int *status);
+void lfo_factor_solve(const lfo_factor *f, int k, const double *b, double *x);
+void lfo_factor_free(lfo_factor *f);
+
 /* Block (compact -> dense 6x6 row-major) reconstructions of
  * StokesSolver.cpp:154-231 (rows of the lower block, columns of the column
  * particle). */

@@ -57,7 +57,14 @@ typedef struct cholmod_factor_struct {
 	size_t n;
 	int is_ll;
 	double *L; /* dense lower factor, column-major n x n (compat only) */
+	void *blk; /* block mode: the oracle's factor of the 6x6-block matrix */
 } cholmod_factor;
+
+/* Block mode (compat only): factorise through the oracle's block-matrix
+ * factor (supernodal with BLAS kernels when those are set) instead of the
+ * dense stand-in; for LF_DEM's 6x6-block R_FU at sizes where a dense factor
+ * does not fit.  Solves with CHOLMOD_A only. */
+void cholmod_compat_use_blocks(int on);
 
 int cholmod_start(cholmod_common *c);
 int cholmod_finish(cholmod_common *c);

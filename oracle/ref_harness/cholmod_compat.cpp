@@ -1,7 +1,11 @@
 // cholmod_compat.cpp -- dense FP64 stand-in for the CHOLMOD calls made by
 // LF_DEM's StokesSolver.cpp.  TEST INFRASTRUCTURE ONLY (see cholmod.h).
 #include "cholmod.h"
+#include "../lfdem_oracle.h"
 #include <cmath>
+#include <cstdio>
+#include <map>
+#include <utility>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -110,18 +114,67 @@ cholmod_sparse *cholmod_transpose(cholmod_sparse *A, int, cholmod_common *c)
 	return T;
 }
 
+static int g_blocks = 0;
+void cholmod_compat_use_blocks(int on) { g_blocks = on; }
+
 cholmod_factor *cholmod_analyze(cholmod_sparse *A, cholmod_common *)
 {
 	cholmod_factor *L = (cholmod_factor *)std::calloc(1, sizeof(cholmod_factor));
 	L->n = A->nrow;
 	L->is_ll = 1;
-	L->L = (double *)std::calloc(L->n*L->n, sizeof(double));
+	if (!g_blocks) L->L = (double *)std::calloc(L->n*L->n, sizeof(double));
 	return L;
+}
+
+// block mode: the lower scalar CSC (stype -1) as 6x6 blocks, factored by the
+// oracle (row-major blocks; off-diagonal ones with block row > block column)
+static int factorize_blocks(cholmod_sparse *A, cholmod_factor *L, cholmod_common *c)
+{
+	size_t n = A->nrow;
+	if (n%6) { std::fprintf(stderr, "cholmod_compat: block mode needs 6 unknowns per particle\n"); std::abort(); }
+	int nblk = (int)(n/6);
+	const int *p = (const int *)A->p, *ii = (const int *)A->i;
+	const double *x = (const double *)A->x;
+	std::vector<double> diag((size_t)nblk*36, 0.0), off;
+	std::vector<int> brow, bcol;
+	std::map<std::pair<int, int>, int> index;
+	for (size_t j = 0; j < A->ncol; j++) {
+		int bj = (int)(j/6), cj = (int)(j%6);
+		for (int k = p[j]; k < p[j+1]; k++) {
+			int i = ii[k];
+			if ((size_t)i < j) continue;   // lower part only
+			int bi = i/6, ci = i%6;
+			if (bi == bj) {
+				diag[(size_t)bi*36+ci*6+cj] += x[k];
+				if (ci != cj) diag[(size_t)bi*36+cj*6+ci] += x[k];
+			} else {
+				auto key = std::make_pair(bi, bj);
+				auto it = index.find(key);
+				int e;
+				if (it == index.end()) {
+					e = (int)brow.size();
+					index[key] = e;
+					brow.push_back(bi); bcol.push_back(bj);
+					off.resize(off.size()+36, 0.0);
+				} else {
+					e = it->second;
+				}
+				off[(size_t)e*36+ci*6+cj] += x[k];
+			}
+		}
+	}
+	if (L->blk) lfo_factor_free((lfo_factor *)L->blk);
+	int status = 0;
+	L->blk = lfo_factor_create(nblk, diag.data(), (int)brow.size(), brow.data(), bcol.data(),
+	                           off.empty() ? nullptr : off.data(), &status);
+	c->status = status ? CHOLMOD_NOT_POSDEF : CHOLMOD_OK;
+	return status ? 0 : 1;
 }
 
 // dense right-looking Cholesky of the lower triangle, column-major
 int cholmod_factorize(cholmod_sparse *A, cholmod_factor *L, cholmod_common *c)
 {
+	if (g_blocks) return factorize_blocks(A, L, c);
 	size_t n = A->nrow;
 	double *M = L->L;
 	to_dense_sym(A, M);
@@ -146,12 +199,16 @@ int cholmod_factorize(cholmod_sparse *A, cholmod_factor *L, cholmod_common *c)
 
 int cholmod_free_factor(cholmod_factor **L, cholmod_common *)
 {
-	if (L && *L) { std::free((*L)->L); std::free(*L); *L = nullptr; }
+	if (L && *L) {
+		if ((*L)->blk) lfo_factor_free((lfo_factor *)(*L)->blk);
+		std::free((*L)->L); std::free(*L); *L = nullptr;
+	}
 	return 1;
 }
 
 cholmod_factor *cholmod_copy_factor(cholmod_factor *L, cholmod_common *)
 {
+	if (L->blk) { std::fprintf(stderr, "cholmod_compat: no factor copy in block mode\n"); std::abort(); }
 	cholmod_factor *C = (cholmod_factor *)std::calloc(1, sizeof(cholmod_factor));
 	C->n = L->n; C->is_ll = L->is_ll;
 	C->L = (double *)std::malloc(sizeof(double)*L->n*L->n);
@@ -161,6 +218,7 @@ cholmod_factor *cholmod_copy_factor(cholmod_factor *L, cholmod_common *)
 
 cholmod_sparse *cholmod_factor_to_sparse(cholmod_factor *L, cholmod_common *c)
 {
+	if (L->blk) { std::fprintf(stderr, "cholmod_compat: no sparse factor in block mode\n"); std::abort(); }
 	size_t n = L->n;
 	size_t nnz = n*(n+1)/2;
 	cholmod_sparse *S = cholmod_allocate_sparse(n, n, nnz, 1, 1, 0, CHOLMOD_REAL, c);
@@ -183,6 +241,13 @@ int cholmod_solve2(int sys, cholmod_factor *L, cholmod_dense *B, cholmod_sparse 
 	if (!*X_Handle || (*X_Handle)->nrow != B->nrow || (*X_Handle)->ncol != B->ncol) {
 		cholmod_free_dense(X_Handle, c);
 		*X_Handle = cholmod_allocate_dense(B->nrow, B->ncol, B->nrow, CHOLMOD_REAL, c);
+	}
+	if (L->blk) {
+		if (sys != CHOLMOD_A) { std::fprintf(stderr, "cholmod_compat: block mode solves CHOLMOD_A only\n"); std::abort(); }
+		for (size_t col = 0; col < B->ncol; col++)
+			lfo_factor_solve((const lfo_factor *)L->blk, 1, (const double *)B->x+col*B->d,
+			                 (double *)(*X_Handle)->x+col*(*X_Handle)->d);
+		return 1;
 	}
 	for (size_t col = 0; col < B->ncol; col++) {
 		const double *b = (const double *)B->x + col*B->d;

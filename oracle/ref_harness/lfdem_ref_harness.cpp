@@ -50,8 +50,23 @@
 #undef private
 #undef protected
 
+#include "../lfdem_oracle.h"
+#include <chrono>
+
 // main.cpp:25 defines this flag; the harness replaces main.cpp.
 volatile sig_atomic_t sig_caught = 0;
+
+// scipy's OpenBLAS (linked by oracle/Makefile's ref target)
+extern "C" {
+void scipy_dpotrf_(const char *, const int *, double *, const int *, int *);
+void scipy_dtrsm_(const char *, const char *, const char *, const char *, const int *, const int *, const double *,
+                  const double *, const int *, double *, const int *);
+void scipy_dsyrk_(const char *, const char *, const int *, const int *, const double *, const double *, const int *,
+                  const double *, double *, const int *);
+void scipy_dgemm_(const char *, const char *, const int *, const int *, const int *, const double *, const double *,
+                  const int *, const double *, const int *, const double *, double *, const int *);
+void scipy_openblas_set_num_threads(int);
+}
 
 static FILE *g_out = nullptr;
 
@@ -189,6 +204,14 @@ int main(int argc, char **argv)
 	int calc_stress = argc > 8 ? atoi(argv[8]) : 0;
 	int stage = argc > 9 ? atoi(argv[9]) : 1;
 
+	// HARNESS_SUPERNODAL: CHOLMOD's calls go to the oracle's supernodal
+	// block factorisation with OpenBLAS kernels (the method of CHOLMOD's
+	// supernodal factorisation) instead of the dense stand-in
+	if (getenv("HARNESS_SUPERNODAL")) {
+		lfo_set_blas((void *)scipy_dpotrf_, (void *)scipy_dtrsm_, (void *)scipy_dsyrk_, (void *)scipy_dgemm_,
+		             (void *)scipy_openblas_set_num_threads, lfo_num_threads());
+		cholmod_compat_use_blocks(1);
+	}
 	std::cout.setstate(std::ios_base::failbit);
 	Simulation sim;
 	sim.sys.ext_flow = false;
@@ -254,6 +277,31 @@ int main(int argc, char **argv)
 			sim.generateOutput(ev, counter);
 		}
 		std::cout.clear();
+		return 0;
+	}
+	// Timing mode: with HARNESS_TIME_STEPS set, the reference's own time
+	// step (System::adaptTimeStep + timeEvolutionPredictorCorrectorMethod,
+	// the loop of System::timeEvolution, System.cpp:1243-1250) runs
+	// HARNESS_WARMUP steps (default 1), then HARNESS_TIME_STEPS steps are
+	// timed (wall clock) and reported on stdout in one line.
+	if (const char *ts = getenv("HARNESS_TIME_STEPS")) {
+		int K = atoi(ts), W = getenv("HARNESS_WARMUP") ? atoi(getenv("HARNESS_WARMUP")) : 1;
+		std::cout.setstate(std::ios_base::failbit);
+		sys.timeEvolution(-1, 0);   // the first-time set-up (and one stress step)
+		auto loop = [&](int nsteps) {
+			for (int k = 0; k < nsteps; k++) {
+				if (!sys.brownian && !sys.p.fixed_dt) sys.adaptTimeStep(-1, 1e9);
+				if (sys.p.integration_method == 0) sys.timeEvolutionEulersMethod(false, -1, 1e9);
+				else sys.timeEvolutionPredictorCorrectorMethod(false, -1, 1e9);
+			}
+		};
+		loop(W);
+		auto t0 = std::chrono::steady_clock::now();
+		loop(K);
+		double sec = std::chrono::duration<double>(std::chrono::steady_clock::now()-t0).count();
+		std::cout.clear();
+		printf("steps %d seconds %.3f particle_steps_per_s %.1f np %d threads %d supernodal %d\n", K, sec,
+		       (double)sys.np*K/sec, sys.np, lfo_num_threads(), getenv("HARNESS_SUPERNODAL") ? 1 : 0);
 		return 0;
 	}
 	// System::timeEvolution first-time block (System.cpp:1216-1226)
