@@ -171,6 +171,24 @@ def _errors(a, b):
     return out
 
 
+def rebuild_cost(E, packing, device, steps=12, skin=0.001):
+    """The host cost of one pattern change at this workload: a short run with
+    a pair-superset skin so thin that the superset goes stale nearly every
+    step, so that each rebuild (candidate pairs, symbolic analysis, upload,
+    graph capture) is timed; the default skin changes the pattern far less
+    often (pattern_changes)."""
+    g = E.Sim(workload_params(), packing.position, packing.radius, packing.lx, packing.ly, packing.lz,
+              precision=E.PREC_FP32_REFINE, device=device, skin=skin)
+    g.run(2)
+    g.clear_step_times()
+    g.run(steps)
+    tim = g.timing()
+    g.close()
+    r = tim["rebuilds"]
+    return {"steps": steps, "skin": skin, "rebuilds": r,
+            "rebuild_host_ms_mean": tim["rebuild_ms"] / r if r else None}
+
+
 def pattern_changes(E, packing, device, steps):
     """A longer run of the FP32 + refinement form from the packing, long
     enough for the pair superset to run out of skin: how often the pattern of
@@ -634,7 +652,7 @@ def bench_serve(args):
                        "max_active": args.max_active, "hbm_budget_gb": args.hbm_budget_gb,
                        "note": f"strain target {args.strain} instead of 1 strain unit"},
             "server": st, "total_steps": int(sum(r.steps for r in res)), "span_s": span}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
@@ -646,7 +664,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 form")
     ap.add_argument("--no-others", action="store_true",
-                    help="skip the short cfg3 (2D monolayer) and sweep measurements of the default run")
+                    help="skip the short cfg3 (2D monolayer), sweep and serve measurements of the default run")
     ap.add_argument("--profile", action="store_true",
                     help="profiling driver: FP32 form only, W + K steps, no measurement (for ncu)")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"], help="form used by --profile")
@@ -654,7 +672,7 @@ def main():
                     help="cfg2: the metric's workload (default); cfg3: the 2D monolayer; "
                          "sweep / serve: the batched and serving forms")
     ap.add_argument("--count", type=int, default=0, help="suspensions (sweep) or requests (serve)")
-    ap.add_argument("--long-steps", type=int, default=400,
+    ap.add_argument("--long-steps", type=int, default=1500,
                     help="steps of the run that counts pattern changes (0: skip)")
     ap.add_argument("--strain", type=float, default=0.002, help="serve: strain target of each request")
     ap.add_argument("--max-active", type=int, default=8, help="serve: concurrent requests")
@@ -667,7 +685,7 @@ def main():
         print(json.dumps(bench_sweep(args)), flush=True)
         return
     if args.workload == "serve":
-        bench_serve(args)
+        print(json.dumps(bench_serve(args)), flush=True)
         return
     if args.profile:
         import lf_dem_gb300 as E
@@ -762,6 +780,7 @@ def main():
     line["e2e"] = run_e2e(E, pk, E.PREC_FP32_REFINE, args.steps, local)
     if args.long_steps > 0:
         line["pattern_changes"] = pattern_changes(E, pk, local, args.long_steps)
+        line["pattern_changes"]["forced_rebuilds"] = rebuild_cost(E, pk, local)
     oracle_ref = None
     if not args.no_cpu:
         line["cpu_baseline"], oracle_ref = cpu_baseline(pk)
@@ -777,6 +796,9 @@ def main():
         a4 = copy.copy(args)
         a4.steps, a4.warmup, a4.count, a4.sweep_modes = 5, 3, 0, ("fused", "concurrent")
         line["sweep"] = bench_sweep(a4)
+        a5 = copy.copy(args)
+        a5.count, a5.strain, a5.max_active, a5.hbm_budget_gb = 24, 0.0005, 8, 200.0
+        line["serve"] = bench_serve(a5)
     print(json.dumps(line), flush=True)
 
 

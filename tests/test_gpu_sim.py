@@ -86,3 +86,26 @@ def test_fp32_refine_step(oracle, engine):
     po, pg = o.particles(), g.particles()
     err = np.abs(po["vel"] - pg["vel"]).max() / np.abs(po["vel"]).max()
     assert err <= 1e-8, err
+
+
+@pytest.mark.parametrize("params,n,vf,seed,twod", [(RATE_PARAMS, 400, 0.52, 36, False),
+                                                  (RATE_PARAMS, 500, 0.75, 37, True)], ids=["3d", "2d"])
+def test_thin_skin_rebuilds_keep_pair_lists(oracle, engine, params, n, vf, seed, twod):
+    """A thin pair-superset skin makes the per-step superset check (one CTA
+    per cell, neighbour cells staged in shared memory) trigger rebuilds
+    often; every step's interactions must still be exactly the oracle's."""
+    from lf_dem_gb300 import packing as PK
+    p = PK.generate(n, vf, seed=seed, twodim=twod)
+    o = oracle.OracleSim(params, p.position, p.radius, p.lx, p.ly, p.lz)
+    o.first_time()
+    g = engine.Sim(params, p.position, p.radius, p.lx, p.ly, p.lz, skin=0.001)
+    for k in range(25):
+        o.step()
+        g.step()
+        qo, qg = o.pairs(), g.pairs()
+        assert np.array_equal(_pair_keys(qo), _pair_keys(qg)), k
+        assert np.array_equal(qo["contact_active"], qg["contact_active"]), k
+        err = np.abs(o.particles()["pos"] - g.particles()["pos"]).max()
+        assert err <= 1e-10 * max(p.lx, p.lz), k
+    assert g.scalars()["n_symbolic_runs"] >= 3
+    g.close()
