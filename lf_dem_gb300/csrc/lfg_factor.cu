@@ -269,7 +269,7 @@ __global__ void k_scatter(int nd, int nod, const int *__restrict__ dlist, const 
 }
 
 // ---------------------------------------------------------------------------
-// diagonal block of panel k (k_diag): one CTA (128 threads) per front.  The
+// diagonal block of panel k (k_diag): one CTA (256 threads) per front.  The
 // NB x NB block (NB = 32 or 64) is factored by 32 x 32 sub-blocks, each by
 // one warp holding its rows in registers (lane = row), then inverted:
 // Linv = L_kk^-1 (lower triangular).  k_diag writes L_kk back into the front
@@ -331,10 +331,38 @@ __device__ __forceinline__ float pivot_rsqrt(float x)
 }
 __device__ __forceinline__ double pivot_rsqrt(double x) { return rsqrt(x); }
 
+// Progress flags of the FP32 diagonal-block pipeline (shared memory): the
+// producer warp publishes "columns [0, v) are in Lsh" with a release store
+// after the __syncwarp that follows its lanes' stores; a follower warp polls
+// with acquire loads.  The wait is bounded: past the limit it records status 0
+// (LFG_ERR_TIMEOUT) and goes on, so a broken pipeline cannot hang the SM.
+__device__ __forceinline__ void flag_publish(int *p, int v)
+{
+	asm volatile("st.release.cta.shared::cta.u32 [%0], %1;"
+	             :: "r"((unsigned)__cvta_generic_to_shared(p)), "r"(v) : "memory");
+}
+__device__ __forceinline__ int flag_read(const int *p)
+{
+	int v;
+	asm volatile("ld.acquire.cta.shared::cta.u32 %0, [%1];"
+	             : "=r"(v) : "r"((unsigned)__cvta_generic_to_shared(p)) : "memory");
+	return v;
+}
+constexpr int FLAG_SPIN_LIMIT = 1 << 22;   // ~0.1 s of polls
+__device__ __forceinline__ void flag_wait(const int *p, int need, int *fail)
+{
+	if (!p) return;
+	for (int it = 0; it < FLAG_SPIN_LIMIT; it++)
+		if (flag_read(p) >= need) return;
+	if (fail) atomicMin(fail, 0);
+}
+
 // Cholesky of S (lower part), lane = row; S's lower part becomes L and its
-// upper part zero; Lsh receives L's columns
+// upper part zero; Lsh receives L's columns, and *flag (if given) the number
+// of columns already there.  Two steps per loop iteration: the second step's
+// chain can start while the first step's updates of later columns issue.
 template <typename T>
-__device__ void warp_potrf32(T *S, int ld, T *Lsh, int lane, int jlim, int gcol0, int *fail)
+__device__ void warp_potrf32(T *S, int ld, T *Lsh, int lane, int jlim, int gcol0, int *fail, int *flag)
 {
 	T a[32];   // at step j: a[q] = S[lane][j + q]
 #pragma unroll
@@ -345,7 +373,7 @@ __device__ void warp_potrf32(T *S, int ld, T *Lsh, int lane, int jlim, int gcol0
 		djj = T(1);
 	}
 	T rs = pivot_rsqrt(djj);
-#pragma unroll 1
+#pragma unroll 2
 	for (int j = 0; j < 32; j++) {
 		T lij = a[0]*rs;
 		// the next pivot first: lane j + 1 updates its own diagonal entry with
@@ -364,31 +392,42 @@ __device__ void warp_potrf32(T *S, int ld, T *Lsh, int lane, int jlim, int gcol0
 		for (int q = 1; q < 32; q++) a[q-1] = a[q]-lij*c[q];   // entries past the block are dead
 		djj = dn;
 		rs = rsn;
+		if (flag && lane == 0) flag_publish(flag, j+1);
 	}
 	__syncwarp();
 }
 
 // X L^T = A for 32 rows (lane = row) of X (stride ldx), L lower given by its
 // columns in Lsh; X replaces A.  Columns alternate between two register
-// buffers, each loaded one step before its use.
+// buffers, each loaded one step before its use.  With a flag the routine
+// follows a warp_potrf32 still producing Lsh (each column is loaded once the
+// flag shows it), and with pub it publishes its own solved columns of X.
 template <typename T>
-__device__ void warp_trsm32(T *X, int ldx, const T *Lsh, int lane)
+__device__ void warp_trsm32(T *X, int ldx, const T *Lsh, int lane, const int *flag = nullptr, int *fail = nullptr,
+                            int *pub = nullptr)
 {
 	T x[32];   // at step t: x[q] = X[lane][t + q]
 #pragma unroll
 	for (int l = 0; l < 32; l++) x[l] = X[lane*ldx+l];
 	T c[32], d[32];
+	flag_wait(flag, 1, fail);
 	lsh_column<T>(Lsh, 0, c);
 #pragma unroll 1
 	for (int t = 0; t < 32; t += 2) {
+		flag_wait(flag, t+2, fail);
 		lsh_column<T>(Lsh, t+1, d);
 		T xt = x[0]*c[0];
 		X[lane*ldx+t] = xt;
 #pragma unroll
 		for (int q = 1; q < 32; q++) x[q-1] = x[q]-xt*c[q];
+		flag_wait(flag, min(t+3, 32), fail);
 		lsh_column<T>(Lsh, (t+2) & 31, c);   // after the last pair: column 0 again, unused
 		xt = x[0]*d[0];
 		X[lane*ldx+t+1] = xt;
+		if (pub) {
+			__syncwarp();
+			if (lane == 0) flag_publish(pub, t+2);
+		}
 #pragma unroll
 		for (int q = 1; q < 32; q++) x[q-1] = x[q]-xt*d[q];
 	}
@@ -396,22 +435,25 @@ __device__ void warp_trsm32(T *X, int ldx, const T *Lsh, int lane)
 }
 
 // V = L^-1 (lower; lane = column), V row-major with stride ldv; L's columns
-// in Lsh (loaded as in warp_trsm32)
+// in Lsh (loaded as in warp_trsm32, following the producer when flag is given)
 template <typename T>
-__device__ void warp_trtri32(const T *Lsh, T *V, int ldv, int lane)
+__device__ void warp_trtri32(const T *Lsh, T *V, int ldv, int lane, const int *flag = nullptr, int *fail = nullptr)
 {
 	T y[32];   // at step t: y[q] = V[t + q][lane]
 #pragma unroll
 	for (int i = 0; i < 32; i++) y[i] = (i == lane) ? T(1) : T(0);
 	T c[32], d[32];
+	flag_wait(flag, 1, fail);
 	lsh_column<T>(Lsh, 0, c);
 #pragma unroll 1
 	for (int t = 0; t < 32; t += 2) {
+		flag_wait(flag, t+2, fail);
 		lsh_column<T>(Lsh, t+1, d);
 		T yt = y[0]*c[0];
 		V[t*ldv+lane] = yt;
 #pragma unroll
 		for (int q = 1; q < 32; q++) y[q-1] = y[q]-c[q]*yt;
+		flag_wait(flag, min(t+3, 32), fail);
 		lsh_column<T>(Lsh, (t+2) & 31, c);
 		yt = y[0]*d[0];
 		V[(t+1)*ldv+lane] = yt;
@@ -510,7 +552,7 @@ __device__ void cta_gemm32(T (&c8)[8], const T *A, int lda, const T *B, int ldb_
 }
 
 // Factor and invert the NB x NB diagonal block at (p0, p0) of a front (width
-// w, identity-padded past it), with the calling CTA (>= 128 threads).  L_kk
+// w, identity-padded past it), with the calling CTA (256 threads).  L_kk
 // goes back into the front, Linv_kk^T (row-major NB x NB) to vt.  Ls, Vs:
 // NB x (NB + 1), Ts: 32 x 33 and Lsh: 2 x 32 x 32 (16-byte aligned) shared
 // arrays of the caller.
@@ -545,71 +587,80 @@ __device__ void diag_load(const T *base, int ld, int p0, int w, T *Ls, T *Vs)
 	}
 }
 
+// A11 -= L21 L21^T (the 32 x 32 lower-right quadrant of a 64 x 64 block in
+// Ls, stride LD), accumulated while warp_trsm32 still produces L21: it runs
+// behind the published columns, four at a time (128 threads: row i = tid / 4,
+// columns tid % 4 + 4 q).  The sum over t runs in increasing t, as in
+// cta_gemm32.
+template <typename T>
+__device__ void syrk32_follow(T *Ls, int LD, int tid, const int *flag, int *fail)
+{
+	int i = tid/4, c0 = tid%4;
+	T acc[8];
+#pragma unroll
+	for (int q = 0; q < 8; q++) acc[q] = T(0);
+	const T *L21 = Ls+32*LD;
+#pragma unroll 1
+	for (int t0 = 0; t0 < 32; t0 += 4) {
+		flag_wait(flag, t0+4, fail);
+#pragma unroll
+		for (int t = t0; t < t0+4; t++) {
+			T av = L21[i*LD+t];
+#pragma unroll
+			for (int q = 0; q < 8; q++) acc[q] += av*L21[(c0+4*q)*LD+t];
+		}
+	}
+#pragma unroll
+	for (int q = 0; q < 8; q++)
+		if (c0+4*q <= i) Ls[(32+i)*LD+32+c0+4*q] -= acc[q];
+}
+
+// flags: 3 ints of shared memory, zeroed by the caller before a
+// __syncthreads that precedes the call.  FP32 needs 256 threads.
 template <typename T>
 __device__ void diag_factor(T *base, int ld, int p0, int w, int gcol0, int *fail, T *Ls, T *Vs, T *Ts, T *Lsh,
-                            T *vt)
+                            T *vt, int *flags)
 {
 	constexpr int NB = Cfg<T>::NB, LD = NB+1;
 	static_assert(NB == 32 || NB == 64, "panel width");
 	int warp = threadIdx.x/32, lane = threadIdx.x%32;
-	constexpr bool unrolled = sizeof(T) == 8;
-	if (warp == 0) {
-		if constexpr (unrolled) warp_potrf32_unrolled<T>(Ls, LD, lane, w, gcol0, fail);
-		else warp_potrf32<T>(Ls, LD, Lsh, lane, w, gcol0, fail);
-	}
-	__syncthreads();
-	if (warp == 0) {                                                                   // Linv11
-		if constexpr (unrolled) warp_trtri32_unrolled<T>(Ls, LD, Vs, LD, lane);
-		else warp_trtri32<T>(Lsh, Vs, LD, lane);
-	} else if (NB == 64 && warp == 1) {                                                // L21 = A21 L11^-T
-		if constexpr (unrolled) warp_trsm32_unrolled<T>(Ls+32*LD, LD, Ls, LD, lane);
-		else warp_trsm32<T>(Ls+32*LD, LD, Lsh, lane);
-	}
-	__syncthreads();
-	if (NB == 64) {
-		bool act = threadIdx.x < 128;   // cta_gemm32 covers 32 x 32 with 128 threads
-		T c8[8], u8[8];
-		int i = threadIdx.x/4, c0 = threadIdx.x%4;
-		if (blockDim.x >= 256) {
-			// the two products side by side: L21 L21^T (on the chain to the
-			// next pivot block) by threads 0-127, T1 by threads 128-255
+	if constexpr (sizeof(T) == 4) {
+		static_assert(NB == 64, "FP32 panels are 64 wide");
+		// FP32, one pipeline over the two 32 x 32 halves.  First half: warp 0
+		// factors A00 and publishes L00's columns; warp 1 solves L21 = A21
+		// L00^-T and warp 2 inverts L00 as the columns appear; warps 3-6
+		// accumulate A11 -= L21 L21^T behind warp 1.  Second half: warp 0
+		// factors A11, warp 1 inverts L11 behind it, warps 4-7 form T1 = L21
+		// Linv00.  Then Linv21 = -Linv11 T1.
+		if (warp == 0) warp_potrf32<T>(Ls, LD, Lsh, lane, w, gcol0, fail, flags);
+		else if (warp == 1) warp_trsm32<T>(Ls+32*LD, LD, Lsh, lane, flags, fail, flags+2);
+		else if (warp == 2) warp_trtri32<T>(Lsh, Vs, LD, lane, flags, fail);
+		else if (warp < 7) syrk32_follow<T>(Ls, LD, threadIdx.x-96, flags+2, fail);
+		__syncthreads();
+		if (warp == 0) warp_potrf32<T>(Ls+32*LD+32, LD, Lsh+1024, lane, w-32, gcol0+32, fail, flags+1);
+		else if (warp == 1) warp_trtri32<T>(Lsh+1024, Vs+32*LD+32, LD, lane, flags+1, fail);
+		else if (warp >= 4) {
+			T c8[8];
 			int t2 = threadIdx.x-128;
-			if (act) {
-				cta_gemm32<T>(u8, Ls+32*LD, LD, Ls+32*LD, 1, LD, threadIdx.x);
+			cta_gemm32<T>(c8, Ls+32*LD, LD, Vs, LD, 1, t2);                    // T1 = L21 Linv00
 #pragma unroll
-				for (int q = 0; q < 8; q++)
-					if (c0+4*q <= i) Ls[(32+i)*LD+32+c0+4*q] -= u8[q];
-			} else if (t2 < 128) {
-				cta_gemm32<T>(c8, Ls+32*LD, LD, Vs, LD, 1, t2);
-#pragma unroll
-				for (int q = 0; q < 8; q++) Ts[(t2/4)*33+t2%4+4*q] = c8[q];
-			}
-		} else if (act) {
-			cta_gemm32<T>(c8, Ls+32*LD, LD, Vs, LD, 1, threadIdx.x);          // T1 = L21 Linv11
-			cta_gemm32<T>(u8, Ls+32*LD, LD, Ls+32*LD, 1, LD, threadIdx.x);     // L21 L21^T
-#pragma unroll
-			for (int q = 0; q < 8; q++) {
-				int c = c0+4*q;
-				Ts[i*33+c] = c8[q];
-				if (c <= i) Ls[(32+i)*LD+32+c] -= u8[q];
-			}
+			for (int q = 0; q < 8; q++) Ts[(t2/4)*33+t2%4+4*q] = c8[q];
 		}
 		__syncthreads();
-		if (warp == 0) {
-			if constexpr (unrolled) warp_potrf32_unrolled<T>(Ls+32*LD+32, LD, lane, w-32, gcol0+32, fail);
-			else warp_potrf32<T>(Ls+32*LD+32, LD, Lsh+1024, lane, w-32, gcol0+32, fail);
-		}
-		__syncthreads();
-		if (warp == 0) {                                                               // Linv22
-			if constexpr (unrolled) warp_trtri32_unrolled<T>(Ls+32*LD+32, LD, Vs+32*LD+32, LD, lane);
-			else warp_trtri32<T>(Lsh+1024, Vs+32*LD+32, LD, lane);
-		}
-		__syncthreads();
-		if (act) {
+		if (threadIdx.x < 128) {
+			T c8[8];
+			int i = threadIdx.x/4, c0 = threadIdx.x%4;
 			cta_gemm32<T>(c8, Vs+32*LD+32, LD, Ts, 33, 1, threadIdx.x);       // Linv22 T1
 #pragma unroll
 			for (int q = 0; q < 8; q++) Vs[(32+i)*LD+c0+4*q] = -c8[q];
 		}
+		__syncthreads();
+	} else {
+		// FP64: NB = 32, one half (fully unrolled routines)
+		(void)Ts; (void)flags;
+		if (warp == 0) warp_potrf32_unrolled<T>(Ls, LD, lane, w, gcol0, fail);
+		__syncthreads();
+		if (warp == 0) warp_trtri32_unrolled<T>(Ls, LD, Vs, LD, lane);
 		__syncthreads();
 	}
 	// batches of 8 elements per thread: shared loads first, then the stores
@@ -637,11 +688,13 @@ __device__ void diag_factor(T *base, int ld, int p0, int w, int gcol0, int *fail
 }
 
 template <typename T>
-__device__ void diag_block(T *base, int ld, int p0, int w, int gcol0, int *fail, T *Ls, T *Vs, T *Ts, T *Lsh, T *vt)
+__device__ void diag_block(T *base, int ld, int p0, int w, int gcol0, int *fail, T *Ls, T *Vs, T *Ts, T *Lsh, T *vt,
+                           int *flags)
 {
 	diag_load<T>(base, ld, p0, w, Ls, Vs);
+	if (threadIdx.x < 3) flags[threadIdx.x] = 0;
 	__syncthreads();
-	diag_factor<T>(base, ld, p0, w, gcol0, fail, Ls, Vs, Ts, Lsh, vt);
+	diag_factor<T>(base, ld, p0, w, gcol0, fail, Ls, Vs, Ts, Lsh, vt, flags);
 }
 
 // Linv slot of supernode s for panel k: two slots per supernode, by the
@@ -657,7 +710,7 @@ __device__ inline T *linv_slot(T *linv, int nsn, int s, int k)
 // diagonal block of panel 0 of every front of a level (later panels' blocks
 // are factored by the update launch of the previous panel)
 template <typename T>
-__global__ void __launch_bounds__(128) k_diag(const int4 *__restrict__ tasks, const int *__restrict__ sn_first,
+__global__ void __launch_bounds__(256) k_diag(const int4 *__restrict__ tasks, const int *__restrict__ sn_first,
                                               const int *__restrict__ sn_ld, const int64_t *__restrict__ sn_off,
                                               T *__restrict__ arena, T *__restrict__ linv, int nsn, int *fail, int dof)
 {
@@ -666,11 +719,12 @@ __global__ void __launch_bounds__(128) k_diag(const int4 *__restrict__ tasks, co
 	__shared__ T Vs[NB*LD];
 	__shared__ T Ts[32*33];
 	__shared__ __align__(16) T Lsh[2*32*32];
+	__shared__ int flags[3];
 	int4 tk = tasks[blockIdx.x];
 	int s = tk.x, p0 = tk.y, k = tk.z, w = tk.w;
 	pdl_wait();
 	diag_block<T>(arena+sn_off[s], sn_ld[s], p0, w, dof*sn_first[s]+p0, fail, Ls, Vs, Ts, Lsh,
-	              linv_slot<T>(linv, nsn, s, k));
+	              linv_slot<T>(linv, nsn, s, k), flags);
 }
 
 // ---------------------------------------------------------------------------
@@ -852,6 +906,7 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 	T *Ls = Lsh+2*32*32;
 	T *Vs = Ls+NB*LD;
 	T *Ts = Vs+NB*LD;
+	int *flags = reinterpret_cast<int *>(Ts+32*33);
 	const int w1 = min(NB, n6-t0);   // width of panel k + 1
 	// With NB == TL the diagonal tile is panel k + 1's diagonal block: its
 	// entries in the block's rows go to Ls directly (diag_factor writes them
@@ -884,8 +939,10 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 	if (diag) {
 		__syncthreads();   // this CTA's updates of the block are visible to all its threads
 		if (!handoff) diag_load<T>(base, ld, t0, w1, Ls, Vs);
+		if (threadIdx.x < 3) flags[threadIdx.x] = 0;
 		__syncthreads();
-		diag_factor<T>(base, ld, t0, w1, dof*sn_first[s]+t0, fail, Ls, Vs, Ts, Lsh, linv_slot<T>(linv, nsn, s, k+1));
+		diag_factor<T>(base, ld, t0, w1, dof*sn_first[s]+t0, fail, Ls, Vs, Ts, Lsh, linv_slot<T>(linv, nsn, s, k+1),
+		               flags);
 	}
 }
 
@@ -1214,9 +1271,9 @@ __global__ void __launch_bounds__(umma::THREADS, 1) k_syrk_tc(const int4 *__rest
 
 template <typename T> static size_t update_smem()
 {
-	// the tile's two panels, or diag_factor's Lsh, Ls, Vs and Ts
+	// the tile's two panels, or diag_factor's Lsh, Ls, Vs, Ts and flags
 	constexpr int NB = Cfg<T>::NB;
-	return sizeof(T)*std::max(2*NB*Cfg<T>::TILE, 2*32*32+2*NB*(NB+1)+32*33);
+	return std::max(sizeof(T)*2*NB*Cfg<T>::TILE, sizeof(T)*(2*32*32+2*NB*(NB+1)+32*33)+4*sizeof(int));
 }
 
 // assembly: one column of the largest front
@@ -1340,7 +1397,7 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 			break;
 		}
 		case PLAN_DIAG:
-			launch_pdl(k_diag<T>, L.count, 128, 0, st, (const int4 *)D.diag_tasks+L.off, (const int *)D.sn_first,
+			launch_pdl(k_diag<T>, L.count, 256, 0, st, (const int4 *)D.diag_tasks+L.off, (const int *)D.sn_first,
 			           (const int *)D.sn_ld, (const int64_t *)D.sn_off, F.arena, F.linv, D.nsn, F.status, D.dof);
 			break;
 		case PLAN_PANEL:
