@@ -437,7 +437,8 @@ __device__ void warp_trsm32(T *X, int ldx, const T *Lsh, int lane, const int *fl
 // V = L^-1 (lower; lane = column), V row-major with stride ldv; L's columns
 // in Lsh (loaded as in warp_trsm32, following the producer when flag is given)
 template <typename T>
-__device__ void warp_trtri32(const T *Lsh, T *V, int ldv, int lane, const int *flag = nullptr, int *fail = nullptr)
+__device__ void warp_trtri32(const T *Lsh, T *V, int ldv, int lane, const int *flag = nullptr, int *fail = nullptr,
+                             int *pub = nullptr)
 {
 	T y[32];   // at step t: y[q] = V[t + q][lane]
 #pragma unroll
@@ -457,6 +458,10 @@ __device__ void warp_trtri32(const T *Lsh, T *V, int ldv, int lane, const int *f
 		lsh_column<T>(Lsh, (t+2) & 31, c);
 		yt = y[0]*d[0];
 		V[(t+1)*ldv+lane] = yt;
+		if (pub) {   // rows t and t + 1 of V are complete
+			__syncwarp();
+			if (lane == 0) flag_publish(pub, t+2);
+		}
 #pragma unroll
 		for (int q = 1; q < 32; q++) y[q-1] = y[q]-d[q]*yt;
 	}
@@ -587,6 +592,38 @@ __device__ void diag_load(const T *base, int ld, int p0, int w, T *Ls, T *Vs)
 	}
 }
 
+// Stores of the factored block for rows [ilo, ihi) and columns [jlo, jhi):
+// L's lower part (rows below w excluded) back into the front, Linv^T to vt
+// (vt[j NB + i] = Linv[i][j]); batches of 8 per thread, shared loads first.
+template <typename T>
+__device__ void diag_store(T *base, int ld, int p0, int w, const T *Ls, const T *Vs, T *vt, int ilo, int ihi,
+                           int jlo, int jhi, bool store_l, bool store_v, int tid, int nthr)
+{
+	constexpr int NB = Cfg<T>::NB, LD = NB+1;
+	const int ni = ihi-ilo, cnt = ni*(jhi-jlo);
+	for (int e0 = tid; e0 < cnt; e0 += 8*nthr) {
+		T lv[8], vv[8];
+#pragma unroll
+		for (int u = 0; u < 8; u++) {
+			int e = e0+u*nthr;
+			if (e < cnt) {
+				int i = ilo+e%ni, j = jlo+e/ni;
+				lv[u] = Ls[i*LD+j];
+				vv[u] = Vs[i*LD+j];
+			}
+		}
+#pragma unroll
+		for (int u = 0; u < 8; u++) {
+			int e = e0+u*nthr;
+			if (e < cnt) {
+				int i = ilo+e%ni, j = jlo+e/ni;
+				if (store_l && j <= i && i < w) base[(int64_t)(p0+j)*ld+p0+i] = lv[u];
+				if (store_v) vt[j*NB+i] = vv[u];
+			}
+		}
+	}
+}
+
 // A11 -= L21 L21^T (the 32 x 32 lower-right quadrant of a 64 x 64 block in
 // Ls, stride LD), accumulated while warp_trsm32 still produces L21: it runs
 // behind the published columns, four at a time (128 threads: row i = tid / 4,
@@ -615,7 +652,7 @@ __device__ void syrk32_follow(T *Ls, int LD, int tid, const int *flag, int *fail
 		if (c0+4*q <= i) Ls[(32+i)*LD+32+c0+4*q] -= acc[q];
 }
 
-// flags: 3 ints of shared memory, zeroed by the caller before a
+// flags: 4 ints of shared memory, zeroed by the caller before a
 // __syncthreads that precedes the call.  FP32 needs 256 threads.
 template <typename T>
 __device__ void diag_factor(T *base, int ld, int p0, int w, int gcol0, int *fail, T *Ls, T *Vs, T *Ts, T *Lsh,
@@ -630,31 +667,38 @@ __device__ void diag_factor(T *base, int ld, int p0, int w, int gcol0, int *fail
 		// factors A00 and publishes L00's columns; warp 1 solves L21 = A21
 		// L00^-T and warp 2 inverts L00 as the columns appear; warps 3-6
 		// accumulate A11 -= L21 L21^T behind warp 1.  Second half: warp 0
-		// factors A11, warp 1 inverts L11 behind it, warps 4-7 form T1 = L21
-		// Linv00.  Then Linv21 = -Linv11 T1.
+		// factors A11, warp 1 inverts L11 behind it and publishes its rows,
+		// warps 2-3 store what is final, warps 4-7 form T1 = L21 Linv00 and
+		// then Linv21 = -Linv11 T1 row by row behind warp 1.
 		if (warp == 0) warp_potrf32<T>(Ls, LD, Lsh, lane, w, gcol0, fail, flags);
 		else if (warp == 1) warp_trsm32<T>(Ls+32*LD, LD, Lsh, lane, flags, fail, flags+2);
 		else if (warp == 2) warp_trtri32<T>(Lsh, Vs, LD, lane, flags, fail);
 		else if (warp < 7) syrk32_follow<T>(Ls, LD, threadIdx.x-96, flags+2, fail);
 		__syncthreads();
 		if (warp == 0) warp_potrf32<T>(Ls+32*LD+32, LD, Lsh+1024, lane, w-32, gcol0+32, fail, flags+1);
-		else if (warp == 1) warp_trtri32<T>(Lsh+1024, Vs+32*LD+32, LD, lane, flags+1, fail);
-		else if (warp >= 4) {
+		else if (warp == 1) warp_trtri32<T>(Lsh+1024, Vs+32*LD+32, LD, lane, flags+1, fail, flags+3);
+		else if (warp < 4) {
+			// what is final already: L00, L21, Linv00 and the zero upper-right of Linv^T
+			diag_store<T>(base, ld, p0, w, Ls, Vs, vt, 0, 32, 0, 32, true, true, threadIdx.x-64, 64);
+			diag_store<T>(base, ld, p0, w, Ls, Vs, vt, 32, 64, 0, 32, true, false, threadIdx.x-64, 64);
+			diag_store<T>(base, ld, p0, w, Ls, Vs, vt, 0, 32, 32, 64, false, true, threadIdx.x-64, 64);
+		} else {
 			T c8[8];
-			int t2 = threadIdx.x-128;
+			int t2 = threadIdx.x-128, i = t2/4, c0 = t2%4;
 			cta_gemm32<T>(c8, Ls+32*LD, LD, Vs, LD, 1, t2);                    // T1 = L21 Linv00
 #pragma unroll
-			for (int q = 0; q < 8; q++) Ts[(t2/4)*33+t2%4+4*q] = c8[q];
-		}
-		__syncthreads();
-		if (threadIdx.x < 128) {
-			T c8[8];
-			int i = threadIdx.x/4, c0 = threadIdx.x%4;
-			cta_gemm32<T>(c8, Vs+32*LD+32, LD, Ts, 33, 1, threadIdx.x);       // Linv22 T1
+			for (int q = 0; q < 8; q++) Ts[i*33+c0+4*q] = c8[q];
+			asm volatile("bar.sync 1, 128;" ::: "memory");                     // T1 complete (warps 4-7)
+			// Linv21 = -Linv11 T1, row i once row i of Linv11 is published
+			flag_wait(flags+3, i+1, fail);
+			cta_gemm32<T>(c8, Vs+32*LD+32, LD, Ts, 33, 1, t2);
 #pragma unroll
 			for (int q = 0; q < 8; q++) Vs[(32+i)*LD+c0+4*q] = -c8[q];
 		}
 		__syncthreads();
+		diag_store<T>(base, ld, p0, w, Ls, Vs, vt, 32, 64, 0, 32, false, true, threadIdx.x, blockDim.x);
+		diag_store<T>(base, ld, p0, w, Ls, Vs, vt, 32, 64, 32, 64, true, true, threadIdx.x, blockDim.x);
+		return;
 	} else {
 		// FP64: NB = 32, one half (fully unrolled routines)
 		(void)Ts; (void)flags;
@@ -663,28 +707,7 @@ __device__ void diag_factor(T *base, int ld, int p0, int w, int gcol0, int *fail
 		if (warp == 0) warp_trtri32_unrolled<T>(Ls, LD, Vs, LD, lane);
 		__syncthreads();
 	}
-	// batches of 8 elements per thread: shared loads first, then the stores
-	for (int e0 = threadIdx.x; e0 < NB*NB; e0 += 8*blockDim.x) {
-		T lv[8], vv[8];
-#pragma unroll
-		for (int u = 0; u < 8; u++) {
-			int e = e0+u*blockDim.x;
-			if (e < NB*NB) {
-				int i = e%NB, j = e/NB;
-				lv[u] = Ls[i*LD+j];
-				vv[u] = Vs[i*LD+j];
-			}
-		}
-#pragma unroll
-		for (int u = 0; u < 8; u++) {
-			int e = e0+u*blockDim.x;
-			if (e < NB*NB) {
-				int i = e%NB, j = e/NB;
-				if (j <= i && i < w) base[(int64_t)(p0+j)*ld+p0+i] = lv[u];
-				vt[j*NB+i] = vv[u];   // Linv^T[t = j][col = i]
-			}
-		}
-	}
+	diag_store<T>(base, ld, p0, w, Ls, Vs, vt, 0, NB, 0, NB, true, true, threadIdx.x, blockDim.x);
 }
 
 template <typename T>
@@ -692,7 +715,7 @@ __device__ void diag_block(T *base, int ld, int p0, int w, int gcol0, int *fail,
                            int *flags)
 {
 	diag_load<T>(base, ld, p0, w, Ls, Vs);
-	if (threadIdx.x < 3) flags[threadIdx.x] = 0;
+	if (threadIdx.x < 4) flags[threadIdx.x] = 0;
 	__syncthreads();
 	diag_factor<T>(base, ld, p0, w, gcol0, fail, Ls, Vs, Ts, Lsh, vt, flags);
 }
@@ -719,7 +742,7 @@ __global__ void __launch_bounds__(256) k_diag(const int4 *__restrict__ tasks, co
 	__shared__ T Vs[NB*LD];
 	__shared__ T Ts[32*33];
 	__shared__ __align__(16) T Lsh[2*32*32];
-	__shared__ int flags[3];
+	__shared__ int flags[4];
 	int4 tk = tasks[blockIdx.x];
 	int s = tk.x, p0 = tk.y, k = tk.z, w = tk.w;
 	pdl_wait();
@@ -876,11 +899,14 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 			av[u] = (t < w && ra < rlim) ? base[(int64_t)(p0+t)*ld+ra] : T(0);
 			bv[u] = (t < w && rb < clim) ? base[(int64_t)(p0+t)*ld+rb] : T(0);
 		}
+		// row i = x + TD a of the tile (thread x's a-th row) goes to position
+		// TPT x + a, so a thread's TPT values of one t are one vector load
 #pragma unroll
 		for (int u = 0; u < PU; u++) {
 			int e = threadIdx.x+256*u;
-			As[e/TL][e%TL] = av[u];
-			Bs[e/TL][e%TL] = bv[u];
+			int i = e%TL, pi = TPT*(i%TD)+i/TD;
+			As[e/TL][pi] = av[u];
+			Bs[e/TL][pi] = bv[u];
 		}
 	}
 	__syncthreads();
@@ -891,10 +917,8 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 		for (int b = 0; b < TPT; b++) acc[a][b] = 0;
 	for (int t = 0; t < w; t++) {
 		T av[TPT], bv[TPT];
-#pragma unroll
-		for (int a = 0; a < TPT; a++) av[a] = As[t][tx+TD*a];
-#pragma unroll
-		for (int b = 0; b < TPT; b++) bv[b] = Bs[t][ty+TD*b];
+		lds_chunk<T, TPT>(&As[t][TPT*tx], av);
+		lds_chunk<T, TPT>(&Bs[t][TPT*ty], bv);
 #pragma unroll
 		for (int a = 0; a < TPT; a++)
 #pragma unroll
@@ -939,7 +963,7 @@ __global__ void __launch_bounds__(256, 2) k_update(const int4 *__restrict__ task
 	if (diag) {
 		__syncthreads();   // this CTA's updates of the block are visible to all its threads
 		if (!handoff) diag_load<T>(base, ld, t0, w1, Ls, Vs);
-		if (threadIdx.x < 3) flags[threadIdx.x] = 0;
+		if (threadIdx.x < 4) flags[threadIdx.x] = 0;
 		__syncthreads();
 		diag_factor<T>(base, ld, t0, w1, dof*sn_first[s]+t0, fail, Ls, Vs, Ts, Lsh, linv_slot<T>(linv, nsn, s, k+1),
 		               flags);
