@@ -1071,7 +1071,9 @@ __global__ void __launch_bounds__(256) k_syrk(const int4 *__restrict__ tasks, co
 // in *fail.
 // ---------------------------------------------------------------------------
 namespace umma {
-constexpr int M = 128, N = 128, KC = 32, STAGES = 3, THREADS = 256;
+constexpr int M = 128, N = 128, KC = 32, STAGES = 3;
+constexpr int PRODUCERS = 256;          // warps 0-7: staging and epilogue
+constexpr int THREADS = PRODUCERS+32;    // + warp 8: MMA issue
 constexpr int TILE_BYTES = M*KC*4;           // one operand part (16 KB)
 constexpr int STAGE_BYTES = 4*TILE_BYTES;    // A hi, A lo, B hi, B lo
 constexpr int SMEM_BYTES = STAGES*STAGE_BYTES+1024;
@@ -1113,69 +1115,100 @@ __device__ inline void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t 
 	             "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n"
 	             :: "r"(tmem), "l"(a), "l"(b), "r"(IDESC), "r"(accumulate));
 }
+
+__device__ inline void mbar_init(uint64_t *b, int count)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(saddr(b)), "r"(count));
+}
+__device__ inline void mbar_arrive(uint64_t *b)
+{
+	asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" :: "r"(saddr(b)) : "memory");
+}
+__device__ inline void mma_commit(uint64_t *b)
+{
+	asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+	             :: "r"(saddr(b)) : "memory");
+}
 } // namespace umma
+
+// Barriers of a tensor-core tile: per ring stage "full" (the producers'
+// stores are in) and "empty" (the stage's MMAs are complete), and "done" (all
+// MMAs complete).
+struct TcBars { uint64_t full[umma::STAGES], empty[umma::STAGES], done; };
 
 // One 128 x 128 tile C -= A B^T on the tensor cores, for the calling CTA
 // (umma::THREADS threads): rows r0 + [0, 128) of A and c0 + [0, 128) of B
 // taken from the front's columns [k0, k1) (A and B are rows of the same
 // column-major front), C[r][c] at base[c ld + r] for r < rlim, c < clim and,
-// when lower_only, r >= c.  tmem: this CTA's 128 accumulator columns; mbar:
-// its STAGES mbarriers (fresh: phase 0).  Returns false if a wait timed out.
+// when lower_only, r >= c.  tmem: this CTA's 128 accumulator columns; bars:
+// fresh (phase 0).  Returns false if a wait timed out.
+//
+// Warp-specialised: warps 0-7 load the K chunks (two chunks ahead, in
+// registers), split them into TF32 hi / lo parts in the swizzled ring stage
+// and arrive on its full barrier; warp 8 waits on that, issues the stage's
+// MMAs and commits them to the stage's empty barrier, which the producers
+// wait on before they reuse the stage.  No CTA-wide barrier in the K loop.
+// Then warps 0-7 run the epilogue (old values first, TMEM, stores).
 __device__ bool tc_tile_update(float *base, int ld, int r0, int c0, int k0, int k1, int rlim, int clim,
-                               bool lower_only, unsigned char *sm, uint64_t *mbar, uint32_t tmem)
+                               bool lower_only, unsigned char *sm, TcBars &bars, uint32_t tmem)
 {
 	using namespace umma;
 	const int tid = threadIdx.x, warp = tid/32, lane = tid%32;
-	int nchunk = (k1-k0+KC-1)/KC;
-	uint32_t phase_bits = 0;   // bit q: parity expected at the next wait on stage q
+	const int nchunk = (k1-k0+KC-1)/KC;
 	bool ok = true;
-	int issued = 0;
-	// staging role: row m of both operands, K half h of the chunk.  The global
-	// loads of chunk ch + 2 are issued right after chunk ch is staged, so two
-	// chunks of loads are in flight while the MMAs of earlier chunks run.
-	const int m = tid & (M-1), h = tid >> 7;
-	const int ra = r0+m, rb = c0+m;
-	const bool va = ra < rlim, vb = rb < clim;
-	auto load = [&](int ch, float (&av)[16], float (&bv)[16]) {
-		int tb = k0+ch*KC+16*h;
+	if (warp < PRODUCERS/32) {
+		// row m of both operands, K half h of each chunk
+		const int m = tid & (M-1), h = tid >> 7;
+		const int ra = r0+m, rb = c0+m;
+		const bool va = ra < rlim, vb = rb < clim;
+		auto load = [&](int ch, float (&a)[16], float (&b)[16]) {
+			int tb = k0+ch*KC+16*h;
+			const float *pa = base+(int64_t)tb*ld+ra, *pb = base+(int64_t)tb*ld+rb;
+			int nk = ch < nchunk ? min(16, k1-tb) : 0;
 #pragma unroll
-		for (int k = 0; k < 16; k++) {
-			int t = tb+k;
-			av[k] = (ch < nchunk && t < k1 && va) ? base[(int64_t)t*ld+ra] : 0.f;
-			bv[k] = (ch < nchunk && t < k1 && vb) ? base[(int64_t)t*ld+rb] : 0.f;
-		}
-	};
-	// stage chunk ch (registers av, bv) into ring slot ch % STAGES and issue
-	// its MMAs; false once a wait has timed out
-	auto step = [&](int ch, float (&av)[16], float (&bv)[16]) -> bool {
-		int b = ch % STAGES;
-		if (ch >= STAGES) {
-			if (!mbar_wait(saddr(&mbar[b]), (phase_bits >> b) & 1u)) ok = false;
-			phase_bits ^= 1u << b;
-		}
-		if (!__syncthreads_and(ok)) { ok = false; return false; }
-		unsigned char *stg = sm+b*STAGE_BYTES;
+			for (int k = 0; k < 16; k++) {
+				a[k] = (k < nk && va) ? *pa : 0.f;
+				b[k] = (k < nk && vb) ? *pb : 0.f;
+				pa += ld;
+				pb += ld;
+			}
+		};
 		// 16-byte chunks (4 consecutive K): the 8 lanes of a quarter warp
 		// (consecutive m) land on 8 distinct rows and swizzled chunk columns,
 		// i.e. on all 32 banks
+		auto stage = [&](int ch, float (&av)[16], float (&bv)[16]) {
+			int b = ch % STAGES;
+			if (ch >= STAGES && !mbar_wait(saddr(&bars.empty[b]), ((ch/STAGES)-1) & 1)) ok = false;
+			unsigned char *stg = sm+b*STAGE_BYTES;
 #pragma unroll
-		for (int c4 = 0; c4 < 4; c4++) {
-			int ck = 4*h+c4;
-			uint32_t off = (uint32_t)((m >> 3)*1024+(m & 7)*128+((ck ^ (m & 7)) << 4));
-			const float *a = av+4*c4, *bq = bv+4*c4;
-			*reinterpret_cast<float4 *>(stg+0*TILE_BYTES+off) = make_float4(a[0], a[1], a[2], a[3]);
-			*reinterpret_cast<float4 *>(stg+1*TILE_BYTES+off) =
-				make_float4(tf32_lo(a[0]), tf32_lo(a[1]), tf32_lo(a[2]), tf32_lo(a[3]));
-			*reinterpret_cast<float4 *>(stg+2*TILE_BYTES+off) = make_float4(bq[0], bq[1], bq[2], bq[3]);
-			*reinterpret_cast<float4 *>(stg+3*TILE_BYTES+off) =
-				make_float4(tf32_lo(bq[0]), tf32_lo(bq[1]), tf32_lo(bq[2]), tf32_lo(bq[3]));
+			for (int c4 = 0; c4 < 4; c4++) {
+				int ck = 4*h+c4;
+				uint32_t off = (uint32_t)((m >> 3)*1024+(m & 7)*128+((ck ^ (m & 7)) << 4));
+				const float *a = av+4*c4, *bq = bv+4*c4;
+				*reinterpret_cast<float4 *>(stg+0*TILE_BYTES+off) = make_float4(a[0], a[1], a[2], a[3]);
+				*reinterpret_cast<float4 *>(stg+1*TILE_BYTES+off) =
+					make_float4(tf32_lo(a[0]), tf32_lo(a[1]), tf32_lo(a[2]), tf32_lo(a[3]));
+				*reinterpret_cast<float4 *>(stg+2*TILE_BYTES+off) = make_float4(bq[0], bq[1], bq[2], bq[3]);
+				*reinterpret_cast<float4 *>(stg+3*TILE_BYTES+off) =
+					make_float4(tf32_lo(bq[0]), tf32_lo(bq[1]), tf32_lo(bq[2]), tf32_lo(bq[3]));
+			}
+			asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // visible to the tensor cores
+			mbar_arrive(&bars.full[b]);
+			load(ch+2, av, bv);
+		};
+		float a0[16], b0[16], a1[16], b1[16];
+		load(0, a0, b0);
+		load(1, a1, b1);
+		for (int ch = 0; ch < nchunk; ch += 2) {
+			stage(ch, a0, b0);
+			if (ch+1 < nchunk) stage(ch+1, a1, b1);
 		}
-		load(ch+2, av, bv);
-		asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-		__syncthreads();
-		if (tid == 0) {
+	} else if (lane == 0) {
+		for (int ch = 0; ch < nchunk; ch++) {
+			int b = ch % STAGES;
+			if (!mbar_wait(saddr(&bars.full[b]), (ch/STAGES) & 1)) { ok = false; break; }
 			asm volatile("tcgen05.fence::after_thread_sync;");
-			uint32_t sa = saddr(stg);
+			uint32_t sa = saddr(sm+b*STAGE_BYTES);
 #pragma unroll
 			for (int kk = 0; kk < KC/8; kk++) {
 				uint64_t ahi = sdesc(sa+0*TILE_BYTES+32*kk), alo = sdesc(sa+1*TILE_BYTES+32*kk);
@@ -1184,37 +1217,28 @@ __device__ bool tc_tile_update(float *base, int ld, int r0, int c0, int k0, int 
 				mma_tf32(tmem, ahi, blo, 1u);
 				mma_tf32(tmem, alo, bhi, 1u);
 			}
-			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-			             :: "r"(saddr(&mbar[b])) : "memory");
+			mma_commit(&bars.empty[b]);
 		}
-		issued = ch+1;
-		return true;
-	};
-	float a0[16], b0[16], a1[16], b1[16];
-	load(0, a0, b0);
-	load(1, a1, b1);
-	for (int ch = 0; ch < nchunk; ch += 2) {
-		if (!step(ch, a0, b0)) break;
-		if (ch+1 < nchunk && !step(ch+1, a1, b1)) break;
+		mma_commit(&bars.done);   // every MMA issued above is complete
 	}
-	// every issued MMA is complete once the last commit has arrived
-	if (issued > 0) {
-		int b = (issued-1) % STAGES;
-		if (!mbar_wait(saddr(&mbar[b]), (phase_bits >> b) & 1u)) ok = false;
+	if (warp < PRODUCERS/32) {
+		if (!mbar_wait(saddr(&bars.done), 0)) ok = false;
+		asm volatile("tcgen05.fence::after_thread_sync;");
 	}
-	asm volatile("tcgen05.fence::after_thread_sync;");
 	ok = __syncthreads_and(ok);
-	if (ok && issued == nchunk && nchunk > 0) {
+	if (ok && nchunk > 0 && warp < PRODUCERS/32) {
 		// warp w reads TMEM lanes 32 (w % 4) .. +32 (rows) and columns 64 (w / 4) .. +64
 		int q = warp & 3, half = warp >> 2;
 		int r = r0+32*q+lane;
 		// the thread's 64 old values, loaded before any store (the stores
 		// would otherwise serialise the loads: the addresses may alias)
 		float old[64];
+		const float *po = base+(int64_t)(c0+64*half)*ld+r;
 #pragma unroll
 		for (int j = 0; j < 64; j++) {
 			int c = c0+64*half+j;
-			old[j] = (r < rlim && c < clim && (!lower_only || r >= c)) ? base[(int64_t)c*ld+r] : 0.f;
+			old[j] = (r < rlim && c < clim && (!lower_only || r >= c)) ? *po : 0.f;
+			po += ld;
 		}
 #pragma unroll
 		for (int cb = 64*half; cb < 64*half+64; cb += 16) {
@@ -1240,8 +1264,8 @@ __device__ bool tc_tile_update(float *base, int ld, int r0, int c0, int k0, int 
 	return ok;
 }
 
-// tensor memory (128 columns) and the stage mbarriers of a tensor-core CTA
-__device__ inline uint32_t tc_setup(uint32_t *tmem_slot, uint64_t *mbar)
+// tensor memory (128 columns) and the barriers of a tensor-core CTA
+__device__ inline uint32_t tc_setup(uint32_t *tmem_slot, TcBars &bars)
 {
 	using namespace umma;
 	if (threadIdx.x/32 == 0) {
@@ -1251,7 +1275,11 @@ __device__ inline uint32_t tc_setup(uint32_t *tmem_slot, uint64_t *mbar)
 		asm volatile("tcgen05.fence::before_thread_sync;");
 	}
 	if (threadIdx.x == 0) {
-		for (int q = 0; q < STAGES; q++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(&mbar[q])));
+		for (int q = 0; q < STAGES; q++) {
+			mbar_init(&bars.full[q], PRODUCERS);
+			mbar_init(&bars.empty[q], 1);
+		}
+		mbar_init(&bars.done, 1);
 		asm volatile("fence.mbarrier_init.release.cluster;");
 	}
 	__syncthreads();
@@ -1274,7 +1302,7 @@ __global__ void __launch_bounds__(umma::THREADS, 1) k_syrk_tc(const int4 *__rest
                                                               float *__restrict__ arena, int *fail, int dof)
 {
 	extern __shared__ unsigned char smem_tc[];
-	__shared__ __align__(8) uint64_t mbar[umma::STAGES];
+	__shared__ __align__(8) TcBars bars;
 	__shared__ uint32_t tmem_slot;
 	unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_tc)+1023) &
 	                                                      ~static_cast<uintptr_t>(1023));
@@ -1282,8 +1310,8 @@ __global__ void __launch_bounds__(umma::THREADS, 1) k_syrk_tc(const int4 *__rest
 	int s = tk.x, r0 = tk.y, c0 = tk.z;
 	int n6 = dof*sn_n[s], F6 = n6+dof*sn_m[s], ld = sn_ld[s];
 	pdl_wait();   // before the tensor-memory allocation, too
-	uint32_t tmem = tc_setup(&tmem_slot, mbar);
-	bool ok = tc_tile_update(arena+sn_off[s], ld, r0, c0, 0, n6, F6, F6, true, sm, mbar, tmem);
+	uint32_t tmem = tc_setup(&tmem_slot, bars);
+	bool ok = tc_tile_update(arena+sn_off[s], ld, r0, c0, 0, n6, F6, F6, true, sm, bars, tmem);
 	tc_teardown(tmem);
 	if (!ok && threadIdx.x == 0 && fail) atomicMin(fail, 0);
 }
