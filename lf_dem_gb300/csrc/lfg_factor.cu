@@ -1071,12 +1071,19 @@ __global__ void __launch_bounds__(256) k_syrk(const int4 *__restrict__ tasks, co
 // in *fail.
 // ---------------------------------------------------------------------------
 namespace umma {
-constexpr int M = 128, N = 128, KC = 32, STAGES = 3;
-constexpr int PRODUCERS = 256;          // warps 0-7: staging and epilogue
-constexpr int THREADS = PRODUCERS+32;    // + warp 8: MMA issue
+constexpr int M = 128, N = 128, KC = 32, STAGES = 4;
+constexpr int GROUP = 256;                // threads of a producer group (8 warps)
+constexpr int GROUPS = 2;                 // group g stages the chunks ch = g (mod GROUPS)
+constexpr int PRODUCERS = GROUPS*GROUP;   // warps 0-15: staging and epilogue
+constexpr int THREADS = PRODUCERS+32;     // + warp 16: MMA issue
 constexpr int TILE_BYTES = M*KC*4;           // one operand part (16 KB)
-constexpr int STAGE_BYTES = 4*TILE_BYTES;    // A hi, A lo, B hi, B lo
+constexpr int STAGE_BYTES = 2*TILE_BYTES;    // B hi, B lo (A's parts are in tensor memory)
 constexpr int SMEM_BYTES = STAGES*STAGE_BYTES+1024;
+// tensor memory: the accumulator in columns [0, N), stage b's A hi / lo in
+// columns ACOL + 2 KC b + [0, KC) / + KC + [0, KC)
+constexpr int ACOL = N;
+constexpr int TMEM_COLS = 512;
+static_assert(ACOL+STAGES*2*KC <= TMEM_COLS, "tensor memory columns");
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
 
 __device__ inline uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -1108,12 +1115,22 @@ __device__ inline bool mbar_wait(uint32_t bar, uint32_t parity)
 	return false;
 }
 
-__device__ inline void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate)
+// D (tensor memory) += A (tensor memory, lane = row, one column per K
+// element) B^T (shared memory descriptor)
+__device__ inline void mma_tf32(uint32_t dt, uint32_t at, uint64_t b, uint32_t accumulate)
 {
 	asm volatile("{\n\t.reg .pred p;\n\t"
 	             "setp.ne.b32 p, %4, 0;\n\t"
-	             "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n"
-	             :: "r"(tmem), "l"(a), "l"(b), "r"(IDESC), "r"(accumulate));
+	             "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}\n"
+	             :: "r"(dt), "r"(at), "l"(b), "r"(IDESC), "r"(accumulate));
+}
+__device__ inline void tmem_st16(uint32_t ta, const uint32_t (&v)[16])
+{
+	asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+	             "{%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};"
+	             :: "r"(ta), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]),
+	                "r"(v[7]), "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]),
+	                "r"(v[15]) : "memory");
 }
 
 __device__ inline void mbar_init(uint64_t *b, int count)
@@ -1140,25 +1157,30 @@ struct TcBars { uint64_t full[umma::STAGES], empty[umma::STAGES], done; };
 // (umma::THREADS threads): rows r0 + [0, 128) of A and c0 + [0, 128) of B
 // taken from the front's columns [k0, k1) (A and B are rows of the same
 // column-major front), C[r][c] at base[c ld + r] for r < rlim, c < clim and,
-// when lower_only, r >= c.  tmem: this CTA's 128 accumulator columns; bars:
-// fresh (phase 0).  Returns false if a wait timed out.
+// when lower_only, r >= c.  tmem: this CTA's tensor memory; bars: fresh
+// (phase 0).  Returns false if a wait timed out.
 //
-// Warp-specialised: warps 0-7 load the K chunks (two chunks ahead, in
-// registers), split them into TF32 hi / lo parts in the swizzled ring stage
-// and arrive on its full barrier; warp 8 waits on that, issues the stage's
-// MMAs and commits them to the stage's empty barrier, which the producers
-// wait on before they reuse the stage.  No CTA-wide barrier in the K loop.
-// Then warps 0-7 run the epilogue (old values first, TMEM, stores).
+// Warp-specialised: two producer groups of 8 warps take alternate K chunks.
+// A producer thread (row m, K half h) loads its chunk's values of A row m
+// and B row m into registers one chunk of its group ahead, writes A's TF32
+// hi / lo parts to tensor memory (tcgen05.st: a warp owns the 32 lanes =
+// rows of its quarter) and B's parts to the swizzled shared stage, then
+// arrives on the stage's full barrier.  The MMA warp waits on that, issues
+// the stage's three products per K step (A hi B hi, A hi B lo, A lo B hi)
+// and commits them to the stage's empty barrier, which the producers wait on
+// before they reuse the stage.  No CTA-wide barrier in the K loop.  Then the
+// producer warps run the epilogue (old values first, TMEM, stores).
 __device__ bool tc_tile_update(float *base, int ld, int r0, int c0, int k0, int k1, int rlim, int clim,
                                bool lower_only, unsigned char *sm, TcBars &bars, uint32_t tmem)
 {
 	using namespace umma;
 	const int tid = threadIdx.x, warp = tid/32, lane = tid%32;
 	const int nchunk = (k1-k0+KC-1)/KC;
+	constexpr int PW = PRODUCERS/32;
 	bool ok = true;
-	if (warp < PRODUCERS/32) {
-		// row m of both operands, K half h of each chunk
-		const int m = tid & (M-1), h = tid >> 7;
+	if (warp < PW) {
+		const int g = warp/(GROUP/32), gt = tid-GROUP*g;
+		const int m = gt & (M-1), h = gt >> 7, q = warp & 3;
 		const int ra = r0+m, rb = c0+m;
 		const bool va = ra < rlim, vb = rb < clim;
 		auto load = [&](int ch, float (&a)[16], float (&b)[16]) {
@@ -1173,75 +1195,80 @@ __device__ bool tc_tile_update(float *base, int ld, int r0, int c0, int k0, int 
 				pb += ld;
 			}
 		};
-		// 16-byte chunks (4 consecutive K): the 8 lanes of a quarter warp
-		// (consecutive m) land on 8 distinct rows and swizzled chunk columns,
-		// i.e. on all 32 banks
-		auto stage = [&](int ch, float (&av)[16], float (&bv)[16]) {
+		float av[16], bv[16];
+		load(g, av, bv);
+		for (int ch = g; ch < nchunk; ch += GROUPS) {
 			int b = ch % STAGES;
 			if (ch >= STAGES && !mbar_wait(saddr(&bars.empty[b]), ((ch/STAGES)-1) & 1)) ok = false;
+			// B: 16-byte chunks (4 consecutive K); the 8 lanes of a quarter
+			// warp (consecutive m) land on 8 distinct rows and swizzled chunk
+			// columns, i.e. on all 32 banks
 			unsigned char *stg = sm+b*STAGE_BYTES;
 #pragma unroll
 			for (int c4 = 0; c4 < 4; c4++) {
 				int ck = 4*h+c4;
 				uint32_t off = (uint32_t)((m >> 3)*1024+(m & 7)*128+((ck ^ (m & 7)) << 4));
-				const float *a = av+4*c4, *bq = bv+4*c4;
-				*reinterpret_cast<float4 *>(stg+0*TILE_BYTES+off) = make_float4(a[0], a[1], a[2], a[3]);
+				const float *bq = bv+4*c4;
+				*reinterpret_cast<float4 *>(stg+0*TILE_BYTES+off) = make_float4(bq[0], bq[1], bq[2], bq[3]);
 				*reinterpret_cast<float4 *>(stg+1*TILE_BYTES+off) =
-					make_float4(tf32_lo(a[0]), tf32_lo(a[1]), tf32_lo(a[2]), tf32_lo(a[3]));
-				*reinterpret_cast<float4 *>(stg+2*TILE_BYTES+off) = make_float4(bq[0], bq[1], bq[2], bq[3]);
-				*reinterpret_cast<float4 *>(stg+3*TILE_BYTES+off) =
 					make_float4(tf32_lo(bq[0]), tf32_lo(bq[1]), tf32_lo(bq[2]), tf32_lo(bq[3]));
 			}
-			asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // visible to the tensor cores
+			// A: lane = row of the warp's quarter, 16 columns = this K half
+			uint32_t hi[16], lo[16];
+#pragma unroll
+			for (int k = 0; k < 16; k++) {
+				hi[k] = __float_as_uint(av[k]);
+				lo[k] = __float_as_uint(tf32_lo(av[k]));
+			}
+			uint32_t ta = tmem+((uint32_t)(32*q) << 16)+(uint32_t)(ACOL+2*KC*b+16*h);
+			tmem_st16(ta, hi);
+			tmem_st16(ta+KC, lo);
+			asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+			asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // B visible to the tensor cores
+			asm volatile("tcgen05.fence::before_thread_sync;");
 			mbar_arrive(&bars.full[b]);
-			load(ch+2, av, bv);
-		};
-		float a0[16], b0[16], a1[16], b1[16];
-		load(0, a0, b0);
-		load(1, a1, b1);
-		for (int ch = 0; ch < nchunk; ch += 2) {
-			stage(ch, a0, b0);
-			if (ch+1 < nchunk) stage(ch+1, a1, b1);
+			load(ch+GROUPS, av, bv);
 		}
-	} else if (lane == 0) {
+	} else if (warp == PW && lane == 0) {
 		for (int ch = 0; ch < nchunk; ch++) {
 			int b = ch % STAGES;
 			if (!mbar_wait(saddr(&bars.full[b]), (ch/STAGES) & 1)) { ok = false; break; }
 			asm volatile("tcgen05.fence::after_thread_sync;");
 			uint32_t sa = saddr(sm+b*STAGE_BYTES);
+			uint32_t at = tmem+(uint32_t)(ACOL+2*KC*b);
 #pragma unroll
 			for (int kk = 0; kk < KC/8; kk++) {
-				uint64_t ahi = sdesc(sa+0*TILE_BYTES+32*kk), alo = sdesc(sa+1*TILE_BYTES+32*kk);
-				uint64_t bhi = sdesc(sa+2*TILE_BYTES+32*kk), blo = sdesc(sa+3*TILE_BYTES+32*kk);
-				mma_tf32(tmem, ahi, bhi, (ch > 0 || kk > 0) ? 1u : 0u);
-				mma_tf32(tmem, ahi, blo, 1u);
-				mma_tf32(tmem, alo, bhi, 1u);
+				uint64_t bhi = sdesc(sa+0*TILE_BYTES+32*kk), blo = sdesc(sa+1*TILE_BYTES+32*kk);
+				mma_tf32(tmem, at+8*kk, bhi, (ch > 0 || kk > 0) ? 1u : 0u);
+				mma_tf32(tmem, at+8*kk, blo, 1u);
+				mma_tf32(tmem, at+KC+8*kk, bhi, 1u);
 			}
 			mma_commit(&bars.empty[b]);
 		}
 		mma_commit(&bars.done);   // every MMA issued above is complete
 	}
-	if (warp < PRODUCERS/32) {
+	if (warp < PW) {
 		if (!mbar_wait(saddr(&bars.done), 0)) ok = false;
 		asm volatile("tcgen05.fence::after_thread_sync;");
 	}
 	ok = __syncthreads_and(ok);
-	if (ok && nchunk > 0 && warp < PRODUCERS/32) {
-		// warp w reads TMEM lanes 32 (w % 4) .. +32 (rows) and columns 64 (w / 4) .. +64
-		int q = warp & 3, half = warp >> 2;
+	if (ok && nchunk > 0 && warp < PW) {
+		// warp w reads TMEM lanes 32 (w % 4) .. +32 (rows) and CPW columns
+		constexpr int CPW = N/(PW/4);
+		int q = warp & 3, grp = warp >> 2;
 		int r = r0+32*q+lane;
-		// the thread's 64 old values, loaded before any store (the stores
+		// the thread's old values, loaded before any store (the stores
 		// would otherwise serialise the loads: the addresses may alias)
-		float old[64];
-		const float *po = base+(int64_t)(c0+64*half)*ld+r;
+		float old[CPW];
+		const float *po = base+(int64_t)(c0+CPW*grp)*ld+r;
 #pragma unroll
-		for (int j = 0; j < 64; j++) {
-			int c = c0+64*half+j;
+		for (int j = 0; j < CPW; j++) {
+			int c = c0+CPW*grp+j;
 			old[j] = (r < rlim && c < clim && (!lower_only || r >= c)) ? *po : 0.f;
 			po += ld;
 		}
 #pragma unroll
-		for (int cb = 64*half; cb < 64*half+64; cb += 16) {
+		for (int cb = CPW*grp; cb < CPW*grp+CPW; cb += 16) {
 			uint32_t v[16];
 			uint32_t ta = tmem+((uint32_t)(32*q) << 16)+(uint32_t)cb;
 			asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
@@ -1255,7 +1282,7 @@ __device__ bool tc_tile_update(float *base, int ld, int r0, int c0, int k0, int 
 			for (int j = 0; j < 16; j++) {
 				int c = c0+cb+j;
 				if (r < rlim && c < clim && (!lower_only || r >= c))
-					base[(int64_t)c*ld+r] = old[cb-64*half+j]-__uint_as_float(v[j]);
+					base[(int64_t)c*ld+r] = old[cb-CPW*grp+j]-__uint_as_float(v[j]);
 			}
 		}
 	}
@@ -1264,19 +1291,20 @@ __device__ bool tc_tile_update(float *base, int ld, int r0, int c0, int k0, int 
 	return ok;
 }
 
-// tensor memory (128 columns) and the barriers of a tensor-core CTA
+// tensor memory (all TMEM_COLS columns: one CTA per SM) and the barriers of a
+// tensor-core CTA
 __device__ inline uint32_t tc_setup(uint32_t *tmem_slot, TcBars &bars)
 {
 	using namespace umma;
 	if (threadIdx.x/32 == 0) {
 		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-		             :: "r"(saddr(tmem_slot)), "r"(N));
+		             :: "r"(saddr(tmem_slot)), "r"(TMEM_COLS));
 		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
 		asm volatile("tcgen05.fence::before_thread_sync;");
 	}
 	if (threadIdx.x == 0) {
 		for (int q = 0; q < STAGES; q++) {
-			mbar_init(&bars.full[q], PRODUCERS);
+			mbar_init(&bars.full[q], GROUP);
 			mbar_init(&bars.empty[q], 1);
 		}
 		mbar_init(&bars.done, 1);
@@ -1290,7 +1318,7 @@ __device__ inline uint32_t tc_setup(uint32_t *tmem_slot, TcBars &bars)
 __device__ inline void tc_teardown(uint32_t tmem)
 {
 	if (threadIdx.x/32 == 0)
-		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(umma::N));
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(umma::TMEM_COLS));
 }
 
 // Schur complement tile: U[r][c] -= sum_{t < 6n} L[r][t] L[c][t], lower part of [6n, 6F)^2
