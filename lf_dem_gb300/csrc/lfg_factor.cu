@@ -38,6 +38,7 @@ constexpr int PANEL_ROWS = 64;   // rows per panel (k_trsm) task (must match the
 constexpr int SOLVE_WARPS = 8;
 constexpr int SOLVE_CB = 8;      // columns per CTA of the solve's column kernels
 constexpr int SOLVE_JC = 256;    // columns per chunk of the solve's row kernels
+constexpr int SOLVE_WARP_ROWS = 256;   // column products with at most this many rows: one warp per unit
 
 template <typename T> struct Cfg;
 // NB: panel width; TILE/TPT: trailing-update tile edge / outputs per thread
@@ -1615,11 +1616,11 @@ template <typename T> struct SolveUnroll { static constexpr int U = sizeof(T) ==
 // rows) and factor entries
 template <typename T, int U, int MODE>
 __device__ __forceinline__ void cols_batch(int i0, int nrow, int f6, const int *R, const T *M, int ld, int j0, int jn,
-                                           int dof, int64_t (&g)[U], T (&e)[U][SOLVE_CB])
+                                           int dof, int64_t (&g)[U], T (&e)[U][SOLVE_CB], int stride)
 {
 #pragma unroll
 	for (int u = 0; u < U; u++) {
-		int i = i0+u*blockDim.x;
+		int i = i0+u*stride;
 		g[u] = i >= nrow ? -1 : MODE == 0 ? f6+i : dof*R[bdiv(i, dof)]+bmod(i, dof);
 #pragma unroll
 		for (int c = 0; c < SOLVE_CB; c++)
@@ -1648,7 +1649,7 @@ __device__ void unit_cols(const SolveArgs<T> &A, const int *lev, int bx, int by,
 		for (int q = 0; q < K; q++) acc[c][q] = 0;
 	int64_t g[U];
 	T e[U][SOLVE_CB];
-	cols_batch<T, U, MODE>(threadIdx.x, nrow, f6, R, M, ld, j0, jn, dof, g, e);   // before the wait
+	cols_batch<T, U, MODE>(threadIdx.x, nrow, f6, R, M, ld, j0, jn, dof, g, e, blockDim.x);   // before the wait
 	pdl_wait();
 	for (int i0 = threadIdx.x; i0 < nrow; i0 += U*blockDim.x) {
 		T v[U][K];
@@ -1668,7 +1669,7 @@ __device__ void unit_cols(const SolveArgs<T> &A, const int *lev, int bx, int by,
 			}
 		}
 		int i1 = i0+U*blockDim.x;
-		if (i1 < nrow) cols_batch<T, U, MODE>(i1, nrow, f6, R, M, ld, j0, jn, dof, g, e);
+		if (i1 < nrow) cols_batch<T, U, MODE>(i1, nrow, f6, R, M, ld, j0, jn, dof, g, e, blockDim.x);
 	}
 	int warp = threadIdx.x/32, lane = threadIdx.x%32;
 #pragma unroll
@@ -1688,6 +1689,86 @@ __device__ void unit_cols(const SolveArgs<T> &A, const int *lev, int bx, int by,
 			T *o = A.yp+(int64_t)q*A.n6tot+f6+j0+c;
 			if (MODE == 0) *o = a;
 			else *o -= a;
+		}
+	}
+}
+
+// The same column products with one warp per unit (SOLVE_CB columns of one
+// front), for levels whose products have few rows (at most SOLVE_WARP_ROWS):
+// eight units per CTA instead of one, so a level of many small fronts fits
+// in one wave.  Lanes take rows lane, lane + 32, ...; the SOLVE_CB x K
+// partial sums are combined by a butterfly reduce-scatter (lane l ends with
+// sum number l).
+template <typename T, int K, int MODE>
+__device__ void unit_cols_warp(const SolveArgs<T> &A, const int *lev, int units_x, int nfronts)
+{
+	constexpr int U = SolveUnroll<T>::U;
+	constexpr int NV = SOLVE_CB*K;                            // sums of the unit
+	constexpr int NVP = NV <= 8 ? 8 : NV <= 16 ? 16 : 32;     // padded to a power of two
+	static_assert(NV <= 32, "one sum per lane");
+	const int lane = threadIdx.x%32;
+	const int unit = blockIdx.x*(blockDim.x/32)+threadIdx.x/32;
+	const int bx = unit%units_x, by = unit/units_x;
+	if (by >= nfronts) return;
+	int s = lev[by];
+	const int dof = A.dof;
+	int n6 = dof*A.sn_n[s], m6 = dof*A.sn_m[s], ld = A.sn_ld[s];
+	int j0 = bx*SOLVE_CB;
+	if (j0 >= n6 || (MODE == 1 && m6 == 0)) return;
+	int jn = min(SOLVE_CB, n6-j0);
+	int f6 = dof*A.sn_first[s];
+	const T *M = A.arena+A.sn_off[s]+(MODE == 0 ? n6+m6 : n6)+(int64_t)j0*ld;
+	const int *R = A.rows+A.sn_rows_off[s];
+	int nrow = MODE == 0 ? j0+jn : m6;
+	T acc[NVP];
+#pragma unroll
+	for (int v = 0; v < NVP; v++) acc[v] = 0;
+	int64_t g[U];
+	T e[U][SOLVE_CB];
+	cols_batch<T, U, MODE>(lane, nrow, f6, R, M, ld, j0, jn, dof, g, e, 32);   // before the wait
+	pdl_wait();
+	for (int i0 = lane; i0 < nrow; i0 += U*32) {
+		T v[U][K];
+#pragma unroll
+		for (int u = 0; u < U; u++)
+#pragma unroll
+			for (int q = 0; q < K; q++) v[u][q] = g[u] < 0 ? T(0) : A.xp[(int64_t)q*A.n6tot+g[u]];
+#pragma unroll
+		for (int u = 0; u < U; u++) {
+			if (g[u] < 0) continue;
+			int i = i0+u*32;
+#pragma unroll
+			for (int c = 0; c < SOLVE_CB; c++) {
+				if (c >= jn || (MODE == 0 && i > j0+c)) continue;
+#pragma unroll
+				for (int q = 0; q < K; q++) acc[c*K+q] += e[u][c]*v[u][q];
+			}
+		}
+		int i1 = i0+U*32;
+		if (i1 < nrow) cols_batch<T, U, MODE>(i1, nrow, f6, R, M, ld, j0, jn, dof, g, e, 32);
+	}
+	// reduce-scatter: halving steps over the lane bits below NVP; at each step
+	// a lane keeps the half of its values whose index bit matches its lane
+	// bit; then sums over the lane bits above
+#pragma unroll
+	for (int w = NVP/2; w >= 1; w /= 2) {
+		const bool upper = (lane & w) != 0;
+#pragma unroll
+		for (int v = 0; v < w; v++) {
+			T mine = upper ? acc[v+w] : acc[v];
+			T other = upper ? acc[v] : acc[v+w];
+			acc[v] = mine+__shfl_xor_sync(0xffffffffu, other, w);
+		}
+	}
+#pragma unroll
+	for (int w = NVP; w < 32; w *= 2) acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], w);
+	// lane l holds sum l % NVP
+	if (lane < NV) {
+		int c = lane/K, q = lane%K;
+		if (c < jn) {
+			T *o = A.yp+(int64_t)q*A.n6tot+f6+j0+c;
+			if (MODE == 0) *o = acc[0];
+			else *o -= acc[0];
 		}
 	}
 }
@@ -1847,6 +1928,8 @@ __global__ void __launch_bounds__(256) k_solve_phase(SolveArgs<T> A, SolvePhase 
 	if (TYPE == SP_COLS0) unit_cols<T, K, 0>(A, lev, bx, by, sh);
 	if (TYPE == SP_ROWS0) unit_rows<T, K, 0>(A, lev, bx, by, bz, ph.nchunk, sh);
 	if (TYPE == SP_COLS1) unit_cols<T, K, 1>(A, lev, bx, by, sh);
+	if (TYPE == SP_COLS0W) unit_cols_warp<T, K, 0>(A, lev, ph.gx, ph.gy);
+	if (TYPE == SP_COLS1W) unit_cols_warp<T, K, 1>(A, lev, ph.gx, ph.gy);
 	if (TYPE == SP_ROWS1) unit_rows<T, K, 1>(A, lev, bx, by, bz, ph.nchunk, sh);
 	if (TYPE == SP_PERM_OUT) unit_permute<T, K>(A, bx, false);
 	if (TYPE == SP_PERM_IN_Y) unit_permute<T, K>(A, bx, true, true);
@@ -1868,6 +1951,12 @@ static void launch_phase(const SolveArgs<T> &A, const SolvePhase &p, cudaStream_
 	case SP_PERM_IN_Y: launch_pdl(k_solve_phase<T, K, SP_PERM_IN_Y>, g, 256, 0, st, A, p); break;
 	case SP_MUL_TOP: launch_pdl(k_solve_phase<T, K, SP_MUL_TOP>, g, 256, 0, st, A, p); break;
 	case SP_MUL_UPD: launch_pdl(k_solve_phase<T, K, SP_MUL_UPD>, g, 256, 0, st, A, p); break;
+	case SP_COLS0W: case SP_COLS1W: {
+		dim3 gw((p.gx*p.gy+7)/8, 1, 1);   // eight warp units per CTA
+		if (p.type == SP_COLS0W) launch_pdl(k_solve_phase<T, K, SP_COLS0W>, gw, 256, 0, st, A, p);
+		else launch_pdl(k_solve_phase<T, K, SP_COLS1W>, gw, 256, 0, st, A, p);
+		break;
+	}
 	default: launch_pdl(k_solve_phase<T, K, SP_PERM_OUT>, g, 256, 0, st, A, p); break;
 	}
 }
@@ -1887,7 +1976,7 @@ void solve_plan_build(DevSymbolic &D, cudaStream_t st)
 		if (!cnt) continue;
 		int n6 = D.h_level_maxn6[l], m6 = D.h_level_maxm6[l];
 		add(SP_GATHER, off, (n6+m6+255)/256, cnt, 1, 1);
-		add(SP_COLS0, off, (n6+SOLVE_CB-1)/SOLVE_CB, cnt, 1, 1);
+		add(n6 <= SOLVE_WARP_ROWS ? SP_COLS0W : SP_COLS0, off, (n6+SOLVE_CB-1)/SOLVE_CB, cnt, 1, 1);
 		if (m6 > 0) {
 			int nch = (n6+SOLVE_JC-1)/SOLVE_JC;
 			add(SP_ROWS0, off, (m6+31)/32, cnt, nch, nch);
@@ -1897,7 +1986,7 @@ void solve_plan_build(DevSymbolic &D, cudaStream_t st)
 		int off = D.h_level_off[l], cnt = D.h_level_off[l+1]-off;
 		if (!cnt) continue;
 		int n6 = D.h_level_maxn6[l], m6 = D.h_level_maxm6[l];
-		if (m6 > 0) add(SP_COLS1, off, (n6+SOLVE_CB-1)/SOLVE_CB, cnt, 1, 1);
+		if (m6 > 0) add(m6 <= SOLVE_WARP_ROWS ? SP_COLS1W : SP_COLS1, off, (n6+SOLVE_CB-1)/SOLVE_CB, cnt, 1, 1);
 		int nch = (n6+SOLVE_JC-1)/SOLVE_JC;
 		add(SP_ROWS1, off, (n6+31)/32, cnt, nch, nch);
 	}

@@ -92,7 +92,7 @@ void symbolic_concat(Symbolic &J, const std::vector<const Symbolic *> &parts);
 // One phase of a solve sweep: gx x gy x gz work units of one type over the
 // supernodes level_sn[lev_off ...] of one level (gy of them).
 enum { SP_PERM_IN, SP_GATHER, SP_COLS0, SP_ROWS0, SP_COLS1, SP_ROWS1, SP_PERM_OUT, SP_PERM_IN_Y, SP_MUL_TOP,
-       SP_MUL_UPD };
+       SP_MUL_UPD, SP_COLS0W, SP_COLS1W };
 struct SolvePhase { int type, lev_off, gx, gy, gz, nchunk; };
 
 struct DevSymbolic {
