@@ -118,6 +118,7 @@ typedef struct {
 	double internal_to_output;
 	double input_value;
 	int out_data_particle, out_data_interaction, origin_zero_flow, pad_;
+	char out_particle_stress[32];   /* the out_particle_stress letters, quotes removed ("" by default) */
 } lfg_output_units;
 int lfg_config_output(const char *parameter_text, char control, const char *control_value, lfg_output_units *out,
                       lfg_status *st);
@@ -384,8 +385,14 @@ int lfg_sim_set_brownian_force(lfg_sim *s, const double *fb, lfg_status *st);
  * unit / internal_to_output / input_value as lfg_config_output gives them;
  * version goes into the "# LF_DEM version" header line; volume_fraction into
  * "# VF".  Existing files are an error unless force_overwrite.  Rows of int_
- * are sorted by particle pair.  Simple shear, no walls (what the engine runs);
- * pst_ (per-particle stress) is not written. */
+ * are sorted by particle pair.  Simple shear, no walls (what the engine runs).
+ * With out_particle_stress letters (the Parameter_File keyword, e.g. "tc";
+ * NULL or "" for none) each output event also writes a pst_<name>.dat block
+ * (Simulation::outputPstFileTxt, Simulation.cpp:823-852): per particle, for
+ * each group the letters name (l hydro, c contact, r repulsion, b brownian,
+ * d dashpot, t total; any other letter the unnamed empty group, all zeros),
+ * in group-name order, the sum of its stress components' per-particle
+ * stresslets (Simulation::getParticleStressGroup, Simulation.cpp:628-639). */
 typedef struct lfg_output lfg_output;
 typedef struct {
 	const char *directory;          /* NULL or "": the working directory */
@@ -396,10 +403,11 @@ typedef struct {
 	double input_value;
 	double volume_fraction;
 	int out_data_particle, out_data_interaction, origin_zero_flow, diminish_output, force_overwrite;
+	const char *out_particle_stress;  /* NULL or "": no pst_ file */
 } lfg_output_config;
 int lfg_output_open(lfg_sim *s, const lfg_output_config *cfg, lfg_output **out, lfg_status *st);
-/* One output event at the current state: a data_ / st_ line, a par_ and an
- * int_ block. */
+/* One output event at the current state: a data_ / st_ line, a par_, an
+ * int_ and a pst_ block. */
 int lfg_output_write(lfg_output *o, lfg_status *st);
 void lfg_output_close(lfg_output *o);
 

@@ -35,7 +35,7 @@ class Status(C.Structure):
 class OutputUnits(C.Structure):
     _fields_ = [("unit", C.c_char * 32), ("internal_to_output", C.c_double), ("input_value", C.c_double),
                 ("out_data_particle", C.c_int), ("out_data_interaction", C.c_int), ("origin_zero_flow", C.c_int),
-                ("pad_", C.c_int)]
+                ("pad_", C.c_int), ("out_particle_stress", C.c_char * 32)]
 
 
 class OutputConfig(C.Structure):
@@ -43,7 +43,7 @@ class OutputConfig(C.Structure):
                 ("unit", C.c_char_p), ("internal_to_output", C.c_double), ("input_value", C.c_double),
                 ("volume_fraction", C.c_double), ("out_data_particle", C.c_int),
                 ("out_data_interaction", C.c_int), ("origin_zero_flow", C.c_int), ("diminish_output", C.c_int),
-                ("force_overwrite", C.c_int)]
+                ("force_overwrite", C.c_int), ("out_particle_stress", C.c_char_p)]
 
 
 class Params(C.Structure):
@@ -380,20 +380,23 @@ def output_units(parameter_text: str, control: str, control_value: str) -> dict:
                                     C.byref(st)), st)
     return {"unit": u.unit.decode(), "internal_to_output": u.internal_to_output, "input_value": u.input_value,
             "out_data_particle": u.out_data_particle, "out_data_interaction": u.out_data_interaction,
-            "origin_zero_flow": u.origin_zero_flow}
+            "origin_zero_flow": u.origin_zero_flow, "out_particle_stress": u.out_particle_stress.decode()}
 
 
 class Output:
-    """LF_DEM's data_/st_/par_/int_ files for a Sim (lfg_output_*)."""
+    """LF_DEM's data_/st_/par_/int_ files (and pst_ when units name
+    out_particle_stress groups) for a Sim (lfg_output_*)."""
 
     def __init__(self, sim, simu_name: str, units: dict, volume_fraction: float, directory: str = "",
                  version: str = "lf_dem_gb300", diminish_output: bool = False, force_overwrite: bool = False):
         L = load()
-        self._keep = [directory.encode(), simu_name.encode(), version.encode(), units["unit"].encode()]
+        self._keep = [directory.encode(), simu_name.encode(), version.encode(), units["unit"].encode(),
+                      units.get("out_particle_stress", "").encode()]
         cfg = OutputConfig(self._keep[0], self._keep[1], self._keep[2], self._keep[3],
                            units["internal_to_output"], units["input_value"], volume_fraction,
                            int(units.get("out_data_particle", 1)), int(units.get("out_data_interaction", 1)),
-                           int(units.get("origin_zero_flow", 1)), int(diminish_output), int(force_overwrite))
+                           int(units.get("origin_zero_flow", 1)), int(diminish_output), int(force_overwrite),
+                           self._keep[4])
         h = C.c_void_p()
         st = Status()
         _check(L.lfg_output_open(sim.h, C.byref(cfg), C.byref(h), C.byref(st)), st)

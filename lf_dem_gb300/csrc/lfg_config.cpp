@@ -167,7 +167,11 @@ public:
 		else if (f("theta_shear")) p.theta_shear = a*M_PI/180;
 		else if (f("strain_reversal")) p.strain_reversal = a;
 		else if (f("event_handler")) p.event_handler = v;
-		else if (f("out_particle_stress")) p.out_particle_stress = v;
+		else if (f("out_particle_stress")) {
+			// quotes removed (SimulationInit.cpp:871-873)
+			p.out_particle_stress.clear();
+			for (char ch : v) if (ch != '"') p.out_particle_stress += ch;
+		}
 		else if (f("out_bond_order_parameter6")) p.out_bond_order_parameter6 = str2bool(v);
 		else if (f("out_binary_conf")) p.out_binary_conf = str2bool(v);
 		else if (f("np_fixed")) p.np_fixed = i;
@@ -463,6 +467,7 @@ extern "C" int lfg_config_output(const char *text, char control, const char *con
 		u.out_data_particle = R.p.out_data_particle;
 		u.out_data_interaction = R.p.out_data_interaction;
 		u.origin_zero_flow = R.p.origin_zero_flow;
+		std::snprintf(u.out_particle_stress, sizeof u.out_particle_stress, "%s", R.p.out_particle_stress.c_str());
 		*out = u;
 		return ok(st);
 	} catch (const std::exception &e) {

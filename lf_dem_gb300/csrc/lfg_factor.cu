@@ -39,6 +39,7 @@ constexpr int SOLVE_WARPS = 8;
 constexpr int SOLVE_CB = 8;      // columns per CTA of the solve's column kernels
 constexpr int SOLVE_JC = 256;    // columns per chunk of the solve's row kernels
 constexpr int SOLVE_WARP_ROWS = 256;   // column products with at most this many rows: one warp per unit
+constexpr unsigned FULL_MASK = 0xffffffffu;
 
 template <typename T> struct Cfg;
 // NB: panel width; TILE/TPT: trailing-update tile edge / outputs per thread
@@ -121,6 +122,7 @@ static void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t sme
 // triangle lands on the parent's).  The children's parameters are fetched
 // by one thread each, up to ASM_CHILDREN at a time.
 constexpr int ASM_CHILDREN = 32;
+constexpr int ASM_BATCH = 4;       // rows per thread and pass of a child's column
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_assemble(const int *__restrict__ col_tasks, const int *__restrict__ sn_n,
@@ -165,9 +167,24 @@ __global__ void __launch_bounds__(256) k_assemble(const int *__restrict__ col_ta
 			// child fronts are complete and not written here: read-only loads
 			const T *src = arena+c_off[u]+(int64_t)jc*c_ld[u];
 			const int *fw = cfwd+c_ro[u];
-			for (int i = jc+threadIdx.x; i < F6c; i += blockDim.x) {
-				int pr = dof*__ldg(&fw[bdiv(i, dof)-nbc])+bmod(i, dof);
-				buf[pr-c] += __ldg(&src[i]);
+			// ASM_BATCH rows per thread and pass, their loads issued first
+			// (within a child the parent rows are distinct)
+			for (int i0 = jc+threadIdx.x; i0 < F6c; i0 += ASM_BATCH*blockDim.x) {
+				T v[ASM_BATCH];
+				int pr[ASM_BATCH];
+#pragma unroll
+				for (int b = 0; b < ASM_BATCH; b++) {
+					int i = i0+b*blockDim.x;
+					pr[b] = -1;
+					v[b] = T(0);
+					if (i < F6c) {
+						pr[b] = dof*__ldg(&fw[bdiv(i, dof)-nbc])+bmod(i, dof);
+						v[b] = __ldg(&src[i]);
+					}
+				}
+#pragma unroll
+				for (int b = 0; b < ASM_BATCH; b++)
+					if (pr[b] >= 0) buf[pr[b]-c] += v[b];
 			}
 			__syncthreads();   // adds of one child complete before the next child's
 		}
@@ -176,6 +193,93 @@ __global__ void __launch_bounds__(256) k_assemble(const int *__restrict__ col_ta
 	for (int r = c+threadIdx.x; r < F6; r += blockDim.x) col[r] = buf[r-c];
 	if (c < n6)
 		for (int r = threadIdx.x; r < n6; r += blockDim.x) col[F6+r] = (r == c) ? T(1) : T(0);
+}
+
+// The same column assembly with one warp per column, ASM_WARPS columns per
+// CTA, for levels of short fronts (the CTA-per-column form leaves most of its
+// threads idle there and is bound by CTA turnover).  Each warp owns a
+// shared-memory column buffer of bufw entries (>= the level's largest front
+// order); the children's parameters are loaded by one lane each and
+// broadcast.  Within a child the parent rows are distinct (cfwd is
+// injective), so each lane adds ASM_BATCH rows per pass with all their loads
+// issued first; children follow one another in the same fixed order as in
+// k_assemble, so every entry is the same sum, bit for bit.
+constexpr int ASM_WARPS = 8;
+constexpr int ASM_WARP_MAXF = 1536;   // levels whose fronts are at most this order use the warp form
+
+template <typename T>
+__global__ void __launch_bounds__(32*ASM_WARPS) k_assemble_warp(const int *__restrict__ col_tasks, int ncols, int bufw,
+                                                                const int *__restrict__ sn_n,
+                                                                const int *__restrict__ sn_m,
+                                                                const int *__restrict__ sn_ld,
+                                                                const int64_t *__restrict__ sn_off,
+                                                                const int *__restrict__ child_off,
+                                                                const int *__restrict__ children,
+                                                                const int64_t *__restrict__ cinv_off,
+                                                                const int *__restrict__ cinv,
+                                                                const int *__restrict__ sn_rows_off,
+                                                                const int *__restrict__ cfwd, T *__restrict__ arena,
+                                                                int dof)
+{
+	extern __shared__ __align__(16) unsigned char smem_asm[];
+	const int warp = threadIdx.x/32, lane = threadIdx.x%32;
+	const int task = blockIdx.x*ASM_WARPS+warp;
+	if (task >= ncols) return;   // whole warps only; nothing below synchronises the CTA
+	T *buf = reinterpret_cast<T *>(smem_asm)+(size_t)warp*bufw;   // buf[r - c], r in [c, 6F)
+	const int s = col_tasks[2*task], c = col_tasks[2*task+1];
+	const int n6 = dof*sn_n[s], F6 = n6+dof*sn_m[s], ld = sn_ld[s];
+	T *col = arena+sn_off[s]+(int64_t)c*ld;
+	const int cb = bdiv(c, dof), cr = bmod(c, dof);
+	const int ca = child_off[s], cz = child_off[s+1];
+	for (int r = lane; r < F6-c; r += 32) buf[r] = T(0);
+	pdl_wait();
+	for (int q0 = ca; q0 < cz; q0 += 32) {
+		const int nq = min(32, cz-q0);
+		int jc = -1, nbc = 0, F6c = 0, cld = 0, cro = 0;
+		int64_t coff = 0;
+		if (lane < nq) {
+			int ch = children[q0+lane];
+			int ic = cinv[cinv_off[ch]+cb];
+			jc = ic < 0 ? -1 : dof*ic+cr;
+			nbc = sn_n[ch];   // in particles
+			F6c = dof*(sn_n[ch]+sn_m[ch]);
+			cld = sn_ld[ch];
+			cro = sn_rows_off[ch];
+			coff = sn_off[ch];
+		}
+		for (int u = 0; u < nq; u++) {
+			const int ju = __shfl_sync(FULL_MASK, jc, u);
+			if (ju < 0) continue;   // uniform: column c is not in this child's update
+			const int nbu = __shfl_sync(FULL_MASK, nbc, u), Fu = __shfl_sync(FULL_MASK, F6c, u);
+			const int ldu = __shfl_sync(FULL_MASK, cld, u), rou = __shfl_sync(FULL_MASK, cro, u);
+			const int64_t offu = __shfl_sync(FULL_MASK, coff, u);
+			// child fronts are complete and not written here: read-only loads
+			const T *src = arena+offu+(int64_t)ju*ldu;
+			const int *fw = cfwd+rou;
+			for (int i0 = ju+lane; i0 < Fu; i0 += 32*ASM_BATCH) {
+				T v[ASM_BATCH];
+				int pr[ASM_BATCH];
+#pragma unroll
+				for (int b = 0; b < ASM_BATCH; b++) {
+					int i = i0+32*b;
+					pr[b] = -1;
+					v[b] = T(0);
+					if (i < Fu) {
+						pr[b] = dof*__ldg(&fw[bdiv(i, dof)-nbu])+bmod(i, dof);
+						v[b] = __ldg(&src[i]);
+					}
+				}
+#pragma unroll
+				for (int b = 0; b < ASM_BATCH; b++)
+					if (pr[b] >= 0) buf[pr[b]-c] += v[b];
+			}
+			__syncwarp();   // adds of one child complete before the next child's
+		}
+	}
+	__syncwarp();
+	for (int r = c+lane; r < F6; r += 32) col[r] = buf[r-c];
+	if (c < n6)
+		for (int r = lane; r < n6; r += 32) col[F6+r] = (r == c) ? T(1) : T(0);
 }
 
 // R_FU blocks of one level added into its fronts, one thread per block: the
@@ -280,7 +384,6 @@ __global__ void k_scatter(int nd, int nod, const int *__restrict__ dlist, const 
 // are padded with the identity.  A non-positive pivot is replaced by 1 and
 // reported through *fail (first global scalar column + 1).
 // ---------------------------------------------------------------------------
-constexpr unsigned FULL_MASK = 0xffffffffu;
 
 // Warp routines on 32 x 32 blocks in shared memory (row-major, stride ld),
 // one row or column per lane in registers.  The step loops are not fully
@@ -1362,6 +1465,11 @@ template <typename T> static size_t assemble_smem(const DevSymbolic &D) { return
 
 template <typename T> static void set_assemble_smem(const DevSymbolic &D)
 {
+	static std::once_flag warp_once;
+	std::call_once(warp_once, [] {
+		LFG_CUDA(cudaFuncSetAttribute(k_assemble_warp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                              (int)(sizeof(T)*ASM_WARP_MAXF*ASM_WARPS)));
+	});
 	static std::mutex mu;
 	static size_t set = 48*1024;
 	size_t need = assemble_smem<T>(D);
@@ -1462,12 +1570,25 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 	for (const auto &L : D.factor_plan) {
 		if (L.count <= 0) continue;
 		switch (L.kind) {
-		case PLAN_ASSEMBLE:
-			launch_pdl(k_assemble<T>, L.count, 256, assemble_smem<T>(D), st, (const int *)D.col_tasks+2*L.off,
-			           (const int *)D.sn_n, (const int *)D.sn_m, (const int *)D.sn_ld, (const int64_t *)D.sn_off,
-			           (const int *)D.child_off, (const int *)D.children, (const int64_t *)D.cinv_off,
-			           (const int *)D.cinv, (const int *)D.sn_rows_off, (const int *)D.cfwd, F.arena, D.dof);
+		case PLAN_ASSEMBLE: {
+			const int fmax = D.h_level_maxF6[L.level];
+			if (fmax <= ASM_WARP_MAXF) {
+				const int bufw = (fmax+3) & ~3;   // 16-byte aligned per-warp buffers
+				launch_pdl(k_assemble_warp<T>, (L.count+ASM_WARPS-1)/ASM_WARPS, 32*ASM_WARPS,
+				           sizeof(T)*(size_t)bufw*ASM_WARPS, st, (const int *)D.col_tasks+2*L.off, L.count, bufw,
+				           (const int *)D.sn_n, (const int *)D.sn_m, (const int *)D.sn_ld,
+				           (const int64_t *)D.sn_off, (const int *)D.child_off, (const int *)D.children,
+				           (const int64_t *)D.cinv_off, (const int *)D.cinv, (const int *)D.sn_rows_off,
+				           (const int *)D.cfwd, F.arena, D.dof);
+			} else {
+				launch_pdl(k_assemble<T>, L.count, 256, assemble_smem<T>(D), st, (const int *)D.col_tasks+2*L.off,
+				           (const int *)D.sn_n, (const int *)D.sn_m, (const int *)D.sn_ld,
+				           (const int64_t *)D.sn_off, (const int *)D.child_off, (const int *)D.children,
+				           (const int64_t *)D.cinv_off, (const int *)D.cinv, (const int *)D.sn_rows_off,
+				           (const int *)D.cfwd, F.arena, D.dof);
+			}
 			break;
+		}
 		case PLAN_SCATTER: {
 			int d0 = D.h_level_d_off[L.level], nd = D.h_level_d_off[L.level+1]-d0;
 			int o0 = D.h_level_od_off[L.level], nod = D.h_level_od_off[L.level+1]-o0;

@@ -122,6 +122,7 @@ struct DevSymbolic {
 	std::vector<Launch> factor_plan;
 	std::vector<int> h_level_off, h_level_d_off, h_level_od_off;
 	std::vector<int> h_level_maxn6, h_level_maxm6;   // per-level maxima of dof n and dof m (scalar)
+	std::vector<int> h_level_maxF6;                  // per-level maximum front order dof (n + m) (scalar)
 	std::vector<int64_t> h_col_task_off;
 	int64_t arena_elems = 0, w_elems = 0;
 	int max_F = 0;
@@ -203,6 +204,11 @@ struct OutputSnapshot {
 	std::vector<double> radius, pos, vel, ang, na, na_disp, angle;   // n, 3n, 3n, 3n, 6n, 3n, n
 	std::vector<double> pairs;                // OUT_W doubles per interaction, sorted by (p0, p1)
 	int out_w = 0;
+	// per-particle stresslets of every stress slot (NSC x 6n) and which slots
+	// the run declares; filled only when want_particle_stress is set
+	bool want_particle_stress = false;
+	std::vector<double> particle_stress;
+	std::vector<char> slot_declared;
 };
 
 // Fused batch (lfg_sim.cpp): suspensions stepping in lockstep through one

@@ -4,6 +4,8 @@
 //  - st_<name>.dat   : its stress-tensor part (Simulation.cpp:781-792)
 //  - par_<name>.dat  : Simulation::outputParFileTxt (Simulation.cpp:884-965)
 //  - int_<name>.dat  : Simulation::outputIntFileTxt (Simulation.cpp:967-1006)
+//  - pst_<name>.dat  : Simulation::outputPstFileTxt (Simulation.cpp:823-852),
+//                      when out_particle_stress names groups
 // each file starting with Simulation::createDataHeader (Simulation.cpp:
 // 857-869), the per-snapshot blocks of par_/int_ with getSnapshotHeader
 // (Simulation.cpp:811-836).  The column mechanics follow OutputData
@@ -140,8 +142,8 @@ double vdot3(const double *a, const double *b) { return a[0]*b[0]+a[1]*b[1]+a[2]
 struct lfg_output {
 	lfg_sim *sim = nullptr;
 	lfg_output_config cfg;
-	std::string unit, version;
-	Table data, st, par, inter;
+	std::string unit, version, pst_letters;
+	Table data, st, par, inter, pst;
 	int flags = 0;   // 1 par_, 2 int_
 };
 
@@ -322,6 +324,57 @@ void write_int(lfg_output &o, const lfg::OutputSnapshot &S)
 	if (npair > 0) T.write(snapshot_header(o, S));
 }
 
+// The stress components System::declareStressComponents (Stress.cpp:20-75)
+// creates, in the key order of its std::map (which fixes the order of the
+// per-particle sums), with the engine's slot and the component's group.
+struct PstComponent { const char *key; int slot; const char *group; };
+const PstComponent PST_COMPONENTS[] = {
+	{"M_E_hydro", lfg::SC_ME, "hydro"},
+	{"brownian", lfg::SC_GU_BROWNIAN, "brownian"},
+	{"brownian_predictor", lfg::SC_BROWNIAN_PRED, "brownian"},
+	{"contact", lfg::SC_GU_CONTACT, "contact"},
+	{"dashpot", lfg::SC_GU_DASHPOT, "dashpot"},
+	{"hydro", lfg::SC_GU_HYDRO, "hydro"},
+	{"repulsion", lfg::SC_GU_REPULSION, "repulsion"},
+	{"xF_contact", lfg::SC_XF_CONTACT, "contact"},
+	{"xF_contact_rateindep", lfg::SC_XF_RATEINDEP, "contact"},
+	{"xF_contact_rateprop", lfg::SC_XF_RATEPROP, "contact"},
+	{"xF_repulsion", lfg::SC_XF_REPULSION, "repulsion"},
+};
+
+// Simulation::outputPstFileTxt (Simulation.cpp:823-852): the groups the
+// letters name (Simulation.cpp:832-838; a letter outside the table names the
+// empty group) in the order of their names (a std::map), per particle the
+// sum of the group's declared components' stresslets in key order
+// (Simulation::getParticleStressGroup, Simulation.cpp:628-639; "total": all),
+// in stress units.
+void write_pst(lfg_output &o, const lfg::OutputSnapshot &S)
+{
+	static const std::map<char, std::string> shorts = {{'l', "hydro"}, {'c', "contact"}, {'r', "repulsion"},
+	                                                   {'b', "brownian"}, {'d', "dashpot"}, {'t', "total"}};
+	std::map<std::string, std::vector<int>> groups;   // group -> slots summed, in key order
+	for (char ch : o.pst_letters) {
+		auto it = shorts.find(ch);
+		const std::string g = it == shorts.end() ? std::string() : it->second;
+		std::vector<int> &slots = groups[g];
+		slots.clear();
+		for (const PstComponent &c : PST_COMPONENTS)
+			if (S.slot_declared[c.slot] && (g == "total" || g == c.group)) slots.push_back(c.slot);
+	}
+	Table &T = o.pst;
+	const int n = S.n;
+	for (int i = 0; i < n; i++)
+		for (const auto &g : groups) {
+			double v[6] = {0, 0, 0, 0, 0, 0};
+			for (int slot : g.second) {
+				const double *x = S.particle_stress.data()+((size_t)slot*n+i)*6;
+				for (int e = 0; e < 6; e++) v[e] += x[e];
+			}
+			T.entry(g.first+" stress (xx, xy, xz, yz, yy, zz)", "stress", 6, v);
+		}
+	T.write(snapshot_header(o, S));
+}
+
 } // namespace
 
 extern "C" {
@@ -357,12 +410,15 @@ int lfg_output_open(lfg_sim *sim, const lfg_output_config *cfg, lfg_output **out
 	bool good = o->data.open(dir+"data_"+name+".dat", h.str(), ow) && o->st.open(dir+"st_"+name+".dat", h.str(), ow);
 	if (good && cfg->out_data_particle) good = o->par.open(dir+"par_"+name+".dat", h.str(), ow);
 	if (good && cfg->out_data_interaction) good = o->inter.open(dir+"int_"+name+".dat", h.str(), ow);
+	o->pst_letters = cfg->out_particle_stress ? cfg->out_particle_stress : "";
+	o->cfg.out_particle_stress = o->pst_letters.c_str();
+	if (good && !o->pst_letters.empty()) good = o->pst.open(dir+"pst_"+name+".dat", h.str(), ow);
 	if (!good) {
 		delete o;
 		return fail(st, LFG_ERR_BAD_ARG, 0, "cannot create the output files (existing files need force_overwrite)");
 	}
 	const double d = cfg->internal_to_output;
-	for (Table *t : {&o->data, &o->st, &o->par, &o->inter}) t->set_units(o->unit, d);
+	for (Table *t : {&o->data, &o->st, &o->par, &o->inter, &o->pst}) t->set_units(o->unit, d);
 	// Simulation::outputParFileTxt: precision 4 with diminish_output
 	o->par.set_precision(cfg->diminish_output ? 4 : 6);
 	o->inter.set_precision(cfg->diminish_output ? 4 : 6);
@@ -375,10 +431,12 @@ int lfg_output_write(lfg_output *o, lfg_status *st)
 	if (!o) return fail(st, LFG_ERR_BAD_ARG, 0, "bad arguments");
 	try {
 		lfg::OutputSnapshot S;
+		S.want_particle_stress = !o->pst_letters.empty();
 		lfg::sim_output_snapshot(o->sim, S);
 		write_data(*o, S);
 		if (o->cfg.out_data_particle) write_par(*o, S);
 		if (o->cfg.out_data_interaction) write_int(*o, S);
+		if (!o->pst_letters.empty()) write_pst(*o, S);
 	} catch (const lfg::Error &e) {
 		return fail(st, e.code, e.info, e.msg.c_str());
 	}

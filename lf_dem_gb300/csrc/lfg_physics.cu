@@ -288,26 +288,72 @@ __global__ void k_cell_assign(DevParams P, CellView C, const double *__restrict_
 	atomicAdd(&count[c], 1);
 }
 
-// exclusive scan of n ints by one CTA (n up to a few 10^5)
-__global__ void k_scan(int n, const int *__restrict__ in, int *__restrict__ out, int *total)
+// exclusive scan of n ints by one CTA of 1024 threads (cell counts, candidate
+// counts: n up to a few 10^5): tiles of 4096 entries, four consecutive
+// entries per thread (one vector load), warp-shuffle scans of the thread and
+// warp sums, the tile total carried to the next tile; out[n] = total.
+constexpr unsigned PFULL = 0xffffffffu;
+__global__ void __launch_bounds__(1024) k_scan(int n, const int *__restrict__ in, int *__restrict__ out, int *total)
 {
-	__shared__ int part[1024];
-	int t = threadIdx.x, T = blockDim.x;
-	int chunk = (n+T-1)/T;
-	int lo = t*chunk, hi = min(n, lo+chunk);
-	int s = 0;
-	for (int k = lo; k < hi; k++) s += in[k];
-	part[t] = s;
-	__syncthreads();
-	if (t == 0) {
-		int acc = 0;
-		for (int k = 0; k < T; k++) { int v = part[k]; part[k] = acc; acc += v; }
-		if (total) *total = acc;
-		out[n] = acc;
+	__shared__ int wsum[32];
+	const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+	int carry = 0;
+	for (int base = 0; base < n; base += 4*1024) {
+		const int i0 = base+4*t;
+		int v[4];
+		if (i0+3 < n) {
+			int4 q = *reinterpret_cast<const int4 *>(in+i0);   // base and i0 are multiples of 4
+			v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+		} else {
+#pragma unroll
+			for (int k = 0; k < 4; k++) v[k] = i0+k < n ? in[i0+k] : 0;
+		}
+		const int sum = v[0]+v[1]+v[2]+v[3];
+		int x = sum;   // inclusive scan over the warp
+#pragma unroll
+		for (int o = 1; o < 32; o <<= 1) {
+			int y = __shfl_up_sync(PFULL, x, o);
+			if (lane >= o) x += y;
+		}
+		if (lane == 31) wsum[wid] = x;
+		__syncthreads();
+		if (wid == 0) {
+			int w = wsum[lane];
+#pragma unroll
+			for (int o = 1; o < 32; o <<= 1) {
+				int y = __shfl_up_sync(PFULL, w, o);
+				if (lane >= o) w += y;
+			}
+			wsum[lane] = w;
+		}
+		__syncthreads();
+		int excl = carry+(wid ? wsum[wid-1] : 0)+x-sum;
+#pragma unroll
+		for (int k = 0; k < 4; k++) {
+			if (i0+k < n) out[i0+k] = excl;
+			excl += v[k];
+		}
+		carry += wsum[31];
+		__syncthreads();   // wsum is rewritten by the next tile
 	}
-	__syncthreads();
-	int acc = part[t];
-	for (int k = lo; k < hi; k++) { out[k] = acc; acc += in[k]; }
+	if (t == 0) {
+		out[n] = carry;
+		if (total) *total = carry;
+	}
+}
+
+// ascending sort of 32 values, one per lane (bitonic network over shuffles)
+__device__ __forceinline__ int warp_sort32(int v, int lane)
+{
+#pragma unroll
+	for (int k = 2; k <= 32; k <<= 1)
+#pragma unroll
+		for (int j = k >> 1; j > 0; j >>= 1) {
+			int o = __shfl_xor_sync(PFULL, v, j);
+			bool up = (lane & k) == 0, lower = (lane & j) == 0;
+			v = (lower == up) ? min(v, o) : max(v, o);
+		}
+	return v;
 }
 
 __global__ void k_cell_fill(int n, const int *__restrict__ cell_of, const int *__restrict__ start,
@@ -320,50 +366,244 @@ __global__ void k_cell_fill(int n, const int *__restrict__ cell_of, const int *_
 	list[start[c]+k] = i;
 }
 
-// sort each cell's particle list (deterministic neighbour order)
+// Each cell's particle list sorted (deterministic neighbour order), one warp
+// per cell: up to 32 members sorted in registers (bitonic), larger cells by
+// lane 0 in place.  The warp then writes the cell-ordered records (x, y, z,
+// radius) of its members, so the neighbour searches read a cell's particles
+// as contiguous 32-byte records (two vector loads each).
 __global__ void k_cell_sort(int ncell, const int *__restrict__ start, const int *__restrict__ count,
-                            int *__restrict__ list)
+                            int *__restrict__ list, const double *__restrict__ pos, const double *__restrict__ radius,
+                            double *__restrict__ rec)
 {
-	int c = blockIdx.x*blockDim.x+threadIdx.x;
-	if (c >= ncell) return;
-	int s = start[c], e = s+count[c];
-	for (int a = s+1; a < e; a++) {
-		int x = list[a], b = a-1;
-		while (b >= s && list[b] > x) { list[b+1] = list[b]; b--; }
-		list[b+1] = x;
+	const int c = (blockIdx.x*blockDim.x+threadIdx.x) >> 5, lane = threadIdx.x & 31;
+	if (c >= ncell) return;   // whole warps
+	const int s = start[c], m = count[c];
+	if (m <= 32) {
+		int v = lane < m ? list[s+lane] : 0x7fffffff;
+		v = warp_sort32(v, lane);
+		if (lane < m) list[s+lane] = v;
+	} else {
+		if (lane == 0)
+			for (int a = s+1; a < s+m; a++) {
+				int x = list[a], b = a-1;
+				while (b >= s && list[b] > x) { list[b+1] = list[b]; b--; }
+				list[b+1] = x;
+			}
+		__syncwarp();
+	}
+	for (int k = s+lane; k < s+m; k += 32) {
+		int j = list[k];
+		double4 r = make_double4(pos[3*j], pos[3*j+1], pos[3*j+2], radius[j]);
+		reinterpret_cast<double4 *>(rec)[k] = r;
 	}
 }
 
-// candidate pairs within the superset range (range + skin (a_i+a_j)/2)
+// Candidate pairs within the superset range (range + skin (a_i+a_j)/2), one
+// warp per particle i: the lanes take the members of each neighbour cell (the
+// cells for_neighbours visits, in its order) as contiguous cell-ordered
+// records, a ballot compacts the hits in visit order, and the row is sorted
+// in registers (bitonic; rows longer than 32 by lane 0 in place).  Pass 1
+// (ptr null) counts, pass 2 fills.  Systems too small for cells (brute) take
+// every j > i from the particle arrays.
 __global__ void k_candidates(DevParams P, CellView C, const DevClock *__restrict__ clk,
                              const double *__restrict__ pos, const double *__restrict__ radius,
-                             int *__restrict__ count, const int *__restrict__ ptr, int *__restrict__ cand)
+                             const double *__restrict__ rec, int *__restrict__ count, const int *__restrict__ ptr,
+                             int *__restrict__ cand)
 {
-	int i = blockIdx.x*blockDim.x+threadIdx.x;
-	if (i >= C.n) return;
+	const int i = (int)(((int64_t)blockIdx.x*blockDim.x+threadIdx.x) >> 5), lane = threadIdx.x & 31;
+	if (i >= C.n) return;   // whole warps
 	const double *sd = clk->shear_disp;
-	v3 pi = ld3(pos+3*i);
-	double ri = radius[i];
-	int c = 0;
-	int base = ptr ? ptr[i] : 0;
-	for_neighbours(C, P, sd, i, pi, [&](int j) {
-		v3 d = vsub(ld3(pos+3*j), pi);
-		periodize_diff(P, sd, d);
-		double rj = radius[j];
-		double rs = inter_range(P, ri, rj)+P.skin*0.5*(ri+rj);
-		if (vsq(d) < rs*rs) {
-			if (ptr) cand[base+c] = j;
-			c++;
+	const v3 pi = ld3(pos+3*i);
+	const double ri = radius[i];
+	const int base = ptr ? ptr[i] : 0;
+	int c = 0;   // hits so far (the same in every lane)
+	auto scan = [&](int s, int e, bool brute) {
+		for (int k0 = s; k0 < e; k0 += 32) {
+			const int k = k0+lane;
+			bool hit = false;
+			int j = -1;
+			if (k < e) {
+				v3 pj;
+				double rj;
+				if (brute) {
+					j = k;
+					pj = ld3(pos+3*j);
+					rj = radius[j];
+				} else {
+					j = C.list[k];
+					const double4 r = reinterpret_cast<const double4 *>(rec)[k];
+					pj = V(r.x, r.y, r.z);
+					rj = r.w;
+				}
+				if (j > i) {
+					v3 d = vsub(pj, pi);
+					periodize_diff(P, sd, d);
+					double rs = inter_range(P, ri, rj)+P.skin*0.5*(ri+rj);
+					hit = vsq(d) < rs*rs;
+				}
+			}
+			const unsigned b = __ballot_sync(PFULL, hit);
+			if (ptr && hit) cand[base+c+__popc(b & ((1u << lane)-1))] = j;
+			c += __popc(b);
 		}
-	});
-	if (!ptr) count[i] = c;
-	else {
-		// sort the row
+	};
+	if (C.brute) {
+		scan(i+1, C.n, true);
+	} else {
+		const int cz = cell_coord(pi.z, P.lz, C.csz, C.ncz);
+		for (int dz = -1; dz <= 1; dz++) {
+			int zc = cz+dz;
+			double sx = 0, sy = 0;
+			if (zc < 0) { zc += C.ncz; sx = sd[0]; sy = sd[1]; }
+			else if (zc >= C.ncz) { zc -= C.ncz; sx = -sd[0]; sy = -sd[1]; }
+			const int xc = cell_coord(pi.x+sx, P.lx, C.csx, C.ncx);
+			const int yc = P.twodim ? 0 : cell_coord(pi.y+sy, P.ly, C.csy, C.ncy);
+			const int ylo = P.twodim ? 0 : -1, yhi = P.twodim ? 0 : 1;
+			for (int dy = ylo; dy <= yhi; dy++) {
+				const int yy = P.twodim ? 0 : wrapc(yc+dy, C.ncy);
+				for (int dx = -1; dx <= 1; dx++) {
+					const int cell = (zc*C.ncy+yy)*C.ncx+wrapc(xc+dx, C.ncx);
+					const int s0 = C.start[cell];
+					scan(s0, s0+C.count[cell], false);
+				}
+			}
+		}
+	}
+	if (!ptr) {
+		if (lane == 0) count[i] = c;
+		return;
+	}
+	__syncwarp();   // the row's stores are visible to the warp
+	if (c <= 32) {
+		int v = lane < c ? cand[base+lane] : 0x7fffffff;
+		v = warp_sort32(v, lane);
+		if (lane < c) cand[base+lane] = v;
+	} else if (lane == 0) {
 		for (int a = base+1; a < base+c; a++) {
-			int x = cand[a], b = a-1;
-			while (b >= base && cand[b] > x) { cand[b+1] = cand[b]; b--; }
-			cand[b+1] = x;
+			int x = cand[a], q = a-1;
+			while (q >= base && cand[q] > x) { cand[q+1] = cand[q]; q--; }
+			cand[q+1] = x;
 		}
+	}
+}
+
+// System::checkNewInteraction's test (System.cpp:1328-1373): every pair
+// (i, j > i) within the interaction range must be in the superset.  One CTA
+// per home cell: the records of the cells its particles search are staged in
+// shared memory (in passes of CHK_CAP), and one warp per home particle i
+// tests them, its superset row (the sorted candidate list) held in lanes and
+// matched by shuffles.  The staged cells are a superset of those
+// for_neighbours visits from any particle of the home cell: a Lees-Edwards
+// shifted row takes five x (and, with a y shift, five y) cells around the
+// shifted cell of the home cell's centre, since a particle's shifted cell is
+// at most one away from it.  Extra or repeated cells only repeat tests.
+constexpr int CHK_CAP = 640;   // staged records per pass
+constexpr int CHK_SLOTS = 75;  // 3 rows x 5 x 5 cells at most
+__global__ void __launch_bounds__(128) k_check_cells(DevParams P, CellView C, DevClock *__restrict__ clk,
+                                                     const double *__restrict__ rec, const int *__restrict__ row_ptr,
+                                                     const int *__restrict__ cand)
+{
+	__shared__ double4 srec[CHK_CAP];
+	__shared__ int sidx[CHK_CAP];
+	__shared__ int cs[CHK_SLOTS], cpre[CHK_SLOTS+1];
+	const int h = blockIdx.x;
+	const int hs = C.start[h], hn = C.count[h];
+	if (hn == 0) return;   // the same in every thread
+	const int hx = h%C.ncx, hy = (h/C.ncx)%C.ncy, hz = h/(C.ncx*C.ncy);
+	const double *sd = clk->shear_disp;
+	const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+	if (t < CHK_SLOTS) {
+		// slot (row dz, y offset, x offset) -> cell and member count (0 if unused)
+		const int dz = t/25-1, yq = (t/5)%5, xq = t%5;
+		int zc = hz+dz;
+		double sx = 0, sy = 0;
+		bool sh = false;
+		if (zc < 0) { zc += C.ncz; sx = sd[0]; sy = sd[1]; sh = true; }
+		else if (zc >= C.ncz) { zc -= C.ncz; sx = -sd[0]; sy = -sd[1]; sh = true; }
+		int xa = hx-1, xn = 3;
+		if (sh && sx != 0) { xa = cell_coord((hx+0.5)*C.csx+sx, P.lx, C.csx, C.ncx)-2; xn = 5; }
+		int ya = 0, yn = 1;
+		if (!P.twodim) {
+			ya = hy-1; yn = 3;
+			if (sh && sy != 0) { ya = cell_coord((hy+0.5)*C.csy+sy, P.ly, C.csy, C.ncy)-2; yn = 5; }
+		}
+		int cnt = 0, st0 = 0;
+		if (xq < xn && yq < yn) {
+			const int yy = P.twodim ? 0 : wrapc(ya+yq, C.ncy);
+			const int cell = (zc*C.ncy+yy)*C.ncx+wrapc(xa+xq, C.ncx);
+			st0 = C.start[cell];
+			cnt = C.count[cell];
+		}
+		cs[t] = st0;
+		cpre[t+1] = cnt;
+	}
+	__syncthreads();
+	if (warp == 0) {
+		// inclusive prefix of the slot counts: lane l sums slots 3l .. 3l + 2
+		int v[3], sum = 0;
+#pragma unroll
+		for (int u = 0; u < 3; u++) { int q = 3*lane+u; v[u] = q < CHK_SLOTS ? cpre[q+1] : 0; sum += v[u]; }
+		int x = sum;
+#pragma unroll
+		for (int o = 1; o < 32; o <<= 1) {
+			int y = __shfl_up_sync(PFULL, x, o);
+			if (lane >= o) x += y;
+		}
+		int run = x-sum;
+#pragma unroll
+		for (int u = 0; u < 3; u++) {
+			int q = 3*lane+u;
+			run += v[u];
+			if (q < CHK_SLOTS) cpre[q+1] = run;
+		}
+		if (lane == 0) cpre[0] = 0;
+	}
+	__syncthreads();
+	const int R = cpre[CHK_SLOTS];
+	for (int f0 = 0; f0 < R; f0 += CHK_CAP) {
+		const int fn = min(CHK_CAP, R-f0);
+		for (int f = t; f < fn; f += blockDim.x) {
+			const int g = f0+f;
+			int lo = 0, hi = CHK_SLOTS-1;   // last slot with cpre <= g
+			while (lo < hi) {
+				int mid = (lo+hi+1) >> 1;
+				if (cpre[mid] <= g) lo = mid; else hi = mid-1;
+			}
+			const int k = cs[lo]+g-cpre[lo];
+			srec[f] = reinterpret_cast<const double4 *>(rec)[k];
+			sidx[f] = C.list[k];
+		}
+		__syncthreads();
+		for (int hp = warp; hp < hn; hp += blockDim.x >> 5) {
+			const int i = C.list[hs+hp];
+			const double4 r4 = reinterpret_cast<const double4 *>(rec)[hs+hp];
+			const v3 pi = V(r4.x, r4.y, r4.z);
+			const int lo = row_ptr[i], len = row_ptr[i+1]-lo;
+			const int rv0 = lane < len ? cand[lo+lane] : -2;
+			for (int fb = 0; fb < fn; fb += 32) {
+				const int f = fb+lane;
+				int need = -1;
+				if (f < fn) {
+					const int j = sidx[f];
+					if (j > i) {
+						const double4 r = srec[f];
+						v3 d = vsub(V(r.x, r.y, r.z), pi);
+						periodize_diff(P, sd, d);
+						double range = inter_range(P, r4.w, r.w);
+						if (vsq(d) < range*range) need = j;
+					}
+				}
+				if (!__any_sync(PFULL, need >= 0)) continue;
+				bool found = false;
+				for (int e0 = 0; e0 < len; e0 += 32) {
+					const int rv = e0 == 0 ? rv0 : (e0+lane < len ? cand[lo+e0+lane] : -2);
+					const int m = min(32, len-e0);
+					for (int e = 0; e < m; e++) found |= __shfl_sync(PFULL, rv, e) == need;
+				}
+				if (need >= 0 && !found) atomicOr(&clk->stale, 1);
+			}
+		}
+		__syncthreads();   // srec is restaged by the next pass
 	}
 }
 
@@ -1482,14 +1722,16 @@ void phys_cells(DevSim &S, double, cudaStream_t st)
 	// reuse cand_count as the fill counter
 	LFG_CUDA(cudaMemsetAsync(S.cand_count, 0, sizeof(int)*ncell, st));
 	k_cell_fill<<<blocks_for(S.n, 128), 128, 0, st>>>(S.n, S.cell_of, S.cell_start, S.cand_count, S.cell_list);
-	k_cell_sort<<<blocks_for(ncell, 128), 128, 0, st>>>(ncell, S.cell_start, S.cell_count, S.cell_list);
+	k_cell_sort<<<blocks_for((int64_t)32*ncell, 128), 128, 0, st>>>(ncell, S.cell_start, S.cell_count, S.cell_list,
+	                                                                 S.pos, S.radius, S.cell_rec);
 	S.launches += 4;
 }
 
 void phys_candidates(DevSim &S, cudaStream_t st, int *h_total)
 {
 	CellView C = view(S);
-	k_candidates<<<blocks_for(S.n, 128), 128, 0, st>>>(S.P, C, S.clock, S.pos, S.radius, S.cand_count, nullptr, nullptr);
+	k_candidates<<<blocks_for((int64_t)32*S.n, 128), 128, 0, st>>>(S.P, C, S.clock, S.pos, S.radius, S.cell_rec,
+	                                                                S.cand_count, nullptr, nullptr);
 	k_scan<<<1, 1024, 0, st>>>(S.n, S.cand_count, S.cand_ptr, nullptr);
 	LFG_CUDA(cudaMemcpyAsync(h_total, S.cand_ptr+S.n, sizeof(int), cudaMemcpyDeviceToHost, st));
 	LFG_CUDA(cudaStreamSynchronize(st));
@@ -1498,15 +1740,19 @@ void phys_candidates(DevSim &S, cudaStream_t st, int *h_total)
 		S.cand_cap = *h_total+*h_total/4+1024;
 		LFG_CUDA(cudaMalloc((void **)&S.cand, sizeof(int)*S.cand_cap));
 	}
-	k_candidates<<<blocks_for(S.n, 128), 128, 0, st>>>(S.P, C, S.clock, S.pos, S.radius, S.cand_count, S.cand_ptr, S.cand);
+	k_candidates<<<blocks_for((int64_t)32*S.n, 128), 128, 0, st>>>(S.P, C, S.clock, S.pos, S.radius, S.cell_rec,
+	                                                                S.cand_count, S.cand_ptr, S.cand);
 	S.launches += 3;
 }
 
 void phys_check_superset(DevSim &S, cudaStream_t st)
 {
 	CellView C = view(S);
-	k_check_superset<<<blocks_for((S.P.twodim ? 9 : 27)*S.n, 256), 256, 0, st>>>(S.P, C, S.clock, S.pos, S.radius,
-	                                                                           S.row_ptr, S.pairs);
+	if (S.brute)
+		k_check_superset<<<blocks_for((S.P.twodim ? 9 : 27)*S.n, 256), 256, 0, st>>>(S.P, C, S.clock, S.pos, S.radius,
+		                                                                           S.row_ptr, S.pairs);
+	else
+		k_check_cells<<<S.ncx*S.ncy*S.ncz, 128, 0, st>>>(S.P, C, S.clock, S.cell_rec, S.row_ptr, S.cand);
 	S.launches++;
 }
 

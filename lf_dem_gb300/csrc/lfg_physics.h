@@ -101,6 +101,7 @@ struct DevSim {
 	int ncx = 0, ncy = 0, ncz = 0, brute = 0;
 	double csx = 0, csy = 0, csz = 0;
 	int *cell_of = nullptr, *cell_start = nullptr, *cell_count = nullptr, *cell_list = nullptr;
+	double *cell_rec = nullptr;        // 4n: (x, y, z, radius) of cell_list[k] at 4k (cell order)
 	int *cand_count = nullptr, *cand_ptr = nullptr, *cand = nullptr;
 	int cand_cap = 0;
 	int ncell_cap = 0;

@@ -728,10 +728,12 @@ void dev_symbolic_upload(DevSymbolic &D, const Symbolic &S, int nb, int panel_nb
 	for (int s = 0; s < S.nsn; s++) D.max_n6 = std::max(D.max_n6, dof*S.sn_n[s]);
 	D.h_level_maxn6.assign(S.nlevels, 0);
 	D.h_level_maxm6.assign(S.nlevels, 0);
+	D.h_level_maxF6.assign(S.nlevels, 0);
 	for (int s = 0; s < S.nsn; s++) {
 		int l = S.sn_level[s];
 		D.h_level_maxn6[l] = std::max(D.h_level_maxn6[l], dof*S.sn_n[s]);
 		D.h_level_maxm6[l] = std::max(D.h_level_maxm6[l], dof*S.sn_m[s]);
+		D.h_level_maxF6[l] = std::max(D.h_level_maxF6[l], dof*(S.sn_n[s]+S.sn_m[s]));
 	}
 	// assembly column tasks, panel tasks and update tiles, level by level
 	std::vector<int> col_tasks;

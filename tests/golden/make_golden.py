@@ -9,7 +9,7 @@ R_FU (lower CSC) and force / velocity / stress components at that state, and
 the state after the step.  The tests replay each step from the stored state
 with the CPU oracle and with the GPU engine and compare.
 
-usage: LFDEM_REF=<LF_DEM source dir> make -C oracle ref && python tests/golden/make_golden.py [case | writers_case ...]
+usage: LFDEM_REF=<LF_DEM source dir> make -C oracle ref && python tests/golden/make_golden.py [case | writers_case | writers_pst_case ...]
 """
 import os
 import subprocess
@@ -147,34 +147,40 @@ def run_case(name, c, workdir):
 WRITER_CASES = ["rate_n200", "stress_n200", "rate_normal_n200", "rate_2d_n200"]
 WRITER_DSTRAIN = 1e-4
 WRITER_OUTPUTS = 2
+# The per-particle stress file pst_ (Simulation::outputPstFileTxt): the same
+# runs with out_particle_stress letters appended to the Parameter_File; every
+# group letter, and one letter outside the reference's table (its group has
+# the empty name and no components)
+PST_CASES = {"stress_n200": "tcldrb", "rate_normal_n200": "rcxt"}
 
 
-def run_writers(name, c, workdir):
+def run_writers(name, c, workdir, pst=None):
     p = packing.generate(c["n"], c["vf"], seed=c["seed"], twodim=c.get("twodim", False))
     conf = os.path.join(workdir, f"w_{name}.dat")
     packing.write_conf(p, conf)
     par = os.path.join(workdir, f"w_{name}_params.txt")
+    params = c["params"] + (f'out_particle_stress = "{pst}";\n' if pst else "")
     with open(par, "w") as f:
-        f.write(c["params"])
-    out = os.path.join(workdir, "w_" + name)
+        f.write(params)
+    out = os.path.join(workdir, ("p_" if pst else "w_") + name)
     os.makedirs(out, exist_ok=True)
     env = dict(os.environ, HARNESS_OUTPUT_DSTRAIN=repr(WRITER_DSTRAIN))
     r = subprocess.run([HARNESS, conf, par, c["control"], c["value"], c["suffix"], str(WRITER_OUTPUTS), out],
                        capture_output=True, text=True, env=env)
     if r.returncode != 0:
         raise RuntimeError(f"harness (output mode) failed for {name}: {r.stderr[-2000:]}")
-    data = {"param_file": np.frombuffer(c["params"].encode(), dtype=np.uint8),
+    data = {"param_file": np.frombuffer(params.encode(), dtype=np.uint8),
             "control": np.frombuffer(c["control"].encode(), dtype=np.uint8),
             "control_value": np.frombuffer((c["value"]+c["suffix"]).encode(), dtype=np.uint8),
             "dstrain": np.array([WRITER_DSTRAIN]), "outputs": np.array([WRITER_OUTPUTS])}
     with open(conf) as f:
         data["conf_file"] = np.frombuffer(f.read().encode(), dtype=np.uint8)
-    for kind in ("data", "st", "par", "int"):
+    for kind in (("pst",) if pst else ("data", "st", "par", "int")):
         files = [f for f in os.listdir(out) if f.startswith(kind + "_") and f.endswith(".dat")]
         assert len(files) == 1, (kind, files)
         with open(os.path.join(out, files[0]), "rb") as f:
             data[kind] = np.frombuffer(f.read(), dtype=np.uint8)
-    path = os.path.join(HERE, f"writers_{name}.npz")
+    path = os.path.join(HERE, f"writers_pst_{name}.npz" if pst else f"writers_{name}.npz")
     np.savez_compressed(path, **data)
     return os.path.getsize(path)
 
@@ -192,6 +198,9 @@ def main(only=None):
             if name in WRITER_CASES and (not only or name in only or "writers_" + name in only):
                 size = run_writers(name, c, wd)
                 print(f"writers_{name}: {size/1e3:.0f} kB")
+            if name in PST_CASES and (not only or name in only or "writers_pst_" + name in only):
+                size = run_writers(name, c, wd, pst=PST_CASES[name])
+                print(f"writers_pst_{name}: {size/1e3:.0f} kB")
 
 
 if __name__ == "__main__":

@@ -159,3 +159,51 @@ def test_output_files_match_reference(engine, case):
             with open(os.path.join(d, f"{kind}_gpu.dat")) as f:
                 got = f.read()
             _compare(kind, txt[kind], got)
+
+
+PST_CASES = ["stress_n200", "rate_normal_n200"]
+
+
+def _load_pst(case):
+    F = dict(np.load(os.path.join(GOLDEN, f"writers_pst_{case}.npz")))
+    txt = {k: F[k].tobytes().decode() for k in ("param_file", "control", "control_value", "conf_file", "pst")}
+    return F, txt
+
+
+@pytest.mark.parametrize("case", PST_CASES)
+def test_output_units_carry_particle_stress_letters(lib, case):
+    """out_particle_stress reaches the output units without its quotes  (CPU)"""
+    F, txt = _load_pst(case)
+    u = lib.output_units(txt["param_file"], txt["control"], txt["control_value"])
+    line = [ln for ln in txt["param_file"].splitlines() if ln.startswith("out_particle_stress")][0]
+    assert u["out_particle_stress"] == line.split("=")[1].strip().strip(";").strip('"')
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", PST_CASES)
+def test_particle_stress_file_matches_reference(engine, case):
+    """pst_ (Simulation::outputPstFileTxt) against the file the reference wrote
+    for the same run: the column list (the groups the letters name, in name
+    order, including the unnamed group of a letter outside the table), the
+    snapshot headers and every particle's group stresses."""
+    from lf_dem_gb300 import packing
+    F, txt = _load_pst(case)
+    with tempfile.TemporaryDirectory() as d:
+        conf = os.path.join(d, "conf.dat")
+        with open(conf, "w") as f:
+            f.write(txt["conf_file"])
+        p = packing.read_conf(conf)
+        params, _, _ = engine.resolve_config(txt["param_file"], txt["control"], txt["control_value"])
+        units = engine.output_units(txt["param_file"], txt["control"], txt["control_value"])
+        assert units["out_particle_stress"]
+        g = engine.Sim(params, p.position, p.radius, p.lx, p.ly, p.lz, precision=engine.PREC_FP64)
+        out = engine.Output(g, "gpu", units, volume_fraction=p.vf, directory=d, version="reference-sources")
+        ds = float(F["dstrain"][0])
+        for k in range(1, int(F["outputs"][0]) + 1):
+            g.advance(strain_end=k * ds)
+            out.write()
+        out.close()
+        g.close()
+        with open(os.path.join(d, "pst_gpu.dat")) as f:
+            got = f.read()
+    _compare("pst", txt["pst"], got)
