@@ -122,10 +122,11 @@ static void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t sme
 // triangle lands on the parent's).  The children's parameters are fetched
 // by one thread each, up to ASM_CHILDREN at a time.
 constexpr int ASM_CHILDREN = 32;
-constexpr int ASM_BATCH = 4;       // rows per thread and pass of a child's column
+constexpr int ASM_BATCH = 8;       // rows per thread and pass of a child's column
+constexpr int ASM_THREADS = 128;   // threads of the CTA-per-column form
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_assemble(const int *__restrict__ col_tasks, const int *__restrict__ sn_n,
+__global__ void __launch_bounds__(ASM_THREADS) k_assemble(const int *__restrict__ col_tasks, const int *__restrict__ sn_n,
                                                   const int *__restrict__ sn_m, const int *__restrict__ sn_ld,
                                                   const int64_t *__restrict__ sn_off,
                                                   const int *__restrict__ child_off,
@@ -1581,7 +1582,8 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 				           (const int64_t *)D.cinv_off, (const int *)D.cinv, (const int *)D.sn_rows_off,
 				           (const int *)D.cfwd, F.arena, D.dof);
 			} else {
-				launch_pdl(k_assemble<T>, L.count, 256, assemble_smem<T>(D), st, (const int *)D.col_tasks+2*L.off,
+				launch_pdl(k_assemble<T>, L.count, ASM_THREADS, assemble_smem<T>(D), st,
+				           (const int *)D.col_tasks+2*L.off,
 				           (const int *)D.sn_n, (const int *)D.sn_m, (const int *)D.sn_ld,
 				           (const int64_t *)D.sn_off, (const int *)D.child_off, (const int *)D.children,
 				           (const int64_t *)D.cinv_off, (const int *)D.cinv, (const int *)D.sn_rows_off,

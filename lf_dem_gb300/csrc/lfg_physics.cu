@@ -366,14 +366,18 @@ __global__ void k_cell_fill(int n, const int *__restrict__ cell_of, const int *_
 	list[start[c]+k] = i;
 }
 
+// A particle's cell-ordered FP64 record: position and radius (32 bytes)
+struct __align__(32) PRec { double x, y, z, w; };
+
 // Each cell's particle list sorted (deterministic neighbour order), one warp
 // per cell: up to 32 members sorted in registers (bitonic), larger cells by
 // lane 0 in place.  The warp then writes the cell-ordered records (x, y, z,
-// radius) of its members, so the neighbour searches read a cell's particles
-// as contiguous 32-byte records (two vector loads each).
+// radius) of its members, in FP64 and rounded to FP32, so the neighbour
+// searches read a cell's particles as contiguous records (one 16-byte vector
+// load each for the FP32 prefilter, two for the FP64 test).
 __global__ void k_cell_sort(int ncell, const int *__restrict__ start, const int *__restrict__ count,
                             int *__restrict__ list, const double *__restrict__ pos, const double *__restrict__ radius,
-                            double *__restrict__ rec)
+                            double *__restrict__ rec, float *__restrict__ rec32)
 {
 	const int c = (blockIdx.x*blockDim.x+threadIdx.x) >> 5, lane = threadIdx.x & 31;
 	if (c >= ncell) return;   // whole warps
@@ -393,9 +397,71 @@ __global__ void k_cell_sort(int ncell, const int *__restrict__ start, const int 
 	}
 	for (int k = s+lane; k < s+m; k += 32) {
 		int j = list[k];
-		double4 r = make_double4(pos[3*j], pos[3*j+1], pos[3*j+2], radius[j]);
-		reinterpret_cast<double4 *>(rec)[k] = r;
+		const PRec r = {pos[3*j], pos[3*j+1], pos[3*j+2], radius[j]};
+		reinterpret_cast<PRec *>(rec)[k] = r;
+		reinterpret_cast<float4 *>(rec32)[k] = make_float4((float)r.x, (float)r.y, (float)r.z, (float)r.w);
 	}
+}
+
+// FP32 prefilter of the neighbour tests.  The decision "|d|^2 < range^2"
+// must be the FP64 one bit for bit, and the FP64 arithmetic (periodic wrap,
+// range, squares) runs on GB300's narrow FP64 pipe.  So each test is first
+// made from FP32-rounded records: every component of d is then within 8
+// roundings of the box size of its FP64 value (positions, the wrap and the
+// Lees-Edwards shift), so |d|^2 is within 2 sqrt(3) r e + O(e^2) of it near
+// |d| = r, and the FP32 range within a few roundings of r; prefilter_tol
+// bounds both with a factor 4 to spare.  Outside [r^2 - tol, r^2 + tol] the
+// FP32 answer is the FP64 one; inside, the exact FP64 test decides.  (A
+// different wrap decision in FP32 only happens at |d_x| ~ L/2, far beyond
+// any range: out either way.)
+struct Box32 { float lx, ly, lz, lxh, lyh, lzh, sx, sy, sz, lmax; int twodim; };
+__device__ __forceinline__ Box32 box32(const DevParams &P, const double *sd)
+{
+	Box32 B;
+	B.lx = (float)P.lx; B.ly = (float)P.ly; B.lz = (float)P.lz;
+	B.lxh = (float)P.lx_half; B.lyh = (float)P.ly_half; B.lzh = (float)P.lz_half;
+	B.sx = (float)sd[0]; B.sy = (float)sd[1]; B.sz = (float)sd[2];
+	B.lmax = fmaxf(fmaxf(B.lx, fmaxf(B.ly, B.lz)), fmaxf(fabsf(B.sx), fmaxf(fabsf(B.sy), fabsf(B.sz))));
+	B.twodim = P.twodim;
+	return B;
+}
+// periodize_diff in FP32, then |d|^2
+__device__ __forceinline__ float dist2_32(const Box32 &B, float dx, float dy, float dz)
+{
+	if (dz > B.lzh) { dz -= B.lz; dx -= B.sx; dy -= B.sy; dz -= B.sz; }
+	else if (dz < -B.lzh) { dz += B.lz; dx += B.sx; dy += B.sy; dz += B.sz; }
+	while (dx > B.lxh) dx -= B.lx;
+	while (dx < -B.lxh) dx += B.lx;
+	if (!B.twodim) {
+		if (dy > B.lyh) dy -= B.ly;
+		else if (dy < -B.lyh) dy += B.ly;
+	}
+	return dx*dx+dy*dy+dz*dz;
+}
+// FP32 bounds [lo, hi] of inter_range(ri, rj) + extra: both branches of the
+// radius-ratio test when the ratio is within 1e-5 of a branch point
+__device__ __forceinline__ void range32(const DevParams &P, float ri, float rj, float extra, float &lo, float &hi)
+{
+	if (P.interaction_range >= 0) {
+		lo = hi = (float)P.interaction_range*0.5f*(ri+rj)+extra;
+		return;
+	}
+	const float g = (float)P.lub_max_gap;
+	const float a = (2.0f+g)*0.5f*(ri+rj), b = ri+rj+g*fminf(ri, rj);
+	const float q = ri/rj;
+	const bool ina = q < 2.0f && q > 0.5f;
+	const bool near = fabsf(q-2.0f) < 2e-5f || fabsf(q-0.5f) < 1e-5f;
+	const float r = ina ? a : b;
+	lo = (near ? fminf(a, b) : r)+extra;
+	hi = (near ? fmaxf(a, b) : r)+extra;
+}
+// -1: out, 1: in, 0: undecided (the FP64 test decides)
+__device__ __forceinline__ int prefilter(const Box32 &B, float d2, float lo, float hi)
+{
+	const float tol = 1.6e-5f*B.lmax*hi+1e-6f*hi*hi;
+	if (d2 < lo*lo-tol) return 1;
+	if (d2 > hi*hi+tol) return -1;
+	return 0;
 }
 
 // Candidate pairs within the superset range (range + skin (a_i+a_j)/2), one
@@ -407,14 +473,16 @@ __global__ void k_cell_sort(int ncell, const int *__restrict__ start, const int 
 // every j > i from the particle arrays.
 __global__ void k_candidates(DevParams P, CellView C, const DevClock *__restrict__ clk,
                              const double *__restrict__ pos, const double *__restrict__ radius,
-                             const double *__restrict__ rec, int *__restrict__ count, const int *__restrict__ ptr,
-                             int *__restrict__ cand)
+                             const double *__restrict__ rec, const float *__restrict__ rec32,
+                             int *__restrict__ count, const int *__restrict__ ptr, int *__restrict__ cand)
 {
 	const int i = (int)(((int64_t)blockIdx.x*blockDim.x+threadIdx.x) >> 5), lane = threadIdx.x & 31;
 	if (i >= C.n) return;   // whole warps
 	const double *sd = clk->shear_disp;
 	const v3 pi = ld3(pos+3*i);
 	const double ri = radius[i];
+	const Box32 B = box32(P, sd);
+	const float pxf = (float)pi.x, pyf = (float)pi.y, pzf = (float)pi.z, rif = (float)ri, skf = (float)P.skin;
 	const int base = ptr ? ptr[i] : 0;
 	int c = 0;   // hits so far (the same in every lane)
 	auto scan = [&](int s, int e, bool brute) {
@@ -431,11 +499,23 @@ __global__ void k_candidates(DevParams P, CellView C, const DevClock *__restrict
 					rj = radius[j];
 				} else {
 					j = C.list[k];
-					const double4 r = reinterpret_cast<const double4 *>(rec)[k];
-					pj = V(r.x, r.y, r.z);
-					rj = r.w;
+					if (j > i) {
+						// FP32 prefilter; the FP64 record only when it cannot decide
+						const float4 f = reinterpret_cast<const float4 *>(rec32)[k];
+						float lo, hi;
+						range32(P, rif, f.w, skf*0.5f*(rif+f.w), lo, hi);
+						const int v = prefilter(B, dist2_32(B, f.x-pxf, f.y-pyf, f.z-pzf), lo, hi);
+						if (v != 0) {
+							hit = v > 0;
+							j = v > 0 ? j : -1;
+						} else {
+							const PRec r = reinterpret_cast<const PRec *>(rec)[k];
+							pj = V(r.x, r.y, r.z);
+							rj = r.w;
+						}
+					}
 				}
-				if (j > i) {
+				if (j > i && (brute || !hit)) {
 					v3 d = vsub(pj, pi);
 					periodize_diff(P, sd, d);
 					double rs = inter_range(P, ri, rj)+P.skin*0.5*(ri+rj);
@@ -491,8 +571,8 @@ __global__ void k_candidates(DevParams P, CellView C, const DevClock *__restrict
 // (i, j > i) within the interaction range must be in the superset.  One CTA
 // per home cell: the records of the cells its particles search are staged in
 // shared memory (in passes of CHK_CAP), and one warp per home particle i
-// tests them, its superset row (the sorted candidate list) held in lanes and
-// matched by shuffles.  The staged cells are a superset of those
+// tests them (FP32 prefilter, FP64 where it cannot decide), its superset row
+// (the sorted candidate list) held in lanes and matched by shuffles.  The staged cells are a superset of those
 // for_neighbours visits from any particle of the home cell: a Lees-Edwards
 // shifted row takes five x (and, with a y shift, five y) cells around the
 // shifted cell of the home cell's centre, since a particle's shifted cell is
@@ -500,17 +580,18 @@ __global__ void k_candidates(DevParams P, CellView C, const DevClock *__restrict
 constexpr int CHK_CAP = 640;   // staged records per pass
 constexpr int CHK_SLOTS = 75;  // 3 rows x 5 x 5 cells at most
 __global__ void __launch_bounds__(128) k_check_cells(DevParams P, CellView C, DevClock *__restrict__ clk,
-                                                     const double *__restrict__ rec, const int *__restrict__ row_ptr,
-                                                     const int *__restrict__ cand)
+                                                     const double *__restrict__ rec, const float *__restrict__ rec32,
+                                                     const int *__restrict__ row_ptr, const int *__restrict__ cand)
 {
-	__shared__ double4 srec[CHK_CAP];
-	__shared__ int sidx[CHK_CAP];
+	__shared__ float4 srec[CHK_CAP];
+	__shared__ int sidx[CHK_CAP], skey[CHK_CAP];
 	__shared__ int cs[CHK_SLOTS], cpre[CHK_SLOTS+1];
 	const int h = blockIdx.x;
 	const int hs = C.start[h], hn = C.count[h];
 	if (hn == 0) return;   // the same in every thread
 	const int hx = h%C.ncx, hy = (h/C.ncx)%C.ncy, hz = h/(C.ncx*C.ncy);
 	const double *sd = clk->shear_disp;
+	const Box32 B = box32(P, sd);
 	const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
 	if (t < CHK_SLOTS) {
 		// slot (row dz, y offset, x offset) -> cell and member count (0 if unused)
@@ -570,14 +651,14 @@ __global__ void __launch_bounds__(128) k_check_cells(DevParams P, CellView C, De
 				if (cpre[mid] <= g) lo = mid; else hi = mid-1;
 			}
 			const int k = cs[lo]+g-cpre[lo];
-			srec[f] = reinterpret_cast<const double4 *>(rec)[k];
+			srec[f] = reinterpret_cast<const float4 *>(rec32)[k];
 			sidx[f] = C.list[k];
+			skey[f] = k;
 		}
 		__syncthreads();
 		for (int hp = warp; hp < hn; hp += blockDim.x >> 5) {
 			const int i = C.list[hs+hp];
-			const double4 r4 = reinterpret_cast<const double4 *>(rec)[hs+hp];
-			const v3 pi = V(r4.x, r4.y, r4.z);
+			const float4 p4 = reinterpret_cast<const float4 *>(rec32)[hs+hp];
 			const int lo = row_ptr[i], len = row_ptr[i+1]-lo;
 			const int rv0 = lane < len ? cand[lo+lane] : -2;
 			for (int fb = 0; fb < fn; fb += 32) {
@@ -586,11 +667,21 @@ __global__ void __launch_bounds__(128) k_check_cells(DevParams P, CellView C, De
 				if (f < fn) {
 					const int j = sidx[f];
 					if (j > i) {
-						const double4 r = srec[f];
-						v3 d = vsub(V(r.x, r.y, r.z), pi);
-						periodize_diff(P, sd, d);
-						double range = inter_range(P, r4.w, r.w);
-						if (vsq(d) < range*range) need = j;
+						// FP32 prefilter; the FP64 records only when it cannot decide
+						const float4 q = srec[f];
+						float rlo, rhi;
+						range32(P, p4.w, q.w, 0.0f, rlo, rhi);
+						const int v = prefilter(B, dist2_32(B, q.x-p4.x, q.y-p4.y, q.z-p4.z), rlo, rhi);
+						if (v > 0) {
+							need = j;
+						} else if (v == 0) {
+							const PRec a = reinterpret_cast<const PRec *>(rec)[hs+hp];
+							const PRec r = reinterpret_cast<const PRec *>(rec)[skey[f]];
+							v3 d = vsub(V(r.x, r.y, r.z), V(a.x, a.y, a.z));
+							periodize_diff(P, sd, d);
+							double range = inter_range(P, a.w, r.w);
+							if (vsq(d) < range*range) need = j;
+						}
 					}
 				}
 				if (!__any_sync(PFULL, need >= 0)) continue;
@@ -1723,7 +1814,7 @@ void phys_cells(DevSim &S, double, cudaStream_t st)
 	LFG_CUDA(cudaMemsetAsync(S.cand_count, 0, sizeof(int)*ncell, st));
 	k_cell_fill<<<blocks_for(S.n, 128), 128, 0, st>>>(S.n, S.cell_of, S.cell_start, S.cand_count, S.cell_list);
 	k_cell_sort<<<blocks_for((int64_t)32*ncell, 128), 128, 0, st>>>(ncell, S.cell_start, S.cell_count, S.cell_list,
-	                                                                 S.pos, S.radius, S.cell_rec);
+	                                                                 S.pos, S.radius, S.cell_rec, S.cell_rec32);
 	S.launches += 4;
 }
 
@@ -1731,7 +1822,7 @@ void phys_candidates(DevSim &S, cudaStream_t st, int *h_total)
 {
 	CellView C = view(S);
 	k_candidates<<<blocks_for((int64_t)32*S.n, 128), 128, 0, st>>>(S.P, C, S.clock, S.pos, S.radius, S.cell_rec,
-	                                                                S.cand_count, nullptr, nullptr);
+	                                                                S.cell_rec32, S.cand_count, nullptr, nullptr);
 	k_scan<<<1, 1024, 0, st>>>(S.n, S.cand_count, S.cand_ptr, nullptr);
 	LFG_CUDA(cudaMemcpyAsync(h_total, S.cand_ptr+S.n, sizeof(int), cudaMemcpyDeviceToHost, st));
 	LFG_CUDA(cudaStreamSynchronize(st));
@@ -1741,7 +1832,7 @@ void phys_candidates(DevSim &S, cudaStream_t st, int *h_total)
 		LFG_CUDA(cudaMalloc((void **)&S.cand, sizeof(int)*S.cand_cap));
 	}
 	k_candidates<<<blocks_for((int64_t)32*S.n, 128), 128, 0, st>>>(S.P, C, S.clock, S.pos, S.radius, S.cell_rec,
-	                                                                S.cand_count, S.cand_ptr, S.cand);
+	                                                                S.cell_rec32, S.cand_count, S.cand_ptr, S.cand);
 	S.launches += 3;
 }
 
@@ -1752,7 +1843,8 @@ void phys_check_superset(DevSim &S, cudaStream_t st)
 		k_check_superset<<<blocks_for((S.P.twodim ? 9 : 27)*S.n, 256), 256, 0, st>>>(S.P, C, S.clock, S.pos, S.radius,
 		                                                                           S.row_ptr, S.pairs);
 	else
-		k_check_cells<<<S.ncx*S.ncy*S.ncz, 128, 0, st>>>(S.P, C, S.clock, S.cell_rec, S.row_ptr, S.cand);
+		k_check_cells<<<S.ncx*S.ncy*S.ncz, 128, 0, st>>>(S.P, C, S.clock, S.cell_rec, S.cell_rec32, S.row_ptr,
+		                                                 S.cand);
 	S.launches++;
 }
 

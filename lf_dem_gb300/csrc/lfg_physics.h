@@ -102,6 +102,7 @@ struct DevSim {
 	double csx = 0, csy = 0, csz = 0;
 	int *cell_of = nullptr, *cell_start = nullptr, *cell_count = nullptr, *cell_list = nullptr;
 	double *cell_rec = nullptr;        // 4n: (x, y, z, radius) of cell_list[k] at 4k (cell order)
+	float *cell_rec32 = nullptr;       // 4n: the same rounded to FP32 (neighbour-test prefilter)
 	int *cand_count = nullptr, *cand_ptr = nullptr, *cand = nullptr;
 	int cand_cap = 0;
 	int ncell_cap = 0;

@@ -245,6 +245,7 @@ Sim::Sim(const lfg_params &p, const lfg_options &o, int n, const double *pos, co
 	int ncell = S_.ncx*S_.ncy*S_.ncz;
 	dalloc(S_.cell_of, n, st_); dalloc(S_.cell_count, ncell, st_); dalloc(S_.cell_start, ncell+1, st_); dalloc(S_.cell_list, n, st_);
 	dalloc(S_.cell_rec, 4*(size_t)n, st_);
+	dalloc(S_.cell_rec32, 4*(size_t)n, st_);
 	dalloc(S_.cand_count, std::max(n, ncell), st_); dalloc(S_.cand_ptr, n+1, st_);
 	// a monolayer's in-plane unknowns (x, z, rotation about y) decouple from
 	// the others: solve them alone unless asked for LF_DEM's 6x6 blocks
@@ -262,7 +263,7 @@ Sim::~Sim()
 	void *p[] = {S_.clock, S_.pos, S_.radius, S_.vel, S_.ang, S_.vel_pred, S_.ang_pred, S_.u_inf, S_.na, S_.na_disp,
 	             S_.angle, psi_, S_.vc,
 	             S_.fc, S_.rhs, S_.sol, S_.sc, S_.sc_tot, S_.pairs, S_.pconst, S_.row_ptr, S_.col_ptr, S_.col_idx,
-	             S_.blk_scratch, S_.pair_scratch, S_.cell_of, S_.cell_start, S_.cell_count, S_.cell_list, S_.cell_rec,
+	             S_.blk_scratch, S_.pair_scratch, S_.cell_of, S_.cell_start, S_.cell_count, S_.cell_list, S_.cell_rec, S_.cell_rec32,
 	             S_.cand_count, S_.cand_ptr, S_.cand, d_err_};
 	for (void *q : p) if (q) cudaFree(q);
 	if (h_clock_) cudaFreeHost(h_clock_);
