@@ -753,8 +753,9 @@ def main():
         pass
     roof = {"bound": "tensor", "achieved": achieved, "peak": bf16s, "unit": "TFLOP/s",
             "frac": achieved / bf16s, "traffic": traffic,
-            "traffic_source": "profile-derived: DRAM bytes of the factorisation kernels per factorisation, "
-                              "from the ncu launch list in profiles/ (not measured in this run)",
+            "traffic_source": "profile-derived: DRAM bytes of the factorisation kernels of one factorisation, "
+                              "cold caches (profiles/factorisation_and_solve_traffic_n4096_fp32.md; not measured "
+                              "in this run)",
             "kernel": "FP32 multifrontal factorisation graph: k_assemble, k_scatter, k_diag, k_trsm, k_update "
                       "(CUDA cores) and k_syrk_tc (Schur complements, tcgen05 3xTF32)",
             "peak_source": f"bf16_tflops_sustained ({src}); the panel steps run on FP32 CUDA cores, "
