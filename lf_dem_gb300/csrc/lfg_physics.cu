@@ -1862,8 +1862,10 @@ void phys_pairs_update(DevSim &S, int mode, int in_predictor, bool zero_dt, cuda
 {
 	k_clear_sliding<<<1, 1, 0, st>>>(S.clock);
 	if (S.npairs)
-		k_pairs_update<<<blocks_for(S.npairs, 256), 256, 0, st>>>(S.P, S.npairs, S.clock, S.pos, S.vel, S.ang, S.pairs,
-		                                                          S.pconst, mode, in_predictor, zero_dt ? 1 : 0);
+		// 64 threads per CTA: one thread per pair holds a whole pair record, so
+		// small CTAs spread the ~10^4 pairs over every SM
+		k_pairs_update<<<blocks_for(S.npairs, 64), 64, 0, st>>>(S.P, S.npairs, S.clock, S.pos, S.vel, S.ang, S.pairs,
+		                                                        S.pconst, mode, in_predictor, zero_dt ? 1 : 0);
 	k_finish_sliding<<<1, 1, 0, st>>>(S.clock);
 	S.launches += 3;
 }
@@ -1871,7 +1873,7 @@ void phys_pairs_update(DevSim &S, int mode, int in_predictor, bool zero_dt, cuda
 void phys_blocks(DevSim &S, double *dbl, double *odbl, cudaStream_t st)
 {
 	if (S.npairs)
-		k_pair_blocks<<<blocks_for(S.npairs, 128), 128, 0, st>>>(S.P, S.npairs, S.pairs, S.pconst, odbl, S.blk_scratch);
+		k_pair_blocks<<<blocks_for(S.npairs, 64), 64, 0, st>>>(S.P, S.npairs, S.pairs, S.pconst, odbl, S.blk_scratch);
 	k_dblocks<<<blocks_for(15*(int64_t)S.n, 128), 128, 0, st>>>(S.P, S.n, S.radius, S.row_ptr, S.col_ptr, S.col_idx,
 	                                                S.blk_scratch, dbl);
 	S.launches += 2;
