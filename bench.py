@@ -255,6 +255,7 @@ def run_e2e(E, packing, precision, steps, device):
     rad = np.ascontiguousarray(packing.radius)
     t0 = time.perf_counter()
     g = E.Sim(params, pos, rad, packing.lx, packing.ly, packing.lz, precision=precision, device=device)
+    t_created = time.perf_counter()
     L = E.load()
     outp = np.zeros(3 * len(rad))
     outv = np.zeros(3 * len(rad))
@@ -268,7 +269,10 @@ def run_e2e(E, packing, precision, steps, device):
     n = len(rad)
     return {"value": n * steps / (t1 - t0), "unit": "particle-steps/s",
             "h2d_bytes_per_step": int((pos.nbytes + rad.nbytes) / steps),
-            "d2h_bytes_per_step": int(outp.nbytes + outv.nbytes + 8 * 6),
+            # positions and velocities, and lfg_sim_get_scalars: the clock (240 B), the
+            # per-component stress totals (11 x 6 doubles) and the interaction counts
+            "d2h_bytes_per_step": int(outp.nbytes + outv.nbytes + 240 + 11 * 6 * 8 + 16),
+            "create_ms": 1e3 * (t_created - t0), "steps_ms": 1e3 * (t1 - t_created),
             "note": "includes creation (H2D of the configuration, symbolic analysis, graph capture)"}
 
 

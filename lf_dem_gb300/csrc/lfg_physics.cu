@@ -1778,6 +1778,26 @@ __global__ void k_merge(int np, int n, const int *__restrict__ new_row_ptr, cons
 	(void)np;
 }
 
+// Interaction counts of the current state (lfg_sim_scalars: interactions,
+// contacts, lubricated pairs, pairs with a resistance): one thread per pair
+// slot, a warp sum by ballot, one atomic per warp and count.  out[4] must
+// start at zero.
+__global__ void k_pair_counts(int np, int lub_on, const DPair *__restrict__ pairs, int *__restrict__ out)
+{
+	const int t = blockIdx.x*blockDim.x+threadIdx.x;
+	const int f = t < np ? pairs[t].flags : 0;
+	const bool inter = f & PF_INTER;
+	const bool res = lub_on ? ((f & PF_DASHPOT) || (f & PF_LUB)) : (f & PF_DASHPOT);
+	const unsigned b0 = __ballot_sync(PFULL, inter), b1 = __ballot_sync(PFULL, inter && (f & PF_CONTACT));
+	const unsigned b2 = __ballot_sync(PFULL, inter && (f & PF_LUB)), b3 = __ballot_sync(PFULL, inter && res);
+	if ((threadIdx.x & 31) == 0) {
+		if (b0) atomicAdd(out, __popc(b0));
+		if (b1) atomicAdd(out+1, __popc(b1));
+		if (b2) atomicAdd(out+2, __popc(b2));
+		if (b3) atomicAdd(out+3, __popc(b3));
+	}
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
@@ -2110,6 +2130,14 @@ void phys_sticky_status(const int *status, int *err, cudaStream_t st)
 void phys_merge_pairs(DevSim &S, const DPair *old_pairs, const int *old_row_ptr, int old_n, cudaStream_t st)
 {
 	k_merge<<<blocks_for(S.n, 128), 128, 0, st>>>(S.npairs, S.n, S.cand_ptr, S.cand, old_pairs, old_row_ptr, old_n, S.pairs);
+	S.launches++;
+}
+
+void phys_pair_counts(DevSim &S, int *d_out, cudaStream_t st)
+{
+	LFG_CUDA(cudaMemsetAsync(d_out, 0, 4*sizeof(int), st));
+	if (S.npairs)
+		k_pair_counts<<<blocks_for(S.npairs, 256), 256, 0, st>>>(S.npairs, S.P.lub_on ? 1 : 0, S.pairs, d_out);
 	S.launches++;
 }
 

@@ -154,6 +154,8 @@ void phys_set_dt(DevSim &S, double dt, cudaStream_t st);
 void phys_sticky_status(const int *status, int *err, cudaStream_t st);
 // merge: for each new superset pair find the old record (binary search in the
 // old row) and copy it, else initialise an empty record
+// interactions, contacts, lubricated pairs, pairs with a resistance of the current state (4 ints)
+void phys_pair_counts(DevSim &S, int *d_out, cudaStream_t st);
 void phys_merge_pairs(DevSim &S, const DPair *old_pairs, const int *old_row_ptr, int old_n,
                       cudaStream_t st);
 

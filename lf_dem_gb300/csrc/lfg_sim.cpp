@@ -109,6 +109,7 @@ private:
 	bool firsttime_ = true;
 	DevClock *h_clock_ = nullptr;
 	int *d_err_ = nullptr, *h_err_ = nullptr;
+	int *d_counts_ = nullptr;   // interaction counts (lfg_sim_scalars)
 	std::vector<double> h_pos_;
 	int symbolic_runs_ = 0;
 	// Brownian force: draws so far, psi work vector, a force given for the
@@ -219,6 +220,7 @@ Sim::Sim(const lfg_params &p, const lfg_options &o, int n, const double *pos, co
 	dalloc(S_.sc, (size_t)NSC*6*n, st_); dalloc(S_.sc_tot, (size_t)NSC*6+12*(size_t)n, st_);
 	dalloc(S_.row_ptr, n+1, st_); dalloc(S_.col_ptr, n+1, st_);
 	dalloc(d_err_, 1, st_);
+	dalloc(d_counts_, 4, st_);
 	LFG_CUDA(cudaMallocHost((void **)&h_clock_, sizeof(DevClock)));
 	LFG_CUDA(cudaMallocHost((void **)&h_err_, sizeof(int)));
 	LFG_CUDA(cudaMemcpyAsync(S_.pos, pos, sizeof(double)*3*n, cudaMemcpyHostToDevice, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
@@ -264,7 +266,7 @@ Sim::~Sim()
 	             S_.angle, psi_, S_.vc,
 	             S_.fc, S_.rhs, S_.sol, S_.sc, S_.sc_tot, S_.pairs, S_.pconst, S_.row_ptr, S_.col_ptr, S_.col_idx,
 	             S_.blk_scratch, S_.pair_scratch, S_.cell_of, S_.cell_start, S_.cell_count, S_.cell_list, S_.cell_rec, S_.cell_rec32,
-	             S_.cand_count, S_.cand_ptr, S_.cand, d_err_};
+	             S_.cand_count, S_.cand_ptr, S_.cand, d_err_, d_counts_};
 	for (void *q : p) if (q) cudaFree(q);
 	if (h_clock_) cudaFreeHost(h_clock_);
 	if (h_err_) cudaFreeHost(h_err_);
@@ -696,7 +698,15 @@ void Sim::output_snapshot(OutputSnapshot &o)
 
 void Sim::scalars(lfg_sim_scalars *o)
 {
-	pull_clock();
+	// the clock, the per-component stress totals and the interaction counts,
+	// read back with one synchronisation
+	std::vector<double> tot(NSC*6);
+	int cnt[4];
+	LFG_CUDA(cudaMemcpyAsync(h_clock_, S_.clock, sizeof(DevClock), cudaMemcpyDeviceToHost, st_));
+	LFG_CUDA(cudaMemcpyAsync(tot.data(), S_.sc_tot, sizeof(double)*6*NSC, cudaMemcpyDeviceToHost, st_));
+	phys_pair_counts(S_, d_counts_, st_);
+	LFG_CUDA(cudaMemcpyAsync(cnt, d_counts_, sizeof cnt, cudaMemcpyDeviceToHost, st_));
+	LFG_CUDA(cudaStreamSynchronize(st_));
 	std::memset(o, 0, sizeof *o);
 	const DevClock &K = *h_clock_;
 	o->time = K.time; o->strain = K.strain; o->shear_rate = K.shear_rate; o->dt = K.dt;
@@ -705,8 +715,6 @@ void Sim::scalars(lfg_sim_scalars *o)
 	o->rate_prop_shearstress = K.rate_prop; o->rate_indep_shearstress = K.rate_indep;
 	o->total_num_timesteps = K.steps;
 	// System::calcStress (Stress.cpp:342-384) from the per-component totals
-	std::vector<double> tot(NSC*6);
-	LFG_CUDA(cudaMemcpyAsync(tot.data(), S_.sc_tot, sizeof(double)*6*NSC, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
 	const DevParams &P = S_.P;
 	bool has[NSC] = {(bool)P.lub_on, (bool)P.lub_on, (bool)P.lub_on, (bool)P.lub_on,
 	                 P.lub_on && P.repulsiveforce, P.control == 0, P.control == 1, P.control == 1,
@@ -730,16 +738,11 @@ void Sim::scalars(lfg_sim_scalars *o)
 		o->N1 = (s[0]-s[5])/K.shear_rate;
 		o->N2 = (s[5]-s[4])/K.shear_rate;
 	}
-	std::vector<DPair> pairs(S_.npairs);
-	if (S_.npairs) LFG_CUDA(cudaMemcpyAsync(pairs.data(), S_.pairs, sizeof(DPair)*S_.npairs, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
-	for (const DPair &q : pairs) {
-		if (!(q.flags & PF_INTER)) continue;
-		o->n_pairs++;
-		if (q.flags & PF_CONTACT) o->n_contacts++;
-		if (q.flags & PF_LUB) o->n_lub++;
-		bool res = P.lub_on ? ((q.flags & PF_DASHPOT) || (q.flags & PF_LUB)) : (q.flags & PF_DASHPOT);
-		if (res) o->n_resistance_pairs++;
-	}
+	// interaction counts, counted on the device (not the pair records copied here)
+	o->n_pairs = cnt[0];
+	o->n_contacts = cnt[1];
+	o->n_lub = cnt[2];
+	o->n_resistance_pairs = cnt[3];
 	o->n_superset_pairs = S_.npairs;
 	o->n_symbolic_runs = symbolic_runs_;
 	o->last_refine_iters = solver_->last_iters();
@@ -765,11 +768,11 @@ void Sim::particles(double *pos, double *vel, double *ang, double *na_vel, doubl
 
 int Sim::num_pairs()
 {
-	std::vector<DPair> pairs(S_.npairs);
-	if (S_.npairs) LFG_CUDA(cudaMemcpyAsync(pairs.data(), S_.pairs, sizeof(DPair)*S_.npairs, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
-	int c = 0;
-	for (const DPair &q : pairs) c += (q.flags & PF_INTER) ? 1 : 0;
-	return c;
+	int cnt[4];
+	phys_pair_counts(S_, d_counts_, st_);
+	LFG_CUDA(cudaMemcpyAsync(cnt, d_counts_, sizeof cnt, cudaMemcpyDeviceToHost, st_));
+	LFG_CUDA(cudaStreamSynchronize(st_));
+	return cnt[0];
 }
 
 // active contacts with their springs (System::getContacts, System.cpp:306-320),

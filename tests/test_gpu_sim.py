@@ -109,3 +109,19 @@ def test_thin_skin_rebuilds_keep_pair_lists(oracle, engine, params, n, vf, seed,
         assert err <= 1e-10 * max(p.lx, p.lz), k
     assert g.scalars()["n_symbolic_runs"] >= 3
     g.close()
+
+
+@pytest.mark.parametrize("params", [RATE_PARAMS, STRESS_PARAMS], ids=["rate", "stress"])
+def test_scalar_interaction_counts(engine, params):
+    """lfg_sim_scalars' interaction counts (a device reduction) against the interaction list."""
+    p = make_packing(300, 0.52, 41)
+    g = engine.Sim(params, p.position, p.radius, p.lx, p.ly, p.lz)
+    for _ in range(3):
+        g.run(2)
+        s = g.scalars()
+        pg = g.pairs()
+        assert s["n_pairs"] == len(pg)
+        assert s["n_contacts"] == int(np.count_nonzero(pg["contact_active"]))
+        assert s["n_lub"] == int(np.count_nonzero(pg["lub_active"]))
+        assert 0 < s["n_resistance_pairs"] <= s["n_pairs"]
+    g.close()
