@@ -752,12 +752,17 @@ void Sim::scalars(lfg_sim_scalars *o)
 void Sim::particles(double *pos, double *vel, double *ang, double *na_vel, double *na_ang)
 {
 	int n = S_.n;
-	if (pos) LFG_CUDA(cudaMemcpyAsync(pos, S_.pos, sizeof(double)*3*n, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
-	if (vel) LFG_CUDA(cudaMemcpyAsync(vel, S_.vel, sizeof(double)*3*n, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
-	if (ang) LFG_CUDA(cudaMemcpyAsync(ang, S_.ang, sizeof(double)*3*n, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+	// the copies share one synchronisation
+	if (pos) LFG_CUDA(cudaMemcpyAsync(pos, S_.pos, sizeof(double)*3*n, cudaMemcpyDeviceToHost, st_));
+	if (vel) LFG_CUDA(cudaMemcpyAsync(vel, S_.vel, sizeof(double)*3*n, cudaMemcpyDeviceToHost, st_));
+	if (ang) LFG_CUDA(cudaMemcpyAsync(ang, S_.ang, sizeof(double)*3*n, cudaMemcpyDeviceToHost, st_));
+	std::vector<double> na;
 	if (na_vel || na_ang) {
-		std::vector<double> na(6*n);
-		LFG_CUDA(cudaMemcpyAsync(na.data(), S_.na, sizeof(double)*6*n, cudaMemcpyDeviceToHost, st_)); LFG_CUDA(cudaStreamSynchronize(st_));
+		na.resize(6*(size_t)n);
+		LFG_CUDA(cudaMemcpyAsync(na.data(), S_.na, sizeof(double)*6*n, cudaMemcpyDeviceToHost, st_));
+	}
+	LFG_CUDA(cudaStreamSynchronize(st_));
+	if (na_vel || na_ang) {
 		for (int i = 0; i < n; i++)
 			for (int e = 0; e < 3; e++) {
 				if (na_vel) na_vel[3*i+e] = na[6*i+e];
