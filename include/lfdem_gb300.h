@@ -359,7 +359,10 @@ typedef struct {
 	                            upload, plus the capture of the new factorisation and solve
 	                            graphs after them */
 	int rebuilds;            /* number of those rebuilds */
-	int pad_;
+	int run_steps;           /* steps of the last lfg_sim_run */
+	double run_ms;           /* device duration of the last lfg_sim_run as a whole: CUDA
+	                            events on the simulation's stream before its first step and
+	                            after its last, the gaps between the steps included */
 } lfg_sim_timing;
 int lfg_sim_get_timing(lfg_sim *s, lfg_sim_timing *out);
 

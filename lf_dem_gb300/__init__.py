@@ -130,7 +130,8 @@ class BatchStats(C.Structure):
 
 class SimTiming(C.Structure):
     _fields_ = [("ms", C.c_double * 8), ("launches", C.c_int64), ("factor_flops", C.c_double),
-                ("solve_bytes", C.c_double), ("rebuild_ms", C.c_double), ("rebuilds", C.c_int), ("pad_", C.c_int)]
+                ("solve_bytes", C.c_double), ("rebuild_ms", C.c_double), ("rebuilds", C.c_int), ("run_steps", C.c_int),
+                ("run_ms", C.c_double)]
 
 
 # Every extern "C" symbol declared in include/lfdem_gb300.h.
@@ -658,7 +659,8 @@ class Sim:
         t = SimTiming()
         load().lfg_sim_get_timing(self.h, C.byref(t))
         return {"ms": list(t.ms), "launches": t.launches, "factor_flops": t.factor_flops,
-                "solve_bytes": t.solve_bytes, "rebuild_ms": t.rebuild_ms, "rebuilds": t.rebuilds}
+                "solve_bytes": t.solve_bytes, "rebuild_ms": t.rebuild_ms, "rebuilds": t.rebuilds,
+                "run_steps": t.run_steps, "run_ms": t.run_ms}
 
 
 def footprint_estimate(n: int, precision: int = PREC_FP32_REFINE) -> int:

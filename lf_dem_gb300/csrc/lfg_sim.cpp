@@ -49,6 +49,7 @@ public:
 	int force_component(int comp, double *out);
 	void force_component_noalloc(int comp, double *d_out, int device);
 	void timing(lfg_sim_timing *o) const;
+	void run(int nsteps, double time_end, double strain_end);
 	void set_leaf_size(int leaf) { solver_->reanalyze(leaf); symbolic_runs_++; }
 	void output_snapshot(OutputSnapshot &o);
 	void set_brownian_force(const double *fb);
@@ -131,6 +132,9 @@ private:
 	int64_t launches_mark_ = 0;
 	int64_t last_launches_ = 0;
 	cudaEvent_t step_a_ = nullptr, step_b_ = nullptr;
+	cudaEvent_t run_a_ = nullptr, run_b_ = nullptr;   // around a whole run()
+	double run_ms_ = 0;
+	int run_steps_ = 0;
 };
 
 static DevParams make_dev_params(const lfg_params &p, int n, double lx, double ly, double lz, double skin)
@@ -273,6 +277,8 @@ Sim::~Sim()
 	for (auto &e : evs_) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
 	if (step_a_) cudaEventDestroy(step_a_);
 	if (step_b_) cudaEventDestroy(step_b_);
+	if (run_a_) cudaEventDestroy(run_a_);
+	if (run_b_) cudaEventDestroy(run_b_);
 }
 
 // Build the pair superset at the current positions, carry the pair state of
@@ -971,6 +977,34 @@ void Sim::timing(lfg_sim_timing *o) const
 	o->solve_bytes = 2.0*(double)solver_->nnz_L()*(opt_.precision == LFG_PREC_FP64 ? 8 : 4);
 	o->rebuild_ms = rebuild_ms_+(solver_->capture_ms()-capture_mark_);
 	o->rebuilds = rebuilds_;
+	o->run_steps = run_steps_;
+	o->run_ms = run_ms_;
+}
+
+// nsteps loop steps (lfg_sim_run), timed as a whole on the device: one event
+// before the first step's work and one after the last step's, so the host's
+// part between steps (the end-of-step read of the clock, the next step's
+// launches) counts as well
+void Sim::run(int nsteps, double time_end, double strain_end)
+{
+	first_time();
+	if (!run_a_) {
+		LFG_CUDA(cudaEventCreate(&run_a_));
+		LFG_CUDA(cudaEventCreate(&run_b_));
+	}
+	run_ms_ = 0;
+	run_steps_ = 0;
+	LFG_CUDA(cudaEventRecord(run_a_, st_));
+	for (int k = 0; k < nsteps; k++) {
+		step(0, time_end, strain_end);
+		run_steps_++;
+		if (error_code) break;
+	}
+	LFG_CUDA(cudaEventRecord(run_b_, st_));
+	LFG_CUDA(cudaEventSynchronize(run_b_));
+	float ms = 0;
+	LFG_CUDA(cudaEventElapsedTime(&ms, run_a_, run_b_));
+	run_ms_ = ms;
 }
 
 
@@ -1481,10 +1515,7 @@ int lfg_sim_run(lfg_sim *h, int nsteps, double time_end, double strain_end, lfg_
 	if (!h || nsteps < 0) return fail(st, LFG_ERR_BAD_ARG, 0, "bad arguments");
 	SIM_GUARD_BEGIN
 	cudaSetDevice(h->device);
-	for (int k = 0; k < nsteps; k++) {
-		h->s->step(0, time_end, strain_end);
-		if (h->s->error_code) break;
-	}
+	h->s->run(nsteps, time_end, strain_end);
 	return sim_status(h, st);
 	SIM_GUARD_END
 }
