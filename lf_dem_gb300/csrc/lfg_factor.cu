@@ -1481,12 +1481,21 @@ template <typename T> static void set_assemble_smem(const DevSymbolic &D)
 	set = need;
 }
 
+// FP32 update launches of at most UPDATE_SOLO_TILES tiles (about three waves
+// at one CTA per SM) ask for more shared memory than two CTAs can share, so
+// the CTA that factors the next diagonal block -- the launch's critical path
+// -- has its SM to itself.  Measured at N = 4096 over thresholds 0 to 1000:
+// 480 was best, 7.58 -> 7.53 ms per step; at 1000 the tiles' waves outlast
+// the diagonal block (7.89 ms).
+constexpr int UPDATE_SOLO_TILES = 480;
+constexpr size_t UPDATE_SOLO_SMEM = 120*1024;
+
 template <typename T> static void set_update_smem()
 {
 	static std::once_flag once;
 	std::call_once(once, [] {
 		LFG_CUDA(cudaFuncSetAttribute(k_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                              (int)update_smem<T>()));
+		                              (int)std::max(update_smem<T>(), UPDATE_SOLO_SMEM)));
 		LFG_CUDA(cudaFuncSetAttribute(k_syrk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, umma::SMEM_BYTES));
 	});
 }
@@ -1609,7 +1618,9 @@ int factor_numeric(DevFactor<T> &F, const DevSymbolic &D, const double *dbl, con
 			           (const int *)D.sn_ld, (const int64_t *)D.sn_off, F.arena, F.linv, D.nsn, D.dof);
 			break;
 		case PLAN_UPDATE:
-			launch_pdl(k_update<T>, L.count, 256, update_smem<T>(), st, (const int4 *)D.tile_tasks+L.off,
+			launch_pdl(k_update<T>, L.count, 256,
+			           std::is_same<T, float>::value && L.count <= UPDATE_SOLO_TILES ? UPDATE_SOLO_SMEM : update_smem<T>(),
+			           st, (const int4 *)D.tile_tasks+L.off,
 			           (const int *)D.sn_first, (const int *)D.sn_n, (const int *)D.sn_m, (const int *)D.sn_ld,
 			           (const int64_t *)D.sn_off, F.arena, F.linv, D.nsn, F.status, D.dof);
 			break;
