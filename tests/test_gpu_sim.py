@@ -125,3 +125,20 @@ def test_scalar_interaction_counts(engine, params):
         assert s["n_lub"] == int(np.count_nonzero(pg["lub_active"]))
         assert 0 < s["n_resistance_pairs"] <= s["n_pairs"]
     g.close()
+
+
+def test_run_timing_covers_every_step(engine):
+    """lfg_sim_timing.run_ms: one event pair around a whole lfg_sim_run, so it
+    counts every step and the gaps between them (at least the sum of the
+    per-step event times, and not far above it)."""
+    p = make_packing(400, 0.52, 42)
+    g = engine.Sim(STRESS_PARAMS, p.position, p.radius, p.lx, p.ly, p.lz, precision=1)
+    g.run(2)
+    g.clear_step_times()
+    g.run(5)
+    t = g.timing()
+    ms, _ = g.step_times()
+    assert t["run_steps"] == 5 and len(ms) == 5
+    assert t["run_ms"] >= 0.999 * float(np.sum(ms))
+    assert t["run_ms"] <= 2.0 * float(np.sum(ms)) + 5.0
+    g.close()
